@@ -1,0 +1,701 @@
+// tp_host.cu -- C ABI of the GB300 tile processor (include/tp.h).
+//
+// Host-side equivalent of com.elphel.imagej.gpu.GPUTileProcessor: it owns the
+// device buffers of one scene geometry, converts the reference's host data
+// formats on upload, and launches the stage kernels on one CUDA stream.
+// Errors never abort: every entry point returns a tp_status and records a
+// message retrievable with tp_last_error().
+#include "../../include/tp.h"
+#include "tp_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+struct tp_handle {
+  tp_config cfg;
+  int tilesX = 0, tilesY = 0, ntiles = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // device buffers
+  void *d_images[TP_MAXS] = {};
+  int img_dtype[TP_MAXS] = {};
+  float *d_kern[TP_MAXS] = {};
+  float *d_kext[TP_MAXS] = {};
+  int *d_task_txy = nullptr, *d_task_op = nullptr;
+  float *d_task_disp = nullptr, *d_task_xy = nullptr;
+  int *d_tile_op = nullptr;
+  float *d_tile_disp = nullptr;
+  int *d_num_tasks = nullptr;
+  double *d_ports = nullptr;
+  double *d_port_deriv = nullptr;
+  SubtilePlan *d_plan = nullptr;
+  int *d_tile_task = nullptr;
+  float *d_clt = nullptr, *d_corr = nullptr, *d_disp = nullptr, *d_rbg = nullptr;
+  float *d_lpf_rbg = nullptr;
+  GeomDev *d_geom = nullptr;
+  double *d_rdist = nullptr;
+  CorrDev *d_corr_cfg = nullptr;
+  // host state
+  int num_tasks = 0;
+  int ports_from_geometry = 0;
+  int have_geometry = 0, have_tasks = 0, have_corr = 0, lpf_on = 0, planned = 0;
+  int num_pairs = 0, corr_capacity = 0;
+  float color_scale[3] = {1.f, 1.f, 1.f};
+  GeomDev geom_host;
+  CorrDev corr_host;
+};
+
+static tp_status fail(tp_handle *h, tp_status st, const std::string &msg) {
+  if (h) h->err = msg;
+  return st;
+}
+static tp_status cuda_fail(tp_handle *h, cudaError_t e, const char *where) {
+  return fail(h, TP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, where)                                    \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
+  } while (0)
+
+static cudaStream_t pick_stream(tp_handle *h, void *s) { return s ? (cudaStream_t)s : h->stream; }
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t n) {
+  return cudaMalloc((void **)p, n * sizeof(T) > 0 ? n * sizeof(T) : 1);
+}
+
+static SceneDev scene_of(tp_handle *h) {
+  SceneDev sc;
+  memset(&sc, 0, sizeof(sc));
+  const tp_config &c = h->cfg;
+  sc.num_sensors = c.num_sensors;
+  sc.num_colors = c.num_colors;
+  sc.width = c.width;
+  sc.height = c.height;
+  sc.tilesX = h->tilesX;
+  sc.tilesY = h->tilesY;
+  sc.kh = c.kernels_hor;
+  sc.kv = c.kernels_vert;
+  sc.kernel_step = c.kernel_step;
+  sc.bayer_red_row = c.bayer_red_row;
+  sc.bayer_red_col = c.bayer_red_col;
+  sc.img_pitch = c.width;
+  for (int i = 0; i < 3; i++) sc.color_scale[i] = h->color_scale[i];
+  for (int s = 0; s < c.num_sensors; s++) {
+    sc.images[s] = h->d_images[s];
+    sc.img_dtype[s] = h->img_dtype[s];
+    sc.kernels[s] = h->d_kern[s];
+    sc.kext[s] = h->d_kext[s];
+  }
+  sc.num_tasks = h->num_tasks;
+  sc.task_txy = h->d_task_txy;
+  sc.task_op = h->d_task_op;
+  sc.task_disp = h->d_task_disp;
+  sc.task_xy = h->d_task_xy;
+  sc.ports_from_geometry = h->ports_from_geometry;
+  sc.geom = h->d_geom;
+  sc.rdist_tbl = h->d_rdist;
+  sc.ports = h->d_ports;
+  sc.port_deriv = nullptr;
+  sc.plan = h->d_plan;
+  sc.tile_task = h->d_tile_task;
+  sc.clt = h->d_clt;
+  sc.corr = h->d_corr;
+  sc.disp = h->d_disp;
+  sc.rbg = h->d_rbg;
+  sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
+  sc.corr_cfg = h->d_corr_cfg;
+  sc.num_pairs = h->num_pairs;
+  return sc;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry set-up on the host (GeometryCorrection.java), FP64.  Operation order
+// follows the reference so the device ports are those of the FP64 CPU path.
+// ---------------------------------------------------------------------------
+static void m3mul(const double a[3][3], const double b[3][3], double c[3][3]) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += a[i][k] * b[k][j];
+      c[i][j] = s;
+    }
+}
+
+// CorrVector.getRotMatrices (1043-1076) and getRotDeriveMatrices (1083-1147)
+static void host_rotations(const tp_geometry *g, int S, GeomDev *gd) {
+  for (int chn = 0; chn < S; chn++) {
+    double ca = cos(g->azimuth[chn]), sa = sin(g->azimuth[chn]);
+    double ct = cos(g->tilt[chn]), st = sin(g->tilt[chn]);
+    double zoom = (1.0 + g->zoom[chn]);
+    double cr0 = cos(g->roll[chn]), sr0 = sin(g->roll[chn]);
+    double cr = cr0 * zoom, sr = sr0 * zoom;
+    const double AZ = -1.0, TL = 1.0, RL = 1.0;  // ROT_AZ_SGN, ROT_TL_SGN, ROT_RL_SGN
+    double a_az[3][3] = {{ca, 0.0, sa * AZ}, {0.0, 1.0, 0.0}, {-sa * AZ, 0.0, ca}};
+    double a_t[3][3] = {{1.0, 0.0, 0.0}, {0.0, ct, st * TL}, {0.0, -st * TL, ct}};
+    double a_r[3][3] = {{cr, sr * RL, 0.0}, {-sr * RL, cr, 0.0}, {0.0, 0.0, 1.0}};
+    double tmp[3][3];
+    m3mul(a_t, a_az, tmp);
+    m3mul(a_r, tmp, gd->rots[chn]);
+    double a_rz[3][3] = {{cr0 * zoom, sr0 * zoom * RL, 0.0}, {-sr0 * zoom * RL, cr0 * zoom, 0.0}, {0.0, 0.0, 1.0}};
+    double a_daz[3][3] = {{-sa, 0.0, ca * AZ}, {0.0, 0.0, 0.0}, {-ca * AZ, 0.0, -sa}};
+    double a_dt[3][3] = {{0.0, 0.0, 0.0}, {0.0, -st, ct * TL}, {0.0, -ct * TL, -st}};
+    double a_dr[3][3] = {{-sr0 * zoom, cr0 * zoom * RL, 0.0}, {-cr0 * zoom * RL, -sr0 * zoom, 0.0}, {0.0, 0.0, 0.0}};
+    double a_dz[3][3] = {{cr0, sr0 * RL, 0.0}, {-sr0 * RL, cr0, 0.0}, {0.0, 0.0, 0.0}};
+    m3mul(a_t, a_daz, tmp); m3mul(a_rz, tmp, gd->drots[chn][0]);
+    m3mul(a_dt, a_az, tmp); m3mul(a_rz, tmp, gd->drots[chn][1]);
+    m3mul(a_t, a_az, tmp); m3mul(a_dr, tmp, gd->drots[chn][2]);
+    m3mul(a_t, a_az, tmp); m3mul(a_dz, tmp, gd->drots[chn][3]);
+  }
+}
+
+// calcReverseDistortionTable (2707-2757)
+static int host_rdist_table(const tp_geometry *g, std::vector<double> &tbl) {
+  const double delta = 1E-8, minDerivative = 0.1, stepR = 0.001, maxR = 2.0;
+  const int numIterations = 1000;
+  double drDistDr = 1.0;
+  double A8 = g->distortion[6], A7 = g->distortion[5], A6 = g->distortion[4], A5 = g->distortion[3];
+  double A = g->distortion[2], B = g->distortion[1], C = g->distortion[0];
+  bool use8 = (A8 != 0.0) || (A7 != 0.0) || (A6 != 0.0);
+  double d = 1.0 - A8 - A7 - A6 - A5 - A - B - C;
+  double rPrev = 0.0;
+  int len = (int)ceil(maxR / stepR) + 1;
+  tbl.assign(len, NAN);
+  tbl[0] = 1.0 / d;
+  for (int i = 1; i < len; i++) {
+    double rDist = stepR * i;
+    double r = rPrev + stepR / drDistDr;
+    for (int it = 0; it < numIterations; it++) {
+      double k;
+      if (use8) {
+        k = (((((((A8)*r + A7) * r + A6) * r + A5) * r + A) * r + B) * r + C) * r + d;
+        drDistDr = (((((((8 * A8) * r + 7 * A7) * r + 6 * A6) * r + 5 * A5) * r + 4 * A) * r + 3 * B) * r + 2 * C) * r + d;
+      } else {
+        k = (((A5 * r + A) * r + B) * r + C) * r + d;
+        drDistDr = (((5 * A5 * r + 4 * A) * r + 3 * B) * r + 2 * C) * r + d;
+      }
+      double rD = r * k;
+      if (drDistDr < minDerivative) return len;  // too much distortion: rest stays NaN
+      if (fabs(rD - rDist) < delta) break;
+      r += (rDist - rD) / drDistDr;
+    }
+    rPrev = r;
+    tbl[i] = r / rDist;
+  }
+  return len;
+}
+
+// ImageDtt.java:1662-1690 (sigma used unsquared, as there)
+static void host_corr_lpf(double corr_sigma, float *out) {
+  const int ts = 8;
+  double fd[64];
+  if (corr_sigma == 0) {
+    fd[0] = 1.0;
+    for (int i = 1; i < 64; i++) fd[i] = 0;
+  } else {
+    for (int i = 0; i < ts; i++)
+      for (int j = 0; j < ts; j++) fd[i * ts + j] = exp(-(i * i + j * j) / (2 * corr_sigma));
+  }
+  double sum = 0;
+  for (int i = 0; i < ts; i++)
+    for (int j = 0; j < ts; j++) {
+      double d = fd[i * ts + j];
+      d *= cos(M_PI * i / (2 * ts)) * cos(M_PI * j / (2 * ts));
+      if (i > 0) d *= 2.0;
+      if (j > 0) d *= 2.0;
+      sum += d;
+    }
+  for (int i = 0; i < 64; i++) fd[i] /= sum;
+  // DttRad2.dttt_iiie (mode 0): DCT-IIIe along rows (transposed store), then along rows again
+  double c3[8][8];
+  double scale = sqrt(2.0 / 8);
+  for (int j = 0; j < 8; j++) {
+    double ej = ((j == 0) || (j == 7)) ? 0.5 : 1.0;
+    for (int k = 0; k < 8; k++) c3[k][j] = scale * ej * cos(j * (2 * k + 1) * M_PI / 16);
+  }
+  double tmp[64], y[64];
+  for (int i = 0; i < 8; i++)
+    for (int k = 0; k < 8; k++) {
+      double s = 0;
+      for (int j = 0; j < 8; j++) s += c3[k][j] * fd[i * 8 + j];
+      tmp[k * 8 + i] = s;
+    }
+  for (int i = 0; i < 8; i++)
+    for (int k = 0; k < 8; k++) {
+      double s = 0;
+      for (int j = 0; j < 8; j++) s += c3[k][j] * tmp[i * 8 + j];
+      y[i * 8 + k] = s;
+    }
+  for (int i = 0; i < 64; i++) out[i] = (float)(y[i] * 2 * ts);
+}
+
+// Correlation2d.halfFlatTopWindow (1047-1081)
+static void host_half_flat_top(int n, double hwidth, double blur, bool notch, double scale, float *out) {
+  std::vector<double> w(n);
+  for (int i = 0; i < n; i++) {
+    if (blur <= 0.0) w[i] = (i < hwidth) ? 1.0 : 0.0;
+    else if (i < hwidth - blur / 2) w[i] = 1.0;
+    else if (i > hwidth + blur / 2) w[i] = 0.0;
+    else w[i] = 0.5 * (1.0 - sin(M_PI * (i - hwidth) / blur));
+    if (notch) w[i] = 1.0 - w[i];
+  }
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s += ((i == 0) ? 1.0 : 2.0) * w[i];
+  s = 1 / s;
+  for (int i = 0; i < n; i++) out[i] = (float)(w[i] * s * scale);
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+tp_status tp_default_corr_params(tp_corr_params *p) {
+  if (!p) return TP_ERR_ARG;
+  p->fat_zero = 0.05f;
+  p->corr_sigma = 0.8f;
+  p->corr_red = 0.5f;
+  p->corr_blue = 0.2f;
+  p->corr_offset = 0.1f;
+  p->min_corr = 0.02f;
+  p->corr_strip_hight = 9;
+  p->twice_diagonal = 1;
+  p->enhortho_width = 2;
+  p->enhortho_scale = 0.0f;
+  p->corr_wndy_size = 2; p->corr_wndy_hwidth = 1.0f; p->corr_wndy_blur = 1.0f;
+  p->corr_wndx_size = 9; p->corr_wndx_hwidth = 6.0f; p->corr_wndx_blur = 5.0f;
+  return TP_OK;
+}
+
+tp_status tp_quad_pairs(tp_pair *pairs, int *n) {
+  static const int c1[6] = {0, 2, 0, 1, 0, 2}, c2[6] = {1, 3, 2, 3, 3, 1}, kind[6] = {0, 0, 1, 1, 2, 3};
+  static const float bx[6] = {1, 1, 0, 0, 1, 1}, by[6] = {0, 0, 1, 1, 1, -1};
+  if (!pairs || !n) return TP_ERR_ARG;
+  for (int i = 0; i < 6; i++) {
+    pairs[i].cam1 = c1[i]; pairs[i].cam2 = c2[i]; pairs[i].kind = kind[i]; pairs[i].in_combo = 1;
+    pairs[i].bx = bx[i]; pairs[i].by = by[i];
+  }
+  *n = 6;
+  return TP_OK;
+}
+
+tp_status tp_create(const tp_config *cfg, tp_handle **out) {
+  if (!cfg || !out) return TP_ERR_ARG;
+  *out = nullptr;
+  if (cfg->num_sensors < 1 || cfg->num_sensors > TP_MAX_SENSORS) return TP_ERR_ARG;
+  if (cfg->num_colors != 1 && cfg->num_colors != 3) return TP_ERR_ARG;
+  if (cfg->width < 16 || cfg->height < 16 || (cfg->width % 8) || (cfg->height % 8) || (cfg->width & 1) ||
+      cfg->width > 65535 * 8 || cfg->height > 32767 * 8)
+    return TP_ERR_ARG;
+  if (cfg->kernels_hor < 0 || cfg->kernels_vert < 0 || ((cfg->kernels_hor > 0) != (cfg->kernels_vert > 0)))
+    return TP_ERR_ARG;
+  if (cfg->kernels_hor > 0 && cfg->kernel_step <= 0) return TP_ERR_ARG;
+  tp_handle *h = new tp_handle();
+  h->cfg = *cfg;
+  h->tilesX = cfg->width / 8;
+  h->tilesY = cfg->height / 8;
+  h->ntiles = h->tilesX * h->tilesY;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
+    delete h;
+    return TP_ERR_NOT_BUILT;
+  }
+  const int S = cfg->num_sensors, C = cfg->num_colors;
+  const size_t nt = h->ntiles, npix = (size_t)cfg->width * cfg->height;
+  bool ok = cudaSetDevice(cfg->device) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && upload_kernel_constants() == cudaSuccess;
+  for (int s = 0; ok && s < S; s++) {
+    ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
+    if (ok && cfg->kernels_hor > 0) {
+      size_t nk = (size_t)cfg->kernels_hor * cfg->kernels_vert * C;
+      ok = dalloc(&h->d_kern[s], nk * TP_CLT) == cudaSuccess && dalloc(&h->d_kext[s], nk * 8) == cudaSuccess;
+    }
+  }
+  ok = ok && dalloc(&h->d_task_txy, nt) == cudaSuccess && dalloc(&h->d_task_op, nt) == cudaSuccess;
+  ok = ok && dalloc(&h->d_task_disp, nt) == cudaSuccess && dalloc(&h->d_task_xy, nt * S * 2) == cudaSuccess;
+  ok = ok && dalloc(&h->d_tile_op, nt) == cudaSuccess && dalloc(&h->d_tile_disp, nt) == cudaSuccess;
+  ok = ok && dalloc(&h->d_num_tasks, 1) == cudaSuccess;
+  ok = ok && dalloc(&h->d_ports, nt * S * 2) == cudaSuccess;
+  ok = ok && dalloc(&h->d_plan, nt * S * C) == cudaSuccess && dalloc(&h->d_tile_task, nt) == cudaSuccess;
+  ok = ok && dalloc(&h->d_clt, nt * S * C * TP_CLT) == cudaSuccess;
+  ok = ok && dalloc(&h->d_disp, nt * TP_NDISP) == cudaSuccess;
+  ok = ok && dalloc(&h->d_lpf_rbg, 3 * 64) == cudaSuccess;
+  ok = ok && dalloc(&h->d_geom, 1) == cudaSuccess && dalloc(&h->d_rdist, 2048 + 64) == cudaSuccess;
+  ok = ok && dalloc(&h->d_corr_cfg, 1) == cudaSuccess;
+  if (ok) ok = cudaMemsetAsync(h->d_clt, 0, nt * S * C * TP_CLT * sizeof(float), h->stream) == cudaSuccess;
+  if (ok) ok = cudaStreamSynchronize(h->stream) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    tp_destroy(h);
+    return TP_ERR_NOMEM;
+  }
+  // default correlation set-up: quad pairs for 4 sensors, none otherwise
+  tp_corr_params cp;
+  tp_default_corr_params(&cp);
+  if (S == 4) {
+    tp_pair pr[6];
+    int n = 0;
+    tp_quad_pairs(pr, &n);
+    tp_set_corr(h, &cp, pr, n);
+  }
+  *out = h;
+  return TP_OK;
+}
+
+tp_status tp_destroy(tp_handle *h) {
+  if (!h) return TP_ERR_ARG;
+  for (int s = 0; s < TP_MAXS; s++) {
+    cudaFree(h->d_images[s]);
+    cudaFree(h->d_kern[s]);
+    cudaFree(h->d_kext[s]);
+  }
+  void *bufs[] = {h->d_task_txy, h->d_task_op, h->d_task_disp, h->d_task_xy, h->d_tile_op, h->d_tile_disp,
+                  h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
+                  h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg};
+  for (void *b : bufs) cudaFree(b);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return TP_OK;
+}
+
+tp_status tp_last_error(const tp_handle *h, char *buf, int n) {
+  if (!h || !buf || n <= 0) return TP_ERR_ARG;
+  snprintf(buf, (size_t)n, "%s", h->err.c_str());
+  return TP_OK;
+}
+
+tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
+  if (!h || !g) return TP_ERR_ARG;
+  const int S = h->cfg.num_sensors;
+  GeomDev &gd = h->geom_host;
+  memset(&gd, 0, sizeof(gd));
+  gd.num_sensors = S;
+  gd.pixel_width = g->pixel_width;
+  gd.pixel_height = g->pixel_height;
+  gd.focal_length = g->focal_length;
+  gd.pixel_size = g->pixel_size;
+  gd.distortion_radius = g->distortion_radius;
+  for (int i = 0; i < 7; i++) gd.rad_coeff[i] = g->distortion[i];
+  for (int s = 0; s < S; s++)
+    for (int k = 0; k < 2; k++) {
+      gd.rXY[s][k] = g->rXY[s][k];
+      gd.pXY0[s][k] = g->pXY0[s][k];
+    }
+  host_rotations(g, S, &gd);
+  std::vector<double> tbl;
+  gd.tbl_len = host_rdist_table(g, tbl);
+  if (gd.tbl_len > 2048 + 64) return fail(h, TP_ERR_ARG, "distortion table too long");
+  CK(cudaMemcpyAsync(h->d_geom, &gd, sizeof(gd), cudaMemcpyHostToDevice, h->stream), "tp_set_geometry");
+  CK(cudaMemcpyAsync(h->d_rdist, tbl.data(), sizeof(double) * gd.tbl_len, cudaMemcpyHostToDevice, h->stream),
+     "tp_set_geometry");
+  CK(cudaStreamSynchronize(h->stream), "tp_set_geometry");
+  h->have_geometry = 1;
+  h->planned = 0;
+  return TP_OK;
+}
+
+tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const float *offs, int layout) {
+  if (!h || !kernels || !offs) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_kernels: bad camera");
+  if (h->cfg.kernels_hor <= 0) return fail(h, TP_ERR_STATE, "tp_set_kernels: handle created without kernels");
+  size_t nk = (size_t)h->cfg.kernels_hor * h->cfg.kernels_vert * h->cfg.num_colors;
+  if (layout == TP_KERNELS_GPU) {
+    // undo the 8x8 transpose of GPUTileProcessor.setConvolutionKernels (406-410)
+    std::vector<float> t(nk * TP_CLT);
+    for (size_t k = 0; k < nk * 4; k++)
+      for (int i0 = 0; i0 < 64; i0++) t[k * 64 + (((i0 & 7) << 3) | (i0 >> 3))] = kernels[k * 64 + i0];
+    CK(cudaMemcpy(h->d_kern[cam], t.data(), nk * TP_CLT * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
+  } else if (layout == TP_KERNELS_CPU) {
+    CK(cudaMemcpy(h->d_kern[cam], kernels, nk * TP_CLT * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
+  } else {
+    return fail(h, TP_ERR_ARG, "tp_set_kernels: bad layout");
+  }
+  CK(cudaMemcpy(h->d_kext[cam], offs, nk * 8 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
+  h->planned = 0;
+  return TP_OK;
+}
+
+tp_status tp_set_color_scales(tp_handle *h, const float *scales) {
+  if (!h || !scales) return TP_ERR_ARG;
+  for (int i = 0; i < 3; i++) h->color_scale[i] = scales[i];
+  return TP_OK;
+}
+
+tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size_t pitch) {
+  if (!h || !image) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_image: bad camera");
+  if (dtype != TP_F32 && dtype != TP_U16) return fail(h, TP_ERR_ARG, "tp_set_image: bad dtype");
+  size_t es = dtype == TP_U16 ? 2 : 4;
+  if (pitch == 0) pitch = h->cfg.width;
+  if (pitch < (size_t)h->cfg.width) return fail(h, TP_ERR_ARG, "tp_set_image: pitch < width");
+  CK(cudaMemcpy2DAsync(h->d_images[cam], h->cfg.width * es, image, pitch * es, h->cfg.width * es, h->cfg.height,
+                       cudaMemcpyHostToDevice, h->stream),
+     "tp_set_image");
+  CK(cudaStreamSynchronize(h->stream), "tp_set_image");
+  h->img_dtype[cam] = dtype;
+  return TP_OK;
+}
+
+tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
+  if (!h || (!packed && n > 0)) return TP_ERR_ARG;
+  if (n < 0 || n > h->ntiles) return fail(h, TP_ERR_ARG, "tp_set_tasks: bad task count");
+  const int S = h->cfg.num_sensors, rec = 2 + 2 * S;
+  std::vector<int> txy(n), op(n);
+  std::vector<float> xy((size_t)n * S * 2);
+  for (int i = 0; i < n; i++) {
+    memcpy(&op[i], packed + (size_t)i * rec, 4);
+    memcpy(&txy[i], packed + (size_t)i * rec + 1, 4);
+    int tx = txy[i] & 0xffff, ty = txy[i] >> 16;
+    if (tx >= h->tilesX || ty >= h->tilesY || ty < 0) return fail(h, TP_ERR_ARG, "tp_set_tasks: tile out of range");
+    for (int k = 0; k < 2 * S; k++) xy[(size_t)i * 2 * S + k] = packed[(size_t)i * rec + 2 + k];
+  }
+  if (n > 0) {
+    CK(cudaMemcpyAsync(h->d_task_txy, txy.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream), "tp_set_tasks");
+    CK(cudaMemcpyAsync(h->d_task_op, op.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream), "tp_set_tasks");
+    CK(cudaMemcpyAsync(h->d_task_xy, xy.data(), xy.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream),
+       "tp_set_tasks");
+  }
+  CK(cudaStreamSynchronize(h->stream), "tp_set_tasks");
+  h->num_tasks = n;
+  h->ports_from_geometry = 0;
+  h->have_tasks = 1;
+  h->planned = 0;
+  return TP_OK;
+}
+
+tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
+  if (!h || !tile_op || !disp) return TP_ERR_ARG;
+  if (!h->have_geometry) return fail(h, TP_ERR_STATE, "tp_set_tile_ops: geometry not set");
+  CK(cudaMemcpyAsync(h->d_tile_op, tile_op, h->ntiles * sizeof(int), cudaMemcpyHostToDevice, h->stream),
+     "tp_set_tile_ops");
+  CK(cudaMemcpyAsync(h->d_tile_disp, disp, h->ntiles * sizeof(float), cudaMemcpyHostToDevice, h->stream),
+     "tp_set_tile_ops");
+  CK(launch_compact_tasks(h->d_tile_op, h->d_tile_disp, h->tilesX, h->ntiles, h->d_task_txy, h->d_task_op,
+                          h->d_task_disp, h->d_num_tasks, h->stream),
+     "tp_set_tile_ops");
+  CK(cudaMemcpyAsync(&h->num_tasks, h->d_num_tasks, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+     "tp_set_tile_ops");
+  CK(cudaStreamSynchronize(h->stream), "tp_set_tile_ops");
+  h->ports_from_geometry = 1;
+  h->have_tasks = 1;
+  h->planned = 0;
+  return TP_OK;
+}
+
+tp_status tp_set_lpf(tp_handle *h, const float *lpf) {
+  if (!h) return TP_ERR_ARG;
+  if (!lpf) {
+    h->lpf_on = 0;
+    return TP_OK;
+  }
+  CK(cudaMemcpy(h->d_lpf_rbg, lpf, h->cfg.num_colors * 64 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_lpf");
+  h->lpf_on = 1;
+  return TP_OK;
+}
+
+tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int np) {
+  if (!h || !p || (!pairs && np > 0)) return TP_ERR_ARG;
+  if (np < 0 || np > TP_MAX_PAIRS) return fail(h, TP_ERR_ARG, "tp_set_corr: too many pairs");
+  if (p->corr_strip_hight < 1 || p->corr_strip_hight > TP_MAX_STRIP || p->corr_wndy_size < 1 ||
+      p->corr_wndy_size > TP_MAX_STRIP || p->corr_wndx_size < 1 || p->corr_wndx_size > 32)
+    return fail(h, TP_ERR_ARG, "tp_set_corr: window sizes out of range");
+  CorrDev &cd = h->corr_host;
+  memset(&cd, 0, sizeof(cd));
+  cd.num_pairs = np;
+  cd.strip_rows = p->corr_strip_hight;
+  cd.twice_diagonal = p->twice_diagonal;
+  cd.wndy_size = p->corr_wndy_size;
+  cd.wndx_size = p->corr_wndx_size;
+  cd.fat_zero = p->fat_zero;
+  cd.corr_offset = p->corr_offset;
+  cd.min_corr = p->min_corr;
+  double g = 1.0 / (1.0 + p->corr_red + p->corr_blue);  // ImageDtt.java:1571-1581
+  cd.col_weights[2] = (float)g;
+  cd.col_weights[0] = (float)(p->corr_red * g);
+  cd.col_weights[1] = (float)(p->corr_blue * g);
+  host_corr_lpf(p->corr_sigma, cd.lpf);
+  host_half_flat_top(p->corr_wndy_size, p->corr_wndy_hwidth, p->corr_wndy_blur, false, 1.0, cd.wndy);
+  host_half_flat_top(p->corr_wndx_size, p->corr_wndx_hwidth, p->corr_wndx_blur, false, 2.0, cd.wndx);
+  for (int i = 0; i < 15; i++) {  // Correlation2d.createOrtoNotch (2654-2675)
+    double v = ((i < (8 - p->enhortho_width)) || (i > (8 - 2 + p->enhortho_width))) ? 1.0 : p->enhortho_scale;
+    if (i == 7) v = 0.0;
+    cd.notch[i] = (float)(v * sin(M_PI * (i + 1.0) / 16));
+  }
+  bool general = np > 6;
+  for (int i = 0; i < np; i++) {
+    if (pairs[i].cam1 < 0 || pairs[i].cam1 >= h->cfg.num_sensors || pairs[i].cam2 < 0 ||
+        pairs[i].cam2 >= h->cfg.num_sensors || pairs[i].kind < 0 || pairs[i].kind > 4)
+      return fail(h, TP_ERR_ARG, "tp_set_corr: bad pair");
+    cd.pairs[i].cam1 = pairs[i].cam1;
+    cd.pairs[i].cam2 = pairs[i].cam2;
+    cd.pairs[i].kind = pairs[i].kind;
+    cd.pairs[i].in_combo = pairs[i].in_combo;
+    cd.pairs[i].bx = pairs[i].bx;
+    cd.pairs[i].by = pairs[i].by;
+    if (pairs[i].in_combo) cd.num_combo++;
+    if (pairs[i].kind == 0) cd.num_hor++;
+    if (pairs[i].kind == 1) cd.num_vert++;
+    if (pairs[i].kind == 4) general = true;
+  }
+  cd.log_combine = general ? 1 : 0;
+  if (general) cd.num_hor = cd.num_vert = 0;  // ortho maxima are defined for the quad layout only
+  if (np > h->corr_capacity) {
+    cudaFree(h->d_corr);
+    h->d_corr = nullptr;
+    h->corr_capacity = 0;
+    if (dalloc(&h->d_corr, (size_t)h->ntiles * np * TP_CORR) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_set_corr: correlation buffer");
+    }
+    h->corr_capacity = np;
+  }
+  CK(cudaMemcpy(h->d_corr_cfg, &cd, sizeof(cd), cudaMemcpyHostToDevice), "tp_set_corr");
+  h->num_pairs = np;
+  h->have_corr = 1;
+  return TP_OK;
+}
+
+static tp_status ensure_plan(tp_handle *h, cudaStream_t st) {
+  if (!h->have_tasks) return fail(h, TP_ERR_STATE, "no tasks set (tp_set_tasks / tp_set_tile_ops)");
+  if (h->ports_from_geometry && !h->have_geometry) return fail(h, TP_ERR_STATE, "geometry not set");
+  if (h->planned) return TP_OK;
+  SceneDev sc = scene_of(h);
+  CK(launch_plan(sc, st), "plan");
+  CK(launch_tile_task_map(sc, st), "tile map");
+  h->planned = 1;
+  return TP_OK;
+}
+
+tp_status tp_ports(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  h->planned = 0;
+  return ensure_plan(h, pick_stream(h, stream));
+}
+
+tp_status tp_convert_correct(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  CK(launch_convert_correct(scene_of(h), st), "convert_correct");
+  return TP_OK;
+}
+
+tp_status tp_correlate(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_correlate: no pairs set");
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  CK(launch_correlate(scene_of(h), st), "correlate");
+  return TP_OK;
+}
+
+tp_status tp_extract(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_extract: no pairs set");
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  CK(launch_extract(scene_of(h), st), "extract");
+  return TP_OK;
+}
+
+tp_status tp_imclt(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  if (!h->d_rbg) {
+    size_t n = (size_t)h->cfg.num_sensors * h->cfg.num_colors * (h->cfg.width + 8) * (h->cfg.height + 8);
+    if (dalloc(&h->d_rbg, n) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_imclt: frame buffer");
+    }
+  }
+  CK(launch_imclt(scene_of(h), st), "imclt");
+  return TP_OK;
+}
+
+tp_status tp_process(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  h->planned = 0;
+  tp_status r = tp_convert_correct(h, stream);
+  if (r == TP_OK && h->num_pairs > 0) r = tp_correlate(h, stream);
+  if (r == TP_OK && h->num_pairs > 0) r = tp_extract(h, stream);
+  return r;
+}
+
+tp_status tp_synchronize(tp_handle *h) {
+  if (!h) return TP_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream), "tp_synchronize");
+  return TP_OK;
+}
+
+tp_status tp_get_num_tasks(const tp_handle *h, int *n) {
+  if (!h || !n) return TP_ERR_ARG;
+  *n = h->num_tasks;
+  return TP_OK;
+}
+
+static tp_status d2h(tp_handle *h, void *dst, const void *src, size_t bytes, const char *where) {
+  if (!dst) return fail(h, TP_ERR_ARG, where);
+  if (!src) return fail(h, TP_ERR_STATE, std::string(where) + ": not computed");
+  CK(cudaStreamSynchronize(h->stream), where);
+  CK(cudaDeviceSynchronize(), where);
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), where);
+  return TP_OK;
+}
+
+tp_status tp_get_ports(tp_handle *h, double *ports) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, ports, h->d_ports, (size_t)h->num_tasks * h->cfg.num_sensors * 2 * sizeof(double), "tp_get_ports");
+}
+
+tp_status tp_get_task_tiles(tp_handle *h, int *txy) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, txy, h->d_task_txy, (size_t)h->num_tasks * sizeof(int), "tp_get_task_tiles");
+}
+
+tp_status tp_get_subtiles(tp_handle *h, int *int_tl, float *residual) {
+  if (!h || !int_tl || !residual) return TP_ERR_ARG;
+  size_t n = (size_t)h->num_tasks * h->cfg.num_sensors * h->cfg.num_colors;
+  std::vector<SubtilePlan> p(n);
+  tp_status r = d2h(h, p.data(), h->d_plan, n * sizeof(SubtilePlan), "tp_get_subtiles");
+  if (r != TP_OK) return r;
+  for (size_t i = 0; i < n; i++) {
+    int_tl[2 * i] = p[i].tlx;
+    int_tl[2 * i + 1] = p[i].tly;
+    residual[2 * i] = p[i].rx;
+    residual[2 * i + 1] = p[i].ry;
+  }
+  return TP_OK;
+}
+
+tp_status tp_get_clt(tp_handle *h, float *clt) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, clt, h->d_clt, (size_t)h->ntiles * h->cfg.num_sensors * h->cfg.num_colors * TP_CLT * sizeof(float),
+             "tp_get_clt");
+}
+
+tp_status tp_get_corr(tp_handle *h, float *corr) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, corr, h->d_corr, (size_t)h->ntiles * h->num_pairs * TP_CORR * sizeof(float), "tp_get_corr");
+}
+
+tp_status tp_get_disparity(tp_handle *h, float *disp) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, disp, h->d_disp, (size_t)h->ntiles * TP_NDISP * sizeof(float), "tp_get_disparity");
+}
+
+tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg) {
+  if (!h) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_get_rbg: bad camera");
+  size_t plane = (size_t)(h->cfg.width + 8) * (h->cfg.height + 8) * h->cfg.num_colors;
+  return d2h(h, rbg, h->d_rbg ? h->d_rbg + plane * cam : nullptr, plane * sizeof(float), "tp_get_rbg");
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// tp_internal.h -- device-side data layout of the GB300 tile processor.
+//
+// One "scene" = the per-camera image set, kernel tables, geometry and task
+// list that GPUTileProcessor keeps in its device buffers
+// (GPUTileProcessor.java:296-358).  All kernels take a SceneDev by value so a
+// batch of scenes is an array of these.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define TP_DTT 8
+#define TP_CLT 256          // 4 quadrants x 64 coefficients
+#define TP_CORR 225         // 15 x 15 correlation surface
+#define TP_MAXS 16
+#define TP_MAXP 120
+#define TP_MAX_STRIP 16     // rows of the combined strip
+#define TP_NDISP 9
+
+// one (task, sensor, colour) sub-tile: integer window corner, residual shift
+// and kernel-table index, computed in FP64 by the plan kernel
+struct SubtilePlan {
+  int tlx, tly;   // ctile_left, ctile_top (ImageDtt.java:4940-4941)
+  int kidx;       // (ktileY * KH + ktileX) * C + colour, -1 for identity kernels
+  float rx, ry;   // residual_shift (ImageDtt.java:4942-4943)
+};
+
+struct GeomDev {
+  int num_sensors;
+  int pixel_width, pixel_height;
+  int tbl_len;
+  double focal_length, pixel_size, distortion_radius;
+  double rad_coeff[7];
+  double rXY[TP_MAXS][2];
+  double pXY0[TP_MAXS][2];
+  double rots[TP_MAXS][3][3];
+  double drots[TP_MAXS][4][3][3];
+};
+
+struct PairDev {
+  int cam1, cam2, kind, in_combo;
+  float bx, by;
+};
+
+struct CorrDev {
+  int num_pairs;
+  int strip_rows;
+  int twice_diagonal;
+  int wndy_size, wndx_size;
+  int num_hor, num_vert;  // pairs of kind 0 / 1 used for ortho extraction
+  int num_combo;          // pairs contributing to the combined strip
+  int log_combine;        // 1: geometric mean in log domain (generalised pair sets)
+  float fat_zero;
+  float corr_offset;
+  float min_corr;
+  float col_weights[3];
+  float lpf[64];          // correlation LPF (ImageDtt.java:1662-1690)
+  float wndy[TP_MAX_STRIP];
+  float wndx[32];
+  float notch[15];
+  PairDev pairs[TP_MAXP];
+};
+
+struct SceneDev {
+  int num_sensors, num_colors;
+  int width, height, tilesX, tilesY;
+  int kh, kv, kernel_step;
+  int bayer_red_row, bayer_red_col;
+  int img_dtype[TP_MAXS];   // per camera: 0 f32, 1 u16
+  int64_t img_pitch;        // elements
+  float color_scale[3];
+  const void *images[TP_MAXS];
+  const float *kernels[TP_MAXS];   // [kv][kh][C][4][64] CPU orientation
+  const float *kext[TP_MAXS];      // [kv][kh][C][8]
+  // task list
+  int num_tasks;
+  const int *task_txy;       // [n] tx | ty << 16
+  const int *task_op;        // [n]
+  const float *task_disp;    // [n] target disparity (tile-op mode)
+  const float *task_xy;      // [n][S][2] ports as given by tp_set_tasks (float mode)
+  int ports_from_geometry;   // 1: compute ports in FP64 from GeomDev
+  const GeomDev *geom;
+  const double *rdist_tbl;   // reverse distortion table
+  // products
+  double *ports;             // [n][S][2]
+  double *port_deriv;        // [n][S][2][4] or null
+  SubtilePlan *plan;         // [n][S][C]
+  int *tile_task;            // [tilesY*tilesX] -> task index or -1
+  float *clt;                // [tiles][S][C][256]
+  float *corr;               // [tiles][P][225]
+  float *disp;               // [tiles][TP_NDISP]
+  float *rbg;                // [S][C][H+8][W+8]
+  const float *lpf_rbg;      // [C][64] or null
+  const CorrDev *corr_cfg;
+  int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
+};
+
+// launchers (tp_plan.cu / tp_kernels.cu)
+cudaError_t launch_plan(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_tile_task_map(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_convert_correct(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_correlate(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_extract(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_imclt(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_compact_tasks(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                 int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
+                                 cudaStream_t st);
+cudaError_t upload_kernel_constants();

@@ -1,0 +1,181 @@
+/*
+ * tp.h -- C ABI of the GB300 tile processor (libtp.so).
+ *
+ * Drop-in boundary for the imagej-elphel tile-processor path.  The reference
+ * has no C ABI: its GPU boundary is the Java class
+ * com.elphel.imagej.gpu.GPUTileProcessor (JCuda + NVRTC), and its CPU twin is
+ * ImageDtt.clt_aberrations_quad_corr.  Each entry point below names the
+ * reference method it replaces (paths relative to src/main/java/com/elphel/imagej/).
+ *
+ * Conventions
+ *  - every function returns tp_status (0 = TP_OK) and never aborts;
+ *    tp_last_error() returns the message of the last failure on a handle;
+ *  - host pointers are borrowed for the duration of the call (copied);
+ *  - device memory is owned by the handle and released by tp_destroy
+ *    (the reference never frees its buffers);
+ *  - one handle per host thread / stream; a handle is not thread-safe;
+ *  - `stream` arguments are cudaStream_t passed as void* (NULL = the handle's
+ *    own stream);  get/set calls synchronise their stream before returning.
+ *
+ * Array layouts (row-major, C order):
+ *  image       [height][pitch]           f32 or u16 (Bayer mosaic or mono)
+ *  kernels     [kernels_vert][kernels_hor][num_colors][4][64]  f32
+ *  kernel_offs [kernels_vert][kernels_hor][num_colors][8]      f32 (CltExtra)
+ *  clt         [tilesY*tilesX][num_sensors][num_colors][4][64] f32
+ *              (CLT index = horizontal_freq*8 + vertical_freq, the
+ *               ImageDtt.extract_correct_tile orientation)
+ *  corr        [tilesY*tilesX][num_pairs][15*15]                f32
+ *  disparity   [tilesY*tilesX][TP_DISP_N]                       f32
+ *  rbg         [num_colors][height+8][width+8]                  f32 per sensor
+ */
+#ifndef TP_H
+#define TP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TP_MAX_SENSORS 16
+#define TP_MAX_PAIRS 120
+
+typedef struct tp_handle tp_handle;
+
+typedef enum {
+  TP_OK = 0,
+  TP_ERR_ARG = 1,      /* invalid argument / size */
+  TP_ERR_CUDA = 2,     /* CUDA runtime error */
+  TP_ERR_STATE = 3,    /* call order (e.g. no tasks set) */
+  TP_ERR_NOMEM = 4,    /* device allocation failed */
+  TP_ERR_TIMEOUT = 5,  /* a bounded device wait expired */
+  TP_ERR_NOT_BUILT = 6 /* the CUDA kernels are not available */
+} tp_status;
+
+typedef enum { TP_F32 = 0, TP_U16 = 1 } tp_dtype;
+
+typedef enum {
+  TP_KERNELS_GPU = 0,  /* GPUTileProcessor.setConvolutionKernel layout: 64 coefficients transposed */
+  TP_KERNELS_CPU = 1   /* ImageDtt clt_kernels coefficient order (not transposed) */
+} tp_kernel_layout;
+
+/* per-tile disparity record (subset of ImageDtt.java:64-76 disparity_map) */
+enum {
+  TP_DISP_INT = 0, TP_DISP_CM = 1, TP_DISP_STRENGTH = 2, TP_DISP_HOR = 3, TP_DISP_HOR_STRENGTH = 4,
+  TP_DISP_VERT = 5, TP_DISP_VERT_STRENGTH = 6, TP_DISP_CM_S0 = 7, TP_DISP_IXY = 8, TP_DISP_N = 9
+};
+
+/* Compile-time #defines of GPUTileProcessor (GPUTileProcessor.java:79-98, 262-276),
+ * runtime values here. */
+typedef struct {
+  int num_sensors;     /* NUM_CAMS, 1..16 */
+  int num_colors;      /* NUM_COLORS: 1 (mono) or 3 (Bayer: R, B, G planes) */
+  int width, height;   /* IMG_WIDTH, IMG_HEIGHT (multiples of 8) */
+  int kernels_hor;     /* KERNELS_HOR (0 = identity kernels, no aberration correction) */
+  int kernels_vert;    /* KERNELS_VERT */
+  int kernel_step;     /* KERNELS_STEP (16) */
+  int bayer_red_row;   /* BAYER_RED_ROW (reference 0) */
+  int bayer_red_col;   /* BAYER_RED_COL (reference 1) */
+  int device;          /* CUDA device ordinal */
+} tp_config;
+
+/* GeometryCorrection lens/extrinsic model (GeometryCorrection.java:36-90, 1004-1076),
+ * generalised to free per-sensor azimuth/tilt/roll/zoom. */
+typedef struct {
+  int pixel_width, pixel_height;  /* pixelCorrectionWidth/Height */
+  double focal_length;            /* mm */
+  double pixel_size;              /* um */
+  double distortion_radius;       /* mm */
+  double distortion[7];           /* distortionC, B, A, A5, A6, A7, A8 */
+  double rXY[TP_MAX_SENSORS][2];  /* lens offsets in disparity units */
+  double pXY0[TP_MAX_SENSORS][2]; /* sensor centres, pixels */
+  double azimuth[TP_MAX_SENSORS]; /* radians */
+  double tilt[TP_MAX_SENSORS];
+  double roll[TP_MAX_SENSORS];    /* full roll (CorrVector roll + factory roll), radians */
+  double zoom[TP_MAX_SENSORS];    /* zoom - 1 */
+} tp_geometry;
+
+/* correlation pair: Correlation2d.PAIRS entry (Correlation2d.java:52-71) */
+typedef struct {
+  int cam1, cam2;
+  int kind;          /* 0 horizontal, 1 vertical, 2 main diagonal, 3 other diagonal, 4 general */
+  int in_combo;      /* contributes to the combined strip (dbg_pair_mask bit) */
+  float bx, by;      /* strip direction (disparity-axis step), used by kind 4 */
+} tp_pair;
+
+/* ImageDttParameters subset (ImageDttParameters.java:30-112) + per-call values */
+typedef struct {
+  float fat_zero;        /* corr_fat_zero */
+  float corr_sigma;      /* LPF sigma (as in ImageDtt.java:1669: not squared) */
+  float corr_red, corr_blue;
+  float corr_offset;
+  float min_corr;
+  int corr_strip_hight;  /* rows of the combined strip (<= 16) */
+  int twice_diagonal;
+  float enhortho_width, enhortho_scale;
+  int corr_wndy_size; float corr_wndy_hwidth, corr_wndy_blur;
+  int corr_wndx_size; float corr_wndx_hwidth, corr_wndx_blur;
+} tp_corr_params;
+
+/* lifecycle: GPUTileProcessor() (GPUTileProcessor.java:243-360) */
+tp_status tp_create(const tp_config *cfg, tp_handle **out);
+tp_status tp_destroy(tp_handle *h);
+/* copies the last error message (NUL-terminated) */
+tp_status tp_last_error(const tp_handle *h, char *buf, int buf_len);
+/* fills the reference defaults (ImageDttParameters.java:30-112, fat_zero 0.05, corr_sigma 0.8) */
+tp_status tp_default_corr_params(tp_corr_params *p);
+/* the 6 quad pairs Correlation2d.PAIRS[0..5]; returns the count in *n */
+tp_status tp_quad_pairs(tp_pair *pairs, int *n);
+
+/* inputs */
+/* GeometryCorrection set-up used by stage 1 (getPortsCoordinatesAndDerivatives) */
+tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g);
+/* setConvolutionKernel (GPUTileProcessor.java:373-379) / setConvolutionKernels (381-435) */
+tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const float *kernel_offsets, int layout);
+/* setBayerImage (GPUTileProcessor.java:437-450); pitch in elements (0 = width) */
+tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size_t pitch);
+/* per-colour gain applied while reading the mosaic (QuadCLT.java:181-185 scales green by 0.5
+ * before the GPU mosaic is formed); default {1, 1, 1} for R, B, G */
+tp_status tp_set_color_scales(tp_handle *h, const float *scales);
+/* setTasks (GPUTileProcessor.java:363-371): TpTask.asFloatArray layout,
+ * per task {task (int bits), tx | ty << 16 (int bits), xy[num_sensors][2]} */
+tp_status tp_set_tasks(tp_handle *h, const float *packed_tasks, int num_tasks);
+/* setFullFrameImages(float[] target_disparities) + getTileSubcamOffsets
+ * (GPUTileProcessor.java:472-527, 686-778) computed on the device in FP64:
+ * tiles with tile_op != 0 (ImageDtt tile_op[ty][tx]) become tasks in row-major order. */
+tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *target_disparity);
+/* setLpfRbg (GPUTileProcessor.java:780-812): lpf[num_colors][64] applied by tp_imclt; NULL = off */
+tp_status tp_set_lpf(tp_handle *h, const float *lpf);
+/* correlation set-up (ImageDtt.clt_aberrations_quad_corr_new arguments, ImageDtt.java:1491-1546) */
+tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int num_pairs);
+
+/* execution */
+/* stage 1 on the device when tile ops are set (getTileSubcamOffsets, GPUTileProcessor.java:686-778) */
+tp_status tp_ports(tp_handle *h, void *stream);
+/* execConverCorrectTiles (GPUTileProcessor.java:530-558): stage 2 */
+tp_status tp_convert_correct(tp_handle *h, void *stream);
+/* ImageDtt.java:2101-2245 on the device: pair correlation (stage 3a) */
+tp_status tp_correlate(tp_handle *h, void *stream);
+/* ImageDtt.java:2114-2245: strips, combination, argmax, centroid, ortho (stage 3b) */
+tp_status tp_extract(tp_handle *h, void *stream);
+/* execImcltRbg (GPUTileProcessor.java:560-597): stage 4a */
+tp_status tp_imclt(tp_handle *h, void *stream);
+/* ports + convert_correct + correlate + extract in one call (ImageDtt.clt_aberrations_quad_corr) */
+tp_status tp_process(tp_handle *h, void *stream);
+tp_status tp_synchronize(tp_handle *h);
+
+/* outputs (host copies) */
+tp_status tp_get_num_tasks(const tp_handle *h, int *n);
+tp_status tp_get_ports(tp_handle *h, double *ports);            /* [num_tasks][S][2] */
+tp_status tp_get_task_tiles(tp_handle *h, int *txy);            /* [num_tasks] tx | ty << 16 */
+tp_status tp_get_subtiles(tp_handle *h, int *int_tl, float *residual); /* [num_tasks][S][C][2] each */
+tp_status tp_get_clt(tp_handle *h, float *clt);
+tp_status tp_get_corr(tp_handle *h, float *corr);
+tp_status tp_get_disparity(tp_handle *h, float *disparity);
+/* getRBG (GPUTileProcessor.java:599-626): [num_colors][height+8][width+8] */
+tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1331 @@
+/*
+ * tp_oracle.c -- FP64 CPU restatement of the imagej-elphel tile-processor path.
+ *
+ * TEST INFRASTRUCTURE ONLY (correctness oracle and timed CPU baseline).  The
+ * product library never links this file.  Every function names the reference
+ * method and line range it restates; J/ = src/main/java/com/elphel/imagej/.
+ * Loop orders and operation orders follow the reference so that the FP64
+ * results are those the Java code computes (up to libm last-ulp differences).
+ */
+#include "tp_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------- */
+/* DttRad2 (J/tileprocessor/DttRad2.java)                                     */
+/* ------------------------------------------------------------------------- */
+
+static double CN1[2][4], SN1[2][4];           /* setup_arrays (1043-1058) */
+static double COSPI_1_8_SQRT2, COSPI_3_8_SQRT2, SQRT2;
+static double CIIe[8][8], CIIIe[8][8], SIIe[8][8], SIIIe[8][8], CIV[8][8], CII[8][8];
+static double HWINDOW[8];
+static int FOLD_INDEX[64][4];
+static int UNFOLD_INDEX[256];
+static double UNFOLD_K[4][256];
+static pthread_once_t tables_once = PTHREAD_ONCE_INIT;
+
+/* DttRad2.get_fold_indices (109-144) */
+static void fold_indices(int x, int n, int ind[2][6]) {
+  int n1 = n >> 1;
+  if (x < n1) {
+    ind[0][0] = n + n1 - x - 1; ind[0][1] = n1 + x;     ind[0][2] = -1; ind[0][3] = 1;
+    ind[0][4] = n1 - x - 1;     ind[0][5] = -1;
+    ind[1][0] = n + n1 + x;     ind[1][1] = n1 - x - 1; ind[1][2] = -1; ind[1][3] = -1;
+    ind[1][4] = n1 + x;         ind[1][5] = -1;
+  } else {
+    x -= n1;
+    ind[0][0] = x;              ind[0][1] = x;          ind[0][2] = 1;  ind[0][3] = 1;
+    ind[0][4] = n - x - 1;      ind[0][5] = 1;
+    ind[1][0] = n - x - 1;      ind[1][1] = n - x - 1;  ind[1][2] = -1; ind[1][3] = 1;
+    ind[1][4] = x;              ind[1][5] = 1;
+  }
+}
+
+/* DttRad2.get_unfold_index_signs (392-404) */
+static void unfold_index_signs(int x, int n, int is2[3]) {
+  int n1 = n >> 1;
+  int segm = x / n1;
+  x = x % n1;
+  switch (segm) {
+    case 0: is2[0] = x + n1;     is2[1] = 1;  is2[2] = 1;  break;
+    case 1: is2[0] = n - x - 1;  is2[1] = -1; is2[2] = 1;  break;
+    case 2: is2[0] = n1 - x - 1; is2[1] = -1; is2[2] = 1;  break;
+    default: is2[0] = x;         is2[1] = -1; is2[2] = -1; break;
+  }
+}
+
+static void init_tables(void) {
+  const int n = 8;
+  COSPI_1_8_SQRT2 = cos(M_PI / 8) * sqrt(2.0);
+  COSPI_3_8_SQRT2 = cos(3 * M_PI / 8) * sqrt(2.0);
+  SQRT2 = sqrt(2.0);
+  for (int t = 0; t < 2; t++) {                 /* setup_arrays (1043-1058) */
+    int n1 = 2 << t;
+    double pi_4n = M_PI / (8 * n1);
+    for (int k = 0; k < n1; k++) {
+      CN1[t][k] = cos((2 * k + 1) * pi_4n);
+      SN1[t][k] = sin((2 * k + 1) * pi_4n);
+    }
+  }
+  double scale = sqrt(2.0 / n);
+  double pi_2n = M_PI / (2 * n);
+  double pi_4n = M_PI / (4 * n);
+  for (int j = 0; j < n; j++) {
+    double ejc = (j == 0) ? sqrt(0.5) : 1.0;
+    double ej3 = ((j == 0) || (j == (n - 1))) ? 0.5 : 1.0;
+    double ejs = (j == (n - 1)) ? 0.5 : 1.0;
+    for (int k = 0; k < n; k++) {
+      CII[j][k] = scale * ejc * cos(j * (2 * k + 1) * pi_2n);          /* setup_CII  (1074-1093) */
+      CIIe[j][k] = scale * cos(j * (2 * k + 1) * pi_2n);               /* setup_CIIe (1095-1111) */
+      CIIIe[k][j] = scale * ej3 * cos(j * (2 * k + 1) * pi_2n);        /* setup_CIIIe (1113-1133) */
+      SIIe[j][k] = scale * sin((j + 1) * (2 * k + 1) * pi_2n);         /* setup_SIIe (1154-1170) */
+      SIIIe[k][j] = scale * ejs * sin((j + 1) * (2 * k + 1) * pi_2n);  /* setup_SIIIe (1172-1192) */
+    }
+  }
+  for (int j = 0; j < n; j++)                                          /* setup_CIV (1136-1152) */
+    for (int k = j; k < n; k++) {
+      CIV[j][k] = scale * cos((2 * j + 1) * (2 * k + 1) * pi_4n);
+      CIV[k][j] = CIV[j][k];
+    }
+  double f = M_PI / (2.0 * n);                                         /* set_window(1) (674-694) */
+  for (int i = 0; i < n; i++) HWINDOW[i] = sin(f * (i + 0.5));
+  /* set_fold_2d index part (146-170) */
+  for (int i = 0; i < n; i++) {
+    int fi[2][6], fj[2][6];
+    fold_indices(i, n, fi);
+    for (int j = 0; j < n; j++) {
+      fold_indices(j, n, fj);
+      int vert_ind[2] = {fi[0][0], fi[1][0]};
+      int hor_ind[2] = {fj[0][0], fj[1][0]};
+      for (int k = 0; k < 4; k++) FOLD_INDEX[n * i + j][k] = 2 * n * vert_ind[(k >> 1) & 1] + hor_ind[k & 1];
+    }
+  }
+  /* set_unfold_2d (405-434) */
+  int n2 = 2 * n;
+  for (int i = 0; i < n2; i++) {
+    int iv[3];
+    unfold_index_signs(i, n, iv);
+    double wv = HWINDOW[(i < n) ? i : n2 - i - 1];
+    double k_vert[2] = {iv[1] * wv, iv[2] * wv};
+    int index_vert = iv[0] * n;
+    for (int j = 0; j < n2; j++) {
+      int ih[3];
+      unfold_index_signs(j, n, ih);
+      double wh = HWINDOW[(j < n) ? j : n2 - j - 1];
+      double k_hor[2] = {ih[1] * wh, ih[2] * wh};
+      UNFOLD_INDEX[n2 * i + j] = index_vert + ih[0];
+      for (int mode = 0; mode < 4; mode++) UNFOLD_K[mode][n2 * i + j] = k_vert[(mode >> 1) & 1] * k_hor[mode & 1];
+    }
+  }
+}
+static void tables(void) { pthread_once(&tables_once, init_tables); }
+
+static int ilog2(int n) { int i = 0; for (; n > 1; n >>= 1) i++; return i; }
+
+static void dctiv_recurs(const double *x, int n, double *y);
+
+/* DttRad2._dctii_recurs (1083-1105) */
+static void dctii_recurs(const double *x, int n, double *y) {
+  if (n == 2) { y[0] = x[0] + x[1]; y[1] = x[0] - x[1]; return; }
+  int n1 = n >> 1;
+  double u0[4] = {0}, u1[4] = {0}, v0[4], v1[4];
+  for (int j = 0; j < n1; j++) {
+    u0[j] = (x[j] + x[n - j - 1]);
+    u1[j] = (x[j] - x[n - j - 1]);
+  }
+  dctii_recurs(u0, n1, v0);
+  dctiv_recurs(u1, n1, v1);
+  for (int j = 0; j < n1; j++) { y[2 * j] = v0[j]; y[2 * j + 1] = v1[j]; }
+}
+
+/* DttRad2._dctiv_recurs (1107-1146) */
+static void dctiv_recurs(const double *x, int n, double *y) {
+  if (n == 2) {
+    y[0] = COSPI_1_8_SQRT2 * x[0] + COSPI_3_8_SQRT2 * x[1];
+    y[1] = COSPI_3_8_SQRT2 * x[0] - COSPI_1_8_SQRT2 * x[1];
+    return;
+  }
+  int n1 = n >> 1;
+  int t = ilog2(n1) - 1;
+  double u0[4] = {0}, u1[4] = {0}, v0[4], v1[4], w0[4] = {0}, w1[4] = {0};
+  for (int j = 0; j < n1; j++) {
+    u0[j] = (CN1[t][j] * x[j] + SN1[t][j] * x[n - j - 1]);
+    u1[j] = (double)(1 - 2 * (j & 1)) * (-SN1[t][n1 - j - 1] * x[n1 - j - 1] + CN1[t][n1 - j - 1] * x[n1 + j]);
+  }
+  dctii_recurs(u0, n1, v0);
+  dctii_recurs(u1, n1, v1);
+  w0[0] = SQRT2 * v0[0];
+  w1[n1 - 1] = SQRT2 * v1[0];
+  for (int j = 0; j < n1; j++) {
+    int sgn = (1 - 2 * (j & 1));
+    if (j > 0) w0[j] = v0[j] - sgn * v1[n1 - j];
+    if (j < (n1 - 1)) w1[j] = v0[j + 1] - sgn * v1[n1 - j - 1];
+  }
+  for (int j = 0; j < n1; j++) { y[2 * j] = w0[j]; y[2 * j + 1] = w1[j]; }
+}
+
+void or_dct_iv8(const double *x, double *y) {  /* dct_iv (80-85) */
+  tables();
+  dctiv_recurs(x, 8, y);
+  double scale = 1.0 / sqrt(8);
+  for (int i = 0; i < 8; i++) y[i] *= scale;
+}
+
+void or_dst_iv8(const double *x, double *y) {  /* dst_iv (87-98) */
+  tables();
+  double xr[8];
+  for (int i = 0, j = 7; i < 8; i++) xr[i] = x[j--];
+  dctiv_recurs(xr, 8, y);
+  double scale = 1.0 / sqrt(8);
+  for (int i = 0; i < 8; i++) { y[i] *= scale; scale = -scale; }
+}
+
+void or_dct_ii8(const double *x, double *y) {  /* dct_ii (68-78) */
+  tables();
+  dctii_recurs(x, 8, y);
+  double scale = 1.0 / sqrt(8);
+  for (int i = 0; i < 8; i++) y[i] *= scale;
+}
+
+static void mat8(const double m[8][8], const double *x, double *y) {
+  for (int i = 0; i < 8; i++) {
+    y[i] = 0.0;
+    for (int j = 0; j < 8; j++) y[i] += m[i][j] * x[j];
+  }
+}
+
+void or_dctiv_direct(const double *x, double *y) { tables(); mat8(CIV, x, y); }
+
+/* generic two-pass separable transform with transposed store (dttt_* pattern) */
+static void dttt_generic(const double *x, double *y, int mode,
+                         void (*fc)(const double *, double *), void (*fs)(const double *, double *)) {
+  double line[8], out[8], tmp[64];
+  for (int i = 0; i < 8; i++) {
+    memcpy(line, x + 8 * i, sizeof(line));
+    ((mode & 1) ? fs : fc)(line, out);
+    for (int j = 0; j < 8; j++) tmp[j * 8 + i] = out[j];
+  }
+  for (int i = 0; i < 8; i++) {
+    memcpy(line, tmp + 8 * i, sizeof(line));
+    ((mode & 2) ? fs : fc)(line, out);
+    memcpy(y + 8 * i, out, sizeof(out));
+  }
+}
+static void dctiie_direct(const double *x, double *y) { mat8(CIIe, x, y); }
+static void dstiie_direct(const double *x, double *y) { mat8(SIIe, x, y); }
+static void dctiiie_direct(const double *x, double *y) { mat8(CIIIe, x, y); }
+static void dstiiie_direct(const double *x, double *y) { mat8(SIIIe, x, y); }
+
+void or_dttt_iv(const double *x, double *y, int mode) { tables(); dttt_generic(x, y, mode, or_dct_iv8, or_dst_iv8); }
+void or_dttt_iie(const double *x, double *y, int mode) { tables(); dttt_generic(x, y, mode, dctiie_direct, dstiie_direct); }
+void or_dttt_iiie(const double *x, double *y, int mode) { tables(); dttt_generic(x, y, mode, dctiiie_direct, dstiiie_direct); }
+
+void or_hwindow(double *hw8) { tables(); memcpy(hw8, HWINDOW, sizeof(HWINDOW)); }
+void or_fold_index(int fi[64][4]) { tables(); memcpy(fi, FOLD_INDEX, sizeof(FOLD_INDEX)); }
+
+/* DttRad2.get_shifted_fold_2d (263-314) */
+void or_shifted_fold(double shift_hor, double shift_vert, double fold_sk[4][64][4]) {
+  tables();
+  const int n = 8, n2 = 16;
+  double ahc = cos(M_PI / n2 * shift_hor);
+  double ahs = sin(M_PI / n2 * shift_hor);
+  double avc = cos(M_PI / n2 * shift_vert);
+  double avs = sin(M_PI / n2 * shift_vert);
+  for (int i = 0; i < n; i++) {
+    int fi[2][6];
+    fold_indices(i, n, fi);
+    double vw0 = avc * HWINDOW[fi[0][1]] + avs * HWINDOW[fi[0][4]] * fi[0][5];
+    double vw1 = avc * HWINDOW[fi[1][1]] + avs * HWINDOW[fi[1][4]] * fi[1][5];
+    double vert_k[2][2] = {{fi[0][2] * vw0, fi[1][2] * vw1}, {fi[0][3] * vw0, fi[1][3] * vw1}};
+    for (int j = 0; j < n; j++) {
+      int fj[2][6];
+      fold_indices(j, n, fj);
+      double hw0 = ahc * HWINDOW[fj[0][1]] + ahs * HWINDOW[fj[0][4]] * fj[0][5];
+      double hw1 = ahc * HWINDOW[fj[1][1]] + ahs * HWINDOW[fj[1][4]] * fj[1][5];
+      double hor_k[2][2] = {{fj[0][2] * hw0, fj[1][2] * hw1}, {fj[0][3] * hw0, fj[1][3] * hw1}};
+      int indx = n * i + j;
+      for (int mode = 0; mode < 4; mode++)
+        for (int k = 0; k < 4; k++)
+          fold_sk[mode][indx][k] = vert_k[(mode >> 1) & 1][(k >> 1) & 1] * hor_k[mode & 1][k & 1];
+    }
+  }
+}
+
+/* DttRad2.fold_tile (724-738) */
+void or_fold_tile(const double *x, int mode, const double fold_k[4][64][4], double *y) {
+  tables();
+  for (int i = 0; i < 64; i++) {
+    y[i] = 0;
+    for (int k = 0; k < 4; k++) y[i] += x[FOLD_INDEX[i][k]] * fold_k[mode][i][k];
+  }
+}
+
+/* DttRad2.unfold_tile (770-780) */
+void or_unfold_tile(const double *x, int mode, double *y) {
+  tables();
+  for (int i = 0; i < 256; i++) y[i] = UNFOLD_K[mode][i] * x[UNFOLD_INDEX[i]];
+}
+
+/* DttRad2.corr_unfold_tile (443-489) */
+void or_corr_unfold_tile(const double q[4][64], double *rslt) {
+  const int ts = 8, cs = 15;
+  const double sc = 0.25;
+  rslt[cs * ts - ts] = sc * q[0][0];
+  for (int j = 1; j < ts; j++) {
+    rslt[cs * ts - ts + j] = sc * (q[0][j] + q[1][j - 1]);
+    rslt[cs * ts - ts - j] = sc * (q[0][j] - q[1][j - 1]);
+  }
+  for (int i = 1; i < ts; i++) {
+    rslt[cs * (ts + i) - ts] = sc * (q[0][i * ts] + q[2][(i - 1) * ts]);
+    rslt[cs * (ts - i) - ts] = sc * (q[0][i * ts] - q[2][(i - 1) * ts]);
+    for (int j = 1; j < ts; j++) {
+      double a = q[0][i * ts + j], b = q[1][i * ts + j - 1], c = q[2][(i - 1) * ts + j], d = q[3][(i - 1) * ts + j - 1];
+      rslt[cs * (ts + i) - ts + j] = sc * (a + b + c + d);
+      rslt[cs * (ts + i) - ts - j] = sc * (a + -b + c + -d);
+      rslt[cs * (ts - i) - ts + j] = sc * (a + b + -c + -d);
+      rslt[cs * (ts - i) - ts - j] = sc * (a + -b + -c + d);
+    }
+  }
+}
+
+/* DttRad2.getWin2d (697-713) */
+void or_win2d(double *rslt) {
+  tables();
+  const int size = 8, size2 = 16;
+  for (int i = 0; i < size; i++) {
+    int ia0 = i * size2, ia1 = (size2 - i - 1) * size2;
+    for (int j = 0; j < size; j++) {
+      double d = HWINDOW[i] * HWINDOW[j];
+      rslt[ia0 + j] = d; rslt[ia1 + j] = d;
+      rslt[ia0 + size2 - j - 1] = d; rslt[ia1 + size2 - j - 1] = d;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* ImageDtt stage 2 (J/tileprocessor/ImageDtt.java)                           */
+/* ------------------------------------------------------------------------- */
+
+/* java.lang.Math.round(double): round half up, exact */
+static long java_round(double x) {
+  double f = floor(x);
+  return (long)((x - f >= 0.5) ? f + 1.0 : f);
+}
+
+/* ImageDtt.convolve_tile (5429-5488) */
+void or_convolve_tile(double data[4][64], const double *kernel) {
+  static const int zi[4][4] = {{0, -1, -2, 3}, {1, 0, -3, -2}, {2, -3, 0, -1}, {3, 2, 1, 0}};
+  double rslt[4][64];
+  for (int i = 0; i < 64; i++)
+    for (int n = 0; n < 4; n++) {
+      rslt[n][i] = 0;
+      for (int k = 0; k < 4; k++) {
+        if (zi[n][k] < 0) rslt[n][i] -= data[-zi[n][k]][i] * kernel[k * 64 + i];
+        else rslt[n][i] += data[zi[n][k]][i] * kernel[k * 64 + i];
+      }
+    }
+  memcpy(data, rslt, sizeof(rslt));
+}
+
+/* ImageDtt.fract_shift (5490-5584) */
+void or_fract_shift(double clt[4][64], double shiftX, double shiftY) {
+  const int ts = 8;
+  double cos_hor[64], sin_hor[64], cos_vert[64], sin_vert[64];
+  for (int i = 0; i < ts; i++) {
+    double ch = cos((i + 0.5) * M_PI * shiftX / ts);
+    double sh = sin((i + 0.5) * M_PI * shiftX / ts);
+    double cv = cos((i + 0.5) * M_PI * shiftY / ts);
+    double sv = sin((i + 0.5) * M_PI * shiftY / ts);
+    for (int j = 0; j < ts; j++) {
+      int iv = ts * j + i, ih = ts * i + j;
+      cos_hor[ih] = ch; sin_hor[ih] = sh;
+      cos_vert[iv] = cv; sin_vert[iv] = sv;
+    }
+  }
+  double t[4][64];
+  for (int i = 0; i < 64; i++) {
+    t[0][i] = clt[0][i] * cos_hor[i] - clt[1][i] * sin_hor[i];
+    t[1][i] = clt[1][i] * cos_hor[i] + clt[0][i] * sin_hor[i];
+    t[2][i] = clt[2][i] * cos_hor[i] - clt[3][i] * sin_hor[i];
+    t[3][i] = clt[3][i] * cos_hor[i] + clt[2][i] * sin_hor[i];
+  }
+  for (int i = 0; i < 64; i++) {
+    clt[0][i] = t[0][i] * cos_vert[i] - t[2][i] * sin_vert[i];
+    clt[2][i] = t[2][i] * cos_vert[i] + t[0][i] * sin_vert[i];
+    clt[1][i] = t[1][i] * cos_vert[i] - t[3][i] * sin_vert[i];
+    clt[3][i] = t[3][i] * cos_vert[i] + t[1][i] * sin_vert[i];
+  }
+}
+
+/* ImageDtt.extract_correct_tile (4867-5426), non-debug branch */
+void or_extract_correct_tile(const double *image, int width, int height,
+                             const double *kern, const double *kext,
+                             int kh, int kv, int kernel_step,
+                             double centerX, double centerY,
+                             double clt[4][64], double residual[2], int int_tl[2], int ktile[2]) {
+  tables();
+  const int ts = 8, ts2 = 16;
+  int use_kernels = (kern != NULL);
+  double px = centerX - ts, py = centerY - ts;
+  int ktileX = 0, ktileY = 0;
+  if (use_kernels) {
+    ktileX = (int)java_round(centerX / kernel_step) + 1;
+    ktileY = (int)java_round(centerY / kernel_step) + 1;
+    if (ktileY < 0) ktileY = 0; else if (ktileY >= kv) ktileY = kv - 1;
+    if (ktileX < 0) ktileX = 0; else if (ktileX >= kh) ktileX = kh - 1;
+    const double *ce = kext + ((size_t)ktileY * kh + ktileX) * 8;
+    double kdx = centerX - (ktileX - 1 + 0.5) * kernel_step;
+    double kdy = centerY - (ktileY - 1 + 0.5) * kernel_step;
+    px = centerX - ts - (ce[0] + ce[4] * kdx + ce[5] * kdy);
+    py = centerY - ts - (ce[1] + ce[6] * kdx + ce[7] * kdy);
+  }
+  int ctile_left = (int)-java_round(-px);
+  int ctile_top = (int)-java_round(-py);
+  residual[0] = -(px - ctile_left);
+  residual[1] = -(py - ctile_top);
+  if (int_tl) { int_tl[0] = ctile_left; int_tl[1] = ctile_top; }
+  if (ktile) { ktile[0] = ktileX; ktile[1] = ktileY; }
+  double tile_in[256];
+  for (int i = 0; i < ts2; i++) {
+    int pi = ctile_top + i;
+    if (pi < 0) pi &= 1;
+    else if (pi >= height) pi = height - 2 + (pi & 1);
+    for (int j = 0; j < ts2; j++) {
+      int pj = ctile_left + j;
+      if (pj < 0) pj &= 1;
+      else if (pj >= width) pj = width - 2 + (pj & 1);
+      tile_in[ts2 * i + j] = image[(size_t)pi * width + pj];
+    }
+  }
+  double fold_coeff[4][64][4];
+  or_shifted_fold(residual[0], residual[1], fold_coeff);
+  for (int mode = 0; mode < 4; mode++) {
+    double folded[64];
+    or_fold_tile(tile_in, mode, fold_coeff, folded);
+    or_dttt_iv(folded, clt[mode], mode);
+  }
+  if (use_kernels) or_convolve_tile(clt, kern + ((size_t)ktileY * kh + ktileX) * 256);
+}
+
+/* correlation LPF filter, ImageDtt.clt_aberrations_quad_corr_new (1662-1690) */
+void or_corr_lpf(double corr_sigma, double *filter) {
+  tables();
+  const int ts = 8;
+  double fd[64];
+  if (corr_sigma == 0) {
+    fd[0] = 1.0;
+    for (int i = 1; i < 64; i++) fd[i] = 0;
+  } else {
+    for (int i = 0; i < ts; i++)
+      for (int j = 0; j < ts; j++) fd[i * ts + j] = exp(-(i * i + j * j) / (2 * corr_sigma));
+  }
+  double sum = 0;
+  for (int i = 0; i < ts; i++)
+    for (int j = 0; j < ts; j++) {
+      double d = fd[i * ts + j];
+      d *= cos(M_PI * i / (2 * ts)) * cos(M_PI * j / (2 * ts));
+      if (i > 0) d *= 2.0;
+      if (j > 0) d *= 2.0;
+      sum += d;
+    }
+  for (int i = 0; i < 64; i++) fd[i] /= sum;
+  or_dttt_iiie(fd, filter, 0);
+  for (int i = 0; i < 64; i++) filter[i] *= 2 * ts;
+}
+
+/* GPUTileProcessor.setCltLpf (814-848) + setLpfRbg scaling (780-812) */
+void or_clt_lpf(double sigma, double *lpf) {
+  tables();
+  const int ts = 8;
+  double l[64];
+  if (sigma == 0.0) {
+    l[0] = 1.0;
+    for (int i = 1; i < 64; i++) l[i] = 0.0;
+  } else {
+    for (int i = 0; i < ts; i++)
+      for (int j = 0; j < ts; j++) l[i * ts + j] = (double)(float)exp(-(i * i + j * j) / (2 * sigma));
+    double sum = 0;
+    for (int i = 0; i < ts; i++)
+      for (int j = 0; j < ts; j++) {
+        double d = l[i * ts + j];
+        d *= cos(M_PI * i / (2 * ts)) * cos(M_PI * j / (2 * ts));
+        if (i > 0) d *= 2.0;
+        if (j > 0) d *= 2.0;
+        sum += d;
+      }
+    for (int i = 0; i < 64; i++) l[i] /= sum;
+  }
+  or_dttt_iiie(l, lpf, 0);
+  for (int i = 0; i < 64; i++) lpf[i] = lpf[i] * 2 * ts;
+}
+
+/* ------------------------------------------------------------------------- */
+/* GeometryCorrection (J/tileprocessor/GeometryCorrection.java)               */
+/* ------------------------------------------------------------------------- */
+
+static void mat3_mul(const double a[3][3], const double b[3][3], double c[3][3]) {
+  /* Jama Matrix.times: c[i][j] = sum_k a[i][k]*b[k][j] accumulated in k order */
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += a[i][k] * b[k][j];
+      c[i][j] = s;
+    }
+}
+
+/* CorrVector.getRotMatrices (1043-1076) with ROT_AZ_SGN=-1, ROT_TL_SGN=1, ROT_RL_SGN=1 */
+void or_rot_matrices(const or_geometry *g, double rots[][3][3]) {
+  for (int chn = 0; chn < g->num_sensors; chn++) {
+    double ca = cos(g->azimuth[chn]), sa = sin(g->azimuth[chn]);
+    double ct = cos(g->tilt[chn]), st = sin(g->tilt[chn]);
+    double zoom = (1.0 + g->zoom[chn]);
+    double cr = cos(g->roll[chn]) * zoom, sr = sin(g->roll[chn]) * zoom;
+    double a_az[3][3] = {{ca, 0.0, sa * -1.0}, {0.0, 1.0, 0.0}, {-sa * -1.0, 0.0, ca}};
+    double a_t[3][3] = {{1.0, 0.0, 0.0}, {0.0, ct, st * 1.0}, {0.0, -st * 1.0, ct}};
+    double a_r[3][3] = {{cr, sr * 1.0, 0.0}, {-sr * 1.0, cr, 0.0}, {0.0, 0.0, 1.0}};
+    double tmp[3][3];
+    mat3_mul(a_t, a_az, tmp);
+    mat3_mul(a_r, tmp, rots[chn]);
+  }
+}
+
+/* CorrVector.getRotDeriveMatrices (1083-1147): [chn][0 az, 1 tilt, 2 roll, 3 zoom] */
+void or_rot_deriv_matrices(const or_geometry *g, double d[][4][3][3]) {
+  for (int chn = 0; chn < g->num_sensors; chn++) {
+    double ca = cos(g->azimuth[chn]), sa = sin(g->azimuth[chn]);
+    double ct = cos(g->tilt[chn]), st = sin(g->tilt[chn]);
+    double zoom = (1.0 + g->zoom[chn]);
+    double cr = cos(g->roll[chn]), sr = sin(g->roll[chn]);
+    double a_az[3][3] = {{ca, 0.0, sa * -1.0}, {0.0, 1.0, 0.0}, {-sa * -1.0, 0.0, ca}};
+    double a_t[3][3] = {{1.0, 0.0, 0.0}, {0.0, ct, st * 1.0}, {0.0, -st * 1.0, ct}};
+    double a_r[3][3] = {{cr * zoom, sr * zoom * 1.0, 0.0}, {-sr * zoom * 1.0, cr * zoom, 0.0}, {0.0, 0.0, 1.0}};
+    double a_daz[3][3] = {{-sa, 0.0, ca * -1.0}, {0.0, 0.0, 0.0}, {-ca * -1.0, 0.0, -sa}};
+    double a_dt[3][3] = {{0.0, 0.0, 0.0}, {0.0, -st, ct * 1.0}, {0.0, -ct * 1.0, -st}};
+    double a_dr[3][3] = {{-sr * zoom, cr * zoom * 1.0, 0.0}, {-cr * zoom * 1.0, -sr * zoom, 0.0}, {0.0, 0.0, 0.0}};
+    double a_dzoom[3][3] = {{cr, sr * 1.0, 0.0}, {-sr * 1.0, cr, 0.0}, {0.0, 0.0, 0.0}};
+    double tmp[3][3];
+    mat3_mul(a_t, a_daz, tmp); mat3_mul(a_r, tmp, d[chn][0]);
+    mat3_mul(a_dt, a_az, tmp); mat3_mul(a_r, tmp, d[chn][1]);
+    mat3_mul(a_t, a_az, tmp); mat3_mul(a_dr, tmp, d[chn][2]);
+    mat3_mul(a_t, a_az, tmp); mat3_mul(a_dzoom, tmp, d[chn][3]);
+  }
+}
+
+/* calcReverseDistortionTable (2707-2757): stepR=0.001, maxR=2.0 */
+int or_reverse_distortion_table(const or_geometry *g, double *tbl, int cap) {
+  const double delta = 1E-8, minDerivative = 0.1, stepR = 0.001, maxR = 2.0;
+  const int numIterations = 1000;
+  double drDistDr = 1.0;
+  double A8 = g->distortion[6], A7 = g->distortion[5], A6 = g->distortion[4], A5 = g->distortion[3];
+  double A = g->distortion[2], B = g->distortion[1], C = g->distortion[0];
+  int use8 = (A8 != 0.0) || (A7 != 0.0) || (A6 != 0.0);
+  double d = 1.0 - A8 - A7 - A6 - A5 - A - B - C;
+  double rPrev = 0.0;
+  int len = (int)ceil(maxR / stepR) + 1;
+  if (len > cap) return -1;
+  for (int j = 1; j < len; j++) tbl[j] = NAN;
+  tbl[0] = 1.0 / d;
+  for (int i = 1; i < len; i++) {
+    double rDist = stepR * i;
+    double r = rPrev + stepR / drDistDr;
+    for (int it = 0; it < numIterations; it++) {
+      double k;
+      if (use8) {
+        k = (((((((A8)*r + A7) * r + A6) * r + A5) * r + A) * r + B) * r + C) * r + d;
+        drDistDr = (((((((8 * A8) * r + 7 * A7) * r + 6 * A6) * r + 5 * A5) * r + 4 * A) * r + 3 * B) * r + 2 * C) * r + d;
+      } else {
+        k = (((A5 * r + A) * r + B) * r + C) * r + d;
+        drDistDr = (((5 * A5 * r + 4 * A) * r + 3 * B) * r + 2 * C) * r + d;
+      }
+      double rD = r * k;
+      if (drDistDr < minDerivative) return len; /* bail out: rest stays NaN */
+      if (fabs(rD - rDist) < delta) break;
+      r += (rDist - rD) / drDistDr;
+    }
+    rPrev = r;
+    tbl[i] = r / rDist;
+  }
+  return len;
+}
+
+/* getRByRDist (2802-2827) */
+double or_r_by_rdist(const double *tbl, int len, double rDist) {
+  const double stepR = 0.001;
+  if (rDist < 0) return NAN;
+  int index = (int)floor(rDist / stepR);
+  if (index >= (len - 1)) return NAN;
+  return tbl[index] + (tbl[index + 1] - tbl[index]) * (rDist / stepR - index);
+}
+
+static void mat3_vec(const double m[3][3], const double v[3], double r[3]) {
+  for (int i = 0; i < 3; i++) {
+    double s = 0;
+    for (int k = 0; k < 3; k++) s += m[i][k] * v[k];
+    r[i] = s;
+  }
+}
+
+/* getPortsCoordinatesAndDerivatives (2159-2314), main camera (gc_main == this, no rig) */
+void or_ports(const or_geometry *g, const double rots[][3][3], const double drots[][4][3][3],
+              const double *tbl, int tbl_len, double px, double py, double disparity,
+              double pXY[][2], double deriv[][2][4]) {
+  double pXcd = px - 0.5 * g->pixel_width;
+  double pYcd = py - 0.5 * g->pixel_height;
+  double rD = sqrt(pXcd * pXcd + pYcd * pYcd) * 0.001 * g->pixel_size;
+  double rND2R = or_r_by_rdist(tbl, tbl_len, rD / g->distortion_radius);
+  double pXc = pXcd * rND2R;
+  double pYc = pYcd * rND2R;
+  const double *rad_coeff = g->distortion; /* C, B, A, A5, A6, A7, A8 */
+  double fl_pix = g->focal_length / (0.001 * g->pixel_size);
+  double ri_scale = 0.001 * g->pixel_size / g->distortion_radius;
+  for (int i = 0; i < g->num_sensors; i++) {
+    double pXci0 = pXc - disparity * g->rXY[i][0];
+    double pYci0 = pYc - disparity * g->rXY[i][1];
+    double vi[3] = {pXci0, pYci0, fl_pix};
+    double rvi[3];
+    mat3_vec(rots[i], vi, rvi);
+    double norm_z = fl_pix / rvi[2];
+    double pXci = rvi[0] * norm_z;
+    double pYci = rvi[1] * norm_z;
+    double rNDi = sqrt(pXci * pXci + pYci * pYci);
+    double ri = rNDi * ri_scale;
+    double rD2rND = 1.0, rri = 1.0;
+    for (int j = 0; j < 7; j++) {
+      rri *= ri;
+      rD2rND += rad_coeff[j] * (rri - 1.0);
+    }
+    double pXid = pXci * rD2rND;
+    double pYid = pYci * rD2rND;
+    pXY[i][0] = pXid + g->pXY0[i][0];
+    pXY[i][1] = pYid + g->pXY0[i][1];
+    if (deriv) {
+      double dr[4][3];
+      for (int k = 0; k < 4; k++) mat3_vec(drots[i][k], vi, dr[k]);
+      double dpX[4], dpY[4];
+      for (int k = 0; k < 4; k++) { /* az, tilt, roll, zoom */
+        dpX[k] = dr[k][0] * norm_z - pXci * dr[k][2] / rvi[2];
+        dpY[k] = dr[k][1] * norm_z - pYci * dr[k][2] / rvi[2];
+      }
+      double drD2rND_dri = 0.0;
+      rri = 1.0;
+      for (int j = 0; j < 7; j++) {
+        drD2rND_dri += rad_coeff[j] * (j + 1) * rri;
+        rri *= ri;
+      }
+      for (int k = 0; k < 4; k++) {
+        if (k == 2) { /* roll: reference drops the radial term (2279-2280) */
+          deriv[i][0][k] = dpX[k] * rD2rND;
+          deriv[i][1][k] = dpY[k] * rD2rND;
+        } else {
+          double dri = ri_scale / rNDi * (pXci * dpX[k] + pYci * dpY[k]);
+          double drD = drD2rND_dri * dri;
+          deriv[i][0][k] = dpX[k] * rD2rND + pXci * drD;
+          deriv[i][1][k] = dpY[k] * rD2rND + pYci * drD;
+        }
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Correlation2d (J/tileprocessor/Correlation2d.java)                         */
+/* ------------------------------------------------------------------------- */
+
+void or_default_corr_params(or_corr_params *p) {
+  /* ImageDttParameters.java:30-112 defaults, fat_zero/corr_sigma per config */
+  p->fat_zero = 0.05;
+  p->corr_sigma = 0.8;       /* CLTParameters.corr_sigma default */
+  p->corr_red = 0.5;
+  p->corr_blue = 0.2;
+  p->corr_offset = 0.1;
+  p->min_corr = 0.02;
+  p->corr_strip_hight = 9;
+  p->twice_diagonal = 1;
+  p->enhortho_width = 2;
+  p->enhortho_scale = 0.0;
+  p->corr_wndy_size = 2; p->corr_wndy_hwidth = 1.0; p->corr_wndy_blur = 1.0;
+  p->corr_wndx_size = 9; p->corr_wndx_hwidth = 6.0; p->corr_wndx_blur = 5.0;
+}
+
+void or_quad_pairs(or_pairs *pp) {
+  /* PAIRS[0..5] (Correlation2d.java:52-58) */
+  static const int c1[6] = {0, 2, 0, 1, 0, 2}, c2[6] = {1, 3, 2, 3, 3, 1}, kind[6] = {0, 0, 1, 1, 2, 3};
+  static const double bx[6] = {1, 1, 0, 0, 1, 1}, by[6] = {0, 0, 1, 1, 1, -1};
+  memset(pp, 0, sizeof(*pp));
+  pp->num_pairs = 6;
+  for (int i = 0; i < 6; i++) {
+    pp->cam1[i] = c1[i]; pp->cam2[i] = c2[i]; pp->kind[i] = kind[i];
+    pp->bx[i] = bx[i]; pp->by[i] = by[i];
+  }
+  pp->combo_mask_lo = 0x3f;
+  pp->combo_mask_hi = 0;
+}
+
+/* correlateSingleColorFD (197-231) */
+static void correlate_single(const double *d1, const double *d2, double fat_zero, double t[4][64]) {
+  static const int ZI[4][4] = {{0, 1, 2, 3}, {-1, 0, -3, 2}, {-2, -3, 0, 1}, {3, -2, -1, 0}};
+  double a2[64], sa2 = 0.0;
+  for (int i = 0; i < 64; i++) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int n = 0; n < 4; n++) {
+      s1 += d1[n * 64 + i] * d1[n * 64 + i];
+      s2 += d2[n * 64 + i] * d2[n * 64 + i];
+    }
+    a2[i] = sqrt(s1 * s2);
+    sa2 += a2[i];
+  }
+  double fz2 = sa2 / 64 * fat_zero * fat_zero;
+  for (int i = 0; i < 64; i++) {
+    double scale = 1.0 / (a2[i] + fz2);
+    for (int n = 0; n < 4; n++) {
+      t[n][i] = 0;
+      for (int k = 0; k < 4; k++) {
+        if (ZI[n][k] < 0) t[n][i] -= d1[(-ZI[n][k]) * 64 + i] * d2[k * 64 + i];
+        else t[n][i] += d1[ZI[n][k] * 64 + i] * d2[k * 64 + i];
+      }
+      t[n][i] *= scale;
+    }
+  }
+}
+
+/* correlateCompositeFD (275-328) */
+void or_correlate_pair(const double *clt1, const double *clt2, int nc, const double *col_weights,
+                       const double *lpf, double fat_zero, double *corr) {
+  double one = 1.0;
+  if (nc == 1) col_weights = &one;
+  double acc[4][64], t[4][64];
+  for (int col = 0; col < nc; col++) {
+    correlate_single(clt1 + col * 256, clt2 + col * 256, fat_zero, t);
+    for (int n = 0; n < 4; n++)
+      for (int i = 0; i < 64; i++) {
+        if (col == 0) acc[n][i] = t[n][i] * col_weights[col];
+        else acc[n][i] += t[n][i] * col_weights[col];
+      }
+  }
+  if (lpf)
+    for (int n = 0; n < 4; n++)
+      for (int i = 0; i < 64; i++) acc[n][i] *= lpf[i];
+  double q[4][64];
+  for (int quadrant = 0; quadrant < 4; quadrant++) {
+    int mode = ((quadrant << 1) & 2) | ((quadrant >> 1) & 1);
+    or_dttt_iie(acc[quadrant], q[quadrant], mode);
+  }
+  or_corr_unfold_tile(q, corr);
+}
+
+static double corr_at(const double *c, int iy, int ix) { return c[iy * 15 + ix]; }
+
+/*
+ * scaleRotateInterpoateSingleCorrelation (610-718) for kinds 0..3 with ss=1
+ * (exact restatement); kind 4 is the documented generalisation to an
+ * arbitrary baseline b: strip(row,col) samples the correlation at
+ * (col + (row&1)/2) * b +/- (row/2) * b_perp (b_perp = b rotated 90 deg),
+ * bilinearly interpolated, NaN outside the 15x15 support.  For b along the
+ * four quad directions the kind-4 sampler visits the same points.
+ */
+void or_strip(const double *corr, double bx, double by, int kind, int hwidth, double *strip) {
+  const int center = 7, width = 15;
+  for (int i = 0; i < hwidth * width; i++) strip[i] = 0.0;
+  if (kind <= 3) {
+    int dir = kind, ss = 1;
+    int denom = ss * ((dir > 1) ? 1 : 2);
+    double rdenom = denom;
+    int ilimit = center * denom;
+    int xnum = 0, ynum = 0;
+    for (int row = 0; row < hwidth; row++)
+      for (int scol = -center; scol <= center; scol++) {
+        int indx = row * width + scol + center;
+        for (int down = -1; down < ((row == 0) ? 0 : 2); down += 2) {
+          switch (dir) {
+            case 0: xnum = 2 * scol + (row & 1); ynum = down * row; break;
+            case 1: xnum = down * row; ynum = 2 * scol + (row & 1); break;
+            case 2: xnum = scol - ((down * row) >> 1); ynum = scol + ((down * row + 1) >> 1); break;
+            default: xnum = scol - ((down * row) >> 1); ynum = -scol - ((down * row + 1) >> 1); break;
+          }
+          if ((xnum > ilimit) || (xnum < -ilimit) || (ynum > ilimit) || (ynum < -ilimit)) {
+            strip[indx] = NAN;
+          } else {
+            int ix0 = (xnum + ilimit) / denom, iy0 = (ynum + ilimit) / denom;
+            int int_x = (xnum % denom) == 0, int_y = (ynum % denom) == 0;
+            double d;
+            if (int_x && int_y) {
+              d = corr_at(corr, iy0, ix0);
+            } else {
+              double dx = (xnum + ilimit) / rdenom - ix0;
+              double dy = (ynum + ilimit) / rdenom - iy0;
+              if (int_y) d = (1.0 - dx) * corr_at(corr, iy0, ix0) + dx * corr_at(corr, iy0, ix0 + 1);
+              else if (int_x) d = (1.0 - dy) * corr_at(corr, iy0, ix0) + dy * corr_at(corr, iy0 + 1, ix0);
+              else
+                d = ((1.0 - dx) * (1.0 - dy) * corr_at(corr, iy0, ix0)) + (dx * (1.0 - dy) * corr_at(corr, iy0, ix0 + 1)) +
+                    ((1.0 - dx) * dy * corr_at(corr, iy0 + 1, ix0)) + (dx * dy * corr_at(corr, iy0 + 1, ix0 + 1));
+            }
+            if (row == 0) strip[indx] = d;
+            else strip[indx] += 0.5 * d;
+          }
+        }
+      }
+    return;
+  }
+  /* kind 4: general baseline */
+  for (int row = 0; row < hwidth; row++)
+    for (int scol = -center; scol <= center; scol++) {
+      int indx = row * width + scol + center;
+      for (int down = -1; down < ((row == 0) ? 0 : 2); down += 2) {
+        double a = scol + 0.5 * (row & 1), p = 0.5 * down * row;
+        double x = a * bx - p * by, y = a * by + p * bx;
+        if ((x > center) || (x < -center) || (y > center) || (y < -center)) {
+          strip[indx] = NAN;
+          continue;
+        }
+        double fx = x + center, fy = y + center;
+        int ix0 = (int)floor(fx), iy0 = (int)floor(fy);
+        if (ix0 > 2 * center - 1) ix0 = 2 * center - 1;
+        if (iy0 > 2 * center - 1) iy0 = 2 * center - 1;
+        double dx = fx - ix0, dy = fy - iy0;
+        double d = ((1.0 - dx) * (1.0 - dy) * corr_at(corr, iy0, ix0)) + (dx * (1.0 - dy) * corr_at(corr, iy0, ix0 + 1)) +
+                   ((1.0 - dx) * dy * corr_at(corr, iy0 + 1, ix0)) + (dx * dy * corr_at(corr, iy0 + 1, ix0 + 1));
+        if (row == 0) strip[indx] = d;
+        else strip[indx] += 0.5 * d;
+      }
+    }
+}
+
+/* combineInterpolatedCorrelations (730-790) */
+void or_combine_strips(const double *strips, const int *use, int np, const int *is_diag, int hwidth,
+                       double offset, int twice_diagonal, double *combo) {
+  int len = hwidth * 15, ncombined = 0, have = 0;
+  if (offset >= 0) {
+    for (int p = 0; p < np; p++) {
+      if (!use[p]) continue;
+      const double *s = strips + (size_t)p * len;
+      if (!have) { for (int i = 0; i < len; i++) combo[i] = 1.0; have = 1; }
+      /* the reference squares every selected pair when twice_diagonal is set (759-765) */
+      if (twice_diagonal) {
+        for (int i = 0; i < len; i++) { double d = s[i] + offset; if (d < 0.0) d = 0.0; combo[i] *= d * d; }
+        ncombined++;
+      } else {
+        for (int i = 0; i < len; i++) { double d = s[i] + offset; if (d < 0.0) d = 0.0; combo[i] *= d; }
+      }
+      ncombined++;
+    }
+    double pwr = 1.0 / ncombined;
+    if (have)
+      for (int i = 0; i < len; i++) if (combo[i] > 0.0) combo[i] = pow(combo[i], pwr) - offset;
+  } else {
+    for (int p = 0; p < np; p++) {
+      if (!use[p]) continue;
+      const double *s = strips + (size_t)p * len;
+      if (!have) { for (int i = 0; i < len; i++) combo[i] = 0.0; have = 1; }
+      if (twice_diagonal) { for (int i = 0; i < len; i++) combo[i] += 2 * s[i]; ncombined++; }
+      else { for (int i = 0; i < len; i++) combo[i] += s[i]; }
+      ncombined++;
+    }
+    double scale = 1.0 / ncombined;
+    for (int i = 0; i < len; i++) combo[i] *= scale;
+  }
+}
+
+/* getMaxXYInt (802-843), strip form => axis_only on row 0 */
+int or_max_xy_int_axis(const double *data, int hwidth, double minMax, int *ix) {
+  (void)hwidth;
+  int imx = 0;
+  for (int i = 1; i < 15; i++)
+    if (isnan(data[imx]) || (data[i] > data[imx])) imx = i;
+  if (!(data[imx] >= minMax)) return 0;
+  *ix = imx % 15 - 7;
+  return 1;
+}
+
+/* halfFlatTopWindow (1047-1081) */
+void or_half_flat_top_window(int ihwidth, double hwidth, double blur, int normalize, int notch,
+                             double scale, double *wnd) {
+  for (int i = 0; i < ihwidth; i++) {
+    if (blur <= 0.0) wnd[i] = (i < hwidth) ? 1.0 : 0.0;
+    else {
+      if (i < hwidth - blur / 2) wnd[i] = 1.0;
+      else if (i > hwidth + blur / 2) wnd[i] = 0.0;
+      else wnd[i] = 0.5 * (1.0 - sin(M_PI * (i - hwidth) / blur));
+    }
+    if (notch) wnd[i] = 1.0 - wnd[i];
+  }
+  if (normalize) {
+    double s = 0.0;
+    for (int i = 0; i < ihwidth; i++) s += ((i == 0) ? 1.0 : 2.0) * wnd[i];
+    s = 1 / s;
+    for (int i = 0; i < ihwidth; i++) wnd[i] *= s;
+  }
+  for (int i = 0; i < ihwidth; i++) wnd[i] *= scale;
+}
+
+/* getMaxXCm (936-1032) */
+int or_max_x_cm(const double *data, int hwidth, int ixcenter, const double *window_y, int wy_len,
+                const double *window_x, int wx_len, double rslt[3]) {
+  const int center = 7, data_width = 15;
+  int data_height = hwidth;
+  double wy_scale = 1.0;
+  if (data_height > wy_len) data_height = wy_len;
+  else if (data_height < wy_len) {
+    double swy = window_y[0];
+    for (int i = 1; i < data_height; i++) swy += window_y[i];
+    wy_scale = 1.0 / swy;
+  }
+  double s0 = 0.0, sx = 0.0, sx2 = 0.0;
+  int x0 = center + ixcenter;
+  for (int dy = 0; dy < data_height; dy++) {
+    int odd = dy & 1;
+    double wy = ((dy == 0) ? wy_scale : (2.0 * wy_scale)) * window_y[dy];
+    int indx0 = data_width * dy;
+    for (int adx = odd; adx < wx_len; adx += 2)
+      for (int dir = (adx == 0) ? 1 : -1; dir <= 1; dir += 2) {
+        int idx = (adx * dir) >> 1;
+        int x = 2 * idx + odd;
+        int x1 = x0 + idx;
+        if ((x1 >= 0) && (x1 < data_width)) {
+          double d = data[indx0 + x1];
+          if (!isnan(d) && (d > 0.0)) {
+            d *= wy * window_x[adx];
+            s0 += d;
+            sx += d * x;
+            sx2 += d * x * x;
+          }
+        }
+      }
+  }
+  if (s0 == 0.0) return 0;
+  rslt[0] = ixcenter + sx / s0 / 2;
+  rslt[1] = s0;
+  rslt[2] = sqrt(s0 * sx2 - sx * sx) / s0 / 2;
+  return 1;
+}
+
+/* createOrtoNotch (2654-2675) */
+void or_ortho_notch(double enhortho_width, double enhortho_scale, double *notch) {
+  const int ts = 8;
+  for (int i = 0; i < 15; i++) {
+    if ((i < (ts - enhortho_width)) || (i > (ts - 2 + enhortho_width))) notch[i] = 1.0;
+    else notch[i] = enhortho_scale;
+    if (i == (ts - 1)) notch[i] = 0.0;
+    notch[i] *= sin(M_PI * (i + 1.0) / (2 * ts));
+  }
+}
+
+/*
+ * getMaxXSOrtho (2502-2651), symmetric=true, offset>=0 branch.  The 3-point
+ * quadratic fit (PolynomialApproximation.polynomialApproximation1d, exact
+ * interpolation through 3 points) is evaluated in closed form.
+ */
+int or_max_xs_ortho(const double *corrs, const int *use, int np, double offset, int is_vert,
+                    const double *notch, double rslt[2]) {
+  const int cs = 15;
+  int pairs[OR_MAX_PAIRS], n = 0;
+  for (int p = 0; p < np; p++) if (use[p]) pairs[n++] = p;
+  if (n == 0) return 0;
+  double w = 1.0 / n;
+  double c1d[15];
+  for (int j = 0; j < cs; j++) {
+    c1d[j] = 0;
+    for (int i = 0; i < cs; i++) {
+      double combo = 1.0;
+      for (int ip = 0; ip < n; ip++) {
+        const double *c = corrs + (size_t)pairs[ip] * 225;
+        double d;
+        if (is_vert) d = (0.5 * (c[j * cs + i] + c[j * cs + (cs - i - 1)])) + offset;
+        else d = (0.5 * (c[i * cs + j] + c[(cs - i - 1) * cs + j])) + offset;
+        combo *= d;
+      }
+      if (combo > 0.0) combo = pow(combo, w) - offset;
+      else combo = -offset;
+      c1d[j] += combo * notch[i];
+    }
+  }
+  int icenter = 0;
+  for (int i = 1; i < cs; i++) if (c1d[i] > c1d[icenter]) icenter = i;
+  double xcenter = icenter;
+  if ((icenter > 0) && (icenter < (cs - 1))) {
+    double f0 = c1d[icenter - 1], f1 = c1d[icenter], f2 = c1d[icenter + 1];
+    double den = f0 - 2.0 * f1 + f2;
+    if (den != 0.0) xcenter = icenter + 0.5 * (f0 - f2) / den;
+  }
+  icenter = (int)java_round(xcenter);
+  if (icenter < 0) icenter = 0;
+  if (icenter > cs - 1) icenter = cs - 1;
+  rslt[0] = xcenter - 7;
+  rslt[1] = c1d[icenter] / ((cs + 1) / 2);
+  return 1;
+}
+
+/* ------------------------------------------------------------------------- */
+/* IMCLT (ImageDtt.iclt_2d, 3559-3666) into the padded frame                  */
+/* ------------------------------------------------------------------------- */
+void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty, double *frame, int fw) {
+  for (int dct_mode = 0; dct_mode < 4; dct_mode++) {
+    int idct_mode = ((dct_mode << 1) & 2) | ((dct_mode >> 1) & 1);
+    double tile_dct[64], mdct[256];
+    or_dttt_iv(clt[dct_mode], tile_dct, idct_mode);
+    or_unfold_tile(tile_dct, dct_mode, mdct);
+    for (int i = 0; i < 16; i++) {
+      double *row = frame + (size_t)(ty * 8 + i) * fw + tx * 8;
+      for (int j = 0; j < 16; j++) row[j] += scale * mdct[16 * i + j];
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Kernel preparation (QuadCLT.calculateCLTKernel 433-667, ImageDtt 4625-4851) */
+/* ------------------------------------------------------------------------- */
+void or_calc_clt_kernel(const double *src, int normalize, double clt[4][64], double extra[8]) {
+  tables();
+  const int src_size = 64, dtt_size = 8;
+  double dst[225 + 8];
+  memset(dst, 0, sizeof(dst));
+  /* clt_convert_double_kernel (4625-4672) */
+  static const int indices[9] = {0, -64, -1, 1, 64, -65, -63, 63, 65};
+  static const double weights[9] = {1.0, 0.5, 0.5, 0.5, 0.5, 0.25, 0.25, 0.25, 0.25};
+  int src_center = src_size / 2;
+  double sx = 0.0, sy = 0.0, s = 0.0;
+  int indx = 0;
+  for (int i = -src_center; i < src_center; i++)
+    for (int j = -src_center; j < src_center; j++) {
+      double d = src[indx++];
+      sx += j * d; sy += i * d; s += d;
+    }
+  int src_x = (int)java_round(sx / s) + src_center;
+  int src_y = (int)java_round(sy / s) + src_center;
+  if (src_x < 2 * dtt_size) src_x = 2 * dtt_size - 1;
+  else if (src_x > (src_size - 2 * dtt_size)) src_x = src_size - 2 * dtt_size;
+  if (src_y < 2 * dtt_size) src_y = 2 * dtt_size - 1;
+  else if (src_y > (src_size - 2 * dtt_size)) src_y = src_size - 2 * dtt_size;
+  indx = 0;
+  for (int i = -dtt_size + 1; i < dtt_size; i++) {
+    int src_i = (src_y + 2 * i) * src_size + src_x;
+    for (int j = -dtt_size + 1; j < dtt_size; j++) {
+      double d = 0.0;
+      for (int k = 0; k < 9; k++) d += weights[k] * src[src_i + 2 * j + indices[k]];
+      dst[indx++] = d;
+    }
+  }
+  dst[indx++] = 0.5 * (src_x - src_center);
+  dst[indx++] = 0.5 * (src_y - src_center);
+  dst[indx++] = 0.5 * (sx / s);
+  dst[indx++] = 0.5 * (sy / s);
+  /* clt_normalize_kernel (4674-4696) with norm_sym_weights (QuadCLT.java:465-472) */
+  if (normalize) {
+    double window[64];
+    for (int i = 0; i < dtt_size; i++)
+      for (int j = 0; j < dtt_size; j++)
+        window[i * dtt_size + j] = cos(M_PI * i / (2 * dtt_size)) * cos(M_PI * j / (2 * dtt_size));
+    double sn = 0.0;
+    indx = 0;
+    for (int i = -dtt_size + 1; i < dtt_size; i++) {
+      int ai = (i < 0) ? -i : i;
+      for (int j = -dtt_size + 1; j < dtt_size; j++) {
+        int aj = (j < 0) ? -j : j;
+        sn += dst[indx++] * window[ai * dtt_size + aj];
+      }
+    }
+    sn = 1.0 / sn;
+    for (int i = 0; i < 225; i++) dst[i] *= 16 * sn;
+  }
+  /* clt_symmetrize_kernel (4698-4723) */
+  double sym[4][64];
+  memset(sym, 0, sizeof(sym));
+  int in_size = 15, m1 = 7, center = m1 * in_size + m1;
+  for (int i = 0; i < dtt_size; i++) {
+    for (int j = 0; j < dtt_size; j++) {
+      int i0 = center - i * in_size - j, i1 = center - i * in_size + j;
+      int i2 = center + i * in_size - j, i3 = center + i * in_size + j;
+      sym[0][i * 8 + j] = 0.25 * (dst[i0] + dst[i1] + dst[i2] + dst[i3]);
+      if (j > 0) sym[1][i * 8 + j - 1] = 0.25 * (-dst[i0] + dst[i1] - dst[i2] + dst[i3]);
+      if (i > 0) sym[2][(i - 1) * 8 + j] = 0.25 * (-dst[i0] - dst[i1] + dst[i2] + dst[i3]);
+      if ((i > 0) && (j > 0)) sym[3][(i - 1) * 8 + (j - 1)] = 0.25 * (-dst[i0] + dst[i1] - dst[i2] + dst[i3]);
+    }
+    sym[1][i * 8 + m1] = 0.0;
+    sym[2][m1 * 8 + i] = 0.0;
+    sym[3][i * 8 + m1] = 0.0;
+    sym[3][m1 * 8 + i] = 0.0;
+  }
+  /* clt_dtt3_kernel (4725-4734) */
+  for (int q = 0; q < 4; q++) or_dttt_iiie(sym[q], clt[q], q);
+  for (int i = 0; i < 8; i++) extra[i] = dst[225 + i];
+}
+
+/* ImageDtt.clt_fill_coord_corr (4792-4851) for one colour plane ext[kv][kh][8] */
+void or_fill_coord_corr(double *ext, int kh, int kv, int kern_step) {
+  for (int ty = 0; ty < kv; ty++)
+    for (int tx = 0; tx < kh; tx++) {
+      double s0 = 0, sx = 0, sx2 = 0, sy = 0, sy2 = 0, sz = 0, sxz = 0, syz = 0, sw = 0, sxw = 0, syw = 0;
+      for (int dty = -1; dty < 2; dty++) {
+        int y = ty + dty;
+        if ((y < 0) || (y >= kv)) continue;
+        for (int dtx = -1; dtx < 2; dtx++) {
+          int x = tx + dtx;
+          if ((x < 0) || (x >= kh)) continue;
+          const double *ce = ext + ((size_t)y * kh + x) * 8;
+          s0 += 1; sx += dtx; sx2 += dtx * dtx; sy += dty; sy2 += dty * dty;
+          sz += ce[2]; sxz += dtx * ce[2]; syz += dty * ce[2];
+          sw += ce[3]; sxw += dtx * ce[3]; syw += dty * ce[3];
+        }
+      }
+      double *ce = ext + ((size_t)ty * kh + tx) * 8;
+      double denom_x = (sx2 * s0 - sx * sx) * kern_step;
+      double denom_y = (sy2 * s0 - sy * sy) * kern_step;
+      ce[4] = (sxz * s0 - sz * sx) / denom_x;
+      ce[5] = (syz * s0 - sz * sy) / denom_y;
+      ce[6] = (sxw * s0 - sw * sx) / denom_x;
+      ce[7] = (syw * s0 - sw * sy) / denom_y;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Driver: clt_aberrations_quad_corr_new tile loop (ImageDtt.java:1491-2824)   */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  const or_run_cfg *cfg;
+  const or_geometry *g;
+  const double *ports_in;
+  const double *const *images, *const *kern, *const *kext;
+  const int *tile_op;
+  const double *disparity;
+  const or_pairs *pairs;
+  const or_corr_params *cp;
+  double *ports, *clt, *corr, *disp;
+  int *int_tl;
+  double *residual;
+  double (*rots)[3][3];
+  double *tbl;
+  int tbl_len;
+  double filter[64];
+  double col_weights[3];
+  double wndx[32], wndy[32], notch[15];
+  int num_tiles;
+  volatile int next;
+} run_ctx;
+
+static void run_tile(run_ctx *c, int nTile, double *wk_clt, double *wk_corr, double *wk_strips) {
+  const or_run_cfg *cfg = c->cfg;
+  const int S = cfg->num_sensors, C = cfg->num_colors;
+  const int tilesX = cfg->width / 8;
+  int tileY = nTile / tilesX, tileX = nTile % tilesX;
+  const int P = c->pairs->num_pairs;
+  const int hw = c->cp->corr_strip_hight;
+  if (c->disp)
+    for (int i = 0; i < OR_DISP_N; i++)
+      c->disp[(size_t)nTile * OR_DISP_N + i] =
+          ((i == OR_DISP_STRENGTH) || (i == OR_DISP_HOR_STRENGTH) || (i == OR_DISP_VERT_STRENGTH)) ? 0.0 : NAN;
+  if (c->tile_op[nTile] == 0) return;
+  double centerX = tileX * 8 + 8 / 2;
+  double centerY = tileY * 8 + 8 / 2;
+  double pxy[OR_MAX_SENSORS][2];
+  if (cfg->use_ports_in) {
+    for (int i = 0; i < S; i++) {
+      pxy[i][0] = c->ports_in[((size_t)nTile * S + i) * 2];
+      pxy[i][1] = c->ports_in[((size_t)nTile * S + i) * 2 + 1];
+    }
+  } else {
+    or_ports(c->g, (const double(*)[3][3])c->rots, NULL, c->tbl, c->tbl_len, centerX, centerY,
+             c->disparity[nTile], pxy, NULL);
+  }
+  if (c->ports)
+    for (int i = 0; i < S; i++) {
+      c->ports[((size_t)nTile * S + i) * 2] = pxy[i][0];
+      c->ports[((size_t)nTile * S + i) * 2 + 1] = pxy[i][1];
+    }
+  /* stage 2: per colour, per sensor extract + fract_shift (1904-2061) */
+  for (int chn = 0; chn < C; chn++) {
+    for (int i = 0; i < S; i++) {
+      double(*t)[64] = (double(*)[64])(wk_clt + ((size_t)i * C + chn) * 256);
+      const double *kern = NULL, *kext = NULL;
+      if (cfg->kernels_hor > 0) {
+        size_t kplane = (size_t)cfg->kernels_hor * cfg->kernels_vert;
+        kern = c->kern[i] + kplane * 256 * chn;
+        kext = c->kext[i] + kplane * 8 * chn;
+      }
+      double res[2];
+      int tl[2];
+      or_extract_correct_tile(c->images[i * C + chn], cfg->width, cfg->height, kern, kext,
+                              cfg->kernels_hor, cfg->kernels_vert, cfg->kernel_step, pxy[i][0], pxy[i][1],
+                              t, res, tl, NULL);
+      or_fract_shift(t, res[0], res[1]);
+      size_t o = (((size_t)nTile * S + i) * C + chn) * 2;
+      if (c->int_tl) { c->int_tl[o] = tl[0]; c->int_tl[o + 1] = tl[1]; }
+      if (c->residual) { c->residual[o] = res[0]; c->residual[o + 1] = res[1]; }
+    }
+  }
+  if (c->clt) memcpy(c->clt + (size_t)nTile * S * C * 256, wk_clt, sizeof(double) * S * C * 256);
+  if (!cfg->corr) return;
+  /* stage 3 (2101-2245) */
+  for (int p = 0; p < P; p++)
+    or_correlate_pair(wk_clt + (size_t)c->pairs->cam1[p] * C * 256, wk_clt + (size_t)c->pairs->cam2[p] * C * 256, C,
+                      c->col_weights, c->filter, c->cp->fat_zero, wk_corr + (size_t)p * 225);
+  if (c->corr) memcpy(c->corr + (size_t)nTile * P * 225, wk_corr, sizeof(double) * P * 225);
+  if (!c->disp) return;
+  int use[OR_MAX_PAIRS], is_diag[OR_MAX_PAIRS];
+  for (int p = 0; p < P; p++) {
+    use[p] = (p < 64) ? ((c->pairs->combo_mask_lo >> p) & 1) : ((c->pairs->combo_mask_hi >> (p - 64)) & 1);
+    if (P > 6) use[p] = 1;
+    is_diag[p] = (c->pairs->kind[p] == 2) || (c->pairs->kind[p] == 3);
+    if (use[p]) or_strip(wk_corr + (size_t)p * 225, c->pairs->bx[p], c->pairs->by[p], c->pairs->kind[p], hw,
+                         wk_strips + (size_t)p * hw * 15);
+  }
+  double combo[15 * 32];
+  int general = P > 6;
+  for (int p = 0; p < P; p++) general |= (c->pairs->kind[p] == 4);
+  if (general) {
+    /* Generalised pair sets (not in the reference): the same geometric mean of
+     * the clipped offset strips, evaluated in the log domain so that products of
+     * up to 120 factors neither overflow nor underflow. */
+    int len = hw * 15, n = 0;
+    for (int p = 0; p < P; p++) n += use[p];
+    for (int i = 0; i < len; i++) {
+      double ls = 0.0;
+      int nan_ = 0, zero = 0;
+      for (int p = 0; p < P; p++) {
+        if (!use[p]) continue;
+        double d = wk_strips[(size_t)p * len + i] + c->cp->corr_offset;
+        if (d < 0.0) d = 0.0;
+        if (isnan(d)) nan_ = 1;
+        else if (d == 0.0) zero = 1;
+        else ls += log(d);
+      }
+      combo[i] = nan_ ? NAN : (zero ? 0.0 : exp(ls / n) - c->cp->corr_offset);
+    }
+  } else {
+    or_combine_strips(wk_strips, use, P, is_diag, hw, c->cp->corr_offset, c->cp->twice_diagonal, combo);
+  }
+  double *dm = c->disp + (size_t)nTile * OR_DISP_N;
+  int ix;
+  if (or_max_xy_int_axis(combo, hw, c->cp->min_corr, &ix)) {
+    double strength = combo[ix + 8 - 1];
+    dm[OR_DISP_INT] = -ix;
+    dm[OR_DISP_STRENGTH] = strength;
+    dm[OR_DISP_IXY] = ix;
+    double cs[3];
+    if (or_max_x_cm(combo, hw, ix, c->wndy, c->cp->corr_wndy_size, c->wndx, c->cp->corr_wndx_size, cs)) {
+      dm[OR_DISP_CM] = -cs[0];
+      dm[OR_DISP_CM_S0] = cs[1];
+    }
+  }
+  int useo[OR_MAX_PAIRS];
+  double r[2];
+  for (int p = 0; p < P; p++) useo[p] = (c->pairs->kind[p] == 0);
+  if (or_max_xs_ortho(wk_corr, useo, P, c->cp->corr_offset, 0, c->notch, r)) {
+    dm[OR_DISP_HOR] = -r[0];
+    dm[OR_DISP_HOR_STRENGTH] = r[1];
+  }
+  for (int p = 0; p < P; p++) useo[p] = (c->pairs->kind[p] == 1);
+  if (or_max_xs_ortho(wk_corr, useo, P, c->cp->corr_offset, 1, c->notch, r)) {
+    dm[OR_DISP_VERT] = -r[0];
+    dm[OR_DISP_VERT_STRENGTH] = r[1];
+  }
+}
+
+static void *run_worker(void *arg) {
+  run_ctx *c = (run_ctx *)arg;
+  const int S = c->cfg->num_sensors, C = c->cfg->num_colors, P = c->pairs->num_pairs;
+  double *wk_clt = (double *)malloc(sizeof(double) * S * C * 256);
+  double *wk_corr = (double *)malloc(sizeof(double) * (P + 1) * 225);
+  double *wk_strips = (double *)malloc(sizeof(double) * (P + 1) * 15 * 32);
+  for (int nTile = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED); nTile < c->num_tiles;
+       nTile = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED))
+    run_tile(c, nTile, wk_clt, wk_corr, wk_strips);
+  free(wk_clt); free(wk_corr); free(wk_strips);
+  return NULL;
+}
+
+int or_run(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
+           const double *const *images, const double *const *kern, const double *const *kext,
+           const int *tile_op, const double *disparity, const or_pairs *pairs, const or_corr_params *cp,
+           double *ports, double *clt, double *corr, double *disp, int *int_tl, double *residual) {
+  tables();
+  if (cfg->num_sensors < 1 || cfg->num_sensors > OR_MAX_SENSORS) return -1;
+  if (cfg->num_colors != 1 && cfg->num_colors != 3) return -2;
+  if (cp->corr_strip_hight > 32 || cp->corr_wndx_size > 32 || cp->corr_wndy_size > 32) return -3;
+  run_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.cfg = cfg; c.g = g; c.ports_in = ports_in; c.images = images; c.kern = kern; c.kext = kext;
+  c.tile_op = tile_op; c.disparity = disparity; c.pairs = pairs; c.cp = cp;
+  c.ports = ports; c.clt = clt; c.corr = corr; c.disp = disp; c.int_tl = int_tl; c.residual = residual;
+  c.num_tiles = (cfg->width / 8) * (cfg->height / 8);
+  double rots[OR_MAX_SENSORS][3][3];
+  double tbl[2100];
+  if (!cfg->use_ports_in) {
+    or_rot_matrices(g, rots);
+    c.tbl_len = or_reverse_distortion_table(g, tbl, 2100);
+    if (c.tbl_len < 0) return -4;
+  }
+  c.rots = rots;
+  c.tbl = tbl;
+  or_corr_lpf(cp->corr_sigma, c.filter);
+  c.col_weights[2] = 1.0 / (1.0 + cp->corr_red + cp->corr_blue);  /* ImageDtt.java:1571-1581 */
+  c.col_weights[0] = cp->corr_red * c.col_weights[2];
+  c.col_weights[1] = cp->corr_blue * c.col_weights[2];
+  or_half_flat_top_window(cp->corr_wndy_size, cp->corr_wndy_hwidth, cp->corr_wndy_blur, 1, 0, 1.0, c.wndy);
+  or_half_flat_top_window(cp->corr_wndx_size, cp->corr_wndx_hwidth, cp->corr_wndx_blur, 1, 0, 2.0, c.wndx);
+  or_ortho_notch(cp->enhortho_width, cp->enhortho_scale, c.notch);
+  int nt = cfg->num_threads > 0 ? cfg->num_threads : 1;
+  pthread_t th[256];
+  if (nt > 256) nt = 256;
+  for (int i = 0; i < nt; i++) pthread_create(&th[i], NULL, run_worker, &c);
+  for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* IMCLT of whole frames, threaded like ImageDtt.iclt_2d (3559-3666): four     */
+/* passes over the tile parities, tiles of one pass never overlap.            */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  const double *clt;
+  const int *present;
+  const double *lpf;
+  double *frames;
+  int tilesX, tilesY, S, C, pass;
+  double scale;
+  volatile int next;
+} iclt_ctx;
+
+static void *iclt_worker(void *arg) {
+  iclt_ctx *c = (iclt_ctx *)arg;
+  const int nx = (c->tilesX + 1 - (c->pass & 1)) / 2, ny = (c->tilesY + 1 - ((c->pass >> 1) & 1)) / 2;
+  const int fw = c->tilesX * 8 + 8, fh = c->tilesY * 8 + 8;
+  for (int n = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED); n < nx * ny;
+       n = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED)) {
+    int tx = 2 * (n % nx) + (c->pass & 1), ty = 2 * (n / nx) + ((c->pass >> 1) & 1);
+    int tile = ty * c->tilesX + tx;
+    if (c->present && !c->present[tile]) continue;
+    for (int s = 0; s < c->S; s++)
+      for (int col = 0; col < c->C; col++) {
+        const double *src = c->clt + (((size_t)tile * c->S + s) * c->C + col) * 256;
+        double q[4][64];
+        for (int m = 0; m < 4; m++)
+          for (int i = 0; i < 64; i++) q[m][i] = src[m * 64 + i] * (c->lpf ? c->lpf[col * 64 + i] : 1.0);
+        or_iclt_tile_add((const double(*)[64])q, c->scale, tx, ty,
+                         c->frames + ((size_t)s * c->C + col) * fw * fh, fw);
+      }
+  }
+  return NULL;
+}
+
+int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
+                    const double *lpf, double *frames, int num_threads) {
+  tables();
+  iclt_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.clt = clt; c.present = present; c.lpf = lpf; c.frames = frames;
+  c.tilesX = tilesX; c.tilesY = tilesY; c.S = S; c.C = C; c.scale = scale;
+  size_t n = (size_t)S * C * (tilesX * 8 + 8) * (tilesY * 8 + 8);
+  memset(frames, 0, n * sizeof(double));
+  int nt = num_threads > 0 ? (num_threads > 256 ? 256 : num_threads) : 1;
+  pthread_t th[256];
+  for (int pass = 0; pass < 4; pass++) {
+    c.pass = pass;
+    c.next = 0;
+    for (int i = 0; i < nt; i++) pthread_create(&th[i], NULL, iclt_worker, &c);
+    for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
+  }
+  return 0;
+}

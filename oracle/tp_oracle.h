@@ -1,0 +1,225 @@
+/*
+ * tp_oracle.h -- FP64 CPU restatement of the imagej-elphel tile-processor path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness oracle for the
+ * GB300 kernels and the timed CPU baseline ("port" of the reference CPU path).
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may
+ * load it.  The product (libtp) never links or calls anything here.
+ *
+ * Reference: Elphel imagej-elphel (Java), files cited per function as
+ *   J/ = src/main/java/com/elphel/imagej/
+ *   DttRad2            J/tileprocessor/DttRad2.java
+ *   ImageDtt           J/tileprocessor/ImageDtt.java
+ *   Correlation2d      J/tileprocessor/Correlation2d.java
+ *   GeometryCorrection J/tileprocessor/GeometryCorrection.java
+ *   QuadCLT            J/tileprocessor/QuadCLT.java
+ *
+ * Parity status: the reference ships no tests, golden vectors or fixtures for
+ * this path and its CPU path is Java (no JVM on this machine), so the CPU
+ * stages are pinned by the restated source.  Stage 2 (convert/correct) and
+ * IMCLT are additionally pinned against the reference's own CUDA kernels
+ * (compiled from its sources by oracle/build_ref_gpu.py) through golden
+ * fixtures under tests/golden/.
+ *
+ * All arithmetic is double; compiled with -ffp-contract=off so that results
+ * are identical on x86_64 and aarch64.
+ */
+#ifndef TP_ORACLE_H
+#define TP_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OR_DTT 8          /* transform_size */
+#define OR_DTT2 16
+#define OR_CORR 15        /* 2*transform_size-1 */
+#define OR_MAX_SENSORS 16
+#define OR_MAX_PAIRS 120
+
+/* disparity_map layout per tile (subset of ImageDtt.java:64-76 indices) */
+enum {
+  OR_DISP_INT = 0,          /* DISPARITY_INDEX_INT   */
+  OR_DISP_CM = 1,           /* DISPARITY_INDEX_CM    */
+  OR_DISP_STRENGTH = 2,     /* DISPARITY_STRENGTH_INDEX */
+  OR_DISP_HOR = 3,          /* DISPARITY_INDEX_HOR   */
+  OR_DISP_HOR_STRENGTH = 4, /* DISPARITY_INDEX_HOR_STRENGTH */
+  OR_DISP_VERT = 5,         /* DISPARITY_INDEX_VERT  */
+  OR_DISP_VERT_STRENGTH = 6,/* DISPARITY_INDEX_VERT_STRENGTH */
+  OR_DISP_CM_S0 = 7,        /* getMaxXCm weight  (diagnostic) */
+  OR_DISP_IXY = 8,          /* integer argmax column (diagnostic, NaN if none) */
+  OR_DISP_N = 9
+};
+
+/* ---- DttRad2 ---- */
+void or_dct_iv8(const double *x, double *y);           /* DttRad2.dct_iv   (80-85)  */
+void or_dst_iv8(const double *x, double *y);           /* DttRad2.dst_iv   (87-98)  */
+void or_dct_ii8(const double *x, double *y);           /* DttRad2.dct_ii   (68-78)  */
+/* mode bit0: horizontal sine, bit1: vertical sine; output transposed */
+void or_dttt_iv(const double *x, double *y, int mode);   /* DttRad2.dttt_iv   (503-519) */
+void or_dttt_iie(const double *x, double *y, int mode);  /* DttRad2.dttt_iie  (595-614) */
+void or_dttt_iiie(const double *x, double *y, int mode); /* DttRad2.dttt_iiie (648-666) */
+void or_dctiv_direct(const double *x, double *y);        /* DttRad2.dctiv_direct (848-862) */
+void or_hwindow(double *hw8);                            /* set_window(1) (674-694) */
+void or_shifted_fold(double shift_hor, double shift_vert,
+                     double fold_k[4][64][4]);           /* get_shifted_fold_2d (263-314) */
+void or_fold_index(int fold_index[64][4]);               /* set_fold_2d (146-203) */
+void or_fold_tile(const double *tile256, int mode,
+                  const double fold_k[4][64][4], double *y64); /* fold_tile (724-738) */
+void or_unfold_tile(const double *x64, int mode, double *y256);  /* unfold_tile (770-780) */
+void or_corr_unfold_tile(const double q[4][64], double *rslt225); /* corr_unfold_tile (443-489) */
+void or_win2d(double *w256);                             /* getWin2d (697-713) */
+
+/* ---- ImageDtt stage 2 ---- */
+/*
+ * extract_correct_tile (ImageDtt.java:4867-5426, non-debug branch).
+ * image: one colour plane, row-major [height][width] (double).
+ * kern/kext: kernel table for this colour, or NULL for identity (use_kernels=false):
+ *   kern layout [kv][kh][4][64] CPU orientation, kext [kv][kh][8] (CltExtra order).
+ * Writes clt[4][64], residual[2], and optionally int_tl[2] / ktile[2].
+ */
+void or_extract_correct_tile(const double *image, int width, int height,
+                             const double *kern, const double *kext,
+                             int kernels_hor, int kernels_vert, int kernel_step,
+                             double centerX, double centerY,
+                             double clt[4][64], double residual[2],
+                             int int_tl[2], int ktile[2]);
+void or_convolve_tile(double data[4][64], const double *kernel4x64); /* 5429-5488 */
+void or_fract_shift(double clt[4][64], double shiftX, double shiftY); /* 5490-5584 */
+
+/* correlation LPF (ImageDtt.java:1662-1690) -> filter[64] */
+void or_corr_lpf(double corr_sigma, double *filter64);
+/* setCltLpf + dttt_iiie * 2n (GPUTileProcessor.java:780-848) */
+void or_clt_lpf(double sigma, double *lpf64);
+
+/* ---- GeometryCorrection ---- */
+typedef struct {
+  int num_sensors;
+  int pixel_width, pixel_height;   /* pixelCorrectionWidth/Height */
+  double focal_length;             /* mm */
+  double pixel_size;               /* um */
+  double distortion_radius;        /* mm */
+  double distortion[7];            /* C, B, A, A5, A6, A7, A8 */
+  double rXY[OR_MAX_SENSORS][2];   /* disparity-normalised lens offsets */
+  double pXY0[OR_MAX_SENSORS][2];  /* sensor centres, pixels */
+  double azimuth[OR_MAX_SENSORS];  /* radians */
+  double tilt[OR_MAX_SENSORS];
+  double roll[OR_MAX_SENSORS];     /* full roll (vector roll + factory roll), radians */
+  double zoom[OR_MAX_SENSORS];     /* zoom - 1 */
+} or_geometry;
+
+/* CorrVector.getRotMatrices (GeometryCorrection.java:1043-1076) */
+void or_rot_matrices(const or_geometry *g, double rots[][3][3]);
+/* CorrVector.getRotDeriveMatrices (1083-1147): [sensor][az,tilt,roll,zoom] */
+void or_rot_deriv_matrices(const or_geometry *g, double drots[][4][3][3]);
+/* calcReverseDistortionTable (2707-2757); returns table length, fills tbl (>= 2002) */
+int or_reverse_distortion_table(const or_geometry *g, double *tbl, int tbl_cap);
+/* getRByRDist (2802-2827) */
+double or_r_by_rdist(const double *tbl, int tbl_len, double rDist);
+/*
+ * getPortsCoordinatesAndDerivatives (2159-2314), generalised to S sensors with
+ * free per-sensor parameters.  deriv (nullable) receives [S][2][4] derivatives
+ * of (x,y) w.r.t. (azimuth, tilt, roll, zoom) of that sensor (the reference
+ * writes the same values into its 13-parameter layout).
+ */
+void or_ports(const or_geometry *g, const double rots[][3][3],
+              const double drots[][4][3][3], const double *tbl, int tbl_len,
+              double px, double py, double disparity,
+              double pXY[][2], double deriv[][2][4]);
+
+/* ---- Correlation2d ---- */
+typedef struct {
+  int num_pairs;
+  int cam1[OR_MAX_PAIRS], cam2[OR_MAX_PAIRS];
+  /* strip direction b (disparity units per strip column) and flags */
+  double bx[OR_MAX_PAIRS], by[OR_MAX_PAIRS];
+  int kind[OR_MAX_PAIRS];     /* 0 hor, 1 vert, 2 diag main, 3 diag other, 4 general */
+  int combo_mask_lo, combo_mask_hi;  /* pairs combined into strip_combo (bits 0..63, 64..119) */
+} or_pairs;
+
+typedef struct {
+  double fat_zero;
+  double corr_sigma;
+  double corr_red, corr_blue;
+  double corr_offset;
+  double min_corr;
+  int corr_strip_hight;
+  int twice_diagonal;
+  int enhortho_width;
+  double enhortho_scale;
+  int corr_wndy_size; double corr_wndy_hwidth, corr_wndy_blur;
+  int corr_wndx_size; double corr_wndx_hwidth, corr_wndx_blur;
+} or_corr_params;
+
+void or_default_corr_params(or_corr_params *p);
+/* the 6 quad pairs PAIRS[0..5] (Correlation2d.java:52-58) */
+void or_quad_pairs(or_pairs *pp);
+
+/* correlateCompositeFD for one pair (Correlation2d.java:275-389); clt1/clt2: [C][4][64] */
+void or_correlate_pair(const double *clt1, const double *clt2, int num_colors,
+                       const double *col_weights, const double *lpf64,
+                       double fat_zero, double *corr225);
+/* scaleRotateInterpoateSingleCorrelation generalised (610-718) */
+void or_strip(const double *corr225, double bx, double by, int kind, int hwidth, double *strip);
+/* combineInterpolatedCorrelations (730-790) */
+void or_combine_strips(const double *strips, const int *use, int num_pairs, const int *is_diag,
+                       int hwidth, double offset, int twice_diagonal, double *combo);
+/* getMaxXYInt axis_only (802-843): returns 1 and ix, or 0 */
+int or_max_xy_int_axis(const double *combo, int hwidth, double minMax, int *ix);
+/* halfFlatTopWindow (1047-1081) */
+void or_half_flat_top_window(int ihwidth, double hwidth, double blur, int normalize,
+                             int notch, double scale, double *wnd);
+/* getMaxXCm (936-1032): returns 1 and rslt[3] or 0 (null) */
+int or_max_x_cm(const double *combo, int hwidth, int ixcenter,
+                const double *wy, int wy_len, const double *wx, int wx_len, double rslt[3]);
+/* createOrtoNotch (2654-2675) */
+void or_ortho_notch(double enhortho_width, double enhortho_scale, double *notch15);
+/* getMaxXSOrtho (2502-2651) with the 3-point parabola in closed form */
+int or_max_xs_ortho(const double *corrs, const int *use, int num_pairs, double offset,
+                    int is_vert, const double *notch15, double rslt[2]);
+
+/* ---- IMCLT / textures ---- */
+/* iclt_2d (ImageDtt.java:3559-3666) into the padded frame (W+8)x(H+8) (no edge
+ * trimming); clt: [tilesY][tilesX][4][64]; accumulated into out (caller zeroes). */
+void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty,
+                      double *frame, int frame_width);
+/* all tiles of clt [tiles][S][C][256] into frames [S][C][H+8][W+8] (zeroed here),
+ * optional per-colour lpf [C][64]; present[tile] == 0 skips a tile */
+int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
+                    const double *lpf, double *frames, int num_threads);
+
+/* ---- kernel preparation (QuadCLT.java:433-667, ImageDtt.java:4625-4851) ---- */
+/* one 64x64 double-resolution kernel -> 4x64 CLT (CPU orientation) + 8 extras */
+void or_calc_clt_kernel(const double *src64x64, int normalize, double clt[4][64], double extra[8]);
+/* clt_fill_coord_corr on one colour plane of [kv][kh][8] extras */
+void or_fill_coord_corr(double *ext, int kh, int kv, int kern_step);
+
+/* ---- full tile loop (clt_aberrations_quad_corr_new, ImageDtt.java:1491-2824) ---- */
+typedef struct {
+  int width, height;
+  int num_sensors, num_colors;
+  int kernels_hor, kernels_vert, kernel_step; /* kernels_hor==0 -> identity */
+  int num_threads;
+  int use_ports_in;   /* 1: take ports from ports_in instead of geometry */
+  int corr;           /* run stage 3 */
+} or_run_cfg;
+
+/*
+ * images: [S][C][H*W] planes (sparse colour planes for Bayer).
+ * kern: [S] -> [C][kv][kh][4][64]; kext: [S] -> [C][kv][kh][8] (NULL when identity).
+ * tile_op: [T] (0 = skip); disparity: [T].
+ * outputs (nullable): ports [T][S][2], clt [T][S][C][4][64], corr [T][P][225],
+ * disp [T][OR_DISP_N], int_tl [T][S][C][2], residual [T][S][C][2].
+ * Returns 0 on success.
+ */
+int or_run(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
+           const double *const *images, const double *const *kern, const double *const *kext,
+           const int *tile_op, const double *disparity,
+           const or_pairs *pairs, const or_corr_params *cp,
+           double *ports, double *clt, double *corr, double *disp,
+           int *int_tl, double *residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,219 @@
+"""GPU path vs the FP64 oracle on seeded synthetic scenes (needs a GB300).
+
+Tolerances (stated by the port specification):
+  * tile list, task order, integer window corners, kernel tiles: bit-exact;
+  * ports (FP64 on the device): bit-exact;
+  * CLT coefficients: relative L2 per (tile, sensor, colour) <= 2e-6;
+  * correlation surfaces: relative L2 per (tile, pair) <= 1e-5;
+  * disparity (centroid and ortho): |gpu - oracle| <= 0.005 px on tiles whose
+    integer argmax is not a near-tie (top two strip values differ by > 1e-4).
+"""
+import numpy as np
+import pytest
+
+from helpers import make_gpu, rel_l2, run_oracle
+from tileproc import synth
+
+pytestmark = pytest.mark.gpu
+
+CLT_TOL = 2e-6
+CORR_TOL = 1e-5
+DISP_TOL = 0.005
+
+
+def _check_tiles(O, tp, ref, num_colors):
+    ports = tp.getPorts()
+    assert np.array_equal(ports, ref["ports"]), "ports differ: max %g" % np.abs(ports - ref["ports"]).max()
+    tl, res = tp.getSubtiles()
+    assert np.array_equal(tl, ref["int_tl"]), "integer window corners differ at %d sub-tiles" % (tl != ref["int_tl"]).sum()
+    assert np.array_equal(res, ref["residual"].astype(np.float32)), "residual shifts differ"
+
+
+def _check_clt(tp, ref, tile_mask=None):
+    clt = tp.getClt().astype(np.float64)
+    e = rel_l2(clt, ref["clt"], axis=(-2, -1))
+    if tile_mask is not None:
+        e = e[tile_mask]
+    assert e.max() <= CLT_TOL, "CLT rel L2 max %.3g (median %.3g)" % (e.max(), np.median(e))
+    return e
+
+
+def _check_corr(tp, ref, tile_mask=None):
+    corr = tp.getCorr().astype(np.float64)
+    e = rel_l2(corr, ref["corr"], axis=-1)
+    if tile_mask is not None:
+        e = e[tile_mask]
+    assert e.max() <= CORR_TOL, "corr rel L2 max %.3g (median %.3g)" % (e.max(), np.median(e))
+    return e
+
+
+def _check_disp(O, tp, ref, check_ortho=True, min_frac=0.995):
+    d = tp.getDisparity().astype(np.float64)
+    r = ref["disp"]
+    both = np.isfinite(r[:, O.DISP_CM]) & np.isfinite(d[:, O.DISP_CM])
+    agree = both & (d[:, O.DISP_IXY] == r[:, O.DISP_IXY])
+    n = np.isfinite(r[:, O.DISP_CM]).sum()
+    assert n > 0
+    frac = agree.sum() / n
+    assert frac >= min_frac, "integer argmax agrees on %.4f of tiles" % frac
+    err = np.abs(d[agree, O.DISP_CM] - r[agree, O.DISP_CM])
+    assert err.max() <= DISP_TOL, "centroid disparity max err %.4g px" % err.max()
+    if check_ortho:
+        for k in (O.DISP_HOR, O.DISP_VERT):
+            ok = np.isfinite(r[:, k]) & np.isfinite(d[:, k])
+            e = np.abs(d[ok, k] - r[ok, k])
+            assert np.quantile(e, 0.995) <= DISP_TOL, "ortho %d err q99.5 %.4g" % (k, np.quantile(e, 0.995))
+    # tiles without a task keep the reference's initial values
+    return err
+
+
+def test_quad_mono_identity(oracle):
+    """4 mono sensors 512x384, identity kernels, 6 pairs, fat zero 0.05 (the CPU-runnable config)."""
+    sc = synth.make_scene("quad_mono", seed=1)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    ref = run_oracle(oracle, sc, 4.0)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation(fat_zero=0.05)
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        assert tp.numTasks() == T
+        txy = tp.getTaskTiles()
+        assert np.array_equal(txy, (np.arange(T) % (sc["width"] // 8)) | ((np.arange(T) // (sc["width"] // 8)) << 16))
+        _check_tiles(oracle, tp, ref, 1)
+        _check_clt(tp, ref)
+        _check_corr(tp, ref)
+        _check_disp(oracle, tp, ref)
+
+
+def test_quad_bayer_kernels(oracle):
+    """4 Bayer sensors (uint16, GR/BG), per-sensor/colour CLT kernels on a 16-px grid with margins."""
+    sc = synth.make_scene("quad_bayer", seed=3, width=256, height=192)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    rng = np.random.default_rng(7)
+    kv, kh = H // 16 + 2, W // 16 + 2
+    k, e = synth.random_clt_kernels(rng, 4, kv, kh, 3)
+    disp = rng.uniform(2.0, 6.0, T).astype(np.float32)
+    ref = run_oracle(oracle, sc, disp.astype(np.float64), kernels=k, kext=e)
+    with make_gpu(sc, k, e) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(disp)
+        tp.process()
+        _check_tiles(oracle, tp, ref, 3)
+        _check_clt(tp, ref)
+        _check_corr(tp, ref)
+        _check_disp(oracle, tp, ref)
+
+
+def test_quad_bayer_rggb(oracle):
+    """Same path with the RGGB phase (red at row 0, column 0)."""
+    sc = synth.make_scene("quad_bayer", seed=4, width=128, height=96, bayer_red_row=0, bayer_red_col=0)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    ref = run_oracle(oracle, sc, 4.0)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        _check_tiles(oracle, tp, ref, 3)
+        _check_clt(tp, ref)
+        _check_corr(tp, ref)
+
+
+def test_circle16_extrinsics(oracle):
+    """16 LWIR sensors on a circle with extrinsic perturbations, all 120 pairs (generalised strips)."""
+    sc = synth.make_scene("circle_lwir", seed=5, width=160, height=128)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    pairs = synth.circle_pairs(sc["geometry"])
+    opairs = [(a, b, bx, by, kind) for (a, b, kind, _, bx, by) in pairs]
+    ref = run_oracle(oracle, sc, 2.0, pairs=opairs)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation(pairs=pairs)
+        tp.setFullFrameImages(np.full(T, 2.0, np.float32))
+        tp.process()
+        _check_tiles(oracle, tp, ref, 1)
+        _check_clt(tp, ref)
+        _check_corr(tp, ref)
+        _check_disp(oracle, tp, ref, check_ortho=False, min_frac=0.99)
+
+
+def test_float_tasks_ragged(oracle):
+    """setTasks with reference-layout float ports on a ragged subset of tiles incl. borders."""
+    sc = synth.make_scene("quad_mono", seed=6, width=128, height=96)
+    W, H = sc["width"], sc["height"]
+    tX, tY = W // 8, H // 8
+    T = tX * tY
+    rng = np.random.default_rng(11)
+    sel = np.sort(rng.choice(T, size=T // 3, replace=False))
+    sel = np.union1d(sel, [0, tX - 1, T - tX, T - 1])
+    tx, ty = sel % tX, sel // tX
+    cx, cy = tx * 8 + 4.0, ty * 8 + 4.0
+    # ports pushed out of the image on some tiles to exercise the mirrored border
+    xy = np.stack([np.stack([cx - d * 5 * r[0], cy - d * 5 * r[1]], -1) for d, r in zip([1, 1, 1, 1], synth.QUAD_RXY)],
+                  1).astype(np.float32) + rng.uniform(-3, 3, size=(len(sel), 4, 2)).astype(np.float32)
+    ports_in = np.zeros((T, 4, 2))
+    ports_in[sel] = xy.astype(np.float64)
+    op = np.zeros(T, np.int32)
+    op[sel] = 1
+    ref = run_oracle(oracle, sc, 0.0, tile_op=op, ports_in=ports_in)
+    from tileproc import GPUTileProcessor
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setTasks(GPUTileProcessor.packTasks(np.ones(len(sel)), tx, ty, xy))
+        tp.process()
+        assert np.array_equal(tp.getPorts(), ports_in[sel])
+        tl, res = tp.getSubtiles()
+        assert np.array_equal(tl, ref["int_tl"][sel])
+        _check_clt(tp, ref, tile_mask=sel)
+        _check_corr(tp, ref, tile_mask=sel)
+        d = tp.getDisparity()
+        untasked = np.setdiff1d(np.arange(T), sel)
+        assert np.all(np.isnan(d[untasked, oracle.DISP_CM])) and np.all(d[untasked, oracle.DISP_STRENGTH] == 0)
+
+
+def test_empty_task_list(oracle):
+    sc = synth.make_scene("quad_mono", seed=8, width=64, height=64)
+    T = 64
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.zeros(T, np.float32), tile_op=np.zeros(T, np.int32))
+        tp.process()
+        assert tp.numTasks() == 0
+        d = tp.getDisparity()
+        assert np.all(np.isnan(d[:, oracle.DISP_CM]))
+
+
+def _oracle_rbg(O, clt, tilesX, tilesY, S, C, W, H, lpf=None):
+    frames = np.zeros((S, C, H + 8, W + 8))
+    for s in range(S):
+        for c in range(C):
+            f = frames[s, c]
+            for t in range(tilesX * tilesY):
+                q = clt[t, s, c]
+                if lpf is not None:
+                    q = q * lpf[c][None, :]
+                O.iclt_tile_add(q, 0.25, t % tilesX, t // tilesX, f)
+    return frames
+
+
+def test_imclt(oracle):
+    """IMCLT overlap-add into (W+8)x(H+8) frames vs ImageDtt.iclt_2d (x0.25) on the GPU's own CLT."""
+    sc = synth.make_scene("quad_bayer", seed=9, width=192, height=128)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        tp.execImcltRbg()
+        clt = tp.getClt().astype(np.float64)
+        want = _oracle_rbg(oracle, clt, W // 8, H // 8, 4, 3, W, H)
+        for s in range(4):
+            got = tp.getRBG(s).astype(np.float64)
+            err = np.abs(got - want[s]).max() / np.abs(want[s]).max()
+            assert err < 2e-6, "sensor %d IMCLT max rel err %.3g" % (s, err)
+        lpf = np.stack([oracle.clt_lpf(sg) for sg in (1.1, 1.1, 0.7)])
+        tp.setLpfRbg(lpf)
+        tp.execImcltRbg()
+        want = _oracle_rbg(oracle, clt, W // 8, H // 8, 4, 3, W, H, lpf=lpf)
+        got = tp.getRBG(2).astype(np.float64)
+        assert np.abs(got - want[2]).max() / np.abs(want[2]).max() < 2e-6

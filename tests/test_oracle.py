@@ -1,0 +1,162 @@
+"""Self-consistency checks of the FP64 oracle (CPU only).
+
+The reference ships no tests or fixtures for this path; its own cross-checks
+(DttRad2 GPU-mirror methods, analytic vs finite-difference port derivatives in
+AlignmentCorrection.java:2952-2990, GPU/CPU debug dumps) become these
+automated checks.
+"""
+import numpy as np
+import pytest
+
+from tileproc import synth
+
+
+def test_dct_iv_recursive_matches_direct(oracle):
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        x = rng.standard_normal(8)
+        assert np.abs(oracle.dct_iv8(x) - oracle.dctiv_direct(x)).max() < 1e-14
+
+
+def test_dct_dst_iv_are_involutions(oracle):
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(8)
+    assert np.abs(oracle.dct_iv8(oracle.dct_iv8(x)) - x).max() < 1e-14
+    assert np.abs(oracle.dst_iv8(oracle.dst_iv8(x)) - x).max() < 1e-14
+    for mode in range(4):
+        t = rng.standard_normal(64)
+        y = oracle.dttt_iv(t, mode)
+        # second application with the swapped mode undoes the transposed 2D transform
+        swapped = ((mode << 1) & 2) | ((mode >> 1) & 1)
+        assert np.abs(oracle.dttt_iv(y, swapped) - t).max() < 1e-13
+
+
+def test_dst_iie_identity_used_by_gpu(oracle):
+    """SIIe[j][k] = (-1)^k CIIe[7-j][k]: the GPU computes DST-IIe with the DCT-IIe matrix."""
+    C = np.array([[np.sqrt(2 / 8) * np.cos(j * (2 * k + 1) * np.pi / 16) for k in range(8)] for j in range(8)])
+    S = np.array([[np.sqrt(2 / 8) * np.sin((j + 1) * (2 * k + 1) * np.pi / 16) for k in range(8)] for j in range(8)])
+    alt = np.array([(-1) ** k for k in range(8)])
+    assert np.abs(S - (C[::-1, :] * alt[None, :])).max() < 1e-15
+
+
+def test_mclt_perfect_reconstruction(oracle):
+    """Forward MCLT of every tile + IMCLT overlap-add (x0.25) reproduces the image (Princen-Bradley)."""
+    rng = np.random.default_rng(3)
+    H, W = 64, 80
+    img = rng.standard_normal((H, W))
+    frame = np.zeros((H + 8, W + 8))
+    for ty in range(H // 8):
+        for tx in range(W // 8):
+            clt, res, tl, _ = oracle.extract_correct_tile(img, tx * 8 + 4, ty * 8 + 4)
+            assert tuple(tl) == (tx * 8 - 4, ty * 8 - 4) and np.all(res == 0)
+            oracle.iclt_tile_add(clt, 0.25, tx, ty, frame)
+    inner = frame[4:-4, 4:-4]
+    assert np.abs(inner[8:-8, 8:-8] - img[8:-8, 8:-8]).max() < 1e-12
+
+
+def test_fract_shift_is_a_rotation(oracle):
+    rng = np.random.default_rng(4)
+    c = rng.standard_normal((4, 64))
+    s = oracle.fract_shift(c, 0.37, -0.21)
+    assert abs(np.sum(s ** 2) - np.sum(c ** 2)) < 1e-12 * np.sum(c ** 2)
+    back = oracle.fract_shift(s, -0.37, 0.21)
+    assert np.abs(back - c).max() < 1e-13
+    assert np.abs(oracle.fract_shift(c, 0.0, 0.0) - c).max() == 0
+
+
+def test_fract_shift_moves_the_image(oracle):
+    """A smooth image extracted at a fractional centre equals the integer-centre tile
+    shifted in the CLT domain (the decomposition extract_correct_tile relies on)."""
+    H = W = 64
+    yy, xx = np.mgrid[0:H, 0:W]
+    f = lambda x, y: np.sin(0.21 * x + 0.1) * np.cos(0.17 * y - 0.3) + 0.3 * np.sin(0.11 * (x + y))
+    img = f(xx, yy)
+    dx, dy = 0.3, -0.2
+    frame = np.zeros((H + 8, W + 8))
+    for ty in range(H // 8):
+        for tx in range(W // 8):
+            clt, res, tl, _ = oracle.extract_correct_tile(img, tx * 8 + 4 + dx, ty * 8 + 4 + dy)
+            oracle.iclt_tile_add(oracle.fract_shift(clt, res[0], res[1]), 0.25, tx, ty, frame)
+    got = frame[4:-4, 4:-4][12:-12, 12:-12]
+    want = f(xx + dx, yy + dy)[12:-12, 12:-12]
+    assert np.abs(got - want).max() < 0.02 * np.abs(want).max()
+
+
+def test_convolve_identity_kernel(oracle):
+    rng = np.random.default_rng(5)
+    c = rng.standard_normal((4, 64))
+    k = np.zeros((4, 64))
+    k[0] = 1.0
+    assert np.abs(oracle.convolve_tile(c, k) - c).max() == 0
+
+
+def test_port_derivatives_match_finite_differences(oracle):
+    """Analytic d(port)/d(azimuth, tilt, roll, zoom) vs central differences
+    (the reference's own check, AlignmentCorrection.java:2952-2990)."""
+    rng = np.random.default_rng(6)
+    g = synth.circle_geometry(16, 640, 512, rng=rng, sigma=3e-3)
+    g["distortion"] = [0.02, -0.01, 0.005, 0.0, 0.0, 0.0, 0.0]
+    keys = ("azimuth", "tilt", "roll", "zoom")
+    for _ in range(5):
+        px, py, d = rng.uniform(50, 590), rng.uniform(50, 460), rng.uniform(0, 4)
+        p0, dv = oracle.ports(g, px, py, d, deriv=True)
+        for k, key in enumerate(keys):
+            for s in (0, 5, 11):
+                h = 1e-6
+                gp = {kk: (list(vv) if isinstance(vv, list) else vv) for kk, vv in g.items()}
+                gm = {kk: (list(vv) if isinstance(vv, list) else vv) for kk, vv in g.items()}
+                gp[key][s] += h
+                gm[key][s] -= h
+                fd = (oracle.ports(gp, px, py, d)[s] - oracle.ports(gm, px, py, d)[s]) / (2 * h)
+                an = dv[s, :, k]
+                if key == "roll":
+                    # the reference drops the radial-distortion term of d/droll (GeometryCorrection.java:2279-2280)
+                    assert np.abs(an - fd).max() < 2e-2 * max(1.0, np.abs(fd).max())
+                else:
+                    assert np.abs(an - fd).max() < 1e-5 * max(1.0, np.abs(fd).max()), (key, s, an, fd)
+
+
+def test_general_strip_reduces_to_reference(oracle):
+    """The generalised (kind 4) strip sampler visits the reference's sample points for the quad directions."""
+    rng = np.random.default_rng(7)
+    corr = rng.standard_normal(225)
+    for kind, b in ((0, (1, 0)), (1, (0, 1)), (2, (1, 1)), (3, (1, -1))):
+        a = oracle.strip(corr, b[0], b[1], kind, 9)
+        g = oracle.strip(corr, b[0], b[1], 4, 9)
+        both = np.isfinite(a) & np.isfinite(g)
+        assert np.array_equal(np.isnan(a), np.isnan(g)), kind
+        assert np.abs(a[both] - g[both]).max() < 1e-14, kind
+
+
+def test_constant_disparity_recovered(oracle):
+    """Residual disparity sign and accuracy on constant-disparity synthetic scenes."""
+    from helpers import run_oracle
+    for gt, target in ((4.0, 4.0), (4.6, 4.0)):
+        sc = synth.make_scene("quad_mono", seed=2, width=192, height=160, dmin=gt, dmax=gt)
+        r = run_oracle(oracle, sc, target)
+        d = r["disp"].reshape(20, 24, -1)[2:-2, 2:-2, oracle.DISP_CM]
+        med = np.nanmedian(d)
+        assert abs(med - (gt - target)) < 0.05 + 0.2 * abs(gt - target), med
+        assert np.sign(med) == np.sign(gt - target) or gt == target
+
+
+def test_kernel_chain_symmetric_kernel(oracle):
+    """A centred symmetric PSF yields (near) zero antisymmetric CLT parts and zero centre offsets."""
+    yy, xx = np.mgrid[-32:32, -32:32]
+    src = np.exp(-(xx ** 2 + yy ** 2) / (2 * 2.0 ** 2))
+    clt, ext = oracle.calc_clt_kernel(src)
+    assert np.abs(clt[1:]).max() < 1e-12 * np.abs(clt[0]).max()
+    assert np.abs(ext[:4]).max() < 1e-12
+    # normalisation: kernel * window sums to 16 -> DC of the DCT-IIIe kernel
+    assert np.isfinite(clt).all()
+
+
+def test_fill_coord_corr_linear_field(oracle):
+    kv, kh = 6, 7
+    ext = np.zeros((kv, kh, 8))
+    yy, xx = np.mgrid[0:kv, 0:kh]
+    ext[..., 2] = 0.3 * xx - 0.1 * yy
+    ext[..., 3] = 0.05 * xx + 0.2 * yy
+    oracle.fill_coord_corr(ext, 16)
+    assert np.allclose(ext[..., 4], 0.3 / 16) and np.allclose(ext[..., 5], -0.1 / 16)
+    assert np.allclose(ext[..., 6], 0.05 / 16) and np.allclose(ext[..., 7], 0.2 / 16)
