@@ -1,0 +1,395 @@
+"""Benchmark of the GB300 tile processor (one JSON line on rank 0).
+
+Workload (default): 4 Bayer sensors 2592x1936 uint16 (12-bit), per-sensor /
+per-colour CLT kernel tables on a 16-px grid (164x123), all 78,408 tiles:
+stage 1 ports (FP64) -> stage 2 convert+correct -> 6-pair correlation ->
+disparity extraction -> IMCLT colour frames.  One step = one pass over one
+scene.  Inputs are seeded synthetic scenes (no public dataset exists for this
+path); the per-step working set (~1.9 GB) exceeds the 129 MB L2, so no L2
+flush is needed between steps.
+
+  value : tiles/s with all inputs resident in HBM (CUDA events on the launch stream)
+  e2e   : tiles/s through the public C ABI with host buffers: H2D of the 4 raw
+          images and the tile ops + disparity from pinned memory, the forward,
+          and D2H of the disparity map, every step (host wall clock)
+  --impl reference : the reference CPU path (the FP64 C restatement of
+          ImageDtt/Correlation2d, the Java reference cannot run here) on all
+          host cores, a bounded tile sample per step.
+Multi-GPU: replicas only (independent scenes per rank, no collective on the
+data path); value = tiles of all ranks / max time over ranks.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "imagej-elphel_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "CLT tiles/s fwd & fwd+adjoint on 1 GB300 vs plain and CPU; err vs FP64 oracle"
+
+CONFIGS = {
+    # name: (kind, width, height, kernels, pairs)
+    "c2_bayer_4x2592x1936": dict(kind="quad_bayer", width=2592, height=1936, kernels=True),
+    # quarter-size Bayer scene for ncu captures (CLT 240 MB > L2, ~0.5 GB on the device)
+    "c2q_bayer_4x1296x968": dict(kind="quad_bayer", width=1296, height=968, kernels=True),
+    "c1_mono_4x512x384": dict(kind="quad_mono", width=512, height=384, kernels=False),
+    "c3_lwir_16x640x512": dict(kind="circle_lwir", width=640, height=512, kernels=False),
+}
+DEFAULT_CONFIG = "c2_bayer_4x2592x1936"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(CONFIGS))
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles per CPU sample (0 = auto)")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, use_cuda):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend="nccl" if use_cuda else "gloo")
+    return dist
+
+
+def make_workload(cfg_name, seed, rank=0):
+    from tileproc import synth
+    c = CONFIGS[cfg_name]
+    sc = synth.make_scene(c["kind"], seed=seed + 1000 * rank, width=c["width"], height=c["height"])
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    rng = np.random.default_rng(seed + 7)
+    S = sc["geometry"]["num_sensors"]
+    k = e = None
+    if c["kernels"]:
+        k, e = synth.random_clt_kernels(rng, S, H // 16 + 2, W // 16 + 2, sc["num_colors"])
+    if sc["num_colors"] == 3 or S == 4:
+        target = np.full(T, 4.0, np.float32)
+        pairs = None
+    else:
+        target = np.full(T, 2.0, np.float32)
+        pairs = synth.circle_pairs(sc["geometry"])
+    return dict(scene=sc, kernels=k, kext=e, target=target, pairs=pairs, T=T, W=W, H=H, S=S,
+                C=sc["num_colors"], P=6 if pairs is None else len(pairs),
+                KH=(W // 16 + 2) if k is not None else 0, KV=(H // 16 + 2) if k is not None else 0)
+
+
+def algorithmic_bytes(w):
+    """Each datum counted once (fixed per config): inputs + kernel tables + tasks + CLT +
+    correlation surfaces + disparity + IMCLT frames."""
+    S, C, T, P, W, H = w["S"], w["C"], w["T"], w["P"], w["W"], w["H"]
+    b_in = 2 if w["scene"]["images"].dtype == np.uint16 else 4
+    parts = {
+        "images": S * W * H * b_in,
+        "kernels": S * C * w["KH"] * w["KV"] * (1024 + 32),
+        "tasks": T * (8 + 8 * S),
+        "clt": T * S * C * 1024,
+        "corr": T * P * 900,
+        "disparity": T * 8,
+        "imclt": S * C * (W + 8) * (H + 8) * 4,
+    }
+    stage = {  # per-launch algorithmic bytes of each kernel
+        "ports": T * 8 + T * S * 16 + T * S * C * (20 + 32),
+        "convert_correct": parts["images"] + S * C * w["KH"] * w["KV"] * 1024 + T * S * C * 20 + parts["clt"],
+        "correlate": parts["clt"] + parts["corr"],
+        "extract": parts["corr"] + T * 36,
+        "imclt": parts["clt"] + parts["imclt"],
+    }
+    return sum(parts.values()), parts, stage
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, cfg_name):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if present."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        v = d.get(cfg_name, {}).get(kernel)
+        if v is not None:
+            return float(v)
+    return None
+
+
+def cpu_baseline(w, sample_tiles, threads):
+    """Oracle (FP64 C restatement of the reference CPU path) on a bounded tile sample.
+    Input conversion to the oracle's double planes/kernels happens once, outside the timing."""
+    from oracle import oracle as O
+    sc = w["scene"]
+    T = w["T"]
+    if "_cpu" not in w:
+        if sc["num_colors"] == 3:
+            from tileproc import synth
+            planes = np.stack([synth.bayer_planes(m, sc["color_index"]) for m in sc["images"]])
+        else:
+            planes = sc["images"][:, None].astype(np.float64)
+        kern = kx = None
+        if w["kernels"] is not None:
+            kern = np.ascontiguousarray(np.moveaxis(w["kernels"].astype(np.float64), 3, 1))
+            kx = np.ascontiguousarray(np.moveaxis(w["kext"].astype(np.float64), 3, 1))
+        pairs = None
+        if w["pairs"] is not None:
+            pairs = O.make_pairs([(a, b, bx, by, kind) for (a, b, kind, _, bx, by) in w["pairs"]])
+        w["_cpu"] = (planes, kern, kx, pairs, w["target"].astype(np.float64))
+    planes, kern, kx, pairs, target = w["_cpu"]
+    step = max(1, T // max(sample_tiles, 1))
+    op = np.zeros(T, np.int32)
+    op[::step] = 1
+    n = int(op.sum())
+    t0 = time.perf_counter()
+    r = O.run(w["W"], w["H"], planes, op, target, geometry=sc["geometry"], kernels=kern, kernel_ext=kx,
+              pairs=pairs, num_threads=threads, want=("clt", "corr", "disp"))
+    O.imclt_frames(r["clt"], w["W"] // 8, w["H"] // 8, present=op, num_threads=threads)
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    w = make_workload(args.config, args.seed)
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample_tiles or (4000 if w["C"] == 3 else 2000)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, n, dt = cpu_baseline(w, sample, threads)
+        if i >= args.warmup:
+            vals.append((v, n, dt))
+    tot_tiles = sum(x[1] for x in vals)
+    tot_t = sum(x[2] for x in vals)
+    value = tot_tiles / tot_t
+    line = {"metric": METRIC, "value": value, "unit": "tiles/s", "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.config, "tiles_per_scene": w["T"], "sample_tiles_per_step": vals[0][1]},
+            "cpu_baseline": {"value": value, "unit": "tiles/s", "cores": threads, "kind": "port",
+                             "sample": "%d of %d tiles per step, stages 1-4a" % (vals[0][1], w["T"])},
+            "e2e": {"value": value, "unit": "tiles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    assert torch.cuda.is_available(), "bench.py needs a CUDA GPU"
+    torch.cuda.set_device(local)
+    dist = dist_init(world, True)
+    import build as tp_build
+    tp_build.build()
+    from tileproc import GPUTileProcessor
+    from tileproc import _lib as L
+    w = make_workload(args.config, args.seed, rank)
+    sc = w["scene"]
+    T, S, Cn = w["T"], w["S"], w["C"]
+    # a dedicated stream: the C ABI treats a NULL stream as "the handle's own stream",
+    # so the events must be recorded on the stream handed to the launches
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = C.c_void_p(stream.cuda_stream)
+    assert sptr.value, "need a non-default stream"
+    tp = GPUTileProcessor(S, w["W"], w["H"], num_colors=Cn, kernels_hor=w["KH"], kernels_vert=w["KV"],
+                          device=local)
+    tp.setGeometry(sc["geometry"])
+    if w["kernels"] is not None:
+        tp.setConvolutionKernels(w["kernels"], w["kext"], layout=L.TP_KERNELS_CPU)
+    if Cn == 3:
+        tp.setColorScales([1.0, 1.0, 0.5])
+    tp.setBayerImages(sc["images"])
+    tp.setCorrelation(pairs=w["pairs"])
+    tp.setFullFrameImages(w["target"])
+    lib = tp._lib
+    stages = ["ports", "convert_correct", "correlate", "extract", "imclt"]
+    fns = [lib.tp_ports, lib.tp_convert_correct, lib.tp_correlate, lib.tp_extract, lib.tp_imclt]
+
+    def step(evs=None):
+        for i, f in enumerate(fns):
+            if evs is not None:
+                evs[i].record(stream)
+            st = f(tp.h, sptr)
+            if st != 0:
+                tp._ck(st, stages[i])
+        if evs is not None:
+            evs[-1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(fns) + 1)] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    elapsed = t0.elapsed_time(t1) / 1000.0
+    if dist:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    stage_ms = {s: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
+                for i, s in enumerate(stages)}
+    value = world * T * args.steps / elapsed
+    total_b, parts, stage_b = algorithmic_bytes(w)
+    dom = max(stage_ms, key=stage_ms.get)
+    peak, peak_kind = measured_peaks()
+    ach = stage_b[dom] / (stage_ms[dom] / 1000.0) / 1e9
+    traffic = ncu_traffic(dom, args.config)
+
+    # ---- e2e through the public API with host buffers ----
+    pin_imgs = [torch.from_numpy(np.ascontiguousarray(sc["images"][s])).pin_memory() for s in range(S)]
+    pin_op = torch.ones(T, dtype=torch.int32).pin_memory()
+    pin_disp = torch.from_numpy(w["target"].copy()).pin_memory()
+    out_disp = torch.empty((T, L.DISP_N), dtype=torch.float32).pin_memory()
+    np_imgs = [p.numpy() for p in pin_imgs]
+    np_op, np_disp, np_out = pin_op.numpy(), pin_disp.numpy(), out_disp.numpy()
+    h2d = sum(a.nbytes for a in np_imgs) + np_op.nbytes + np_disp.nbytes
+    d2h = np_out.nbytes
+
+    def e2e_step():
+        for s in range(S):
+            tp._ck(lib.tp_set_image(tp.h, s, C.c_void_p(np_imgs[s].ctypes.data), 1 if Cn == 3 else 0, 0), "img")
+        tp._ck(lib.tp_set_tile_ops(tp.h, C.c_void_p(np_op.ctypes.data), C.c_void_p(np_disp.ctypes.data)), "ops")
+        tp._ck(lib.tp_process(tp.h, None), "process")
+        tp._ck(lib.tp_imclt(tp.h, None), "imclt")
+        tp._ck(lib.tp_get_disparity(tp.h, C.c_void_p(np_out.ctypes.data)), "disp")
+
+    for _ in range(min(args.warmup, 3)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - te
+    if dist:
+        t = torch.tensor([e2e_t], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_val = world * T * args.steps / e2e_t
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = args.cpu_sample_tiles or (4000 if Cn == 3 else 2000)
+        v, n, dt = cpu_baseline(w, sample, threads)
+        cpu = {"value": v, "unit": "tiles/s", "cores": threads, "kind": "port",
+               "sample": "%d of %d tiles (every %d-th), stages 1-4a, FP64 C restatement" % (n, T, max(1, T // sample))}
+    launches_per_step = 6  # plan, tile map, convert_correct, correlate, extract, imclt
+    line = {
+        "metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.config, "tiles_per_scene": T, "sensors": S, "colors": Cn, "pairs": w["P"],
+                   "kernels": "%dx%d" % (w["KH"], w["KV"]) if w["KH"] else "identity",
+                   "stages": "ports(fp64)+convert_correct+correlate+extract+imclt",
+                   "l2": "per-step working set %.2f GB > 129 MB L2, no flush" % (total_b / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+        "algorithmic_bytes_per_step": total_b,
+        "algorithmic_gbs": total_b / (elapsed / args.steps) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_per_launch": stage_b[dom]},
+        "e2e": {"value": e2e_val, "unit": "tiles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    tp.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

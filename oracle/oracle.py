@@ -412,7 +412,8 @@ def imclt_frames(clt, tilesX, tilesY, scale=0.25, lpf=None, present=None, num_th
     """ImageDtt.iclt_2d over all tiles of clt [tiles][S][C][4][64] -> [S][C][H+8][W+8]."""
     L = lib()
     if not getattr(L, "_imclt_set", False):
-        L.or_imclt_frames.argtypes = [_dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int]
+        L.or_imclt_frames.argtypes = [_dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int,
+                                      C.c_int]
         L.or_imclt_frames.restype = C.c_int
         L._imclt_set = True
     clt = _f64(clt)
@@ -421,5 +422,5 @@ def imclt_frames(clt, tilesX, tilesY, scale=0.25, lpf=None, present=None, num_th
     lp = _f64(lpf).reshape(Cn, 64) if lpf is not None else None
     pr = np.ascontiguousarray(present, dtype=np.int32) if present is not None else None
     L.or_imclt_frames(_d(clt), _i(pr) if pr is not None else None, tilesX, tilesY, S, Cn, float(scale),
-                      _d(lp) if lp is not None else None, _d(out), int(num_threads or os.cpu_count() or 1))
+                      _d(lp) if lp is not None else None, _d(out), int(num_threads or os.cpu_count() or 1), 0)
     return out

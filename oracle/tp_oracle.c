@@ -1311,14 +1311,14 @@ static void *iclt_worker(void *arg) {
 }
 
 int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
-                    const double *lpf, double *frames, int num_threads) {
+                    const double *lpf, double *frames, int num_threads, int zero_frames) {
   tables();
   iclt_ctx c;
   memset(&c, 0, sizeof(c));
   c.clt = clt; c.present = present; c.lpf = lpf; c.frames = frames;
   c.tilesX = tilesX; c.tilesY = tilesY; c.S = S; c.C = C; c.scale = scale;
   size_t n = (size_t)S * C * (tilesX * 8 + 8) * (tilesY * 8 + 8);
-  memset(frames, 0, n * sizeof(double));
+  if (zero_frames) memset(frames, 0, n * sizeof(double));
   int nt = num_threads > 0 ? (num_threads > 256 ? 256 : num_threads) : 1;
   pthread_t th[256];
   for (int pass = 0; pass < 4; pass++) {

@@ -183,10 +183,11 @@ int or_max_xs_ortho(const double *corrs, const int *use, int num_pairs, double o
  * trimming); clt: [tilesY][tilesX][4][64]; accumulated into out (caller zeroes). */
 void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty,
                       double *frame, int frame_width);
-/* all tiles of clt [tiles][S][C][256] into frames [S][C][H+8][W+8] (zeroed here),
- * optional per-colour lpf [C][64]; present[tile] == 0 skips a tile */
+/* all tiles of clt [tiles][S][C][256] accumulated into frames [S][C][H+8][W+8]
+ * (zeroed first when zero_frames), optional per-colour lpf [C][64];
+ * present[tile] == 0 skips a tile */
 int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
-                    const double *lpf, double *frames, int num_threads);
+                    const double *lpf, double *frames, int num_threads, int zero_frames);
 
 /* ---- kernel preparation (QuadCLT.java:433-667, ImageDtt.java:4625-4851) ---- */
 /* one 64x64 double-resolution kernel -> 4x64 CLT (CPU orientation) + 8 extras */
