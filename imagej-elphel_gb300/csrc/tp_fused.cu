@@ -1,0 +1,742 @@
+// tp_fused.cu -- fused forward tile kernel: convert+correct -> pair correlation
+// -> strip combination -> disparity extraction, one CTA per group of tiles.
+//
+// Same arithmetic as the stage kernels (ImageDtt.extract_correct_tile,
+// convolve_tile, fract_shift; Correlation2d.correlateCompositeFD,
+// scaleRotateInterpoateSingleCorrelation, combineInterpolatedCorrelations,
+// getMaxXYInt, getMaxXCm, getMaxXSOrtho) but organised for GB300:
+//
+//  phase A  one warp = one colour of 4 sensors of a tile; lanes 8q..8q+7 own
+//           sensor q, lane r owns folded row r.  The fold reads each needed
+//           pixel once (L1-cached __ldg); 8-point DCT-IV/DST-IV run in
+//           registers (Plonka-Tasche recursion, DttRad2.java:1107-1146, scale
+//           folded into the first stage); the 8x8 transpose goes through a
+//           9-padded shared buffer.  For Bayer planes only the transforms that
+//           are not symmetric images of another are computed: a red/blue
+//           window is sparse on a 2x2 lattice, so SC/CS/SS are index reversals
+//           of CC with window-phase signs; a green window is a checkerboard, so
+//           CS and SS are reversals of SC and CC.  That is 4 instead of 12 2D
+//           transforms per sensor.  CLT goes to shared memory (for phase B) and
+//           to HBM (a declared output); per-frequency amplitudes are cached.
+//  phase B  one warp = one (tile, pair): the correlation product, fat-zero
+//           normalisation, colour mix and LPF on 2 CLT indices per lane, the
+//           four 2D DCT-IIe/DST-IIe in registers, the 15x15 unfold, the surface
+//           to HBM, and that pair's strip folded into a per-warp running product.
+//  phase C  one warp = one tile: combine the per-warp strip products, integer
+//           argmax on the disparity axis, windowed centroid, hor/vert maxima.
+#include "tp_internal.h"
+
+#include <math_constants.h>
+
+#include <cmath>
+#include <cstdint>
+
+namespace {
+
+__constant__ float k_hwin[8];      // sine half-window
+__constant__ float k_dct2e[64];    // CIIe (used for the odd half of DCT-IIe)
+__constant__ float k_d4c[4], k_d4s[4];  // scaled DCT-IV stage-1 rotations
+
+constexpr int FW_MAX_WARPS = 16;
+constexpr int SCR = 2 * 288;       // per-warp scratch floats
+
+// ---------------------------------------------------------------------------
+// 8-point transforms
+// ---------------------------------------------------------------------------
+// orthonormal DCT-IV (Plonka-Tasche recursion as in DttRad2._dctiv_recurs)
+__device__ __forceinline__ void dct4_fast(const float x[8], float y[8]) {
+  const float C18 = 1.3065629648763766f, C38 = 0.5411961001461970f, SQ2 = 1.4142135623730951f;
+  float u0[4], u1[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    u0[j] = fmaf(k_d4c[j], x[j], k_d4s[j] * x[7 - j]);
+    float t = fmaf(k_d4c[3 - j], x[4 + j], -k_d4s[3 - j] * x[3 - j]);
+    u1[j] = (j & 1) ? -t : t;
+  }
+  float v0[4], v1[4];
+  {
+    float a0 = u0[0] + u0[3], a1 = u0[1] + u0[2], b0 = u0[0] - u0[3], b1 = u0[1] - u0[2];
+    v0[0] = a0 + a1; v0[2] = a0 - a1;
+    v0[1] = fmaf(C18, b0, C38 * b1); v0[3] = fmaf(C38, b0, -C18 * b1);
+  }
+  {
+    float a0 = u1[0] + u1[3], a1 = u1[1] + u1[2], b0 = u1[0] - u1[3], b1 = u1[1] - u1[2];
+    v1[0] = a0 + a1; v1[2] = a0 - a1;
+    v1[1] = fmaf(C18, b0, C38 * b1); v1[3] = fmaf(C38, b0, -C18 * b1);
+  }
+  y[0] = SQ2 * v0[0];
+  y[7] = SQ2 * v1[0];
+  y[2] = v0[1] + v1[3];  // w0[1] = v0[1] - (-1) v1[3]
+  y[4] = v0[2] - v1[2];  // w0[2]
+  y[6] = v0[3] + v1[1];  // w0[3]
+  y[1] = v0[1] - v1[3];  // w1[0]
+  y[3] = v0[2] + v1[2];  // w1[1]
+  y[5] = v0[3] - v1[1];  // w1[2]
+}
+__device__ __forceinline__ void dtt4_fast(const float x[8], float y[8], bool sine) {
+  float xr[8];
+#pragma unroll
+  for (int n = 0; n < 8; n++) xr[n] = sine ? x[7 - n] : x[n];
+  dct4_fast(xr, y);
+#pragma unroll
+  for (int k = 1; k < 8; k += 2) y[k] = sine ? -y[k] : y[k];
+}
+// DCT-IIe (CIIe rows); DST-IIe via SIIe[j][k] = (-1)^k CIIe[7-j][k]
+__device__ __forceinline__ void dtt2e_fast(const float x[8], float y[8], bool sine) {
+  const float S = 0.5f;  // sqrt(2/8)
+  const float C4 = 0.7071067811865476f, C8 = 0.9238795325112867f, C38 = 0.3826834323650898f;
+  float xs[8];
+#pragma unroll
+  for (int n = 0; n < 8; n++) xs[n] = (sine && (n & 1)) ? -x[n] : x[n];
+  float u0[4], u1[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) { u0[j] = xs[j] + xs[7 - j]; u1[j] = xs[j] - xs[7 - j]; }
+  float a0 = u0[0] + u0[3], a1 = u0[1] + u0[2], b0 = u0[0] - u0[3], b1 = u0[1] - u0[2];
+  float t[8];
+  t[0] = S * (a0 + a1);
+  t[4] = (S * C4) * (a0 - a1);
+  t[2] = S * fmaf(C8, b0, C38 * b1);
+  t[6] = S * fmaf(C38, b0, -C8 * b1);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int k = 2 * j + 1;  // rows of CIIe for odd outputs, columns 0..3 (x[k]-x[7-k] symmetric)
+    t[k] = fmaf(k_dct2e[k * 8 + 0], u1[0], fmaf(k_dct2e[k * 8 + 1], u1[1], fmaf(k_dct2e[k * 8 + 2], u1[2],
+                k_dct2e[k * 8 + 3] * u1[3])));
+  }
+#pragma unroll
+  for (int j = 0; j < 8; j++) y[j] = sine ? t[7 - j] : t[j];
+}
+
+struct FoldIdx {
+  int src0, win0, dwin0, src1, win1, dwin1;
+  float sc0, ss0, ds0, sc1, ss1, ds1;
+};
+// DttRad2.get_fold_indices (DttRad2.java:109-144), n = 8
+__device__ __forceinline__ FoldIdx fold_idx(int x) {
+  FoldIdx f;
+  if (x < 4) {
+    f.src0 = 11 - x; f.win0 = 4 + x; f.sc0 = -1.f; f.ss0 = 1.f; f.dwin0 = 3 - x; f.ds0 = -1.f;
+    f.src1 = 12 + x; f.win1 = 3 - x; f.sc1 = -1.f; f.ss1 = -1.f; f.dwin1 = 4 + x; f.ds1 = -1.f;
+  } else {
+    x -= 4;
+    f.src0 = x; f.win0 = x; f.sc0 = 1.f; f.ss0 = 1.f; f.dwin0 = 7 - x; f.ds0 = 1.f;
+    f.src1 = 7 - x; f.win1 = 7 - x; f.sc1 = -1.f; f.ss1 = 1.f; f.dwin1 = x; f.ds1 = 1.f;
+  }
+  return f;
+}
+
+__device__ __forceinline__ int mirror(int p, int n) {
+  if (p < 0) return p & 1;
+  if (p >= n) return n - 2 + (p & 1);
+  return p;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// one pixel of the window: (row, col) relative to the window corner
+struct Win {
+  const void *img;
+  int64_t pitch;
+  int tlx, tly, W, H, u16, inside;
+  float scale;
+  __device__ __forceinline__ float at(int row, int col) const {
+    int y = tly + row, x = tlx + col;
+    if (!inside) { y = mirror(y, H); x = mirror(x, W); }
+    size_t o = (size_t)y * pitch + x;
+    float v = u16 ? (float)__ldg((const uint16_t *)img + o) : __ldg((const float *)img + o);
+    return v * scale;
+  }
+};
+
+// transpose of an 8x8 block held as one row per lane of an 8-lane group
+__device__ __forceinline__ void group_transpose(float v[8], float *buf, int r) {
+#pragma unroll
+  for (int j = 0; j < 8; j++) buf[j * 9 + r] = v[j];
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = buf[r * 9 + i];
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// phase A: CLT of one sub-tile, lane r of the 8-lane group holds row r
+// (= horizontal frequency r) of each quadrant on return: o[m][v].
+// ---------------------------------------------------------------------------
+template <int KIND>  // 0 mono, 1 Bayer red/blue, 2 Bayer green
+__device__ __forceinline__ void subtile_clt(const Win &w, float rx, float ry, int pc, int pr, int pg, int r,
+                                            float *tbuf, float o[4][8]) {
+  float ahs, ahc, avs, avc;
+  __sincosf(CUDART_PI_F * 0.0625f * rx, &ahs, &ahc);
+  __sincosf(CUDART_PI_F * 0.0625f * ry, &avs, &avc);
+  const FoldIdx fv = fold_idx(r);
+  const float vw0 = avc * k_hwin[fv.win0] + avs * k_hwin[fv.dwin0] * fv.ds0;
+  const float vw1 = avc * k_hwin[fv.win1] + avs * k_hwin[fv.dwin1] * fv.ds1;
+  float hw0[8], hw1[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const FoldIdx fh = fold_idx(j);
+    hw0[j] = ahc * k_hwin[fh.win0] + ahs * k_hwin[fh.dwin0] * fh.ds0;
+    hw1[j] = ahc * k_hwin[fh.win1] + ahs * k_hwin[fh.dwin1] * fh.ds1;
+  }
+  if (KIND == 1) {
+    // one nonzero pixel per folded value: the term whose source row/column has the colour's parity
+    const bool a1 = (fv.src0 & 1) != pr;
+    const int srow = a1 ? fv.src1 : fv.src0;
+    const float vk = a1 ? fv.sc1 * vw1 : fv.sc0 * vw0;
+    float y[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const FoldIdx fh = fold_idx(j);
+      const bool b1 = (fh.src0 & 1) != pc;
+      const int scol = b1 ? fh.src1 : fh.src0;
+      const float hk = b1 ? fh.sc1 * hw1[j] : fh.sc0 * hw0[j];
+      y[j] = (vk * hk) * w.at(srow, scol);
+    }
+    float z[8];
+    dct4_fast(y, z);
+    group_transpose(z, tbuf, r);
+    dct4_fast(z, o[0]);
+    // SC[h][v] = sh CC[7-h][v], CS[h][v] = sv CC[h][7-v], SS = sh sv CC[7-h][7-v]
+    const float sh = pc ? -1.f : 1.f, sv = pr ? -1.f : 1.f;
+#pragma unroll
+    for (int v = 0; v < 8; v++) o[1][v] = sh * __shfl_xor_sync(0xffffffffu, o[0][v], 7);
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      o[2][v] = sv * o[0][7 - v];
+      o[3][v] = sv * o[1][7 - v];
+    }
+  } else if (KIND == 2) {
+    // two nonzero pixels per folded value (checkerboard): CC and SC folds
+    float ycc[8], ysc[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const FoldIdx fh = fold_idx(j);
+      float cc = 0.f, sc = 0.f;
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        const int srow = a ? fv.src1 : fv.src0;
+        const float vk = a ? fv.sc1 * vw1 : fv.sc0 * vw0;
+        const bool b1 = ((fh.src0 + srow) & 1) != pg;  // column term with (row + col) parity pg
+        const int scol = b1 ? fh.src1 : fh.src0;
+        const float x = vk * w.at(srow, scol);
+        cc = fmaf(b1 ? fh.sc1 * hw1[j] : fh.sc0 * hw0[j], x, cc);
+        sc = fmaf(b1 ? fh.ss1 * hw1[j] : fh.ss0 * hw0[j], x, sc);
+      }
+      ycc[j] = cc;
+      ysc[j] = sc;
+    }
+    float z[8];
+    dct4_fast(ycc, z);
+    group_transpose(z, tbuf, r);
+    dct4_fast(z, o[0]);
+    dtt4_fast(ysc, z, true);
+    group_transpose(z, tbuf, r);
+    dct4_fast(z, o[1]);
+    // CS[h][v] = sg SC[7-h][7-v], SS[h][v] = sg CC[7-h][7-v]
+    const float sg = pg ? -1.f : 1.f;
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      o[2][7 - v] = sg * __shfl_xor_sync(0xffffffffu, o[1][v], 7);
+      o[3][7 - v] = sg * __shfl_xor_sync(0xffffffffu, o[0][v], 7);
+    }
+  } else {
+    // dense plane: vertical 2-tap combine once, then the two horizontal variants
+#pragma unroll
+    for (int vb = 0; vb < 2; vb++) {
+      const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
+      float vc[16];
+#pragma unroll
+      for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+#pragma unroll
+      for (int hb = 0; hb < 2; hb++) {
+        float y[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const FoldIdx fh = fold_idx(j);
+          const float h0 = (hb ? fh.ss0 : fh.sc0) * hw0[j], h1 = (hb ? fh.ss1 : fh.sc1) * hw1[j];
+          y[j] = fmaf(h1, vc[fh.src1], h0 * vc[fh.src0]);
+        }
+        float z[8];
+        dtt4_fast(y, z, hb);
+        group_transpose(z, tbuf, r);
+        dtt4_fast(z, o[vb * 2 + hb], vb);
+      }
+    }
+  }
+}
+
+// convolution with the kernel tile and the phase-rotation shift, in place on o[m][v]
+__device__ __forceinline__ void conv_shift(float o[4][8], const float *kp, float rx, float ry, int r) {
+  if (kp) {
+    float k[4][8];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const float4 *p = (const float4 *)(kp + m * 64 + r * 8);
+      float4 a = __ldg(p), b = __ldg(p + 1);
+      k[m][0] = a.x; k[m][1] = a.y; k[m][2] = a.z; k[m][3] = a.w;
+      k[m][4] = b.x; k[m][5] = b.y; k[m][6] = b.z; k[m][7] = b.w;
+    }
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      const float d0 = o[0][v], d1 = o[1][v], d2 = o[2][v], d3 = o[3][v];
+      const float k0 = k[0][v], k1 = k[1][v], k2 = k[2][v], k3 = k[3][v];
+      o[0][v] = d0 * k0 - d1 * k1 - d2 * k2 + d3 * k3;
+      o[1][v] = d1 * k0 + d0 * k1 - d3 * k2 - d2 * k3;
+      o[2][v] = d2 * k0 - d3 * k1 + d0 * k2 - d1 * k3;
+      o[3][v] = d3 * k0 + d2 * k1 + d1 * k2 + d0 * k3;
+    }
+  }
+  float ch, shh, cvr, svr;
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * rx, &shh, &ch);
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * ry, &svr, &cvr);
+  const int base = threadIdx.x & 24;  // first lane of this 8-lane group
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float cv = __shfl_sync(0xffffffffu, cvr, base + v), sv = __shfl_sync(0xffffffffu, svr, base + v);
+    const float t0 = o[0][v] * ch - o[1][v] * shh, t1 = o[1][v] * ch + o[0][v] * shh;
+    const float t2 = o[2][v] * ch - o[3][v] * shh, t3 = o[3][v] * ch + o[2][v] * shh;
+    o[0][v] = t0 * cv - t2 * sv;
+    o[2][v] = t2 * cv + t0 * sv;
+    o[1][v] = t1 * cv - t3 * sv;
+    o[3][v] = t3 * cv + t1 * sv;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase B helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float strip_sample(const float *c, int kind, float bx, float by, int row, int scol, int down) {
+  if (kind <= 3) {
+    const int sh = (kind > 1) ? 0 : 1, ilimit = 7 << sh;  // denom = 1 << sh
+    int xnum, ynum;
+    if (kind == 0) { xnum = 2 * scol + (row & 1); ynum = down * row; }
+    else if (kind == 1) { xnum = down * row; ynum = 2 * scol + (row & 1); }
+    else if (kind == 2) { xnum = scol - ((down * row) >> 1); ynum = scol + ((down * row + 1) >> 1); }
+    else { xnum = scol - ((down * row) >> 1); ynum = -scol - ((down * row + 1) >> 1); }
+    if (xnum > ilimit || xnum < -ilimit || ynum > ilimit || ynum < -ilimit) return CUDART_NAN_F;
+    const int ix0 = (xnum + ilimit) >> sh, iy0 = (ynum + ilimit) >> sh;
+    const bool int_x = (xnum & ((1 << sh) - 1)) == 0, int_y = (ynum & ((1 << sh) - 1)) == 0;
+    if (int_x && int_y) return c[iy0 * 15 + ix0];
+    const float dx = int_x ? 0.f : 0.5f, dy = int_y ? 0.f : 0.5f;
+    if (int_y) return (1.0f - dx) * c[iy0 * 15 + ix0] + dx * c[iy0 * 15 + ix0 + 1];
+    if (int_x) return (1.0f - dy) * c[iy0 * 15 + ix0] + dy * c[(iy0 + 1) * 15 + ix0];
+    return ((1.0f - dx) * (1.0f - dy) * c[iy0 * 15 + ix0]) + (dx * (1.0f - dy) * c[iy0 * 15 + ix0 + 1]) +
+           ((1.0f - dx) * dy * c[(iy0 + 1) * 15 + ix0]) + (dx * dy * c[(iy0 + 1) * 15 + ix0 + 1]);
+  }
+  const float a = scol + 0.5f * (row & 1), pp = 0.5f * down * row;
+  const float x = a * bx - pp * by, y = a * by + pp * bx;
+  if (x > 7.f || x < -7.f || y > 7.f || y < -7.f) return CUDART_NAN_F;
+  const float fx = x + 7.f, fy = y + 7.f;
+  const int ix0 = min((int)floorf(fx), 13), iy0 = min((int)floorf(fy), 13);
+  const float dx = fx - ix0, dy = fy - iy0;
+  return ((1.0f - dx) * (1.0f - dy) * c[iy0 * 15 + ix0]) + (dx * (1.0f - dy) * c[iy0 * 15 + ix0 + 1]) +
+         ((1.0f - dx) * dy * c[(iy0 + 1) * 15 + ix0]) + (dx * dy * c[(iy0 + 1) * 15 + ix0 + 1]);
+}
+
+// one strip sample from a precomputed code (quad kinds): same arithmetic as
+// Correlation2d.java:664-690 with dx, dy in {0, 0.5}
+__device__ __forceinline__ float sample_code(const float *c, int code) {
+  if (code < 0) return CUDART_NAN_F;
+  const int idx = code & 255, cs = code >> 8;
+  const float v = c[idx];
+  if (cs == 0) return v;
+  if (cs == 1) return 0.5f * v + 0.5f * c[idx + 1];
+  if (cs == 2) return 0.5f * v + 0.5f * c[idx + 15];
+  return ((0.25f * v + 0.25f * c[idx + 1]) + 0.25f * c[idx + 15]) + 0.25f * c[idx + 16];
+}
+
+struct FwdShape {
+  int nw;                 // warps per CTA (each warp owns whole tiles)
+  int S, C, P, RE, quad;  // sensors, colours, pairs, strip entries, quad layout
+  int clt_floats, per_warp;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// the fused kernel: one warp carries a tile through all stages, no CTA barriers
+// ---------------------------------------------------------------------------
+template <int C>  // colours: 1 (mono) or 3 (Bayer R, B, G)
+__global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_constant__ SceneDev sc,
+                                                               const __grid_constant__ FwdShape fs,
+                                                               const __grid_constant__ CorrConst cfg) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
+  // per-warp shared memory: CLT of the tile [S][C][4][64] and two 288-float scratch buffers
+  float *s_clt = sm + warp * fs.per_warp;
+  float *scr = s_clt + fs.clt_floats;
+  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+  const int groups = (S + 3) >> 2;
+  const int q = lane >> 3, r = lane & 7;
+  const bool log_mode = cfg.log_combine;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  const int rr = sc.bayer_red_row, rc = sc.bayer_red_col;
+
+  for (int task = blockIdx.x * NW + warp; task < sc.num_tasks; task += gridDim.x * NW) {
+    const int txy = sc.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+    // ---------------- stage 2: CLT of every (sensor, colour) ----------------
+    for (int gt = 0; gt < C * groups; gt++) {
+      const int c = gt / groups, g = gt - c * groups;
+      const int s = g * 4 + q;
+      const bool act = s < S;
+      const int sidx = act ? s : S - 1;
+      const SubtilePlan p = sc.plan[((size_t)task * S + sidx) * C + c];
+      Win w;
+      w.img = sc.images[sidx];
+      w.pitch = sc.img_pitch;
+      w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
+      w.u16 = sc.img_dtype[sidx];
+      w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
+      w.scale = sc.color_scale[c];
+      float o[4][8];
+      float *tbuf = scr + q * 72;
+      float sg0 = 1.f, sg1 = 1.f;  // symmetry signs kept for the correlation reads
+      if (C == 1) {
+        subtile_clt<0>(w, p.rx, p.ry, 0, 0, 0, r, tbuf, o);
+      } else if (c < 2) {
+        const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
+        subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
+        sg0 = pc ? -1.f : 1.f;
+        sg1 = pr ? -1.f : 1.f;
+      } else {
+        const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
+        subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
+        sg0 = pg ? -1.f : 1.f;
+      }
+      const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
+      conv_shift(o, kp, p.rx, p.ry, r);
+      if (act) {
+        float *gdst = sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+          *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+        }
+        // all four quadrants: after the convolution and the shift the Bayer symmetries no longer hold
+        float *sdst = s_clt + ((size_t)s * C + c) * TP_CLT + r * 8;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          *(float4 *)(sdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+          *(float4 *)(sdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+        }
+      }
+      (void)sg0;
+      (void)sg1;
+    }
+    __syncwarp();
+    // ---------------- stage 3a/3b: pairs, strips ----------------
+    float cmb[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    float *qb = scr, *tb = scr + 288;
+    for (int pi = 0; pi < P; pi++) {
+      const PairDev pd = cfg.pairs[pi];
+      const float *c1 = s_clt + (size_t)pd.cam1 * C * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * C * TP_CLT;
+      float acc[4][2];
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        float d1[4][2], d2[4][2], a2[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            d1[m][h] = c1[c * TP_CLT + m * 64 + lane + 32 * h];
+            d2[m][h] = c2[c * TP_CLT + m * 64 + lane + 32 * h];
+            s1 = fmaf(d1[m][h], d1[m][h], s1);
+            s2 = fmaf(d2[m][h], d2[m][h], s2);
+          }
+          a2[h] = sqrtf(s1 * s2);
+        }
+        const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * cfg.fat_zero * cfg.fat_zero;
+        const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const float sw = wgt / (a2[h] + fz2);
+          const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
+          const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
+          const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
+          const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
+          if (c == 0) {
+            acc[0][h] = t0 * sw; acc[1][h] = t1 * sw; acc[2][h] = t2 * sw; acc[3][h] = t3 * sw;
+          } else {
+            acc[0][h] = fmaf(t0, sw, acc[0][h]); acc[1][h] = fmaf(t1, sw, acc[1][h]);
+            acc[2][h] = fmaf(t2, sw, acc[2][h]); acc[3][h] = fmaf(t3, sw, acc[3][h]);
+          }
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int idx = lane + 32 * h;
+        const float l = cfg.lpf[idx];
+        const int off = (idx >> 3) * 9 + (idx & 7);
+#pragma unroll
+        for (int qq = 0; qq < 4; qq++) qb[qq * 72 + off] = acc[qq][h] * l;
+      }
+      __syncwarp();
+      {
+        float x[8], y[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) x[e] = qb[q * 72 + r * 9 + e];
+        dtt2e_fast(x, y, (q >> 1) & 1);
+#pragma unroll
+        for (int j = 0; j < 8; j++) tb[q * 72 + j * 9 + r] = y[j];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 8; e++) x[e] = tb[q * 72 + r * 9 + e];
+        dtt2e_fast(x, y, q & 1);
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 8; e++) qb[q * 72 + r * 9 + e] = y[e];
+      }
+      __syncwarp();
+      // 15x15 unfold (DttRad2.corr_unfold_tile): each lane owns 2 cells (a, b) and writes their mirror images
+      float *cs = tb;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int a = (lane >> 3) + 4 * k, b = lane & 7;
+        const float A = qb[a * 9 + b];
+        const float B = b ? qb[72 + a * 9 + b - 1] : 0.f;
+        const float Cc = a ? qb[144 + (a - 1) * 9 + b] : 0.f;
+        const float D = (a && b) ? qb[216 + (a - 1) * 9 + b - 1] : 0.f;
+        cs[(7 + a) * 15 + 7 + b] = 0.25f * (((A + B) + Cc) + D);
+        if (b) cs[(7 + a) * 15 + 7 - b] = 0.25f * (((A - B) + Cc) - D);
+        if (a) cs[(7 - a) * 15 + 7 + b] = 0.25f * (((A + B) - Cc) - D);
+        if (a && b) cs[(7 - a) * 15 + 7 - b] = 0.25f * (((A - B) - Cc) + D);
+      }
+      __syncwarp();
+      float *gc = sc.corr + (tile * P + pi) * TP_CORR;
+      for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
+      if (pd.in_combo) {
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+          const int e = lane + 32 * t;
+          if (e < RE) {
+            const int row = e / 15;
+            float d;
+            if (pd.kind <= 3) {
+              const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+              d = sample_code(cs, code.x);
+              if (row > 0) {
+                const float d2 = sample_code(cs, code.y);
+                d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+              }
+            } else {
+              const int scol = e - row * 15 - 7;
+              d = strip_sample(cs, 4, pd.bx, pd.by, row, scol, -1);
+              if (row > 0) {
+                const float d2 = strip_sample(cs, 4, pd.bx, pd.by, row, scol, 1);
+                d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+              }
+            }
+            float v = d + cfg.corr_offset;
+            if (v < 0.0f) v = 0.0f;
+            if (log_mode) cmb[t] += logf(v);
+            else cmb[t] *= cfg.twice_diagonal ? v * v : v;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    // ---------------- stage 3c: extraction ----------------
+    float *combo = scr;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int e = lane + 32 * t;
+      if (e < RE) {
+        float v = cmb[t];
+        if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
+        else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
+        combo[e] = v;
+      }
+    }
+    __syncwarp();
+    float res[TP_NDISP];
+#pragma unroll
+    for (int k = 0; k < TP_NDISP; k++) res[k] = (k == 2 || k == 4 || k == 6) ? 0.f : CUDART_NAN_F;
+    {
+      // integer argmax on row 0 (getMaxXYInt): first maximum over the non-NaN entries
+      const float v = (lane < 15) ? combo[lane] : CUDART_NAN_F;
+      float best = isnan(v) ? -CUDART_INF_F : v;
+      int bi = lane < 15 ? lane : 99;
+#pragma unroll
+      for (int o2 = 16; o2 > 0; o2 >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      const unsigned finite = __ballot_sync(0xffffffffu, lane < 15 && !isnan(v));
+      const int imx = finite ? bi : 14;
+      const float vmax = combo[imx];
+      if (vmax >= cfg.min_corr) {
+        const int ix = imx - 7;
+        res[0] = (float)(-ix);
+        res[2] = vmax;
+        res[8] = (float)ix;
+        int dh = cfg.strip_rows;
+        float wys = 1.0f;
+        if (dh > cfg.wndy_size) dh = cfg.wndy_size;
+        else if (dh < cfg.wndy_size) {
+          float swy = cfg.wndy[0];
+          for (int i = 1; i < dh; i++) swy += cfg.wndy[i];
+          wys = 1.0f / swy;
+        }
+        float s0 = 0.f, sx = 0.f;
+        const int x0 = 7 + ix, nk = dh * 2 * cfg.wndx_size;
+        for (int k = lane; k < nk; k += 32) {  // windowed centroid (getMaxXCm), one sample per lane
+          const int dy = k / (2 * cfg.wndx_size), rest = k - dy * 2 * cfg.wndx_size;
+          const int adx = rest >> 1, dir = (rest & 1) ? 1 : -1, odd = dy & 1;
+          if (((adx - odd) & 1) || (adx == 0 && dir < 0)) continue;
+          const int idx = (adx * dir) >> 1, xx = 2 * idx + odd, x1 = x0 + idx;
+          if (x1 < 0 || x1 >= 15) continue;
+          float d = combo[dy * 15 + x1];
+          if (isnan(d) || !(d > 0.0f)) continue;
+          d *= (((dy == 0) ? wys : 2.0f * wys) * cfg.wndy[dy]) * cfg.wndx[adx];
+          s0 += d;
+          sx += d * xx;
+        }
+        s0 = warp_sum(s0);
+        sx = warp_sum(sx);
+        if (s0 != 0.0f) {
+          res[1] = -(ix + sx / s0 / 2);
+          res[7] = s0;
+        }
+      }
+    }
+    if (fs.quad && (cfg.num_hor > 0 || cfg.num_vert > 0)) {
+      // getMaxXSOrtho: lanes 0-14 horizontal pairs, lanes 16-30 vertical pairs
+      // the surfaces of this tile were just written by this warp (L1/L2 resident)
+      const int half = lane >> 4, j = lane & 15;
+      const int np = half ? cfg.num_vert : cfg.num_hor;
+      float sum = -CUDART_INF_F;
+      if (j < 15 && np > 0) {
+        sum = 0.f;
+        for (int i = 0; i < 15; i++) {
+          float prod = 1.f;
+          for (int k = 0; k < np; k++) {
+            const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
+            const float d = half ? 0.5f * (cc[j * 15 + i] + cc[j * 15 + 14 - i])
+                                 : 0.5f * (cc[i * 15 + j] + cc[(14 - i) * 15 + j]);
+            prod *= d + cfg.corr_offset;
+          }
+          const float v = (prod > 0.0f) ? ((np == 2) ? sqrtf(prod) : ((np == 1) ? prod : powf(prod, 1.0f / np))) -
+                                              cfg.corr_offset
+                                        : -cfg.corr_offset;
+          sum += v * cfg.notch[i];
+        }
+      }
+      float best = sum;
+      int bi = (j < 15) ? j : 99;
+#pragma unroll
+      for (int o2 = 8; o2 > 0; o2 >>= 1) {  // within each 16-lane half
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      const int ic = bi, base = half << 4;
+      const float f0 = __shfl_sync(0xffffffffu, sum, base + (ic > 0 ? ic - 1 : 0));
+      const float f1 = __shfl_sync(0xffffffffu, sum, base + ic);
+      const float f2 = __shfl_sync(0xffffffffu, sum, base + (ic < 14 ? ic + 1 : 14));
+      float xc = (float)ic;
+      if (ic > 0 && ic < 14) {
+        const float den = f0 - 2.0f * f1 + f2;
+        if (den != 0.0f) xc = ic + 0.5f * (f0 - f2) / den;
+      }
+      int ir = (int)floorf(xc + 0.5f);
+      ir = ir < 0 ? 0 : (ir > 14 ? 14 : ir);
+      const float fr = __shfl_sync(0xffffffffu, sum, base + ir);
+      const float hx = __shfl_sync(0xffffffffu, xc, 0), hs = __shfl_sync(0xffffffffu, fr, 0);
+      const float vx = __shfl_sync(0xffffffffu, xc, 16), vs = __shfl_sync(0xffffffffu, fr, 16);
+      if (cfg.num_hor > 0) { res[3] = -(hx - 7.0f); res[4] = hs / 8.0f; }
+      if (cfg.num_vert > 0) { res[5] = -(vx - 7.0f); res[6] = vs / 8.0f; }
+    }
+    float *dm = sc.disp + tile * TP_NDISP;
+    if (lane < TP_NDISP) {
+      float v = res[0];
+#pragma unroll
+      for (int k = 1; k < TP_NDISP; k++) if (lane == k) v = res[k];
+      dm[lane] = v;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void disp_init_kernel(float *disp, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n * TP_NDISP) {
+    int k = i % TP_NDISP;
+    disp[i] = (k == 2 || k == 4 || k == 6) ? 0.0f : CUDART_NAN_F;
+  }
+}
+
+cudaError_t upload_fused_constants() {
+  float hw[8], d2[64], c4[4], s4[4];
+  const double pi = 3.14159265358979323846, sc = 1.0 / std::sqrt(8.0);
+  for (int i = 0; i < 8; i++) hw[i] = (float)std::sin(pi / 16.0 * (i + 0.5));
+  for (int k = 0; k < 8; k++)
+    for (int n = 0; n < 8; n++) d2[k * 8 + n] = (float)(std::sqrt(2.0 / 8) * std::cos(pi * k * (2 * n + 1) / 16.0));
+  for (int k = 0; k < 4; k++) {
+    c4[k] = (float)(sc * std::cos((2 * k + 1) * pi / 32));
+    s4[k] = (float)(sc * std::sin((2 * k + 1) * pi / 32));
+  }
+  cudaError_t e = cudaMemcpyToSymbol(k_hwin, hw, sizeof(hw));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_dct2e, d2, sizeof(d2));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_d4c, c4, sizeof(c4));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_d4s, s4, sizeof(s4));
+  return e;
+}
+
+static FwdShape make_shape(const SceneDev &sc, int nw) {
+  FwdShape f;
+  f.S = sc.num_sensors;
+  f.C = sc.num_colors;
+  f.P = sc.num_pairs;
+  f.RE = sc.strip_rows * 15;
+  f.quad = (sc.num_pairs <= 8) ? 1 : 0;
+  f.nw = nw > 0 ? nw : (f.C == 3 ? 1 : 4);  // one-warp CTAs pack best when the tile CLT is large
+  f.clt_floats = f.S * f.C * TP_CLT;
+  f.per_warp = f.clt_floats + SCR;
+  f.per_warp = (f.per_warp + 3) & ~3;
+  return f;
+}
+
+int fused_smem_bytes(const SceneDev &sc, int tpb, int nw) {
+  (void)tpb;
+  FwdShape f = make_shape(sc, nw);
+  return f.per_warp * f.nw * 4;
+}
+
+// tpb is accepted for the schedule interface; one warp always owns one tile here
+template <int C>
+static cudaError_t launch_fused_c(const SceneDev &sc, const CorrConst &cc, const FwdShape &f, cudaStream_t st) {
+  const int bytes = f.per_warp * f.nw * 4;
+  cudaError_t e = cudaFuncSetAttribute(fused_forward_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_forward_kernel<C>, f.nw * 32, bytes);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int need = (sc.num_tasks + f.nw - 1) / f.nw;
+  const int grid = need < sms * per_sm ? need : sms * per_sm;
+  fused_forward_kernel<C><<<grid, f.nw * 32, bytes, st>>>(sc, f, cc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st) {
+  (void)tpb;
+  const int ntiles = sc.tilesX * sc.tilesY;
+  disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || sc.num_tasks <= 0) return e;
+  if (sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidConfiguration;
+  FwdShape f = make_shape(sc, nw);
+  if (f.nw > 4) return cudaErrorInvalidConfiguration;
+  return sc.num_colors == 3 ? launch_fused_c<3>(sc, cc, f, st) : launch_fused_c<1>(sc, cc, f, st);
+}

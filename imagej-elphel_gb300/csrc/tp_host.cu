@@ -43,6 +43,7 @@ struct tp_handle {
   int ports_from_geometry = 0;
   int have_geometry = 0, have_tasks = 0, have_corr = 0, lpf_on = 0, planned = 0;
   int num_pairs = 0, corr_capacity = 0;
+  int sched_tpb = 0, sched_nw = 0;  // fused-kernel schedule (0 = defaults)
   float color_scale[3] = {1.f, 1.f, 1.f};
   GeomDev geom_host;
   CorrDev corr_host;
@@ -110,6 +111,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
   sc.corr_cfg = h->d_corr_cfg;
   sc.num_pairs = h->num_pairs;
+  sc.strip_rows = h->corr_host.strip_rows;
   return sc;
 }
 
@@ -307,6 +309,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   bool ok = cudaSetDevice(cfg->device) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
   ok = ok && upload_kernel_constants() == cudaSuccess;
+  ok = ok && upload_fused_constants() == cudaSuccess;
   for (int s = 0; ok && s < S; s++) {
     ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
     if (ok && cfg->kernels_hor > 0) {
@@ -542,6 +545,31 @@ tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pair
   }
   cd.log_combine = general ? 1 : 0;
   if (general) cd.num_hor = cd.num_vert = 0;  // ortho maxima are defined for the quad layout only
+  if (cd.num_hor > 8 || cd.num_vert > 8) return fail(h, TP_ERR_ARG, "tp_set_corr: more than 8 hor/vert pairs");
+  for (int i = 0, nh = 0, nv = 0; i < np && !general; i++) {
+    if (pairs[i].kind == 0) cd.hor_pairs[nh++] = i;
+    if (pairs[i].kind == 1) cd.vert_pairs[nv++] = i;
+  }
+  // sample points of Correlation2d.scaleRotateInterpoateSingleCorrelation (610-718) for the quad kinds
+  for (int kind = 0; kind < 4; kind++)
+    for (int e = 0; e < TP_MAX_STRIP * 15; e++)
+      for (int dn = 0; dn < 2; dn++) {
+        const int row = e / 15, scol = e % 15 - 7, down = dn ? 1 : -1;
+        const int sh = (kind > 1) ? 0 : 1, ilimit = 7 << sh;
+        int xn, yn;
+        if (kind == 0) { xn = 2 * scol + (row & 1); yn = down * row; }
+        else if (kind == 1) { xn = down * row; yn = 2 * scol + (row & 1); }
+        else if (kind == 2) { xn = scol - ((down * row) >> 1); yn = scol + ((down * row + 1) >> 1); }
+        else { xn = scol - ((down * row) >> 1); yn = -scol - ((down * row + 1) >> 1); }
+        short code = -1;
+        if (!(xn > ilimit || xn < -ilimit || yn > ilimit || yn < -ilimit)) {
+          const int ix0 = (xn + ilimit) >> sh, iy0 = (yn + ilimit) >> sh;
+          const bool ix = (xn & ((1 << sh) - 1)) == 0, iy = (yn & ((1 << sh) - 1)) == 0;
+          const int cs = (ix && iy) ? 0 : (iy ? 1 : (ix ? 2 : 3));
+          code = (short)((iy0 * 15 + ix0) | (cs << 8));
+        }
+        cd.strip_code[kind][e][dn] = code;
+      }
   if (np > h->corr_capacity) {
     cudaFree(h->d_corr);
     h->d_corr = nullptr;
@@ -622,11 +650,24 @@ tp_status tp_imclt(tp_handle *h, void *stream) {
 
 tp_status tp_process(tp_handle *h, void *stream) {
   if (!h) return TP_ERR_ARG;
-  h->planned = 0;
-  tp_status r = tp_convert_correct(h, stream);
-  if (r == TP_OK && h->num_pairs > 0) r = tp_correlate(h, stream);
-  if (r == TP_OK && h->num_pairs > 0) r = tp_extract(h, stream);
-  return r;
+  // the plan (ports, window corners) is recomputed only when geometry, kernels or tasks changed
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  if (h->num_pairs == 0) return tp_convert_correct(h, stream);
+  CK(launch_fused_forward(scene_of(h), h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
+  return TP_OK;
+}
+
+tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block) {
+  if (!h) return TP_ERR_ARG;
+  // the fused kernel gives each warp whole tiles: tiles per CTA == warps per CTA (<= 4)
+  if (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4)
+    return fail(h, TP_ERR_ARG, "tp_set_schedule: out of range");
+  if (warps_per_block == 0) warps_per_block = tiles_per_block;
+  h->sched_tpb = tiles_per_block;
+  h->sched_nw = warps_per_block;
+  return TP_OK;
 }
 
 tp_status tp_synchronize(tp_handle *h) {

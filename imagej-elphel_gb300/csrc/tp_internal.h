@@ -41,7 +41,9 @@ struct PairDev {
   float bx, by;
 };
 
-struct CorrDev {
+// correlation set-up read uniformly by every warp: passed to the fused kernel by value
+// (__grid_constant__), so its fields are constant-bank operands
+struct CorrConst {
   int num_pairs;
   int strip_rows;
   int twice_diagonal;
@@ -57,7 +59,15 @@ struct CorrDev {
   float wndy[TP_MAX_STRIP];
   float wndx[32];
   float notch[15];
+  int hor_pairs[8], vert_pairs[8];  // pair indices of kind 0 / 1 (ortho maxima)
   PairDev pairs[TP_MAXP];
+};
+
+struct CorrDev : CorrConst {
+  // strip sample codes of the quad kinds 0..3 per (row*15+col, down): source index
+  // iy0*15+ix0 in bits 0-7, interpolation case in bits 8-9, -1 outside the surface
+  // (lane-divergent reads: kept in global memory, L1-cached)
+  short strip_code[4][TP_MAX_STRIP * 15][2];
 };
 
 struct SceneDev {
@@ -92,6 +102,7 @@ struct SceneDev {
   const float *lpf_rbg;      // [C][64] or null
   const CorrDev *corr_cfg;
   int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
+  int strip_rows;            // host copy of corr_cfg->strip_rows
 };
 
 // launchers (tp_plan.cu / tp_kernels.cu)
@@ -105,3 +116,8 @@ cudaError_t launch_compact_tasks(const int *tile_op, const float *disparity, int
                                  int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
                                  cudaStream_t st);
 cudaError_t upload_kernel_constants();
+// fused forward (tp_fused.cu): convert+correct, correlation, extraction in one kernel;
+// tpb/nw = tiles and warps per CTA (<= 0: defaults for the sensor/colour layout)
+cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st);
+cudaError_t upload_fused_constants();
+int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);

@@ -72,6 +72,7 @@ PROTOTYPES = {
     "tp_extract": [_H, _vp],
     "tp_imclt": [_H, _vp],
     "tp_process": [_H, _vp],
+    "tp_set_schedule": [_H, C.c_int, C.c_int],
     "tp_synchronize": [_H],
     "tp_get_num_tasks": [_H, C.POINTER(C.c_int)],
     "tp_get_ports": [_H, _vp],

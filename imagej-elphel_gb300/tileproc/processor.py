@@ -225,3 +225,7 @@ class GPUTileProcessor:
         out = np.zeros((self.num_colors, self.height + 8, self.width + 8), dtype=np.float32)
         self._ck(self._lib.tp_get_rbg(self.h, int(ncam), _ptr(out)), "tp_get_rbg")
         return out
+
+    def setSchedule(self, tiles_per_block=0, warps_per_block=0):
+        """Fused-kernel schedule (0, 0 = defaults for the sensor/colour layout)."""
+        self._ck(self._lib.tp_set_schedule(self.h, int(tiles_per_block), int(warps_per_block)), "tp_set_schedule")

@@ -162,6 +162,10 @@ tp_status tp_extract(tp_handle *h, void *stream);
 tp_status tp_imclt(tp_handle *h, void *stream);
 /* ports + convert_correct + correlate + extract in one call (ImageDtt.clt_aberrations_quad_corr) */
 tp_status tp_process(tp_handle *h, void *stream);
+/* schedule of the fused forward kernel: tiles per CTA and warps per CTA (0 = defaults);
+ * chosen by tileproc.autotune (no reference counterpart: the reference hard-codes
+ * TILES_PER_BLOCK, GPUTileProcessor.java:92) */
+tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block);
 tp_status tp_synchronize(tp_handle *h);
 
 /* outputs (host copies) */

@@ -217,3 +217,34 @@ def test_imclt(oracle):
         want = _oracle_rbg(oracle, clt, W // 8, H // 8, 4, 3, W, H, lpf=lpf)
         got = tp.getRBG(2).astype(np.float64)
         assert np.abs(got - want[2]).max() / np.abs(want[2]).max() < 2e-6
+
+
+@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (2, 2), (4, 4)])
+def test_stage_kernels_and_schedules_agree(oracle, sched):
+    """Per-stage kernels (execConverCorrectTiles/execCorrelate/execExtract) and the fused
+    kernel under several CTA schedules give the same results."""
+    sc = synth.make_scene("quad_bayer", seed=12, width=192, height=128)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    rng = np.random.default_rng(3)
+    k, e = synth.random_clt_kernels(rng, 4, 128 // 16 + 2, 192 // 16 + 2, 3)
+    ref = run_oracle(oracle, sc, 4.0, kernels=k, kext=e)
+    with make_gpu(sc, k, e) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.execPorts()
+        tp.execConverCorrectTiles()
+        tp.execCorrelate()
+        tp.execExtract()
+        clt_s, corr_s, d_s = tp.getClt(), tp.getCorr(), tp.getDisparity()
+        tp.setSchedule(*sched)
+        tp.process()
+        clt_f, corr_f, d_f = tp.getClt(), tp.getCorr(), tp.getDisparity()
+    for clt in (clt_s, clt_f):
+        e1 = rel_l2(clt.astype(np.float64), ref["clt"], axis=(-2, -1))
+        assert e1.max() <= CLT_TOL
+    for corr in (corr_s, corr_f):
+        e2 = rel_l2(corr.astype(np.float64), ref["corr"], axis=-1)
+        assert e2.max() <= CORR_TOL
+    ok = np.isfinite(ref["disp"][:, oracle.DISP_CM]) & (d_f[:, oracle.DISP_IXY] == ref["disp"][:, oracle.DISP_IXY])
+    assert np.abs(d_f[ok, oracle.DISP_CM] - ref["disp"][ok, oracle.DISP_CM]).max() <= DISP_TOL
+    assert np.abs(d_f[ok, oracle.DISP_CM] - d_s[ok, oracle.DISP_CM]).max() <= DISP_TOL
