@@ -667,6 +667,110 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
   }
 }
 
+// ---------------------------------------------------------------------------
+// IMCLT (ImageDtt.iclt_2d, the reference GPU imclt_rbg) with overlap-add into the
+// padded colour frames.  CTA = one 64x64-pixel region of one (sensor, colour)
+// plane; the 9x9 tiles touching it are processed in the four tile-parity phases
+// (tiles of one phase never overlap), so the region accumulates in shared memory
+// without atomics and in a fixed order.  A warp carries 4 tiles at once, one per
+// 8-lane group, lane r owning row r of each quadrant.
+// ---------------------------------------------------------------------------
+constexpr int IR = 8;            // region = IR x IR blocks of 8x8 pixels
+constexpr int IPX = IR * 8;
+constexpr int ISTR = IPX + 1;
+
+__global__ void __launch_bounds__(256) imclt_fast_kernel(const __grid_constant__ SceneDev sc) {
+  __shared__ float acc[IPX * ISTR];
+  __shared__ float tbuf_all[8][4 * 72];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
+  const int S = sc.num_sensors, C = sc.num_colors;
+  const int plane = blockIdx.z, s = plane / C, c = plane - s * C;
+  const int bx0 = blockIdx.x * IR, by0 = blockIdx.y * IR;
+  const int fw = sc.width + 8, fh = sc.height + 8;
+  for (int i = threadIdx.x; i < IPX * ISTR; i += blockDim.x) acc[i] = 0.f;
+  __syncthreads();
+  float *tbuf = tbuf_all[warp] + q * 72;
+  const float *lpf = sc.lpf_rbg ? sc.lpf_rbg + c * 64 : nullptr;
+  // unfold rows fed by source row r (DttRad2.get_unfold_index_signs, 392-404)
+  const int i1 = (r >= 4) ? r - 4 : 11 - r, i2 = (r >= 4) ? 11 - r : r + 12;
+  const float sa1 = (r >= 4) ? 1.f : -1.f, sb1 = 1.f;    // signs (cos, sin branch) of row i1
+  const float sa2 = -1.f, sb2 = (r >= 4) ? 1.f : -1.f;   // signs of row i2
+  const float w1 = k_hwin[i1 < 8 ? i1 : 15 - i1], w2 = k_hwin[i2 < 8 ? i2 : 15 - i2];
+  const float kc1 = sa1 * w1, ks1 = sb1 * w1, kc2 = sa2 * w2, ks2 = sb2 * w2;
+  for (int ph = 0; ph < 4; ph++) {
+    const int pxp = ph & 1, pyp = ph >> 1;
+    int tx0 = bx0 - 1, ty0 = by0 - 1;
+    if ((tx0 & 1) != pxp) tx0++;
+    if ((ty0 & 1) != pyp) ty0++;
+    const int ntx = (bx0 + IR - 1 - tx0) / 2 + 1, nty = (by0 + IR - 1 - ty0) / 2 + 1;
+    for (int k0 = warp * 4; k0 < ntx * nty; k0 += 32) {
+      const int k = k0 + q;
+      const int tx = tx0 + 2 * (k % ntx), ty = ty0 + 2 * (k / ntx);
+      bool act = k < ntx * nty && tx >= 0 && ty >= 0 && tx < sc.tilesX && ty < sc.tilesY;
+      size_t tile = act ? (size_t)ty * sc.tilesX + tx : 0;
+      if (act && sc.tile_task[tile] < 0) act = false;
+      float o[4][8];
+      const float *src = sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+        if (act) {
+          a = __ldg((const float4 *)(src + m * 64));
+          b = __ldg((const float4 *)(src + m * 64 + 4));
+        }
+        o[m][0] = a.x; o[m][1] = a.y; o[m][2] = a.z; o[m][3] = a.w;
+        o[m][4] = b.x; o[m][5] = b.y; o[m][6] = b.z; o[m][7] = b.w;
+      }
+#pragma unroll
+      for (int v = 0; v < 8; v++) {
+        const float l = 0.25f * (lpf ? lpf[r * 8 + v] : 1.0f);
+#pragma unroll
+        for (int m = 0; m < 4; m++) o[m][v] *= l;
+      }
+      // inverse 2D DCT-IV/DST-IV with the swapped mode (ImageDtt.java:3628):
+      // rows (vertical frequency) first, then columns
+      float t[4][8];
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        float z[8];
+        dtt4_fast(o[m], z, (m >> 1) & 1);
+        group_transpose(z, tbuf, r);
+        dtt4_fast(z, t[m], m & 1);  // lane r: vertical position r, t[m][x] horizontal position x
+      }
+      // unfold (DttRad2.unfold_tile) into rows i1, i2 and accumulate
+      const int gy1 = ty * 8 + i1 - by0 * 8, gy2 = ty * 8 + i2 - by0 * 8;
+#pragma unroll
+      for (int jj = 0; jj < 16; jj++) {
+        const int seg = jj >> 2, xx = jj & 3;
+        const int ih = (seg == 0) ? xx + 4 : ((seg == 1) ? 7 - xx : ((seg == 2) ? 3 - xx : xx));
+        const float hs1 = (seg == 0) ? 1.f : -1.f, hs2 = (seg == 3) ? -1.f : 1.f;
+        const float wh = k_hwin[jj < 8 ? jj : 15 - jj];
+        const float khc = hs1 * wh, khs = hs2 * wh;
+        const float A = fmaf(khs, t[1][ih], khc * t[0][ih]);
+        const float B = fmaf(khs, t[3][ih], khc * t[2][ih]);
+        const int gx = tx * 8 + jj - bx0 * 8;
+        if (act && gx >= 0 && gx < IPX) {
+          if (gy1 >= 0 && gy1 < IPX) acc[gy1 * ISTR + gx] += fmaf(ks1, B, kc1 * A);
+          if (gy2 >= 0 && gy2 < IPX) acc[gy2 * ISTR + gx] += fmaf(ks2, B, kc2 * A);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  float *dst = sc.rbg + (size_t)plane * fw * fh;
+  for (int i = threadIdx.x; i < IPX * IPX; i += blockDim.x) {
+    const int ly = i / IPX, lx = i - ly * IPX;
+    const int gx = bx0 * 8 + lx, gy = by0 * 8 + ly;
+    if (gx < fw && gy < fh) dst[(size_t)gy * fw + gx] = acc[ly * ISTR + lx];
+  }
+}
+
+cudaError_t launch_imclt_fast(const SceneDev &sc, cudaStream_t st) {
+  dim3 grid((sc.tilesX + 1 + IR - 1) / IR, (sc.tilesY + 1 + IR - 1) / IR, sc.num_sensors * sc.num_colors);
+  imclt_fast_kernel<<<grid, 256, 0, st>>>(sc);
+  return cudaGetLastError();
+}
+
 __global__ void disp_init_kernel(float *disp, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n * TP_NDISP) {

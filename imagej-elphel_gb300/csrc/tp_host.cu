@@ -644,7 +644,7 @@ tp_status tp_imclt(tp_handle *h, void *stream) {
       return fail(h, TP_ERR_NOMEM, "tp_imclt: frame buffer");
     }
   }
-  CK(launch_imclt(scene_of(h), st), "imclt");
+  CK(launch_imclt_fast(scene_of(h), st), "imclt");
   return TP_OK;
 }
 

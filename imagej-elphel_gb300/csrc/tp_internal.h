@@ -112,6 +112,7 @@ cudaError_t launch_convert_correct(const SceneDev &sc, cudaStream_t st);
 cudaError_t launch_correlate(const SceneDev &sc, cudaStream_t st);
 cudaError_t launch_extract(const SceneDev &sc, cudaStream_t st);
 cudaError_t launch_imclt(const SceneDev &sc, cudaStream_t st);
+cudaError_t launch_imclt_fast(const SceneDev &sc, cudaStream_t st);
 cudaError_t launch_compact_tasks(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
                                  int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
                                  cudaStream_t st);
