@@ -801,7 +801,9 @@ static FwdShape make_shape(const SceneDev &sc, int nw) {
   f.S = sc.num_sensors;
   f.C = sc.num_colors;
   f.P = sc.num_pairs;
-  f.RE = sc.strip_rows * 15;
+  // only the strip rows the extraction reads are built: getMaxXYInt uses row 0 and
+  // getMaxXCm clips the strip to the y-window (Correlation2d.java:944-951)
+  f.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
   f.quad = (sc.num_pairs <= 8) ? 1 : 0;
   f.nw = nw > 0 ? nw : (f.C == 3 ? 1 : 4);  // one-warp CTAs pack best when the tile CLT is large
   f.clt_floats = f.S * f.C * TP_CLT;

@@ -112,6 +112,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.corr_cfg = h->d_corr_cfg;
   sc.num_pairs = h->num_pairs;
   sc.strip_rows = h->corr_host.strip_rows;
+  sc.wndy_size = h->corr_host.wndy_size;
   return sc;
 }
 
@@ -320,7 +321,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && dalloc(&h->d_task_txy, nt) == cudaSuccess && dalloc(&h->d_task_op, nt) == cudaSuccess;
   ok = ok && dalloc(&h->d_task_disp, nt) == cudaSuccess && dalloc(&h->d_task_xy, nt * S * 2) == cudaSuccess;
   ok = ok && dalloc(&h->d_tile_op, nt) == cudaSuccess && dalloc(&h->d_tile_disp, nt) == cudaSuccess;
-  ok = ok && dalloc(&h->d_num_tasks, 1) == cudaSuccess;
+  ok = ok && dalloc(&h->d_num_tasks, 2 + nt / 1024 + 1) == cudaSuccess;  // count + per-block counts
   ok = ok && dalloc(&h->d_ports, nt * S * 2) == cudaSuccess;
   ok = ok && dalloc(&h->d_plan, nt * S * C) == cudaSuccess && dalloc(&h->d_tile_task, nt) == cudaSuccess;
   ok = ok && dalloc(&h->d_clt, nt * S * C * TP_CLT) == cudaSuccess;

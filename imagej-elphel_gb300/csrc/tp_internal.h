@@ -103,6 +103,7 @@ struct SceneDev {
   const CorrDev *corr_cfg;
   int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
   int strip_rows;            // host copy of corr_cfg->strip_rows
+  int wndy_size;             // host copy of corr_cfg->wndy_size
 };
 
 // launchers (tp_plan.cu / tp_kernels.cu)

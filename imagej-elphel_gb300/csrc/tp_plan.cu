@@ -96,53 +96,107 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
   }
 }
 
-// one thread per (task, sensor): ports, then the window plan of each colour
-__global__ void plan_kernel(SceneDev sc) {
-  int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  int S = sc.num_sensors, C = sc.num_colors;
-  int task = gid / S, s = gid - task * S;
-  if (task >= sc.num_tasks) return;
-  int txy = sc.task_txy[task];
-  int tx = txy & 0xffff, ty = txy >> 16;
-  double cx, cy;
-  if (sc.ports_from_geometry) {
-    double dv[8];
-    port_xy(*sc.geom, sc.rdist_tbl, (double)(tx * TP_DTT + TP_DTT / 2), (double)(ty * TP_DTT + TP_DTT / 2),
-            (double)sc.task_disp[task], s, cx, cy, sc.port_deriv ? dv : nullptr);
-    if (sc.port_deriv) {
-      double *o = sc.port_deriv + ((size_t)task * S + s) * 8;
+// undistorted tile centre, the sensor-independent head of getPortsCoordinatesAndDerivatives
+__device__ __forceinline__ void center_undistort(const GeomDev &g, const double *tbl, double px, double py,
+                                                 double &pXc, double &pYc) {
+  const double pXcd = DSUB(px, DMUL(0.5, (double)g.pixel_width));
+  const double pYcd = DSUB(py, DMUL(0.5, (double)g.pixel_height));
+  const double rD = DMUL(DMUL(DSQRT(DADD(DMUL(pXcd, pXcd), DMUL(pYcd, pYcd))), 0.001), g.pixel_size);
+  const double rND2R = r_by_rdist(tbl, g.tbl_len, DDIV(rD, g.distortion_radius));
+  pXc = DMUL(pXcd, rND2R);
+  pYc = DMUL(pYcd, rND2R);
+}
+
+// sensor part of getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2190-2217)
+__device__ __forceinline__ void sensor_port(const GeomDev &g, double pXc, double pYc, double disparity, int i,
+                                            double &ox, double &oy) {
+  const double fl_pix = DDIV(g.focal_length, DMUL(0.001, g.pixel_size));
+  const double ri_scale = DDIV(DMUL(0.001, g.pixel_size), g.distortion_radius);
+  const double vi[3] = {DSUB(pXc, DMUL(disparity, g.rXY[i][0])), DSUB(pYc, DMUL(disparity, g.rXY[i][1])), fl_pix};
+  double rvi[3];
+  mat3_vec(g.rots[i], vi, rvi);
+  const double norm_z = DDIV(fl_pix, rvi[2]);
+  const double pXci = DMUL(rvi[0], norm_z), pYci = DMUL(rvi[1], norm_z);
+  const double ri = DMUL(DSQRT(DADD(DMUL(pXci, pXci), DMUL(pYci, pYci))), ri_scale);
+  double rD2rND = 1.0, rri = 1.0;
 #pragma unroll
-      for (int k = 0; k < 8; k++) o[k] = dv[k];
-    }
-  } else {
-    cx = (double)sc.task_xy[((size_t)task * S + s) * 2];
-    cy = (double)sc.task_xy[((size_t)task * S + s) * 2 + 1];
+  for (int j = 0; j < 7; j++) {
+    rri = DMUL(rri, ri);
+    rD2rND = DADD(rD2rND, DMUL(g.rad_coeff[j], DSUB(rri, 1.0)));
   }
-  sc.ports[((size_t)task * S + s) * 2] = cx;
-  sc.ports[((size_t)task * S + s) * 2 + 1] = cy;
-  for (int c = 0; c < C; c++) {
-    double px = DSUB(cx, (double)TP_DTT), py = DSUB(cy, (double)TP_DTT);
-    int kidx = -1;
-    if (sc.kh > 0) {  // ImageDtt.java:4904-4932
-      int ktx = (int)java_round(DDIV(cx, (double)sc.kernel_step)) + 1;
-      int kty = (int)java_round(DDIV(cy, (double)sc.kernel_step)) + 1;
+  ox = DADD(DMUL(pXci, rD2rND), g.pXY0[i][0]);
+  oy = DADD(DMUL(pYci, rD2rND), g.pXY0[i][1]);
+}
+
+// One thread per task: the centre is undistorted once, the kernel tile is found
+// once per sensor (it depends on the port only), then each colour's window
+// corner and residual shift (ImageDtt.java:4904-4943).  A division by a
+// power-of-two kernel step is replaced by the multiplication with its exact
+// reciprocal, which IEEE rounding makes bit-identical.
+__global__ void plan_kernel(SceneDev sc) {
+  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  if (task >= sc.num_tasks) return;
+  const int S = sc.num_sensors, C = sc.num_colors;
+  const int txy = sc.task_txy[task];
+  const int tx = txy & 0xffff, ty = txy >> 16;
+  const double ctx = (double)(tx * TP_DTT + TP_DTT / 2), cty = (double)(ty * TP_DTT + TP_DTT / 2);
+  double pXc = 0.0, pYc = 0.0, disparity = 0.0;
+  if (sc.ports_from_geometry) {
+    center_undistort(*sc.geom, sc.rdist_tbl, ctx, cty, pXc, pYc);
+    disparity = (double)sc.task_disp[task];
+  }
+  const int ks = sc.kernel_step;
+  const bool pow2 = ks > 0 && (ks & (ks - 1)) == 0;
+  const double inv_ks = pow2 ? 1.0 / (double)ks : 0.0;
+  for (int s = 0; s < S; s++) {
+    double cx, cy;
+    if (sc.ports_from_geometry) {
+      if (sc.port_deriv) {
+        double dv[8];
+        port_xy(*sc.geom, sc.rdist_tbl, ctx, cty, disparity, s, cx, cy, dv);
+        double *o = sc.port_deriv + ((size_t)task * S + s) * 8;
+#pragma unroll
+        for (int k = 0; k < 8; k++) o[k] = dv[k];
+      } else {
+        sensor_port(*sc.geom, pXc, pYc, disparity, s, cx, cy);
+      }
+    } else {
+      cx = (double)sc.task_xy[((size_t)task * S + s) * 2];
+      cy = (double)sc.task_xy[((size_t)task * S + s) * 2 + 1];
+    }
+    sc.ports[((size_t)task * S + s) * 2] = cx;
+    sc.ports[((size_t)task * S + s) * 2 + 1] = cy;
+    int ktx = 0, kty = 0;
+    double kdx = 0.0, kdy = 0.0;
+    if (sc.kh > 0) {
+      const double qx = pow2 ? DMUL(cx, inv_ks) : DDIV(cx, (double)ks);
+      const double qy = pow2 ? DMUL(cy, inv_ks) : DDIV(cy, (double)ks);
+      ktx = (int)java_round(qx) + 1;
+      kty = (int)java_round(qy) + 1;
       kty = kty < 0 ? 0 : (kty >= sc.kv ? sc.kv - 1 : kty);
       ktx = ktx < 0 ? 0 : (ktx >= sc.kh ? sc.kh - 1 : ktx);
-      kidx = (kty * sc.kh + ktx) * C + c;
-      const float *ce = sc.kext[s] + (size_t)kidx * 8;
-      double kdx = DSUB(cx, DMUL(DADD((double)(ktx - 1), 0.5), (double)sc.kernel_step));
-      double kdy = DSUB(cy, DMUL(DADD((double)(kty - 1), 0.5), (double)sc.kernel_step));
-      px = DSUB(DSUB(cx, (double)TP_DTT), DADD(DADD((double)ce[0], DMUL((double)ce[4], kdx)), DMUL((double)ce[5], kdy)));
-      py = DSUB(DSUB(cy, (double)TP_DTT), DADD(DADD((double)ce[1], DMUL((double)ce[6], kdx)), DMUL((double)ce[7], kdy)));
+      kdx = DSUB(cx, DMUL(DADD((double)(ktx - 1), 0.5), (double)ks));
+      kdy = DSUB(cy, DMUL(DADD((double)(kty - 1), 0.5), (double)ks));
     }
-    double tl = -java_round(-px), tt = -java_round(-py);
-    SubtilePlan p;
-    p.tlx = (int)tl;
-    p.tly = (int)tt;
-    p.kidx = kidx;
-    p.rx = (float)(-(DSUB(px, tl)));
-    p.ry = (float)(-(DSUB(py, tt)));
-    sc.plan[((size_t)task * S + s) * C + c] = p;
+    for (int c = 0; c < C; c++) {
+      double px = DSUB(cx, (double)TP_DTT), py = DSUB(cy, (double)TP_DTT);
+      int kidx = -1;
+      if (sc.kh > 0) {
+        kidx = (kty * sc.kh + ktx) * C + c;
+        const float4 *ce4 = (const float4 *)(sc.kext[s] + (size_t)kidx * 8);
+        const float4 e0 = __ldg(ce4), e1 = __ldg(ce4 + 1);  // data_x, data_y, -, -, dxc_dx, dxc_dy, dyc_dx, dyc_dy
+        px = DSUB(DSUB(cx, (double)TP_DTT), DADD(DADD((double)e0.x, DMUL((double)e1.x, kdx)), DMUL((double)e1.y, kdy)));
+        py = DSUB(DSUB(cy, (double)TP_DTT), DADD(DADD((double)e0.y, DMUL((double)e1.z, kdx)), DMUL((double)e1.w, kdy)));
+      }
+      const double tl = -java_round(-px), tt = -java_round(-py);
+      SubtilePlan p;
+      p.tlx = (int)tl;
+      p.tly = (int)tt;
+      p.kidx = kidx;
+      p.rx = (float)(-(DSUB(px, tl)));
+      p.ry = (float)(-(DSUB(py, tt)));
+      sc.plan[((size_t)task * S + s) * C + c] = p;
+    }
   }
 }
 
@@ -198,9 +252,9 @@ __global__ void compact_tasks_kernel(const int *tile_op, const float *disparity,
 }
 
 cudaError_t launch_plan(const SceneDev &sc, cudaStream_t st) {
-  int n = sc.num_tasks * sc.num_sensors;
+  const int n = sc.num_tasks;
   if (n <= 0) return cudaSuccess;
-  plan_kernel<<<(n + 127) / 128, 128, 0, st>>>(sc);
+  plan_kernel<<<(n + 63) / 64, 64, 0, st>>>(sc);
   return cudaGetLastError();
 }
 
@@ -212,10 +266,70 @@ cudaError_t launch_tile_task_map(const SceneDev &sc, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// multi-block compaction: per-block counts, then each block adds the counts of
+// the blocks before it and scatters its tiles in row-major order
+constexpr int CB = 1024;
+__global__ void compact_count_kernel(const int *tile_op, int num_tiles, int *block_counts) {
+  const int i = blockIdx.x * CB + threadIdx.x;
+  const int n = __syncthreads_count(i < num_tiles && tile_op[i] != 0);
+  if (threadIdx.x == 0) block_counts[blockIdx.x] = n;
+}
+
+__global__ void compact_scatter_kernel(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                       const int *block_counts, int *task_txy, int *task_op, float *task_disp,
+                                       int *num_tasks) {
+  __shared__ int warp_sums[32];
+  __shared__ int base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    int b = 0;
+    for (int k = lane; k < blockIdx.x; k += 32) b += block_counts[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+    if (lane == 0) {
+      base = b;
+      if (blockIdx.x == gridDim.x - 1) *num_tasks = b + block_counts[blockIdx.x];
+    }
+  }
+  const int i = blockIdx.x * CB + threadIdx.x;
+  const int op = (i < num_tiles) ? tile_op[i] : 0;
+  const int flag = op != 0;
+  const unsigned m = __ballot_sync(0xffffffffu, flag);
+  const int pre = __popc(m & ((1u << lane) - 1u));
+  if (lane == 31) warp_sums[warp] = pre + flag;
+  __syncthreads();
+  if (warp == 0) {
+    const int v = warp_sums[lane];
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    warp_sums[lane] = incl - v;
+  }
+  __syncthreads();
+  if (flag) {
+    const int pos = base + warp_sums[warp] + pre;
+    const int ty = i / tilesX, tx = i - ty * tilesX;
+    task_txy[pos] = tx | (ty << 16);
+    task_op[pos] = op;
+    task_disp[pos] = disparity ? disparity[i] : 0.0f;
+  }
+}
+
 cudaError_t launch_compact_tasks(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
                                  int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
                                  cudaStream_t st) {
-  compact_tasks_kernel<<<1, 1024, 0, st>>>(tile_op, disparity, tilesX, num_tiles, task_txy, task_op, task_disp,
-                                           num_tasks_dev);
+  const int nb = (num_tiles + CB - 1) / CB;
+  if (nb <= 1) {
+    compact_tasks_kernel<<<1, 1024, 0, st>>>(tile_op, disparity, tilesX, num_tiles, task_txy, task_op, task_disp,
+                                             num_tasks_dev);
+    return cudaGetLastError();
+  }
+  int *counts = num_tasks_dev + 1;  // the caller sizes num_tasks_dev for 1 + nb ints
+  compact_count_kernel<<<nb, CB, 0, st>>>(tile_op, num_tiles, counts);
+  compact_scatter_kernel<<<nb, CB, 0, st>>>(tile_op, disparity, tilesX, num_tiles, counts, task_txy, task_op,
+                                            task_disp, num_tasks_dev);
   return cudaGetLastError();
 }
