@@ -3,8 +3,8 @@
 Workload (default): 4 Bayer sensors 2592x1936 uint16 (12-bit), per-sensor /
 per-colour CLT kernel tables on a 16-px grid (164x123), all 78,408 tiles:
 stage 1 ports (FP64) -> stage 2 convert+correct -> 6-pair correlation ->
-disparity extraction -> IMCLT colour frames.  One step = one pass over one
-scene.  Inputs are seeded synthetic scenes (no public dataset exists for this
+disparity extraction -> IMCLT colour frames -> RGBA texture tiles (with the
+port weights and rms rows).  One step = one pass over one scene.  Inputs are seeded synthetic scenes (no public dataset exists for this
 path); the per-step working set (~1.9 GB) exceeds the 129 MB L2, so no L2
 flush is needed between steps.
 
@@ -112,6 +112,9 @@ def algorithmic_bytes(w):
         "disparity": T * 8,
         "imclt": S * C * (W + 8) * (H + 8) * 4,
     }
+    tex = S == 4 and C == 3
+    if tex:
+        parts["textures"] = T * (12 * 1024 + 64)
     stage = {  # per-launch algorithmic bytes of each kernel
         "ports": T * 8 + T * S * 16 + T * S * C * (20 + 32),
         # fused: images + kernel tables + plan in, CLT + correlation surfaces + disparity out
@@ -119,6 +122,8 @@ def algorithmic_bytes(w):
         + parts["corr"] + T * 36,
         "imclt": parts["clt"] + parts["imclt"],
     }
+    if tex:  # CLT + task + disparity in, 12 texture rows + 16 aux floats out
+        stage["textures"] = parts["clt"] + T * 12 + parts["textures"]
     return sum(parts.values()), parts, stage
 
 
@@ -212,6 +217,10 @@ def cpu_baseline(w, sample_tiles, threads):
     r = O.run(w["W"], w["H"], planes, op, target, geometry=sc["geometry"], kernels=kern, kernel_ext=kx,
               pairs=pairs, num_threads=threads, want=("clt", "corr", "disp"))
     O.imclt_frames(r["clt"], w["W"] // 8, w["H"] // 8, present=op, num_threads=threads)
+    if w["S"] == 4 and w["C"] == 3:
+        tiles = np.nonzero(op)[0]
+        g = 1.0 / (1.0 + 0.5 + 0.2)
+        O.texture_tiles(r["clt"], tiles, 0xF, O.corr_lpf(0.8), (0.5 * g, 0.2 * g, g), num_threads=threads)
     dt = time.perf_counter() - t0
     return n / dt, n, dt
 
@@ -236,7 +245,8 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.config, "tiles_per_scene": w["T"], "sample_tiles_per_step": vals[0][1]},
             "cpu_baseline": {"value": value, "unit": "tiles/s", "cores": threads, "kind": "port",
-                             "sample": "%d of %d tiles per step, stages 1-4a" % (vals[0][1], w["T"])},
+                             "sample": "%d of %d tiles per step, stages 1-4%s" % (vals[0][1], w["T"],
+                                                                                  "b" if w["C"] == 3 else "a")},
             "e2e": {"value": value, "unit": "tiles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -270,12 +280,18 @@ def run_ours(args):
         tp.setColorScales([1.0, 1.0, 0.5])
     tp.setBayerImages(sc["images"])
     tp.setCorrelation(pairs=w["pairs"])
-    tp.setFullFrameImages(w["target"])
+    tile_op = np.full(T, 0xF, np.int32)  # all four ports (ImageDtt image mask), all tiles
+    tp.setFullFrameImages(w["target"], tile_op=tile_op)
     lib = tp._lib
     # ports: stage 1 (FP64) + window plan; forward: fused convert+correct / correlate / extract;
-    # imclt: inverse CLT into the colour frames
+    # imclt: inverse CLT into the colour frames; textures: RGBA texture tiles (quad colour only)
     stages = ["ports", "forward", "imclt"]
     fns = [lib.tp_ports, lib.tp_process, lib.tp_imclt]
+    with_tex = S == 4 and Cn == 3
+    if with_tex:
+        tp.setTextureParams()
+        stages.append("textures")
+        fns.append(lib.tp_textures)
 
     def step(evs=None):
         for i, f in enumerate(fns):
@@ -318,7 +334,7 @@ def run_ours(args):
 
     # ---- e2e through the public API with host buffers ----
     pin_imgs = [torch.from_numpy(np.ascontiguousarray(sc["images"][s])).pin_memory() for s in range(S)]
-    pin_op = torch.ones(T, dtype=torch.int32).pin_memory()
+    pin_op = torch.from_numpy(tile_op).pin_memory()
     pin_disp = torch.from_numpy(w["target"].copy()).pin_memory()
     out_disp = torch.empty((T, L.DISP_N), dtype=torch.float32).pin_memory()
     np_imgs = [p.numpy() for p in pin_imgs]
@@ -332,6 +348,8 @@ def run_ours(args):
         tp._ck(lib.tp_set_tile_ops(tp.h, C.c_void_p(np_op.ctypes.data), C.c_void_p(np_disp.ctypes.data)), "ops")
         tp._ck(lib.tp_process(tp.h, None), "process")
         tp._ck(lib.tp_imclt(tp.h, None), "imclt")
+        if with_tex:
+            tp._ck(lib.tp_textures(tp.h, None), "textures")
         tp._ck(lib.tp_get_disparity(tp.h, C.c_void_p(np_out.ctypes.data)), "disp")
 
     for _ in range(min(args.warmup, 3)):
@@ -356,15 +374,17 @@ def run_ours(args):
         sample = args.cpu_sample_tiles or (4000 if Cn == 3 else 2000)
         v, n, dt = cpu_baseline(w, sample, threads)
         cpu = {"value": v, "unit": "tiles/s", "cores": threads, "kind": "port",
-               "sample": "%d of %d tiles (every %d-th), stages 1-4a, FP64 C restatement" % (n, T, max(1, T // sample))}
-    launches_per_step = 5  # plan, tile map, disparity init, fused forward, imclt
+               "sample": "%d of %d tiles (every %d-th), stages 1-4%s, FP64 C restatement" % (
+                   n, T, max(1, T // sample), "b" if with_tex else "a")}
+    launches_per_step = 5 + int(with_tex)  # plan, tile map, disparity init, fused forward, imclt, textures
     line = {
         "metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.config, "tiles_per_scene": T, "sensors": S, "colors": Cn, "pairs": w["P"],
                    "kernels": "%dx%d" % (w["KH"], w["KV"]) if w["KH"] else "identity",
-                   "stages": "ports(fp64)+fused(convert_correct,correlate,extract)+imclt",
+                   "stages": "ports(fp64)+fused(convert_correct,correlate,extract)+imclt" + (
+                       "+textures(12 rows)" if with_tex else ""),
                    "l2": "per-step working set %.2f GB > 129 MB L2, no flush" % (total_b / 1e9),
                    "parallelism": "replicas" if world > 1 else "single"},
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},

@@ -38,6 +38,8 @@ struct tp_handle {
   GeomDev *d_geom = nullptr;
   double *d_rdist = nullptr;
   CorrDev *d_corr_cfg = nullptr;
+  float *d_tex = nullptr, *d_tex_aux = nullptr;
+  int tex_rows_alloc = 0, tex_rows = 0;  // allocated rows, rows of the last run
   // host state
   int num_tasks = 0;
   int ports_from_geometry = 0;
@@ -47,6 +49,7 @@ struct tp_handle {
   float color_scale[3] = {1.f, 1.f, 1.f};
   GeomDev geom_host;
   CorrDev corr_host;
+  tp_texture_params tex_params;
 };
 
 static tp_status fail(tp_handle *h, tp_status st, const std::string &msg) {
@@ -110,6 +113,8 @@ static SceneDev scene_of(tp_handle *h) {
   sc.rbg = h->d_rbg;
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
   sc.corr_cfg = h->d_corr_cfg;
+  sc.tex = h->d_tex;
+  sc.tex_aux = h->tex_params.aux ? h->d_tex_aux : nullptr;
   sc.num_pairs = h->num_pairs;
   sc.strip_rows = h->corr_host.strip_rows;
   sc.wndy_size = h->corr_host.wndy_size;
@@ -272,6 +277,19 @@ tp_status tp_default_corr_params(tp_corr_params *p) {
   return TP_OK;
 }
 
+tp_status tp_default_texture_params(tp_texture_params *p) {
+  if (!p) return TP_ERR_ARG;
+  p->min_shot = 10.0f;         // CLTParameters.min_shot
+  p->scale_shot = 3.0f;        // CLTParameters.scale_shot
+  p->diff_sigma = 5.0f;        // CLTParameters.diff_sigma
+  p->corr_magic_scale = 0.85f; // CLTParameters.corr_magic_scale
+  p->dust_remove = 1;
+  p->keep_weights = 1;
+  p->corr_mode = 2;
+  p->aux = 1;
+  return TP_OK;
+}
+
 tp_status tp_quad_pairs(tp_pair *pairs, int *n) {
   static const int c1[6] = {0, 2, 0, 1, 0, 2}, c2[6] = {1, 3, 2, 3, 3, 1}, kind[6] = {0, 0, 1, 1, 2, 3};
   static const float bx[6] = {1, 1, 0, 0, 1, 1}, by[6] = {0, 0, 1, 1, 1, -1};
@@ -311,6 +329,8 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
   ok = ok && upload_kernel_constants() == cudaSuccess;
   ok = ok && upload_fused_constants() == cudaSuccess;
+  ok = ok && upload_texture_constants() == cudaSuccess;
+  tp_default_texture_params(&h->tex_params);
   for (int s = 0; ok && s < S; s++) {
     ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
     if (ok && cfg->kernels_hor > 0) {
@@ -358,7 +378,8 @@ tp_status tp_destroy(tp_handle *h) {
   }
   void *bufs[] = {h->d_task_txy, h->d_task_op, h->d_task_disp, h->d_task_xy, h->d_tile_op, h->d_tile_disp,
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
-                  h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg};
+                  h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
+                  h->d_tex, h->d_tex_aux};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -649,6 +670,60 @@ tp_status tp_imclt(tp_handle *h, void *stream) {
   return TP_OK;
 }
 
+tp_status tp_set_texture_params(tp_handle *h, const tp_texture_params *p) {
+  if (!h || !p) return TP_ERR_ARG;
+  if (!(p->diff_sigma > 0.f) || !(p->corr_magic_scale > 0.f) || (p->scale_shot > 0.f && !(p->min_shot > 0.f)))
+    return fail(h, TP_ERR_ARG, "tp_set_texture_params: diff_sigma, corr_magic_scale and min_shot must be > 0");
+  if (p->corr_mode < -1 || p->corr_mode > 4)
+    return fail(h, TP_ERR_ARG, "tp_set_texture_params: corr_mode out of range");
+  h->tex_params = *p;
+  return TP_OK;
+}
+
+tp_status tp_textures(tp_handle *h, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  if (h->cfg.num_sensors != 4 || h->cfg.num_colors != 3)
+    return fail(h, TP_ERR_ARG, "tp_textures: texture tiles need 4 sensors x 3 colours");
+  if (!h->have_corr) return fail(h, TP_ERR_STATE, "tp_textures: correlation set-up (LPF, colour weights) missing");
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  if (r != TP_OK) return r;
+  const tp_texture_params &p = h->tex_params;
+  const int rows = p.keep_weights ? 12 : 4;
+  if (rows > h->tex_rows_alloc) {
+    cudaFree(h->d_tex);
+    h->d_tex = nullptr;
+    h->tex_rows_alloc = 0;
+    if (dalloc(&h->d_tex, (size_t)h->ntiles * rows * 256) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_textures: texture buffer");
+    }
+    h->tex_rows_alloc = rows;
+  }
+  if (p.aux && !h->d_tex_aux && dalloc(&h->d_tex_aux, (size_t)h->ntiles * 16) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, TP_ERR_NOMEM, "tp_textures: aux buffer");
+  }
+  TexConst tc;
+  memset(&tc, 0, sizeof(tc));
+  for (int i = 0; i < 64; i++) tc.lpf[i] = h->corr_host.lpf[i];
+  for (int i = 0; i < 3; i++) tc.col_weights[i] = h->corr_host.col_weights[i];
+  tc.min_shot = p.min_shot;
+  tc.scale_shot = p.scale_shot;
+  tc.rsqrt_min_shot = p.min_shot > 0.f ? (float)(1.0 / std::sqrt((double)p.min_shot)) : 0.f;
+  tc.diff_sigma = p.diff_sigma;
+  tc.corr_magic_scale = p.corr_magic_scale;
+  tc.dust_remove = p.dust_remove;
+  tc.rows = rows;
+  // corr_mode -> disparity slot (ImageDtt.java:2422-2426); POLY is not produced here
+  static const int slot[5] = {0, 1, -1, 3, 5};
+  tc.extra_index = (p.corr_mode >= 0) ? slot[p.corr_mode] : -1;
+  if (tc.extra_index >= 0 && h->num_pairs == 0) tc.extra_index = -1;
+  CK(launch_textures(scene_of(h), tc, st), "textures");
+  h->tex_rows = rows;
+  return TP_OK;
+}
+
 tp_status tp_process(tp_handle *h, void *stream) {
   if (!h) return TP_ERR_ARG;
   // the plan (ports, window corners) is recomputed only when geometry, kernels or tasks changed
@@ -738,6 +813,17 @@ tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg) {
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_get_rbg: bad camera");
   size_t plane = (size_t)(h->cfg.width + 8) * (h->cfg.height + 8) * h->cfg.num_colors;
   return d2h(h, rbg, h->d_rbg ? h->d_rbg + plane * cam : nullptr, plane * sizeof(float), "tp_get_rbg");
+}
+
+tp_status tp_get_textures(tp_handle *h, float *tex) {
+  if (!h) return TP_ERR_ARG;
+  const int rows = h->tex_rows;
+  return d2h(h, tex, rows ? h->d_tex : nullptr, (size_t)h->ntiles * rows * 256 * sizeof(float), "tp_get_textures");
+}
+
+tp_status tp_get_texture_aux(tp_handle *h, float *aux) {
+  if (!h) return TP_ERR_ARG;
+  return d2h(h, aux, h->d_tex_aux, (size_t)h->ntiles * 16 * sizeof(float), "tp_get_texture_aux");
 }
 
 }  // extern "C"

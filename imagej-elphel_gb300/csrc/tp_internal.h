@@ -101,9 +101,23 @@ struct SceneDev {
   float *rbg;                // [S][C][H+8][W+8]
   const float *lpf_rbg;      // [C][64] or null
   const CorrDev *corr_cfg;
+  float *tex;                // [tiles][rows][256] texture tiles (R, B, G, alpha[, 4 weights, 4 rms])
+  float *tex_aux;            // [tiles][16] max_diff[4], ports_rgb[12] or null
   int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
   int strip_rows;            // host copy of corr_cfg->strip_rows
   int wndy_size;             // host copy of corr_cfg->wndy_size
+};
+
+// texture-tile settings (CLTParameters defaults in tp_host.cu), read uniformly
+struct TexConst {
+  float lpf[64];            // correlation LPF (ImageDtt.java:1662-1690)
+  float col_weights[3];     // R, B, G
+  float min_shot, scale_shot, rsqrt_min_shot;
+  float diff_sigma;
+  float corr_magic_scale;
+  int dust_remove;
+  int rows;                 // 4 (RGBA) or 12 (keep_weights)
+  int extra_index;          // disparity slot for the extra shift, -1: none
 };
 
 // launchers (tp_plan.cu / tp_kernels.cu)
@@ -123,3 +137,6 @@ cudaError_t upload_kernel_constants();
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st);
 cudaError_t upload_fused_constants();
 int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);
+// texture tiles (tp_texture.cu)
+cudaError_t launch_textures(const SceneDev &sc, const TexConst &tc, cudaStream_t st);
+cudaError_t upload_texture_constants();

@@ -48,6 +48,12 @@ class TpCorrParams(C.Structure):
                 ("corr_wndx_blur", C.c_float)]
 
 
+class TpTextureParams(C.Structure):
+    _fields_ = [("min_shot", C.c_float), ("scale_shot", C.c_float), ("diff_sigma", C.c_float),
+                ("corr_magic_scale", C.c_float), ("dust_remove", C.c_int), ("keep_weights", C.c_int),
+                ("corr_mode", C.c_int), ("aux", C.c_int)]
+
+
 _H = C.c_void_p
 _vp = C.c_void_p
 
@@ -57,6 +63,7 @@ PROTOTYPES = {
     "tp_destroy": [_H],
     "tp_last_error": [_H, C.c_char_p, C.c_int],
     "tp_default_corr_params": [C.POINTER(TpCorrParams)],
+    "tp_default_texture_params": [C.POINTER(TpTextureParams)],
     "tp_quad_pairs": [C.POINTER(TpPair), C.POINTER(C.c_int)],
     "tp_set_geometry": [_H, C.POINTER(TpGeometry)],
     "tp_set_kernels": [_H, C.c_int, _vp, _vp, C.c_int],
@@ -66,11 +73,13 @@ PROTOTYPES = {
     "tp_set_tile_ops": [_H, _vp, _vp],
     "tp_set_lpf": [_H, _vp],
     "tp_set_corr": [_H, C.POINTER(TpCorrParams), C.POINTER(TpPair), C.c_int],
+    "tp_set_texture_params": [_H, C.POINTER(TpTextureParams)],
     "tp_ports": [_H, _vp],
     "tp_convert_correct": [_H, _vp],
     "tp_correlate": [_H, _vp],
     "tp_extract": [_H, _vp],
     "tp_imclt": [_H, _vp],
+    "tp_textures": [_H, _vp],
     "tp_process": [_H, _vp],
     "tp_set_schedule": [_H, C.c_int, C.c_int],
     "tp_synchronize": [_H],
@@ -82,6 +91,8 @@ PROTOTYPES = {
     "tp_get_corr": [_H, _vp],
     "tp_get_disparity": [_H, _vp],
     "tp_get_rbg": [_H, C.c_int, _vp],
+    "tp_get_textures": [_H, _vp],
+    "tp_get_texture_aux": [_H, _vp],
 }
 
 _lib = None

@@ -161,6 +161,16 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_set_corr(self.h, C.byref(params), arr, np_), "tp_set_corr")
         self.num_pairs = np_
 
+    def setTextureParams(self, params=None, **kw):
+        """Texture-tile settings: TpTextureParams or None (CLTParameters defaults), keyword overrides."""
+        if params is None:
+            params = L.TpTextureParams()
+            self._ck(self._lib.tp_default_texture_params(C.byref(params)), "tp_default_texture_params")
+        for k, v in kw.items():
+            setattr(params, k, v)
+        self._ck(self._lib.tp_set_texture_params(self.h, C.byref(params)), "tp_set_texture_params")
+        self._tex_rows = 12 if params.keep_weights else 4
+
     # ---- execution ----
     def execPorts(self, stream=None):
         self._ck(self._lib.tp_ports(self.h, stream), "tp_ports")
@@ -176,6 +186,10 @@ class GPUTileProcessor:
 
     def execImcltRbg(self, stream=None):
         self._ck(self._lib.tp_imclt(self.h, stream), "tp_imclt")
+
+    def execTextures(self, stream=None):
+        """Texture tiles (ImageDtt texture_tiles) of the current CLT and disparity."""
+        self._ck(self._lib.tp_textures(self.h, stream), "tp_textures")
 
     def process(self, stream=None):
         self._ck(self._lib.tp_process(self.h, stream), "tp_process")
@@ -224,6 +238,19 @@ class GPUTileProcessor:
     def getRBG(self, ncam):
         out = np.zeros((self.num_colors, self.height + 8, self.width + 8), dtype=np.float32)
         self._ck(self._lib.tp_get_rbg(self.h, int(ncam), _ptr(out)), "tp_get_rbg")
+        return out
+
+    def getTextures(self):
+        """[tilesY * tilesX][4 or 12][256]: R, B, G, alpha (+ 4 port weights, 4 rms)."""
+        rows = getattr(self, "_tex_rows", 12)
+        out = np.zeros((self.tilesY * self.tilesX, rows, 256), dtype=np.float32)
+        self._ck(self._lib.tp_get_textures(self.h, _ptr(out)), "tp_get_textures")
+        return out
+
+    def getTextureAux(self):
+        """[tilesY * tilesX][16]: max_diff[4], ports_rgb[12] (colour * 4 + port)."""
+        out = np.zeros((self.tilesY * self.tilesX, 16), dtype=np.float32)
+        self._ck(self._lib.tp_get_texture_aux(self.h, _ptr(out)), "tp_get_texture_aux")
         return out
 
     def setSchedule(self, tiles_per_block=0, warps_per_block=0):

@@ -117,6 +117,19 @@ typedef struct {
   int corr_wndx_size; float corr_wndx_hwidth, corr_wndx_blur;
 } tp_corr_params;
 
+/* texture tiles (CLTParameters fields read by ImageDtt.java:2662-2812) */
+typedef struct {
+  float min_shot;          /* 10.0: shot-noise correction below this is linear */
+  float scale_shot;        /* 3.0: scale after sqrt; <= 0 disables the correction */
+  float diff_sigma;        /* 5.0: pixel value difference sigma of the port weights */
+  float corr_magic_scale;  /* 0.85: extra shift = disparity x port offset / this */
+  int dust_remove;         /* 1 */
+  int keep_weights;        /* 1: 12 rows per tile (RGBA, 4 port weights, 4 rms), 0: 4 rows */
+  int corr_mode;           /* 2: disparity used for the extra shift: 0 INT, 1 CM, 3 HOR, 4 VERT;
+                              2 (POLY, not computed here) and -1 give no extra shift */
+  int aux;                 /* 1: also keep per tile max_diff[4] and ports_rgb[12] */
+} tp_texture_params;
+
 /* lifecycle: GPUTileProcessor() (GPUTileProcessor.java:243-360) */
 tp_status tp_create(const tp_config *cfg, tp_handle **out);
 tp_status tp_destroy(tp_handle *h);
@@ -124,6 +137,9 @@ tp_status tp_destroy(tp_handle *h);
 tp_status tp_last_error(const tp_handle *h, char *buf, int buf_len);
 /* fills the reference defaults (ImageDttParameters.java:30-112, fat_zero 0.05, corr_sigma 0.8) */
 tp_status tp_default_corr_params(tp_corr_params *p);
+/* CLTParameters defaults of the texture path (min_shot 10, scale_shot 3, diff_sigma 5,
+ * corr_magic_scale 0.85, dust_remove, keep_weights, corr_mode 2) */
+tp_status tp_default_texture_params(tp_texture_params *p);
 /* the 6 quad pairs Correlation2d.PAIRS[0..5]; returns the count in *n */
 tp_status tp_quad_pairs(tp_pair *pairs, int *n);
 
@@ -148,6 +164,8 @@ tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *target_
 tp_status tp_set_lpf(tp_handle *h, const float *lpf);
 /* correlation set-up (ImageDtt.clt_aberrations_quad_corr_new arguments, ImageDtt.java:1491-1546) */
 tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int num_pairs);
+/* texture set-up; the LPF and colour weights are those of tp_set_corr */
+tp_status tp_set_texture_params(tp_handle *h, const tp_texture_params *p);
 
 /* execution */
 /* stage 1 on the device when tile ops are set (getTileSubcamOffsets, GPUTileProcessor.java:686-778) */
@@ -160,6 +178,9 @@ tp_status tp_correlate(tp_handle *h, void *stream);
 tp_status tp_extract(tp_handle *h, void *stream);
 /* execImcltRbg (GPUTileProcessor.java:560-597): stage 4a */
 tp_status tp_imclt(tp_handle *h, void *stream);
+/* texture tiles of the current CLT and disparity (ImageDtt.java:2662-2812, tile_combine_rgba
+ * 2830-3000): 4 sensors x 3 colours only (TP_ERR_ARG otherwise) */
+tp_status tp_textures(tp_handle *h, void *stream);
 /* ports + convert_correct + correlate + extract in one call (ImageDtt.clt_aberrations_quad_corr) */
 tp_status tp_process(tp_handle *h, void *stream);
 /* schedule of the fused forward kernel: tiles per CTA and warps per CTA (0 = defaults);
@@ -178,6 +199,10 @@ tp_status tp_get_corr(tp_handle *h, float *corr);
 tp_status tp_get_disparity(tp_handle *h, float *disparity);
 /* getRBG (GPUTileProcessor.java:599-626): [num_colors][height+8][width+8] */
 tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg);
+/* texture_tiles[ty][tx]: [tilesY*tilesX][4 or 12][256] (R, B, G, alpha, weights, rms) */
+tp_status tp_get_textures(tp_handle *h, float *tex);
+/* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
+tp_status tp_get_texture_aux(tp_handle *h, float *aux);
 
 #ifdef __cplusplus
 }

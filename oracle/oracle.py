@@ -424,3 +424,59 @@ def imclt_frames(clt, tilesX, tilesY, scale=0.25, lpf=None, present=None, num_th
     L.or_imclt_frames(_d(clt), _i(pr) if pr is not None else None, tilesX, tilesY, S, Cn, float(scale),
                       _d(lp) if lp is not None else None, _d(out), int(num_threads or os.cpu_count() or 1), 0)
     return out
+
+
+class TexParams(C.Structure):
+    _fields_ = [("min_shot", C.c_double), ("scale_shot", C.c_double), ("diff_sigma", C.c_double),
+                ("diff_threshold", C.c_double), ("min_agree", C.c_double), ("dust_remove", C.c_int),
+                ("keep_weights", C.c_int), ("corr_magic_scale", C.c_double)]
+
+
+def texture_params(**kw):
+    """CLTParameters defaults of the texture path, with keyword overrides."""
+    p = TexParams(10.0, 3.0, 5.0, 1.5, 3.0, 1, 1, 0.85)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def texture_tile(clt, lpf, img_mask=0xf, col_weights=(0.25, 0.25, 0.5), extra_disparity=0.0, params=None):
+    """ImageDtt texture branch (2662-2812) for one tile: clt [4][3][4][64] ->
+    (rgba [12][256], aux [16] = max_diff[4], ports_rgb[12])."""
+    L = lib()
+    if not getattr(L, "_tex_set", False):
+        L.or_texture_tile.argtypes = [_dp, _dp, C.c_int, _dp, C.c_double, C.POINTER(TexParams), _dp, _dp]
+        L.or_texture_tile.restype = None
+        L._tex_set = True
+    c = _f64(clt).reshape(4, 3, 4, 64)
+    lp = _f64(lpf).reshape(64)
+    cw = _f64(col_weights).reshape(3)
+    out = np.zeros((12, 256))
+    aux = np.zeros(16)
+    L.or_texture_tile(_d(c), _d(lp), int(img_mask), _d(cw), float(extra_disparity),
+                      C.byref(params if params is not None else texture_params()), _d(out), _d(aux))
+    return out, aux
+
+
+def texture_tiles(clt, tiles, img_mask, lpf, col_weights=(0.25, 0.25, 0.5), extra=None, params=None,
+                  num_threads=None):
+    """texture_tile over `tiles` of clt [tiles][4][3][4][64] on a thread pool ->
+    (rgba [n][12][256], aux [n][16])."""
+    L = lib()
+    if not getattr(L, "_texs_set", False):
+        L.or_texture_tiles.argtypes = [_dp, _ip, _ip, _dp, C.c_int, _dp, _dp, C.POINTER(TexParams), _dp, _dp,
+                                       C.c_int]
+        L.or_texture_tiles.restype = C.c_int
+        L._texs_set = True
+    c = _f64(clt)
+    assert c.shape[1:3] == (4, 3)
+    t = np.ascontiguousarray(tiles, dtype=np.int32)
+    m = np.ascontiguousarray(np.broadcast_to(np.asarray(img_mask, dtype=np.int32), t.shape))
+    n = len(t)
+    ex = _f64(np.broadcast_to(np.asarray(extra, dtype=np.float64), t.shape)) if extra is not None else None
+    out = np.zeros((n, 12, 256))
+    aux = np.zeros((n, 16))
+    L.or_texture_tiles(_d(c), _i(t), _i(m), _d(ex) if ex is not None else None, n, _d(_f64(lpf).reshape(64)),
+                       _d(_f64(col_weights).reshape(3)), C.byref(params if params is not None else texture_params()),
+                       _d(out), _d(aux), int(num_threads or os.cpu_count() or 1))
+    return out, aux

@@ -975,6 +975,230 @@ void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty, dou
 }
 
 /* ------------------------------------------------------------------------- */
+/* Texture tiles (ImageDtt.java:2662-2812, 2830-3147)                          */
+/* ------------------------------------------------------------------------- */
+static const double KERN_G[9] = {0.0, 0.125, 0.0, 0.125, 0.5, 0.125, 0.0, 0.125, 0.0};        /* ImageDtt.java:43-46 */
+static const double KERN_RB[9] = {0.0625, 0.125, 0.0625, 0.125, 0.25, 0.125, 0.0625, 0.125, 0.0625}; /* 47-50 */
+static const int CORN_SIDE_N[9] = {4, 6, 4, 6, 9, 6, 4, 6, 4};
+static const int CORN_SIDE[9][9] = {                                                          /* 52-61 */
+    {4, 5, 7, 8}, {3, 4, 5, 6, 7, 8}, {3, 4, 6, 7}, {1, 2, 4, 5, 7, 8}, {0, 1, 2, 3, 4, 5, 6, 7, 8},
+    {0, 1, 3, 4, 6, 7}, {1, 2, 4, 5}, {0, 1, 2, 3, 4, 5}, {0, 1, 3, 4}};
+
+/* tile_debayer (3047-3147) for a 16x16 tile */
+static void tile_debayer(int rb, const double *tile, double *rslt) {
+  const int ts = 16, tsm1 = 15;
+  const int nb[9] = {-ts - 1, -ts, -ts + 1, -1, 0, 1, ts - 1, ts, ts + 1};
+  const double *kern = rb ? KERN_RB : KERN_G;
+  const double k_corn = rb ? (16.0 / 9.0) : (4.0 / 3.0), k_side = rb ? (4.0 / 3.0) : (8.0 / 7.0);
+  for (int i = 0; i < 256; i++) rslt[i] = 0.0;
+  for (int i = 0; i < ts; i++)
+    for (int j = 0; j < ts; j++) {
+      int rowt = (i == 0) ? 0 : ((i == tsm1) ? 2 : 1), colt = (j == 0) ? 0 : ((j == tsm1) ? 2 : 1);
+      int type = rowt * 3 + colt, indx = i * ts + j;
+      for (int k = 0; k < CORN_SIDE_N[type]; k++) {
+        int dr = CORN_SIDE[type][k];
+        rslt[indx] += tile[indx + nb[dr]] * kern[dr];
+      }
+      if (type != 4) rslt[indx] *= ((rowt != 1) && (colt != 1)) ? k_corn : k_side;
+    }
+}
+
+/* tile_debayer_shot_corr (3022-3045) */
+static void tile_debayer_shot_corr(int rb, const double *tile, const double *window2, double min_shot,
+                                   double scale_shot, double *out) {
+  double nw[256];
+  for (int i = 0; i < 256; i++) nw[i] = tile[i] / window2[i];
+  tile_debayer(rb, nw, out);
+  if (scale_shot > 0) {
+    double k = 1.0 / sqrt(min_shot);
+    for (int i = 0; i < 256; i++) out[i] = scale_shot * ((out[i] > min_shot) ? sqrt(out[i]) : (k * out[i]));
+  }
+  for (int i = 0; i < 256; i++) out[i] = out[i] * window2[i];
+}
+
+/* dust_remove (3002-3019), port weights [4][256] */
+static void dust_remove(double pw[4][256]) {
+  const int np = 4;
+  for (int i = 0; i < 256; i++) {
+    int wi = 0;
+    for (int ip = 1; ip < np; ip++) if (pw[ip][i] < pw[wi][i]) wi = ip;
+    double avg = 0;
+    for (int ip = 1; ip < np; ip++) if (ip != wi) avg += pw[ip][i];
+    avg /= (np - 1);
+    double scale = 1.0 + (avg - pw[wi][i]) / (avg * (np - 1));
+    for (int ip = 1; ip < np; ip++) if (ip != wi) pw[ip][i] *= scale;
+    pw[wi][i] *= pw[wi][i] / avg;
+  }
+}
+
+static const double PORT_OFFSETS[4][2] = {{-0.5, -0.5}, {0.5, -0.5}, {-0.5, 0.5}, {0.5, 0.5}};
+
+/* tile_combine_rgba (2830-3000), keep_weights layout; iclt [4][3][256], window = lt_window2 */
+static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, int port_mask, double diff_sigma,
+                              const double *chn_weights, int dust, double *rgba /* [12][256] */) {
+  const int ports = 4, numcol = 3;
+  int usedPorts = ((port_mask >> 0) & 1) + ((port_mask >> 1) & 1) + ((port_mask >> 2) & 1) + ((port_mask >> 3) & 1);
+  double pw[4][256], color_avg[3][256];
+  memset(pw, 0, sizeof(pw));
+  memset(color_avg, 0, sizeof(color_avg));
+  const int rms_start = numcol + 1 + ports;
+  for (int i = 0; i < 256; i++) {
+    double sw = 0.0;
+    for (int chn = 0; chn < numcol; chn++) {
+      double s0 = 0, s1 = 0, s2 = 0;
+      for (int ip = 0; ip < ports; ip++)
+        if (port_mask & (1 << ip)) {
+          s0 += 1;
+          s1 += iclt[ip][chn][i];
+          s2 += iclt[ip][chn][i] * iclt[ip][chn][i];
+        }
+      rgba[(rms_start + chn) * 256 + i] = sqrt(s0 * s2 - s1 * s1) / s0;
+      sw += chn_weights[chn] * rgba[(rms_start + chn) * 256 + i] * rgba[(rms_start + chn) * 256 + i];
+    }
+    rgba[(rms_start + numcol) * 256 + i] = sqrt(sw);
+  }
+  if (usedPorts > 1) {
+    double pair_dist2r[6];
+    int pp[6][2], np = 0;
+    double ksigma = 1.0 / (2.0 * diff_sigma * diff_sigma);
+    for (int i = 0; i < ports; i++)
+      if (port_mask & (1 << i))
+        for (int j = i + 1; j < ports; j++)
+          if (port_mask & (1 << j)) {
+            double dx = PORT_OFFSETS[j][0] - PORT_OFFSETS[i][0], dy = PORT_OFFSETS[j][1] - PORT_OFFSETS[i][1];
+            pp[np][0] = i; pp[np][1] = j;
+            pair_dist2r[np++] = ksigma / (dx * dx + dy * dy);
+          }
+    for (int i = 0; i < 256; i++) {
+      for (int ip = 0; ip < ports; ip++) pw[ip][i] = 0.0;
+      for (int ip = 0; ip < np; ip++) {
+        double d = 0;
+        for (int chn = 0; chn < numcol; chn++) {
+          double dc = iclt[pp[ip][0]][chn][i] - iclt[pp[ip][1]][chn][i];
+          dc /= lt_window[i];
+          d += chn_weights[chn] * dc * dc;
+        }
+        d = exp(-pair_dist2r[ip] * d);
+        pw[pp[ip][0]][i] += d;
+        pw[pp[ip][1]][i] += d;
+      }
+      int b1 = 0;
+      for (int ip = b1 + 1; ip < ports; ip++) if (pw[ip][i] > pw[b1][i]) b1 = ip;
+      int b2 = (b1 == 0) ? 1 : 0;
+      for (int ip = b2 + 1; ip < ports; ip++) if ((ip != b1) && (pw[ip][i] > pw[b2][i])) b2 = ip;
+      double w1 = pw[b1][i] / (pw[b1][i] + pw[b2][i]), w2 = 1.0 - w1;
+      for (int chn = 0; chn < numcol; chn++) color_avg[chn][i] = w1 * iclt[b1][chn][i] + w2 * iclt[b2][chn][i];
+      double d2[4];
+      for (int ip = 0; ip < ports; ip++)
+        if (port_mask & (1 << ip)) {
+          d2[ip] = 0;
+          for (int chn = 0; chn < numcol; chn++) {
+            double dc = iclt[ip][chn][i] - color_avg[chn][i];
+            dc /= lt_window[i];
+            d2[ip] += chn_weights[chn] * dc * dc;
+          }
+          pw[ip][i] = exp(-ksigma * d2[ip]);
+        }
+      double k = 0.0;
+      for (int ip = 0; ip < ports; ip++) k += pw[ip][i];
+      k = 1.0 / k;
+      for (int chn = 0; chn < numcol; chn++) {
+        color_avg[chn][i] = 0;
+        for (int ip = 0; ip < ports; ip++) color_avg[chn][i] += k * pw[ip][i] * iclt[ip][chn][i];
+      }
+    }
+  } else if (usedPorts > 0) {
+    for (int ip = 0; ip < ports; ip++)
+      if (port_mask & (1 << ip))
+        for (int i = 0; i < 256; i++) {
+          for (int chn = 0; chn < numcol; chn++) color_avg[chn][i] = iclt[ip][chn][i];
+          pw[ip][i] = 1.0;
+        }
+  }
+  if (dust && (usedPorts == 4)) dust_remove(pw);
+  for (int i = 0; i < 256; i++) {
+    double alpha = 0.0;
+    for (int ip = 0; ip < ports; ip++) if (port_mask & (1 << ip)) alpha += pw[ip][i];
+    alpha *= lt_window[i] / usedPorts;
+    rgba[3 * 256 + i] = alpha;
+  }
+  for (int chn = 0; chn < numcol; chn++) memcpy(rgba + chn * 256, color_avg[chn], sizeof(color_avg[chn]));
+  for (int ip = 0; ip < ports; ip++) memcpy(rgba + (numcol + 1 + ip) * 256, pw[ip], sizeof(pw[ip]));
+}
+
+void or_texture_tile(const double *clt_in, const double *filter, int img_mask, const double *col_weights,
+                     double extra_disparity, const or_tex_params *tp, double *out, double *aux) {
+  tables();
+  double lt_window[256], lt_window2[256];
+  or_win2d(lt_window);
+  for (int i = 0; i < 256; i++) lt_window2[i] = lt_window[i] * lt_window[i];
+  double(*ic)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
+  double(*db)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
+  double *clt = (double *)malloc(sizeof(double) * 4 * 3 * 256);
+  memcpy(clt, clt_in, sizeof(double) * 4 * 3 * 256);
+  if (extra_disparity != 0.0) /* 2663-2678 */
+    for (int chn = 0; chn < 3; chn++)
+      for (int i = 0; i < 4; i++)
+        or_fract_shift((double(*)[64])(clt + (i * 3 + chn) * 256),
+                       extra_disparity * PORT_OFFSETS[i][0] / tp->corr_magic_scale,
+                       extra_disparity * PORT_OFFSETS[i][1] / tp->corr_magic_scale);
+  const double scale = 0.25;
+  for (int i = 0; i < 4; i++)
+    for (int chn = 0; chn < 3; chn++) {
+      for (int dct_mode = 0; dct_mode < 4; dct_mode++) {
+        double t[64], tdct[64], mdct[256];
+        const double *src = clt + ((i * 3 + chn) * 4 + dct_mode) * 64;
+        for (int j = 0; j < 64; j++) t[j] = src[j] * (scale * filter[j]);
+        int idct_mode = ((dct_mode << 1) & 2) | ((dct_mode >> 1) & 1);
+        or_dttt_iv(t, tdct, idct_mode);
+        or_unfold_tile(tdct, dct_mode, mdct);
+        for (int j = 0; j < 256; j++) {
+          if (dct_mode == 0) ic[i][chn][j] = mdct[j];
+          else ic[i][chn][j] += mdct[j];
+        }
+      }
+      tile_debayer_shot_corr(chn != 2, ic[i][chn], lt_window2, tp->min_shot, tp->scale_shot, db[i][chn]);
+    }
+  tile_combine_rgba(db, lt_window2, img_mask, tp->diff_sigma, col_weights, tp->dust_remove, out);
+  if (aux) { /* max_diff (2964-2981) from the combined average, ports_rgb (2982-2994) */
+    for (int ip = 0; ip < 4; ip++) {
+      double md = 0;
+      if (img_mask & (1 << ip))
+        for (int i = 0; i < 256; i++) {
+          double d2 = 0.0;
+          for (int chn = 0; chn < 3; chn++) {
+            double dc = db[ip][chn][i] - out[chn * 256 + i];
+            d2 += dc * dc * col_weights[chn];
+          }
+          d2 *= lt_window2[i];
+          if (d2 > md) md = d2;
+        }
+      aux[ip] = sqrt(md);
+    }
+    for (int ip = 0; ip < 4; ip++)
+      for (int chn = 0; chn < 3; chn++) {
+        double s = 0;
+        for (int i = 0; i < 256; i++) s += db[ip][chn][i];
+        aux[4 + chn * 4 + ip] = s / 256;
+      }
+  }
+  /* RGB from the un-debayered tiles weighted by the port weights (ImageDtt.java:2788-2801) */
+  for (int i = 0; i < 256; i++) {
+    double sw = 0.0;
+    for (int ip = 0; ip < 4; ip++) sw += out[(3 + 1 + ip) * 256 + i];
+    if (sw != 0) sw = 1.0 / sw;
+    for (int chn = 0; chn < 3; chn++) {
+      double v = 0.0;
+      for (int ip = 0; ip < 4; ip++) v += sw * out[(3 + 1 + ip) * 256 + i] * ic[ip][chn][i];
+      out[chn * 256 + i] = v;
+    }
+  }
+  free(ic);
+  free(db);
+  free(clt);
+}
+
+/* ------------------------------------------------------------------------- */
 /* Kernel preparation (QuadCLT.calculateCLTKernel 433-667, ImageDtt 4625-4851) */
 /* ------------------------------------------------------------------------- */
 void or_calc_clt_kernel(const double *src, int normalize, double clt[4][64], double extra[8]) {
@@ -1327,5 +1551,45 @@ int or_imclt_frames(const double *clt, const int *present, int tilesX, int tiles
     for (int i = 0; i < nt; i++) pthread_create(&th[i], NULL, iclt_worker, &c);
     for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
   }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Texture tiles of many tiles on a thread pool (the reference's per-tile     */
+/* worker threads, ImageDtt.java:1750-2812)                                   */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  const double *clt, *filter, *col_weights, *extra;
+  const int *tiles, *img_mask;
+  int n;
+  const or_tex_params *tp;
+  double *out, *aux;
+  int next;
+} tex_ctx;
+
+static void *tex_worker(void *arg) {
+  tex_ctx *c = (tex_ctx *)arg;
+  for (int k = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED); k < c->n;
+       k = __atomic_fetch_add(&c->next, 1, __ATOMIC_RELAXED)) {
+    const int t = c->tiles[k];
+    or_texture_tile(c->clt + (size_t)t * 4 * 3 * 256, c->filter, c->img_mask[k], c->col_weights,
+                    c->extra ? c->extra[k] : 0.0, c->tp, c->out + (size_t)k * 12 * 256,
+                    c->aux ? c->aux + (size_t)k * 16 : NULL);
+  }
+  return NULL;
+}
+
+int or_texture_tiles(const double *clt, const int *tiles, const int *img_mask, const double *extra, int n,
+                     const double *filter, const double *col_weights, const or_tex_params *tp, double *out,
+                     double *aux, int num_threads) {
+  tables();
+  tex_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.clt = clt; c.filter = filter; c.col_weights = col_weights; c.extra = extra;
+  c.tiles = tiles; c.img_mask = img_mask; c.n = n; c.tp = tp; c.out = out; c.aux = aux;
+  int nt = num_threads > 0 ? (num_threads > 256 ? 256 : num_threads) : 1;
+  pthread_t th[256];
+  for (int i = 0; i < nt; i++) pthread_create(&th[i], NULL, tex_worker, &c);
+  for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
   return 0;
 }

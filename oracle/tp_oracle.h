@@ -19,7 +19,9 @@
  * stages are pinned by the restated source.  Stage 2 (convert/correct) and
  * IMCLT are additionally pinned against the reference's own CUDA kernels
  * (compiled from its sources by oracle/build_ref_gpu.py) through golden
- * fixtures under tests/golden/.
+ * fixtures under tests/golden/.  The texture-tile stage (or_texture_tile) has
+ * no reference kernel to run and no fixture: parity unpinned for that stage,
+ * which rests on the restated source alone.
  *
  * All arithmetic is double; compiled with -ffp-contract=off so that results
  * are identical on x86_64 and aarch64.
@@ -188,6 +190,31 @@ void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty,
  * present[tile] == 0 skips a tile */
 int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
                     const double *lpf, double *frames, int num_threads, int zero_frames);
+
+/* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
+typedef struct {
+  double min_shot, scale_shot;        /* CLTParameters 10.0, 3.0 */
+  double diff_sigma, diff_threshold;  /* 5.0, 1.5 */
+  double min_agree;                   /* 3.0 (not used by tile_combine_rgba) */
+  int dust_remove, keep_weights;      /* true, true */
+  double corr_magic_scale;            /* 0.85 */
+} or_tex_params;
+
+/*
+ * One tile of 4 quad sensors x 3 colours (R, B, G): clt [4][3][4][64], shifted
+ * by extra_disparity x port offset / corr_magic_scale first when non-zero;
+ * filter = correlation LPF [64].  out [12][256]: R, B, G, alpha, 4 port
+ * weights, 3 colour rms + weighted rms (the keep_weights layout of
+ * tile_combine_rgba, colour order RBG).  aux (optional) [16]: max_diff[4],
+ * ports_rgb[12] (chn * 4 + port).
+ */
+void or_texture_tile(const double *clt, const double *filter, int img_mask, const double *col_weights,
+                     double extra_disparity, const or_tex_params *tp, double *out, double *aux);
+/* or_texture_tile over tiles[n] of clt [tiles][4][3][256] on num_threads threads;
+ * out [n][12][256], aux [n][16] (or NULL), extra [n] (or NULL) */
+int or_texture_tiles(const double *clt, const int *tiles, const int *img_mask, const double *extra, int n,
+                     const double *filter, const double *col_weights, const or_tex_params *tp, double *out,
+                     double *aux, int num_threads);
 
 /* ---- kernel preparation (QuadCLT.java:433-667, ImageDtt.java:4625-4851) ---- */
 /* one 64x64 double-resolution kernel -> 4x64 CLT (CPU orientation) + 8 extras */

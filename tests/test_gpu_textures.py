@@ -1,0 +1,159 @@
+"""GPU texture tiles (ImageDtt.java:2662-2812) vs the FP64 oracle (needs a GB300).
+
+The oracle is fed the GPU's own CLT (so only the texture stage is compared) and,
+in the end-to-end case, its own CLT.  Tolerances: per tile and output row group,
+relative L2 <= 2e-5 for RGB and alpha, <= 1e-4 for the port weights (exp of a
+weighted squared difference divided by window^2), absolute <= 1e-3 x the tile's
+RGB scale for the rms rows (the oracle's s0*s2 - s1^2 loses digits the GPU's
+centred sum keeps); the best-pair choice may flip on exact near-ties, so 99.5%
+of tiles must meet the bounds and every tile must meet 10x them.  Pixels where
+the FP64 reference's weights underflow (0/0 -> NaN) must be NaN on the GPU too.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_gpu, rel_l2, run_oracle
+from tileproc import synth
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 2e-5
+W_TOL = 1e-4
+
+
+def _col_weights(corr_red=0.5, corr_blue=0.2):
+    g = 1.0 / (1.0 + corr_red + corr_blue)
+    return np.array([corr_red * g, corr_blue * g, g])
+
+
+def _oracle_textures(O, clt, disp, tile_op, tiles, extra_slot=None, params=None, **kw):
+    lpf = O.corr_lpf(0.8)
+    cw = _col_weights()
+    outs, auxs = [], []
+    for t in tiles:
+        op = int(tile_op[t])
+        extra = 0.0
+        if extra_slot is not None and not (op & 0x100):
+            extra = float(disp[t, extra_slot])
+            if not np.isfinite(extra):
+                extra = 0.0
+        o, a = O.texture_tile(clt[t], lpf, op & 0xF, cw, extra, params or O.texture_params(**kw))
+        outs.append(o)
+        auxs.append(a)
+    return np.array(outs), np.array(auxs)
+
+
+def _compare(got, aux, want, want_aux, frac=0.995):
+    n = len(got)
+    # NaN where the FP64 reference's weights underflow to 0/0 must be NaN on the GPU too
+    nan_g, nan_w = np.isnan(got[:, :8]), np.isnan(want[:, :8])
+    assert (nan_g != nan_w).mean() <= 1e-4, "NaN pattern differs at %d values" % (nan_g != nan_w).sum()
+    both = nan_g | nan_w
+    g8 = np.where(both, 0.0, got[:, :8])
+    w8 = np.where(both, 0.0, want[:, :8])
+    e_rgb = rel_l2(g8[:, 0:3].reshape(n, -1), w8[:, 0:3].reshape(n, -1), axis=-1)
+    e_a = rel_l2(g8[:, 3], w8[:, 3], axis=-1)
+    e_w = rel_l2(g8[:, 4:8].reshape(n, -1), w8[:, 4:8].reshape(n, -1), axis=-1)
+    scale = np.abs(w8[:, 0:3]).reshape(n, -1).max(axis=-1)
+    rms_d = np.where(np.isnan(want[:, 8:12]), 0.0, np.abs(got[:, 8:12] - want[:, 8:12]))
+    e_r = rms_d.reshape(n, -1).max(axis=-1) / np.maximum(scale, 1e-30)
+    good = (e_rgb <= RGB_TOL) & (e_a <= RGB_TOL) & (e_w <= W_TOL) & (e_r <= 1e-3)
+    msg = "rgb %.3g alpha %.3g weights %.3g rms %.3g (max), good %.4f, NaN values %d" % (
+        e_rgb.max(), e_a.max(), e_w.max(), e_r.max(), good.mean(), nan_w.sum())
+    assert good.mean() >= frac, msg
+    assert e_rgb.max() <= 10 * RGB_TOL and e_a.max() <= 10 * RGB_TOL and e_w.max() <= 10 * W_TOL, msg
+    # max_diff and ports_rgb
+    e_md = np.abs(aux[:, :4] - want_aux[:, :4]) / np.maximum(np.abs(want_aux[:, :4]).max(), 1e-30)
+    e_pr = np.abs(aux[:, 4:] - want_aux[:, 4:]) / np.maximum(np.abs(want_aux[:, 4:]).max(), 1e-30)
+    assert np.quantile(e_md, frac) <= 1e-4 and e_pr.max() <= 1e-5, "max_diff %.3g ports_rgb %.3g" % (
+        e_md.max(), e_pr.max())
+    return msg
+
+
+def _scene_ops(T, rng):
+    ops = np.full(T, 0xF, np.int32)
+    k = rng.integers(0, 10, T)
+    ops[k == 0] = 0x7
+    ops[k == 1] = 0x9
+    ops[k == 2] = 0x4
+    ops[k == 3] |= 0x100  # forced disparity: no extra shift
+    ops[rng.integers(0, 25, T) == 0] = 0  # no task
+    return ops
+
+
+def test_textures_on_gpu_clt(oracle):
+    """Texture stage alone: the oracle gets the GPU's CLT and centroid disparity (corr_mode 1)."""
+    sc = synth.make_scene("quad_bayer", seed=21, width=192, height=128)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    rng = np.random.default_rng(22)
+    ops = _scene_ops(T, rng)
+    disp = sc["disparity_gt"].reshape(-1).astype(np.float32) + rng.normal(0, 0.3, T).astype(np.float32)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(disp, tile_op=ops)
+        tp.process()
+        tp.setTextureParams(corr_mode=1)
+        tp.execTextures()
+        got = tp.getTextures().astype(np.float64)
+        aux = tp.getTextureAux().astype(np.float64)
+        clt = tp.getClt().astype(np.float64)
+        d = tp.getDisparity().astype(np.float64)
+    tiles = np.nonzero(ops)[0]
+    want, want_aux = _oracle_textures(oracle, clt, d, ops, tiles, extra_slot=oracle.DISP_CM)
+    print(_compare(got[tiles], aux[tiles], want, want_aux))
+
+
+def test_textures_end_to_end(oracle):
+    """Image -> CLT -> textures on the GPU vs the oracle's own chain (default corr_mode: no extra shift)."""
+    sc = synth.make_scene("quad_bayer", seed=23, width=128, height=96)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    ops = _scene_ops(T, np.random.default_rng(24))
+    disp = sc["disparity_gt"].reshape(-1).astype(np.float64)
+    ref = run_oracle(oracle, sc, disp, tile_op=ops)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(disp.astype(np.float32), tile_op=ops)
+        tp.process()
+        tp.setTextureParams()
+        tp.execTextures()
+        got = tp.getTextures().astype(np.float64)
+        aux = tp.getTextureAux().astype(np.float64)
+    tiles = np.nonzero(ops)[0]
+    want, want_aux = _oracle_textures(oracle, ref["clt"], ref["disp"], ops, tiles)
+    print(_compare(got[tiles], aux[tiles], want, want_aux))
+
+
+def test_textures_rgba_only_and_no_shot(oracle):
+    """keep_weights off (4 rows), shot-noise correction and dust removal off."""
+    sc = synth.make_scene("quad_bayer", seed=25, width=128, height=96)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    ops = np.full(T, 0xF, np.int32)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 3.0, np.float32), tile_op=ops)
+        tp.process()
+        tp.setTextureParams(keep_weights=0, scale_shot=0.0, dust_remove=0, aux=0)
+        tp.execTextures()
+        got = tp.getTextures().astype(np.float64)
+        clt = tp.getClt().astype(np.float64)
+        d = tp.getDisparity().astype(np.float64)
+    assert got.shape[1] == 4
+    tiles = np.arange(T)
+    want, _ = _oracle_textures(oracle, clt, d, ops, tiles, scale_shot=0.0, dust_remove=0)
+    bad = np.isnan(got[:, :4]) | np.isnan(want[:, :4])
+    assert (np.isnan(got[:, :4]) != np.isnan(want[:, :4])).mean() <= 1e-4
+    g, wv = np.where(bad, 0.0, got[:, :4]), np.where(bad, 0.0, want[:, :4])
+    e = rel_l2(g.reshape(T, -1), wv.reshape(T, -1), axis=-1)
+    assert np.mean(e <= RGB_TOL) >= 0.995 and e.max() <= 10 * RGB_TOL, "rgba rel L2 max %.3g" % e.max()
+
+
+def test_textures_reject_mono(oracle):
+    sc = synth.make_scene("quad_mono", seed=2, width=128, height=96)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full((sc["width"] // 8) * (sc["height"] // 8), 2.0, np.float32))
+        tp.process()
+        with pytest.raises(RuntimeError, match="4 sensors x 3 colours"):
+            tp.execTextures()

@@ -160,3 +160,60 @@ def test_fill_coord_corr_linear_field(oracle):
     oracle.fill_coord_corr(ext, 16)
     assert np.allclose(ext[..., 4], 0.3 / 16) and np.allclose(ext[..., 5], -0.1 / 16)
     assert np.allclose(ext[..., 6], 0.05 / 16) and np.allclose(ext[..., 7], 0.2 / 16)
+
+
+def _iclt_tile(oracle, clt4x64, lpf):
+    """Full 16x16 IMCLT of one sub-tile (x0.25 x LPF), the texture branch's per-port tile."""
+    out = np.zeros(256)
+    for m in range(4):
+        t = np.asarray(clt4x64[m]) * (0.25 * lpf)
+        idct = ((m << 1) & 2) | ((m >> 1) & 1)
+        out += oracle.unfold_tile(oracle.dttt_iv(t, idct), m)
+    return out
+
+
+def test_texture_identical_ports(oracle):
+    """Identical ports: every port weight 1, alpha = window^2, RGB = the port's IMCLT tile, rms 0."""
+    rng = np.random.default_rng(5)
+    one = rng.normal(size=(3, 4, 64)) * 40.0
+    clt = np.broadcast_to(one, (4, 3, 4, 64)).copy()
+    lpf = oracle.corr_lpf(0.8)
+    rgba, aux = oracle.texture_tile(clt, lpf)
+    w2 = oracle.win2d() ** 2
+    assert np.allclose(rgba[4:8], 1.0)
+    assert np.allclose(rgba[3], w2)
+    for c in range(3):
+        assert np.allclose(rgba[c], _iclt_tile(oracle, one[c], lpf), rtol=1e-12, atol=1e-9)
+    assert np.all(np.abs(rgba[8:12]) < 1e-6) or np.isnan(rgba[8:12]).any()
+    assert np.allclose(aux[:4], 0.0)
+
+
+def test_texture_single_port_and_forced(oracle):
+    """One used port: its weight is 1, the others 0, RGB = that port's tile (tile_combine_rgba 2942-2950)."""
+    rng = np.random.default_rng(6)
+    clt = rng.normal(size=(4, 3, 4, 64)) * 30.0
+    lpf = oracle.corr_lpf(0.8)
+    rgba, _ = oracle.texture_tile(clt, lpf, img_mask=0x4)
+    assert np.allclose(rgba[6], 1.0) and np.allclose(rgba[[4, 5, 7]], 0.0)
+    for c in range(3):
+        assert np.allclose(rgba[c], _iclt_tile(oracle, clt[2, c], lpf), rtol=1e-12, atol=1e-9)
+    # the extra shift moves every port by disparity x port offset / corr_magic_scale
+    shifted, _ = oracle.texture_tile(clt, lpf, img_mask=0x4, extra_disparity=0.85)
+    c2 = clt[2].copy()
+    for c in range(3):
+        c2[c] = oracle.fract_shift(c2[c], -0.5, 0.5)
+    for c in range(3):
+        assert np.allclose(shifted[c], _iclt_tile(oracle, c2[c], lpf), rtol=1e-12, atol=1e-9)
+
+
+def test_texture_outlier_port_is_suppressed(oracle):
+    """A port that disagrees with the other three gets a small weight; dust_remove keeps the sum."""
+    rng = np.random.default_rng(8)
+    one = rng.normal(size=(3, 4, 64)) * 40.0
+    clt = np.broadcast_to(one, (4, 3, 4, 64)).copy()
+    clt[1] += rng.normal(size=(3, 4, 64)) * 400.0
+    rgba, _ = oracle.texture_tile(clt, oracle.corr_lpf(0.8))
+    centre = np.zeros((16, 16), bool)
+    centre[4:12, 4:12] = True
+    w = rgba[4:8].reshape(4, 16, 16)[:, centre]
+    assert np.median(w[1]) < 0.2 and np.median(w[0]) > 0.9
