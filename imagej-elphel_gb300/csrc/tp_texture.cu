@@ -12,10 +12,12 @@
 // GB300 layout: one CTA of 128 threads per tile (grid-stride over the task
 // list).  The 12 (port, colour) inverse transforms run on 12 of the CTA's 16
 // 8-lane groups, lane r owning row r of each quadrant (the same register
-// butterflies as the forward kernel); the 16x16 results stay in shared memory
-// for the debayer (9-tap stencil per pixel) and the per-pixel combination
-// (two pixels per thread).  Per tile the kernel reads the 12 KB CLT once and
-// writes the 4 or 12 texture rows.
+// butterflies as the forward kernel).  Their unfold writes the tiles already
+// divided by window^2 (the debayer's input) into zero-bordered 18x18 shared
+// tiles, so the 3x3 stencil needs no edge tests.  Each thread then carries two
+// pixels through debayer, shot-noise correction, port weighting and the RGB
+// mix in registers; max_diff / ports_rgb take one block reduction.  Per tile
+// the kernel reads the 12 KB CLT once and writes the 4 or 12 texture rows.
 #include "tp_dtt.cuh"
 
 namespace {
@@ -27,6 +29,7 @@ constexpr float TX_EXP_UNDERFLOW = 745.13f;
 
 __device__ float d_tex_win2[256];   // lt_window2 = getWin2d()^2 (ImageDtt.java:2702, 697-713)
 __device__ float d_tex_rwin2[256];  // 1 / lt_window2
+__constant__ float k_rhwin[8];      // 1 / sine half-window
 
 // the four quad ports' offsets used to scale the extra shift and the pair
 // distances (ImageDtt.java:1564-1569)
@@ -39,7 +42,7 @@ __device__ __forceinline__ constexpr float kern_tap(bool rb, int dr) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_constant__ SceneDev sc,
+__global__ void __launch_bounds__(TX_THREADS, 5) texture_kernel(const __grid_constant__ SceneDev sc,
                                                              const __grid_constant__ TexConst tc) {
   // per-port IMCLT tiles [port * 3 + colour][18 x 18]: the 16x16 tile inside a zero border,
   // so the debayer stencil needs no edge tests (the border is never written)
@@ -61,7 +64,9 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
   const int i1 = (r >= 4) ? r - 4 : 11 - r, i2 = (r >= 4) ? 11 - r : r + 12;
   const float sa1 = (r >= 4) ? 1.f : -1.f, sb1 = 1.f;
   const float sa2 = -1.f, sb2 = (r >= 4) ? 1.f : -1.f;
-  const float w1 = k_hwin[i1 < 8 ? i1 : 15 - i1], w2 = k_hwin[i2 < 8 ? i2 : 15 - i2];
+  // the unfold writes the un-windowed tile (IMCLT / window^2, the debayer's input): the
+  // window factors of DttRad2.unfold_tile become their reciprocals
+  const float w1 = k_rhwin[i1 < 8 ? i1 : 15 - i1], w2 = k_rhwin[i2 < 8 ? i2 : 15 - i2];
   const float kc1 = sa1 * w1, ks1 = sb1 * w1, kc2 = sa2 * w2, ks2 = sb2 * w2;
   const float ksigma = 1.0f / (2.0f * tc.diff_sigma * tc.diff_sigma);
   __syncthreads();
@@ -128,7 +133,7 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
         const int seg = jj >> 2, xx = jj & 3;
         const int ih = (seg == 0) ? xx + 4 : ((seg == 1) ? 7 - xx : ((seg == 2) ? 3 - xx : xx));
         const float hs1 = (seg == 0) ? 1.f : -1.f, hs2 = (seg == 3) ? -1.f : 1.f;
-        const float wh = k_hwin[jj < 8 ? jj : 15 - jj];
+        const float wh = k_rhwin[jj < 8 ? jj : 15 - jj];
         const float khc = hs1 * wh, khs = hs2 * wh;
         const float A = fmaf(khs, t[1][ih], khc * t[0][ih]);
         const float B = fmaf(khs, t[3][ih], khc * t[2][ih]);
@@ -140,6 +145,7 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
     // ---------------- per pixel: debayer + shot noise, port weights, alpha, RGB ----------------
     float *out = sc.tex + tile * (size_t)tc.rows * 256;
     const int used = (mask & 1) + ((mask >> 1) & 1) + ((mask >> 2) & 1) + ((mask >> 3) & 1);
+    const float inv_used = 1.0f / used;  // inf for an empty mask: alpha is then 0 * inf = NaN as in double
     float part[16];  // this thread's max_diff[4] and ports_rgb[12] partials
 #pragma unroll
     for (int k = 0; k < 16; k++) part[k] = 0.f;
@@ -151,24 +157,24 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
       const bool ey = (y == 0) || (y == 15), ex = (x == 0) || (x == 15);
       const float f_rb = (ey && ex) ? (16.0f / 9.0f) : ((ey || ex) ? (4.0f / 3.0f) : 1.0f);
       const float f_g = (ey && ex) ? (4.0f / 3.0f) : ((ey || ex) ? (8.0f / 7.0f) : 1.0f);
-      float rw[9];  // 1 / window^2 of the neighbours (0 outside the tile)
-#pragma unroll
-      for (int dr = 0; dr < 9; dr++) rw[dr] = s_rwin2[p + (dr / 3 - 1) * TX_P + (dr % 3 - 1)];
-      const float lw = s_win2[i], rlw = s_rwin2[p];
+      const float lw = s_win2[i], rlw = s_rwin2[p], rlw2 = rlw * rlw;
       float d[4][3];
 #pragma unroll
       for (int ip = 0; ip < 4; ip++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const float *tl = s_ic[ip * 3 + c] + p;
-          float acc = 0.f;
-#pragma unroll
-          for (int dr = 0; dr < 9; dr++)
-            if (kern_tap(c != 2, dr) != 0.f)
-              acc = fmaf(tl[(dr / 3 - 1) * TX_P + (dr % 3 - 1)] * rw[dr], kern_tap(c != 2, dr), acc);
+          const float *u = s_ic[ip * 3 + c] + p;  // un-windowed tile, zero outside
+          const float sides = (u[-TX_P] + u[-1]) + (u[1] + u[TX_P]);
+          float acc;
+          if (c != 2) {  // kern_rb: corners 1/16, sides 1/8, centre 1/4
+            const float corners = (u[-TX_P - 1] + u[-TX_P + 1]) + (u[TX_P - 1] + u[TX_P + 1]);
+            acc = fmaf(0.0625f, corners, fmaf(0.125f, sides, 0.25f * u[0]));
+          } else {       // kern_g: sides 1/8, centre 1/2
+            acc = fmaf(0.125f, sides, 0.5f * u[0]);
+          }
           acc *= (c != 2) ? f_rb : f_g;
           if (tc.scale_shot > 0.f)  // tile_debayer_shot_corr (3022-3045)
-            acc = tc.scale_shot * ((acc > tc.min_shot) ? sqrtf(acc) : (tc.rsqrt_min_shot * acc));
+            acc = tc.scale_shot * ((acc > tc.min_shot) ? acc * rsqrtf(acc) : (tc.rsqrt_min_shot * acc));
           d[ip][c] = acc * lw;
           part[4 + c * 4 + ip] += d[ip][c];
         }
@@ -181,12 +187,12 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
           for (int ip = 0; ip < 4; ip++)
             if (mask & (1 << ip)) { s0 += 1.f; s1 += d[ip][c]; }
           // sqrt(s0*s2 - s1^2)/s0 evaluated as the centred sum (no cancellation)
-          const float m = s1 / s0;
+          const float m = __fdividef(s1, s0);
           float v = 0.f;
 #pragma unroll
           for (int ip = 0; ip < 4; ip++)
             if (mask & (1 << ip)) v = fmaf(d[ip][c] - m, d[ip][c] - m, v);
-          const float rms = sqrtf(v * s0) / s0;
+          const float rms = __fdividef(sqrtf(v * s0), s0);
           out[(8 + c) * 256 + i] = rms;
           sw = fmaf(tc.col_weights[c] * rms, rms, sw);
         }
@@ -207,15 +213,15 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
           for (int b = a + 1; b < 4; b++, k++) {
             ea[k] = CUDART_INF_F;
             if ((mask >> a) & (mask >> b) & 1) {
-              const float dx = k_port_off[b][0] - k_port_off[a][0], dy = k_port_off[b][1] - k_port_off[a][1];
-              const float pd = ksigma / (dx * dx + dy * dy);
+              // squared port distance: 1 for side pairs, 2 for the diagonals (0,3) and (1,2)
+              const float pd = (a + b == 3) ? 0.5f * ksigma : ksigma;
               float dd = 0.f;
 #pragma unroll
               for (int c = 0; c < 3; c++) {
-                const float dc = (d[a][c] - d[b][c]) * rlw;
+                const float dc = d[a][c] - d[b][c];
                 dd = fmaf(tc.col_weights[c] * dc, dc, dd);
               }
-              ea[k] = pd * dd;
+              ea[k] = pd * (dd * rlw2);
               amin = fminf(amin, ea[k]);
             }
           }
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
 #pragma unroll
             for (int b = a + 1; b < 4; b++, k++)
               if ((mask >> a) & (mask >> b) & 1) {
-                const float e = expf(amin - ea[k]);
+                const float e = __expf(amin - ea[k]);
                 pw[a] += e;
                 pw[b] += e;
               }
@@ -242,7 +248,7 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
           float p1 = 0.f, p2 = 0.f;  // register-resident selection of the two best ports
 #pragma unroll
           for (int ip = 0; ip < 4; ip++) { if (ip == b1) p1 = pw[ip]; if (ip == b2) p2 = pw[ip]; }
-          const float wa = p1 / (p1 + p2), wb = 1.0f - wa;
+          const float wa = __fdividef(p1, p1 + p2), wb = 1.0f - wa;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             float v1 = 0.f, v2 = 0.f;
@@ -257,18 +263,18 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
             float d2 = 0.f;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-              const float dc = (d[ip][c] - avg[c]) * rlw;
+              const float dc = d[ip][c] - avg[c];
               d2 = fmaf(tc.col_weights[c] * dc, dc, d2);
             }
-            eb[ip] = ksigma * d2;
+            eb[ip] = ksigma * (d2 * rlw2);
             if (mask & (1 << ip)) bmin = fminf(bmin, eb[ip]);
           }
           const bool zero = bmin > TX_EXP_UNDERFLOW;  // all weights 0 in double
 #pragma unroll
           for (int ip = 0; ip < 4; ip++)
-            if (mask & (1 << ip)) pw[ip] = zero ? 0.f : expf(bmin - eb[ip]);
+            if (mask & (1 << ip)) pw[ip] = zero ? 0.f : __expf(bmin - eb[ip]);
           sc_w = zero ? 1.f : expf(-bmin);
-          const float kk = 1.0f / (((pw[0] + pw[1]) + pw[2]) + pw[3]);
+          const float kk = __fdividef(1.0f, ((pw[0] + pw[1]) + pw[2]) + pw[3]);
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             float v = 0.f;
@@ -293,17 +299,17 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
         float a = 0.f, pwi = 0.f;
 #pragma unroll
         for (int ip = 0; ip < 4; ip++) { if (ip >= 1 && ip != wi) a += pw[ip]; if (ip == wi) pwi = pw[ip]; }
-        a /= 3.f;
-        const float scl = 1.0f + (a - pwi) / (a * 3.f);
+        a *= (1.0f / 3.0f);
+        const float scl = 1.0f + __fdividef(a - pwi, a * 3.f);
 #pragma unroll
         for (int ip = 1; ip < 4; ip++) if (ip != wi) pw[ip] *= scl;
 #pragma unroll
-        for (int ip = 0; ip < 4; ip++) if (ip == wi) pw[ip] *= pwi / a;
+        for (int ip = 0; ip < 4; ip++) if (ip == wi) pw[ip] *= __fdividef(pwi, a);
       }
       float alpha = 0.f;
 #pragma unroll
       for (int ip = 0; ip < 4; ip++) if (mask & (1 << ip)) alpha += pw[ip];
-      out[3 * 256 + i] = (alpha * sc_w) * (lw / used);
+      out[3 * 256 + i] = (alpha * sc_w) * (lw * inv_used);
       if (tc.rows > 4) {
 #pragma unroll
         for (int ip = 0; ip < 4; ip++) out[(4 + ip) * 256 + i] = pw[ip] * sc_w;
@@ -322,12 +328,13 @@ __global__ void __launch_bounds__(TX_THREADS, 6) texture_kernel(const __grid_con
         }
       // RGB mix of the un-debayered tiles (ImageDtt.java:2788-2801)
       float sw = ((pw[0] + pw[1]) + pw[2]) + pw[3];
-      if (sw != 0.f) sw = 1.0f / sw;
+      if (sw != 0.f) sw = __fdividef(1.0f, sw);
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         float v = 0.f;
 #pragma unroll
         for (int ip = 0; ip < 4; ip++) v += sw * pw[ip] * s_ic[ip * 3 + c][p];
+        v *= lw;  // the tiles are kept un-windowed
         out[c * 256 + i] = v;
       }
     }
@@ -370,7 +377,10 @@ cudaError_t upload_texture_constants() {
       w2[i * 16 + j] = (float)(w * w);
       rw2[i * 16 + j] = (float)(1.0 / (w * w));
     }
-  e = cudaMemcpyToSymbol(d_tex_win2, w2, sizeof(w2));
+  float rh[8];
+  for (int i = 0; i < 8; i++) rh[i] = (float)(1.0 / std::sin(3.14159265358979323846 / 16.0 * (i + 0.5)));
+  e = cudaMemcpyToSymbol(k_rhwin, rh, sizeof(rh));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(d_tex_win2, w2, sizeof(w2));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(d_tex_rwin2, rw2, sizeof(rw2));
   return e;
 }
