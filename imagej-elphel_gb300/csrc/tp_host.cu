@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -824,6 +825,42 @@ tp_status tp_get_textures(tp_handle *h, float *tex) {
 tp_status tp_get_texture_aux(tp_handle *h, float *aux) {
   if (!h) return TP_ERR_ARG;
   return d2h(h, aux, h->d_tex_aux, (size_t)h->ntiles * 16 * sizeof(float), "tp_get_texture_aux");
+}
+
+// Device address of the compaction scratch array, looked up once per device
+// (cudaGetSymbolAddress with that device current) and cached.
+static std::mutex g_scratch_mu;
+static int *g_scratch_ptr[TP_NOALLOC_MAX_DEVICES];
+
+tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                      int *task_txy, int *task_op, float *task_disp, int *num_tasks,
+                                      void *stream) {
+  if (!tile_op || !task_txy || !task_op || !task_disp || !num_tasks || tilesX <= 0 || tilesX > 65535 ||
+      num_tiles < 0 || num_tiles / tilesX > 32767)
+    return TP_ERR_ARG;
+  if (num_tiles > compact_scratch_max_tiles()) return TP_ERR_SCRATCH_LIMIT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TP_ERR_CUDA;
+  if (dev < 0 || dev >= TP_NOALLOC_MAX_DEVICES) return TP_ERR_ARG;
+  int *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      int *p = nullptr;
+      if (compact_scratch_address(&p) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return TP_ERR_CUDA;
+      }
+      g_scratch_ptr[dev] = p;
+    }
+    scratch = g_scratch_ptr[dev];
+  }
+  if (launch_compact_tasks_scratch(tile_op, disparity, tilesX, num_tiles, task_txy, task_op, task_disp, num_tasks,
+                                   scratch, (cudaStream_t)stream) != cudaSuccess) {
+    cudaGetLastError();
+    return TP_ERR_CUDA;
+  }
+  return TP_OK;
 }
 
 }  // extern "C"

@@ -137,6 +137,12 @@ cudaError_t upload_kernel_constants();
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st);
 cudaError_t upload_fused_constants();
 int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);
+// task compaction into a fixed device scratch array (tp_plan.cu), no allocation
+int compact_scratch_max_tiles();
+cudaError_t compact_scratch_address(int **ptr);
+cudaError_t launch_compact_tasks_scratch(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                         int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
+                                         int *scratch, cudaStream_t st);
 // texture tiles (tp_texture.cu)
 cudaError_t launch_textures(const SceneDev &sc, const TexConst &tc, cudaStream_t st);
 cudaError_t upload_texture_constants();

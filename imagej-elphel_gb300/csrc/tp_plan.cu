@@ -333,3 +333,35 @@ cudaError_t launch_compact_tasks(const int *tile_op, const float *disparity, int
                                             task_disp, num_tasks_dev);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Task compaction that allocates nothing: the per-block counts go to a fixed
+// file-scope device array instead of a handle's buffer.  Every count slot the
+// scatter reads is written earlier in the same call by compact_count_kernel,
+// so nothing has to start at zero; concurrent calls on one device share the
+// array and race.
+// ---------------------------------------------------------------------------
+constexpr int COMPACT_SCRATCH_BLOCKS = 1024;  // x CB tiles per block = 1,048,576 tiles
+static __device__ __align__(256) int g_compact_scratch[COMPACT_SCRATCH_BLOCKS];
+
+int compact_scratch_max_tiles() { return COMPACT_SCRATCH_BLOCKS * CB; }
+
+cudaError_t compact_scratch_address(int **ptr) {
+  return cudaGetSymbolAddress((void **)ptr, g_compact_scratch);
+}
+
+cudaError_t launch_compact_tasks_scratch(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                         int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
+                                         int *scratch, cudaStream_t st) {
+  const int nb = (num_tiles + CB - 1) / CB;
+  if (nb > COMPACT_SCRATCH_BLOCKS) return cudaErrorInvalidValue;
+  if (nb <= 1) {
+    compact_tasks_kernel<<<1, 1024, 0, st>>>(tile_op, disparity, tilesX, num_tiles, task_txy, task_op, task_disp,
+                                             num_tasks_dev);
+    return cudaGetLastError();
+  }
+  compact_count_kernel<<<nb, CB, 0, st>>>(tile_op, num_tiles, scratch);
+  compact_scatter_kernel<<<nb, CB, 0, st>>>(tile_op, disparity, tilesX, num_tiles, scratch, task_txy, task_op,
+                                            task_disp, num_tasks_dev);
+  return cudaGetLastError();
+}

@@ -12,7 +12,8 @@ LIB_PATH = os.path.join(PKG, "_build", "libtp.so")
 
 TP_MAX_SENSORS = 16
 TP_MAX_PAIRS = 120
-TP_OK, TP_ERR_ARG, TP_ERR_CUDA, TP_ERR_STATE, TP_ERR_NOMEM, TP_ERR_TIMEOUT, TP_ERR_NOT_BUILT = range(7)
+TP_OK, TP_ERR_ARG, TP_ERR_CUDA, TP_ERR_STATE, TP_ERR_NOMEM, TP_ERR_TIMEOUT, TP_ERR_NOT_BUILT, TP_ERR_SCRATCH_LIMIT = range(8)
+TP_COMPACT_MAX_TILES = 1024 * 1024
 TP_F32, TP_U16 = 0, 1
 TP_KERNELS_GPU, TP_KERNELS_CPU = 0, 1
 DISP_N = 9
@@ -93,6 +94,7 @@ PROTOTYPES = {
     "tp_get_rbg": [_H, C.c_int, _vp],
     "tp_get_textures": [_H, _vp],
     "tp_get_texture_aux": [_H, _vp],
+    "tp_compact_tile_ops_noalloc": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
 }
 
 _lib = None

@@ -49,7 +49,8 @@ typedef enum {
   TP_ERR_STATE = 3,    /* call order (e.g. no tasks set) */
   TP_ERR_NOMEM = 4,    /* device allocation failed */
   TP_ERR_TIMEOUT = 5,  /* a bounded device wait expired */
-  TP_ERR_NOT_BUILT = 6 /* the CUDA kernels are not available */
+  TP_ERR_NOT_BUILT = 6, /* the CUDA kernels are not available */
+  TP_ERR_SCRATCH_LIMIT = 7 /* request larger than the fixed scratch of a no-allocation entry point */
 } tp_status;
 
 typedef enum { TP_F32 = 0, TP_U16 = 1 } tp_dtype;
@@ -203,6 +204,28 @@ tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg);
 tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
 tp_status tp_get_texture_aux(tp_handle *h, float *aux);
+
+/* ---- no-allocation entry point ----
+ * Row-major compaction of tile_op[num_tiles] into the task list, the same
+ * result as tp_set_tile_ops (task_txy = tx | ty << 16, task_op, task_disp,
+ * *num_tasks), on caller-owned DEVICE buffers: tile_op, disparity (may be
+ * NULL: task_disp = 0), task_txy/task_op/task_disp (num_tiles entries each)
+ * and num_tasks (one int).  No reference counterpart: the reference packs its
+ * task list on the host (GPUTileProcessor.setTasks, GPUTileProcessor.java:
+ * 686-778).  It allocates nothing -- no cudaMalloc/cudaFree and no allocating
+ * library; its per-block counts live in a fixed device array of
+ * TP_COMPACT_MAX_TILES / 1024 ints inside libtp.  num_tiles above
+ * TP_COMPACT_MAX_TILES returns TP_ERR_SCRATCH_LIMIT.  The first call on a
+ * device looks the array's address up (cudaGetSymbolAddress) and caches it;
+ * make that first call before any stream capture.  Calls on one device share
+ * the array: calls that overlap in time (different streams or threads) race;
+ * serialise them.  Runs on the current device and `stream` (NULL = the default
+ * stream), asynchronously. */
+#define TP_COMPACT_MAX_TILES (1024 * 1024)
+#define TP_NOALLOC_MAX_DEVICES 64
+tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
+                                      int *task_txy, int *task_op, float *task_disp, int *num_tasks,
+                                      void *stream);
 
 #ifdef __cplusplus
 }
