@@ -1,0 +1,602 @@
+// tp_adjoint.cu -- hand-written adjoint of the forward chain for mono sensors.
+//
+// For every tile the centroid disparity d (getMaxXCm over the combined strip,
+// Correlation2d.java:936-1032) is a function of the residual shifts (rx, ry)
+// of each sensor's window (ImageDtt.java:4940-4943), which follow the port
+// coordinates, which follow the per-sensor extrinsics and the tile's target
+// disparity (GeometryCorrection.getPortsCoordinatesAndDerivatives,
+// GeometryCorrection.java:2159-2314).  The adjoint kernel computes, per tile,
+// d and dd/d(port x, port y) of every sensor by reverse mode through
+//   centroid -> strip combination (geometric mean) -> strip sampling ->
+//   15x15 unfold -> 2D DCT-IIe/DST-IIe -> LPF -> fat-zero normalised product
+// (Correlation2d.java:197-231, 556-790; DttRad2.java:443-489, 595-614) down to
+// dd/dCLT of each sensor, then by forward mode through the CLT's dependence
+// on the residual shift: the phase rotation (fract_shift, ImageDtt.java:
+// 5490-5584) differentiated analytically, and the shifted fold window
+// (DttRad2.get_shifted_fold_2d, 263-314) differentiated through its cos/sin
+// mix.  The integer window corners and the integer argmax are piecewise
+// constant and are held fixed.
+//
+// A second kernel contracts those port sensitivities with the FP64 port
+// derivatives of the plan (azimuth, tilt, roll, zoom, disparity) into the
+// per-tile Jacobian rows and the gradient of a per-tile loss.
+//
+// GB300 layout: warp per tile as in the forward kernel.  Per warp the tile's
+// CLT [S][256] (read back from HBM or recomputed from the image), its
+// gradient [S][256], and small surface / quadrant buffers live in shared
+// memory; pairs are processed in order by the one warp, so the gradient
+// accumulates without atomics.
+#include "tp_dtt.cuh"
+
+namespace {
+
+__constant__ float k_t2e[2][64];  // DCT-IIe / DST-IIe as matrices, y = T x (T[k][n] at k * 8 + n)
+
+constexpr float K16 = 0.19634954084936207f;  // pi / 16
+
+struct AdjShape {
+  int S, P, RE;
+  int per_warp;   // floats of shared memory per warp
+  int recompute;  // 1: recompute the CLT from the image instead of reading it back
+};
+
+__device__ __forceinline__ void convolve(float o[4][8], const float *kp, int r) {
+  if (!kp) return;
+  float k[4][8];
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    const float4 *p = (const float4 *)(kp + m * 64 + r * 8);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    k[m][0] = a.x; k[m][1] = a.y; k[m][2] = a.z; k[m][3] = a.w;
+    k[m][4] = b.x; k[m][5] = b.y; k[m][6] = b.z; k[m][7] = b.w;
+  }
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float d0 = o[0][v], d1 = o[1][v], d2 = o[2][v], d3 = o[3][v];
+    const float k0 = k[0][v], k1 = k[1][v], k2 = k[2][v], k3 = k[3][v];
+    o[0][v] = d0 * k0 - d1 * k1 - d2 * k2 + d3 * k3;
+    o[1][v] = d1 * k0 + d0 * k1 - d3 * k2 - d2 * k3;
+    o[2][v] = d2 * k0 - d3 * k1 + d0 * k2 - d1 * k3;
+    o[3][v] = d3 * k0 + d2 * k1 + d1 * k2 + d0 * k3;
+  }
+}
+
+// the phase rotation of fract_shift (same angles as the forward kernel)
+__device__ __forceinline__ void rotate(float o[4][8], float rx, float ry, int r) {
+  float ch, shh, cvr, svr;
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * rx, &shh, &ch);
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * ry, &svr, &cvr);
+  const int base = threadIdx.x & 24;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float cv = __shfl_sync(0xffffffffu, cvr, base + v), sv = __shfl_sync(0xffffffffu, svr, base + v);
+    const float t0 = o[0][v] * ch - o[1][v] * shh, t1 = o[1][v] * ch + o[0][v] * shh;
+    const float t2 = o[2][v] * ch - o[3][v] * shh, t3 = o[3][v] * ch + o[2][v] * shh;
+    o[0][v] = t0 * cv - t2 * sv;
+    o[2][v] = t2 * cv + t0 * sv;
+    o[1][v] = t1 * cv - t3 * sv;
+    o[3][v] = t3 * cv + t1 * sv;
+  }
+}
+
+__device__ __forceinline__ Win make_win(const SceneDev &sc, const SubtilePlan &p, int s) {
+  Win w;
+  w.img = sc.images[s];
+  w.pitch = sc.img_pitch;
+  w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
+  w.u16 = sc.img_dtype[s];
+  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
+  w.scale = sc.color_scale[0];
+  return w;
+}
+
+// taps of one strip sample (sample_code / strip_sample): returns the tap count
+__device__ __forceinline__ int code_taps(int code, int idx[4], float wt[4]) {
+  if (code < 0) return 0;
+  const int i = code & 255, cs = code >> 8;
+  idx[0] = i;
+  if (cs == 0) { wt[0] = 1.f; return 1; }
+  if (cs == 1) { wt[0] = 0.5f; idx[1] = i + 1; wt[1] = 0.5f; return 2; }
+  if (cs == 2) { wt[0] = 0.5f; idx[1] = i + 15; wt[1] = 0.5f; return 2; }
+  idx[1] = i + 1; idx[2] = i + 15; idx[3] = i + 16;
+  wt[0] = wt[1] = wt[2] = wt[3] = 0.25f;
+  return 4;
+}
+__device__ __forceinline__ int general_taps(float bx, float by, int row, int scol, int down, int idx[4],
+                                            float wt[4]) {
+  const float a = scol + 0.5f * (row & 1), pp = 0.5f * down * row;
+  const float x = a * bx - pp * by, y = a * by + pp * bx;
+  if (x > 7.f || x < -7.f || y > 7.f || y < -7.f) return 0;
+  const float fx = x + 7.f, fy = y + 7.f;
+  const int ix0 = min((int)floorf(fx), 13), iy0 = min((int)floorf(fy), 13);
+  const float dx = fx - ix0, dy = fy - iy0;
+  idx[0] = iy0 * 15 + ix0; wt[0] = (1.0f - dx) * (1.0f - dy);
+  idx[1] = idx[0] + 1;     wt[1] = dx * (1.0f - dy);
+  idx[2] = idx[0] + 15;    wt[2] = (1.0f - dx) * dy;
+  idx[3] = idx[0] + 16;    wt[3] = dx * dy;
+  return 4;
+}
+
+// one strip entry of a pair exactly as the forward kernel computes it
+__device__ __forceinline__ float strip_entry(const float *c, const short *strip_code, const PairDev &pd, int e) {
+  const int row = e / 15;
+  float d;
+  if (pd.kind <= 3) {
+    const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+    d = sample_code(c, code.x);
+    if (row > 0) {
+      const float d2 = sample_code(c, code.y);
+      d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+    }
+  } else {
+    const int scol = e - row * 15 - 7;
+    d = strip_sample(c, 4, pd.bx, pd.by, row, scol, -1);
+    if (row > 0) {
+      const float d2 = strip_sample(c, 4, pd.bx, pd.by, row, scol, 1);
+      d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+    }
+  }
+  return d;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ SceneDev sc,
+                                                     const __grid_constant__ AdjShape as,
+                                                     const __grid_constant__ CorrConst cfg, float *sens,
+                                                     float *dval) {
+  extern __shared__ float sm[];
+  const int lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
+  const int S = as.S, P = as.P, RE = as.RE;
+  float *s_clt = sm;                  // [S][256]
+  float *s_g = s_clt + S * TP_CLT;    // [S][256] dd/dCLT
+  float *gs = s_g + S * TP_CLT;       // [240] dd/dsurface of the current pair
+  float *qb = gs + 240;               // [4][72] quadrant buffer
+  float *tb = qb + 288;               // [4][72] transpose buffer
+  float *gcmb = tb + 288;             // [240] dd/dcombo
+  float *gG = gcmb + 240;             // [240] combo + offset
+  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+  const int groups = (S + 3) >> 2;
+  const bool log_mode = cfg.log_combine;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  const float inv_n = 1.0f / cfg.num_combo;
+
+  for (int task = blockIdx.x; task < sc.num_tasks; task += gridDim.x) {
+    const int txy = sc.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+    // ---------------- the tile's CLT ----------------
+    if (as.recompute) {
+      for (int g = 0; g < groups; g++) {
+        const int s = g * 4 + q;
+        const int sidx = s < S ? s : S - 1;
+        const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
+        const Win w = make_win(sc, p, sidx);
+        float ahs, ahc, avs, avc;
+        __sincosf(CUDART_PI_F * 0.0625f * p.rx, &ahs, &ahc);
+        __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
+        const FoldIdx fv = fold_idx(r);
+        float vw0, vw1, hw0[8], hw1[8], o[4][8];
+        fold_weights(ahc, ahs, avc, avs, fv, vw0, vw1, hw0, hw1);
+        fold_dtt_dense(w, fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
+        convolve(o, (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr, r);
+        rotate(o, p.rx, p.ry, r);
+        if (s < S) {
+#pragma unroll
+          for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int v = 0; v < 8; v++) s_clt[s * TP_CLT + m * 64 + r * 8 + v] = o[m][v];
+        }
+      }
+    } else {
+      const float4 *src = (const float4 *)(sc.clt + tile * S * TP_CLT);
+      for (int i = lane; i < S * 64; i += 32) ((float4 *)s_clt)[i] = __ldg(src + i);
+    }
+    for (int i = lane; i < S * TP_CLT; i += 32) s_g[i] = 0.f;
+    __syncwarp();
+
+    // ---------------- forward strips, combination and centroid ----------------
+    float cmb[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    for (int pi = 0; pi < P; pi++) {
+      const PairDev pd = cfg.pairs[pi];
+      if (!pd.in_combo) continue;
+      const float *c = sc.corr + (tile * P + pi) * TP_CORR;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int e = lane + 32 * t;
+        if (e < RE) {
+          float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
+          if (v < 0.0f) v = 0.0f;
+          if (log_mode) cmb[t] += logf(v);
+          else cmb[t] *= cfg.twice_diagonal ? v * v : v;
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int e = lane + 32 * t;
+      if (e < RE) {
+        float v = cmb[t];
+        if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
+        else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
+        gG[e] = v;
+        gcmb[e] = 0.f;
+      }
+    }
+    __syncwarp();
+    float dres = CUDART_NAN_F;
+    {
+      const float v = (lane < 15) ? gG[lane] : CUDART_NAN_F;
+      float best = isnan(v) ? -CUDART_INF_F : v;
+      int bi = lane < 15 ? lane : 99;
+#pragma unroll
+      for (int o2 = 16; o2 > 0; o2 >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      const unsigned finite = __ballot_sync(0xffffffffu, lane < 15 && !isnan(v));
+      const int imx = finite ? bi : 14;
+      const float vmax = gG[imx];
+      if (vmax >= cfg.min_corr) {
+        const int ix = imx - 7;
+        int dh = cfg.strip_rows;
+        float wys = 1.0f;
+        if (dh > cfg.wndy_size) dh = cfg.wndy_size;
+        else if (dh < cfg.wndy_size) {
+          float swy = cfg.wndy[0];
+          for (int i = 1; i < dh; i++) swy += cfg.wndy[i];
+          wys = 1.0f / swy;
+        }
+        const int x0 = 7 + ix, nk = dh * 2 * cfg.wndx_size;
+        float s0 = 0.f, sx = 0.f;
+        for (int pass = 0; pass < 2; pass++) {
+          const float xm = (pass == 1) ? sx / s0 : 0.f;
+          for (int k = lane; k < nk; k += 32) {
+            const int dy = k / (2 * cfg.wndx_size), rest = k - dy * 2 * cfg.wndx_size;
+            const int adx = rest >> 1, dir = (rest & 1) ? 1 : -1, odd = dy & 1;
+            if (((adx - odd) & 1) || (adx == 0 && dir < 0)) continue;
+            const int idx = (adx * dir) >> 1, xx = 2 * idx + odd, x1 = x0 + idx;
+            if (x1 < 0 || x1 >= 15) continue;
+            const float d = gG[dy * 15 + x1];
+            if (isnan(d) || !(d > 0.0f)) continue;
+            const float wk = (((dy == 0) ? wys : 2.0f * wys) * cfg.wndy[dy]) * cfg.wndx[adx];
+            if (pass == 0) {
+              s0 += d * wk;
+              sx += d * wk * xx;
+            } else {
+              // d(-(ix + sx/s0/2)) / d(combo): -(wk / (2 s0)) (xx - sx/s0)
+              gcmb[dy * 15 + x1] = -(wk / (2.0f * s0)) * (xx - xm);
+            }
+          }
+          if (pass == 0) {
+            s0 = warp_sum(s0);
+            sx = warp_sum(sx);
+            if (s0 == 0.0f) break;
+            dres = -(ix + sx / s0 / 2);
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (isnan(dres)) {
+      if (lane == 0) dval[tile] = CUDART_NAN_F;
+      for (int i = lane; i < 2 * S; i += 32) sens[tile * 2 * S + i] = 0.f;
+      continue;
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++) {  // G = combo + offset, the geometric mean the strip entries enter
+      const int e = lane + 32 * t;
+      if (e < RE) gG[e] = gG[e] + cfg.corr_offset;
+    }
+    __syncwarp();
+
+    // ---------------- reverse pass over the pairs ----------------
+    for (int pi = 0; pi < P; pi++) {
+      const PairDev pd = cfg.pairs[pi];
+      if (!pd.in_combo) continue;
+      const float *c = sc.corr + (tile * P + pi) * TP_CORR;
+      for (int i = lane; i < 240; i += 32) gs[i] = 0.f;
+      for (int i = lane; i < 288; i += 32) qb[i] = 0.f;
+      __syncwarp();
+      // strip entries: d combo / d v_p = G / (n v_p) for the geometric mean of n pairs
+      bool any = false;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int e = lane + 32 * t;
+        if (e < RE && gcmb[e] != 0.f) {
+          const float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
+          if (v > 0.0f) {
+            const float f = gcmb[e] * gG[e] * inv_n / v;
+            const int row = e / 15;
+            const float half = row > 0 ? 0.5f : 1.0f;
+            for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
+              int idx[4];
+              float wt[4];
+              int n;
+              if (pd.kind <= 3) {
+                const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+                n = code_taps(side ? code.y : code.x, idx, wt);
+              } else {
+                n = general_taps(pd.bx, pd.by, row, e - row * 15 - 7, side ? 1 : -1, idx, wt);
+              }
+              for (int k = 0; k < n; k++) atomicAdd(&gs[idx[k]], f * half * wt[k]);
+            }
+            any = true;
+          }
+        }
+      }
+      if (!__any_sync(0xffffffffu, any)) continue;
+      __syncwarp();
+      // 15x15 unfold (DttRad2.corr_unfold_tile) transposed into the four quadrants
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int a = (lane >> 3) + 4 * k, b = lane & 7;
+        const float g1 = gs[(7 + a) * 15 + 7 + b];
+        const float g2 = b ? gs[(7 + a) * 15 + 7 - b] : 0.f;
+        const float g3 = a ? gs[(7 - a) * 15 + 7 + b] : 0.f;
+        const float g4 = (a && b) ? gs[(7 - a) * 15 + 7 - b] : 0.f;
+        qb[a * 9 + b] = 0.25f * (((g1 + g2) + g3) + g4);
+        if (b) qb[72 + a * 9 + b - 1] = 0.25f * (((g1 - g2) + g3) - g4);
+        if (a) qb[144 + (a - 1) * 9 + b] = 0.25f * (((g1 + g2) - g3) - g4);
+        if (a && b) qb[216 + (a - 1) * 9 + b - 1] = 0.25f * (((g1 - g2) - g3) + g4);
+      }
+      __syncwarp();
+      // 2D DCT-IIe/DST-IIe transposed: forward Z = Ta X^T Tb^T, so Xbar = Tb^T Zbar^T Ta
+      {
+        const float *Ta = k_t2e[(q >> 1) & 1], *Tb = k_t2e[q & 1];
+        float z[8], v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) z[k] = qb[q * 72 + k * 9 + r];  // column r of Zbar
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+          float s = 0.f;
+#pragma unroll
+          for (int k = 0; k < 8; k++) s = fmaf(Ta[k * 8 + n], z[k], s);
+          v[n] = s;
+        }
+#pragma unroll
+        for (int n = 0; n < 8; n++) tb[q * 72 + r * 9 + n] = v[n];  // row r of V = Zbar^T Ta
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 8; k++) z[k] = tb[q * 72 + k * 9 + r];  // column r of V
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          float s = 0.f;
+#pragma unroll
+          for (int j = 0; j < 8; j++) s = fmaf(Tb[j * 8 + k], z[j], s);
+          v[k] = s;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];  // Xbar[k][r]
+        __syncwarp();
+      }
+      // LPF and the fat-zero normalised product (correlateSingleColorFD)
+      const float *c1 = s_clt + (size_t)pd.cam1 * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * TP_CLT;
+      float d1[4][2], d2[4][2], a2[2], s1v[2], s2v[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          d1[m][h] = c1[m * 64 + lane + 32 * h];
+          d2[m][h] = c2[m * 64 + lane + 32 * h];
+          s1 = fmaf(d1[m][h], d1[m][h], s1);
+          s2 = fmaf(d2[m][h], d2[m][h], s2);
+        }
+        a2[h] = sqrtf(s1 * s2);
+        s1v[h] = s1;
+        s2v[h] = s2;
+      }
+      const float fzz = cfg.fat_zero * cfg.fat_zero;
+      const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
+      float tg[4][2], dbar[2], sw[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int idx = lane + 32 * h;
+        const float l = cfg.lpf[idx];
+        const int off = (idx >> 3) * 9 + (idx & 7);
+        float gq[4];
+#pragma unroll
+        for (int qq = 0; qq < 4; qq++) gq[qq] = qb[qq * 72 + off] * l;
+        sw[h] = 1.0f / (a2[h] + fz2);
+        const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
+        const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
+        const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
+        const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
+        const float swbar = gq[0] * t0 + gq[1] * t1 + gq[2] * t2 + gq[3] * t3;
+        dbar[h] = -swbar * sw[h] * sw[h];
+#pragma unroll
+        for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq] * sw[h];
+      }
+      const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int idx = lane + 32 * h;
+        const float a2bar = dbar[h] + dsum;
+        const float T0 = tg[0][h], T1 = tg[1][h], T2 = tg[2][h], T3 = tg[3][h];
+        float g1[4], g2[4];
+        g1[0] = T0 * d2[0][h] + T1 * d2[1][h] + T2 * d2[2][h] + T3 * d2[3][h];
+        g1[1] = T0 * d2[1][h] - T1 * d2[0][h] + T2 * d2[3][h] - T3 * d2[2][h];
+        g1[2] = T0 * d2[2][h] + T1 * d2[3][h] - T2 * d2[0][h] - T3 * d2[1][h];
+        g1[3] = T0 * d2[3][h] - T1 * d2[2][h] - T2 * d2[1][h] + T3 * d2[0][h];
+        g2[0] = T0 * d1[0][h] - T1 * d1[1][h] - T2 * d1[2][h] + T3 * d1[3][h];
+        g2[1] = T0 * d1[1][h] + T1 * d1[0][h] - T2 * d1[3][h] - T3 * d1[2][h];
+        g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
+        g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
+        // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
+        const float k1 = a2[h] > 0.f ? a2bar * s2v[h] / a2[h] : 0.f;
+        const float k2 = a2[h] > 0.f ? a2bar * s1v[h] / a2[h] : 0.f;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          s_g[pd.cam1 * TP_CLT + m * 64 + idx] += fmaf(k1, d1[m][h], g1[m]);
+          s_g[pd.cam2 * TP_CLT + m * 64 + idx] += fmaf(k2, d2[m][h], g2[m]);
+        }
+      }
+      __syncwarp();
+    }
+
+    // ---------------- dd/drx, dd/dry per sensor (forward mode on the CLT) ----------------
+    for (int g = 0; g < groups; g++) {
+      const int s = g * 4 + q;
+      const int sidx = s < S ? s : S - 1;
+      const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
+      const Win w = make_win(sc, p, sidx);
+      const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
+      float ahs, ahc, avs, avc;
+      __sincosf(CUDART_PI_F * 0.0625f * p.rx, &ahs, &ahc);
+      __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
+      const FoldIdx fv = fold_idx(r);
+      const float *cl = s_clt + sidx * TP_CLT + r * 8, *gl = s_g + sidx * TP_CLT + r * 8;
+      float gdir[2];
+#pragma unroll
+      for (int dir = 0; dir < 2; dir++) {
+        float vw0, vw1, hw0[8], hw1[8], o[4][8];
+        if (dir == 0) fold_weights(-K16 * ahs, K16 * ahc, avc, avs, fv, vw0, vw1, hw0, hw1);
+        else fold_weights(ahc, ahs, -K16 * avs, K16 * avc, fv, vw0, vw1, hw0, hw1);
+        fold_dtt_dense(w, fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
+        convolve(o, kp, r);
+        rotate(o, p.rx, p.ry, r);
+        float acc = 0.f;
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+          // the rotation's own derivative: pi/16 (2k+1) x the CLT turned by 90 degrees
+          const float c0 = cl[v], c1 = cl[64 + v], c2 = cl[128 + v], c3 = cl[192 + v];
+          float t0, t1, t2, t3;
+          if (dir == 0) {
+            const float f = K16 * (2 * r + 1);
+            t0 = o[0][v] - f * c1; t1 = o[1][v] + f * c0; t2 = o[2][v] - f * c3; t3 = o[3][v] + f * c2;
+          } else {
+            const float f = K16 * (2 * v + 1);
+            t0 = o[0][v] - f * c2; t1 = o[1][v] - f * c3; t2 = o[2][v] + f * c0; t3 = o[3][v] + f * c1;
+          }
+          acc = fmaf(gl[v], t0, acc);
+          acc = fmaf(gl[64 + v], t1, acc);
+          acc = fmaf(gl[128 + v], t2, acc);
+          acc = fmaf(gl[192 + v], t3, acc);
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+        gdir[dir] = acc;
+      }
+      if (r == 0 && s < S) {
+        // residual = TL - px: dd/dpx = -dd/drx; the kernel-centre offsets add the
+        // dependence of px, py on the port through kdx, kdy (ImageDtt.java:4930-4939)
+        const float gpx = -gdir[0], gpy = -gdir[1];
+        float gx = gpx, gy = gpy;
+        if (p.kidx >= 0) {
+          const float4 e1 = __ldg((const float4 *)(sc.kext[s] + (size_t)p.kidx * 8) + 1);
+          gx = gpx * (1.0f - e1.x) - gpy * e1.z;
+          gy = -gpx * e1.y + gpy * (1.0f - e1.w);
+        }
+        sens[(tile * S + s) * 2] = gx;
+        sens[(tile * S + s) * 2 + 1] = gy;
+      }
+    }
+    if (lane == 0) dval[tile] = dres;
+    __syncwarp();
+  }
+}
+
+// Per tile: Jacobian rows of d w.r.t. the sensors' (azimuth, tilt, roll, zoom)
+// and the tile disparity, and the loss gradient with dL/dd = dl_dd (or 2 d).
+// Per-block partial sums of the extrinsic gradient go to `partial`.
+__global__ void __launch_bounds__(256) adjoint_contract_kernel(const __grid_constant__ SceneDev sc,
+                                                              const float *sens, const float *dval,
+                                                              const float *dl_dd, float *jac_e, float *jac_d,
+                                                              float *grad_d, float *partial) {
+  __shared__ float red[TP_MAXS * 4][8];
+  const int S = sc.num_sensors;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  float gbar = 0.f;
+  size_t tile = 0;
+  bool act = task < sc.num_tasks;
+  if (act) {
+    const int txy = sc.task_txy[task];
+    tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+    const float d = dval[tile];
+    gbar = isnan(d) ? 0.f : (dl_dd ? dl_dd[tile] : 2.0f * d);
+    float jd = 0.f;
+    for (int s = 0; s < S; s++) {
+      const double *pd = sc.port_deriv + ((size_t)task * S + s) * 10;
+      const float jx = sens[(tile * S + s) * 2], jy = sens[(tile * S + s) * 2 + 1];
+      for (int k = 0; k < 4; k++) {
+        const float j = jx * (float)pd[k] + jy * (float)pd[5 + k];
+        jac_e[(tile * S + s) * 4 + k] = j;
+      }
+      jd += jx * (float)pd[4] + jy * (float)pd[9];
+    }
+    jac_d[tile] = jd;
+    grad_d[tile] = gbar * jd;
+  }
+  // block sums of gbar * jac_e over the block's tiles, one (sensor, parameter) at a time
+  for (int sk = 0; sk < S * 4; sk++) {
+    float v = act ? gbar * jac_e[(tile * S + sk / 4) * 4 + (sk & 3)] : 0.f;
+    v = warp_sum(v);
+    if (lane == 0) red[sk][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < S * 4) {
+    float v = 0.f;
+    for (int w = 0; w < 8; w++) v += red[threadIdx.x][w];
+    partial[(size_t)blockIdx.x * S * 4 + threadIdx.x] = v;
+  }
+}
+
+__global__ void adjoint_final_kernel(const float *partial, int nblocks, int n, float *grad_e) {
+  const int i = threadIdx.x;
+  if (i < n) {
+    float v = 0.f;
+    for (int b = 0; b < nblocks; b++) v += partial[(size_t)b * n + i];
+    grad_e[i] = v;
+  }
+}
+
+cudaError_t upload_adjoint_constants() {
+  cudaError_t e = upload_dtt_constants();
+  if (e != cudaSuccess) return e;
+  // DCT-IIe: T[k][n] = 0.5 cos(pi k (2n+1) / 16); DST-IIe: S[j][n] = (-1)^n T[7-j][n]
+  float t[2][64];
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < 8; k++)
+    for (int n = 0; n < 8; n++) t[0][k * 8 + n] = (float)(0.5 * std::cos(pi * k * (2 * n + 1) / 16.0));
+  for (int j = 0; j < 8; j++)
+    for (int n = 0; n < 8; n++) t[1][j * 8 + n] = ((n & 1) ? -1.f : 1.f) * t[0][(7 - j) * 8 + n];
+  return cudaMemcpyToSymbol(k_t2e, t, sizeof(t));
+}
+
+int adjoint_smem_bytes(int S) { return (S * 2 * TP_CLT + 240 + 288 + 288 + 240 + 240) * 4; }
+
+cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
+                           const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
+                           float *grad_e, cudaStream_t st) {
+  if (sc.num_tasks <= 0) return cudaSuccess;
+  if (sc.num_colors != 1 || !sc.port_deriv) return cudaErrorInvalidValue;
+  AdjShape as;
+  as.S = sc.num_sensors;
+  as.P = sc.num_pairs;
+  as.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
+  as.per_warp = adjoint_smem_bytes(as.S) / 4;
+  as.recompute = recompute;
+  const int bytes = adjoint_smem_bytes(as.S);
+  cudaError_t e = cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, 32, bytes);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int grid = sc.num_tasks < sms * per_sm ? sc.num_tasks : sms * per_sm;
+  adjoint_kernel<<<grid, 32, bytes, st>>>(sc, as, cc, sens, dval);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int nb = (sc.num_tasks + 255) / 256;
+  adjoint_contract_kernel<<<nb, 256, 0, st>>>(sc, sens, dval, dl_dd, jac_e, jac_d, grad_d, partial);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  adjoint_final_kernel<<<1, 64, 0, st>>>(partial, nb, sc.num_sensors * 4, grad_e);
+  return cudaGetLastError();
+}

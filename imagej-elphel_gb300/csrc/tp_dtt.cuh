@@ -140,6 +140,93 @@ __device__ __forceinline__ void group_transpose(float v[8], float *buf, int r) {
   __syncwarp();
 }
 
+// fold weights of the shifted sine window (DttRad2.get_shifted_fold_2d, 263-314):
+// (hc, hs) / (vc, vs) are the cosine / sine of pi/16 x the horizontal / vertical
+// shift, or their derivatives (the weights are linear in them)
+__device__ __forceinline__ void fold_weights(float hc, float hs, float vc, float vs, const FoldIdx &fv,
+                                             float &vw0, float &vw1, float hw0[8], float hw1[8]) {
+  vw0 = vc * k_hwin[fv.win0] + vs * k_hwin[fv.dwin0] * fv.ds0;
+  vw1 = vc * k_hwin[fv.win1] + vs * k_hwin[fv.dwin1] * fv.ds1;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const FoldIdx fh = fold_idx(j);
+    hw0[j] = hc * k_hwin[fh.win0] + hs * k_hwin[fh.dwin0] * fh.ds0;
+    hw1[j] = hc * k_hwin[fh.win1] + hs * k_hwin[fh.dwin1] * fh.ds1;
+  }
+}
+
+// fold of a dense 16x16 window and the four 2D DCT-IV/DST-IV (fold_tile, dttt_iv):
+// lane r of the 8-lane group holds horizontal frequency r of each quadrant, o[m][v]
+__device__ __forceinline__ void fold_dtt_dense(const Win &w, const FoldIdx &fv, float vw0, float vw1,
+                                               const float hw0[8], const float hw1[8], int r, float *tbuf,
+                                               float o[4][8]) {
+  // vertical 2-tap combine once, then the two horizontal variants
+#pragma unroll
+  for (int vb = 0; vb < 2; vb++) {
+    const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
+    float vc[16];
+#pragma unroll
+    for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+#pragma unroll
+    for (int hb = 0; hb < 2; hb++) {
+      float y[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const FoldIdx fh = fold_idx(j);
+        const float h0 = (hb ? fh.ss0 : fh.sc0) * hw0[j], h1 = (hb ? fh.ss1 : fh.sc1) * hw1[j];
+        y[j] = fmaf(h1, vc[fh.src1], h0 * vc[fh.src0]);
+      }
+      float z[8];
+      dtt4_fast(y, z, hb);
+      group_transpose(z, tbuf, r);
+      dtt4_fast(z, o[vb * 2 + hb], vb);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// strip samples of a 15x15 correlation surface (Correlation2d.java:610-718)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float strip_sample(const float *c, int kind, float bx, float by, int row, int scol, int down) {
+  if (kind <= 3) {
+    const int sh = (kind > 1) ? 0 : 1, ilimit = 7 << sh;  // denom = 1 << sh
+    int xnum, ynum;
+    if (kind == 0) { xnum = 2 * scol + (row & 1); ynum = down * row; }
+    else if (kind == 1) { xnum = down * row; ynum = 2 * scol + (row & 1); }
+    else if (kind == 2) { xnum = scol - ((down * row) >> 1); ynum = scol + ((down * row + 1) >> 1); }
+    else { xnum = scol - ((down * row) >> 1); ynum = -scol - ((down * row + 1) >> 1); }
+    if (xnum > ilimit || xnum < -ilimit || ynum > ilimit || ynum < -ilimit) return CUDART_NAN_F;
+    const int ix0 = (xnum + ilimit) >> sh, iy0 = (ynum + ilimit) >> sh;
+    const bool int_x = (xnum & ((1 << sh) - 1)) == 0, int_y = (ynum & ((1 << sh) - 1)) == 0;
+    if (int_x && int_y) return c[iy0 * 15 + ix0];
+    const float dx = int_x ? 0.f : 0.5f, dy = int_y ? 0.f : 0.5f;
+    if (int_y) return (1.0f - dx) * c[iy0 * 15 + ix0] + dx * c[iy0 * 15 + ix0 + 1];
+    if (int_x) return (1.0f - dy) * c[iy0 * 15 + ix0] + dy * c[(iy0 + 1) * 15 + ix0];
+    return ((1.0f - dx) * (1.0f - dy) * c[iy0 * 15 + ix0]) + (dx * (1.0f - dy) * c[iy0 * 15 + ix0 + 1]) +
+           ((1.0f - dx) * dy * c[(iy0 + 1) * 15 + ix0]) + (dx * dy * c[(iy0 + 1) * 15 + ix0 + 1]);
+  }
+  const float a = scol + 0.5f * (row & 1), pp = 0.5f * down * row;
+  const float x = a * bx - pp * by, y = a * by + pp * bx;
+  if (x > 7.f || x < -7.f || y > 7.f || y < -7.f) return CUDART_NAN_F;
+  const float fx = x + 7.f, fy = y + 7.f;
+  const int ix0 = min((int)floorf(fx), 13), iy0 = min((int)floorf(fy), 13);
+  const float dx = fx - ix0, dy = fy - iy0;
+  return ((1.0f - dx) * (1.0f - dy) * c[iy0 * 15 + ix0]) + (dx * (1.0f - dy) * c[iy0 * 15 + ix0 + 1]) +
+         ((1.0f - dx) * dy * c[(iy0 + 1) * 15 + ix0]) + (dx * dy * c[(iy0 + 1) * 15 + ix0 + 1]);
+}
+
+// one strip sample from a precomputed code (quad kinds): same arithmetic as
+// Correlation2d.java:664-690 with dx, dy in {0, 0.5}
+__device__ __forceinline__ float sample_code(const float *c, int code) {
+  if (code < 0) return CUDART_NAN_F;
+  const int idx = code & 255, cs = code >> 8;
+  const float v = c[idx];
+  if (cs == 0) return v;
+  if (cs == 1) return 0.5f * v + 0.5f * c[idx + 1];
+  if (cs == 2) return 0.5f * v + 0.5f * c[idx + 15];
+  return ((0.25f * v + 0.25f * c[idx + 1]) + 0.25f * c[idx + 15]) + 0.25f * c[idx + 16];
+}
+
 cudaError_t upload_dtt_constants() {
   float hw[8], d2[64], c4[4], s4[4];
   const double pi = 3.14159265358979323846, sc = 1.0 / std::sqrt(8.0);

@@ -40,6 +40,10 @@ struct tp_handle {
   double *d_rdist = nullptr;
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
+  // adjoint buffers (allocated by the first tp_backward)
+  float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
+  float *d_partial = nullptr, *d_grad_e = nullptr, *d_dldd = nullptr;
+  int adj_recompute = 0, fwd_valid = 0, have_jac = 0;
   int tex_rows_alloc = 0, tex_rows = 0;  // allocated rows, rows of the last run
   // host state
   int num_tasks = 0;
@@ -331,6 +335,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && upload_kernel_constants() == cudaSuccess;
   ok = ok && upload_fused_constants() == cudaSuccess;
   ok = ok && upload_texture_constants() == cudaSuccess;
+  ok = ok && upload_adjoint_constants() == cudaSuccess;
   tp_default_texture_params(&h->tex_params);
   for (int s = 0; ok && s < S; s++) {
     ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
@@ -380,7 +385,8 @@ tp_status tp_destroy(tp_handle *h) {
   void *bufs[] = {h->d_task_txy, h->d_task_op, h->d_task_disp, h->d_task_xy, h->d_tile_op, h->d_tile_disp,
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
-                  h->d_tex, h->d_tex_aux};
+                  h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
+                  h->d_partial, h->d_grad_e, h->d_dldd};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -420,6 +426,7 @@ tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
   CK(cudaStreamSynchronize(h->stream), "tp_set_geometry");
   h->have_geometry = 1;
   h->planned = 0;
+  h->fwd_valid = 0;
   return TP_OK;
 }
 
@@ -441,16 +448,19 @@ tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const floa
   }
   CK(cudaMemcpy(h->d_kext[cam], offs, nk * 8 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
   h->planned = 0;
+  h->fwd_valid = 0;
   return TP_OK;
 }
 
 tp_status tp_set_color_scales(tp_handle *h, const float *scales) {
+  if (h) h->fwd_valid = 0;
   if (!h || !scales) return TP_ERR_ARG;
   for (int i = 0; i < 3; i++) h->color_scale[i] = scales[i];
   return TP_OK;
 }
 
 tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size_t pitch) {
+  if (h) h->fwd_valid = 0;
   if (!h || !image) return TP_ERR_ARG;
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_image: bad camera");
   if (dtype != TP_F32 && dtype != TP_U16) return fail(h, TP_ERR_ARG, "tp_set_image: bad dtype");
@@ -489,6 +499,7 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
   h->ports_from_geometry = 0;
   h->have_tasks = 1;
   h->planned = 0;
+  h->fwd_valid = 0;
   return TP_OK;
 }
 
@@ -508,6 +519,7 @@ tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
   h->ports_from_geometry = 1;
   h->have_tasks = 1;
   h->planned = 0;
+  h->fwd_valid = 0;
   return TP_OK;
 }
 
@@ -523,6 +535,7 @@ tp_status tp_set_lpf(tp_handle *h, const float *lpf) {
 }
 
 tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int np) {
+  if (h) h->fwd_valid = 0;
   if (!h || !p || (!pairs && np > 0)) return TP_ERR_ARG;
   if (np < 0 || np > TP_MAX_PAIRS) return fail(h, TP_ERR_ARG, "tp_set_corr: too many pairs");
   if (p->corr_strip_hight < 1 || p->corr_strip_hight > TP_MAX_STRIP || p->corr_wndy_size < 1 ||
@@ -623,6 +636,7 @@ static tp_status ensure_plan(tp_handle *h, cudaStream_t st) {
 tp_status tp_ports(tp_handle *h, void *stream) {
   if (!h) return TP_ERR_ARG;
   h->planned = 0;
+  h->fwd_valid = 0;
   return ensure_plan(h, pick_stream(h, stream));
 }
 
@@ -733,6 +747,7 @@ tp_status tp_process(tp_handle *h, void *stream) {
   if (r != TP_OK) return r;
   if (h->num_pairs == 0) return tp_convert_correct(h, stream);
   CK(launch_fused_forward(scene_of(h), h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
+  h->fwd_valid = 1;
   return TP_OK;
 }
 
@@ -861,6 +876,76 @@ tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity
     return TP_ERR_CUDA;
   }
   return TP_OK;
+}
+
+tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt) {
+  if (!h) return TP_ERR_ARG;
+  h->adj_recompute = recompute_clt ? 1 : 0;
+  return TP_OK;
+}
+
+tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  if (h->cfg.num_colors != 1) return fail(h, TP_ERR_ARG, "tp_backward: the adjoint is implemented for mono sensors");
+  if (!h->ports_from_geometry || !h->have_geometry)
+    return fail(h, TP_ERR_STATE, "tp_backward: needs tile ops with ports from the geometry (tp_set_tile_ops)");
+  if (!h->fwd_valid || h->num_pairs == 0)
+    return fail(h, TP_ERR_STATE, "tp_backward: run tp_process (with correlation pairs) first");
+  cudaStream_t st = pick_stream(h, stream);
+  const size_t nt = h->ntiles, S = h->cfg.num_sensors;
+  const int nb = (int)((nt + 255) / 256);
+  if (!h->d_sens) {
+    bool ok = dalloc(&h->d_port_deriv, nt * S * 10) == cudaSuccess && dalloc(&h->d_sens, nt * S * 2) == cudaSuccess &&
+              dalloc(&h->d_dval, nt) == cudaSuccess && dalloc(&h->d_jac_e, nt * S * 4) == cudaSuccess &&
+              dalloc(&h->d_jac_d, nt) == cudaSuccess && dalloc(&h->d_grad_d, nt) == cudaSuccess &&
+              dalloc(&h->d_partial, (size_t)nb * S * 4) == cudaSuccess && dalloc(&h->d_grad_e, S * 4) == cudaSuccess &&
+              dalloc(&h->d_dldd, nt) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_backward: adjoint buffers");
+    }
+    CK(cudaMemsetAsync(h->d_grad_d, 0, nt * sizeof(float), st), "tp_backward");
+    CK(cudaMemsetAsync(h->d_jac_d, 0, nt * sizeof(float), st), "tp_backward");
+  }
+  // the plan again with the FP64 port derivatives (same ports, corners and residuals)
+  SceneDev sc = scene_of(h);
+  sc.port_deriv = h->d_port_deriv;
+  CK(launch_plan(sc, st), "tp_backward plan");
+  if (dl_ddisp) CK(cudaMemcpyAsync(h->d_dldd, dl_ddisp, nt * sizeof(float), cudaMemcpyHostToDevice, st), "tp_backward");
+  CK(launch_adjoint(sc, h->corr_host, h->adj_recompute, h->d_sens, h->d_dval, dl_ddisp ? h->d_dldd : nullptr,
+                    h->d_jac_e, h->d_jac_d, h->d_grad_d, h->d_partial, h->d_grad_e, st),
+     "tp_backward adjoint");
+  h->have_jac = 1;
+  if (dl_dextr) CK(cudaMemcpyAsync(dl_dextr, h->d_grad_e, S * 4 * sizeof(float), cudaMemcpyDeviceToHost, st), "tp_backward");
+  if (dl_dtile_disp)
+    CK(cudaMemcpyAsync(dl_dtile_disp, h->d_grad_d, nt * sizeof(float), cudaMemcpyDeviceToHost, st), "tp_backward");
+  if (dl_dextr || dl_dtile_disp) CK(cudaStreamSynchronize(st), "tp_backward");
+  return TP_OK;
+}
+
+tp_status tp_get_disparity_jacobian(tp_handle *h, float *jac_extr, float *jac_disp, float *disparity) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->have_jac) return fail(h, TP_ERR_STATE, "tp_get_disparity_jacobian: run tp_backward first");
+  const size_t nt = h->ntiles, S = h->cfg.num_sensors;
+  tp_status r = TP_OK;
+  if (jac_extr) r = d2h(h, jac_extr, h->d_jac_e, nt * S * 4 * sizeof(float), "tp_get_disparity_jacobian");
+  if (r == TP_OK && jac_disp) r = d2h(h, jac_disp, h->d_jac_d, nt * sizeof(float), "tp_get_disparity_jacobian");
+  if (r == TP_OK && disparity) r = d2h(h, disparity, h->d_dval, nt * sizeof(float), "tp_get_disparity_jacobian");
+  return r;
+}
+
+tp_status tp_get_port_sensitivities(tp_handle *h, float *sens) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->have_jac) return fail(h, TP_ERR_STATE, "tp_get_port_sensitivities: run tp_backward first");
+  return d2h(h, sens, h->d_sens, (size_t)h->ntiles * h->cfg.num_sensors * 2 * sizeof(float),
+             "tp_get_port_sensitivities");
+}
+
+tp_status tp_get_port_derivatives(tp_handle *h, double *deriv) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->have_jac) return fail(h, TP_ERR_STATE, "tp_get_port_derivatives: run tp_backward first");
+  return d2h(h, deriv, h->d_port_deriv, (size_t)h->num_tasks * h->cfg.num_sensors * 10 * sizeof(double),
+             "tp_get_port_derivatives");
 }
 
 }  // extern "C"

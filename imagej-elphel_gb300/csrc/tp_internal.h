@@ -92,7 +92,7 @@ struct SceneDev {
   const double *rdist_tbl;   // reverse distortion table
   // products
   double *ports;             // [n][S][2]
-  double *port_deriv;        // [n][S][2][4] or null
+  double *port_deriv;        // [n][S][2][5] d(x, y)/d(azimuth, tilt, roll, zoom, disparity) or null
   SubtilePlan *plan;         // [n][S][C]
   int *tile_task;            // [tilesY*tilesX] -> task index or -1
   float *clt;                // [tiles][S][C][256]
@@ -143,6 +143,12 @@ cudaError_t compact_scratch_address(int **ptr);
 cudaError_t launch_compact_tasks_scratch(const int *tile_op, const float *disparity, int tilesX, int num_tiles,
                                          int *task_txy, int *task_op, float *task_disp, int *num_tasks_dev,
                                          int *scratch, cudaStream_t st);
+// adjoint (tp_adjoint.cu): per-tile dd/dport, Jacobian rows, loss gradient
+cudaError_t upload_adjoint_constants();
+int adjoint_smem_bytes(int S);
+cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
+                           const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
+                           float *grad_e, cudaStream_t st);
 // texture tiles (tp_texture.cu)
 cudaError_t launch_textures(const SceneDev &sc, const TexConst &tc, cudaStream_t st);
 cudaError_t upload_texture_constants();

@@ -44,7 +44,7 @@ __device__ __forceinline__ void mat3_vec(const double m[3][3], const double v[3]
 
 // getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2159-2314) for one sensor
 __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double py, double disparity, int i,
-                        double &ox, double &oy, double *deriv /* [2][4] or null */) {
+                        double &ox, double &oy, double *deriv /* [2][5] or null */) {
   double pXcd = DSUB(px, DMUL(0.5, (double)g.pixel_width));
   double pYcd = DSUB(py, DMUL(0.5, (double)g.pixel_height));
   double rD = DMUL(DMUL(DSQRT(DADD(DMUL(pXcd, pXcd), DMUL(pYcd, pYcd))), 0.001), g.pixel_size);
@@ -78,19 +78,24 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
       rri = DMUL(rri, ri);
     }
 #pragma unroll
-    for (int k = 0; k < 4; k++) {  // azimuth, tilt, roll, zoom
+    for (int k = 0; k < 5; k++) {  // azimuth, tilt, roll, zoom; then the tile disparity
       double dr[3];
-      mat3_vec(g.drots[i][k], vi, dr);
+      if (k < 4) {
+        mat3_vec(g.drots[i][k], vi, dr);
+      } else {  // d vi / d disparity = (-rX, -rY, 0)
+        const double dvi[3] = {-g.rXY[i][0], -g.rXY[i][1], 0.0};
+        mat3_vec(g.rots[i], dvi, dr);
+      }
       double dpX = DSUB(DMUL(dr[0], norm_z), DDIV(DMUL(pXci, dr[2]), rvi[2]));
       double dpY = DSUB(DMUL(dr[1], norm_z), DDIV(DMUL(pYci, dr[2]), rvi[2]));
       if (k == 2) {  // roll: the reference keeps only the rotation term
         deriv[k] = DMUL(dpX, rD2rND);
-        deriv[4 + k] = DMUL(dpY, rD2rND);
+        deriv[5 + k] = DMUL(dpY, rD2rND);
       } else {
         double dri = DMUL(DDIV(ri_scale, rNDi), DADD(DMUL(pXci, dpX), DMUL(pYci, dpY)));
         double drD = DMUL(drD2rND_dri, dri);
         deriv[k] = DADD(DMUL(dpX, rD2rND), DMUL(pXci, drD));
-        deriv[4 + k] = DADD(DMUL(dpY, rD2rND), DMUL(pYci, drD));
+        deriv[5 + k] = DADD(DMUL(dpY, rD2rND), DMUL(pYci, drD));
       }
     }
   }
@@ -152,11 +157,11 @@ __global__ void plan_kernel(SceneDev sc) {
     double cx, cy;
     if (sc.ports_from_geometry) {
       if (sc.port_deriv) {
-        double dv[8];
+        double dv[10];
         port_xy(*sc.geom, sc.rdist_tbl, ctx, cty, disparity, s, cx, cy, dv);
-        double *o = sc.port_deriv + ((size_t)task * S + s) * 8;
+        double *o = sc.port_deriv + ((size_t)task * S + s) * 10;
 #pragma unroll
-        for (int k = 0; k < 8; k++) o[k] = dv[k];
+        for (int k = 0; k < 10; k++) o[k] = dv[k];
       } else {
         sensor_port(*sc.geom, pXc, pYc, disparity, s, cx, cy);
       }

@@ -95,6 +95,11 @@ PROTOTYPES = {
     "tp_get_textures": [_H, _vp],
     "tp_get_texture_aux": [_H, _vp],
     "tp_compact_tile_ops_noalloc": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
+    "tp_backward": [_H, _vp, _vp, _vp, _vp],
+    "tp_set_adjoint_mode": [_H, C.c_int],
+    "tp_get_disparity_jacobian": [_H, _vp, _vp, _vp],
+    "tp_get_port_sensitivities": [_H, _vp],
+    "tp_get_port_derivatives": [_H, _vp],
 }
 
 _lib = None

@@ -240,6 +240,42 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_get_rbg(self.h, int(ncam), _ptr(out)), "tp_get_rbg")
         return out
 
+    # ---- adjoint ----
+    def setAdjointMode(self, recompute_clt=False):
+        self._ck(self._lib.tp_set_adjoint_mode(self.h, int(bool(recompute_clt))), "tp_set_adjoint_mode")
+
+    def backward(self, dl_ddisp=None, stream=None):
+        """Adjoint of the last process(): returns (dL/d extrinsics [S][4], dL/d tile disparity [tiles])
+        for L = sum l(d) with dl/dd = dl_ddisp (default 2 d)."""
+        T = self.tilesY * self.tilesX
+        ge = np.zeros((self.num_sensors, 4), dtype=np.float32)
+        gd = np.zeros(T, dtype=np.float32)
+        dl = None
+        if dl_ddisp is not None:
+            dl = np.ascontiguousarray(np.broadcast_to(np.asarray(dl_ddisp, dtype=np.float32), (T,)))
+        self._ck(self._lib.tp_backward(self.h, _ptr(dl) if dl is not None else None, _ptr(ge), _ptr(gd), stream),
+                 "tp_backward")
+        return ge, gd
+
+    def getDisparityJacobian(self):
+        """(jac_extr [tiles][S][4], jac_disp [tiles], disparity [tiles]) of the last backward()."""
+        T = self.tilesY * self.tilesX
+        je = np.zeros((T, self.num_sensors, 4), dtype=np.float32)
+        jd = np.zeros(T, dtype=np.float32)
+        d = np.zeros(T, dtype=np.float32)
+        self._ck(self._lib.tp_get_disparity_jacobian(self.h, _ptr(je), _ptr(jd), _ptr(d)), "tp_get_disparity_jacobian")
+        return je, jd, d
+
+    def getPortSensitivities(self):
+        out = np.zeros((self.tilesY * self.tilesX, self.num_sensors, 2), dtype=np.float32)
+        self._ck(self._lib.tp_get_port_sensitivities(self.h, _ptr(out)), "tp_get_port_sensitivities")
+        return out
+
+    def getPortDerivatives(self):
+        out = np.zeros((self.numTasks(), self.num_sensors, 2, 5), dtype=np.float64)
+        self._ck(self._lib.tp_get_port_derivatives(self.h, _ptr(out)), "tp_get_port_derivatives")
+        return out
+
     def getTextures(self):
         """[tilesY * tilesX][4 or 12][256]: R, B, G, alpha (+ 4 port weights, 4 rms)."""
         rows = getattr(self, "_tex_rows", 12)

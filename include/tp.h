@@ -205,6 +205,35 @@ tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
 tp_status tp_get_texture_aux(tp_handle *h, float *aux);
 
+/* ---- adjoint (no reference counterpart: the reference has no derivative of
+ * the correlation chain; its geometric part is GeometryCorrection
+ * .getPortsCoordinatesAndDerivatives, GeometryCorrection.java:2159-2314) ----
+ * For every tile with a centroid disparity d (TP_DISP_CM of the last
+ * tp_process), tp_backward computes dd/d(port x, y) of every sensor by a
+ * hand-written adjoint of centroid -> strip combination -> correlation ->
+ * CLT -> residual window shift, contracts it with the FP64 port derivatives
+ * into the Jacobian rows dd/d(azimuth, tilt, roll, zoom of each sensor) and
+ * dd/d(tile target disparity), and returns the gradient of
+ * L = sum over tiles of l(d) with dl/dd given per tile in dl_ddisp
+ * ([tilesY*tilesX], host; NULL means l = d^2, i.e. 2 d).  Integer window
+ * corners and the integer argmax are held fixed (piecewise constant).
+ * Mono sensors, ports from the geometry (tp_set_tile_ops); run after tp_process.
+ * dl_dextr [num_sensors][4] and dl_dtile_disp [tilesY*tilesX] are host
+ * outputs (either may be NULL). */
+tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream);
+/* 1: the adjoint recomputes each tile's CLT from the images instead of reading
+ * the stored CLT back (for when the CLT buffer is not kept); default 0 */
+tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt);
+/* Jacobian of the last tp_backward: jac_extr [tiles][num_sensors][4] (dd per
+ * azimuth, tilt, roll, zoom), jac_disp [tiles] (dd per target disparity),
+ * disparity [tiles] (d, NaN where none); any pointer may be NULL */
+tp_status tp_get_disparity_jacobian(tp_handle *h, float *jac_extr, float *jac_disp, float *disparity);
+/* dd/d(port x, port y) per tile and sensor: [tiles][num_sensors][2] */
+tp_status tp_get_port_sensitivities(tp_handle *h, float *sens);
+/* FP64 port derivatives of the last tp_backward's plan, per task:
+ * [num_tasks][num_sensors][2 (x, y)][5 (azimuth, tilt, roll, zoom, disparity)] */
+tp_status tp_get_port_derivatives(tp_handle *h, double *deriv);
+
 /* ---- no-allocation entry point ----
  * Row-major compaction of tile_op[num_tiles] into the task list, the same
  * result as tp_set_tile_ops (task_txy = tx | ty << 16, task_op, task_disp,

@@ -1,0 +1,180 @@
+"""Adjoint of the forward chain (tp_backward) on the GPU, checked by central
+finite differences of the FP64 oracle and against the oracle's FP64 port
+derivatives (GeometryCorrection.getPortsCoordinatesAndDerivatives).
+
+Scene: 16 mono LWIR sensors on a circle (radius 100 mm, f 4.9 mm, 12 um
+pixels), 160x128 (320 tiles), all 120 pairs, extrinsics perturbed by
+N(0, 1e-3) rad and target disparities off the truth by N(0, 0.2) px so the
+measured residual disparities d are not zero.
+
+Tolerances: port derivatives (FP64 on the device) to 1e-10 relative; the
+per-tile port sensitivities dd/dport to 2e-3 + 3% of the finite difference on
+95% of the samples; the loss gradient at 200 seeded coordinates to 3% of the
+finite difference on 95% of them.  Steps: 1e-4 for the tile disparities (as
+specified); 1e-6 rad for the extrinsics.  The forward is only piecewise
+smooth (integer window corners and the integer argmax switch), and 1e-4 rad
+moves every port of a sensor by ~0.04 px, switching the corners of ~8% of
+its sub-tiles: on this scene the central difference for sensor 0's azimuth
+is 9029 at 1e-4, 3821 at 1e-5 and 4242 at 3e-6 ... 3e-7, so only the small
+step measures the derivative.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from tileproc import GPUTileProcessor, synth
+
+pytestmark = pytest.mark.gpu
+
+W, H = 160, 128
+T = (W // 8) * (H // 8)
+
+
+def _setup(seed=31):
+    sc = synth.make_scene("circle_lwir", seed=seed, width=W, height=H)
+    rng = np.random.default_rng(seed + 1)
+    g = copy.deepcopy(sc["geometry"])
+    for k in ("azimuth", "tilt", "roll", "zoom"):
+        g[k] = (np.asarray(g[k]) + rng.normal(0, 1e-3, 16)).tolist()
+    pairs = synth.circle_pairs(g)
+    D = (sc["disparity_gt"].reshape(-1) + rng.normal(0, 0.2, T)).astype(np.float32)
+    return sc, g, pairs, D
+
+
+def _gpu(sc, g, pairs, D):
+    tp = GPUTileProcessor(16, W, H)
+    tp.setGeometry(g)
+    tp.setBayerImages(sc["images"])
+    tp.setCorrelation(pairs=pairs)
+    tp.setFullFrameImages(D, tile_op=np.ones(T, np.int32))
+    tp.process()
+    return tp
+
+
+def _oracle_d(O, sc, g, pairs, D, tile_op=None, ports_in=None):
+    op = np.ones(T, np.int32) if tile_op is None else tile_op
+    P = O.make_pairs([(a, b, bx, by, kind) for (a, b, kind, _, bx, by) in pairs])
+    r = O.run(W, H, sc["images"][:, None].astype(np.float64), op, np.asarray(D, np.float64),
+              geometry=None if ports_in is not None else g, ports_in=ports_in, pairs=P, want=("disp",))
+    return r["disp"][:, O.DISP_CM]
+
+
+def test_port_derivatives_match_oracle(oracle):
+    sc, g, pairs, D = _setup()
+    with _gpu(sc, g, pairs, D) as tp:
+        ports0 = tp.getPorts()
+        tp.backward()
+        assert np.array_equal(tp.getPorts(), ports0), "the backward plan moved the ports"
+        dv = tp.getPortDerivatives()
+        txy = tp.getTaskTiles()
+    rng = np.random.default_rng(5)
+    for t in rng.choice(len(txy), 24, replace=False):
+        tx, ty = txy[t] & 0xFFFF, txy[t] >> 16
+        cx, cy, dd = tx * 8 + 4.0, ty * 8 + 4.0, float(D[t])
+        pref, dref = oracle.ports(g, cx, cy, dd, deriv=True)
+        assert np.allclose(dv[t, :, :, :4], dref, rtol=1e-10, atol=1e-12)
+        h = 1e-4
+        fd = (oracle.ports(g, cx, cy, dd + h) - oracle.ports(g, cx, cy, dd - h)) / (2 * h)
+        assert np.allclose(dv[t, :, :, 4], fd, rtol=1e-6, atol=1e-8)
+
+
+def test_port_sensitivities_match_finite_differences(oracle):
+    sc, g, pairs, D = _setup()
+    with _gpu(sc, g, pairs, D) as tp:
+        tp.backward()
+        sens = tp.getPortSensitivities()
+        ports = tp.getPorts()
+        txy = tp.getTaskTiles()
+    d0 = _oracle_d(oracle, sc, g, pairs, D)
+    rng = np.random.default_rng(6)
+    valid = np.nonzero(np.isfinite(d0))[0]
+    h = 1e-3
+    errs = []
+    for t in rng.choice(valid, 10, replace=False):
+        tile = (txy[t] >> 16) * (W // 8) + (txy[t] & 0xFFFF)
+        op = np.zeros(T, np.int32)
+        op[tile] = 1
+        for s in rng.choice(16, 3, replace=False):
+            for ax in range(2):
+                pp = ports.copy()
+                pp[t, s, ax] += h
+                dp = _oracle_d(oracle, sc, g, pairs, D, op, pp)[tile]
+                pp[t, s, ax] -= 2 * h
+                dm = _oracle_d(oracle, sc, g, pairs, D, op, pp)[tile]
+                fd = (dp - dm) / (2 * h)
+                errs.append((sens[tile, s, ax], fd))
+    e = np.array(errs)
+    bad = np.abs(e[:, 0] - e[:, 1]) > 2e-3 + 0.03 * np.abs(e[:, 1])
+    print("dd/dport: max |fd| %.3g, max err %.3g" % (np.abs(e[:, 1]).max(), np.abs(e[:, 0] - e[:, 1]).max()))
+    assert bad.mean() <= 0.05, e[bad]
+
+
+def test_loss_gradient_matches_finite_differences(oracle):
+    """200 seeded coordinates, central differences of L = sum d^2 (FP64 oracle; steps in the module
+    docstring); the adjoint is driven with dL/dd = 2 d of the oracle so only its Jacobian is compared."""
+    sc, g, pairs, D = _setup()
+    d0 = _oracle_d(oracle, sc, g, pairs, D)
+    dl = np.where(np.isfinite(d0), 2 * d0, 0.0).astype(np.float32)
+    with _gpu(sc, g, pairs, D) as tp:
+        ge, gd = tp.backward(dl_ddisp=dl)
+        ports = tp.getPorts()
+        txy = tp.getTaskTiles()
+    rng = np.random.default_rng(7)
+    keys = ("azimuth", "tilt", "roll", "zoom")
+    h, he = 1e-4, 1e-6
+
+    def loss(gg, DD):
+        d = _oracle_d(oracle, sc, gg, pairs, DD)
+        return float(np.nansum(np.where(np.isfinite(d), d * d, 0.0)))
+
+    rows = []
+    for flat in rng.choice(64, 40, replace=False):
+        s, k = flat // 4, flat % 4
+        gp, gm = copy.deepcopy(g), copy.deepcopy(g)
+        gp[keys[k]][s] += he
+        gm[keys[k]][s] -= he
+        rows.append(("e", ge[s, k], (loss(gp, D) - loss(gm, D)) / (2 * he)))
+    valid = np.nonzero(np.isfinite(d0))[0]
+    for t in rng.choice(valid, 160, replace=False):
+        op = np.zeros(T, np.int32)
+        op[t] = 1
+        Dp, Dm = D.astype(np.float64), D.astype(np.float64)
+        Dp[t] += h
+        Dm[t] -= h
+        dp = _oracle_d(oracle, sc, g, pairs, Dp, op)[t]
+        dm = _oracle_d(oracle, sc, g, pairs, Dm, op)[t]
+        rows.append(("d", gd[t], (dp * dp - dm * dm) / (2 * h)))
+    got = np.array([r[1] for r in rows], np.float64)
+    fd = np.array([r[2] for r in rows], np.float64)
+    scale = np.array([np.abs(fd[:40]).max()] * 40 + [np.abs(fd[40:]).max()] * 160)
+    rel = np.abs(got - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
+    print("loss gradient: extrinsic rel err median %.3g max %.3g; disparity median %.3g max %.3g" % (
+        np.median(rel[:40]), rel[:40].max(), np.median(rel[40:]), rel[40:].max()))
+    assert np.mean(rel <= 0.03) >= 0.95, np.sort(rel)[-12:]
+
+
+def test_recompute_mode_matches_stored_clt(oracle):
+    sc, g, pairs, D = _setup()
+    with _gpu(sc, g, pairs, D) as tp:
+        ge0, gd0 = tp.backward()
+        tp.setAdjointMode(recompute_clt=True)
+        ge1, gd1 = tp.backward()
+    assert np.allclose(ge1, ge0, rtol=1e-4, atol=1e-4 * np.abs(ge0).max())
+    assert np.allclose(gd1, gd0, rtol=1e-4, atol=1e-4 * np.abs(gd0).max())
+
+
+def test_lma_reduces_cost(oracle):
+    """Levenberg-Marquardt on the analytic Jacobian from extrinsics perturbed by N(0, 3e-3) rad."""
+    from tileproc import lma
+    sc = synth.make_scene("circle_lwir", seed=41, width=W, height=H)
+    rng = np.random.default_rng(42)
+    g0 = copy.deepcopy(sc["geometry"])
+    for k in lma.KEYS:
+        g0[k] = (np.asarray(g0[k]) + rng.normal(0, 3e-3, 16)).tolist()
+    D = sc["disparity_gt"].reshape(-1).astype(np.float32)
+    with _gpu(sc, g0, synth.circle_pairs(g0), D) as tp:
+        g, Dn, hist = lma.refine(tp, g0, D, iterations=6)
+    print("LMA cost:", ["%.4g" % c for c in hist])
+    assert all(b <= a for a, b in zip(hist, hist[1:]))
+    assert hist[-1] < 0.5 * hist[0]

@@ -1,0 +1,79 @@
+"""Host side of the extrinsic / disparity refinement (tileproc.lma) on a fake
+processor whose residual disparity is linear in the parameters: the damped
+step with the disparity block eliminated must equal the full normal-equation
+solve, and the iterations must drive the cost down."""
+import copy
+
+import numpy as np
+
+from tileproc import lma
+
+S, TX, TY = 4, 6, 5
+T = TX * TY
+
+
+class LinearProcessor:
+    """d = r0 + A e + b * (D - D0): the interface lma.refine uses."""
+
+    def __init__(self, rng):
+        self.tilesX, self.tilesY, self.num_sensors = TX, TY, S
+        self.A = rng.normal(size=(T, S * 4))
+        self.b = rng.uniform(0.5, 1.5, T)
+        self.r0 = rng.normal(size=T)
+        self.D0 = rng.uniform(1, 3, T)
+        self.g = None
+        self.D = None
+
+    def _e(self):
+        return np.array([self.g[k][s] for s in range(S) for k in lma.KEYS])
+
+    def setGeometry(self, g):
+        self.g = copy.deepcopy(g)
+
+    def setFullFrameImages(self, D, tile_op=None):
+        self.D = np.asarray(D, np.float64)
+
+    def process(self):
+        self.d = self.r0 + self.A @ self._e() + self.b * (self.D - self.D0)
+
+    def getDisparity(self):
+        out = np.full((T, 9), np.nan, np.float32)
+        out[:, 1] = self.d
+        return out
+
+    def backward(self):
+        return None
+
+    def getDisparityJacobian(self):
+        return (self.A.reshape(T, S, 4).astype(np.float32), self.b.astype(np.float32), self.d.astype(np.float32))
+
+
+def _geom():
+    return {k: [0.0] * S for k in lma.KEYS}
+
+
+def test_step_equals_full_normal_equations():
+    rng = np.random.default_rng(1)
+    tp = LinearProcessor(rng)
+    lam = 0.3
+    g0, D0 = _geom(), tp.D0.copy()
+    g1, D1, hist = lma.refine(tp, g0, D0, iterations=1, lam=lam)
+    # full system: [A b] with damping lam * diag(J^T J)
+    J = np.concatenate([tp.A, np.diag(tp.b)], axis=1)
+    r = tp.r0
+    JtJ = J.T @ J
+    step = np.linalg.solve(JtJ + lam * np.diag(np.diag(JtJ)), -J.T @ r)
+    de = np.array([g1[k][s] for s in range(S) for k in lma.KEYS])
+    assert np.allclose(de, step[:S * 4], atol=2e-5)
+    assert np.allclose(D1 - D0, step[S * 4:], atol=2e-5)
+    assert hist[1] < hist[0]
+
+
+def test_iterations_reduce_cost_fixed_disparity():
+    rng = np.random.default_rng(2)
+    tp = LinearProcessor(rng)
+    g, D, hist = lma.refine(tp, _geom(), tp.D0.copy(), iterations=8, free_disparity=False)
+    assert all(b <= a for a, b in zip(hist, hist[1:]))
+    e = np.array([g[k][s] for s in range(S) for k in lma.KEYS])
+    best = np.linalg.lstsq(tp.A, -tp.r0, rcond=None)[0]
+    assert np.allclose(e, best, atol=1e-3)
