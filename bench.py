@@ -57,6 +57,9 @@ def parse_args():
     p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(CONFIGS))
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint / LM measurement")
+    p.add_argument("--adjoint-only", action="store_true",
+                   help="only the 16-sensor forward / forward+adjoint / LM measurement (profiling)")
     p.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles per CPU sample (0 = auto)")
     return p.parse_args()
 
@@ -252,6 +255,67 @@ def run_reference(args):
     return 0
 
 
+def measure_fwd_adjoint(seed, steps, warmup, lma_iterations=20):
+    """16-sensor LWIR scene (640x512, 5120 tiles, 120 pairs): forward (ports + fused forward)
+    vs forward + adjoint (tp_backward: plan with FP64 port derivatives, adjoint kernel,
+    Jacobian contraction), CUDA events on the launch stream; then 20 LM iterations on the
+    analytic Jacobian from extrinsics perturbed by N(0, 3e-3) rad."""
+    import copy
+    import torch
+    from tileproc import GPUTileProcessor, lma
+    w = make_workload("c3_lwir_16x640x512", seed)
+    sc = w["scene"]
+    T, S = w["T"], w["S"]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = C.c_void_p(stream.cuda_stream)
+    rng = np.random.default_rng(seed + 11)
+    g0 = copy.deepcopy(sc["geometry"])
+    for k in lma.KEYS:
+        g0[k] = (np.asarray(g0[k]) + rng.normal(0, 3e-3, S)).tolist()
+    D = sc["disparity_gt"].reshape(-1).astype(np.float32)
+    tp = GPUTileProcessor(S, w["W"], w["H"])
+    try:
+        tp.setGeometry(g0)
+        tp.setBayerImages(sc["images"])
+        tp.setCorrelation(pairs=w["pairs"])
+        tp.setFullFrameImages(D, tile_op=np.ones(T, np.int32))
+        lib = tp._lib
+
+        def fwd():
+            tp._ck(lib.tp_ports(tp.h, sptr), "ports")
+            tp._ck(lib.tp_process(tp.h, sptr), "process")
+
+        def fwd_adj():
+            fwd()
+            tp._ck(lib.tp_backward(tp.h, None, None, None, sptr), "backward")
+
+        out = {"workload": "c3_lwir_16x640x512", "tiles": T, "pairs": w["P"]}
+        for name, fn in (("fwd", fwd), ("fwd_adjoint", fwd_adj)):
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            out[name + "_ms"] = ms
+            out[name + "_tiles_per_s"] = T / (ms / 1000.0)
+        out["adjoint_over_fwd"] = out["fwd_adjoint_ms"] / out["fwd_ms"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, hist = lma.refine(tp, g0, D, iterations=lma_iterations)
+        out["lma"] = {"iterations": lma_iterations, "cost_start": hist[0], "cost_end": hist[-1],
+                      "seconds": time.perf_counter() - t0,
+                      "start": "extrinsics + N(0, 3e-3) rad, target disparity = scene truth"}
+    finally:
+        tp.close()
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -368,6 +432,11 @@ def run_ours(args):
         e2e_t = float(t.item())
     e2e_val = world * T * args.steps / e2e_t
 
+    fwd_adj = None
+    if rank == 0 and not args.no_adjoint:
+        fwd_adj = measure_fwd_adjoint(args.seed, max(3, args.steps // 2), args.warmup)
+        torch.cuda.set_stream(stream)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -397,6 +466,7 @@ def run_ours(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "fwd_adjoint": fwd_adj,
     }
     tp.close()
     if rank == 0:
@@ -408,6 +478,13 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.adjoint_only:
+        import torch
+        import build as tp_build
+        tp_build.build()
+        torch.cuda.set_device(0)
+        print(json.dumps(measure_fwd_adjoint(args.seed, args.steps, args.warmup)))
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -21,16 +21,17 @@
 // derivatives of the plan (azimuth, tilt, roll, zoom, disparity) into the
 // per-tile Jacobian rows and the gradient of a per-tile loss.
 //
-// GB300 layout: warp per tile as in the forward kernel.  Per warp the tile's
-// CLT [S][256] (read back from HBM or recomputed from the image), its
-// gradient [S][256], and small surface / quadrant buffers live in shared
-// memory; pairs are processed in order by the one warp, so the gradient
-// accumulates without atomics.
+// GB300 layout: one CTA of four warps per tile.  The tile's CLT [S][256]
+// (read back from HBM or recomputed from the image) and its gradient [S][256]
+// live in shared memory; warp 0 takes the centroid of the combined strip the
+// forward kernel kept; then the warps split the pairs, each running a pair's
+// reverse chain in registers and per-warp buffers (the transposed DCT-IIe is
+// the transposed butterfly of the forward one) and adding into the gradient
+// with shared-memory atomics; finally they split the sensors for the
+// forward-mode shift derivatives.
 #include "tp_dtt.cuh"
 
 namespace {
-
-__constant__ float k_t2e[2][64];  // DCT-IIe / DST-IIe as matrices, y = T x (T[k][n] at k * 8 + n)
 
 constexpr float K16 = 0.19634954084936207f;  // pi / 16
 
@@ -141,24 +142,50 @@ __device__ __forceinline__ float strip_entry(const float *c, const short *strip_
 
 }  // namespace
 
-__global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ SceneDev sc,
-                                                     const __grid_constant__ AdjShape as,
-                                                     const __grid_constant__ CorrConst cfg, float *sens,
-                                                     float *dval) {
+constexpr int AD_NW = 4;  // warps per tile
+
+// x = T^T y for the DCT-IIe / DST-IIe of dtt2e_fast (its transposed data flow)
+__device__ __forceinline__ void dtt2e_transposed(const float y[8], float x[8], bool sine) {
+  const float S = 0.5f;
+  const float C4 = 0.7071067811865476f, C8 = 0.9238795325112867f, C38 = 0.3826834323650898f;
+  float t[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) t[k] = sine ? y[7 - k] : y[k];
+  float u1[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    u1[j] = fmaf(k_dct2e[8 + j], t[1], fmaf(k_dct2e[24 + j], t[3], fmaf(k_dct2e[40 + j], t[5], k_dct2e[56 + j] * t[7])));
+  const float a0 = S * t[0] + (S * C4) * t[4], a1 = S * t[0] - (S * C4) * t[4];
+  const float b0 = S * fmaf(C8, t[2], C38 * t[6]), b1 = S * fmaf(C38, t[2], -C8 * t[6]);
+  const float u0[4] = {a0 + b0, a1 + b1, a1 - b1, a0 - b0};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    x[j] = u0[j] + u1[j];
+    x[7 - j] = u0[j] - u1[j];
+  }
+  if (sine) {
+#pragma unroll
+    for (int n = 1; n < 8; n += 2) x[n] = -x[n];
+  }
+}
+
+__global__ void __launch_bounds__(32 * AD_NW) adjoint_kernel(const __grid_constant__ SceneDev sc,
+                                                             const __grid_constant__ AdjShape as,
+                                                             const __grid_constant__ CorrConst cfg, float *sens,
+                                                             float *dval) {
   extern __shared__ float sm[];
-  const int lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
+  __shared__ float s_d;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = lane >> 3, r = lane & 7;
   const int S = as.S, P = as.P, RE = as.RE;
   float *s_clt = sm;                  // [S][256]
   float *s_g = s_clt + S * TP_CLT;    // [S][256] dd/dCLT
-  float *gs = s_g + S * TP_CLT;       // [240] dd/dsurface of the current pair
+  float *gcmb = s_g + S * TP_CLT;     // [240] dd/dcombo
+  float *gG = gcmb + 240;             // [240] combo + offset
+  float *gs = gG + 240 + warp * 816;  // per warp: [240] dd/dsurface of the current pair
   float *qb = gs + 240;               // [4][72] quadrant buffer
   float *tb = qb + 288;               // [4][72] transpose buffer
-  float *gcmb = tb + 288;             // [240] dd/dcombo
-  float *gG = gcmb + 240;             // [240] combo + offset
   const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
   const int groups = (S + 3) >> 2;
-  const bool log_mode = cfg.log_combine;
-  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
   const float inv_n = 1.0f / cfg.num_combo;
 
   for (int task = blockIdx.x; task < sc.num_tasks; task += gridDim.x) {
@@ -166,7 +193,7 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
     const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
     // ---------------- the tile's CLT ----------------
     if (as.recompute) {
-      for (int g = 0; g < groups; g++) {
+      for (int g = warp; g < groups; g += AD_NW) {
         const int s = g * 4 + q;
         const int sidx = s < S ? s : S - 1;
         const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
@@ -189,44 +216,18 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
       }
     } else {
       const float4 *src = (const float4 *)(sc.clt + tile * S * TP_CLT);
-      for (int i = lane; i < S * 64; i += 32) ((float4 *)s_clt)[i] = __ldg(src + i);
+      for (int i = tid; i < S * 64; i += 32 * AD_NW) ((float4 *)s_clt)[i] = __ldg(src + i);
     }
-    for (int i = lane; i < S * TP_CLT; i += 32) s_g[i] = 0.f;
-    __syncwarp();
+    for (int i = tid; i < S * TP_CLT; i += 32 * AD_NW) s_g[i] = 0.f;
 
-    // ---------------- forward strips, combination and centroid ----------------
-    float cmb[8];
-#pragma unroll
-    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
-    for (int pi = 0; pi < P; pi++) {
-      const PairDev pd = cfg.pairs[pi];
-      if (!pd.in_combo) continue;
-      const float *c = sc.corr + (tile * P + pi) * TP_CORR;
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int e = lane + 32 * t;
-        if (e < RE) {
-          float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
-          if (v < 0.0f) v = 0.0f;
-          if (log_mode) cmb[t] += logf(v);
-          else cmb[t] *= cfg.twice_diagonal ? v * v : v;
-        }
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-      const int e = lane + 32 * t;
-      if (e < RE) {
-        float v = cmb[t];
-        if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
-        else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
-        gG[e] = v;
+    // ---------------- centroid of the forward's combined strip, and dd/dcombo ----------------
+    if (warp == 0) {
+      for (int e = lane; e < 240; e += 32) {
+        gG[e] = (e < RE) ? sc.combo[tile * RE + e] : 0.f;
         gcmb[e] = 0.f;
       }
-    }
-    __syncwarp();
-    float dres = CUDART_NAN_F;
-    {
+      __syncwarp();
+      float dres = CUDART_NAN_F;
       const float v = (lane < 15) ? gG[lane] : CUDART_NAN_F;
       float best = isnan(v) ? -CUDART_INF_F : v;
       int bi = lane < 15 ? lane : 99;
@@ -278,22 +279,22 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
           }
         }
       }
+      __syncwarp();
+      // G = combo + offset, the geometric mean the strip entries enter
+      for (int e = lane; e < RE; e += 32) gG[e] = gG[e] + cfg.corr_offset;
+      if (lane == 0) s_d = dres;
     }
-    __syncwarp();
+    __syncthreads();
+    const float dres = s_d;
     if (isnan(dres)) {
-      if (lane == 0) dval[tile] = CUDART_NAN_F;
-      for (int i = lane; i < 2 * S; i += 32) sens[tile * 2 * S + i] = 0.f;
+      if (tid == 0) dval[tile] = CUDART_NAN_F;
+      for (int i = tid; i < 2 * S; i += 32 * AD_NW) sens[tile * 2 * S + i] = 0.f;
+      __syncthreads();
       continue;
     }
-#pragma unroll
-    for (int t = 0; t < 8; t++) {  // G = combo + offset, the geometric mean the strip entries enter
-      const int e = lane + 32 * t;
-      if (e < RE) gG[e] = gG[e] + cfg.corr_offset;
-    }
-    __syncwarp();
 
-    // ---------------- reverse pass over the pairs ----------------
-    for (int pi = 0; pi < P; pi++) {
+    // ---------------- reverse pass over the pairs, AD_NW pairs at a time ----------------
+    for (int pi = warp; pi < P; pi += AD_NW) {
       const PairDev pd = cfg.pairs[pi];
       if (!pd.in_combo) continue;
       const float *c = sc.corr + (tile * P + pi) * TP_CORR;
@@ -302,30 +303,26 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
       __syncwarp();
       // strip entries: d combo / d v_p = G / (n v_p) for the geometric mean of n pairs
       bool any = false;
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int e = lane + 32 * t;
-        if (e < RE && gcmb[e] != 0.f) {
-          const float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
-          if (v > 0.0f) {
-            const float f = gcmb[e] * gG[e] * inv_n / v;
-            const int row = e / 15;
-            const float half = row > 0 ? 0.5f : 1.0f;
-            for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
-              int idx[4];
-              float wt[4];
-              int n;
-              if (pd.kind <= 3) {
-                const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
-                n = code_taps(side ? code.y : code.x, idx, wt);
-              } else {
-                n = general_taps(pd.bx, pd.by, row, e - row * 15 - 7, side ? 1 : -1, idx, wt);
-              }
-              for (int k = 0; k < n; k++) atomicAdd(&gs[idx[k]], f * half * wt[k]);
-            }
-            any = true;
+      for (int e = lane; e < RE; e += 32) {
+        if (gcmb[e] == 0.f) continue;
+        const float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
+        if (!(v > 0.0f)) continue;
+        const float f = gcmb[e] * gG[e] * inv_n / v;
+        const int row = e / 15;
+        const float half = row > 0 ? 0.5f : 1.0f;
+        for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
+          int idx[4];
+          float wt[4];
+          int n;
+          if (pd.kind <= 3) {
+            const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+            n = code_taps(side ? code.y : code.x, idx, wt);
+          } else {
+            n = general_taps(pd.bx, pd.by, row, e - row * 15 - 7, side ? 1 : -1, idx, wt);
           }
+          for (int k = 0; k < n; k++) atomicAdd(&gs[idx[k]], f * half * wt[k]);
         }
+        any = true;
       }
       if (!__any_sync(0xffffffffu, any)) continue;
       __syncwarp();
@@ -345,31 +342,18 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
       __syncwarp();
       // 2D DCT-IIe/DST-IIe transposed: forward Z = Ta X^T Tb^T, so Xbar = Tb^T Zbar^T Ta
       {
-        const float *Ta = k_t2e[(q >> 1) & 1], *Tb = k_t2e[q & 1];
         float z[8], v[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) z[k] = qb[q * 72 + k * 9 + r];  // column r of Zbar
+        dtt2e_transposed(z, v, (q >> 1) & 1);                        // row r of V = Zbar^T Ta
 #pragma unroll
-        for (int n = 0; n < 8; n++) {
-          float s = 0.f;
-#pragma unroll
-          for (int k = 0; k < 8; k++) s = fmaf(Ta[k * 8 + n], z[k], s);
-          v[n] = s;
-        }
-#pragma unroll
-        for (int n = 0; n < 8; n++) tb[q * 72 + r * 9 + n] = v[n];  // row r of V = Zbar^T Ta
+        for (int n = 0; n < 8; n++) tb[q * 72 + r * 9 + n] = v[n];
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < 8; k++) z[k] = tb[q * 72 + k * 9 + r];  // column r of V
+        dtt2e_transposed(z, v, q & 1);                               // column r of Xbar
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-          float s = 0.f;
-#pragma unroll
-          for (int j = 0; j < 8; j++) s = fmaf(Tb[j * 8 + k], z[j], s);
-          v[k] = s;
-        }
-#pragma unroll
-        for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];  // Xbar[k][r]
+        for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];
         __syncwarp();
       }
       // LPF and the fat-zero normalised product (correlateSingleColorFD)
@@ -391,7 +375,7 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
       }
       const float fzz = cfg.fat_zero * cfg.fat_zero;
       const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
-      float tg[4][2], dbar[2], sw[2];
+      float tg[4][2], dbar[2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const int idx = lane + 32 * h;
@@ -400,15 +384,15 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
         float gq[4];
 #pragma unroll
         for (int qq = 0; qq < 4; qq++) gq[qq] = qb[qq * 72 + off] * l;
-        sw[h] = 1.0f / (a2[h] + fz2);
+        const float sw = 1.0f / (a2[h] + fz2);
         const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
         const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
         const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
         const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
         const float swbar = gq[0] * t0 + gq[1] * t1 + gq[2] * t2 + gq[3] * t3;
-        dbar[h] = -swbar * sw[h] * sw[h];
+        dbar[h] = -swbar * sw * sw;
 #pragma unroll
-        for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq] * sw[h];
+        for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq] * sw;
       }
       const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
 #pragma unroll
@@ -430,15 +414,16 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
         const float k2 = a2[h] > 0.f ? a2bar * s1v[h] / a2[h] : 0.f;
 #pragma unroll
         for (int m = 0; m < 4; m++) {
-          s_g[pd.cam1 * TP_CLT + m * 64 + idx] += fmaf(k1, d1[m][h], g1[m]);
-          s_g[pd.cam2 * TP_CLT + m * 64 + idx] += fmaf(k2, d2[m][h], g2[m]);
+          atomicAdd(&s_g[pd.cam1 * TP_CLT + m * 64 + idx], fmaf(k1, d1[m][h], g1[m]));
+          atomicAdd(&s_g[pd.cam2 * TP_CLT + m * 64 + idx], fmaf(k2, d2[m][h], g2[m]));
         }
       }
       __syncwarp();
     }
+    __syncthreads();
 
     // ---------------- dd/drx, dd/dry per sensor (forward mode on the CLT) ----------------
-    for (int g = 0; g < groups; g++) {
+    for (int g = warp; g < groups; g += AD_NW) {
       const int s = g * 4 + q;
       const int sidx = s < S ? s : S - 1;
       const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
@@ -495,8 +480,8 @@ __global__ void __launch_bounds__(32) adjoint_kernel(const __grid_constant__ Sce
         sens[(tile * S + s) * 2 + 1] = gy;
       }
     }
-    if (lane == 0) dval[tile] = dres;
-    __syncwarp();
+    if (tid == 0) dval[tile] = dres;
+    __syncthreads();
   }
 }
 
@@ -558,23 +543,16 @@ __global__ void adjoint_final_kernel(const float *partial, int nblocks, int n, f
 cudaError_t upload_adjoint_constants() {
   cudaError_t e = upload_dtt_constants();
   if (e != cudaSuccess) return e;
-  // DCT-IIe: T[k][n] = 0.5 cos(pi k (2n+1) / 16); DST-IIe: S[j][n] = (-1)^n T[7-j][n]
-  float t[2][64];
-  const double pi = 3.14159265358979323846;
-  for (int k = 0; k < 8; k++)
-    for (int n = 0; n < 8; n++) t[0][k * 8 + n] = (float)(0.5 * std::cos(pi * k * (2 * n + 1) / 16.0));
-  for (int j = 0; j < 8; j++)
-    for (int n = 0; n < 8; n++) t[1][j * 8 + n] = ((n & 1) ? -1.f : 1.f) * t[0][(7 - j) * 8 + n];
-  return cudaMemcpyToSymbol(k_t2e, t, sizeof(t));
+  return cudaSuccess;
 }
 
-int adjoint_smem_bytes(int S) { return (S * 2 * TP_CLT + 240 + 288 + 288 + 240 + 240) * 4; }
+int adjoint_smem_bytes(int S) { return (S * 2 * TP_CLT + 240 + 240 + AD_NW * 816) * 4; }
 
 cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st) {
   if (sc.num_tasks <= 0) return cudaSuccess;
-  if (sc.num_colors != 1 || !sc.port_deriv) return cudaErrorInvalidValue;
+  if (sc.num_colors != 1 || !sc.port_deriv || !sc.combo) return cudaErrorInvalidValue;
   AdjShape as;
   as.S = sc.num_sensors;
   as.P = sc.num_pairs;
@@ -587,10 +565,10 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, 32, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, 32 * AD_NW, bytes);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   const int grid = sc.num_tasks < sms * per_sm ? sc.num_tasks : sms * per_sm;
-  adjoint_kernel<<<grid, 32, bytes, st>>>(sc, as, cc, sens, dval);
+  adjoint_kernel<<<grid, 32 * AD_NW, bytes, st>>>(sc, as, cc, sens, dval);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int nb = (sc.num_tasks + 255) / 256;

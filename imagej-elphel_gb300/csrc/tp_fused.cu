@@ -352,6 +352,7 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
         if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
         else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
         combo[e] = v;
+        if (sc.combo) sc.combo[tile * RE + e] = v;  // kept for the adjoint
       }
     }
     __syncwarp();

@@ -40,6 +40,7 @@ struct tp_handle {
   double *d_rdist = nullptr;
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
+  float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
   float *d_partial = nullptr, *d_grad_e = nullptr, *d_dldd = nullptr;
@@ -118,6 +119,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.rbg = h->d_rbg;
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
   sc.corr_cfg = h->d_corr_cfg;
+  sc.combo = h->d_combo;
   sc.tex = h->d_tex;
   sc.tex_aux = h->tex_params.aux ? h->d_tex_aux : nullptr;
   sc.num_pairs = h->num_pairs;
@@ -386,7 +388,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd};
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -615,6 +617,10 @@ tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pair
       return fail(h, TP_ERR_NOMEM, "tp_set_corr: correlation buffer");
     }
     h->corr_capacity = np;
+  }
+  if (!h->d_combo && dalloc(&h->d_combo, (size_t)h->ntiles * TP_MAX_STRIP * 15) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, TP_ERR_NOMEM, "tp_set_corr: combined strip buffer");
   }
   CK(cudaMemcpy(h->d_corr_cfg, &cd, sizeof(cd), cudaMemcpyHostToDevice), "tp_set_corr");
   h->num_pairs = np;

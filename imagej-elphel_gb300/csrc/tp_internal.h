@@ -101,6 +101,7 @@ struct SceneDev {
   float *rbg;                // [S][C][H+8][W+8]
   const float *lpf_rbg;      // [C][64] or null
   const CorrDev *corr_cfg;
+  float *combo;              // [tiles][RE] combined strip rows the extraction reads, or null
   float *tex;                // [tiles][rows][256] texture tiles (R, B, G, alpha[, 4 weights, 4 rms])
   float *tex_aux;            // [tiles][16] max_diff[4], ports_rgb[12] or null
   int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
