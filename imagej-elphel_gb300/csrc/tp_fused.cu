@@ -158,6 +158,309 @@ struct FwdShape {
 // ---------------------------------------------------------------------------
 // the fused kernel: one warp carries a tile through all stages, no CTA barriers
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// the three phases of the forward for one tile, shared by the schedules
+// ---------------------------------------------------------------------------
+// phase A item gt = (colour, group of 4 sensors): lanes 8q..8q+7 own sensor 4g+q
+template <int C>
+__device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task, size_t tile, int gt, int groups,
+                                             float *s_clt, float *scr, int lane) {
+  const int q = lane >> 3, r = lane & 7;
+  const int rr = sc.bayer_red_row, rc = sc.bayer_red_col;
+  const int c = gt / groups, g = gt - c * groups;
+  const int s = g * 4 + q;
+  const bool act = s < S;
+  const int sidx = act ? s : S - 1;
+  const SubtilePlan p = sc.plan[((size_t)task * S + sidx) * C + c];
+  Win w;
+  w.img = sc.images[sidx];
+  w.pitch = sc.img_pitch;
+  w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
+  w.u16 = sc.img_dtype[sidx];
+  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
+  w.scale = sc.color_scale[c];
+  float o[4][8];
+  float *tbuf = scr + q * 72;
+  float sg0 = 1.f, sg1 = 1.f;  // symmetry signs kept for the correlation reads
+  if (C == 1) {
+    subtile_clt<0>(w, p.rx, p.ry, 0, 0, 0, r, tbuf, o);
+  } else if (c < 2) {
+    const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
+    subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
+    sg0 = pc ? -1.f : 1.f;
+    sg1 = pr ? -1.f : 1.f;
+  } else {
+    const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
+    subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
+    sg0 = pg ? -1.f : 1.f;
+  }
+  const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
+  conv_shift(o, kp, p.rx, p.ry, r);
+  if (act) {
+    float *gdst = sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+      *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+    }
+    // all four quadrants: after the convolution and the shift the Bayer symmetries no longer hold
+    float *sdst = s_clt + ((size_t)s * C + c) * TP_CLT + r * 8;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      *(float4 *)(sdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+      *(float4 *)(sdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+    }
+  }
+  (void)sg0;
+  (void)sg1;
+}
+
+// phase B for pair pi: correlation surface to HBM, strip entries folded into cmb
+template <int C>
+__device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, size_t tile, int P, int pi, int RE,
+                                         bool log_mode, const short *strip_code, const float *s_clt, float *scr,
+                                         int lane, float cmb[8]) {
+  const int q = lane >> 3, r = lane & 7;
+  float *qb = scr, *tb = scr + 288;
+  const PairDev pd = cfg.pairs[pi];
+  const float *c1 = s_clt + (size_t)pd.cam1 * C * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * C * TP_CLT;
+  float acc[4][2];
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    float d1[4][2], d2[4][2], a2[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        d1[m][h] = c1[c * TP_CLT + m * 64 + lane + 32 * h];
+        d2[m][h] = c2[c * TP_CLT + m * 64 + lane + 32 * h];
+        s1 = fmaf(d1[m][h], d1[m][h], s1);
+        s2 = fmaf(d2[m][h], d2[m][h], s2);
+      }
+      a2[h] = sqrtf(s1 * s2);
+    }
+    const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * cfg.fat_zero * cfg.fat_zero;
+    const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const float sw = wgt / (a2[h] + fz2);
+      const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
+      const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
+      const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
+      const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
+      if (c == 0) {
+        acc[0][h] = t0 * sw; acc[1][h] = t1 * sw; acc[2][h] = t2 * sw; acc[3][h] = t3 * sw;
+      } else {
+        acc[0][h] = fmaf(t0, sw, acc[0][h]); acc[1][h] = fmaf(t1, sw, acc[1][h]);
+        acc[2][h] = fmaf(t2, sw, acc[2][h]); acc[3][h] = fmaf(t3, sw, acc[3][h]);
+      }
+    }
+  }
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int idx = lane + 32 * h;
+    const float l = cfg.lpf[idx];
+    const int off = (idx >> 3) * 9 + (idx & 7);
+#pragma unroll
+    for (int qq = 0; qq < 4; qq++) qb[qq * 72 + off] = acc[qq][h] * l;
+  }
+  __syncwarp();
+  {
+    float x[8], y[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) x[e] = qb[q * 72 + r * 9 + e];
+    dtt2e_fast(x, y, (q >> 1) & 1);
+#pragma unroll
+    for (int j = 0; j < 8; j++) tb[q * 72 + j * 9 + r] = y[j];
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 8; e++) x[e] = tb[q * 72 + r * 9 + e];
+    dtt2e_fast(x, y, q & 1);
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 8; e++) qb[q * 72 + r * 9 + e] = y[e];
+  }
+  __syncwarp();
+  // 15x15 unfold (DttRad2.corr_unfold_tile): each lane owns 2 cells (a, b) and writes their mirror images
+  float *cs = tb;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int a = (lane >> 3) + 4 * k, b = lane & 7;
+    const float A = qb[a * 9 + b];
+    const float B = b ? qb[72 + a * 9 + b - 1] : 0.f;
+    const float Cc = a ? qb[144 + (a - 1) * 9 + b] : 0.f;
+    const float D = (a && b) ? qb[216 + (a - 1) * 9 + b - 1] : 0.f;
+    cs[(7 + a) * 15 + 7 + b] = 0.25f * (((A + B) + Cc) + D);
+    if (b) cs[(7 + a) * 15 + 7 - b] = 0.25f * (((A - B) + Cc) - D);
+    if (a) cs[(7 - a) * 15 + 7 + b] = 0.25f * (((A + B) - Cc) - D);
+    if (a && b) cs[(7 - a) * 15 + 7 - b] = 0.25f * (((A - B) - Cc) + D);
+  }
+  __syncwarp();
+  float *gc = sc.corr + (tile * P + pi) * TP_CORR;
+  for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
+  if (pd.in_combo) {
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int e = lane + 32 * t;
+      if (e < RE) {
+        const int row = e / 15;
+        float d;
+        if (pd.kind <= 3) {
+          const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+          d = sample_code(cs, code.x);
+          if (row > 0) {
+            const float d2 = sample_code(cs, code.y);
+            d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+          }
+        } else {
+          const int scol = e - row * 15 - 7;
+          d = strip_sample(cs, 4, pd.bx, pd.by, row, scol, -1);
+          if (row > 0) {
+            const float d2 = strip_sample(cs, 4, pd.bx, pd.by, row, scol, 1);
+            d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
+          }
+        }
+        float v = d + cfg.corr_offset;
+        if (v < 0.0f) v = 0.0f;
+        if (log_mode) cmb[t] += logf(v);
+        else cmb[t] *= cfg.twice_diagonal ? v * v : v;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// phase C: combined strip, integer argmax, centroid, ortho maxima, disparity record
+__device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
+                                            bool log_mode, int ncomb, size_t tile, float *scr, int lane,
+                                            const float cmb[8]) {
+  // ---------------- stage 3c: extraction ----------------
+  float *combo = scr;
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    const int e = lane + 32 * t;
+    if (e < RE) {
+      float v = cmb[t];
+      if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
+      else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
+      combo[e] = v;
+      if (sc.combo) sc.combo[tile * RE + e] = v;  // kept for the adjoint
+    }
+  }
+  __syncwarp();
+  float res[TP_NDISP];
+#pragma unroll
+  for (int k = 0; k < TP_NDISP; k++) res[k] = (k == 2 || k == 4 || k == 6) ? 0.f : CUDART_NAN_F;
+  {
+    // integer argmax on row 0 (getMaxXYInt): first maximum over the non-NaN entries
+    const float v = (lane < 15) ? combo[lane] : CUDART_NAN_F;
+    float best = isnan(v) ? -CUDART_INF_F : v;
+    int bi = lane < 15 ? lane : 99;
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const unsigned finite = __ballot_sync(0xffffffffu, lane < 15 && !isnan(v));
+    const int imx = finite ? bi : 14;
+    const float vmax = combo[imx];
+    if (vmax >= cfg.min_corr) {
+      const int ix = imx - 7;
+      res[0] = (float)(-ix);
+      res[2] = vmax;
+      res[8] = (float)ix;
+      int dh = cfg.strip_rows;
+      float wys = 1.0f;
+      if (dh > cfg.wndy_size) dh = cfg.wndy_size;
+      else if (dh < cfg.wndy_size) {
+        float swy = cfg.wndy[0];
+        for (int i = 1; i < dh; i++) swy += cfg.wndy[i];
+        wys = 1.0f / swy;
+      }
+      float s0 = 0.f, sx = 0.f;
+      const int x0 = 7 + ix, nk = dh * 2 * cfg.wndx_size;
+      for (int k = lane; k < nk; k += 32) {  // windowed centroid (getMaxXCm), one sample per lane
+        const int dy = k / (2 * cfg.wndx_size), rest = k - dy * 2 * cfg.wndx_size;
+        const int adx = rest >> 1, dir = (rest & 1) ? 1 : -1, odd = dy & 1;
+        if (((adx - odd) & 1) || (adx == 0 && dir < 0)) continue;
+        const int idx = (adx * dir) >> 1, xx = 2 * idx + odd, x1 = x0 + idx;
+        if (x1 < 0 || x1 >= 15) continue;
+        float d = combo[dy * 15 + x1];
+        if (isnan(d) || !(d > 0.0f)) continue;
+        d *= (((dy == 0) ? wys : 2.0f * wys) * cfg.wndy[dy]) * cfg.wndx[adx];
+        s0 += d;
+        sx += d * xx;
+      }
+      s0 = warp_sum(s0);
+      sx = warp_sum(sx);
+      if (s0 != 0.0f) {
+        res[1] = -(ix + sx / s0 / 2);
+        res[7] = s0;
+      }
+    }
+  }
+  if (quad && (cfg.num_hor > 0 || cfg.num_vert > 0)) {
+    // getMaxXSOrtho: lanes 0-14 horizontal pairs, lanes 16-30 vertical pairs
+    // the surfaces of this tile were just written by this warp (L1/L2 resident)
+    const int half = lane >> 4, j = lane & 15;
+    const int np = half ? cfg.num_vert : cfg.num_hor;
+    float sum = -CUDART_INF_F;
+    if (j < 15 && np > 0) {
+      sum = 0.f;
+      for (int i = 0; i < 15; i++) {
+        float prod = 1.f;
+        for (int k = 0; k < np; k++) {
+          const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
+          const float d = half ? 0.5f * (cc[j * 15 + i] + cc[j * 15 + 14 - i])
+                               : 0.5f * (cc[i * 15 + j] + cc[(14 - i) * 15 + j]);
+          prod *= d + cfg.corr_offset;
+        }
+        const float v = (prod > 0.0f) ? ((np == 2) ? sqrtf(prod) : ((np == 1) ? prod : powf(prod, 1.0f / np))) -
+                                            cfg.corr_offset
+                                      : -cfg.corr_offset;
+        sum += v * cfg.notch[i];
+      }
+    }
+    float best = sum;
+    int bi = (j < 15) ? j : 99;
+#pragma unroll
+    for (int o2 = 8; o2 > 0; o2 >>= 1) {  // within each 16-lane half
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int ic = bi, base = half << 4;
+    const float f0 = __shfl_sync(0xffffffffu, sum, base + (ic > 0 ? ic - 1 : 0));
+    const float f1 = __shfl_sync(0xffffffffu, sum, base + ic);
+    const float f2 = __shfl_sync(0xffffffffu, sum, base + (ic < 14 ? ic + 1 : 14));
+    float xc = (float)ic;
+    if (ic > 0 && ic < 14) {
+      const float den = f0 - 2.0f * f1 + f2;
+      if (den != 0.0f) xc = ic + 0.5f * (f0 - f2) / den;
+    }
+    int ir = (int)floorf(xc + 0.5f);
+    ir = ir < 0 ? 0 : (ir > 14 ? 14 : ir);
+    const float fr = __shfl_sync(0xffffffffu, sum, base + ir);
+    const float hx = __shfl_sync(0xffffffffu, xc, 0), hs = __shfl_sync(0xffffffffu, fr, 0);
+    const float vx = __shfl_sync(0xffffffffu, xc, 16), vs = __shfl_sync(0xffffffffu, fr, 16);
+    if (cfg.num_hor > 0) { res[3] = -(hx - 7.0f); res[4] = hs / 8.0f; }
+    if (cfg.num_vert > 0) { res[5] = -(vx - 7.0f); res[6] = vs / 8.0f; }
+  }
+  float *dm = sc.disp + tile * TP_NDISP;
+  if (lane < TP_NDISP) {
+    float v = res[0];
+#pragma unroll
+    for (int k = 1; k < TP_NDISP; k++) if (lane == k) v = res[k];
+    dm[lane] = v;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// warp-per-tile schedule: one warp carries a tile through all stages, no CTA barriers
+// ---------------------------------------------------------------------------
 template <int C>  // colours: 1 (mono) or 3 (Bayer R, B, G)
 __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_constant__ SceneDev sc,
                                                                const __grid_constant__ FwdShape fs,
@@ -170,300 +473,223 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
   float *scr = s_clt + fs.clt_floats;
   const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
   const int groups = (S + 3) >> 2;
-  const int q = lane >> 3, r = lane & 7;
   const bool log_mode = cfg.log_combine;
   const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
-  const int rr = sc.bayer_red_row, rc = sc.bayer_red_col;
-
   for (int task = blockIdx.x * NW + warp; task < sc.num_tasks; task += gridDim.x * NW) {
     const int txy = sc.task_txy[task];
     const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-    // ---------------- stage 2: CLT of every (sensor, colour) ----------------
-    for (int gt = 0; gt < C * groups; gt++) {
-      const int c = gt / groups, g = gt - c * groups;
-      const int s = g * 4 + q;
-      const bool act = s < S;
-      const int sidx = act ? s : S - 1;
-      const SubtilePlan p = sc.plan[((size_t)task * S + sidx) * C + c];
-      Win w;
-      w.img = sc.images[sidx];
-      w.pitch = sc.img_pitch;
-      w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
-      w.u16 = sc.img_dtype[sidx];
-      w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
-      w.scale = sc.color_scale[c];
-      float o[4][8];
-      float *tbuf = scr + q * 72;
-      float sg0 = 1.f, sg1 = 1.f;  // symmetry signs kept for the correlation reads
-      if (C == 1) {
-        subtile_clt<0>(w, p.rx, p.ry, 0, 0, 0, r, tbuf, o);
-      } else if (c < 2) {
-        const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
-        subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
-        sg0 = pc ? -1.f : 1.f;
-        sg1 = pr ? -1.f : 1.f;
-      } else {
-        const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
-        subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
-        sg0 = pg ? -1.f : 1.f;
-      }
-      const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
-      conv_shift(o, kp, p.rx, p.ry, r);
-      if (act) {
-        float *gdst = sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8;
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-          *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
-          *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
-        }
-        // all four quadrants: after the convolution and the shift the Bayer symmetries no longer hold
-        float *sdst = s_clt + ((size_t)s * C + c) * TP_CLT + r * 8;
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-          *(float4 *)(sdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
-          *(float4 *)(sdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
-        }
-      }
-      (void)sg0;
-      (void)sg1;
-    }
+    for (int gt = 0; gt < C * groups; gt++) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
     __syncwarp();
-    // ---------------- stage 3a/3b: pairs, strips ----------------
     float cmb[8];
 #pragma unroll
     for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
-    float *qb = scr, *tb = scr + 288;
-    for (int pi = 0; pi < P; pi++) {
-      const PairDev pd = cfg.pairs[pi];
-      const float *c1 = s_clt + (size_t)pd.cam1 * C * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * C * TP_CLT;
-      float acc[4][2];
+    for (int pi = 0; pi < P; pi++) fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+    fwd_extract(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pair-per-warp schedule: a CTA of nw warps per tile shares the tile's CLT; the
+// warps split the (colour, sensor-group) items, then the pairs, and warp 0
+// combines their partial strip products for the extraction.  For many pairs
+// (16 sensors, 120 pairs) this holds one CLT per CTA instead of one per warp.
+// ---------------------------------------------------------------------------
+template <int C>
+__global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_constant__ SceneDev sc,
+                                                          const __grid_constant__ FwdShape fs,
+                                                          const __grid_constant__ CorrConst cfg) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
+  float *s_clt = sm;
+  float *scr = sm + fs.clt_floats + warp * SCR;
+  float *part = sm + fs.clt_floats + NW * SCR;  // [NW][240] partial strip combinations
+  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+  const int groups = (S + 3) >> 2;
+  const bool log_mode = cfg.log_combine;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  for (int task = blockIdx.x; task < sc.num_tasks; task += gridDim.x) {
+    const int txy = sc.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+    for (int gt = warp; gt < C * groups; gt += NW) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
+    __syncthreads();
+    float cmb[8];
 #pragma unroll
-      for (int c = 0; c < C; c++) {
-        float d1[4][2], d2[4][2], a2[2];
+    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    for (int pi = warp; pi < P; pi += NW)
+      fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          float s1 = 0.f, s2 = 0.f;
+    for (int t = 0; t < 8; t++) {
+      const int e = lane + 32 * t;
+      if (e < RE) part[warp * 240 + e] = cmb[t];
+    }
+    __syncthreads();  // also makes the surfaces every warp wrote visible to warp 0
+    if (warp == 0) {
 #pragma unroll
-          for (int m = 0; m < 4; m++) {
-            d1[m][h] = c1[c * TP_CLT + m * 64 + lane + 32 * h];
-            d2[m][h] = c2[c * TP_CLT + m * 64 + lane + 32 * h];
-            s1 = fmaf(d1[m][h], d1[m][h], s1);
-            s2 = fmaf(d2[m][h], d2[m][h], s2);
-          }
-          a2[h] = sqrtf(s1 * s2);
+      for (int t = 0; t < 8; t++) {
+        const int e = lane + 32 * t;
+        if (e < RE) {
+          float v = part[e];
+          for (int w2 = 1; w2 < NW; w2++) v = log_mode ? v + part[w2 * 240 + e] : v * part[w2 * 240 + e];
+          cmb[t] = v;
         }
-        const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * cfg.fat_zero * cfg.fat_zero;
-        const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const float sw = wgt / (a2[h] + fz2);
-          const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
-          const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
-          const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
-          const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
-          if (c == 0) {
-            acc[0][h] = t0 * sw; acc[1][h] = t1 * sw; acc[2][h] = t2 * sw; acc[3][h] = t3 * sw;
-          } else {
-            acc[0][h] = fmaf(t0, sw, acc[0][h]); acc[1][h] = fmaf(t1, sw, acc[1][h]);
-            acc[2][h] = fmaf(t2, sw, acc[2][h]); acc[3][h] = fmaf(t3, sw, acc[3][h]);
-          }
-        }
       }
+      fwd_extract(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched persistent forward: one launch over many scenes of different sensor
+// counts, colours, pair sets and sizes.  The work is a queue of units in scene
+// order: a unit of a quad / colour scene is 4 tiles (one per warp, the
+// warp-per-tile path), a unit of a many-pair scene is 1 tile whose pairs the 4
+// warps split.  CTAs take units grid-stride; the scene of a unit is found by
+// binary search over the unit offsets; each scene's SceneDev and correlation
+// set-up are read from global memory.
+// ---------------------------------------------------------------------------
+constexpr int BATCH_MAX = 256;
+
+__global__ void disp_init_kernel(float *disp, int n);
+
+__device__ __forceinline__ bool scene_split(const SceneDev &sc) { return sc.num_colors == 1 && sc.num_pairs > 8; }
+
+template <int C>
+__device__ __forceinline__ void batch_warp_tile(const SceneDev &sc, int task, float *s_clt, float *scr, int lane) {
+  const CorrConst &cfg = *sc.corr_cfg;
+  const int S = sc.num_sensors, P = sc.num_pairs;
+  const int RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
+  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+  const int groups = (S + 3) >> 2;
+  const bool log_mode = cfg.log_combine;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  const int txy = sc.task_txy[task];
+  const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+  for (int gt = 0; gt < C * groups; gt++) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
+  __syncwarp();
+  float cmb[8];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int idx = lane + 32 * h;
-        const float l = cfg.lpf[idx];
-        const int off = (idx >> 3) * 9 + (idx & 7);
+  for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+  for (int pi = 0; pi < P; pi++) fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+  fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+}
+
+__global__ void __launch_bounds__(128, 4) fused_batch_kernel(const SceneDev *__restrict__ scenes,
+                                                            const int *__restrict__ unit_off, int nscenes,
+                                                            int total_units, int warp_floats) {
+  extern __shared__ float sm[];
+  __shared__ int s_off[BATCH_MAX + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i <= nscenes; i += blockDim.x) s_off[i] = unit_off[i];
+  __syncthreads();
+  for (int u = blockIdx.x; u < total_units; u += gridDim.x) {
+    int lo = 0, hi = nscenes - 1;  // last scene whose first unit is <= u
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_off[mid] <= u) lo = mid;
+      else hi = mid - 1;
+    }
+    const SceneDev &sc = scenes[lo];
+    const int lu = u - s_off[lo];
+    if (scene_split(sc)) {
+      const CorrConst &cfg = *sc.corr_cfg;
+      const int S = sc.num_sensors, P = sc.num_pairs, NW = 4;
+      const int RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
+      const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+      const int groups = (S + 3) >> 2;
+      const bool log_mode = cfg.log_combine;
+      const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+      float *s_clt = sm;
+      float *scr = sm + S * TP_CLT + warp * SCR;
+      float *part = sm + S * TP_CLT + NW * SCR;
+      const int task = lu;
+      const int txy = sc.task_txy[task];
+      const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+      for (int gt = warp; gt < groups; gt += NW) fwd_clt_item<1>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
+      __syncthreads();
+      float cmb[8];
 #pragma unroll
-        for (int qq = 0; qq < 4; qq++) qb[qq * 72 + off] = acc[qq][h] * l;
+      for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+      for (int pi = warp; pi < P; pi += NW)
+        fwd_pair<1>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int e = lane + 32 * t;
+        if (e < RE) part[warp * 240 + e] = cmb[t];
       }
-      __syncwarp();
-      {
-        float x[8], y[8];
-#pragma unroll
-        for (int e = 0; e < 8; e++) x[e] = qb[q * 72 + r * 9 + e];
-        dtt2e_fast(x, y, (q >> 1) & 1);
-#pragma unroll
-        for (int j = 0; j < 8; j++) tb[q * 72 + j * 9 + r] = y[j];
-        __syncwarp();
-#pragma unroll
-        for (int e = 0; e < 8; e++) x[e] = tb[q * 72 + r * 9 + e];
-        dtt2e_fast(x, y, q & 1);
-        __syncwarp();
-#pragma unroll
-        for (int e = 0; e < 8; e++) qb[q * 72 + r * 9 + e] = y[e];
-      }
-      __syncwarp();
-      // 15x15 unfold (DttRad2.corr_unfold_tile): each lane owns 2 cells (a, b) and writes their mirror images
-      float *cs = tb;
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const int a = (lane >> 3) + 4 * k, b = lane & 7;
-        const float A = qb[a * 9 + b];
-        const float B = b ? qb[72 + a * 9 + b - 1] : 0.f;
-        const float Cc = a ? qb[144 + (a - 1) * 9 + b] : 0.f;
-        const float D = (a && b) ? qb[216 + (a - 1) * 9 + b - 1] : 0.f;
-        cs[(7 + a) * 15 + 7 + b] = 0.25f * (((A + B) + Cc) + D);
-        if (b) cs[(7 + a) * 15 + 7 - b] = 0.25f * (((A - B) + Cc) - D);
-        if (a) cs[(7 - a) * 15 + 7 + b] = 0.25f * (((A + B) - Cc) - D);
-        if (a && b) cs[(7 - a) * 15 + 7 - b] = 0.25f * (((A - B) - Cc) + D);
-      }
-      __syncwarp();
-      float *gc = sc.corr + (tile * P + pi) * TP_CORR;
-      for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
-      if (pd.in_combo) {
+      __syncthreads();
+      if (warp == 0) {
 #pragma unroll
         for (int t = 0; t < 8; t++) {
           const int e = lane + 32 * t;
           if (e < RE) {
-            const int row = e / 15;
-            float d;
-            if (pd.kind <= 3) {
-              const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
-              d = sample_code(cs, code.x);
-              if (row > 0) {
-                const float d2 = sample_code(cs, code.y);
-                d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
-              }
-            } else {
-              const int scol = e - row * 15 - 7;
-              d = strip_sample(cs, 4, pd.bx, pd.by, row, scol, -1);
-              if (row > 0) {
-                const float d2 = strip_sample(cs, 4, pd.bx, pd.by, row, scol, 1);
-                d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
-              }
-            }
-            float v = d + cfg.corr_offset;
-            if (v < 0.0f) v = 0.0f;
-            if (log_mode) cmb[t] += logf(v);
-            else cmb[t] *= cfg.twice_diagonal ? v * v : v;
+            float v = part[e];
+            for (int w2 = 1; w2 < NW; w2++) v = log_mode ? v + part[w2 * 240 + e] : v * part[w2 * 240 + e];
+            cmb[t] = v;
           }
         }
+        fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
-      __syncwarp();
-    }
-    // ---------------- stage 3c: extraction ----------------
-    float *combo = scr;
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-      const int e = lane + 32 * t;
-      if (e < RE) {
-        float v = cmb[t];
-        if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
-        else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
-        combo[e] = v;
-        if (sc.combo) sc.combo[tile * RE + e] = v;  // kept for the adjoint
+    } else {
+      const int task = lu * 4 + warp;
+      float *s_clt = sm + warp * warp_floats;
+      float *scr = s_clt + sc.num_sensors * sc.num_colors * TP_CLT;
+      if (task < sc.num_tasks) {
+        if (sc.num_colors == 3) batch_warp_tile<3>(sc, task, s_clt, scr, lane);
+        else batch_warp_tile<1>(sc, task, s_clt, scr, lane);
       }
     }
-    __syncwarp();
-    float res[TP_NDISP];
-#pragma unroll
-    for (int k = 0; k < TP_NDISP; k++) res[k] = (k == 2 || k == 4 || k == 6) ? 0.f : CUDART_NAN_F;
-    {
-      // integer argmax on row 0 (getMaxXYInt): first maximum over the non-NaN entries
-      const float v = (lane < 15) ? combo[lane] : CUDART_NAN_F;
-      float best = isnan(v) ? -CUDART_INF_F : v;
-      int bi = lane < 15 ? lane : 99;
-#pragma unroll
-      for (int o2 = 16; o2 > 0; o2 >>= 1) {
-        const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      const unsigned finite = __ballot_sync(0xffffffffu, lane < 15 && !isnan(v));
-      const int imx = finite ? bi : 14;
-      const float vmax = combo[imx];
-      if (vmax >= cfg.min_corr) {
-        const int ix = imx - 7;
-        res[0] = (float)(-ix);
-        res[2] = vmax;
-        res[8] = (float)ix;
-        int dh = cfg.strip_rows;
-        float wys = 1.0f;
-        if (dh > cfg.wndy_size) dh = cfg.wndy_size;
-        else if (dh < cfg.wndy_size) {
-          float swy = cfg.wndy[0];
-          for (int i = 1; i < dh; i++) swy += cfg.wndy[i];
-          wys = 1.0f / swy;
-        }
-        float s0 = 0.f, sx = 0.f;
-        const int x0 = 7 + ix, nk = dh * 2 * cfg.wndx_size;
-        for (int k = lane; k < nk; k += 32) {  // windowed centroid (getMaxXCm), one sample per lane
-          const int dy = k / (2 * cfg.wndx_size), rest = k - dy * 2 * cfg.wndx_size;
-          const int adx = rest >> 1, dir = (rest & 1) ? 1 : -1, odd = dy & 1;
-          if (((adx - odd) & 1) || (adx == 0 && dir < 0)) continue;
-          const int idx = (adx * dir) >> 1, xx = 2 * idx + odd, x1 = x0 + idx;
-          if (x1 < 0 || x1 >= 15) continue;
-          float d = combo[dy * 15 + x1];
-          if (isnan(d) || !(d > 0.0f)) continue;
-          d *= (((dy == 0) ? wys : 2.0f * wys) * cfg.wndy[dy]) * cfg.wndx[adx];
-          s0 += d;
-          sx += d * xx;
-        }
-        s0 = warp_sum(s0);
-        sx = warp_sum(sx);
-        if (s0 != 0.0f) {
-          res[1] = -(ix + sx / s0 / 2);
-          res[7] = s0;
-        }
-      }
-    }
-    if (fs.quad && (cfg.num_hor > 0 || cfg.num_vert > 0)) {
-      // getMaxXSOrtho: lanes 0-14 horizontal pairs, lanes 16-30 vertical pairs
-      // the surfaces of this tile were just written by this warp (L1/L2 resident)
-      const int half = lane >> 4, j = lane & 15;
-      const int np = half ? cfg.num_vert : cfg.num_hor;
-      float sum = -CUDART_INF_F;
-      if (j < 15 && np > 0) {
-        sum = 0.f;
-        for (int i = 0; i < 15; i++) {
-          float prod = 1.f;
-          for (int k = 0; k < np; k++) {
-            const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
-            const float d = half ? 0.5f * (cc[j * 15 + i] + cc[j * 15 + 14 - i])
-                                 : 0.5f * (cc[i * 15 + j] + cc[(14 - i) * 15 + j]);
-            prod *= d + cfg.corr_offset;
-          }
-          const float v = (prod > 0.0f) ? ((np == 2) ? sqrtf(prod) : ((np == 1) ? prod : powf(prod, 1.0f / np))) -
-                                              cfg.corr_offset
-                                        : -cfg.corr_offset;
-          sum += v * cfg.notch[i];
-        }
-      }
-      float best = sum;
-      int bi = (j < 15) ? j : 99;
-#pragma unroll
-      for (int o2 = 8; o2 > 0; o2 >>= 1) {  // within each 16-lane half
-        const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      const int ic = bi, base = half << 4;
-      const float f0 = __shfl_sync(0xffffffffu, sum, base + (ic > 0 ? ic - 1 : 0));
-      const float f1 = __shfl_sync(0xffffffffu, sum, base + ic);
-      const float f2 = __shfl_sync(0xffffffffu, sum, base + (ic < 14 ? ic + 1 : 14));
-      float xc = (float)ic;
-      if (ic > 0 && ic < 14) {
-        const float den = f0 - 2.0f * f1 + f2;
-        if (den != 0.0f) xc = ic + 0.5f * (f0 - f2) / den;
-      }
-      int ir = (int)floorf(xc + 0.5f);
-      ir = ir < 0 ? 0 : (ir > 14 ? 14 : ir);
-      const float fr = __shfl_sync(0xffffffffu, sum, base + ir);
-      const float hx = __shfl_sync(0xffffffffu, xc, 0), hs = __shfl_sync(0xffffffffu, fr, 0);
-      const float vx = __shfl_sync(0xffffffffu, xc, 16), vs = __shfl_sync(0xffffffffu, fr, 16);
-      if (cfg.num_hor > 0) { res[3] = -(hx - 7.0f); res[4] = hs / 8.0f; }
-      if (cfg.num_vert > 0) { res[5] = -(vx - 7.0f); res[6] = vs / 8.0f; }
-    }
-    float *dm = sc.disp + tile * TP_NDISP;
-    if (lane < TP_NDISP) {
-      float v = res[0];
-#pragma unroll
-      for (int k = 1; k < TP_NDISP; k++) if (lane == k) v = res[k];
-      dm[lane] = v;
-    }
-    __syncwarp();
+    __syncthreads();
   }
+}
+
+// units per scene and the kernel's shared memory; scenes_dev / unit_off_dev are device arrays
+int batch_units(const SceneDev &sc) {
+  const bool split = sc.num_colors == 1 && sc.num_pairs > 8;
+  return split ? sc.num_tasks : (sc.num_tasks + 3) / 4;
+}
+
+int batch_smem_bytes(const SceneDev *scenes, int n, int *warp_floats) {
+  int wf = 0, sp = 0;
+  for (int i = 0; i < n; i++) {
+    const SceneDev &sc = scenes[i];
+    if (sc.num_colors == 1 && sc.num_pairs > 8) {
+      const int f = sc.num_sensors * TP_CLT + 4 * SCR + 4 * 240;
+      sp = f > sp ? f : sp;
+    } else {
+      const int f = ((sc.num_sensors * sc.num_colors * TP_CLT + SCR) + 3) & ~3;
+      wf = f > wf ? f : wf;
+    }
+  }
+  *warp_floats = wf;
+  const int need = 4 * wf > sp ? 4 * wf : sp;
+  return need * 4;
+}
+
+cudaError_t launch_fused_batch(const SceneDev *scenes_host, const SceneDev *scenes_dev, const int *unit_off_dev,
+                               int n, int total_units, cudaStream_t st) {
+  if (n <= 0 || n > BATCH_MAX) return cudaErrorInvalidValue;
+  for (int i = 0; i < n; i++) {
+    const SceneDev &sc = scenes_host[i];
+    const int ntiles = sc.tilesX * sc.tilesY;
+    disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
+    if (sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidConfiguration;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || total_units <= 0) return e;
+  int warp_floats = 0;
+  const int bytes = batch_smem_bytes(scenes_host, n, &warp_floats);
+  e = cudaFuncSetAttribute(fused_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_batch_kernel, 128, bytes);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int grid = total_units < sms * per_sm ? total_units : sms * per_sm;
+  fused_batch_kernel<<<grid, 128, bytes, st>>>(scenes_dev, unit_off_dev, n, total_units, warp_floats);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -596,37 +822,51 @@ static FwdShape make_shape(const SceneDev &sc, int nw) {
   return f;
 }
 
+static int split_smem_floats(const FwdShape &f) { return f.clt_floats + f.nw * SCR + f.nw * 240; }
+
 int fused_smem_bytes(const SceneDev &sc, int tpb, int nw) {
-  (void)tpb;
   FwdShape f = make_shape(sc, nw);
+  if (tpb == 1 && f.nw > 1) return split_smem_floats(f) * 4;
   return f.per_warp * f.nw * 4;
 }
 
-// tpb is accepted for the schedule interface; one warp always owns one tile here
-template <int C>
-static cudaError_t launch_fused_c(const SceneDev &sc, const CorrConst &cc, const FwdShape &f, cudaStream_t st) {
-  const int bytes = f.per_warp * f.nw * 4;
-  cudaError_t e = cudaFuncSetAttribute(fused_forward_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+template <typename K>
+static cudaError_t launch_persistent(K kernel, int threads, int bytes, int units, const SceneDev &sc,
+                                     const FwdShape &f, const CorrConst &cc, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_forward_kernel<C>, f.nw * 32, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, bytes);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const int need = (sc.num_tasks + f.nw - 1) / f.nw;
-  const int grid = need < sms * per_sm ? need : sms * per_sm;
-  fused_forward_kernel<C><<<grid, f.nw * 32, bytes, st>>>(sc, f, cc);
+  const int grid = units < sms * per_sm ? units : sms * per_sm;
+  kernel<<<grid, threads, bytes, st>>>(sc, f, cc);
   return cudaGetLastError();
 }
 
+// Schedules: tiles_per_block == warps_per_block (<= 4): warp per tile;
+// tiles_per_block == 1 with warps_per_block 2 or 4: pair per warp (CTA per tile).
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st) {
-  (void)tpb;
   const int ntiles = sc.tilesX * sc.tilesY;
   disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || sc.num_tasks <= 0) return e;
   if (sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidConfiguration;
+  if (tpb <= 0 && nw <= 0 && sc.num_pairs > 8) {  // default for many pairs: four warps share a tile
+    tpb = 1;
+    nw = 4;
+  }
   FwdShape f = make_shape(sc, nw);
   if (f.nw > 4) return cudaErrorInvalidConfiguration;
-  return sc.num_colors == 3 ? launch_fused_c<3>(sc, cc, f, st) : launch_fused_c<1>(sc, cc, f, st);
+  if (tpb == 1 && f.nw > 1) {
+    const int bytes = split_smem_floats(f) * 4;
+    return sc.num_colors == 3
+               ? launch_persistent(fused_split_kernel<3>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st)
+               : launch_persistent(fused_split_kernel<1>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st);
+  }
+  const int bytes = f.per_warp * f.nw * 4;
+  const int units = (sc.num_tasks + f.nw - 1) / f.nw;
+  return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3>, f.nw * 32, bytes, units, sc, f, cc, st)
+                            : launch_persistent(fused_forward_kernel<1>, f.nw * 32, bytes, units, sc, f, cc, st);
 }

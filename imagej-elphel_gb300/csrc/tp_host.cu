@@ -759,10 +759,14 @@ tp_status tp_process(tp_handle *h, void *stream) {
 
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block) {
   if (!h) return TP_ERR_ARG;
-  // the fused kernel gives each warp whole tiles: tiles per CTA == warps per CTA (<= 4)
+  // warp per tile: tiles per CTA == warps per CTA (<= 4); pair per warp: 1 tile per CTA of 2 or 4 warps
   if (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4)
     return fail(h, TP_ERR_ARG, "tp_set_schedule: out of range");
   if (warps_per_block == 0) warps_per_block = tiles_per_block;
+  if (tiles_per_block > 1 && tiles_per_block != warps_per_block)
+    return fail(h, TP_ERR_ARG, "tp_set_schedule: several tiles per CTA need one warp per tile");
+  if (tiles_per_block == 1 && warps_per_block == 3)
+    return fail(h, TP_ERR_ARG, "tp_set_schedule: pair-per-warp CTAs have 2 or 4 warps");
   h->sched_tpb = tiles_per_block;
   h->sched_nw = warps_per_block;
   return TP_OK;
@@ -846,6 +850,83 @@ tp_status tp_get_textures(tp_handle *h, float *tex) {
 tp_status tp_get_texture_aux(tp_handle *h, float *aux) {
   if (!h) return TP_ERR_ARG;
   return d2h(h, aux, h->d_tex_aux, (size_t)h->ntiles * 16 * sizeof(float), "tp_get_texture_aux");
+}
+
+// ---------------------------------------------------------------------------
+// batches: many scenes (handles) through one persistent forward launch
+// ---------------------------------------------------------------------------
+struct tp_batch {
+  std::vector<tp_handle *> scenes;
+  std::vector<SceneDev> h_scenes;
+  std::vector<int> h_off, graph_tasks;
+  SceneDev *d_scenes = nullptr;
+  int *d_off = nullptr;
+  int device = 0, total_units = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::string err;
+};
+
+static tp_status bfail(tp_batch *b, tp_status st, const std::string &msg) {
+  if (b) b->err = msg;
+  return st;
+}
+
+// refresh the device scene table (buffers or task counts may have changed)
+static tp_status batch_tables(tp_batch *b) {
+  const int n = (int)b->scenes.size();
+  b->h_scenes.resize(n);
+  b->h_off.resize(n + 1);
+  int u = 0;
+  for (int i = 0; i < n; i++) {
+    tp_handle *h = b->scenes[i];
+    b->h_scenes[i] = scene_of(h);
+    b->h_off[i] = u;
+    u += batch_units(b->h_scenes[i]);
+  }
+  b->h_off[n] = u;
+  b->total_units = u;
+  if (cudaMemcpy(b->d_scenes, b->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_off, b->h_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, TP_ERR_CUDA, "batch: scene table upload");
+  }
+  return TP_OK;
+}
+
+// plans (when asked or missing) and the persistent forward, all on one stream
+static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
+  for (tp_handle *h : b->scenes) {
+    if (replan || !h->planned) {
+      SceneDev sc = scene_of(h);
+      if (launch_plan(sc, st) != cudaSuccess || launch_tile_task_map(sc, st) != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(b, TP_ERR_CUDA, "batch: plan");
+      }
+      h->planned = 1;
+    }
+  }
+  if (launch_fused_batch(b->h_scenes.data(), b->d_scenes, b->d_off, (int)b->scenes.size(), b->total_units, st) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, TP_ERR_CUDA, "batch: forward");
+  }
+  for (tp_handle *h : b->scenes) h->fwd_valid = 1;
+  return TP_OK;
+}
+
+#define CK_B(call)                                                                       \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) return bfail(b, TP_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+static void batch_drop_graph(tp_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
 }
 
 // Device address of the compaction scratch array, looked up once per device
@@ -952,6 +1033,92 @@ tp_status tp_get_port_derivatives(tp_handle *h, double *deriv) {
   if (!h->have_jac) return fail(h, TP_ERR_STATE, "tp_get_port_derivatives: run tp_backward first");
   return d2h(h, deriv, h->d_port_deriv, (size_t)h->num_tasks * h->cfg.num_sensors * 10 * sizeof(double),
              "tp_get_port_derivatives");
+}
+
+tp_status tp_batch_create(tp_handle *const *scenes, int n, tp_batch **out) {
+  if (!scenes || !out || n <= 0 || n > 256) return TP_ERR_ARG;
+  *out = nullptr;
+  const int dev = scenes[0] ? scenes[0]->cfg.device : 0;
+  for (int i = 0; i < n; i++) {
+    tp_handle *h = scenes[i];
+    if (!h || h->cfg.device != dev) return TP_ERR_ARG;
+    if (!h->have_tasks || !h->have_corr || h->num_pairs == 0) return TP_ERR_STATE;
+    const bool split = h->cfg.num_colors == 1 && h->num_pairs > 8;
+    if (!split && h->cfg.num_sensors * h->cfg.num_colors > 16) return TP_ERR_ARG;  // warp-per-tile smem
+  }
+  tp_batch *b = new tp_batch();
+  b->scenes.assign(scenes, scenes + n);
+  b->device = dev;
+  bool ok = cudaSetDevice(dev) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            dalloc(&b->d_scenes, n) == cudaSuccess && dalloc(&b->d_off, n + 1) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    tp_batch_destroy(b);
+    return TP_ERR_NOMEM;
+  }
+  *out = b;
+  return TP_OK;
+}
+
+tp_status tp_batch_destroy(tp_batch *b) {
+  if (!b) return TP_ERR_ARG;
+  batch_drop_graph(b);
+  cudaFree(b->d_scenes);
+  cudaFree(b->d_off);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return TP_OK;
+}
+
+tp_status tp_batch_last_error(const tp_batch *b, char *buf, int n) {
+  if (!b || !buf || n <= 0) return TP_ERR_ARG;
+  snprintf(buf, (size_t)n, "%s", b->err.c_str());
+  return TP_OK;
+}
+
+tp_status tp_batch_process(tp_batch *b, int replan, void *stream) {
+  if (!b) return TP_ERR_ARG;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  for (tp_handle *h : b->scenes) CK_B(cudaStreamSynchronize(h->stream));
+  tp_status r = batch_tables(b);
+  if (r != TP_OK) return r;
+  return batch_enqueue(b, replan, st);
+}
+
+tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
+  if (!b) return TP_ERR_ARG;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  bool stale = !b->exec || b->graph_tasks.size() != b->scenes.size();
+  for (size_t i = 0; !stale && i < b->scenes.size(); i++) stale = b->graph_tasks[i] != b->scenes[i]->num_tasks;
+  if (stale) {
+    batch_drop_graph(b);
+    for (tp_handle *h : b->scenes) CK_B(cudaStreamSynchronize(h->stream));
+    tp_status r = batch_tables(b);
+    if (r != TP_OK) return r;
+    CK_B(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    r = batch_enqueue(b, 1, b->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+    if (r != TP_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (ec != cudaSuccess) return bfail(b, TP_ERR_CUDA, std::string("batch: capture: ") + cudaGetErrorString(ec));
+    b->graph = g;
+    CK_B(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->graph_tasks.clear();
+    for (tp_handle *h : b->scenes) b->graph_tasks.push_back(h->num_tasks);
+  }
+  CK_B(cudaGraphLaunch(b->exec, st));
+  for (tp_handle *h : b->scenes) h->fwd_valid = 1;
+  return TP_OK;
+}
+
+tp_status tp_batch_synchronize(tp_batch *b) {
+  if (!b) return TP_ERR_ARG;
+  CK_B(cudaStreamSynchronize(b->stream));
+  return TP_OK;
 }
 
 }  // extern "C"

@@ -205,6 +205,27 @@ tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
 tp_status tp_get_texture_aux(tp_handle *h, float *aux);
 
+/* ---- batches (no reference counterpart: the reference processes one scene per
+ * GPUTileProcessor instance and launch) ----
+ * A batch runs the forward of many scenes -- handles of any sensor count,
+ * colours, size and pair set, all on one device, each with its tasks and
+ * correlation set up -- as one persistent kernel over a queue of tiles in
+ * scene order (4 tiles per unit for warp-per-tile scenes, 1 tile shared by 4
+ * warps for mono scenes with more than 8 pairs).  Colour scenes need
+ * sensors x colours <= 16.  The handles stay owned by the caller and must
+ * outlive the batch; results are read through each handle's getters. */
+typedef struct tp_batch tp_batch;
+tp_status tp_batch_create(tp_handle *const *scenes, int num_scenes, tp_batch **out);
+tp_status tp_batch_destroy(tp_batch *b);
+tp_status tp_batch_last_error(const tp_batch *b, char *buf, int buf_len);
+/* plans every scene (always when replan != 0, else only where missing), then the one forward launch */
+tp_status tp_batch_process(tp_batch *b, int replan, void *stream);
+/* the same step (with replanning) captured once into a CUDA graph and replayed; the graph is
+ * rebuilt when a scene's task count changed; inputs updated in place (tp_set_image, ...) are
+ * picked up by the replay */
+tp_status tp_batch_run_graph(tp_batch *b, void *stream);
+tp_status tp_batch_synchronize(tp_batch *b);
+
 /* ---- adjoint (no reference counterpart: the reference has no derivative of
  * the correlation chain; its geometric part is GeometryCorrection
  * .getPortsCoordinatesAndDerivatives, GeometryCorrection.java:2159-2314) ----

@@ -119,8 +119,10 @@ def test_quad_bayer_rggb(oracle):
         _check_corr(tp, ref)
 
 
-def test_circle16_extrinsics(oracle):
-    """16 LWIR sensors on a circle with extrinsic perturbations, all 120 pairs (generalised strips)."""
+@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (4, 4), (1, 2)])
+def test_circle16_extrinsics(oracle, sched):
+    """16 LWIR sensors on a circle with extrinsic perturbations, all 120 pairs (generalised strips),
+    under the default (pair per warp, 4 warps), warp-per-tile and 2-warp schedules."""
     sc = synth.make_scene("circle_lwir", seed=5, width=160, height=128)
     T = (sc["width"] // 8) * (sc["height"] // 8)
     pairs = synth.circle_pairs(sc["geometry"])
@@ -129,6 +131,7 @@ def test_circle16_extrinsics(oracle):
     with make_gpu(sc) as tp:
         tp.setCorrelation(pairs=pairs)
         tp.setFullFrameImages(np.full(T, 2.0, np.float32))
+        tp.setSchedule(*sched)
         tp.process()
         _check_tiles(oracle, tp, ref, 1)
         _check_clt(tp, ref)
@@ -219,7 +222,7 @@ def test_imclt(oracle):
         assert np.abs(got - want[2]).max() / np.abs(want[2]).max() < 2e-6
 
 
-@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (2, 2), (4, 4)])
+@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (2, 2), (4, 4), (1, 2), (1, 4)])
 def test_stage_kernels_and_schedules_agree(oracle, sched):
     """Per-stage kernels (execConverCorrectTiles/execCorrelate/execExtract) and the fused
     kernel under several CTA schedules give the same results."""
