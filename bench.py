@@ -58,6 +58,8 @@ def parse_args():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint / LM measurement")
+    p.add_argument("--batch-scenes", type=int, default=64, help="scenes in the batched measurement (0 = skip)")
+    p.add_argument("--batch-only", action="store_true", help="only the batched measurement (profiling)")
     p.add_argument("--adjoint-only", action="store_true",
                    help="only the 16-sensor forward / forward+adjoint / LM measurement (profiling)")
     p.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles per CPU sample (0 = auto)")
@@ -316,6 +318,82 @@ def measure_fwd_adjoint(seed, steps, warmup, lma_iterations=20):
     return out
 
 
+def measure_batch(seed, n_scenes, steps, warmup, types=("c2_bayer_4x2592x1936", "c3_lwir_16x640x512")):
+    """C4: n_scenes scenes alternating over `types` (by default the 4x2592x1936 Bayer type and the
+    16x640x512 LWIR type), each with its own seed-derived images, kernel table (Bayer) and extrinsics.  To keep the
+    set-up short the per-scene inputs are seeded variations of one rendered scene per type
+    (shifted mosaic + noise, scaled kernel table, perturbed extrinsics); the work per scene is
+    unchanged.  Times one step (ports + forward of every scene) three ways on one stream:
+    per-scene calls, one batched persistent launch, and the batch's CUDA graph."""
+    import copy
+    import torch
+    from tileproc import GPUTileProcessor
+    from tileproc import _lib as L
+    from tileproc.batch import Batch
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = C.c_void_p(stream.cuda_stream)
+    base = {t: make_workload(t, seed) for t in types}
+    rng = np.random.default_rng(seed + 99)
+    tps, tiles = [], 0
+    try:
+        for i in range(n_scenes):
+            w = base[types[i % len(types)]]
+            sc = w["scene"]
+            g = copy.deepcopy(sc["geometry"])
+            for k in ("azimuth", "tilt", "roll", "zoom"):
+                g[k] = (np.asarray(g[k]) + rng.normal(0, 1e-3, w["S"])).tolist()
+            shift = 2 * int(rng.integers(0, 8))
+            imgs = np.roll(sc["images"], shift, axis=2)
+            if imgs.dtype == np.uint16:
+                imgs = np.clip(imgs.astype(np.int32) + rng.integers(-2, 3, imgs.shape), 0, 4095).astype(np.uint16)
+            else:
+                imgs = (imgs + rng.normal(0, 0.01, imgs.shape)).astype(np.float32)
+            tp = GPUTileProcessor(w["S"], w["W"], w["H"], num_colors=w["C"], kernels_hor=w["KH"],
+                                  kernels_vert=w["KV"])
+            tps.append(tp)
+            tp.setGeometry(g)
+            if w["kernels"] is not None:
+                f = np.float32(1.0 + 0.02 * rng.standard_normal())
+                tp.setConvolutionKernels(w["kernels"] * f, w["kext"], layout=L.TP_KERNELS_CPU)
+            if w["C"] == 3:
+                tp.setColorScales([1.0, 1.0, 0.5])
+            tp.setBayerImages(imgs)
+            tp.setCorrelation(pairs=w["pairs"])
+            tp.setFullFrameImages(w["target"], tile_op=np.full(w["T"], 0xF, np.int32))
+            tiles += w["T"]
+        lib = tps[0]._lib
+
+        def plain():
+            for tp in tps:
+                tp._ck(lib.tp_ports(tp.h, sptr), "ports")
+                tp._ck(lib.tp_process(tp.h, sptr), "process")
+
+        b = Batch(tps)
+        out = {"workload": "%d scenes alternating %s" % (n_scenes, " / ".join(types)), "tiles_per_step": tiles}
+        for name, fn in (("plain", plain), ("batched", lambda: b.process(True, sptr)),
+                         ("graph", lambda: b.run_graph(sptr))):
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            out[name + "_ms"] = ms
+            out[name + "_tiles_per_s"] = tiles / (ms / 1000.0)
+        out["batched_over_plain"] = out["plain_ms"] / out["batched_ms"]
+        out["graph_over_plain"] = out["plain_ms"] / out["graph_ms"]
+        b.close()
+    finally:
+        for tp in tps:
+            tp.close()
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -432,6 +510,13 @@ def run_ours(args):
         e2e_t = float(t.item())
     e2e_val = world * T * args.steps / e2e_t
 
+    batched = batched_small = None
+    if rank == 0 and args.batch_scenes > 0:
+        batched = measure_batch(args.seed, args.batch_scenes, max(3, args.steps // 4), min(args.warmup, 3))
+        batched_small = measure_batch(args.seed, args.batch_scenes, max(3, args.steps // 4), min(args.warmup, 3),
+                                      types=("c1_mono_4x512x384",))
+        torch.cuda.set_stream(stream)
+
     fwd_adj = None
     if rank == 0 and not args.no_adjoint:
         fwd_adj = measure_fwd_adjoint(args.seed, max(3, args.steps // 2), args.warmup)
@@ -467,6 +552,8 @@ def run_ours(args):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "fwd_adjoint": fwd_adj,
+        "batched": batched,
+        "batched_small_scenes": batched_small,
     }
     tp.close()
     if rank == 0:
@@ -478,6 +565,15 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.batch_only:
+        import torch
+        import build as tp_build
+        tp_build.build()
+        torch.cuda.set_device(0)
+        print(json.dumps(measure_batch(args.seed, args.batch_scenes, args.steps, args.warmup)))
+        print(json.dumps(measure_batch(args.seed, args.batch_scenes, args.steps, args.warmup,
+                                       types=("c1_mono_4x512x384",))))
+        return 0
     if args.adjoint_only:
         import torch
         import build as tp_build

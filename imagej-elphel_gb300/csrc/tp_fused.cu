@@ -26,6 +26,8 @@
 //           argmax on the disparity axis, windowed centroid, hor/vert maxima.
 #include "tp_dtt.cuh"
 
+#include <cstddef>
+
 namespace {
 
 constexpr int FW_MAX_WARPS = 16;
@@ -541,47 +543,45 @@ __global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_consta
 }
 
 // ---------------------------------------------------------------------------
-// Batched persistent forward: one launch over many scenes of different sensor
-// counts, colours, pair sets and sizes.  The work is a queue of units in scene
-// order: a unit of a quad / colour scene is 4 tiles (one per warp, the
-// warp-per-tile path), a unit of a many-pair scene is 1 tile whose pairs the 4
-// warps split.  CTAs take units grid-stride; the scene of a unit is found by
-// binary search over the unit offsets; each scene's SceneDev and correlation
-// set-up are read from global memory.
+// Batched persistent forward over many scenes of different sensor counts,
+// colours, pair sets and sizes.  Scenes are grouped in three classes by the
+// schedule their tiles take (colour warp-per-tile, mono warp-per-tile, mono
+// pair-per-warp); each class is one persistent launch over a queue of units in
+// scene order (NW tiles per unit for warp-per-tile, 1 tile per unit for
+// pair-per-warp).  CTAs take units grid-stride, find the unit's scene by
+// binary search over the unit offsets and keep the current scene's SceneDev in
+// shared memory (reloaded only when the scene changes); the scene's
+// correlation set-up is read through its device pointer.
 // ---------------------------------------------------------------------------
 constexpr int BATCH_MAX = 256;
 
 __global__ void disp_init_kernel(float *disp, int n);
 
-__device__ __forceinline__ bool scene_split(const SceneDev &sc) { return sc.num_colors == 1 && sc.num_pairs > 8; }
-
-template <int C>
-__device__ __forceinline__ void batch_warp_tile(const SceneDev &sc, int task, float *s_clt, float *scr, int lane) {
-  const CorrConst &cfg = *sc.corr_cfg;
-  const int S = sc.num_sensors, P = sc.num_pairs;
-  const int RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
-  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
-  const int groups = (S + 3) >> 2;
-  const bool log_mode = cfg.log_combine;
-  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
-  const int txy = sc.task_txy[task];
-  const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-  for (int gt = 0; gt < C * groups; gt++) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
-  __syncwarp();
-  float cmb[8];
-#pragma unroll
-  for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
-  for (int pi = 0; pi < P; pi++) fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
-  fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+int batch_class(const SceneDev &sc) {
+  if (sc.num_colors == 3) return 0;
+  return sc.num_pairs > 8 ? 2 : 1;
 }
 
-__global__ void __launch_bounds__(128, 4) fused_batch_kernel(const SceneDev *__restrict__ scenes,
-                                                            const int *__restrict__ unit_off, int nscenes,
-                                                            int total_units, int warp_floats) {
-  extern __shared__ float sm[];
+static int class_warps(int cls) { return cls == 0 ? 1 : 4; }
+
+int batch_units(const SceneDev &sc) {
+  const int nw = batch_class(sc) == 2 ? 1 : class_warps(batch_class(sc));
+  return (sc.num_tasks + nw - 1) / nw;
+}
+
+template <int C, bool SPLIT, int NW>
+__global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
+    fused_batch_kernel(const SceneDev *__restrict__ scenes, const int *__restrict__ unit_off, int nscenes,
+                       int total_units, int warp_floats, int cfg_floats) {
+  extern __shared__ float smem[];
   __shared__ int s_off[BATCH_MAX + 1];
+  __shared__ SceneDev s_sc;
+  // the current scene's correlation set-up (header and its pairs) leads the dynamic shared memory
+  CorrConst *s_cfg = (CorrConst *)smem;
+  float *sm = smem + cfg_floats;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i <= nscenes; i += blockDim.x) s_off[i] = unit_off[i];
+  int cur = -1;
   __syncthreads();
   for (int u = blockIdx.x; u < total_units; u += gridDim.x) {
     int lo = 0, hi = nscenes - 1;  // last scene whose first unit is <= u
@@ -590,29 +590,40 @@ __global__ void __launch_bounds__(128, 4) fused_batch_kernel(const SceneDev *__r
       if (s_off[mid] <= u) lo = mid;
       else hi = mid - 1;
     }
-    const SceneDev &sc = scenes[lo];
+    if (lo != cur) {
+      __syncthreads();
+      const int *src = (const int *)(scenes + lo);
+      int *dst = (int *)&s_sc;
+      for (int i = threadIdx.x; i < (int)(sizeof(SceneDev) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+      const int cfg_words = (int)((offsetof(CorrConst, pairs) + scenes[lo].num_pairs * sizeof(PairDev)) / sizeof(int));
+      const int *csrc = (const int *)scenes[lo].corr_cfg;
+      for (int i = threadIdx.x; i < cfg_words; i += blockDim.x) ((int *)s_cfg)[i] = csrc[i];
+      cur = lo;
+      __syncthreads();
+    }
+    const SceneDev &sc = s_sc;
+    const CorrConst &cfg = *s_cfg;
+    const int S = sc.num_sensors, P = sc.num_pairs;
+    const int RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
+    const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+    const int groups = (S + 3) >> 2;
+    const bool log_mode = cfg.log_combine;
+    const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
     const int lu = u - s_off[lo];
-    if (scene_split(sc)) {
-      const CorrConst &cfg = *sc.corr_cfg;
-      const int S = sc.num_sensors, P = sc.num_pairs, NW = 4;
-      const int RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
-      const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
-      const int groups = (S + 3) >> 2;
-      const bool log_mode = cfg.log_combine;
-      const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+    if (SPLIT) {
       float *s_clt = sm;
       float *scr = sm + S * TP_CLT + warp * SCR;
       float *part = sm + S * TP_CLT + NW * SCR;
       const int task = lu;
       const int txy = sc.task_txy[task];
       const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-      for (int gt = warp; gt < groups; gt += NW) fwd_clt_item<1>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
+      for (int gt = warp; gt < groups; gt += NW) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
       __syncthreads();
       float cmb[8];
 #pragma unroll
       for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
       for (int pi = warp; pi < P; pi += NW)
-        fwd_pair<1>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+        fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
       for (int t = 0; t < 8; t++) {
         const int e = lane + 32 * t;
@@ -631,65 +642,68 @@ __global__ void __launch_bounds__(128, 4) fused_batch_kernel(const SceneDev *__r
         }
         fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
+      __syncthreads();
     } else {
-      const int task = lu * 4 + warp;
-      float *s_clt = sm + warp * warp_floats;
-      float *scr = s_clt + sc.num_sensors * sc.num_colors * TP_CLT;
+      const int task = lu * NW + warp;
       if (task < sc.num_tasks) {
-        if (sc.num_colors == 3) batch_warp_tile<3>(sc, task, s_clt, scr, lane);
-        else batch_warp_tile<1>(sc, task, s_clt, scr, lane);
+        float *s_clt = sm + warp * warp_floats;
+        float *scr = s_clt + S * C * TP_CLT;
+        const int txy = sc.task_txy[task];
+        const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+        for (int gt = 0; gt < C * groups; gt++) fwd_clt_item<C>(sc, S, task, tile, gt, groups, s_clt, scr, lane);
+        __syncwarp();
+        float cmb[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+        for (int pi = 0; pi < P; pi++)
+          fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+        fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
     }
-    __syncthreads();
   }
 }
 
-// units per scene and the kernel's shared memory; scenes_dev / unit_off_dev are device arrays
-int batch_units(const SceneDev &sc) {
-  const bool split = sc.num_colors == 1 && sc.num_pairs > 8;
-  return split ? sc.num_tasks : (sc.num_tasks + 3) / 4;
-}
-
-int batch_smem_bytes(const SceneDev *scenes, int n, int *warp_floats) {
-  int wf = 0, sp = 0;
-  for (int i = 0; i < n; i++) {
-    const SceneDev &sc = scenes[i];
-    if (sc.num_colors == 1 && sc.num_pairs > 8) {
-      const int f = sc.num_sensors * TP_CLT + 4 * SCR + 4 * 240;
-      sp = f > sp ? f : sp;
-    } else {
-      const int f = ((sc.num_sensors * sc.num_colors * TP_CLT + SCR) + 3) & ~3;
-      wf = f > wf ? f : wf;
-    }
-  }
-  *warp_floats = wf;
-  const int need = 4 * wf > sp ? 4 * wf : sp;
-  return need * 4;
-}
-
-cudaError_t launch_fused_batch(const SceneDev *scenes_host, const SceneDev *scenes_dev, const int *unit_off_dev,
-                               int n, int total_units, cudaStream_t st) {
-  if (n <= 0 || n > BATCH_MAX) return cudaErrorInvalidValue;
-  for (int i = 0; i < n; i++) {
-    const SceneDev &sc = scenes_host[i];
-    const int ntiles = sc.tilesX * sc.tilesY;
-    disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
-    if (sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidConfiguration;
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || total_units <= 0) return e;
-  int warp_floats = 0;
-  const int bytes = batch_smem_bytes(scenes_host, n, &warp_floats);
-  e = cudaFuncSetAttribute(fused_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+template <typename K>
+static cudaError_t launch_batch_k(K kernel, int threads, int bytes, int total_units, const SceneDev *scenes_dev,
+                                  const int *unit_off_dev, int n, int warp_floats, int cfg_floats, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_batch_kernel, 128, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, bytes);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   const int grid = total_units < sms * per_sm ? total_units : sms * per_sm;
-  fused_batch_kernel<<<grid, 128, bytes, st>>>(scenes_dev, unit_off_dev, n, total_units, warp_floats);
+  kernel<<<grid, threads, bytes, st>>>(scenes_dev, unit_off_dev, n, total_units, warp_floats, cfg_floats);
   return cudaGetLastError();
+}
+
+// one class: scenes_host / scenes_dev hold only that class's scenes, unit_off_dev their unit offsets
+cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const SceneDev *scenes_dev,
+                               const int *unit_off_dev, int n, int total_units, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (n > BATCH_MAX) return cudaErrorInvalidValue;
+  int wf = 0, sp = 0, maxp = 0;
+  for (int i = 0; i < n; i++) {
+    maxp = scenes_host[i].num_pairs > maxp ? scenes_host[i].num_pairs : maxp;
+    const SceneDev &sc = scenes_host[i];
+    if (batch_class(sc) != cls || sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidValue;
+    const int ntiles = sc.tilesX * sc.tilesY;
+    disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
+    const int f = ((sc.num_sensors * sc.num_colors * TP_CLT + SCR) + 3) & ~3;
+    wf = f > wf ? f : wf;
+    const int g = sc.num_sensors * TP_CLT + 4 * SCR + 4 * 240;
+    sp = g > sp ? g : sp;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || total_units <= 0) return e;
+  const int cf = (int)(((offsetof(CorrConst, pairs) + maxp * sizeof(PairDev)) + 15) / 16 * 4);
+  if (cls == 0) return launch_batch_k(fused_batch_kernel<3, false, 1>, 32, (cf + wf) * 4, total_units, scenes_dev,
+                                      unit_off_dev, n, wf, cf, st);
+  if (cls == 1) return launch_batch_k(fused_batch_kernel<1, false, 4>, 128, (cf + 4 * wf) * 4, total_units,
+                                      scenes_dev, unit_off_dev, n, wf, cf, st);
+  return launch_batch_k(fused_batch_kernel<1, true, 4>, 128, (cf + sp) * 4, total_units, scenes_dev, unit_off_dev, n,
+                        0, cf, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -857,12 +857,16 @@ tp_status tp_get_texture_aux(tp_handle *h, float *aux) {
 // ---------------------------------------------------------------------------
 struct tp_batch {
   std::vector<tp_handle *> scenes;
-  std::vector<SceneDev> h_scenes;
-  std::vector<int> h_off, graph_tasks;
-  SceneDev *d_scenes = nullptr;
-  int *d_off = nullptr;
-  int device = 0, total_units = 0;
-  cudaStream_t stream = nullptr;
+  std::vector<SceneDev> h_scenes;           // all scenes, for the batched plan
+  std::vector<int> h_task_off, graph_tasks;
+  std::vector<SceneDev> h_cls[3];           // per schedule class
+  std::vector<int> h_cls_off[3];
+  int cls_units[3] = {0, 0, 0};
+  SceneDev *d_scenes = nullptr, *d_cls[3] = {nullptr, nullptr, nullptr};
+  int *d_task_off = nullptr, *d_cls_off[3] = {nullptr, nullptr, nullptr};
+  int device = 0, total_tasks = 0;
+  cudaStream_t stream = nullptr, cls_stream[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::string err;
@@ -873,44 +877,76 @@ static tp_status bfail(tp_batch *b, tp_status st, const std::string &msg) {
   return st;
 }
 
-// refresh the device scene table (buffers or task counts may have changed)
+// refresh the device scene tables (buffers or task counts may have changed)
 static tp_status batch_tables(tp_batch *b) {
   const int n = (int)b->scenes.size();
   b->h_scenes.resize(n);
-  b->h_off.resize(n + 1);
-  int u = 0;
-  for (int i = 0; i < n; i++) {
-    tp_handle *h = b->scenes[i];
-    b->h_scenes[i] = scene_of(h);
-    b->h_off[i] = u;
-    u += batch_units(b->h_scenes[i]);
+  b->h_task_off.resize(n + 1);
+  for (int c = 0; c < 3; c++) {
+    b->h_cls[c].clear();
+    b->h_cls_off[c].assign(1, 0);
   }
-  b->h_off[n] = u;
-  b->total_units = u;
-  if (cudaMemcpy(b->d_scenes, b->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_off, b->h_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+  int t = 0;
+  for (int i = 0; i < n; i++) {
+    const SceneDev sc = scene_of(b->scenes[i]);
+    b->h_scenes[i] = sc;
+    b->h_task_off[i] = t;
+    t += sc.num_tasks;
+    const int c = batch_class(sc);
+    b->h_cls[c].push_back(sc);
+    b->h_cls_off[c].push_back(b->h_cls_off[c].back() + batch_units(sc));
+  }
+  b->h_task_off[n] = t;
+  b->total_tasks = t;
+  bool ok = cudaMemcpy(b->d_scenes, b->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(b->d_task_off, b->h_task_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
+                cudaSuccess;
+  for (int c = 0; ok && c < 3; c++) {
+    const int m = (int)b->h_cls[c].size();
+    b->cls_units[c] = b->h_cls_off[c].back();
+    if (m == 0) continue;
+    ok = cudaMemcpy(b->d_cls[c], b->h_cls[c].data(), m * sizeof(SceneDev), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_cls_off[c], b->h_cls_off[c].data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+  }
+  if (!ok) {
     cudaGetLastError();
     return bfail(b, TP_ERR_CUDA, "batch: scene table upload");
   }
   return TP_OK;
 }
 
-// plans (when asked or missing) and the persistent forward, all on one stream
+// the plans (all scenes in one launch) and one persistent forward per class on its own
+// stream, forked from and joined back into st
 static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
-  for (tp_handle *h : b->scenes) {
-    if (replan || !h->planned) {
-      SceneDev sc = scene_of(h);
-      if (launch_plan(sc, st) != cudaSuccess || launch_tile_task_map(sc, st) != cudaSuccess) {
+  bool need = replan != 0;
+  for (tp_handle *h : b->scenes) need = need || !h->planned;
+  if (need) {
+    for (size_t i = 0; i < b->scenes.size(); i++) {
+      const SceneDev &sc = b->h_scenes[i];
+      if (cudaMemsetAsync(sc.tile_task, 0xff, sizeof(int) * sc.tilesX * sc.tilesY, st) != cudaSuccess) {
         cudaGetLastError();
-        return bfail(b, TP_ERR_CUDA, "batch: plan");
+        return bfail(b, TP_ERR_CUDA, "batch: tile map");
       }
-      h->planned = 1;
     }
+    if (launch_plan_batch(b->d_scenes, b->d_task_off, (int)b->scenes.size(), b->total_tasks, st) != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b, TP_ERR_CUDA, "batch: plan");
+    }
+    for (tp_handle *h : b->scenes) h->planned = 1;
   }
-  if (launch_fused_batch(b->h_scenes.data(), b->d_scenes, b->d_off, (int)b->scenes.size(), b->total_units, st) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return bfail(b, TP_ERR_CUDA, "batch: forward");
+  if (cudaEventRecord(b->ev_fork, st) != cudaSuccess) return bfail(b, TP_ERR_CUDA, "batch: fork");
+  for (int c = 0; c < 3; c++) {
+    const int m = (int)b->h_cls[c].size();
+    if (m == 0) continue;
+    cudaStream_t cs = b->cls_stream[c];
+    if (cudaStreamWaitEvent(cs, b->ev_fork, 0) != cudaSuccess ||
+        launch_fused_batch(c, b->h_cls[c].data(), b->d_cls[c], b->d_cls_off[c], m, b->cls_units[c], cs) !=
+            cudaSuccess ||
+        cudaEventRecord(b->ev_join[c], cs) != cudaSuccess || cudaStreamWaitEvent(st, b->ev_join[c], 0) != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b, TP_ERR_CUDA, "batch: forward");
+    }
   }
   for (tp_handle *h : b->scenes) h->fwd_valid = 1;
   return TP_OK;
@@ -1045,13 +1081,19 @@ tp_status tp_batch_create(tp_handle *const *scenes, int n, tp_batch **out) {
     if (!h->have_tasks || !h->have_corr || h->num_pairs == 0) return TP_ERR_STATE;
     const bool split = h->cfg.num_colors == 1 && h->num_pairs > 8;
     if (!split && h->cfg.num_sensors * h->cfg.num_colors > 16) return TP_ERR_ARG;  // warp-per-tile smem
+    if (h->cfg.num_colors == 3 && h->num_pairs > 8) return TP_ERR_ARG;
   }
   tp_batch *b = new tp_batch();
   b->scenes.assign(scenes, scenes + n);
   b->device = dev;
   bool ok = cudaSetDevice(dev) == cudaSuccess &&
             cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
-            dalloc(&b->d_scenes, n) == cudaSuccess && dalloc(&b->d_off, n + 1) == cudaSuccess;
+            cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+            dalloc(&b->d_scenes, n) == cudaSuccess && dalloc(&b->d_task_off, n + 1) == cudaSuccess;
+  for (int c = 0; ok && c < 3; c++)
+    ok = cudaStreamCreateWithFlags(&b->cls_stream[c], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&b->ev_join[c], cudaEventDisableTiming) == cudaSuccess &&
+         dalloc(&b->d_cls[c], n) == cudaSuccess && dalloc(&b->d_cls_off[c], n + 1) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     tp_batch_destroy(b);
@@ -1065,7 +1107,14 @@ tp_status tp_batch_destroy(tp_batch *b) {
   if (!b) return TP_ERR_ARG;
   batch_drop_graph(b);
   cudaFree(b->d_scenes);
-  cudaFree(b->d_off);
+  cudaFree(b->d_task_off);
+  for (int c = 0; c < 3; c++) {
+    cudaFree(b->d_cls[c]);
+    cudaFree(b->d_cls_off[c]);
+    if (b->cls_stream[c]) cudaStreamDestroy(b->cls_stream[c]);
+    if (b->ev_join[c]) cudaEventDestroy(b->ev_join[c]);
+  }
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return TP_OK;

@@ -138,10 +138,14 @@ cudaError_t upload_kernel_constants();
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st);
 cudaError_t upload_fused_constants();
 int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);
-// batched persistent forward over many scenes (tp_fused.cu)
+// batched plans (tp_plan.cu) and persistent forward over many scenes (tp_fused.cu):
+// scene classes 0 = colour warp-per-tile, 1 = mono warp-per-tile, 2 = mono pair-per-warp
+cudaError_t launch_plan_batch(const SceneDev *scenes_dev, const int *task_off_dev, int n, int total_tasks,
+                              cudaStream_t st);
+int batch_class(const SceneDev &sc);
 int batch_units(const SceneDev &sc);
-cudaError_t launch_fused_batch(const SceneDev *scenes_host, const SceneDev *scenes_dev, const int *unit_off_dev,
-                               int n, int total_units, cudaStream_t st);
+cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const SceneDev *scenes_dev,
+                               const int *unit_off_dev, int n, int total_units, cudaStream_t st);
 // task compaction into a fixed device scratch array (tp_plan.cu), no allocation
 int compact_scratch_max_tiles();
 cudaError_t compact_scratch_address(int **ptr);

@@ -138,9 +138,7 @@ __device__ __forceinline__ void sensor_port(const GeomDev &g, double pXc, double
 // corner and residual shift (ImageDtt.java:4904-4943).  A division by a
 // power-of-two kernel step is replaced by the multiplication with its exact
 // reciprocal, which IEEE rounding makes bit-identical.
-__global__ void plan_kernel(SceneDev sc) {
-  const int task = blockIdx.x * blockDim.x + threadIdx.x;
-  if (task >= sc.num_tasks) return;
+__device__ __forceinline__ void plan_task(const SceneDev &sc, int task) {
   const int S = sc.num_sensors, C = sc.num_colors;
   const int txy = sc.task_txy[task];
   const int tx = txy & 0xffff, ty = txy >> 16;
@@ -205,6 +203,29 @@ __global__ void plan_kernel(SceneDev sc) {
   }
 }
 
+__global__ void plan_kernel(SceneDev sc) {
+  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  if (task < sc.num_tasks) plan_task(sc, task);
+}
+
+// the plans of a batch of scenes in one launch: thread per task of the
+// concatenated task lists, scene found by binary search over the task offsets
+__global__ void plan_batch_kernel(const SceneDev *__restrict__ scenes, const int *__restrict__ task_off, int n) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= task_off[n]) return;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (task_off[mid] <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  const SceneDev &sc = scenes[lo];
+  const int task = g - task_off[lo];
+  plan_task(sc, task);
+  const int txy = sc.task_txy[task];
+  sc.tile_task[(txy >> 16) * sc.tilesX + (txy & 0xffff)] = task;
+}
+
 __global__ void tile_task_map_kernel(SceneDev sc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < sc.num_tasks) {
@@ -260,6 +281,14 @@ cudaError_t launch_plan(const SceneDev &sc, cudaStream_t st) {
   const int n = sc.num_tasks;
   if (n <= 0) return cudaSuccess;
   plan_kernel<<<(n + 63) / 64, 64, 0, st>>>(sc);
+  return cudaGetLastError();
+}
+
+// tile maps are cleared by the caller (cudaMemsetAsync per scene) before this launch
+cudaError_t launch_plan_batch(const SceneDev *scenes_dev, const int *task_off_dev, int n, int total_tasks,
+                              cudaStream_t st) {
+  if (total_tasks <= 0) return cudaSuccess;
+  plan_batch_kernel<<<(total_tasks + 63) / 64, 64, 0, st>>>(scenes_dev, task_off_dev, n);
   return cudaGetLastError();
 }
 

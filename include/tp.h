@@ -209,10 +209,11 @@ tp_status tp_get_texture_aux(tp_handle *h, float *aux);
  * GPUTileProcessor instance and launch) ----
  * A batch runs the forward of many scenes -- handles of any sensor count,
  * colours, size and pair set, all on one device, each with its tasks and
- * correlation set up -- as one persistent kernel over a queue of tiles in
- * scene order (4 tiles per unit for warp-per-tile scenes, 1 tile shared by 4
- * warps for mono scenes with more than 8 pairs).  Colour scenes need
- * sensors x colours <= 16.  The handles stay owned by the caller and must
+ * correlation set up -- as one launch of the plans of all scenes and one
+ * persistent forward kernel per schedule class (colour warp-per-tile, mono
+ * warp-per-tile, mono with more than 8 pairs: 4 warps per tile) over a queue
+ * of tiles in scene order, the classes running concurrently.  Colour scenes
+ * need sensors x colours <= 16 and at most 8 pairs.  The handles stay owned by the caller and must
  * outlive the batch; results are read through each handle's getters. */
 typedef struct tp_batch tp_batch;
 tp_status tp_batch_create(tp_handle *const *scenes, int num_scenes, tp_batch **out);
