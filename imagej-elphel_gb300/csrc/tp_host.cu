@@ -859,8 +859,9 @@ struct tp_batch {
   std::vector<tp_handle *> scenes;
   std::vector<SceneDev> h_scenes;           // all scenes, for the batched plan
   std::vector<int> h_task_off, graph_tasks;
-  std::vector<SceneDev> h_cls[3];           // per schedule class
+  std::vector<SceneDev> h_cls[3];           // per schedule class: scenes sharing the persistent queue
   std::vector<int> h_cls_off[3];
+  std::vector<tp_handle *> solo[3];         // scenes large enough to keep their own launch
   int cls_units[3] = {0, 0, 0};
   SceneDev *d_scenes = nullptr, *d_cls[3] = {nullptr, nullptr, nullptr};
   int *d_task_off = nullptr, *d_cls_off[3] = {nullptr, nullptr, nullptr};
@@ -886,6 +887,9 @@ static tp_status batch_tables(tp_batch *b) {
     b->h_cls[c].clear();
     b->h_cls_off[c].assign(1, 0);
   }
+  for (int c = 0; c < 3; c++) b->solo[c].clear();
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   int t = 0;
   for (int i = 0; i < n; i++) {
     const SceneDev sc = scene_of(b->scenes[i]);
@@ -893,6 +897,12 @@ static tp_status batch_tables(tp_batch *b) {
     b->h_task_off[i] = t;
     t += sc.num_tasks;
     const int c = batch_class(sc);
+    // a warp-per-tile scene with at least 8 waves of tiles (16 warps per SM) has no tail
+    // worth sharing: it keeps its own launch, captured in the same graph
+    if (c != 2 && sc.num_tasks >= 8 * 16 * sms) {
+      b->solo[c].push_back(b->scenes[i]);
+      continue;
+    }
     b->h_cls[c].push_back(sc);
     b->h_cls_off[c].push_back(b->h_cls_off[c].back() + batch_units(sc));
   }
@@ -938,12 +948,16 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
   if (cudaEventRecord(b->ev_fork, st) != cudaSuccess) return bfail(b, TP_ERR_CUDA, "batch: fork");
   for (int c = 0; c < 3; c++) {
     const int m = (int)b->h_cls[c].size();
-    if (m == 0) continue;
+    if (m == 0 && b->solo[c].empty()) continue;
     cudaStream_t cs = b->cls_stream[c];
-    if (cudaStreamWaitEvent(cs, b->ev_fork, 0) != cudaSuccess ||
-        launch_fused_batch(c, b->h_cls[c].data(), b->d_cls[c], b->d_cls_off[c], m, b->cls_units[c], cs) !=
-            cudaSuccess ||
-        cudaEventRecord(b->ev_join[c], cs) != cudaSuccess || cudaStreamWaitEvent(st, b->ev_join[c], 0) != cudaSuccess) {
+    bool ok = cudaStreamWaitEvent(cs, b->ev_fork, 0) == cudaSuccess;
+    for (tp_handle *h : b->solo[c])
+      ok = ok && launch_fused_forward(scene_of(h), h->corr_host, h->sched_tpb, h->sched_nw, cs) == cudaSuccess;
+    if (m > 0)
+      ok = ok && launch_fused_batch(c, b->h_cls[c].data(), b->d_cls[c], b->d_cls_off[c], m, b->cls_units[c], cs) ==
+                     cudaSuccess;
+    ok = ok && cudaEventRecord(b->ev_join[c], cs) == cudaSuccess && cudaStreamWaitEvent(st, b->ev_join[c], 0) == cudaSuccess;
+    if (!ok) {
       cudaGetLastError();
       return bfail(b, TP_ERR_CUDA, "batch: forward");
     }

@@ -212,8 +212,10 @@ tp_status tp_get_texture_aux(tp_handle *h, float *aux);
  * correlation set up -- as one launch of the plans of all scenes and one
  * persistent forward kernel per schedule class (colour warp-per-tile, mono
  * warp-per-tile, mono with more than 8 pairs: 4 warps per tile) over a queue
- * of tiles in scene order, the classes running concurrently.  Colour scenes
- * need sensors x colours <= 16 and at most 8 pairs.  The handles stay owned by the caller and must
+ * of tiles in scene order, the classes running concurrently.  Warp-per-tile
+ * scenes with at least 8 waves of tiles (8 x 16 x SM count) keep their own
+ * forward launch inside the same step (they have no tail to share).  Colour
+ * scenes need sensors x colours <= 16 and at most 8 pairs.  The handles stay owned by the caller and must
  * outlive the batch; results are read through each handle's getters. */
 typedef struct tp_batch tp_batch;
 tp_status tp_batch_create(tp_handle *const *scenes, int num_scenes, tp_batch **out);

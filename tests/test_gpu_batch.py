@@ -1,7 +1,7 @@
 """Batched persistent forward (tp_batch_*) vs the per-scene forward on the GPU:
-three scenes of different kinds (4 Bayer sensors with kernel tables, 4 mono
-sensors, 16 mono sensors with 120 pairs) in one launch and through a captured
-CUDA graph.  The batch runs the same per-tile code as the per-scene kernels,
+four scenes of different kinds (4 Bayer sensors with kernel tables, 4 mono
+sensors, 16 mono sensors with 120 pairs, and a large 4-sensor Bayer scene that
+keeps its own launch) in one batch step and through a captured CUDA graph.  The batch runs the same per-tile code as the per-scene kernels,
 so CLT, correlation surfaces and disparities agree to FP32 rounding."""
 import numpy as np
 import pytest
@@ -22,6 +22,8 @@ def _scenes():
     out.append((synth.make_scene("quad_mono", seed=52, width=128, height=96), None, None, None, 3.0))
     sc = synth.make_scene("circle_lwir", seed=53, width=160, height=128)
     out.append((sc, None, None, synth.circle_pairs(sc["geometry"]), 2.0))
+    # 162 x 121 = 19602 tiles: enough waves to keep its own launch inside the batch
+    out.append((synth.make_scene("quad_bayer", seed=54, width=1296, height=968), None, None, None, 3.0))
     return out
 
 
