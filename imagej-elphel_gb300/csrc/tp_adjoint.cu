@@ -169,7 +169,7 @@ __device__ __forceinline__ void dtt2e_transposed(const float y[8], float x[8], b
   }
 }
 
-__global__ void __launch_bounds__(32 * AD_NW) adjoint_kernel(const __grid_constant__ SceneDev sc,
+__global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_constant__ SceneDev sc,
                                                              const __grid_constant__ AdjShape as,
                                                              const __grid_constant__ CorrConst cfg, float *sens,
                                                              float *dval) {

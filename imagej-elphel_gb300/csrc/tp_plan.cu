@@ -138,7 +138,8 @@ __device__ __forceinline__ void sensor_port(const GeomDev &g, double pXc, double
 // corner and residual shift (ImageDtt.java:4904-4943).  A division by a
 // power-of-two kernel step is replaced by the multiplication with its exact
 // reciprocal, which IEEE rounding makes bit-identical.
-__device__ __forceinline__ void plan_task(const SceneDev &sc, int task) {
+// sensors [s0, s1) of one task
+__device__ __forceinline__ void plan_task(const SceneDev &sc, int task, int s0, int s1) {
   const int S = sc.num_sensors, C = sc.num_colors;
   const int txy = sc.task_txy[task];
   const int tx = txy & 0xffff, ty = txy >> 16;
@@ -151,7 +152,7 @@ __device__ __forceinline__ void plan_task(const SceneDev &sc, int task) {
   const int ks = sc.kernel_step;
   const bool pow2 = ks > 0 && (ks & (ks - 1)) == 0;
   const double inv_ks = pow2 ? 1.0 / (double)ks : 0.0;
-  for (int s = 0; s < S; s++) {
+  for (int s = s0; s < s1; s++) {
     double cx, cy;
     if (sc.ports_from_geometry) {
       if (sc.port_deriv) {
@@ -203,9 +204,14 @@ __device__ __forceinline__ void plan_task(const SceneDev &sc, int task) {
   }
 }
 
+// thread per (task, group of up to 4 sensors): 16-sensor scenes get 4x the threads
 __global__ void plan_kernel(SceneDev sc) {
-  const int task = blockIdx.x * blockDim.x + threadIdx.x;
-  if (task < sc.num_tasks) plan_task(sc, task);
+  const int groups = (sc.num_sensors + 3) >> 2;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc.num_tasks * groups) return;
+  const int task = i / groups, g = i - task * groups;
+  const int s0 = g * 4, s1 = (s0 + 4 < sc.num_sensors) ? s0 + 4 : sc.num_sensors;
+  plan_task(sc, task, s0, s1);
 }
 
 // the plans of a batch of scenes in one launch: thread per task of the
@@ -221,7 +227,7 @@ __global__ void plan_batch_kernel(const SceneDev *__restrict__ scenes, const int
   }
   const SceneDev &sc = scenes[lo];
   const int task = g - task_off[lo];
-  plan_task(sc, task);
+  plan_task(sc, task, 0, sc.num_sensors);
   const int txy = sc.task_txy[task];
   sc.tile_task[(txy >> 16) * sc.tilesX + (txy & 0xffff)] = task;
 }
@@ -278,7 +284,7 @@ __global__ void compact_tasks_kernel(const int *tile_op, const float *disparity,
 }
 
 cudaError_t launch_plan(const SceneDev &sc, cudaStream_t st) {
-  const int n = sc.num_tasks;
+  const int n = sc.num_tasks * ((sc.num_sensors + 3) / 4);
   if (n <= 0) return cudaSuccess;
   plan_kernel<<<(n + 63) / 64, 64, 0, st>>>(sc);
   return cudaGetLastError();
