@@ -429,6 +429,9 @@ def run_ours(args):
     # imclt: inverse CLT into the colour frames; textures: RGBA texture tiles (quad colour only)
     stages = ["ports", "forward", "imclt"]
     fns = [lib.tp_ports, lib.tp_process, lib.tp_imclt]
+    # schedule of the fused forward picked by the project's autotuner on this scene (outside the timing)
+    from tileproc.autotune import autotune
+    sched, sched_ms = autotune(tp, reps=5, warmup=2)
     with_tex = S == 4 and Cn == 3
     if with_tex:
         tp.setTextureParams()
@@ -540,6 +543,8 @@ def run_ours(args):
                    "stages": "ports(fp64)+fused(convert_correct,correlate,extract)+imclt" + (
                        "+textures(12 rows)" if with_tex else ""),
                    "l2": "per-step working set %.2f GB > 129 MB L2, no flush" % (total_b / 1e9),
+                   "schedule": {"tiles_per_cta": sched[0], "warps_per_cta": sched[1],
+                                "autotune_ms": {"%d,%d" % k: round(v, 4) for k, v in sched_ms.items()}},
                    "parallelism": "replicas" if world > 1 else "single"},
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
         "algorithmic_bytes_per_step": total_b,

@@ -829,7 +829,7 @@ static FwdShape make_shape(const SceneDev &sc, int nw) {
   // getMaxXCm clips the strip to the y-window (Correlation2d.java:944-951)
   f.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
   f.quad = (sc.num_pairs <= 8) ? 1 : 0;
-  f.nw = nw > 0 ? nw : (f.C == 3 ? 1 : 4);  // one-warp CTAs pack best when the tile CLT is large
+  f.nw = nw > 0 ? nw : (f.C == 3 ? 2 : 4);  // the autotuner's pick on 4x2592x1936 Bayer and 4x512x384 mono
   f.clt_floats = f.S * f.C * TP_CLT;
   f.per_warp = f.clt_floats + SCR;
   f.per_warp = (f.per_warp + 3) & ~3;
