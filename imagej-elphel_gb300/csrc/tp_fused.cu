@@ -218,7 +218,8 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
 }
 
 // phase B for pair pi: correlation surface to HBM, strip entries folded into cmb
-template <int C>
+// (NT = strip entries per lane / 32 rounded up: 1 when the extraction reads <= 32 entries)
+template <int C, int NT>
 __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, size_t tile, int P, int pi, int RE,
                                          bool log_mode, const short *strip_code, const float *s_clt, float *scr,
                                          int lane, float cmb[8]) {
@@ -303,7 +304,7 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
   for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
   if (pd.in_combo) {
 #pragma unroll
-    for (int t = 0; t < 8; t++) {
+    for (int t = 0; t < NT; t++) {
       const int e = lane + 32 * t;
       if (e < RE) {
         const int row = e / 15;
@@ -334,13 +335,14 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
 }
 
 // phase C: combined strip, integer argmax, centroid, ortho maxima, disparity record
+template <int NT>
 __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
                                             bool log_mode, int ncomb, size_t tile, float *scr, int lane,
                                             const float cmb[8]) {
   // ---------------- stage 3c: extraction ----------------
   float *combo = scr;
 #pragma unroll
-  for (int t = 0; t < 8; t++) {
+  for (int t = 0; t < NT; t++) {
     const int e = lane + 32 * t;
     if (e < RE) {
       float v = cmb[t];
@@ -463,7 +465,7 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
 // ---------------------------------------------------------------------------
 // warp-per-tile schedule: one warp carries a tile through all stages, no CTA barriers
 // ---------------------------------------------------------------------------
-template <int C>  // colours: 1 (mono) or 3 (Bayer R, B, G)
+template <int C, int NT>  // colours: 1 (mono) or 3 (Bayer R, B, G); strip entries per lane / 32
 __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_constant__ SceneDev sc,
                                                                const __grid_constant__ FwdShape fs,
                                                                const __grid_constant__ CorrConst cfg) {
@@ -484,9 +486,9 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
     __syncwarp();
     float cmb[8];
 #pragma unroll
-    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
-    for (int pi = 0; pi < P; pi++) fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
-    fwd_extract(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+    for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    for (int pi = 0; pi < P; pi++) fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+    fwd_extract<NT>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
   }
 }
 
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
 // combines their partial strip products for the extraction.  For many pairs
 // (16 sensors, 120 pairs) this holds one CLT per CTA instead of one per warp.
 // ---------------------------------------------------------------------------
-template <int C>
+template <int C, int NT>
 __global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_constant__ SceneDev sc,
                                                           const __grid_constant__ FwdShape fs,
                                                           const __grid_constant__ CorrConst cfg) {
@@ -517,18 +519,18 @@ __global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_consta
     __syncthreads();
     float cmb[8];
 #pragma unroll
-    for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
     for (int pi = warp; pi < P; pi += NW)
-      fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+      fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
-    for (int t = 0; t < 8; t++) {
+    for (int t = 0; t < NT; t++) {
       const int e = lane + 32 * t;
       if (e < RE) part[warp * 240 + e] = cmb[t];
     }
     __syncthreads();  // also makes the surfaces every warp wrote visible to warp 0
     if (warp == 0) {
 #pragma unroll
-      for (int t = 0; t < 8; t++) {
+      for (int t = 0; t < NT; t++) {
         const int e = lane + 32 * t;
         if (e < RE) {
           float v = part[e];
@@ -536,7 +538,7 @@ __global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_consta
           cmb[t] = v;
         }
       }
-      fwd_extract(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+      fwd_extract<NT>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
     }
     __syncthreads();
   }
@@ -569,7 +571,7 @@ int batch_units(const SceneDev &sc) {
   return (sc.num_tasks + nw - 1) / nw;
 }
 
-template <int C, bool SPLIT, int NW>
+template <int C, bool SPLIT, int NW, int NT>
 __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
     fused_batch_kernel(const SceneDev *__restrict__ scenes, const int *__restrict__ unit_off, int nscenes,
                        int total_units, int warp_floats, int cfg_floats) {
@@ -621,18 +623,18 @@ __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
       __syncthreads();
       float cmb[8];
 #pragma unroll
-      for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+      for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
       for (int pi = warp; pi < P; pi += NW)
-        fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+        fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
-      for (int t = 0; t < 8; t++) {
+      for (int t = 0; t < NT; t++) {
         const int e = lane + 32 * t;
         if (e < RE) part[warp * 240 + e] = cmb[t];
       }
       __syncthreads();
       if (warp == 0) {
 #pragma unroll
-        for (int t = 0; t < 8; t++) {
+        for (int t = 0; t < NT; t++) {
           const int e = lane + 32 * t;
           if (e < RE) {
             float v = part[e];
@@ -640,7 +642,7 @@ __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
             cmb[t] = v;
           }
         }
-        fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+        fwd_extract<NT>(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
       __syncthreads();
     } else {
@@ -654,10 +656,10 @@ __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
         __syncwarp();
         float cmb[8];
 #pragma unroll
-        for (int t = 0; t < 8; t++) cmb[t] = log_mode ? 0.f : 1.f;
+        for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
         for (int pi = 0; pi < P; pi++)
-          fwd_pair<C>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
-        fwd_extract(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+          fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+        fwd_extract<NT>(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
     }
   }
@@ -683,9 +685,12 @@ cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const Scene
                                const int *unit_off_dev, int n, int total_units, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   if (n > BATCH_MAX) return cudaErrorInvalidValue;
-  int wf = 0, sp = 0, maxp = 0;
+  int wf = 0, sp = 0, maxp = 0, maxre = 0;
   for (int i = 0; i < n; i++) {
     maxp = scenes_host[i].num_pairs > maxp ? scenes_host[i].num_pairs : maxp;
+    const int re = (scenes_host[i].strip_rows < scenes_host[i].wndy_size ? scenes_host[i].strip_rows
+                                                                         : scenes_host[i].wndy_size) * 15;
+    maxre = re > maxre ? re : maxre;
     const SceneDev &sc = scenes_host[i];
     if (batch_class(sc) != cls || sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidValue;
     const int ntiles = sc.tilesX * sc.tilesY;
@@ -698,12 +703,20 @@ cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const Scene
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || total_units <= 0) return e;
   const int cf = (int)(((offsetof(CorrConst, pairs) + maxp * sizeof(PairDev)) + 15) / 16 * 4);
-  if (cls == 0) return launch_batch_k(fused_batch_kernel<3, false, 1>, 32, (cf + wf) * 4, total_units, scenes_dev,
+  if (maxre <= 32) {
+    if (cls == 0) return launch_batch_k(fused_batch_kernel<3, false, 1, 1>, 32, (cf + wf) * 4, total_units,
+                                        scenes_dev, unit_off_dev, n, wf, cf, st);
+    if (cls == 1) return launch_batch_k(fused_batch_kernel<1, false, 4, 1>, 128, (cf + 4 * wf) * 4, total_units,
+                                        scenes_dev, unit_off_dev, n, wf, cf, st);
+    return launch_batch_k(fused_batch_kernel<1, true, 4, 1>, 128, (cf + sp) * 4, total_units, scenes_dev,
+                          unit_off_dev, n, 0, cf, st);
+  }
+  if (cls == 0) return launch_batch_k(fused_batch_kernel<3, false, 1, 8>, 32, (cf + wf) * 4, total_units, scenes_dev,
                                       unit_off_dev, n, wf, cf, st);
-  if (cls == 1) return launch_batch_k(fused_batch_kernel<1, false, 4>, 128, (cf + 4 * wf) * 4, total_units,
+  if (cls == 1) return launch_batch_k(fused_batch_kernel<1, false, 4, 8>, 128, (cf + 4 * wf) * 4, total_units,
                                       scenes_dev, unit_off_dev, n, wf, cf, st);
-  return launch_batch_k(fused_batch_kernel<1, true, 4>, 128, (cf + sp) * 4, total_units, scenes_dev, unit_off_dev, n,
-                        0, cf, st);
+  return launch_batch_k(fused_batch_kernel<1, true, 4, 8>, 128, (cf + sp) * 4, total_units, scenes_dev, unit_off_dev,
+                        n, 0, cf, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -875,12 +888,19 @@ cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tp
   if (f.nw > 4) return cudaErrorInvalidConfiguration;
   if (tpb == 1 && f.nw > 1) {
     const int bytes = split_smem_floats(f) * 4;
+    if (f.RE <= 32)
+      return sc.num_colors == 3
+                 ? launch_persistent(fused_split_kernel<3, 1>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st)
+                 : launch_persistent(fused_split_kernel<1, 1>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st);
     return sc.num_colors == 3
-               ? launch_persistent(fused_split_kernel<3>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st)
-               : launch_persistent(fused_split_kernel<1>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st);
+               ? launch_persistent(fused_split_kernel<3, 8>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st)
+               : launch_persistent(fused_split_kernel<1, 8>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st);
   }
   const int bytes = f.per_warp * f.nw * 4;
   const int units = (sc.num_tasks + f.nw - 1) / f.nw;
-  return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3>, f.nw * 32, bytes, units, sc, f, cc, st)
-                            : launch_persistent(fused_forward_kernel<1>, f.nw * 32, bytes, units, sc, f, cc, st);
+  if (f.RE <= 32)
+    return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3, 1>, f.nw * 32, bytes, units, sc, f, cc, st)
+                              : launch_persistent(fused_forward_kernel<1, 1>, f.nw * 32, bytes, units, sc, f, cc, st);
+  return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3, 8>, f.nw * 32, bytes, units, sc, f, cc, st)
+                            : launch_persistent(fused_forward_kernel<1, 8>, f.nw * 32, bytes, units, sc, f, cc, st);
 }
