@@ -727,12 +727,12 @@ cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const Scene
 // without atomics and in a fixed order.  A warp carries 4 tiles at once, one per
 // 8-lane group, lane r owning row r of each quadrant.
 // ---------------------------------------------------------------------------
-constexpr int IR = 8;            // region = IR x IR blocks of 8x8 pixels
-constexpr int IPX = IR * 8;
-constexpr int ISTR = IPX + 1;
+constexpr int IMCLT_IR = 16;     // region = IR x IR blocks of 8x8 pixels
 
+template <int IR>
 __global__ void __launch_bounds__(256) imclt_fast_kernel(const __grid_constant__ SceneDev sc) {
-  __shared__ float acc[IPX * ISTR];
+  constexpr int IPX = IR * 8, ISTR = IPX + 1;
+  extern __shared__ float acc[];  // [IPX][ISTR]
   __shared__ float tbuf_all[8][4 * 72];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
   const int S = sc.num_sensors, C = sc.num_colors;
@@ -818,8 +818,12 @@ __global__ void __launch_bounds__(256) imclt_fast_kernel(const __grid_constant__
 }
 
 cudaError_t launch_imclt_fast(const SceneDev &sc, cudaStream_t st) {
+  constexpr int IR = IMCLT_IR;
+  const int bytes = IR * 8 * (IR * 8 + 1) * 4;
+  cudaError_t e = cudaFuncSetAttribute(imclt_fast_kernel<IR>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
   dim3 grid((sc.tilesX + 1 + IR - 1) / IR, (sc.tilesY + 1 + IR - 1) / IR, sc.num_sensors * sc.num_colors);
-  imclt_fast_kernel<<<grid, 256, 0, st>>>(sc);
+  imclt_fast_kernel<IR><<<grid, 256, bytes, st>>>(sc);
   return cudaGetLastError();
 }
 
