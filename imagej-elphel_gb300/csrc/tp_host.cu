@@ -41,6 +41,8 @@ struct tp_handle {
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
   float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
+  float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
+  size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
   float *d_partial = nullptr, *d_grad_e = nullptr, *d_dldd = nullptr;
@@ -70,6 +72,10 @@ static tp_status cuda_fail(tp_handle *h, cudaError_t e, const char *where) {
     cudaError_t e_ = (call);                               \
     if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
   } while (0)
+
+extern "C" {
+static tp_status d2h(tp_handle *h, void *dst, const void *src, size_t bytes, const char *where);
+}
 
 static cudaStream_t pick_stream(tp_handle *h, void *s) { return s ? (cudaStream_t)s : h->stream; }
 
@@ -338,6 +344,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && upload_fused_constants() == cudaSuccess;
   ok = ok && upload_texture_constants() == cudaSuccess;
   ok = ok && upload_adjoint_constants() == cudaSuccess;
+  ok = ok && upload_kernprep_constants() == cudaSuccess;
   tp_default_texture_params(&h->tex_params);
   for (int s = 0; ok && s < S; s++) {
     ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
@@ -388,7 +395,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo};
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -452,6 +459,56 @@ tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const floa
   h->planned = 0;
   h->fwd_valid = 0;
   return TP_OK;
+}
+
+tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_device, int normalize, int coord_corr,
+                          void *stream) {
+  if (!h || !psf) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_calc_kernels: bad camera");
+  if (h->cfg.kernels_hor <= 0) return fail(h, TP_ERR_STATE, "tp_calc_kernels: handle created without kernels");
+  cudaStream_t st = pick_stream(h, stream);
+  const size_t nk = (size_t)h->cfg.kernels_hor * h->cfg.kernels_vert * h->cfg.num_colors;
+  if (psf_on_device) {
+    CK(launch_kernel_prep(psf, (int)nk, normalize, h->d_kern[cam], h->d_kext[cam], st), "tp_calc_kernels");
+  } else {
+    const size_t chunk = nk < 8192 ? nk : 8192;  // kernel tiles per staged upload (128 MB)
+    if (h->psf_stage_kernels < chunk) {
+      cudaFree(h->d_psf_stage);
+      h->d_psf_stage = nullptr;
+      h->psf_stage_kernels = 0;
+      if (dalloc(&h->d_psf_stage, chunk * 4096) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, TP_ERR_NOMEM, "tp_calc_kernels: PSF staging buffer");
+      }
+      h->psf_stage_kernels = chunk;
+    }
+    for (size_t k0 = 0; k0 < nk; k0 += chunk) {
+      const size_t n = (nk - k0) < chunk ? (nk - k0) : chunk;
+      CK(cudaMemcpyAsync(h->d_psf_stage, psf + k0 * 4096, n * 4096 * sizeof(float), cudaMemcpyHostToDevice, st),
+         "tp_calc_kernels");
+      CK(launch_kernel_prep(h->d_psf_stage, (int)n, normalize, h->d_kern[cam] + k0 * TP_CLT, h->d_kext[cam] + k0 * 8,
+                            st),
+         "tp_calc_kernels");
+      CK(cudaStreamSynchronize(st), "tp_calc_kernels");  // the staging buffer is reused
+    }
+  }
+  if (coord_corr)
+    CK(launch_fill_coord_corr(h->d_kext[cam], h->cfg.kernels_hor, h->cfg.kernels_vert, h->cfg.num_colors,
+                              h->cfg.kernel_step, st),
+       "tp_calc_kernels");
+  h->planned = 0;
+  h->fwd_valid = 0;
+  return TP_OK;
+}
+
+tp_status tp_get_kernels(tp_handle *h, int cam, float *kernels, float *kernel_offsets) {
+  if (!h) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors || h->cfg.kernels_hor <= 0) return fail(h, TP_ERR_ARG, "tp_get_kernels");
+  const size_t nk = (size_t)h->cfg.kernels_hor * h->cfg.kernels_vert * h->cfg.num_colors;
+  tp_status r = TP_OK;
+  if (kernels) r = d2h(h, kernels, h->d_kern[cam], nk * TP_CLT * sizeof(float), "tp_get_kernels");
+  if (r == TP_OK && kernel_offsets) r = d2h(h, kernel_offsets, h->d_kext[cam], nk * 8 * sizeof(float), "tp_get_kernels");
+  return r;
 }
 
 tp_status tp_set_color_scales(tp_handle *h, const float *scales) {

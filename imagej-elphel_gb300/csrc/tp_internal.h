@@ -158,6 +158,11 @@ int adjoint_smem_bytes(int S);
 cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st);
+// kernel preparation from PSFs (tp_kernprep.cu)
+cudaError_t upload_kernprep_constants();
+cudaError_t launch_kernel_prep(const float *psf_dev, int nk, int normalize, float *clt_out, float *ext_out,
+                               cudaStream_t st);
+cudaError_t launch_fill_coord_corr(float *ext, int kh, int kv, int C, int kern_step, cudaStream_t st);
 // texture tiles (tp_texture.cu)
 cudaError_t launch_textures(const SceneDev &sc, const TexConst &tc, cudaStream_t st);
 cudaError_t upload_texture_constants();

@@ -91,6 +91,26 @@ class GPUTileProcessor:
         for cam in range(self.num_sensors):
             self.setConvolutionKernel(kernels[cam], kernel_offsets[cam], cam, layout)
 
+    def calcConvolutionKernels(self, psf, ncam, normalize=True, coord_corr=True, device_ptr=None, stream=None):
+        """QuadCLT.calculateCLTKernel on the device: psf [kv][kh][C][64][64] float (host array), or
+        device_ptr (an int address of the same layout in device memory)."""
+        if device_ptr is not None:
+            self._ck(self._lib.tp_calc_kernels(self.h, int(ncam), C.c_void_p(int(device_ptr)), 1, int(normalize),
+                                               int(coord_corr), stream), "tp_calc_kernels")
+            return
+        p = np.ascontiguousarray(psf, dtype=np.float32)
+        n = self.kernels_vert * self.kernels_hor * self.num_colors
+        assert p.size == n * 4096, "psf must be [kernels_vert][kernels_hor][num_colors][64][64]"
+        self._ck(self._lib.tp_calc_kernels(self.h, int(ncam), _ptr(p), 0, int(normalize), int(coord_corr), stream),
+                 "tp_calc_kernels")
+
+    def getConvolutionKernels(self, ncam):
+        """(kernels [kv][kh][C][4][64], offsets [kv][kh][C][8]) of one sensor (TP_KERNELS_CPU layout)."""
+        k = np.zeros((self.kernels_vert, self.kernels_hor, self.num_colors, 4, 64), dtype=np.float32)
+        e = np.zeros((self.kernels_vert, self.kernels_hor, self.num_colors, 8), dtype=np.float32)
+        self._ck(self._lib.tp_get_kernels(self.h, int(ncam), _ptr(k), _ptr(e)), "tp_get_kernels")
+        return k, e
+
     def setBayerImage(self, image, ncam):
         img = np.ascontiguousarray(image)
         if img.shape != (self.height, self.width):

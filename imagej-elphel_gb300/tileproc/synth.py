@@ -195,6 +195,27 @@ def bayer_planes(mosaic, color_index, scales=(1.0, 1.0, 0.5)):
     return np.stack([np.where(color_index == c, m * scales[c], 0.0) for c in range(3)])
 
 
+def psf_kernels(rng, kv, kh, num_colors, sigma=(0.6, 1.4), offset=0.3):
+    """Double-resolution (64x64, 0.5-px pitch) elliptical Gaussian PSFs for one sensor:
+    [kv][kh][C][64][64] float32, sigma per axis uniform in `sigma` px, random orientation,
+    centre offset uniform in +-`offset` px -- the input of QuadCLT.calculateCLTKernel."""
+    n = kv * kh * num_colors
+    sx = rng.uniform(*sigma, n) * 2.0
+    sy = rng.uniform(*sigma, n) * 2.0
+    th = rng.uniform(0, np.pi, n)
+    cx = 32.0 + rng.uniform(-offset, offset, n) * 2.0
+    cy = 32.0 + rng.uniform(-offset, offset, n) * 2.0
+    yy, xx = np.mgrid[0:64, 0:64].astype(np.float64)
+    out = np.empty((n, 64, 64), np.float32)
+    for k in range(n):
+        dx, dy = xx - cx[k], yy - cy[k]
+        c, s_ = np.cos(th[k]), np.sin(th[k])
+        u, v = c * dx + s_ * dy, -s_ * dx + c * dy
+        g = np.exp(-0.5 * ((u / sx[k]) ** 2 + (v / sy[k]) ** 2))
+        out[k] = (g / g.sum()).astype(np.float32)
+    return out.reshape(kv, kh, num_colors, 64, 64)
+
+
 def random_clt_kernels(rng, num_sensors, kv, kh, num_colors, strength=0.2, offset=0.5, grad=0.01):
     """Random CLT-domain kernel table ([S][kv][kh][C][4][64], CPU orientation) and
     CltExtra records ([S][kv][kh][C][8]) for exercising the aberration path."""

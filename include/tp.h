@@ -161,6 +161,17 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed_tasks, int num_tasks);
  * (GPUTileProcessor.java:472-527, 686-778) computed on the device in FP64:
  * tiles with tile_op != 0 (ImageDtt tile_op[ty][tx]) become tasks in row-major order. */
 tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *target_disparity);
+/* The aberration-kernel chain of QuadCLT.calculateCLTKernel (QuadCLT.java:433-667,
+ * ImageDtt.java:4625-4734) on the device: psf [kernels_vert][kernels_hor][num_colors][64][64]
+ * double-resolution PSFs (float, host memory, or device memory when psf_on_device) ->
+ * this sensor's kernel table in the TP_KERNELS_CPU layout and its CltExtra records
+ * (data_x, data_y, center_x, center_y); normalize: kernel x window sums to 16
+ * (clt_normalize_kernel); coord_corr: the 3x3 least-squares centre slopes dxc_dx ..
+ * dyc_dy (ImageDtt.clt_fill_coord_corr 4792-4851), else those four are 0. */
+tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_device, int normalize,
+                          int coord_corr, void *stream);
+/* copies a sensor's kernel table (TP_KERNELS_CPU layout) and CltExtra records to the host */
+tp_status tp_get_kernels(tp_handle *h, int cam, float *kernels, float *kernel_offsets);
 /* setLpfRbg (GPUTileProcessor.java:780-812): lpf[num_colors][64] applied by tp_imclt; NULL = off */
 tp_status tp_set_lpf(tp_handle *h, const float *lpf);
 /* correlation set-up (ImageDtt.clt_aberrations_quad_corr_new arguments, ImageDtt.java:1491-1546) */
