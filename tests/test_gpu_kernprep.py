@@ -62,3 +62,28 @@ def test_kernel_preparation_from_device_memory(oracle):
     finally:
         tp.close()
     assert np.array_equal(k_host, k_dev) and np.array_equal(e_host, e_dev)
+
+
+def test_wire_kernel_files_through_both_layouts(tmp_path):
+    """A transposed .kernel dump loaded with the GPUTileProcessor layout and the plain dump loaded
+    with the ImageDtt layout give the same device table."""
+    from tileproc import wire
+    rng = np.random.default_rng(19)
+    W, H = 64, 48
+    kh, kv = W // 16 + 2, H // 16 + 2
+    k = rng.standard_normal((kv, kh, 3, 4, 64)).astype(np.float32)
+    e = rng.standard_normal((kv, kh, 3, 8)).astype(np.float32)
+    prefix = str(tmp_path / "dump")
+    wire.write_kernels(prefix, 0, k, e)
+    wire.write_kernels(prefix, 0, k, e, transposed=True)
+    kt = np.fromfile(wire.kernel_paths(prefix, 0, True)[0], dtype="<f4")
+    kc, ec = wire.read_kernels(prefix, 0, kv, kh, 3)
+    tp = GPUTileProcessor(4, W, H, num_colors=3, kernels_hor=kh, kernels_vert=kv)
+    try:
+        tp.setConvolutionKernel(kt, ec, 1, layout=L.TP_KERNELS_GPU)
+        tp.setConvolutionKernel(kc, ec, 2, layout=L.TP_KERNELS_CPU)
+        a, _ = tp.getConvolutionKernels(1)
+        b, _ = tp.getConvolutionKernels(2)
+    finally:
+        tp.close()
+    assert np.array_equal(a, b) and np.array_equal(b, k)
