@@ -527,13 +527,16 @@ def run_ours(args):
     d2h = np_out.nbytes
 
     def e2e_step():
-        for s in range(S):
-            tp._ck(lib.tp_set_image(tp.h, s, C.c_void_p(np_imgs[s].ctypes.data), 1 if Cn == 3 else 0, 0), "img")
+        # tile ops first (their task count comes back to the host), then the pinned images
+        # enqueued on the processing stream ahead of the kernels, the disparity read back last
         tp._ck(lib.tp_set_tile_ops(tp.h, C.c_void_p(np_op.ctypes.data), C.c_void_p(np_disp.ctypes.data)), "ops")
-        tp._ck(lib.tp_process(tp.h, None), "process")
-        tp._ck(lib.tp_imclt(tp.h, None), "imclt")
+        for s in range(S):
+            tp._ck(lib.tp_set_image_async(tp.h, s, C.c_void_p(np_imgs[s].ctypes.data), 1 if Cn == 3 else 0, 0, sptr),
+                   "img")
+        tp._ck(lib.tp_process(tp.h, sptr), "process")
+        tp._ck(lib.tp_imclt(tp.h, sptr), "imclt")
         if with_tex:
-            tp._ck(lib.tp_textures(tp.h, None), "textures")
+            tp._ck(lib.tp_textures(tp.h, sptr), "textures")
         tp._ck(lib.tp_get_disparity(tp.h, C.c_void_p(np_out.ctypes.data)), "disp")
 
     for _ in range(min(args.warmup, 3)):

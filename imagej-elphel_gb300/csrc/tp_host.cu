@@ -534,6 +534,21 @@ tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size
   return TP_OK;
 }
 
+tp_status tp_set_image_async(tp_handle *h, int cam, const void *image, int dtype, size_t pitch, void *stream) {
+  if (h) h->fwd_valid = 0;
+  if (!h || !image) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_image_async: bad camera");
+  if (dtype != TP_F32 && dtype != TP_U16) return fail(h, TP_ERR_ARG, "tp_set_image_async: bad dtype");
+  size_t es = dtype == TP_U16 ? 2 : 4;
+  if (pitch == 0) pitch = h->cfg.width;
+  if (pitch < (size_t)h->cfg.width) return fail(h, TP_ERR_ARG, "tp_set_image_async: pitch < width");
+  CK(cudaMemcpy2DAsync(h->d_images[cam], h->cfg.width * es, image, pitch * es, h->cfg.width * es, h->cfg.height,
+                       cudaMemcpyHostToDevice, pick_stream(h, stream)),
+     "tp_set_image_async");
+  h->img_dtype[cam] = dtype;
+  return TP_OK;
+}
+
 tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
   if (!h || (!packed && n > 0)) return TP_ERR_ARG;
   if (n < 0 || n > h->ntiles) return fail(h, TP_ERR_ARG, "tp_set_tasks: bad task count");

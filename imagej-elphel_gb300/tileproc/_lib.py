@@ -69,6 +69,7 @@ PROTOTYPES = {
     "tp_set_geometry": [_H, C.POINTER(TpGeometry)],
     "tp_set_kernels": [_H, C.c_int, _vp, _vp, C.c_int],
     "tp_set_image": [_H, C.c_int, _vp, C.c_int, C.c_size_t],
+    "tp_set_image_async": [_H, C.c_int, _vp, C.c_int, C.c_size_t, _vp],
     "tp_set_color_scales": [_H, _vp],
     "tp_set_tasks": [_H, _vp, C.c_int],
     "tp_set_tile_ops": [_H, _vp, _vp],

@@ -151,6 +151,11 @@ tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g);
 tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const float *kernel_offsets, int layout);
 /* setBayerImage (GPUTileProcessor.java:437-450); pitch in elements (0 = width) */
 tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size_t pitch);
+/* as tp_set_image, but only enqueued on `stream` (NULL = the handle's stream): the host buffer
+ * (best page-locked) must stay valid and unchanged until the stream has passed the copy, and
+ * work on other streams that reads this sensor's image must be ordered after it by the caller
+ * (no reference counterpart: setBayerImage copies synchronously) */
+tp_status tp_set_image_async(tp_handle *h, int cam, const void *image, int dtype, size_t pitch, void *stream);
 /* per-colour gain applied while reading the mosaic (QuadCLT.java:181-185 scales green by 0.5
  * before the GPU mosaic is formed); default {1, 1, 1} for R, B, G */
 tp_status tp_set_color_scales(tp_handle *h, const float *scales);
