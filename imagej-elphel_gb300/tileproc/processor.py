@@ -121,8 +121,22 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_set_image(self.h, int(ncam), _ptr(img), dt, 0), "tp_set_image")
 
     def setBayerImages(self, images):
+        """One mosaic (or mono image) per sensor: [S][H][W] float32 or uint16."""
         for cam in range(self.num_sensors):
             self.setBayerImage(images[cam], cam)
+
+    def setBayerPlanes(self, planes, force=True):
+        """GPUTileProcessor.setBayerImages(double[][][] bayer_data, force) (GPUTileProcessor.java:
+        452-468): per sensor the colour planes [C][H*W] (the EyesisCorrections.bayerToDoubleStack
+        split, green already scaled) are summed into one float mosaic and uploaded; with force off
+        a second call is skipped, as in the reference."""
+        if getattr(self, "_planes_set", False) and not force:
+            return
+        for cam in range(self.num_sensors):
+            p = np.asarray(planes[cam], dtype=np.float64).reshape(-1, self.height * self.width)
+            mosaic = p.sum(axis=0).astype(np.float32).reshape(self.height, self.width)
+            self.setBayerImage(mosaic, cam)
+        self._planes_set = True
 
     def setColorScales(self, scales):
         s = np.ascontiguousarray(scales, dtype=np.float32)

@@ -251,3 +251,22 @@ def test_stage_kernels_and_schedules_agree(oracle, sched):
     ok = np.isfinite(ref["disp"][:, oracle.DISP_CM]) & (d_f[:, oracle.DISP_IXY] == ref["disp"][:, oracle.DISP_IXY])
     assert np.abs(d_f[ok, oracle.DISP_CM] - ref["disp"][ok, oracle.DISP_CM]).max() <= DISP_TOL
     assert np.abs(d_f[ok, oracle.DISP_CM] - d_s[ok, oracle.DISP_CM]).max() <= DISP_TOL
+
+
+def test_bayer_planes_input_matches_mosaic(oracle):
+    """setBayerPlanes (colour planes summed into a float mosaic, as GPUTileProcessor.setBayerImages
+    does) with unit colour scales gives the CLT of the uint16 mosaic with scales (1, 1, 0.5)."""
+    from helpers import oracle_planes
+    sc = synth.make_scene("quad_bayer", seed=31, width=128, height=96)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    planes = oracle_planes(sc)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 3.0, np.float32))
+        tp.process()
+        ref = tp.getClt()
+        tp.setBayerPlanes(planes)
+        tp.setColorScales([1.0, 1.0, 1.0])
+        tp.process()
+        got = tp.getClt()
+    assert np.array_equal(got, ref)
