@@ -222,7 +222,7 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
 template <int C, int NT>
 __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, size_t tile, int P, int pi, int RE,
                                          bool log_mode, const short *strip_code, const float *s_clt, float *scr,
-                                         int lane, float cmb[8]) {
+                                         int lane, float cmb[8], float *corr_out = nullptr) {
   const int q = lane >> 3, r = lane & 7;
   float *qb = scr, *tb = scr + 288;
   const PairDev pd = cfg.pairs[pi];
@@ -300,7 +300,7 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
     if (a && b) cs[(7 - a) * 15 + 7 - b] = 0.25f * (((A - B) - Cc) + D);
   }
   __syncwarp();
-  float *gc = sc.corr + (tile * P + pi) * TP_CORR;
+  float *gc = corr_out ? corr_out : sc.corr + (tile * P + pi) * TP_CORR;
   for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
   if (pd.in_combo) {
 #pragma unroll
@@ -717,6 +717,143 @@ cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const Scene
                                       scenes_dev, unit_off_dev, n, wf, cf, st);
   return launch_batch_k(fused_batch_kernel<1, true, 4, 8>, 128, (cf + sp) * 4, total_units, scenes_dev, unit_off_dev,
                         n, 0, cf, st);
+}
+
+// ---------------------------------------------------------------------------
+// Rig (two quad cameras): inter-camera correlation of the sensor-averaged CLT
+// of each camera (Correlation2d.correlateInterCamerasFD / cltMixCameras,
+// Correlation2d.java:401-448) and its disparity along the horizontal rig
+// baseline (ImageDtt.tileInterCamCorrs, ImageDtt.java:7370-7560, without the
+// LMA branch).  Warp per tile of the main camera's task list; the correlation
+// is the forward kernel's pair phase run on the two averaged CLTs.
+// ---------------------------------------------------------------------------
+template <int C, int NT>
+__global__ void __launch_bounds__(128, 4) rig_kernel(const __grid_constant__ SceneDev mn,
+                                                     const __grid_constant__ SceneDev ax,
+                                                     const __grid_constant__ CorrConst cfg, float *rig_corr,
+                                                     float *rig_rec, float cm_norm, int no_int_x0, int per_warp) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, NW = blockDim.x >> 5;
+  float *mix = sm + warp * per_warp;  // [2][C][256]
+  float *scr = mix + 2 * C * TP_CLT;
+  const int RE = (cfg.strip_rows < cfg.wndy_size ? cfg.strip_rows : cfg.wndy_size) * 15;
+  const short *strip_code = &mn.corr_cfg->strip_code[0][0][0];
+  const int ncomb = cfg.twice_diagonal ? 2 : 1;
+  for (int task = blockIdx.x * NW + warp; task < mn.num_tasks; task += gridDim.x * NW) {
+    const int txy = mn.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * mn.tilesX + (txy & 0xffff);
+    float *rec = rig_rec + tile * 4;
+    if (ax.tile_task[tile] < 0) {
+      if (lane < 4) rec[lane] = (lane == 1) ? 0.f : CUDART_NAN_F;
+      continue;
+    }
+    for (int i = lane; i < C * TP_CLT; i += 32) {
+      float a = 0.f, b = 0.f;
+      for (int s = 0; s < mn.num_sensors; s++) a += mn.clt[(tile * mn.num_sensors + s) * C * TP_CLT + i];
+      for (int s = 0; s < ax.num_sensors; s++) b += ax.clt[(tile * ax.num_sensors + s) * C * TP_CLT + i];
+      mix[i] = a * (1.0f / mn.num_sensors);
+      mix[C * TP_CLT + i] = b * (1.0f / ax.num_sensors);
+    }
+    __syncwarp();
+    float cmb[8];
+#pragma unroll
+    for (int t = 0; t < NT; t++) cmb[t] = 1.f;
+    fwd_pair<C, NT>(mn, cfg, tile, 1, 0, RE, false, strip_code, mix, scr, lane, cmb, rig_corr + tile * TP_CORR);
+    float *combo = scr;
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+      const int e = lane + 32 * t;
+      if (e < RE) {
+        float v = cmb[t];
+        if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
+        combo[e] = v;
+      }
+    }
+    __syncwarp();
+    float r0 = CUDART_NAN_F, r1 = 0.f;
+    const float v = (lane < 15) ? combo[lane] : CUDART_NAN_F;
+    float best = isnan(v) ? -CUDART_INF_F : v;
+    int bi = lane < 15 ? lane : 99;
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o2);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o2);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const unsigned finite = __ballot_sync(0xffffffffu, lane < 15 && !isnan(v));
+    const int imx = finite ? bi : 14;
+    const float vmax = combo[imx];
+    if (vmax >= (no_int_x0 ? 0.5f : 1.0f) * cfg.min_corr) {
+      const int ix = imx - 7;
+      r0 = (float)(-ix);
+      r1 = vmax;
+      int dh = cfg.strip_rows;
+      float wys = 1.0f;
+      if (dh > cfg.wndy_size) dh = cfg.wndy_size;
+      else if (dh < cfg.wndy_size) {
+        float swy = cfg.wndy[0];
+        for (int i = 1; i < dh; i++) swy += cfg.wndy[i];
+        wys = 1.0f / swy;
+      }
+      const int ixc = no_int_x0 ? 0 : ix;
+      const int x0 = 7 + ixc, nk = dh * 2 * cfg.wndx_size;
+      float s0 = 0.f, sx = 0.f, sx2 = 0.f;
+      for (int k = lane; k < nk; k += 32) {  // getMaxXCm with the second moment
+        const int dy = k / (2 * cfg.wndx_size), rest = k - dy * 2 * cfg.wndx_size;
+        const int adx = rest >> 1, dir = (rest & 1) ? 1 : -1, odd = dy & 1;
+        if (((adx - odd) & 1) || (adx == 0 && dir < 0)) continue;
+        const int idx = (adx * dir) >> 1, xx = 2 * idx + odd, x1 = x0 + idx;
+        if (x1 < 0 || x1 >= 15) continue;
+        float d = combo[dy * 15 + x1];
+        if (isnan(d) || !(d > 0.0f)) continue;
+        d *= (((dy == 0) ? wys : 2.0f * wys) * cfg.wndy[dy]) * cfg.wndx[adx];
+        s0 += d;
+        sx += d * xx;
+        sx2 += d * xx * xx;
+      }
+      s0 = warp_sum(s0);
+      sx = warp_sum(sx);
+      sx2 = warp_sum(sx2);
+      if (s0 != 0.0f) {
+        r0 = -(ixc + sx / s0 / 2);
+        const float sigma = sqrtf(s0 * sx2 - sx * sx) / s0 / 2, eff = sigma * cm_norm;
+        r1 = s0 / (eff * eff);
+      }
+    }
+    if (lane < 4) rec[lane] = (lane == 0) ? r0 : ((lane == 1) ? r1 : CUDART_NAN_F);
+    __syncwarp();
+  }
+}
+
+// tiles without a main-camera task keep {NaN, 0, NaN, NaN}
+__global__ void rig_init_kernel(float *rig_rec, int ntiles) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ntiles * 4) rig_rec[i] = ((i & 3) == 1) ? 0.f : CUDART_NAN_F;
+}
+
+cudaError_t launch_rig(const SceneDev &mn, const SceneDev &ax, const CorrConst &cc, float *rig_corr, float *rig_rec,
+                       float cm_norm, int no_int_x0, cudaStream_t st) {
+  const int ntiles = mn.tilesX * mn.tilesY;
+  rig_init_kernel<<<(ntiles * 4 + 255) / 256, 256, 0, st>>>(rig_rec, ntiles);
+  if (mn.num_tasks <= 0) return cudaGetLastError();
+  const int C = mn.num_colors;
+  const int RE = (cc.strip_rows < cc.wndy_size ? cc.strip_rows : cc.wndy_size) * 15;
+  const int per_warp = ((2 * C * TP_CLT + SCR) + 3) & ~3, nw = 4, bytes = per_warp * nw * 4;
+  const int units = (mn.num_tasks + nw - 1) / nw;
+  auto go = [&](auto kernel) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nw * 32, bytes);
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int grid = units < sms * per_sm ? units : sms * per_sm;
+    kernel<<<grid, nw * 32, bytes, st>>>(mn, ax, cc, rig_corr, rig_rec, cm_norm, no_int_x0, per_warp);
+    return cudaGetLastError();
+  };
+  if (RE <= 32) return C == 3 ? go(rig_kernel<3, 1>) : go(rig_kernel<1, 1>);
+  return C == 3 ? go(rig_kernel<3, 8>) : go(rig_kernel<1, 8>);
 }
 
 // ---------------------------------------------------------------------------

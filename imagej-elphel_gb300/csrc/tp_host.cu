@@ -42,6 +42,7 @@ struct tp_handle {
   float *d_tex = nullptr, *d_tex_aux = nullptr;
   float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
+  float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
   size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
@@ -395,7 +396,8 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage};
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr,
+                  h->d_rig_rec};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1085,6 +1087,52 @@ tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity
     return TP_ERR_CUDA;
   }
   return TP_OK;
+}
+
+tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_normalization, int no_int_x0,
+                           void *stream) {
+  tp_handle *h = main_h;
+  if (!h || !aux) return TP_ERR_ARG;
+  if (aux->tilesX != h->tilesX || aux->tilesY != h->tilesY || aux->cfg.num_colors != h->cfg.num_colors ||
+      aux->cfg.device != h->cfg.device)
+    return fail(h, TP_ERR_ARG, "tp_rig_correlate: the cameras differ in tile grid, colours or device");
+  if (!h->have_corr) return fail(h, TP_ERR_STATE, "tp_rig_correlate: main camera has no correlation set-up");
+  if (!h->fwd_valid || !aux->fwd_valid)
+    return fail(h, TP_ERR_STATE, "tp_rig_correlate: run tp_process on both cameras first");
+  cudaStream_t st = pick_stream(h, stream);
+  if (!h->d_rig_corr) {
+    if (dalloc(&h->d_rig_corr, (size_t)h->ntiles * TP_CORR) != cudaSuccess ||
+        dalloc(&h->d_rig_rec, (size_t)h->ntiles * 4) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_rig_correlate: buffers");
+    }
+    CK(cudaMemsetAsync(h->d_rig_corr, 0, (size_t)h->ntiles * TP_CORR * sizeof(float), st), "tp_rig_correlate");
+  }
+  CK(cudaStreamSynchronize(aux->stream), "tp_rig_correlate");
+  CK(cudaStreamSynchronize(h->stream), "tp_rig_correlate");
+  CorrConst cc = h->corr_host;  // the main camera's correlation set-up, one horizontal pair
+  cc.num_pairs = 1;
+  cc.num_combo = 1;
+  cc.log_combine = 0;
+  cc.num_hor = cc.num_vert = 0;
+  cc.pairs[0].cam1 = 0;
+  cc.pairs[0].cam2 = 1;
+  cc.pairs[0].kind = 0;
+  cc.pairs[0].in_combo = 1;
+  cc.pairs[0].bx = 1.f;
+  cc.pairs[0].by = 0.f;
+  CK(launch_rig(scene_of(h), scene_of(aux), cc, h->d_rig_corr, h->d_rig_rec, cm_max_normalization, no_int_x0, st),
+     "tp_rig_correlate");
+  return TP_OK;
+}
+
+tp_status tp_get_rig(tp_handle *h, float *corr, float *rec) {
+  if (!h) return TP_ERR_ARG;
+  if (!h->d_rig_corr) return fail(h, TP_ERR_STATE, "tp_get_rig: run tp_rig_correlate first");
+  tp_status r = TP_OK;
+  if (corr) r = d2h(h, corr, h->d_rig_corr, (size_t)h->ntiles * TP_CORR * sizeof(float), "tp_get_rig");
+  if (r == TP_OK && rec) r = d2h(h, rec, h->d_rig_rec, (size_t)h->ntiles * 4 * sizeof(float), "tp_get_rig");
+  return r;
 }
 
 tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt) {

@@ -146,6 +146,9 @@ int batch_class(const SceneDev &sc);
 int batch_units(const SceneDev &sc);
 cudaError_t launch_fused_batch(int cls, const SceneDev *scenes_host, const SceneDev *scenes_dev,
                                const int *unit_off_dev, int n, int total_units, cudaStream_t st);
+// rig inter-camera correlation (tp_fused.cu): rig_corr [tiles][225], rig_rec [tiles][4]
+cudaError_t launch_rig(const SceneDev &mn, const SceneDev &ax, const CorrConst &cc, float *rig_corr, float *rig_rec,
+                       float cm_norm, int no_int_x0, cudaStream_t st);
 // task compaction into a fixed device scratch array (tp_plan.cu), no allocation
 int compact_scratch_max_tiles();
 cudaError_t compact_scratch_address(int **ptr);

@@ -98,6 +98,8 @@ PROTOTYPES = {
     "tp_get_textures": [_H, _vp],
     "tp_get_texture_aux": [_H, _vp],
     "tp_compact_tile_ops_noalloc": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
+    "tp_rig_correlate": [_H, _H, C.c_float, C.c_int, _vp],
+    "tp_get_rig": [_H, _vp, _vp],
     "tp_batch_create": [C.POINTER(_H), C.c_int, C.POINTER(_H)],
     "tp_batch_destroy": [_H],
     "tp_batch_last_error": [_H, C.c_char_p, C.c_int],

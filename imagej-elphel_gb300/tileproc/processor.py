@@ -274,6 +274,18 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_get_rbg(self.h, int(ncam), _ptr(out)), "tp_get_rbg")
         return out
 
+    # ---- rig ----
+    def rigCorrelate(self, aux, cm_max_normalization=0.55, no_int_x0=False, stream=None):
+        """Inter-camera correlation with the auxiliary camera `aux` (another GPUTileProcessor on the
+        same tile grid); returns (corr [tiles][225], rec [tiles][4] = disparity, strength, dx, dy)."""
+        self._ck(self._lib.tp_rig_correlate(self.h, aux.h, float(cm_max_normalization), int(bool(no_int_x0)), stream),
+                 "tp_rig_correlate")
+        T = self.tilesY * self.tilesX
+        corr = np.zeros((T, 225), dtype=np.float32)
+        rec = np.zeros((T, 4), dtype=np.float32)
+        self._ck(self._lib.tp_get_rig(self.h, _ptr(corr), _ptr(rec)), "tp_get_rig")
+        return corr, rec
+
     # ---- adjoint ----
     def setAdjointMode(self, recompute_clt=False):
         self._ck(self._lib.tp_set_adjoint_mode(self.h, int(bool(recompute_clt))), "tp_set_adjoint_mode")

@@ -221,6 +221,21 @@ tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
 tp_status tp_get_texture_aux(tp_handle *h, float *aux);
 
+/* ---- rig: main and auxiliary quad cameras (ImageDtt.clt_bi_quad, ImageDtt.java:8731-) ----
+ * Inter-camera correlation of the sensor-averaged CLT of each camera
+ * (Correlation2d.correlateInterCamerasFD / cltMixCameras, Correlation2d.java:401-448)
+ * with the main camera's correlation set-up, and its disparity along the rig
+ * baseline (ImageDtt.tileInterCamCorrs 7370-7560 without the LMA branch):
+ * rec = {BI_DISP_CROSS, BI_STR_CROSS (mass / (sigma x cm_max_normalization)^2),
+ * BI_DISP_CROSS_DX, BI_DISP_CROSS_DY (NaN: LMA only)}.  Both cameras share the
+ * tile grid and colours and have run tp_process (each with its own geometry and
+ * target disparities); tiles the auxiliary camera has no task for get
+ * {NaN, 0, NaN, NaN}.  Results are kept by the main handle. */
+tp_status tp_rig_correlate(tp_handle *main_camera, tp_handle *aux_camera, float cm_max_normalization, int no_int_x0,
+                           void *stream);
+/* corr [tilesY*tilesX][15*15], rec [tilesY*tilesX][4]; either may be NULL */
+tp_status tp_get_rig(tp_handle *main_camera, float *corr, float *rec);
+
 /* ---- batches (no reference counterpart: the reference processes one scene per
  * GPUTileProcessor instance and launch) ----
  * A batch runs the forward of many scenes -- handles of any sensor count,

@@ -480,3 +480,21 @@ def texture_tiles(clt, tiles, img_mask, lpf, col_weights=(0.25, 0.25, 0.5), extr
                        _d(_f64(col_weights).reshape(3)), C.byref(params if params is not None else texture_params()),
                        _d(out), _d(aux), int(num_threads or os.cpu_count() or 1))
     return out, aux
+
+
+def rig_tile(clt_main, clt_aux, corr_params=None, cm_max_normalization=0.55, no_int_x0=False):
+    """clt_main [S][C][4][64], clt_aux [S'][C][4][64] -> (corr [225], rec [4])."""
+    L = lib()
+    if not getattr(L, "_rig_set", False):
+        L.or_rig_tile.argtypes = [_dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(CorrParams), C.c_double, C.c_int,
+                                  _dp, _dp]
+        L.or_rig_tile.restype = None
+        L._rig_set = True
+    a = _f64(clt_main)
+    b = _f64(clt_aux)
+    cp = corr_params if corr_params is not None else default_corr_params()
+    corr = np.zeros(225)
+    rec = np.zeros(4)
+    L.or_rig_tile(_d(a), a.shape[0], _d(b), b.shape[0], a.shape[1], C.byref(cp), float(cm_max_normalization),
+                  int(bool(no_int_x0)), _d(corr), _d(rec))
+    return corr, rec

@@ -1593,3 +1593,53 @@ int or_texture_tiles(const double *clt, const int *tiles, const int *img_mask, c
   for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
   return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Inter-camera (rig) correlation of two quad cameras for one tile:          */
+/* Correlation2d.correlateInterCamerasFD (401-414) with cltMixCameras        */
+/* (424-448), then ImageDtt.tileInterCamCorrs (7370-7560) without the LMA     */
+/* branch (min_poly_strength above any strength) and with notch mode off.    */
+/* ------------------------------------------------------------------------- */
+void or_rig_tile(const double *clt_main, int s_main, const double *clt_aux, int s_aux, int nc,
+                 const or_corr_params *cp, double cm_max_normalization, int no_int_x0, double *corr225,
+                 double rec[4]) {
+  tables();
+  double mix[2][3 * 256];
+  const double *src[2] = {clt_main, clt_aux};
+  const int ns[2] = {s_main, s_aux};
+  for (int k = 0; k < 2; k++) {
+    for (int i = 0; i < nc * 256; i++) mix[k][i] = 0.0;
+    for (int s = 0; s < ns[k]; s++)
+      for (int i = 0; i < nc * 256; i++) mix[k][i] += src[k][(size_t)s * nc * 256 + i];
+    const double kk = 1.0 / ns[k];
+    for (int i = 0; i < nc * 256; i++) mix[k][i] *= kk;
+  }
+  double lpf[64], cw[3];
+  or_corr_lpf(cp->corr_sigma, lpf);
+  const double g = 1.0 / (1.0 + cp->corr_red + cp->corr_blue);
+  cw[0] = cp->corr_red * g;
+  cw[1] = cp->corr_blue * g;
+  cw[2] = g;
+  or_correlate_pair(mix[0], mix[1], nc, cw, lpf, cp->fat_zero, corr225);
+  const int hw = cp->corr_strip_hight;
+  double strip[16 * 15], combo[16 * 15];
+  or_strip(corr225, 1.0, 0.0, 0, hw, strip);  /* PAIRS[0]: the horizontal pair grid */
+  int use = 1, diag = 0;
+  or_combine_strips(strip, &use, 1, &diag, hw, cp->corr_offset, cp->twice_diagonal, combo);
+  rec[0] = NAN;
+  rec[1] = 0.0;
+  rec[2] = NAN;
+  rec[3] = NAN;
+  int ix;
+  if (!or_max_xy_int_axis(combo, hw, (no_int_x0 ? 0.5 : 1.0) * cp->min_corr, &ix)) return;
+  rec[0] = -ix;
+  rec[1] = combo[ix + 7];
+  double wndy[32], wndx[32], cs[3];
+  or_half_flat_top_window(cp->corr_wndy_size, cp->corr_wndy_hwidth, cp->corr_wndy_blur, 1, 0, 1.0, wndy);
+  or_half_flat_top_window(cp->corr_wndx_size, cp->corr_wndx_hwidth, cp->corr_wndx_blur, 1, 0, 2.0, wndx);
+  if (or_max_x_cm(combo, hw, no_int_x0 ? 0 : ix, wndy, cp->corr_wndy_size, wndx, cp->corr_wndx_size, cs)) {
+    rec[0] = -cs[0];
+    const double eff = cs[2] * cm_max_normalization;
+    rec[1] = cs[1] / (eff * eff);
+  }
+}

@@ -191,6 +191,13 @@ void or_iclt_tile_add(const double clt[4][64], double scale, int tx, int ty,
 int or_imclt_frames(const double *clt, const int *present, int tilesX, int tilesY, int S, int C, double scale,
                     const double *lpf, double *frames, int num_threads, int zero_frames);
 
+/* ---- rig (two quad cameras) inter-camera correlation, one tile ----
+ * clt_main [s_main][nc][4][64], clt_aux [s_aux][nc][4][64] -> corr225 and
+ * rec {disparity, strength, dx (NaN), dy (NaN)} (ImageDtt.tileInterCamCorrs) */
+void or_rig_tile(const double *clt_main, int s_main, const double *clt_aux, int s_aux, int nc,
+                 const or_corr_params *cp, double cm_max_normalization, int no_int_x0, double *corr225,
+                 double rec[4]);
+
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {
   double min_shot, scale_shot;        /* CLTParameters 10.0, 3.0 */

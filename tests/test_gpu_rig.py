@@ -1,0 +1,79 @@
+"""Rig (main + auxiliary quad camera) inter-camera correlation against the oracle (needs a GB300).
+
+The oracle is fed the GPU's own CLTs of both cameras, so the check isolates the
+rig stage: sensor averaging, the pair correlation with the main camera's
+settings, the horizontal strip, argmax and the centroid with its second moment.
+Tolerances: correlation relative L2 per tile <= 1e-5; disparity <= 0.005 px
+and strength relative <= 1e-3 on tiles whose integer argmax agrees.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_gpu, rel_l2
+from tileproc import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _rig_check(oracle, main_tp, aux_tp, aux_op, no_int_x0=False):
+    corr, rec = main_tp.rigCorrelate(aux_tp, no_int_x0=no_int_x0)
+    cm = main_tp.getClt().astype(np.float64)
+    ca = aux_tp.getClt().astype(np.float64)
+    T = cm.shape[0]
+    n_ok = 0
+    errs = []
+    for t in range(T):
+        if not aux_op[t]:
+            assert np.isnan(rec[t, 0]) and rec[t, 1] == 0.0, "tile %d without an aux task" % t
+            continue
+        oc, orec = oracle.rig_tile(cm[t], ca[t], no_int_x0=no_int_x0)
+        e = rel_l2(corr[t].astype(np.float64), oc, axis=-1)
+        assert e <= 1e-5, "tile %d: rig corr rel L2 %.3g" % (t, e)
+        assert np.isnan(rec[t, 2]) and np.isnan(rec[t, 3])
+        if np.isnan(orec[0]):
+            assert np.isnan(rec[t, 0]) and rec[t, 1] == 0.0
+            continue
+        if np.isnan(rec[t, 0]) or abs(rec[t, 0] - orec[0]) > 0.5:
+            continue  # near-tie of the integer argmax (counted below)
+        n_ok += 1
+        errs.append(abs(rec[t, 0] - orec[0]))
+        assert abs(rec[t, 1] - orec[1]) <= 1e-3 * abs(orec[1]) + 1e-6, "tile %d strength %g vs %g" % (
+            t, rec[t, 1], orec[1])
+    assert n_ok >= 0.9 * aux_op.sum()
+    assert max(errs) <= 0.005, "rig disparity max err %.4g px" % max(errs)
+    return rec
+
+
+@pytest.mark.parametrize("kind", ["quad_bayer", "quad_mono"])
+def test_rig_inter_camera(oracle, kind):
+    """Auxiliary camera = the main scene shifted by 2 px, with a ragged task subset; the rig
+    disparity of textured tiles recovers the shift."""
+    sc = synth.make_scene(kind, seed=21, width=128, height=96)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    aux = dict(sc)
+    aux["images"] = np.ascontiguousarray(np.roll(sc["images"], 2, axis=-1))
+    rng = np.random.default_rng(5)
+    aux_op = (rng.uniform(size=T) > 0.25).astype(np.int32)
+    with make_gpu(sc) as tm, make_gpu(aux) as ta:
+        for tp, op in ((tm, np.ones(T, np.int32)), (ta, aux_op)):
+            tp.setCorrelation()
+            tp.setFullFrameImages(np.full(T, 2.0, np.float32), tile_op=op)
+            tp.process()
+        rec = _rig_check(oracle, tm, ta, aux_op)
+        # the 2-pixel roll shows up as the inter-camera disparity on most textured interior tiles
+        tx, ty = np.arange(T) % (W // 8), np.arange(T) // (W // 8)
+        inner = (aux_op > 0) & (tx > 1) & (tx < W // 8 - 2) & (ty > 1) & (ty < H // 8 - 2) & (rec[:, 1] > 0)
+        d = rec[inner, 0]
+        assert np.median(np.abs(np.abs(d) - 2.0)) < 0.5, "median rig disparity %g" % np.median(d)
+        _rig_check(oracle, tm, ta, aux_op, no_int_x0=True)
+
+
+def test_rig_rejects_mismatched_cameras():
+    from tileproc import _lib
+    sc = synth.make_scene("quad_mono", seed=22, width=64, height=64)
+    sc2 = synth.make_scene("quad_mono", seed=22, width=128, height=64)
+    with make_gpu(sc) as tm, make_gpu(sc2) as ta:
+        tm.setCorrelation()
+        with pytest.raises(_lib.TpError, match="differ in tile grid"):
+            tm.rigCorrelate(ta)
