@@ -412,19 +412,30 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
     const int np = half ? cfg.num_vert : cfg.num_hor;
     float sum = -CUDART_INF_F;
     if (j < 15 && np > 0) {
-      sum = 0.f;
-      for (int i = 0; i < 15; i++) {
-        float prod = 1.f;
-        for (int k = 0; k < np; k++) {
-          const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
-          const float d = half ? 0.5f * (cc[j * 15 + i] + cc[j * 15 + 14 - i])
-                               : 0.5f * (cc[i * 15 + j] + cc[(14 - i) * 15 + j]);
-          prod *= d + cfg.corr_offset;
+      // the symmetrised profile is even in i (d[i] == d[14 - i]), so rows 0..7 carry it; all
+      // loads of one pair are issued before their use
+      float prod[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) prod[i] = 1.f;
+      for (int k = 0; k < np; k++) {
+        const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
+        const int stride = half ? 1 : 15, base = half ? j * 15 : j;
+        float a[8], b[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          a[i] = cc[base + i * stride];
+          b[i] = cc[base + (14 - i) * stride];
         }
-        const float v = (prod > 0.0f) ? ((np == 2) ? sqrtf(prod) : ((np == 1) ? prod : powf(prod, 1.0f / np))) -
-                                            cfg.corr_offset
-                                      : -cfg.corr_offset;
-        sum += v * cfg.notch[i];
+#pragma unroll
+        for (int i = 0; i < 8; i++) prod[i] *= 0.5f * (a[i] + b[i]) + cfg.corr_offset;
+      }
+      sum = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float p = prod[i];
+        const float v = (p > 0.0f) ? ((np == 2) ? sqrtf(p) : ((np == 1) ? p : powf(p, 1.0f / np))) - cfg.corr_offset
+                                   : -cfg.corr_offset;
+        sum += v * ((i < 7) ? cfg.notch[i] + cfg.notch[14 - i] : cfg.notch[7]);
       }
     }
     float best = sum;
