@@ -39,6 +39,7 @@ struct AdjShape {
   int S, P, RE;
   int per_warp;   // floats of shared memory per warp
   int recompute;  // 1: recompute the CLT from the image instead of reading it back
+  int use_strips; // 1: the forward recorded its per-pair strip samples in sc.strips
 };
 
 __device__ __forceinline__ void convolve(float o[4][8], const float *kp, int r) {
@@ -294,7 +295,14 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
     }
 
     // ---------------- reverse pass over the pairs, AD_NW pairs at a time ----------------
+    // With the forward's strip samples recorded and one entry per lane, the next pair's sample
+    // is loaded one iteration ahead so its latency overlaps this pair.
+    const bool pre = as.use_strips && RE <= 32;
+    float vnext = 0.f;
+    if (pre && warp < P && lane < RE) vnext = sc.strips[(tile * P + warp) * RE + lane];
     for (int pi = warp; pi < P; pi += AD_NW) {
+      const float vcur = vnext;
+      if (pre && pi + AD_NW < P && lane < RE) vnext = sc.strips[(tile * P + pi + AD_NW) * RE + lane];
       const PairDev pd = cfg.pairs[pi];
       if (!pd.in_combo) continue;
       const float *c = sc.corr + (tile * P + pi) * TP_CORR;
@@ -305,9 +313,11 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
       bool any = false;
       for (int e = lane; e < RE; e += 32) {
         if (gcmb[e] == 0.f) continue;
-        const float v = strip_entry(c, strip_code, pd, e) + cfg.corr_offset;
+        const float d = pre ? vcur
+                            : (as.use_strips ? sc.strips[(tile * P + pi) * RE + e] : strip_entry(c, strip_code, pd, e));
+        const float v = d + cfg.corr_offset;
         if (!(v > 0.0f)) continue;
-        const float f = gcmb[e] * gG[e] * inv_n / v;
+        const float f = __fdividef(gcmb[e] * gG[e] * inv_n, v);
         const int row = e / 15;
         const float half = row > 0 ? 0.5f : 1.0f;
         for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
@@ -358,7 +368,7 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
       }
       // LPF and the fat-zero normalised product (correlateSingleColorFD)
       const float *c1 = s_clt + (size_t)pd.cam1 * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * TP_CLT;
-      float d1[4][2], d2[4][2], a2[2], s1v[2], s2v[2];
+      float d1[4][2], d2[4][2], a2[2], ia2[2], s1v[2], s2v[2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         float s1 = 0.f, s2 = 0.f;
@@ -369,7 +379,10 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
           s1 = fmaf(d1[m][h], d1[m][h], s1);
           s2 = fmaf(d2[m][h], d2[m][h], s2);
         }
-        a2[h] = sqrtf(s1 * s2);
+        // |d1| |d2| with the forward's approximate square root; ia2 = 1 / a2 (0 where a2 = 0)
+        const float pr = s1 * s2;
+        ia2[h] = (pr > 0.0f) ? rsqrtf(pr) : 0.0f;
+        a2[h] = pr * ia2[h];
         s1v[h] = s1;
         s2v[h] = s2;
       }
@@ -384,7 +397,7 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
         float gq[4];
 #pragma unroll
         for (int qq = 0; qq < 4; qq++) gq[qq] = qb[qq * 72 + off] * l;
-        const float sw = 1.0f / (a2[h] + fz2);
+        const float sw = __fdividef(1.0f, a2[h] + fz2);
         const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
         const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
         const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
@@ -410,8 +423,8 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
         g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
         g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
         // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
-        const float k1 = a2[h] > 0.f ? a2bar * s2v[h] / a2[h] : 0.f;
-        const float k2 = a2[h] > 0.f ? a2bar * s1v[h] / a2[h] : 0.f;
+        const float k1 = a2bar * s2v[h] * ia2[h];
+        const float k2 = a2bar * s1v[h] * ia2[h];
 #pragma unroll
         for (int m = 0; m < 4; m++) {
           atomicAdd(&s_g[pd.cam1 * TP_CLT + m * 64 + idx], fmaf(k1, d1[m][h], g1[m]));
@@ -548,7 +561,8 @@ cudaError_t upload_adjoint_constants() {
 
 int adjoint_smem_bytes(int S) { return (S * 2 * TP_CLT + 240 + 240 + AD_NW * 816) * 4; }
 
-cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
+cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, int use_strips, float *sens,
+                           float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st) {
   if (sc.num_tasks <= 0) return cudaSuccess;
@@ -559,6 +573,7 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
   as.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
   as.per_warp = adjoint_smem_bytes(as.S) / 4;
   as.recompute = recompute;
+  as.use_strips = (use_strips && sc.strips) ? 1 : 0;
   const int bytes = adjoint_smem_bytes(as.S);
   cudaError_t e = cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;

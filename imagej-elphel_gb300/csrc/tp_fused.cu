@@ -31,7 +31,7 @@
 namespace {
 
 constexpr int FW_MAX_WARPS = 16;
-constexpr int SCR = 2 * 288;       // per-warp scratch floats
+constexpr int SCR = 288;           // per-warp scratch floats: [4][8][9] transpose / surface buffer
 
 // ---------------------------------------------------------------------------
 // phase A: CLT of one sub-tile, lane r of the 8-lane group holds row r
@@ -224,9 +224,13 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
                                          bool log_mode, const short *strip_code, const float *s_clt, float *scr,
                                          int lane, float cmb[8], float *corr_out = nullptr) {
   const int q = lane >> 3, r = lane & 7;
-  float *qb = scr, *tb = scr + 288;
+  float *qb = scr;
   const PairDev pd = cfg.pairs[pi];
   const float *c1 = s_clt + (size_t)pd.cam1 * C * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * C * TP_CLT;
+  // with one strip entry per lane its sample code is read ahead of the correlation arithmetic
+  short2 code1 = make_short2(-1, -1);
+  if (NT == 1 && pd.in_combo && pd.kind <= 3 && lane < RE)
+    code1 = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + lane) * 2];
   float acc[4][2];
 #pragma unroll
   for (int c = 0; c < C; c++) {
@@ -241,13 +245,14 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
         s1 = fmaf(d1[m][h], d1[m][h], s1);
         s2 = fmaf(d2[m][h], d2[m][h], s2);
       }
-      a2[h] = sqrtf(s1 * s2);
+      const float pr = s1 * s2;
+      a2[h] = (pr > 0.0f) ? pr * rsqrtf(pr) : 0.0f;  // |d1| |d2|; approximate square root (~2 ulp)
     }
     const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * cfg.fat_zero * cfg.fat_zero;
     const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const float sw = wgt / (a2[h] + fz2);
+      const float sw = __fdividef(wgt, a2[h] + fz2);
       const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
       const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
       const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
@@ -270,30 +275,40 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
   }
   __syncwarp();
   {
+    // both passes transpose in place: every row is read into registers before any is overwritten
     float x[8], y[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) x[e] = qb[q * 72 + r * 9 + e];
     dtt2e_fast(x, y, (q >> 1) & 1);
-#pragma unroll
-    for (int j = 0; j < 8; j++) tb[q * 72 + j * 9 + r] = y[j];
     __syncwarp();
 #pragma unroll
-    for (int e = 0; e < 8; e++) x[e] = tb[q * 72 + r * 9 + e];
+    for (int j = 0; j < 8; j++) qb[q * 72 + j * 9 + r] = y[j];
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 8; e++) x[e] = qb[q * 72 + r * 9 + e];
     dtt2e_fast(x, y, q & 1);
     __syncwarp();
 #pragma unroll
     for (int e = 0; e < 8; e++) qb[q * 72 + r * 9 + e] = y[e];
   }
   __syncwarp();
-  // 15x15 unfold (DttRad2.corr_unfold_tile): each lane owns 2 cells (a, b) and writes their mirror images
-  float *cs = tb;
+  // 15x15 unfold (DttRad2.corr_unfold_tile): each lane owns 2 cells (a, b) and writes their mirror
+  // images; the quadrants are read into registers first, the surface then overwrites them
+  float uA[2], uB[2], uC[2], uD[2];
 #pragma unroll
   for (int k = 0; k < 2; k++) {
     const int a = (lane >> 3) + 4 * k, b = lane & 7;
-    const float A = qb[a * 9 + b];
-    const float B = b ? qb[72 + a * 9 + b - 1] : 0.f;
-    const float Cc = a ? qb[144 + (a - 1) * 9 + b] : 0.f;
-    const float D = (a && b) ? qb[216 + (a - 1) * 9 + b - 1] : 0.f;
+    uA[k] = qb[a * 9 + b];
+    uB[k] = b ? qb[72 + a * 9 + b - 1] : 0.f;
+    uC[k] = a ? qb[144 + (a - 1) * 9 + b] : 0.f;
+    uD[k] = (a && b) ? qb[216 + (a - 1) * 9 + b - 1] : 0.f;
+  }
+  __syncwarp();
+  float *cs = qb;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int a = (lane >> 3) + 4 * k, b = lane & 7;
+    const float A = uA[k], B = uB[k], Cc = uC[k], D = uD[k];
     cs[(7 + a) * 15 + 7 + b] = 0.25f * (((A + B) + Cc) + D);
     if (b) cs[(7 + a) * 15 + 7 - b] = 0.25f * (((A - B) + Cc) - D);
     if (a) cs[(7 - a) * 15 + 7 + b] = 0.25f * (((A + B) - Cc) - D);
@@ -310,7 +325,7 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
         const int row = e / 15;
         float d;
         if (pd.kind <= 3) {
-          const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+          const short2 code = (NT == 1) ? code1 : *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
           d = sample_code(cs, code.x);
           if (row > 0) {
             const float d2 = sample_code(cs, code.y);
@@ -324,6 +339,7 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
             d = (isnan(d) || isnan(d2)) ? CUDART_NAN_F : (0.5f * d + 0.5f * d2);
           }
         }
+        if (sc.strips && !corr_out) sc.strips[(tile * P + pi) * RE + e] = d;  // kept for the adjoint
         float v = d + cfg.corr_offset;
         if (v < 0.0f) v = 0.0f;
         if (log_mode) cmb[t] += logf(v);
@@ -483,7 +499,7 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
   extern __shared__ float sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
-  // per-warp shared memory: CLT of the tile [S][C][4][64] and two 288-float scratch buffers
+  // per-warp shared memory: CLT of the tile [S][C][4][64] and a 288-float scratch buffer
   float *s_clt = sm + warp * fs.per_warp;
   float *scr = s_clt + fs.clt_floats;
   const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
@@ -994,7 +1010,7 @@ static FwdShape make_shape(const SceneDev &sc, int nw) {
   // getMaxXCm clips the strip to the y-window (Correlation2d.java:944-951)
   f.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
   f.quad = (sc.num_pairs <= 8) ? 1 : 0;
-  f.nw = nw > 0 ? nw : (f.C == 3 ? 2 : 4);  // the autotuner's pick on 4x2592x1936 Bayer and 4x512x384 mono
+  f.nw = nw > 0 ? nw : 4;  // the autotuner's pick on 4x2592x1936 Bayer and 4x512x384 mono
   f.clt_floats = f.S * f.C * TP_CLT;
   f.per_warp = f.clt_floats + SCR;
   f.per_warp = (f.per_warp + 3) & ~3;

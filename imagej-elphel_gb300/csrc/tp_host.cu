@@ -41,6 +41,10 @@ struct tp_handle {
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
   float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
+  // per-pair strip samples [tiles][pairs][RE], recorded by the forward once the adjoint is in use
+  float *d_strips = nullptr;
+  size_t strips_cap = 0;
+  int record_strips = 0, strips_valid = 0;
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
   size_t psf_stage_kernels = 0;
@@ -85,6 +89,12 @@ static cudaError_t dalloc(T **p, size_t n) {
   return cudaMalloc((void **)p, n * sizeof(T) > 0 ? n * sizeof(T) : 1);
 }
 
+// floats of the per-pair strip-sample buffer for the current correlation set-up
+static size_t strips_need(const tp_handle *h) {
+  const int RE = (h->corr_host.strip_rows < h->corr_host.wndy_size ? h->corr_host.strip_rows : h->corr_host.wndy_size) * 15;
+  return (size_t)h->ntiles * (h->num_pairs > 0 ? h->num_pairs : 1) * RE;
+}
+
 static SceneDev scene_of(tp_handle *h) {
   SceneDev sc;
   memset(&sc, 0, sizeof(sc));
@@ -127,6 +137,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
   sc.corr_cfg = h->d_corr_cfg;
   sc.combo = h->d_combo;
+  sc.strips = (h->record_strips && h->d_strips && strips_need(h) <= h->strips_cap) ? h->d_strips : nullptr;
   sc.tex = h->d_tex;
   sc.tex_aux = h->tex_params.aux ? h->d_tex_aux : nullptr;
   sc.num_pairs = h->num_pairs;
@@ -396,7 +407,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr,
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips,
                   h->d_rig_rec};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -826,8 +837,10 @@ tp_status tp_process(tp_handle *h, void *stream) {
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
   if (h->num_pairs == 0) return tp_convert_correct(h, stream);
-  CK(launch_fused_forward(scene_of(h), h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
+  const SceneDev sc = scene_of(h);
+  CK(launch_fused_forward(sc, h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
   h->fwd_valid = 1;
+  h->strips_valid = sc.strips ? 1 : 0;
   return TP_OK;
 }
 
@@ -966,7 +979,8 @@ static tp_status batch_tables(tp_batch *b) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   int t = 0;
   for (int i = 0; i < n; i++) {
-    const SceneDev sc = scene_of(b->scenes[i]);
+    SceneDev sc = scene_of(b->scenes[i]);
+    sc.strips = nullptr;  // batched forwards do not record strip samples
     b->h_scenes[i] = sc;
     b->h_task_off[i] = t;
     t += sc.num_tasks;
@@ -1025,8 +1039,11 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
     if (m == 0 && b->solo[c].empty()) continue;
     cudaStream_t cs = b->cls_stream[c];
     bool ok = cudaStreamWaitEvent(cs, b->ev_fork, 0) == cudaSuccess;
-    for (tp_handle *h : b->solo[c])
-      ok = ok && launch_fused_forward(scene_of(h), h->corr_host, h->sched_tpb, h->sched_nw, cs) == cudaSuccess;
+    for (tp_handle *h : b->solo[c]) {
+      SceneDev ss = scene_of(h);
+      ss.strips = nullptr;
+      ok = ok && launch_fused_forward(ss, h->corr_host, h->sched_tpb, h->sched_nw, cs) == cudaSuccess;
+    }
     if (m > 0)
       ok = ok && launch_fused_batch(c, b->h_cls[c].data(), b->d_cls[c], b->d_cls_off[c], m, b->cls_units[c], cs) ==
                      cudaSuccess;
@@ -1036,7 +1053,10 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
       return bfail(b, TP_ERR_CUDA, "batch: forward");
     }
   }
-  for (tp_handle *h : b->scenes) h->fwd_valid = 1;
+  for (tp_handle *h : b->scenes) {
+    h->fwd_valid = 1;
+    h->strips_valid = 0;
+  }
   return TP_OK;
 }
 
@@ -1135,10 +1155,30 @@ tp_status tp_get_rig(tp_handle *h, float *corr, float *rec) {
   return r;
 }
 
+// From the first adjoint on, the forward records every pair's strip samples [tiles][pairs][RE]
+// so the adjoint reads them instead of re-interpolating the correlation surfaces.
+static tp_status enable_strip_recording(tp_handle *h) {
+  const size_t need = strips_need(h);
+  if (need > h->strips_cap) {
+    cudaFree(h->d_strips);
+    h->d_strips = nullptr;
+    h->strips_cap = 0;
+    h->strips_valid = 0;
+    if (dalloc(&h->d_strips, need) != cudaSuccess) {
+      cudaGetLastError();
+      h->record_strips = 0;
+      return fail(h, TP_ERR_NOMEM, "adjoint: strip-sample buffer");
+    }
+    h->strips_cap = need;
+  }
+  h->record_strips = 1;
+  return TP_OK;
+}
+
 tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt) {
   if (!h) return TP_ERR_ARG;
   h->adj_recompute = recompute_clt ? 1 : 0;
-  return TP_OK;
+  return enable_strip_recording(h);
 }
 
 tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream) {
@@ -1167,9 +1207,12 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
   // the plan again with the FP64 port derivatives (same ports, corners and residuals)
   SceneDev sc = scene_of(h);
   sc.port_deriv = h->d_port_deriv;
+  const int use_strips = h->strips_valid && sc.strips;
+  tp_status rs = enable_strip_recording(h);  // later forwards keep their strip samples
+  if (rs != TP_OK) return rs;
   CK(launch_plan(sc, st), "tp_backward plan");
   if (dl_ddisp) CK(cudaMemcpyAsync(h->d_dldd, dl_ddisp, nt * sizeof(float), cudaMemcpyHostToDevice, st), "tp_backward");
-  CK(launch_adjoint(sc, h->corr_host, h->adj_recompute, h->d_sens, h->d_dval, dl_ddisp ? h->d_dldd : nullptr,
+  CK(launch_adjoint(sc, h->corr_host, h->adj_recompute, use_strips, h->d_sens, h->d_dval, dl_ddisp ? h->d_dldd : nullptr,
                     h->d_jac_e, h->d_jac_d, h->d_grad_d, h->d_partial, h->d_grad_e, st),
      "tp_backward adjoint");
   h->have_jac = 1;
@@ -1294,7 +1337,10 @@ tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
     for (tp_handle *h : b->scenes) b->graph_tasks.push_back(h->num_tasks);
   }
   CK_B(cudaGraphLaunch(b->exec, st));
-  for (tp_handle *h : b->scenes) h->fwd_valid = 1;
+  for (tp_handle *h : b->scenes) {
+    h->fwd_valid = 1;
+    h->strips_valid = 0;
+  }
   return TP_OK;
 }
 

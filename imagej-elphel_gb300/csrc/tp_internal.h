@@ -102,6 +102,7 @@ struct SceneDev {
   const float *lpf_rbg;      // [C][64] or null
   const CorrDev *corr_cfg;
   float *combo;              // [tiles][RE] combined strip rows the extraction reads, or null
+  float *strips;             // [tiles][pairs][RE] per-pair strip samples (adjoint input), or null
   float *tex;                // [tiles][rows][256] texture tiles (R, B, G, alpha[, 4 weights, 4 rms])
   float *tex_aux;            // [tiles][16] max_diff[4], ports_rgb[12] or null
   int num_pairs;             // host copy of corr_cfg->num_pairs (launch sizing)
@@ -158,7 +159,7 @@ cudaError_t launch_compact_tasks_scratch(const int *tile_op, const float *dispar
 // adjoint (tp_adjoint.cu): per-tile dd/dport, Jacobian rows, loss gradient
 cudaError_t upload_adjoint_constants();
 int adjoint_smem_bytes(int S);
-cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, float *sens, float *dval,
+cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, int use_strips, float *sens, float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st);
 // kernel preparation from PSFs (tp_kernprep.cu)

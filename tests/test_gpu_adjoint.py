@@ -164,6 +164,23 @@ def test_recompute_mode_matches_stored_clt(oracle):
     assert np.allclose(gd1, gd0, rtol=1e-4, atol=1e-4 * np.abs(gd0).max())
 
 
+def test_recorded_strip_samples_match_reinterpolation(oracle):
+    """The first backward re-interpolates the strips from the correlation surfaces; forwards after
+    it record the samples, which the next backward reads.  The samples are the same numbers, so
+    the gradients agree up to the order of the adjoint's shared-memory atomic sums."""
+    sc, g, pairs, D = _setup()
+    with _gpu(sc, g, pairs, D) as tp:
+        ge0, gd0 = tp.backward()
+        tp.process()
+        ge1, gd1 = tp.backward()
+        jd1 = tp.getDisparityJacobian()
+        tp.process()
+        ge2, gd2 = tp.backward()
+    for a, b in ((ge1, ge0), (gd1, gd0), (ge2, ge1), (gd2, gd1)):
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-5 * np.abs(b).max())
+    assert np.isfinite(ge0).all() and np.abs(ge0).max() > 0 and jd1 is not None
+
+
 def test_lma_reduces_cost(oracle):
     """Levenberg-Marquardt on the analytic Jacobian from extrinsics perturbed by N(0, 3e-3) rad."""
     from tileproc import lma
