@@ -17,7 +17,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtp.so")
-SOURCES = ["tp_plan.cu", "tp_kernels.cu", "tp_fused.cu", "tp_texture.cu", "tp_adjoint.cu", "tp_kernprep.cu", "tp_host.cu"]
+SOURCES = ["tp_plan.cu", "tp_kernels.cu", "tp_fused.cu", "tp_texture.cu", "tp_adjoint.cu", "tp_kernprep.cu", "tp_lma.cu",
+           "tp_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -47,6 +47,8 @@ struct tp_handle {
   int record_strips = 0, strips_valid = 0;
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
+  float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
+  int disp_mixed = 0;        // the LMA replaced CM / strength since the last forward
   size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
@@ -357,6 +359,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && upload_texture_constants() == cudaSuccess;
   ok = ok && upload_adjoint_constants() == cudaSuccess;
   ok = ok && upload_kernprep_constants() == cudaSuccess;
+  ok = ok && upload_lma_constants() == cudaSuccess;
   tp_default_texture_params(&h->tex_params);
   for (int s = 0; ok && s < S; s++) {
     ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
@@ -407,7 +410,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips,
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma,
                   h->d_rig_rec};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -841,6 +844,7 @@ tp_status tp_process(tp_handle *h, void *stream) {
   CK(launch_fused_forward(sc, h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
   h->fwd_valid = 1;
   h->strips_valid = sc.strips ? 1 : 0;
+  h->disp_mixed = 0;
   return TP_OK;
 }
 
@@ -1056,6 +1060,7 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
   for (tp_handle *h : b->scenes) {
     h->fwd_valid = 1;
     h->strips_valid = 0;
+    h->disp_mixed = 0;
   }
   return TP_OK;
 }
@@ -1107,6 +1112,89 @@ tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity
     return TP_ERR_CUDA;
   }
   return TP_OK;
+}
+
+tp_status tp_default_lma_params(tp_lma_params *p) {
+  if (!p) return TP_ERR_ARG;
+  // ImageDttParameters.java:32-109
+  p->min_poly_strength = 0.2f;
+  p->mix_corr_poly = 1;
+  p->ortho_vasw_pwr = 2.0f;
+  p->cnvx_hwnd_size = 4;
+  p->cnvx_weight = 0.5f;
+  p->cnvx_add3x3 = 1;
+  p->adjust_wm = 1;
+  p->adjust_wy = 0;
+  p->adjust_wxy = 1;
+  p->adjust_ag = 1;
+  p->half_width = 2.0f;
+  p->cost_wy = 0.1f;
+  p->cost_wxy = 0.1f;
+  p->lambda_initial = 0.1f;
+  p->lambda_scale_good = 0.5f;
+  p->lambda_scale_bad = 8.0f;
+  p->lambda_max = 100.0f;
+  p->rms_diff = 0.001f;
+  p->num_iter = 20;
+  p->pair_mask = 0x3f;
+  return TP_OK;
+}
+
+tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  tp_lma_params prm;
+  if (p) prm = *p;
+  else tp_default_lma_params(&prm);
+  if (prm.cnvx_hwnd_size < 0 || prm.cnvx_hwnd_size > 4 || prm.num_iter < 0)
+    return fail(h, TP_ERR_ARG, "tp_lma_refine: cnvx_hwnd_size must be 0..4");
+  if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_lma_refine: no correlation pairs");
+  if (!h->fwd_valid) return fail(h, TP_ERR_STATE, "tp_lma_refine: run tp_process first");
+  if (h->disp_mixed)
+    return fail(h, TP_ERR_STATE, "tp_lma_refine: the disparity record already holds the LMA result; run tp_process");
+  bool quad = false;
+  for (int i = 0; i < h->num_pairs; i++) {
+    const int k = h->corr_host.pairs[i].kind;
+    if (k >= 0 && k <= 3 && ((prm.pair_mask >> i) & 1)) quad = true;
+  }
+  if (!quad) return fail(h, TP_ERR_ARG, "tp_lma_refine: needs pairs of the quad kinds 0..3");
+  cudaStream_t st = pick_stream(h, stream);
+  if (!h->d_lma) {
+    if (dalloc(&h->d_lma, (size_t)h->ntiles * 4) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_lma_refine: buffer");
+    }
+  }
+  CK(cudaMemsetAsync(h->d_lma, 0xff, (size_t)h->ntiles * 4 * sizeof(float), st), "tp_lma_refine");  // NaN
+  TpLmaConst c;
+  c.min_poly_strength = prm.min_poly_strength;
+  c.mix_corr_poly = prm.mix_corr_poly;
+  c.ortho_vasw_pwr = prm.ortho_vasw_pwr;
+  c.cnvx_hwnd_size = prm.cnvx_hwnd_size;
+  c.cnvx_weight = prm.cnvx_weight;
+  c.cnvx_add3x3 = prm.cnvx_add3x3;
+  c.adjust_wm = prm.adjust_wm;
+  c.adjust_wy = prm.adjust_wy;
+  c.adjust_wxy = prm.adjust_wxy;
+  c.adjust_ag = prm.adjust_ag;
+  c.half_width = prm.half_width;
+  c.cost_wy = prm.cost_wy;
+  c.cost_wxy = prm.cost_wxy;
+  c.lambda_initial = prm.lambda_initial;
+  c.lambda_scale_good = prm.lambda_scale_good;
+  c.lambda_scale_bad = prm.lambda_scale_bad;
+  c.lambda_max = prm.lambda_max;
+  c.rms_diff = prm.rms_diff;
+  c.num_iter = prm.num_iter;
+  c.pair_mask = prm.pair_mask;
+  CK(launch_lma(scene_of(h), h->corr_host, c, h->d_lma, st), "tp_lma_refine");
+  if (prm.mix_corr_poly) h->disp_mixed = 1;
+  return TP_OK;
+}
+
+tp_status tp_get_lma(tp_handle *h, float *out) {
+  if (!h || !out) return TP_ERR_ARG;
+  if (!h->d_lma) return fail(h, TP_ERR_STATE, "tp_get_lma: run tp_lma_refine first");
+  return d2h(h, out, h->d_lma, (size_t)h->ntiles * 4 * sizeof(float), "tp_get_lma");
 }
 
 tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_normalization, int no_int_x0,
@@ -1340,6 +1428,7 @@ tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
   for (tp_handle *h : b->scenes) {
     h->fwd_valid = 1;
     h->strips_valid = 0;
+    h->disp_mixed = 0;
   }
   return TP_OK;
 }

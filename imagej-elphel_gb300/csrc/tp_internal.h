@@ -164,6 +164,21 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
                            float *grad_e, cudaStream_t st);
 // kernel preparation from PSFs (tp_kernprep.cu)
 cudaError_t upload_kernprep_constants();
+// LMA disparity (tp_lma.cu): the fields of tp_lma_params
+struct TpLmaConst {
+  float min_poly_strength;
+  int mix_corr_poly;
+  float ortho_vasw_pwr;
+  int cnvx_hwnd_size;
+  float cnvx_weight;
+  int cnvx_add3x3;
+  int adjust_wm, adjust_wy, adjust_wxy, adjust_ag;
+  float half_width, cost_wy, cost_wxy;
+  float lambda_initial, lambda_scale_good, lambda_scale_bad, lambda_max, rms_diff;
+  int num_iter, pair_mask;
+};
+cudaError_t upload_lma_constants();
+cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out, cudaStream_t st);
 cudaError_t launch_kernel_prep(const float *psf_dev, int nk, int normalize, float *clt_out, float *ext_out,
                                cudaStream_t st);
 cudaError_t launch_fill_coord_corr(float *ext, int kh, int kv, int C, int kern_step, cudaStream_t st);

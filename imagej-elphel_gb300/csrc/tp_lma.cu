@@ -1,0 +1,464 @@
+// tp_lma.cu -- LMA disparity of the quad layout ("POLY", the reference's default
+// disparity when mix_corr_poly is set): Correlation2d.corrLMA
+// (Correlation2d.java:1754-1877) on the correlation surfaces of the last forward.
+//
+//  * the pairs are combined into an ortho group (horizontal as-is, vertical
+//    transposed) and a diagonal group (main as-is, other flipped vertically),
+//    each the mean of its pairs (combineCompatiblePairs 462-490);
+//  * around the CM centre each group keeps the cells reached from it through
+//    bi-convex cells in at most cnvx_hwnd_size steps (filterConvex 2029-2208)
+//    and turns them into samples weighted by weight x pairs x |value|^vasw_pwr
+//    (addSamples 2230-2386);
+//  * the samples are fitted by Ag (1 - ((x - x0) s / Wx)^2 - (y s / Wy)^2) per
+//    group (s = sqrt 2 for the diagonal group) with Levenberg-Marquardt and
+//    the reference's lambda schedule (Correlations2dLMA.java:211-640).
+//
+// One warp per tile: cells and samples are spread over the lanes, the region
+// growth runs one step per warp-synchronous pass, and the normal equations are
+// reduced across the warp and solved redundantly by every lane (FP32).
+#include "tp_dtt.cuh"
+
+#include <cmath>
+
+namespace {
+
+constexpr int LMA_NW = 4;             // warps (tiles) per CTA
+constexpr int LMA_ORTHO_ENTRIES = 81;  // addSamples enumeration, ortho group
+constexpr int LMA_DIAG_ENTRIES = 145;  // addSamples enumeration, diagonal group
+constexpr int LMA_MAX_SAMPLES = 162;   // 9x9 window cells per group
+constexpr int LMA_NP = 6;              // X0, WM, WYD, WXY, AG0, AG1
+
+// sample cell offsets from the (integer) centre, in the reference's enumeration order
+__constant__ signed char k_lma_cx[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+__constant__ signed char k_lma_cy[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+
+// per-warp shared memory (floats)
+constexpr int LMA_PER_WARP = 2 * 225             // group surfaces
+                             + 3 * 2 * 225 / 4   // convex / sel / sel_new flags (bytes)
+                             + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 8  // samples
+                             + 28 * 33 + 64;     // reduction buffer, accepted / trial normal equations
+
+struct LmaDev {
+  const float *corr;   // [tiles][P][225]
+  float *disp;         // [tiles][TP_NDISP]
+  float *lma;          // [tiles][4]
+  const int *task_txy;
+  int num_tasks, tilesX, P;
+  int kinds[TP_MAXP];  // pair kind or -1 when the pair does not take part
+};
+
+__device__ __forceinline__ float lma_weight(const unsigned char *conv, const unsigned char *sel, int idx, int x0,
+                                            int y0, const TpLmaConst &c) {
+  if (sel[idx]) return conv[idx] ? 1.0f : c.cnvx_weight;
+  if (c.cnvx_add3x3) {
+    const int row = idx / 15, col = idx - row * 15;
+    if (row >= y0 - 1 && row <= y0 + 1 && col >= x0 - 1 && col <= x0 + 1) return c.cnvx_weight;
+  }
+  return 0.0f;
+}
+
+constexpr int LMA_NEQ = 28;  // packed normal equations: A (upper 6x6, 21), b (6), weighted rms^2
+
+// Weighted normal equations of the samples at parameters av (getFxJt, getWJtJlambda, getWYmFxRms),
+// written to out[LMA_NEQ] for every lane: per-lane partial sums are transposed through red
+// [LMA_NEQ][33] and lane k sums row k in a fixed order.
+__device__ __forceinline__ void lma_eval(const float *sx, const float *sy, const float *sv, const float *sw,
+                                         const unsigned char *sg, int gdiag_bits, int ns, const float av[LMA_NP],
+                                         float w_wm, float w_wxy, float half_width, float *red, float *out,
+                                         int lane) {
+  float A[21], b[LMA_NP], r2 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 21; k++) A[k] = 0.f;
+#pragma unroll
+  for (int k = 0; k < LMA_NP; k++) b[k] = 0.f;
+  const float Wy = av[1] + av[2], Wx = Wy + av[3];
+  const float iWx = 1.0f / Wx, iWy = 1.0f / Wy;
+  for (int n = lane; n < ns; n += 32) {
+    const int g = sg[n];
+    const float ws = ((gdiag_bits >> g) & 1) ? 1.41421356237f : 1.0f;
+    const float Ag = g ? av[5] : av[4];
+    const float dxw = ws * (sx[n] - av[0]) * iWx, dyw = ws * sy[n] * iWy;
+    const float d = 1.0f - dxw * dxw - dyw * dyw;
+    const float e = sv[n] - d * Ag, w = sw[n], wr = w * e;
+    const float dfdWx = 2.0f * Ag * dxw * dxw * iWx, dfdWy = 2.0f * Ag * dyw * dyw * iWy;
+    const float j[LMA_NP] = {2.0f * ws * Ag * dxw * iWx, dfdWx + dfdWy, dfdWx + dfdWy, dfdWx,
+                             (g == 0) ? d : 0.0f, (g == 1) ? d : 0.0f};
+    r2 = fmaf(wr, e, r2);
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < LMA_NP; a++) {
+      b[a] = fmaf(j[a], wr, b[a]);
+      const float wj = w * j[a];
+#pragma unroll
+      for (int c = a; c < LMA_NP; c++) {
+        A[k] = fmaf(wj, j[c], A[k]);
+        k++;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 21; k++) red[k * 33 + lane] = A[k];
+#pragma unroll
+  for (int k = 0; k < LMA_NP; k++) red[(21 + k) * 33 + lane] = b[k];
+  red[27 * 33 + lane] = r2;
+  __syncwarp();
+  if (lane < LMA_NEQ) {
+    float t = 0.f;
+    for (int i = 0; i < 32; i++) t += red[lane * 33 + i];
+    // the two regularisation samples: WM towards half_width, WXY towards 0
+    const float e1 = half_width - av[1], e2 = -av[3];
+    if (lane == 6) t += w_wm;                 // A (1, 1)
+    if (lane == 15) t += w_wxy;               // A (3, 3)
+    if (lane == 22) t += w_wm * e1;           // b 1
+    if (lane == 24) t += w_wxy * e2;          // b 3
+    if (lane == 27) t += w_wm * e1 * e1 + w_wxy * e2 * e2;
+    out[lane] = t;
+  }
+  __syncwarp();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant__ LmaDev ld,
+                                                         const __grid_constant__ TpLmaConst c) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *gsurf = sm + warp * LMA_PER_WARP;                      // [2][225]
+  unsigned char *conv = (unsigned char *)(gsurf + 450);          // [2][225]
+  unsigned char *sel = conv + 450, *seln = sel + 450;            // [2][225]
+  float *sx = gsurf + 450 + 3 * 450 / 4 + 2;                    // samples
+  float *sy = sx + LMA_MAX_SAMPLES, *sv = sy + LMA_MAX_SAMPLES, *sw = sv + LMA_MAX_SAMPLES;
+  unsigned char *sg = (unsigned char *)(sw + LMA_MAX_SAMPLES);
+  float *red = sx + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1;  // [LMA_NEQ][33] transposed partial sums
+  float *acc = red + LMA_NEQ * 33, *trial = acc + 32;
+  const int hw = c.cnvx_hwnd_size;
+  for (int task = blockIdx.x * LMA_NW + warp; task < ld.num_tasks; task += gridDim.x * LMA_NW) {
+    const int txy = ld.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * ld.tilesX + (txy & 0xffff);
+    float *rec = ld.lma + tile * 4;
+    float *dm = ld.disp + tile * TP_NDISP;
+    const float cm = dm[1], strength = dm[2];  // the record's CM disparity and strength
+    if (lane < 4) rec[lane] = CUDART_NAN_F;
+    if (isnan(cm) || !(strength > c.min_poly_strength)) continue;
+    const float xcenter = -cm;
+    const int ixc = (int)floorf(xcenter + 0.5f);
+    // ---- group surfaces (combineCompatiblePairs) ----
+    int np_ortho = 0, np_diag = 0;
+    for (int pi = 0; pi < ld.P; pi++) {
+      np_ortho += (ld.kinds[pi] == 0 || ld.kinds[pi] == 1);
+      np_diag += (ld.kinds[pi] == 2 || ld.kinds[pi] == 3);
+    }
+    for (int e = lane; e < 450; e += 32) {
+      const int gd = e >= 225, i = e - 225 * gd, r = i / 15, q = i - r * 15;
+      float v = 0.f;
+      for (int pi = 0; pi < ld.P; pi++) {
+        const int k = ld.kinds[pi];
+        if (k < 0 || (k >= 2) != gd) continue;
+        const float *cs = ld.corr + (tile * ld.P + pi) * TP_CORR;
+        v += (k == 1) ? cs[q * 15 + r] : ((k == 3) ? cs[(14 - r) * 15 + q] : cs[i]);
+      }
+      const int npg = gd ? np_diag : np_ortho;
+      gsurf[e] = (npg > 1) ? v / npg : v;
+    }
+    __syncwarp();
+    // ---- filterConvex per group ----
+    for (int gd = 0; gd < 2; gd++) {
+      const int x0 = ixc + 7, y0 = (gd ? ixc : 0) + 7;
+      const int min_row = max(y0 - hw, 0), max_row = min(y0 + hw, 14);
+      const int min_col = max(x0 - hw, 0), max_col = min(x0 + hw, 14);
+      const float *d = gsurf + 225 * gd;
+      unsigned char *cv = conv + 225 * gd, *sl = sel + 225 * gd, *sn = seln + 225 * gd;
+      for (int i = lane; i < 225; i += 32) {
+        const int row = i / 15, col = i - row * 15;
+        bool cx = false;
+        if (row > min_row && row < max_row && col > min_col && col < max_col)
+          cx = (2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - 15] + d[i + 15]));
+        cv[i] = cx;
+        sl[i] = (i == y0 * 15 + x0) && y0 >= min_row && y0 <= max_row && x0 >= min_col && x0 <= max_col;
+      }
+      __syncwarp();
+      if ((gd ? np_diag : np_ortho) == 0) continue;
+      for (int istep = 0; istep < hw; istep++) {
+        for (int i = lane; i < 225; i += 32) sn[i] = sl[i];
+        __syncwarp();
+        const bool first = istep == 0;
+        const int smin_row = max(y0 - istep, 0), smax_row = min(y0 + istep, 14);
+        const int smin_col = max(x0 - istep, 0), smax_col = min(x0 + istep, 14);
+        const int ncol = smax_col - smin_col + 1, nrow = smax_row - smin_row + 1;
+        // items: up / down along the columns, left / right along the rows (all read sel, set sel_new)
+        for (int it = lane; it < 2 * ncol + 2 * nrow; it += 32) {
+          int dir, pos;
+          if (it < ncol) { dir = 0; pos = smin_col + it; }
+          else if (it < 2 * ncol) { dir = 1; pos = smin_col + it - ncol; }
+          else if (it < 2 * ncol + nrow) { dir = 2; pos = smin_row + it - 2 * ncol; }
+          else { dir = 3; pos = smin_row + it - 2 * ncol - nrow; }
+          if (dir == 0 && !(istep < y0)) continue;
+          if (dir == 1 && !((y0 + istep) < max_row)) continue;
+          if (dir == 2 && !(istep < x0)) continue;
+          if (dir == 3 && !((x0 + istep) < max_col)) continue;
+          const int row = (dir == 0) ? y0 - istep : (dir == 1 ? y0 + istep : pos);
+          const int col = (dir == 2) ? x0 - istep : (dir == 3 ? x0 + istep : pos);
+          const int i = row * 15 + col;
+          if (!(sl[i] && (cv[i] || first))) continue;
+          const int step = (dir == 0) ? -15 : (dir == 1 ? 15 : (dir == 2 ? -1 : 1));
+          const int j = i + step;
+          sn[j] = 1;
+          if (cv[j]) {
+            if (dir <= 1) {
+              if (col <= x0 && col > min_col) sn[j - 1] = 1;
+              if (col >= x0 && col < max_col) sn[j + 1] = 1;
+            } else {
+              if (row <= y0 && row > min_row) sn[j - 15] = 1;
+              if (row >= y0 && row < max_row) sn[j + 15] = 1;
+            }
+          }
+        }
+        __syncwarp();
+        bool changed = false;
+        for (int i = lane; i < 225; i += 32) changed |= (sn[i] != sl[i]);
+        if (!__any_sync(0xffffffffu, changed)) break;
+        for (int i = lane; i < 225; i += 32) sl[i] = sn[i];
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+    // ---- samples (addSamples), compacted in the enumeration order ----
+    int ns = 0, ngroups = 0, gdiag_bits = 0;
+    for (int gd = 0; gd < 2; gd++) {
+      const int npg = gd ? np_diag : np_ortho;
+      if (npg == 0) continue;
+      const int base = gd ? LMA_ORTHO_ENTRIES : 0, cnt = gd ? LMA_DIAG_ENTRIES : LMA_ORTHO_ENTRIES;
+      const float *d = gsurf + 225 * gd;
+      int gnum = -1;  // groups are numbered in the order their first sample arrives
+      for (int e0 = 0; e0 < cnt; e0 += 32) {
+        const int e = e0 + lane;
+        float w = 0.f, v = 0.f, x = 0.f, y = 0.f;
+        if (e < cnt) {
+          const int cxo = k_lma_cx[base + e], cyo = k_lma_cy[base + e];
+          const int cx = cxo + ixc, cy = cyo + (gd ? ixc : 0);
+          if (cx >= -7 && cx <= 7 && cy >= -7 && cy <= 7) {
+            const int idx = 112 + 15 * cy + cx;
+            w = lma_weight(conv + 225 * gd, sel + 225 * gd, idx, ixc + 7, (gd ? ixc : 0) + 7, c) * npg;
+            if (w > 0.f) {
+              v = d[idx];
+              if (c.ortho_vasw_pwr == 2.0f) w *= v * v;
+              else if (c.ortho_vasw_pwr != 0.0f) w *= powf(fabsf(v), c.ortho_vasw_pwr);
+              x = (gd ? 0.5f * (cxo + cyo) : (float)cxo) + (float)ixc;
+              y = gd ? 0.5f * (cyo - cxo) : (float)cyo;
+            }
+          }
+        }
+        const unsigned take = __ballot_sync(0xffffffffu, w > 0.f);
+        if (take && gnum < 0) {
+          gnum = ngroups++;
+          gdiag_bits |= gd << gnum;
+        }
+        if (w > 0.f) {
+          const int o = ns + __popc(take & ((1u << lane) - 1u));
+          if (o < LMA_MAX_SAMPLES) {
+            sx[o] = x; sy[o] = y; sv[o] = v; sw[o] = w;
+            sg[o] = (unsigned char)gnum;
+          }
+        }
+        ns = min(ns + __popc(take), LMA_MAX_SAMPLES);
+      }
+    }
+    __syncwarp();
+    if (ns == 0) continue;
+    // ---- initVector / setWeightsValues ----
+    float wsum = 0.f, gw0 = 0.f, gw1 = 0.f, vmax = -CUDART_INF_F, smax = 0.f;
+    int imx = 1 << 30;
+    for (int n = lane; n < ns; n += 32) {
+      float w = sw[n], v = sv[n];
+      if (sg[n] == 0) gw0 += w; else gw1 += w;
+      if (v > smax) smax = v;
+      if (isnan(v) || isnan(w)) { w = 0.f; v = 0.f; sw[n] = 0.f; sv[n] = 0.f; }
+      wsum += w;
+      if (v > vmax) { vmax = v; imx = n; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {  // first maximum of the sample values
+      const float ov = __shfl_xor_sync(0xffffffffu, vmax, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, imx, o);
+      if (ov > vmax || (ov == vmax && oi < imx)) { vmax = ov; imx = oi; }
+    }
+    wsum = warp_sum(wsum);
+    gw0 = warp_sum(gw0);
+    gw1 = warp_sum(gw1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = fmaxf(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    const float pure = wsum;
+    const float tot = wsum + c.cost_wy + c.cost_wxy;
+    const float inv = (tot != 0.f) ? 1.0f / tot : 1.0f;
+    for (int n = lane; n < ns; n += 32) sw[n] *= inv;
+    __syncwarp();
+    const float w_wm = c.cost_wy * inv, w_wxy = c.cost_wxy * inv;
+    const float gwt[2] = {pure > 0.f ? gw0 / pure : gw0, pure > 0.f ? gw1 / pure : gw1};
+    const bool mask[LMA_NP] = {true, c.adjust_wm != 0, c.adjust_wy != 0, c.adjust_wxy != 0,
+                               c.adjust_ag != 0 && ngroups > 0, c.adjust_ag != 0 && ngroups > 1};
+    float av[LMA_NP] = {xcenter, c.half_width, 0.f, 0.f, vmax, vmax};
+    if (ngroups < 2) av[5] = 0.f;
+    // ---- runLma / lmaStep ----
+    // acc: normal equations at the accepted parameters; trial: at the proposed ones
+    lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, av, w_wm, w_wxy, c.half_width, red, acc, lane);
+    float last = sqrtf(acc[27]);
+    const float initial = last;
+    float lambda = c.lambda_initial;
+    bool success = false;
+    for (int iter = 0; iter < c.num_iter; iter++) {
+      // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held
+      float M[LMA_NP][LMA_NP + 1];
+      {
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < LMA_NP; a++)
+#pragma unroll
+          for (int cc = a; cc < LMA_NP; cc++) {
+            const float v = acc[k++];
+            M[a][cc] = v;
+            M[cc][a] = v;
+          }
+      }
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++) {
+        M[a][a] += M[a][a] * lambda;
+        M[a][LMA_NP] = acc[21 + a];
+        if (!mask[a]) {
+#pragma unroll
+          for (int cc = 0; cc <= LMA_NP; cc++) M[a][cc] = (cc == a) ? 1.0f : 0.0f;
+#pragma unroll
+          for (int r = 0; r < LMA_NP; r++)
+            if (r != a) M[r][a] = 0.0f;
+        }
+      }
+      bool singular = false;
+#pragma unroll
+      for (int col = 0; col < LMA_NP; col++) {
+        // partial pivoting by compare-and-swap (static indices keep M in registers)
+#pragma unroll
+        for (int r = col + 1; r < LMA_NP; r++) {
+          const bool sw = fabsf(M[r][col]) > fabsf(M[col][col]);
+#pragma unroll
+          for (int cc = 0; cc <= LMA_NP; cc++) {
+            const float t = M[col][cc];
+            M[col][cc] = sw ? M[r][cc] : t;
+            M[r][cc] = sw ? t : M[r][cc];
+          }
+        }
+        if (M[col][col] == 0.0f) singular = true;
+        const float pinv = (M[col][col] != 0.0f) ? 1.0f / M[col][col] : 0.0f;
+#pragma unroll
+        for (int r = col + 1; r < LMA_NP; r++) {
+          const float f = M[r][col] * pinv;
+#pragma unroll
+          for (int cc = col; cc <= LMA_NP; cc++) M[r][cc] -= f * M[col][cc];
+        }
+      }
+      if (singular) break;
+      float delta[LMA_NP];
+#pragma unroll
+      for (int r = LMA_NP - 1; r >= 0; r--) {
+        float s = M[r][LMA_NP];
+#pragma unroll
+        for (int k = r + 1; k < LMA_NP; k++) s -= M[r][k] * delta[k];
+        delta[r] = s / M[r][r];
+      }
+      float nav[LMA_NP];
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++) nav[a] = av[a] + (mask[a] ? delta[a] : 0.0f);
+      lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, nav, w_wm, w_wxy, c.half_width, red, trial, lane);
+      const float rms = sqrtf(trial[27]);
+      bool done = false;
+      if (rms < last) {
+        success = true;
+        done = rms >= last * (1.0f - c.rms_diff);
+        last = rms;
+#pragma unroll
+        for (int a = 0; a < LMA_NP; a++) av[a] = nav[a];
+        if (lane < LMA_NEQ) acc[lane] = trial[lane];
+        __syncwarp();
+      } else {
+        success = false;
+      }
+      if (done) break;
+      if (success) lambda *= c.lambda_scale_good;
+      else {
+        lambda *= c.lambda_scale_bad;
+        if (lambda > c.lambda_max) break;
+      }
+    }
+    if (!success && last < initial) success = true;
+    if (!success) continue;
+    // ---- getDisparityStrength ----
+    float sum_amp = gwt[0] * av[4] + (ngroups > 1 ? gwt[1] * av[5] : 0.0f);
+    if (sum_amp > 1.25f * smax) sum_amp = smax;
+    if (lane == 0) {
+      rec[0] = -av[0];
+      rec[1] = sum_amp;
+      rec[2] = av[1];
+      rec[3] = av[3];
+      if (c.mix_corr_poly) {
+        dm[1] = -av[0];
+        dm[2] = sum_amp;
+      }
+    }
+  }
+}
+
+cudaError_t upload_lma_constants() {
+  // addSamples enumeration (Correlation2d.java:2314-2382): quadrant signs {-1,-1},{1,-1},{-1,1},{1,1}
+  signed char cx[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES], cy[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+  static const int qs[4][2] = {{-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+  int n = 0;
+  for (int diag = 0; diag < 2; diag++) {
+    const int start = n;
+    for (int arow = 0; arow < 9; arow += diag ? 1 : 2)
+      for (int acol = diag ? (arow & 1) : 0; acol < 9; acol += 2)
+        for (int q = 0; q < 4; q++) {
+          if (!(((arow > 0) || (q & 2)) && ((acol > 0) || (q & 1)))) continue;
+          if (diag) {
+            cx[n] = (signed char)((qs[q][0] * acol - qs[q][1] * arow) / 2);
+            cy[n] = (signed char)((qs[q][0] * acol + qs[q][1] * arow) / 2);
+          } else {
+            cx[n] = (signed char)((qs[q][0] * acol) / 2);
+            cy[n] = (signed char)((qs[q][1] * arow) / 2);
+          }
+          n++;
+        }
+    if (n - start != (diag ? LMA_DIAG_ENTRIES : LMA_ORTHO_ENTRIES)) return cudaErrorInvalidValue;
+  }
+  cudaError_t e = cudaMemcpyToSymbol(k_lma_cx, cx, sizeof(cx));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_lma_cy, cy, sizeof(cy));
+  return e;
+}
+
+int lma_smem_bytes() { return LMA_NW * LMA_PER_WARP * 4; }
+
+cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out, cudaStream_t st) {
+  if (sc.num_tasks <= 0) return cudaSuccess;
+  if (c.cnvx_hwnd_size < 0 || c.cnvx_hwnd_size > 4) return cudaErrorInvalidValue;  // 9x9 sample window
+  LmaDev ld;
+  ld.corr = sc.corr;
+  ld.disp = sc.disp;
+  ld.lma = lma_out;
+  ld.task_txy = sc.task_txy;
+  ld.num_tasks = sc.num_tasks;
+  ld.tilesX = sc.tilesX;
+  ld.P = cc.num_pairs;
+  for (int i = 0; i < TP_MAXP; i++) {
+    const int k = (i < cc.num_pairs) ? cc.pairs[i].kind : -1;
+    ld.kinds[i] = (k >= 0 && k <= 3 && ((c.pair_mask >> i) & 1)) ? k : -1;
+  }
+  const int bytes = lma_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(lma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lma_kernel, 32 * LMA_NW, bytes);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int units = (sc.num_tasks + LMA_NW - 1) / LMA_NW;
+  const int grid = units < sms * per_sm ? units : sms * per_sm;
+  lma_kernel<<<grid, 32 * LMA_NW, bytes, st>>>(ld, c);
+  return cudaGetLastError();
+}

@@ -55,6 +55,15 @@ class TpTextureParams(C.Structure):
                 ("corr_mode", C.c_int), ("aux", C.c_int)]
 
 
+class TpLmaParams(C.Structure):
+    _fields_ = [("min_poly_strength", C.c_float), ("mix_corr_poly", C.c_int), ("ortho_vasw_pwr", C.c_float),
+                ("cnvx_hwnd_size", C.c_int), ("cnvx_weight", C.c_float), ("cnvx_add3x3", C.c_int),
+                ("adjust_wm", C.c_int), ("adjust_wy", C.c_int), ("adjust_wxy", C.c_int), ("adjust_ag", C.c_int),
+                ("half_width", C.c_float), ("cost_wy", C.c_float), ("cost_wxy", C.c_float),
+                ("lambda_initial", C.c_float), ("lambda_scale_good", C.c_float), ("lambda_scale_bad", C.c_float),
+                ("lambda_max", C.c_float), ("rms_diff", C.c_float), ("num_iter", C.c_int), ("pair_mask", C.c_int)]
+
+
 _H = C.c_void_p
 _vp = C.c_void_p
 
@@ -98,6 +107,9 @@ PROTOTYPES = {
     "tp_get_textures": [_H, _vp],
     "tp_get_texture_aux": [_H, _vp],
     "tp_compact_tile_ops_noalloc": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
+    "tp_default_lma_params": [C.POINTER(TpLmaParams)],
+    "tp_lma_refine": [_H, C.POINTER(TpLmaParams), _vp],
+    "tp_get_lma": [_H, _vp],
     "tp_rig_correlate": [_H, _H, C.c_float, C.c_int, _vp],
     "tp_get_rig": [_H, _vp, _vp],
     "tp_batch_create": [C.POINTER(_H), C.c_int, C.POINTER(_H)],

@@ -274,6 +274,23 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_get_rbg(self.h, int(ncam), _ptr(out)), "tp_get_rbg")
         return out
 
+    # ---- LMA disparity ----
+    def lmaRefine(self, params=None, stream=None, **kw):
+        """Correlation2d.corrLMA on the last process(): returns [tiles][4] = {disparity, strength, WM, WXY}
+        (NaN where not run); with mix_corr_poly (default) the disparity record's CM / strength take it."""
+        if params is None:
+            params = L.TpLmaParams()
+            self._ck(self._lib.tp_default_lma_params(C.byref(params)), "tp_default_lma_params")
+        for k, v in kw.items():
+            setattr(params, k, v)
+        self._ck(self._lib.tp_lma_refine(self.h, C.byref(params), stream), "tp_lma_refine")
+        return self.getLma()
+
+    def getLma(self):
+        out = np.zeros((self.tilesY * self.tilesX, 4), dtype=np.float32)
+        self._ck(self._lib.tp_get_lma(self.h, _ptr(out)), "tp_get_lma")
+        return out
+
     # ---- rig ----
     def rigCorrelate(self, aux, cm_max_normalization=0.55, no_int_x0=False, stream=None):
         """Inter-camera correlation with the auxiliary camera `aux` (another GPUTileProcessor on the

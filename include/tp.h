@@ -221,6 +221,38 @@ tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
 tp_status tp_get_texture_aux(tp_handle *h, float *aux);
 
+/* ---- LMA disparity ("POLY"): Correlation2d.corrLMA (Correlation2d.java:1754-1877)
+ * with Correlations2dLMA (Correlations2dLMA.java:211-640), run by ImageDtt at
+ * ImageDtt.java:2254-2288.  After tp_process on a quad pair layout, every tile
+ * whose CM disparity exists and whose integer-max strength exceeds
+ * min_poly_strength is refitted: the ortho pairs (horizontal, vertical
+ * transposed) and the diagonal pairs (main, other flipped) are averaged into
+ * two groups, cells reached from the CM centre through bi-convex cells are
+ * sampled, and a per-group parabola with a common centre and widths is fitted
+ * by Levenberg-Marquardt.  Output per tile {disparity, strength, half-width
+ * WM, WXY} (getDisparityStrengthWidth; NaN where not run or not converged).
+ * With mix_corr_poly the result also replaces TP_DISP_CM and TP_DISP_STRENGTH
+ * of the disparity record, as the reference does; the pass then needs a new
+ * tp_process before it can run again.  Pair kinds 4 (general) do not take
+ * part; cnvx_hwnd_size is at most 4.  Defaults: ImageDttParameters.java:32-109. */
+typedef struct {
+  float min_poly_strength;  /* 0.2 */
+  int mix_corr_poly;        /* 1 */
+  float ortho_vasw_pwr;     /* 2.0: sample weight x |value|^pwr */
+  int cnvx_hwnd_size;       /* 4 */
+  float cnvx_weight;        /* 0.5: weight of selected non-convex cells */
+  int cnvx_add3x3;          /* 1: the 3x3 cells around the centre are always sampled */
+  int adjust_wm, adjust_wy, adjust_wxy, adjust_ag; /* 1, 0, 1, 1 */
+  float half_width, cost_wy, cost_wxy;             /* 2.0, 0.1, 0.1 */
+  float lambda_initial, lambda_scale_good, lambda_scale_bad, lambda_max, rms_diff; /* 0.1, 0.5, 8, 100, 0.001 */
+  int num_iter;             /* 20 */
+  int pair_mask;            /* bit i: pair i takes part (dbg_pair_mask 0x3f) */
+} tp_lma_params;
+tp_status tp_default_lma_params(tp_lma_params *p);
+tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream);
+/* out [tilesY*tilesX][4] */
+tp_status tp_get_lma(tp_handle *h, float *out);
+
 /* ---- rig: main and auxiliary quad cameras (ImageDtt.clt_bi_quad, ImageDtt.java:8731-) ----
  * Inter-camera correlation of the sensor-averaged CLT of each camera
  * (Correlation2d.correlateInterCamerasFD / cltMixCameras, Correlation2d.java:401-448)

@@ -498,3 +498,54 @@ def rig_tile(clt_main, clt_aux, corr_params=None, cm_max_normalization=0.55, no_
     L.or_rig_tile(_d(a), a.shape[0], _d(b), b.shape[0], a.shape[1], C.byref(cp), float(cm_max_normalization),
                   int(bool(no_int_x0)), _d(corr), _d(rec))
     return corr, rec
+
+
+class LmaParams(C.Structure):
+    _fields_ = [("min_poly_strength", C.c_double), ("mix_corr_poly", C.c_int), ("ortho_vasw_pwr", C.c_double),
+                ("cnvx_hwnd_size", C.c_int), ("cnvx_weight", C.c_double), ("cnvx_add3x3", C.c_int),
+                ("adjust_wm", C.c_int), ("adjust_wy", C.c_int), ("adjust_wxy", C.c_int), ("adjust_ag", C.c_int),
+                ("half_width", C.c_double), ("cost_wy", C.c_double), ("cost_wxy", C.c_double),
+                ("lambda_initial", C.c_double), ("lambda_scale_good", C.c_double), ("lambda_scale_bad", C.c_double),
+                ("lambda_max", C.c_double), ("rms_diff", C.c_double), ("num_iter", C.c_int), ("pair_mask", C.c_int)]
+
+
+def _lma_lib():
+    L = lib()
+    if not getattr(L, "_lma_set", False):
+        L.or_default_lma_params.argtypes = [C.POINTER(LmaParams)]
+        L.or_default_lma_params.restype = None
+        L.or_corr_lma.argtypes = [_dp, C.POINTER(C.c_int), C.c_int, C.c_double, C.POINTER(LmaParams), _dp,
+                                  C.POINTER(C.c_int)]
+        L.or_corr_lma.restype = C.c_int
+        L.or_filter_convex.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp]
+        L.or_filter_convex.restype = None
+        L._lma_set = True
+    return L
+
+
+def default_lma_params(**kw):
+    p = LmaParams()
+    _lma_lib().or_default_lma_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def filter_convex(corr225, hwin, x0c, y0c, add3x3=True, nc_cost=0.5):
+    a = _f64(corr225)
+    out = np.zeros(225)
+    _lma_lib().or_filter_convex(_d(a), int(hwin), int(x0c), int(y0c), int(bool(add3x3)), float(nc_cost), _d(out))
+    return out
+
+
+def corr_lma(corrs, kinds, xcenter, params=None):
+    """Correlation2d.corrLMA on one tile: corrs [np][225], quad pair kinds -> (ok, {disparity, strength,
+    WM, WXY}, number of samples)."""
+    a = _f64(corrs)
+    k = np.ascontiguousarray(np.asarray(kinds, dtype=np.int32))
+    p = params if params is not None else default_lma_params()
+    out = np.zeros(4)
+    ns = C.c_int(0)
+    ok = _lma_lib().or_corr_lma(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], float(xcenter),
+                                C.byref(p), _d(out), C.byref(ns))
+    return bool(ok), out, ns.value

@@ -1643,3 +1643,399 @@ void or_rig_tile(const double *clt_main, int s_main, const double *clt_aux, int 
     rec[1] = cs[1] / (eff * eff);
   }
 }
+
+/* ===================== LMA disparity (Correlation2d.corrLMA) ===================== */
+
+void or_default_lma_params(or_lma_params *p) {
+  /* ImageDttParameters.java:32-109 */
+  p->min_poly_strength = 0.2;
+  p->mix_corr_poly = 1;
+  p->ortho_vasw_pwr = 2.0;
+  p->cnvx_hwnd_size = 4;
+  p->cnvx_weight = 0.5;
+  p->cnvx_add3x3 = 1;
+  p->adjust_wm = 1; p->adjust_wy = 0; p->adjust_wxy = 1; p->adjust_ag = 1;
+  p->half_width = 2.0; p->cost_wy = 0.1; p->cost_wxy = 0.1;
+  p->lambda_initial = 0.1; p->lambda_scale_good = 0.5; p->lambda_scale_bad = 8.0; p->lambda_max = 100.0;
+  p->rms_diff = 0.001;
+  p->num_iter = 20;
+  p->pair_mask = 0x3f;
+}
+
+/* Correlation2d.filterConvex (2029-2208) */
+void or_filter_convex(const double *d, int hwin, int x0c, int y0c, int add3x3, double nc_cost, double *weights) {
+  const int W = OR_CORR, center = OR_DTT - 1;
+  const int x0 = x0c + center, y0 = y0c + center;
+  unsigned char convex[OR_CORR * OR_CORR], sel[OR_CORR * OR_CORR], seln[OR_CORR * OR_CORR];
+  memset(convex, 0, sizeof(convex));
+  memset(sel, 0, sizeof(sel));
+  for (int i = 0; i < W * W; i++) weights[i] = 0.0;
+  int min_row = y0 - hwin, max_row = y0 + hwin, min_col = x0 - hwin, max_col = x0 + hwin;
+  if (min_row < 0) min_row = 0;
+  if (max_row >= W) max_row = W - 1;
+  if (min_col < 0) min_col = 0;
+  if (max_col >= W) max_col = W - 1;
+  for (int row = min_row + 1; row < max_row; row++)
+    for (int col = min_col + 1; col < max_col; col++) {
+      const int i = row * W + col;
+      convex[i] = (2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - W] + d[i + W]));
+    }
+  if ((y0 >= min_row) && (y0 <= max_row) && (x0 >= min_col) && (x0 <= max_col)) sel[y0 * W + x0] = 1;
+  for (int istep = 0; istep < hwin; istep++) {
+    memcpy(seln, sel, sizeof(sel));
+    const int first = (istep == 0);
+    int num_new = 0;
+    int smin_row = y0 - istep, smax_row = y0 + istep, smin_col = x0 - istep, smax_col = x0 + istep;
+    if (smin_row < 0) smin_row = 0;
+    if (smax_row >= W) smax_row = W - 1;
+    if (smin_col < 0) smin_col = 0;
+    if (smax_col >= W) smax_col = W - 1;
+    if (istep < y0) { /* up */
+      const int row = y0 - istep;
+      for (int col = smin_col; col <= smax_col; col++) {
+        const int i = row * W + col;
+        if (sel[i] && (convex[i] || first)) {
+          if (!seln[i - W]) { seln[i - W] = 1; num_new++; }
+          const int j = i - W;
+          if (convex[j]) {
+            if ((col <= x0) && (col > min_col) && !seln[j - 1]) { seln[j - 1] = 1; num_new++; }
+            if ((col >= x0) && (col < max_col) && !seln[j + 1]) { seln[j + 1] = 1; num_new++; }
+          }
+        }
+      }
+    }
+    if ((y0 + istep) < max_row) { /* down */
+      const int row = y0 + istep;
+      for (int col = smin_col; col <= smax_col; col++) {
+        const int i = row * W + col;
+        if (sel[i] && (convex[i] || first)) {
+          if (!seln[i + W]) { seln[i + W] = 1; num_new++; }
+          const int j = i + W;
+          if (convex[j]) {
+            if ((col <= x0) && (col > min_col) && !seln[j - 1]) { seln[j - 1] = 1; num_new++; }
+            if ((col >= x0) && (col < max_col) && !seln[j + 1]) { seln[j + 1] = 1; num_new++; }
+          }
+        }
+      }
+    }
+    if (istep < x0) { /* left */
+      const int col = x0 - istep;
+      for (int row = smin_row; row <= smax_row; row++) {
+        const int i = row * W + col;
+        if (sel[i] && (convex[i] || first)) {
+          if (!seln[i - 1]) { seln[i - 1] = 1; num_new++; }
+          const int j = i - 1;
+          if (convex[j]) {
+            if ((row <= y0) && (row > min_row) && !seln[j - W]) { seln[j - W] = 1; num_new++; }
+            if ((row >= y0) && (row < max_row) && !seln[j + W]) { seln[j + W] = 1; num_new++; }
+          }
+        }
+      }
+    }
+    if ((x0 + istep) < max_col) { /* right */
+      const int col = x0 + istep;
+      for (int row = smin_row; row <= smax_row; row++) {
+        const int i = row * W + col;
+        if (sel[i] && (convex[i] || first)) {
+          if (!seln[i + 1]) { seln[i + 1] = 1; num_new++; }
+          const int j = i + 1;
+          if (convex[j]) {
+            if ((row <= y0) && (row > min_row) && !seln[j - W]) { seln[j - W] = 1; num_new++; }
+            if ((row >= y0) && (row < max_row) && !seln[j + W]) { seln[j + W] = 1; num_new++; }
+          }
+        }
+      }
+    }
+    if (num_new == 0) break;
+    memcpy(sel, seln, sizeof(sel));
+  }
+  for (int i = 0; i < W * W; i++)
+    if (sel[i]) weights[i] = convex[i] ? 1.0 : nc_cost;
+  if (add3x3) {
+    for (int row = y0 - 1; row <= y0 + 1; row++)
+      if ((row >= 0) && (row < W))
+        for (int col = x0 - 1; col <= x0 + 1; col++)
+          if ((col >= 0) && (col < W)) {
+            const int i = row * W + col;
+            if (weights[i] == 0.0) weights[i] = nc_cost;
+          }
+  }
+}
+
+#define LMA_MAX_SAMPLES 512
+#define LMA_NPAR 6 /* X0, WM, WYD, WXY, AG0, AG1 */
+typedef struct {
+  int ns;
+  double x[LMA_MAX_SAMPLES], y[LMA_MAX_SAMPLES], v[LMA_MAX_SAMPLES], w[LMA_MAX_SAMPLES];
+  int grp[LMA_MAX_SAMPLES];
+  int ngroups, gdiag[2];
+  /* setWeightsValues */
+  double weights[LMA_MAX_SAMPLES + 2], values[LMA_MAX_SAMPLES + 2], group_weights[2], pure_weight;
+  double all_pars[LMA_NPAR];
+  int par_idx[LMA_NPAR], nv; /* vector -> all_pars index */
+} or_lma;
+
+/* Correlations2dLMA.getFxJt (334-384): fx [ns + 2], jt [nv][ns + 2] (or NULL) */
+static void lma_fx_jt(const or_lma *L, const double *vec, double *fx, double *jt) {
+  double av[LMA_NPAR];
+  memcpy(av, L->all_pars, sizeof(av));
+  for (int k = 0; k < L->nv; k++) av[L->par_idx[k]] = vec[k];
+  const int np = L->ns + 2;
+  const double sqrt2 = sqrt(2.0);
+  for (int n = 0; n < L->ns; n++) {
+    const int g = L->grp[n];
+    const double wScale = L->gdiag[g] ? sqrt2 : 1.0;
+    const double Wy = av[1] * 1.0 + av[2]; /* scales[si] = 1 for the quad layout */
+    const double Wx = Wy + av[3];
+    const double dx = L->x[n] - av[0];
+    const double Ag = av[4 + g];
+    const double dxw = wScale * dx / Wx, dyw = wScale * L->y[n] / Wy;
+    const double d = (1.0 - dxw * dxw - dyw * dyw);
+    fx[n] = d * Ag;
+    if (jt) {
+      const double dfdWx = Ag * 2 * dxw * dxw / Wx, dfdWy = Ag * 2 * dyw * dyw / Wy;
+      for (int k = 0; k < L->nv; k++) {
+        const int pi = L->par_idx[k];
+        double j = 0.0;
+        if (pi == 0) j = wScale * Ag * 2 * dxw / Wx;
+        else if (pi == 1) j = 1.0 * (dfdWx + dfdWy);
+        else if (pi == 2) j = dfdWx + dfdWy;
+        else if (pi == 3) j = dfdWx;
+        else j = (pi - 4 == g) ? d : 0.0;
+        jt[k * np + n] = j;
+      }
+    }
+  }
+  fx[L->ns] = av[1];
+  fx[L->ns + 1] = av[3];
+  if (jt)
+    for (int k = 0; k < L->nv; k++) {
+      jt[k * np + L->ns] = (L->par_idx[k] == 1) ? 1.0 : 0.0;
+      jt[k * np + L->ns + 1] = (L->par_idx[k] == 3) ? 1.0 : 0.0;
+    }
+}
+
+/* getWYmFxRms (432-452): fx becomes weights (y - fx); returns rms (rms_pure optional) */
+static double lma_rms(const or_lma *L, double *fx, double *rms_pure) {
+  double rms = 0.0;
+  for (int i = 0; i < L->ns; i++) {
+    const double d = L->values[i] - fx[i];
+    fx[i] = L->weights[i] * d;
+    rms += fx[i] * d;
+  }
+  if (rms_pure) *rms_pure = sqrt(rms) / L->pure_weight;
+  for (int i = L->ns; i < L->ns + 2; i++) {
+    const double d = L->values[i] - fx[i];
+    fx[i] = L->weights[i] * d;
+    rms += fx[i] * d;
+  }
+  return sqrt(rms);
+}
+
+/* solve A x = b (n x n, row-major) by LU with partial pivoting; 0 if singular (a zero pivot) */
+static int lma_solve(double *A, double *b, int n) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++)
+      if (fabs(A[r * n + c]) > fabs(A[p * n + c])) p = r;
+    if (A[p * n + c] == 0.0) return 0;
+    if (p != c) {
+      for (int k = 0; k < n; k++) { const double t = A[c * n + k]; A[c * n + k] = A[p * n + k]; A[p * n + k] = t; }
+      const double t = b[c]; b[c] = b[p]; b[p] = t;
+    }
+    for (int r = c + 1; r < n; r++) {
+      const double f = A[r * n + c] / A[c * n + c];
+      for (int k = c; k < n; k++) A[r * n + k] -= f * A[c * n + k];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    double s = b[r];
+    for (int k = r + 1; k < n; k++) s -= A[r * n + k] * b[k];
+    b[r] = s / A[r * n + r];
+  }
+  return 1;
+}
+
+static void lma_add_group(or_lma *L, const double *g, int diag, int npairs, double xcenter, const or_lma_params *p) {
+  /* addSamples (2230-2386) for one group, scale 1 */
+  static const int qs[4][2] = {{-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+  const int hw = p->cnvx_hwnd_size, hw2 = 2 * hw + 1, center = OR_DTT - 1, W = OR_CORR;
+  const int center_index = (W + 1) * center;
+  const int ixc = (int)floor(xcenter + 0.5); /* Math.round */
+  const double xcs = ixc * 1.0, scale05 = 0.5;
+  double fw[OR_CORR * OR_CORR];
+  or_filter_convex(g, hw, ixc, diag ? ixc : 0, p->cnvx_add3x3, p->cnvx_weight, fw);
+  int gnum = -1;
+  for (int arow = 0; arow < hw2; arow += diag ? 1 : 2) {
+    const int odd = diag ? (arow & 1) : 0;
+    for (int acol = odd; acol < hw2; acol += 2)
+      for (int q = 0; q < 4; q++) {
+        if (!(((arow > 0) || (q & 2)) && ((acol > 0) || (q & 1)))) continue;
+        int cx, cy;
+        if (diag) {
+          cx = (qs[q][0] * acol - qs[q][1] * arow) / 2 + ixc;
+          cy = (qs[q][0] * acol + qs[q][1] * arow) / 2 + ixc;
+        } else {
+          cx = (qs[q][0] * acol) / 2 + ixc;
+          cy = (qs[q][1] * arow) / 2;
+        }
+        if (cx < -center || cx > center || cy < -center || cy > center) continue;
+        double w = fw[center_index + W * cy + cx] * npairs;
+        if (!(w > 0.0)) continue;
+        const double v = g[center_index + W * cy + cx];
+        if (p->ortho_vasw_pwr != 0) w *= pow(fabs(v), p->ortho_vasw_pwr);
+        if (L->ns >= LMA_MAX_SAMPLES) continue;
+        if (gnum < 0) { /* groups are numbered in the order their first sample arrives */
+          gnum = L->ngroups++;
+          L->gdiag[gnum] = diag;
+        }
+        L->x[L->ns] = qs[q][0] * acol * scale05 + xcs;
+        L->y[L->ns] = qs[q][1] * arow * scale05;
+        L->v[L->ns] = v;
+        L->w[L->ns] = w;
+        L->grp[L->ns] = gnum;
+        L->ns++;
+      }
+  }
+}
+
+int or_corr_lma(const double *corrs, const int *kind, int np, double xcenter, const or_lma_params *p, double out[4],
+                int *n_samples) {
+  out[0] = out[1] = out[2] = out[3] = NAN;
+  static or_lma Ls;  /* large: not on the stack (single-threaded use from the tests) */
+  or_lma *L = &Ls;
+  memset(L, 0, sizeof(*L));
+  /* combineCompatiblePairs (462-490) for GROUPS {ortho, 1}, {diagonal, 1} */
+  for (int gdiag = 0; gdiag < 2; gdiag++) {
+    double g[OR_CORR * OR_CORR];
+    memset(g, 0, sizeof(g));
+    int n = 0;
+    for (int i = 0; i < np; i++) {
+      if (!((p->pair_mask >> i) & 1) || kind[i] < 0 || kind[i] > 3) continue;
+      const int is_diag = kind[i] >= 2;
+      if (is_diag != gdiag) continue;
+      const double *c = corrs + (size_t)i * OR_CORR * OR_CORR;
+      for (int r = 0; r < OR_CORR; r++)
+        for (int q = 0; q < OR_CORR; q++) {
+          double v;
+          if (kind[i] == 0 || kind[i] == 2) v = c[r * OR_CORR + q];
+          else if (kind[i] == 1) v = c[q * OR_CORR + r];                /* getTransposeAllOrtho */
+          else v = c[(OR_CORR - r - 1) * OR_CORR + q];                   /* getTransposeAllDiagonal */
+          g[r * OR_CORR + q] += v;
+        }
+      n++;
+    }
+    if (n == 0) continue;
+    if (n > 1)
+      for (int k = 0; k < OR_CORR * OR_CORR; k++) g[k] /= n;
+    lma_add_group(L, g, gdiag, n, xcenter, p);
+  }
+  if (n_samples) *n_samples = L->ns;
+  /* initVector (211-241) and setWeightsValues (243-275) */
+  const int ns = L->ns, npt = ns + 2;
+  L->all_pars[0] = xcenter;
+  L->all_pars[1] = p->half_width;
+  L->all_pars[2] = 0.0;
+  L->all_pars[3] = 0.0;
+  const int mask[LMA_NPAR] = {1, p->adjust_wm, p->adjust_wy, p->adjust_wxy, p->adjust_ag && L->ngroups > 0,
+                              p->adjust_ag && L->ngroups > 1};
+  L->nv = 0;
+  for (int i = 0; i < 4 + L->ngroups; i++)
+    if (mask[i]) L->par_idx[L->nv++] = i;
+  L->weights[ns] = p->cost_wy;
+  L->weights[ns + 1] = p->cost_wxy;
+  L->values[ns] = p->half_width;
+  L->values[ns + 1] = 0.0;
+  double sw = 0.0;
+  for (int i = 0; i < ns; i++) {
+    L->weights[i] = L->w[i];
+    L->values[i] = L->v[i];
+    L->group_weights[L->grp[i]] += L->w[i];
+    if (isnan(L->values[i]) || isnan(L->weights[i])) {
+      L->weights[i] = 0.0;
+      L->values[i] = 0.0;
+    }
+    sw += L->weights[i];
+  }
+  L->pure_weight = sw;
+  sw += L->weights[ns] + L->weights[ns + 1];
+  if (sw != 0.0) {
+    sw = 1.0 / sw;
+    for (int i = 0; i < npt; i++) L->weights[i] *= sw;
+  }
+  if (L->pure_weight > 0.0)
+    for (int i = 0; i < L->ngroups; i++) L->group_weights[i] /= L->pure_weight;
+  L->pure_weight *= sw;
+  int imx = 0;
+  for (int i = 1; i < ns; i++)
+    if (L->values[i] > L->values[imx]) imx = i;
+  for (int i = 0; i < L->ngroups; i++) L->all_pars[4 + i] = L->values[imx];
+  double vec[LMA_NPAR];
+  for (int k = 0; k < L->nv; k++) vec[k] = L->all_pars[L->par_idx[k]];
+  /* runLma (477-530) with lmaStep (534-637) */
+  const int nv = L->nv;
+  static double fx[LMA_MAX_SAMPLES + 2], jt[LMA_NPAR * (LMA_MAX_SAMPLES + 2)];
+  static double fx1[LMA_MAX_SAMPLES + 2], jt1[LMA_NPAR * (LMA_MAX_SAMPLES + 2)];
+  lma_fx_jt(L, vec, fx, jt);
+  double last_rms = lma_rms(L, fx, NULL);
+  const double initial_rms = last_rms;
+  double lambda = p->lambda_initial;
+  int success = 0, done = 0;
+  for (int iter = 0; iter < p->num_iter; iter++) {
+    double A[LMA_NPAR * LMA_NPAR], b[LMA_NPAR];
+    for (int i = 0; i < nv; i++) {
+      for (int j = i; j < nv; j++) {
+        double d = 0.0;
+        for (int k = 0; k < npt; k++) d += L->weights[k] * jt[i * npt + k] * jt[j * npt + k];
+        A[i * nv + j] = d;
+        if (i == j) A[i * nv + j] += d * lambda;
+        else A[j * nv + i] = d;
+      }
+      double d = 0.0;
+      for (int k = 0; k < npt; k++) d += jt[i * npt + k] * fx[k];
+      b[i] = d;
+    }
+    if (!lma_solve(A, b, nv)) { /* singular: {false, true} */
+      success = 0;
+      done = 1;
+      break;
+    }
+    double nvec[LMA_NPAR];
+    for (int i = 0; i < nv; i++) nvec[i] = vec[i] + b[i];
+    lma_fx_jt(L, nvec, fx1, jt1);
+    const double rms = lma_rms(L, fx1, NULL);
+    if (rms < last_rms) {
+      success = 1;
+      done = rms >= last_rms * (1.0 - p->rms_diff);
+      last_rms = rms;
+      memcpy(vec, nvec, sizeof(vec));
+      memcpy(fx, fx1, sizeof(double) * npt);
+      memcpy(jt, jt1, sizeof(double) * nv * npt);
+    } else {
+      success = 0;
+      done = 0;
+    }
+    if (done) break;
+    if (success) lambda *= p->lambda_scale_good;
+    else {
+      lambda *= p->lambda_scale_bad;
+      if (lambda > p->lambda_max) break;
+    }
+  }
+  if (!success && last_rms < initial_rms) success = 1;
+  (void)done;
+  if (!success) return 0;
+  for (int k = 0; k < nv; k++) L->all_pars[L->par_idx[k]] = vec[k];
+  /* getDisparityStrength (149-163) */
+  double sum_amp = 0.0, max_amp = 0.0;
+  for (int i = 0; i < L->ngroups; i++) sum_amp += L->group_weights[i] * L->all_pars[4 + i];
+  for (int i = 0; i < ns; i++)
+    if (L->v[i] > max_amp) max_amp = L->v[i];
+  if (sum_amp > 1.25 * max_amp) sum_amp = max_amp;
+  out[0] = -L->all_pars[0];
+  out[1] = sum_amp;
+  out[2] = L->all_pars[1];
+  out[3] = L->all_pars[3];
+  return 1;
+}

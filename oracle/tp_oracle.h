@@ -198,6 +198,39 @@ void or_rig_tile(const double *clt_main, int s_main, const double *clt_aux, int 
                  const or_corr_params *cp, double cm_max_normalization, int no_int_x0, double *corr225,
                  double rec[4]);
 
+/* ---- LMA disparity ("POLY"): Correlation2d.corrLMA (Correlation2d.java:1754-1877) ----
+ * Defaults from ImageDttParameters.java:32-109. */
+typedef struct {
+  double min_poly_strength;  /* 0.2: LMA only where the integer-max strength exceeds it */
+  int mix_corr_poly;         /* 1: the LMA result replaces the CM disparity and strength */
+  double ortho_vasw_pwr;     /* 2.0: sample weight x |value|^pwr */
+  int cnvx_hwnd_size;        /* 4 */
+  double cnvx_weight;        /* 0.5: weight of selected non-convex cells */
+  int cnvx_add3x3;           /* 1 */
+  int adjust_wm, adjust_wy, adjust_wxy, adjust_ag; /* 1, 0, 1, 1 */
+  double half_width, cost_wy, cost_wxy;            /* 2.0, 0.1, 0.1 */
+  double lambda_initial, lambda_scale_good, lambda_scale_bad, lambda_max, rms_diff; /* 0.1, 0.5, 8, 100, 0.001 */
+  int num_iter;              /* 20 */
+  int pair_mask;             /* bit i: pair i takes part (dbg_pair_mask 0x3f) */
+} or_lma_params;
+void or_default_lma_params(or_lma_params *p);
+/* filterConvex (Correlation2d.java:2029-2208): weights [225] of the cells
+ * grown from (x0c, y0c) (offsets from the centre) through bi-convex cells */
+void or_filter_convex(const double *corr225, int hwin, int x0c, int y0c, int add3x3, double nc_cost,
+                      double *weights225);
+/*
+ * One tile: corrs [np][225] with quad pair kinds (0 horizontal, 1 vertical,
+ * 2 main diagonal, 3 other diagonal; others ignored), xcenter = the CM x of
+ * the combined strip (= -CM disparity).  Groups ortho / diagonal are combined
+ * (combineCompatiblePairs 462-490), sampled (addSamples 2230-2386) and fitted
+ * (Correlations2dLMA initVector / runLma, 211-640).  Returns 1 when the LMA
+ * succeeded, with out = {disparity, strength, half-width WM, WXY}
+ * (getDisparityStrengthWidth); 0 otherwise (out NaN).  n_samples (optional)
+ * receives the sample count.
+ */
+int or_corr_lma(const double *corrs, const int *kind, int np, double xcenter, const or_lma_params *p,
+                double out[4], int *n_samples);
+
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {
   double min_shot, scale_shot;        /* CLTParameters 10.0, 3.0 */

@@ -1,0 +1,91 @@
+"""LMA disparity (Correlation2d.corrLMA, the reference's default "POLY" disparity) on the GPU
+against the FP64 oracle restatement (needs a GB300).
+
+The oracle is fed the GPU's own correlation surfaces and CM disparity, so the check isolates the
+LMA stage: group combination, convex-cell selection, samples and the Levenberg-Marquardt fit.
+The device fit runs in FP32 and the oracle in FP64: success flags agree on >= 98% of the tiles and
+disparity / strength agree to 0.005 px / 1e-3 relative on >= 98% of the tiles both fitted.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_gpu
+from tileproc import synth
+
+pytestmark = pytest.mark.gpu
+
+KINDS = [0, 0, 1, 1, 2, 3]  # the quad PAIRS[0..5]
+
+
+def _compare(oracle, corr, disp, lma, min_frac=0.98):
+    p = oracle.default_lma_params()
+    n = agree = both = close = 0
+    errs = []
+    for t in range(disp.shape[0]):
+        cm, st = disp[t, oracle.DISP_CM], disp[t, oracle.DISP_STRENGTH]
+        if not np.isfinite(cm) or not st > p.min_poly_strength:
+            assert np.all(np.isnan(lma[t])), "tile %d: LMA ran where the reference does not" % t
+            continue
+        ok, out, ns = oracle.corr_lma(corr[t].astype(np.float64), KINDS, -float(cm), p)
+        n += 1
+        gok = bool(np.isfinite(lma[t, 0]))
+        agree += (gok == ok)
+        if ok and gok:
+            both += 1
+            e = abs(lma[t, 0] - out[0])
+            errs.append(e)
+            close += (e <= 0.005) and abs(lma[t, 1] - out[1]) <= 1e-3 * abs(out[1]) + 1e-6
+    assert n > 20
+    assert agree >= min_frac * n, "success flags agree on %d of %d" % (agree, n)
+    assert close >= min_frac * both, "disparity/strength agree on %d of %d (max err %.3g)" % (close, both, max(errs))
+    return np.array(errs)
+
+
+@pytest.mark.parametrize("kind,size", [("quad_mono", (128, 96)), ("quad_bayer", (128, 96))])
+def test_lma_matches_oracle(oracle, kind, size):
+    sc = synth.make_scene(kind, seed=41, width=size[0], height=size[1])
+    T = (size[0] // 8) * (size[1] // 8)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        corr, disp = tp.getCorr(), tp.getDisparity()
+        lma = tp.lmaRefine(mix_corr_poly=0)
+        assert np.array_equal(tp.getDisparity(), disp, equal_nan=True), "mix_corr_poly=0 changed the record"
+        errs = _compare(oracle, corr, disp, lma)
+        print("%s: LMA |gpu - oracle| median %.2g max %.2g px over %d tiles" % (kind, np.median(errs), errs.max(),
+                                                                              len(errs)))
+
+
+def test_lma_mix_replaces_cm_and_needs_a_new_forward(oracle):
+    from tileproc import _lib
+    sc = synth.make_scene("quad_mono", seed=42, width=128, height=96)
+    T = 16 * 12
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        d0 = tp.getDisparity()
+        lma = tp.lmaRefine()
+        d1 = tp.getDisparity()
+        fit = np.isfinite(lma[:, 0])
+        assert fit.sum() > 20
+        assert np.array_equal(d1[fit, oracle.DISP_CM], lma[fit, 0])
+        assert np.array_equal(d1[fit, oracle.DISP_STRENGTH], lma[fit, 1])
+        assert np.array_equal(d1[~fit], d0[~fit], equal_nan=True)
+        with pytest.raises(_lib.TpError, match="run tp_process"):
+            tp.lmaRefine()
+        tp.process()
+        assert np.array_equal(tp.getDisparity(), d0, equal_nan=True)
+        tp.lmaRefine()
+
+
+def test_lma_rejects_general_pairs(oracle):
+    from tileproc import _lib
+    sc = synth.make_scene("circle_lwir", seed=43, width=64, height=64)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation(pairs=synth.circle_pairs(sc["geometry"]))
+        tp.setFullFrameImages(np.full(64, 2.0, np.float32))
+        tp.process()
+        with pytest.raises(_lib.TpError, match="quad kinds"):
+            tp.lmaRefine()
