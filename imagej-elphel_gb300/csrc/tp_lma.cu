@@ -28,13 +28,22 @@ constexpr int LMA_DIAG_ENTRIES = 145;  // addSamples enumeration, diagonal group
 constexpr int LMA_MAX_SAMPLES = 162;   // 9x9 window cells per group
 constexpr int LMA_NP = 6;              // X0, WM, WYD, WXY, AG0, AG1
 
-// sample cell offsets from the (integer) centre, in the reference's enumeration order
-__constant__ signed char k_lma_cx[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
-__constant__ signed char k_lma_cy[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+// sample cell offsets from the (integer) centre, in the reference's enumeration order (global
+// memory: consecutive lanes read consecutive entries)
+__device__ signed char g_lma_cx[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+__device__ signed char g_lma_cy[LMA_ORTHO_ENTRIES + LMA_DIAG_ENTRIES];
+
+__device__ __forceinline__ void cp_async4(float *dst_smem, const float *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(float *dst_smem, const float *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
 
 // per-warp shared memory (floats)
 constexpr int LMA_PER_WARP = 2 * 225             // group surfaces
-                             + 3 * 2 * 225 / 4   // convex / sel / sel_new flags (bytes)
                              + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 8  // samples
                              + 28 * 33 + 64;     // reduction buffer, accepted / trial normal equations
 
@@ -47,17 +56,14 @@ struct LmaDev {
   int kinds[TP_MAXP];  // pair kind or -1 when the pair does not take part
 };
 
-__device__ __forceinline__ float lma_weight(const unsigned char *conv, const unsigned char *sel, int idx, int x0,
-                                            int y0, const TpLmaConst &c) {
-  if (sel[idx]) return conv[idx] ? 1.0f : c.cnvx_weight;
-  if (c.cnvx_add3x3) {
-    const int row = idx / 15, col = idx - row * 15;
-    if (row >= y0 - 1 && row <= y0 + 1 && col >= x0 - 1 && col <= x0 + 1) return c.cnvx_weight;
-  }
-  return 0.0f;
+// bits a..b (inclusive) of a row mask, none when b < a
+__device__ __forceinline__ unsigned bit_range(int a, int b) {
+  return (b < a) ? 0u : (((2u << b) - 1u) & ~((1u << a) - 1u));
 }
 
 constexpr int LMA_NEQ = 28;  // packed normal equations: A (upper 6x6, 21), b (6), weighted rms^2
+// floats from the sample arrays to the end of the reduction buffer, free before the samples exist
+constexpr int LMA_STAGE = 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1 + 28 * 33;
 
 // Weighted normal equations of the samples at parameters av (getFxJt, getWJtJlambda, getWYmFxRms),
 // written to out[LMA_NEQ] for every lane: per-lane partial sums are transposed through red
@@ -124,9 +130,7 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
   extern __shared__ float sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *gsurf = sm + warp * LMA_PER_WARP;                      // [2][225]
-  unsigned char *conv = (unsigned char *)(gsurf + 450);          // [2][225]
-  unsigned char *sel = conv + 450, *seln = sel + 450;            // [2][225]
-  float *sx = gsurf + 450 + 3 * 450 / 4 + 2;                    // samples
+  float *sx = gsurf + 450;                                      // samples
   float *sy = sx + LMA_MAX_SAMPLES, *sv = sy + LMA_MAX_SAMPLES, *sw = sv + LMA_MAX_SAMPLES;
   unsigned char *sg = (unsigned char *)(sw + LMA_MAX_SAMPLES);
   float *red = sx + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1;  // [LMA_NEQ][33] transposed partial sums
@@ -148,80 +152,114 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
       np_ortho += (ld.kinds[pi] == 0 || ld.kinds[pi] == 1);
       np_diag += (ld.kinds[pi] == 2 || ld.kinds[pi] == 3);
     }
-    for (int e = lane; e < 450; e += 32) {
-      const int gd = e >= 225, i = e - 225 * gd, r = i / 15, q = i - r * 15;
-      float v = 0.f;
-      for (int pi = 0; pi < ld.P; pi++) {
-        const int k = ld.kinds[pi];
-        if (k < 0 || (k >= 2) != gd) continue;
-        const float *cs = ld.corr + (tile * ld.P + pi) * TP_CORR;
-        v += (k == 1) ? cs[q * 15 + r] : ((k == 3) ? cs[(14 - r) * 15 + q] : cs[i]);
+    // The tile's surfaces are contiguous (P x 900 bytes): when they fit they are copied
+    // asynchronously into the (still unused) sample and reduction region, all in flight at once,
+    // in 8-byte pieces when P is even (the tile's offset is then a multiple of 8 bytes).
+    const float *src = ld.corr + tile * ld.P * TP_CORR;
+    if (ld.P * TP_CORR <= LMA_STAGE) {
+      if ((ld.P & 1) == 0) {
+        for (int k = lane; k < ld.P * TP_CORR / 2; k += 32) cp_async8(sx + 2 * k, src + 2 * k);
+      } else {
+        for (int k = lane; k < ld.P * TP_CORR; k += 32) cp_async4(sx + k, src + k);
       }
-      const int npg = gd ? np_diag : np_ortho;
-      gsurf[e] = (npg > 1) ? v / npg : v;
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncwarp();
+      src = sx;
+    }
+    // group sums, pairs in index order (combineCompatiblePairs), 8 cells per lane in registers
+    float go[8], gdg[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) go[t] = gdg[t] = 0.f;
+    for (int pi = 0; pi < ld.P; pi++) {
+      const int k = ld.kinds[pi];
+      if (k < 0) continue;
+      const float *cs = src + pi * TP_CORR;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int i = lane + 32 * t;
+        if (i < 225) {
+          const int r = i / 15, q = i - r * 15;
+          const float v = (k == 1) ? cs[q * 15 + r] : ((k == 3) ? cs[(14 - r) * 15 + q] : cs[i]);
+          if (k >= 2) gdg[t] += v;
+          else go[t] += v;
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int i = lane + 32 * t;
+      if (i < 225) {
+        gsurf[i] = (np_ortho > 1) ? go[t] / np_ortho : go[t];
+        gsurf[225 + i] = (np_diag > 1) ? gdg[t] / np_diag : gdg[t];
+      }
     }
     __syncwarp();
-    // ---- filterConvex per group ----
-    for (int gd = 0; gd < 2; gd++) {
-      const int x0 = ixc + 7, y0 = (gd ? ixc : 0) + 7;
-      const int min_row = max(y0 - hw, 0), max_row = min(y0 + hw, 14);
-      const int min_col = max(x0 - hw, 0), max_col = min(x0 + hw, 14);
-      const float *d = gsurf + 225 * gd;
-      unsigned char *cv = conv + 225 * gd, *sl = sel + 225 * gd, *sn = seln + 225 * gd;
-      for (int i = lane; i < 225; i += 32) {
-        const int row = i / 15, col = i - row * 15;
-        bool cx = false;
-        if (row > min_row && row < max_row && col > min_col && col < max_col)
-          cx = (2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - 15] + d[i + 15]));
-        cv[i] = cx;
-        sl[i] = (i == y0 * 15 + x0) && y0 >= min_row && y0 <= max_row && x0 >= min_col && x0 <= max_col;
-      }
-      __syncwarp();
-      if ((gd ? np_diag : np_ortho) == 0) continue;
+    // ---- filterConvex, both groups at once: lanes 0-14 hold the ortho rows, lanes 16-30 the
+    // diagonal rows, as 15-bit masks (bit = column) of the convex and the selected cells ----
+    const int half = lane >> 4, r = lane & 15, hbase = half << 4;
+    const bool rowlane = r < 15 && (half ? np_diag : np_ortho) > 0;
+    const int x0 = ixc + 7, y0 = (half ? ixc : 0) + 7;
+    const int min_row = max(y0 - hw, 0), max_row = min(y0 + hw, 14);
+    const int min_col = max(x0 - hw, 0), max_col = min(x0 + hw, 14);
+    unsigned conv = 0, sel = 0;
+    if (rowlane) {
+      const float *d = gsurf + 225 * half;
+      if (r > min_row && r < max_row)
+        for (int col = min_col + 1; col < max_col; col++) {
+          const int i = r * 15 + col;
+          if ((2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - 15] + d[i + 15]))) conv |= 1u << col;
+        }
+      if (r == y0 && x0 >= min_col && x0 <= max_col) sel = 1u << x0;
+    }
+    {
+      const unsigned lmask = bit_range(min_col + 1, x0), rmask = bit_range(x0, max_col - 1);
+      const unsigned hmask = 0xffffu << hbase;
+      bool active = rowlane;
       for (int istep = 0; istep < hw; istep++) {
-        for (int i = lane; i < 225; i += 32) sn[i] = sl[i];
-        __syncwarp();
         const bool first = istep == 0;
         const int smin_row = max(y0 - istep, 0), smax_row = min(y0 + istep, 14);
-        const int smin_col = max(x0 - istep, 0), smax_col = min(x0 + istep, 14);
-        const int ncol = smax_col - smin_col + 1, nrow = smax_row - smin_row + 1;
-        // items: up / down along the columns, left / right along the rows (all read sel, set sel_new)
-        for (int it = lane; it < 2 * ncol + 2 * nrow; it += 32) {
-          int dir, pos;
-          if (it < ncol) { dir = 0; pos = smin_col + it; }
-          else if (it < 2 * ncol) { dir = 1; pos = smin_col + it - ncol; }
-          else if (it < 2 * ncol + nrow) { dir = 2; pos = smin_row + it - 2 * ncol; }
-          else { dir = 3; pos = smin_row + it - 2 * ncol - nrow; }
-          if (dir == 0 && !(istep < y0)) continue;
-          if (dir == 1 && !((y0 + istep) < max_row)) continue;
-          if (dir == 2 && !(istep < x0)) continue;
-          if (dir == 3 && !((x0 + istep) < max_col)) continue;
-          const int row = (dir == 0) ? y0 - istep : (dir == 1 ? y0 + istep : pos);
-          const int col = (dir == 2) ? x0 - istep : (dir == 3 ? x0 + istep : pos);
-          const int i = row * 15 + col;
-          if (!(sl[i] && (cv[i] || first))) continue;
-          const int step = (dir == 0) ? -15 : (dir == 1 ? 15 : (dir == 2 ? -1 : 1));
-          const int j = i + step;
-          sn[j] = 1;
-          if (cv[j]) {
-            if (dir <= 1) {
-              if (col <= x0 && col > min_col) sn[j - 1] = 1;
-              if (col >= x0 && col < max_col) sn[j + 1] = 1;
-            } else {
-              if (row <= y0 && row > min_row) sn[j - 15] = 1;
-              if (row >= y0 && row < max_row) sn[j + 15] = 1;
+        const unsigned cols = bit_range(max(x0 - istep, 0), min(x0 + istep, 14));
+        unsigned seln = sel;
+        // up / down: the source row's selected cells (convex, or the start) grow into the next row
+        const unsigned src = sel & cols & (first ? 0x7fffu : conv);
+        const bool up_ok = istep < y0, down_ok = (y0 + istep) < max_row;
+        const unsigned s_up = __shfl_sync(0xffffffffu, src, hbase + max(y0 - istep, 0));
+        const unsigned s_dn = __shfl_sync(0xffffffffu, src, hbase + min(y0 + istep, 14));
+        if (up_ok && r == y0 - istep - 1) {
+          const unsigned c1 = s_up & conv;
+          seln |= s_up | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
+        }
+        if (down_ok && r == y0 + istep + 1) {
+          const unsigned c1 = s_dn & conv;
+          seln |= s_dn | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
+        }
+        // left / right: the source column's cells grow sideways, and from a convex target up or
+        // down towards the centre row's side
+        unsigned push_up = 0, push_dn = 0;
+        const bool in_rows = r >= smin_row && r <= smax_row;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+          const int col = side ? x0 + istep : x0 - istep;
+          const bool ok = side ? ((x0 + istep) < max_col) : (istep < x0);
+          if (!ok || !in_rows || col < 0 || col > 14) continue;
+          const unsigned cb = 1u << col, tb = side ? (cb << 1) : (cb >> 1);
+          if ((sel & cb) && (first || (conv & cb))) {
+            seln |= tb;
+            if (conv & tb) {
+              if (r <= y0 && r > min_row) push_up |= tb;
+              if (r >= y0 && r < max_row) push_dn |= tb;
             }
           }
         }
-        __syncwarp();
-        bool changed = false;
-        for (int i = lane; i < 225; i += 32) changed |= (sn[i] != sl[i]);
-        if (!__any_sync(0xffffffffu, changed)) break;
-        for (int i = lane; i < 225; i += 32) sl[i] = sn[i];
-        __syncwarp();
+        seln |= __shfl_down_sync(0xffffffffu, push_up, 1) | __shfl_up_sync(0xffffffffu, push_dn, 1);
+        if (!rowlane) seln = 0;
+        const unsigned changed = __ballot_sync(0xffffffffu, active && seln != sel) & hmask;
+        if (!changed) active = false;
+        if (active) sel = seln;
+        if (!__any_sync(0xffffffffu, active)) break;
       }
     }
-    __syncwarp();
     // ---- samples (addSamples), compacted in the enumeration order ----
     int ns = 0, ngroups = 0, gdiag_bits = 0;
     for (int gd = 0; gd < 2; gd++) {
@@ -233,12 +271,24 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
       for (int e0 = 0; e0 < cnt; e0 += 32) {
         const int e = e0 + lane;
         float w = 0.f, v = 0.f, x = 0.f, y = 0.f;
+        int cxo = 99, cyo = 99;
         if (e < cnt) {
-          const int cxo = k_lma_cx[base + e], cyo = k_lma_cy[base + e];
-          const int cx = cxo + ixc, cy = cyo + (gd ? ixc : 0);
-          if (cx >= -7 && cx <= 7 && cy >= -7 && cy <= 7) {
-            const int idx = 112 + 15 * cy + cx;
-            w = lma_weight(conv + 225 * gd, sel + 225 * gd, idx, ixc + 7, (gd ? ixc : 0) + 7, c) * npg;
+          cxo = __ldg(&g_lma_cx[base + e]);
+          cyo = __ldg(&g_lma_cy[base + e]);
+        }
+        const int cx = cxo + ixc, cy = cyo + (gd ? ixc : 0);
+        const bool inside = e < cnt && cx >= -7 && cx <= 7 && cy >= -7 && cy <= 7;
+        const int srow = inside ? cy + 7 : 0;
+        const unsigned rsel = __shfl_sync(0xffffffffu, sel, (gd << 4) + srow);
+        const unsigned rconv = __shfl_sync(0xffffffffu, conv, (gd << 4) + srow);
+        if (inside) {
+          {
+            const int idx = 112 + 15 * cy + cx, ccol = cx + 7, gy0 = (gd ? ixc : 0) + 7;
+            float wc = 0.f;
+            if ((rsel >> ccol) & 1) wc = ((rconv >> ccol) & 1) ? 1.0f : c.cnvx_weight;
+            else if (c.cnvx_add3x3 && srow >= gy0 - 1 && srow <= gy0 + 1 && ccol >= ixc + 6 && ccol <= ixc + 8)
+              wc = c.cnvx_weight;
+            w = wc * npg;
             if (w > 0.f) {
               v = d[idx];
               if (c.ortho_vasw_pwr == 2.0f) w *= v * v;
@@ -306,62 +356,61 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
     float lambda = c.lambda_initial;
     bool success = false;
     for (int iter = 0; iter < c.num_iter; iter++) {
-      // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held
-      float M[LMA_NP][LMA_NP + 1];
+      // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held (identity rows).
+      // The matrix is symmetric positive (semi)definite: LDL^T without pivoting; a pivot that is
+      // not positive marks it singular, as the zero pivot of the reference's LU inverse does.
+      float M[LMA_NP][LMA_NP], rhs[LMA_NP];
       {
         int k = 0;
 #pragma unroll
         for (int a = 0; a < LMA_NP; a++)
 #pragma unroll
           for (int cc = a; cc < LMA_NP; cc++) {
-            const float v = acc[k++];
+            const bool keep = mask[a] && mask[cc];
+            const float v = keep ? acc[k] : ((a == cc) ? 1.0f : 0.0f);
             M[a][cc] = v;
             M[cc][a] = v;
+            k++;
           }
       }
 #pragma unroll
       for (int a = 0; a < LMA_NP; a++) {
-        M[a][a] += M[a][a] * lambda;
-        M[a][LMA_NP] = acc[21 + a];
-        if (!mask[a]) {
-#pragma unroll
-          for (int cc = 0; cc <= LMA_NP; cc++) M[a][cc] = (cc == a) ? 1.0f : 0.0f;
-#pragma unroll
-          for (int r = 0; r < LMA_NP; r++)
-            if (r != a) M[r][a] = 0.0f;
-        }
+        if (mask[a]) M[a][a] += M[a][a] * lambda;
+        rhs[a] = mask[a] ? acc[21 + a] : 0.0f;
       }
+      float Lm[LMA_NP][LMA_NP], Dd[LMA_NP], Dinv[LMA_NP];
       bool singular = false;
 #pragma unroll
-      for (int col = 0; col < LMA_NP; col++) {
-        // partial pivoting by compare-and-swap (static indices keep M in registers)
+      for (int r = 0; r < LMA_NP; r++) {
 #pragma unroll
-        for (int r = col + 1; r < LMA_NP; r++) {
-          const bool sw = fabsf(M[r][col]) > fabsf(M[col][col]);
+        for (int cc = 0; cc < r; cc++) {
+          float t = M[r][cc];
 #pragma unroll
-          for (int cc = 0; cc <= LMA_NP; cc++) {
-            const float t = M[col][cc];
-            M[col][cc] = sw ? M[r][cc] : t;
-            M[r][cc] = sw ? t : M[r][cc];
-          }
+          for (int k = 0; k < cc; k++) t -= Lm[r][k] * Lm[cc][k] * Dd[k];
+          Lm[r][cc] = t * Dinv[cc];
         }
-        if (M[col][col] == 0.0f) singular = true;
-        const float pinv = (M[col][col] != 0.0f) ? 1.0f / M[col][col] : 0.0f;
+        float dd = M[r][r];
 #pragma unroll
-        for (int r = col + 1; r < LMA_NP; r++) {
-          const float f = M[r][col] * pinv;
-#pragma unroll
-          for (int cc = col; cc <= LMA_NP; cc++) M[r][cc] -= f * M[col][cc];
-        }
+        for (int k = 0; k < r; k++) dd -= Lm[r][k] * Lm[r][k] * Dd[k];
+        if (!(dd > 0.0f)) singular = true;
+        Dd[r] = dd;
+        Dinv[r] = (dd > 0.0f) ? 1.0f / dd : 0.0f;
       }
       if (singular) break;
       float delta[LMA_NP];
 #pragma unroll
-      for (int r = LMA_NP - 1; r >= 0; r--) {
-        float s = M[r][LMA_NP];
+      for (int r = 0; r < LMA_NP; r++) {
+        float t = rhs[r];
 #pragma unroll
-        for (int k = r + 1; k < LMA_NP; k++) s -= M[r][k] * delta[k];
-        delta[r] = s / M[r][r];
+        for (int k = 0; k < r; k++) t -= Lm[r][k] * delta[k];
+        delta[r] = t;
+      }
+#pragma unroll
+      for (int r = LMA_NP - 1; r >= 0; r--) {
+        float t = delta[r] * Dinv[r];
+#pragma unroll
+        for (int k = r + 1; k < LMA_NP; k++) t -= Lm[k][r] * delta[k];
+        delta[r] = t;
       }
       float nav[LMA_NP];
 #pragma unroll
@@ -427,8 +476,8 @@ cudaError_t upload_lma_constants() {
         }
     if (n - start != (diag ? LMA_DIAG_ENTRIES : LMA_ORTHO_ENTRIES)) return cudaErrorInvalidValue;
   }
-  cudaError_t e = cudaMemcpyToSymbol(k_lma_cx, cx, sizeof(cx));
-  if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_lma_cy, cy, sizeof(cy));
+  cudaError_t e = cudaMemcpyToSymbol(g_lma_cx, cx, sizeof(cx));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_lma_cy, cy, sizeof(cy));
   return e;
 }
 
