@@ -81,6 +81,39 @@ __device__ __forceinline__ void rotate(float o[4][8], float rx, float ry, int r)
   }
 }
 
+// transpose of rotate (both turns are orthogonal: undone in reverse order)
+__device__ __forceinline__ void rotate_t(float o[4][8], float rx, float ry, int r) {
+  float ch, shh, cvr, svr;
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * rx, &shh, &ch);
+  __sincosf(CUDART_PI_F * 0.0625f * (2 * r + 1) * ry, &svr, &cvr);
+  const int base = threadIdx.x & 24;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float cv = __shfl_sync(0xffffffffu, cvr, base + v), sv = __shfl_sync(0xffffffffu, svr, base + v);
+    const float t0 = o[0][v] * cv + o[2][v] * sv, t2 = o[2][v] * cv - o[0][v] * sv;
+    const float t1 = o[1][v] * cv + o[3][v] * sv, t3 = o[3][v] * cv - o[1][v] * sv;
+    o[0][v] = t0 * ch + t1 * shh;
+    o[1][v] = t1 * ch - t0 * shh;
+    o[2][v] = t2 * ch + t3 * shh;
+    o[3][v] = t3 * ch - t2 * shh;
+  }
+}
+
+// transpose of convolve (the per-frequency 4x4 sign matrix of the kernel, transposed)
+__device__ __forceinline__ void convolve_t(float o[4][8], const float *kp, int r) {
+  if (!kp) return;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float k0 = __ldg(kp + r * 8 + v), k1 = __ldg(kp + 64 + r * 8 + v), k2 = __ldg(kp + 128 + r * 8 + v),
+                k3 = __ldg(kp + 192 + r * 8 + v);
+    const float g0 = o[0][v], g1 = o[1][v], g2 = o[2][v], g3 = o[3][v];
+    o[0][v] = k0 * g0 + k1 * g1 + k2 * g2 + k3 * g3;
+    o[1][v] = -k1 * g0 + k0 * g1 - k3 * g2 + k2 * g3;
+    o[2][v] = -k2 * g0 - k3 * g1 + k0 * g2 + k1 * g3;
+    o[3][v] = k3 * g0 - k2 * g1 - k1 * g2 + k0 * g3;
+  }
+}
+
 __device__ __forceinline__ Win make_win(const SceneDev &sc, const SubtilePlan &p, int s) {
   Win w;
   w.img = sc.images[s];
@@ -447,37 +480,72 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
       __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
       const FoldIdx fv = fold_idx(r);
       const float *cl = s_clt + sidx * TP_CLT + r * 8, *gl = s_g + sidx * TP_CLT + r * 8;
-      float gdir[2];
+      // the rotation's own derivative (pi/16 (2k+1) x the CLT turned by 90 degrees) dotted with dd/dCLT
+      float gdir[2] = {0.f, 0.f};
+#pragma unroll
+      for (int v = 0; v < 8; v++) {
+        const float c0 = cl[v], c1 = cl[64 + v], c2 = cl[128 + v], c3 = cl[192 + v];
+        const float g0 = gl[v], g1 = gl[64 + v], g2 = gl[128 + v], g3 = gl[192 + v];
+        const float fx = K16 * (2 * r + 1), fy = K16 * (2 * v + 1);
+        gdir[0] = fmaf(fx, (g1 * c0 - g0 * c1) + (g3 * c2 - g2 * c3), gdir[0]);
+        gdir[1] = fmaf(fy, (g2 * c0 - g0 * c2) + (g3 * c1 - g1 * c3), gdir[1]);
+      }
+      // dd/dCLT taken back once through the phase rotation, the kernel convolution and the 2D
+      // DCT-IV/DST-IV (symmetric transforms: the transpose runs through the same butterflies) to
+      // the folded tile, written over this lane's own dd/dCLT slots: gfs[m * 64 + j] for folded row r
+      float *gfs = s_g + sidx * TP_CLT + r * 8;
+      {
+        float gf[4][8];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+          for (int v = 0; v < 8; v++) gf[m][v] = gl[m * 64 + v];
+        rotate_t(gf, p.rx, p.ry, r);
+        convolve_t(gf, kp, r);
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          float u[8];
+          dtt4_fast(gf[m], u, (m >> 1) & 1);
+          group_transpose(u, tb + q * 72, r);
+          dtt4_fast(u, gf[m], m & 1);
+        }
+        if (s < S) {
+#pragma unroll
+          for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int j2 = 0; j2 < 8; j2++) gfs[m * 64 + j2] = gf[m][j2];
+        }
+      }
+      __syncwarp();
+      // per direction: the fold with the derivative window dotted with the folded gradient
 #pragma unroll
       for (int dir = 0; dir < 2; dir++) {
-        float vw0, vw1, hw0[8], hw1[8], o[4][8];
+        float vw0, vw1, hw0[8], hw1[8];
         if (dir == 0) fold_weights(-K16 * ahs, K16 * ahc, avc, avs, fv, vw0, vw1, hw0, hw1);
         else fold_weights(ahc, ahs, -K16 * avs, K16 * avc, fv, vw0, vw1, hw0, hw1);
-        fold_dtt_dense(w, fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
-        convolve(o, kp, r);
-        rotate(o, p.rx, p.ry, r);
         float acc = 0.f;
 #pragma unroll
-        for (int v = 0; v < 8; v++) {
-          // the rotation's own derivative: pi/16 (2k+1) x the CLT turned by 90 degrees
-          const float c0 = cl[v], c1 = cl[64 + v], c2 = cl[128 + v], c3 = cl[192 + v];
-          float t0, t1, t2, t3;
-          if (dir == 0) {
-            const float f = K16 * (2 * r + 1);
-            t0 = o[0][v] - f * c1; t1 = o[1][v] + f * c0; t2 = o[2][v] - f * c3; t3 = o[3][v] + f * c2;
-          } else {
-            const float f = K16 * (2 * v + 1);
-            t0 = o[0][v] - f * c2; t1 = o[1][v] - f * c3; t2 = o[2][v] + f * c0; t3 = o[3][v] + f * c1;
-          }
-          acc = fmaf(gl[v], t0, acc);
-          acc = fmaf(gl[64 + v], t1, acc);
-          acc = fmaf(gl[128 + v], t2, acc);
-          acc = fmaf(gl[192 + v], t3, acc);
+        for (int vb = 0; vb < 2; vb++) {
+          const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
+          float vc[16];
+#pragma unroll
+          for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+#pragma unroll
+          for (int hb = 0; hb < 2; hb++)
+#pragma unroll
+            for (int j2 = 0; j2 < 8; j2++) {
+              const FoldIdx fh = fold_idx(j2);
+              const float h0 = (hb ? fh.ss0 : fh.sc0) * hw0[j2], h1 = (hb ? fh.ss1 : fh.sc1) * hw1[j2];
+              acc = fmaf(fmaf(h1, vc[fh.src1], h0 * vc[fh.src0]), gfs[(vb * 2 + hb) * 64 + j2], acc);
+            }
         }
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-        gdir[dir] = acc;
+        gdir[dir] += acc;
+      }
+#pragma unroll
+      for (int dir = 0; dir < 2; dir++) {
+        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 1);
+        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 2);
+        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 4);
       }
       if (r == 0 && s < S) {
         // residual = TL - px: dd/dpx = -dd/drx; the kernel-centre offsets add the
@@ -500,46 +568,52 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
 
 // Per tile: Jacobian rows of d w.r.t. the sensors' (azimuth, tilt, roll, zoom)
 // and the tile disparity, and the loss gradient with dL/dd = dl_dd (or 2 d).
-// Per-block partial sums of the extrinsic gradient go to `partial`.
+// One thread per (task, sensor); a block holds 256 / S tasks.  The per-task sum
+// over sensors and the block's partial sums of the extrinsic gradient (to
+// `partial`) are taken in a fixed order, so the result is deterministic.
 __global__ void __launch_bounds__(256) adjoint_contract_kernel(const __grid_constant__ SceneDev sc,
                                                               const float *sens, const float *dval,
                                                               const float *dl_dd, float *jac_e, float *jac_d,
                                                               float *grad_d, float *partial) {
-  __shared__ float red[TP_MAXS * 4][8];
-  const int S = sc.num_sensors;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int task = blockIdx.x * blockDim.x + threadIdx.x;
-  float gbar = 0.f;
+  __shared__ float s_jd[256];
+  __shared__ float s_ge[256][4];
+  const int S = sc.num_sensors, tpb = 256 / S;
+  const int lt = threadIdx.x / S, s = threadIdx.x - lt * S;
+  const int task = blockIdx.x * tpb + lt;
+  const bool act = lt < tpb && task < sc.num_tasks;
+  float jd = 0.f, ge[4] = {0.f, 0.f, 0.f, 0.f};
   size_t tile = 0;
-  bool act = task < sc.num_tasks;
+  float gbar = 0.f;
   if (act) {
     const int txy = sc.task_txy[task];
     tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
     const float d = dval[tile];
     gbar = isnan(d) ? 0.f : (dl_dd ? dl_dd[tile] : 2.0f * d);
-    float jd = 0.f;
-    for (int s = 0; s < S; s++) {
-      const double *pd = sc.port_deriv + ((size_t)task * S + s) * 10;
-      const float jx = sens[(tile * S + s) * 2], jy = sens[(tile * S + s) * 2 + 1];
-      for (int k = 0; k < 4; k++) {
-        const float j = jx * (float)pd[k] + jy * (float)pd[5 + k];
-        jac_e[(tile * S + s) * 4 + k] = j;
-      }
-      jd += jx * (float)pd[4] + jy * (float)pd[9];
+    const double *pd = sc.port_deriv + ((size_t)task * S + s) * 10;
+    const float jx = sens[(tile * S + s) * 2], jy = sens[(tile * S + s) * 2 + 1];
+    float j4[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      j4[k] = jx * (float)pd[k] + jy * (float)pd[5 + k];
+      ge[k] = gbar * j4[k];
     }
-    jac_d[tile] = jd;
-    grad_d[tile] = gbar * jd;
+    *(float4 *)(jac_e + (tile * S + s) * 4) = make_float4(j4[0], j4[1], j4[2], j4[3]);
+    jd = jx * (float)pd[4] + jy * (float)pd[9];
   }
-  // block sums of gbar * jac_e over the block's tiles, one (sensor, parameter) at a time
-  for (int sk = 0; sk < S * 4; sk++) {
-    float v = act ? gbar * jac_e[(tile * S + sk / 4) * 4 + (sk & 3)] : 0.f;
-    v = warp_sum(v);
-    if (lane == 0) red[sk][warp] = v;
-  }
+  s_jd[threadIdx.x] = jd;
+#pragma unroll
+  for (int k = 0; k < 4; k++) s_ge[threadIdx.x][k] = ge[k];
   __syncthreads();
-  if (threadIdx.x < S * 4) {
+  if (act && s == 0) {  // sensors in order
+    float t = 0.f;
+    for (int q = 0; q < S; q++) t += s_jd[lt * S + q];
+    jac_d[tile] = t;
+    grad_d[tile] = gbar * t;
+  }
+  if (threadIdx.x < S * 4) {  // the block's tasks in order
+    const int ss = threadIdx.x >> 2, k = threadIdx.x & 3;
     float v = 0.f;
-    for (int w = 0; w < 8; w++) v += red[threadIdx.x][w];
+    for (int q = 0; q < tpb; q++) v += s_ge[q * S + ss][k];
     partial[(size_t)blockIdx.x * S * 4 + threadIdx.x] = v;
   }
 }
@@ -586,7 +660,7 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
   adjoint_kernel<<<grid, 32 * AD_NW, bytes, st>>>(sc, as, cc, sens, dval);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int nb = (sc.num_tasks + 255) / 256;
+  const int nb = (sc.num_tasks + 256 / sc.num_sensors - 1) / (256 / sc.num_sensors);
   adjoint_contract_kernel<<<nb, 256, 0, st>>>(sc, sens, dval, dl_dd, jac_e, jac_d, grad_d, partial);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -41,10 +41,11 @@ struct tp_handle {
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
   float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
-  // per-pair strip samples [tiles][pairs][RE], recorded by the forward once the adjoint is in use
+  // Once the adjoint is in use (adj_record) the forward keeps what it needs: per-pair strip
+  // samples [tiles][pairs][RE] and the plan's FP64 port derivatives
   float *d_strips = nullptr;
   size_t strips_cap = 0;
-  int record_strips = 0, strips_valid = 0;
+  int adj_record = 0, strips_valid = 0, deriv_valid = 0;
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
   float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
@@ -139,7 +140,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
   sc.corr_cfg = h->d_corr_cfg;
   sc.combo = h->d_combo;
-  sc.strips = (h->record_strips && h->d_strips && strips_need(h) <= h->strips_cap) ? h->d_strips : nullptr;
+  sc.strips = (h->adj_record && h->d_strips && strips_need(h) <= h->strips_cap) ? h->d_strips : nullptr;
   sc.tex = h->d_tex;
   sc.tex_aux = h->tex_params.aux ? h->d_tex_aux : nullptr;
   sc.num_pairs = h->num_pairs;
@@ -451,6 +452,7 @@ tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
   CK(cudaStreamSynchronize(h->stream), "tp_set_geometry");
   h->have_geometry = 1;
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
 }
@@ -473,6 +475,7 @@ tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const floa
   }
   CK(cudaMemcpy(h->d_kext[cam], offs, nk * 8 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
 }
@@ -513,6 +516,7 @@ tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_de
                               h->cfg.kernel_step, st),
        "tp_calc_kernels");
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
 }
@@ -589,6 +593,7 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
   h->ports_from_geometry = 0;
   h->have_tasks = 1;
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
 }
@@ -609,6 +614,7 @@ tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
   h->ports_from_geometry = 1;
   h->have_tasks = 1;
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
 }
@@ -721,15 +727,19 @@ static tp_status ensure_plan(tp_handle *h, cudaStream_t st) {
   if (h->ports_from_geometry && !h->have_geometry) return fail(h, TP_ERR_STATE, "geometry not set");
   if (h->planned) return TP_OK;
   SceneDev sc = scene_of(h);
+  const bool with_deriv = h->adj_record && h->d_port_deriv && h->ports_from_geometry;
+  if (with_deriv) sc.port_deriv = h->d_port_deriv;  // the adjoint's port derivatives, same ports
   CK(launch_plan(sc, st), "plan");
   CK(launch_tile_task_map(sc, st), "tile map");
   h->planned = 1;
+  h->deriv_valid = with_deriv ? 1 : 0;
   return TP_OK;
 }
 
 tp_status tp_ports(tp_handle *h, void *stream) {
   if (!h) return TP_ERR_ARG;
   h->planned = 0;
+  h->deriv_valid = 0;
   h->fwd_valid = 0;
   return ensure_plan(h, pick_stream(h, stream));
 }
@@ -1254,12 +1264,12 @@ static tp_status enable_strip_recording(tp_handle *h) {
     h->strips_valid = 0;
     if (dalloc(&h->d_strips, need) != cudaSuccess) {
       cudaGetLastError();
-      h->record_strips = 0;
+      h->adj_record = 0;
       return fail(h, TP_ERR_NOMEM, "adjoint: strip-sample buffer");
     }
     h->strips_cap = need;
   }
-  h->record_strips = 1;
+  h->adj_record = 1;
   return TP_OK;
 }
 
@@ -1278,7 +1288,7 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
     return fail(h, TP_ERR_STATE, "tp_backward: run tp_process (with correlation pairs) first");
   cudaStream_t st = pick_stream(h, stream);
   const size_t nt = h->ntiles, S = h->cfg.num_sensors;
-  const int nb = (int)((nt + 255) / 256);
+  const int nb = (int)((nt + 256 / S - 1) / (256 / S));  // blocks of the contraction kernel (256 / S tasks each)
   if (!h->d_sens) {
     bool ok = dalloc(&h->d_port_deriv, nt * S * 10) == cudaSuccess && dalloc(&h->d_sens, nt * S * 2) == cudaSuccess &&
               dalloc(&h->d_dval, nt) == cudaSuccess && dalloc(&h->d_jac_e, nt * S * 4) == cudaSuccess &&
@@ -1292,13 +1302,15 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
     CK(cudaMemsetAsync(h->d_grad_d, 0, nt * sizeof(float), st), "tp_backward");
     CK(cudaMemsetAsync(h->d_jac_d, 0, nt * sizeof(float), st), "tp_backward");
   }
-  // the plan again with the FP64 port derivatives (same ports, corners and residuals)
+  // the FP64 port derivatives of the current plan (same ports, corners and residuals): computed
+  // here unless the forward's plan already produced them
   SceneDev sc = scene_of(h);
   sc.port_deriv = h->d_port_deriv;
   const int use_strips = h->strips_valid && sc.strips;
-  tp_status rs = enable_strip_recording(h);  // later forwards keep their strip samples
+  tp_status rs = enable_strip_recording(h);  // later forwards keep their strip samples and derivatives
   if (rs != TP_OK) return rs;
-  CK(launch_plan(sc, st), "tp_backward plan");
+  if (!h->deriv_valid) CK(launch_plan(sc, st), "tp_backward plan");
+  h->deriv_valid = 1;
   if (dl_ddisp) CK(cudaMemcpyAsync(h->d_dldd, dl_ddisp, nt * sizeof(float), cudaMemcpyHostToDevice, st), "tp_backward");
   CK(launch_adjoint(sc, h->corr_host, h->adj_recompute, use_strips, h->d_sens, h->d_dval, dl_ddisp ? h->d_dldd : nullptr,
                     h->d_jac_e, h->d_jac_d, h->d_grad_d, h->d_partial, h->d_grad_e, st),
