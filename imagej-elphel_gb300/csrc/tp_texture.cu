@@ -42,6 +42,205 @@ __device__ __forceinline__ constexpr float kern_tap(bool rb, int dr) {
 
 }  // namespace
 
+// Per-pixel stage of a tile (debayer, shot noise, port weights, dust removal, alpha, RGB mix);
+// FULL: all four ports used (the usual tile mask 0xF), so every mask test folds away.
+template <bool FULL>
+__device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_P * TX_P], const float *s_win2,
+                                           const float *s_rwin2, float *out, int mask_rt, int used_rt,
+                                           float inv_used, float ksigma, int tid, float part[16]) {
+  const int mask = FULL ? 0xF : mask_rt;
+  const int used = FULL ? 4 : used_rt;
+  for (int i = tid; i < 256; i += TX_THREADS) {
+    // tile_debayer (ImageDtt.java:3047-3147): 3x3 stencil over the un-windowed tile, the
+    // taps outside the tile dropped and the sum renormalised (k_corn / k_side); the
+    // neighbour weights (kernel x 1/window^2 x edge factor) serve all 12 planes
+    const int y = i >> 4, x = i & 15, p = (y + 1) * TX_P + x + 1;
+    const bool ey = (y == 0) || (y == 15), ex = (x == 0) || (x == 15);
+    const float f_rb = (ey && ex) ? (16.0f / 9.0f) : ((ey || ex) ? (4.0f / 3.0f) : 1.0f);
+    const float f_g = (ey && ex) ? (4.0f / 3.0f) : ((ey || ex) ? (8.0f / 7.0f) : 1.0f);
+    const float lw = s_win2[i], rlw = s_rwin2[p], rlw2 = rlw * rlw;
+    float d[4][3];
+#pragma unroll
+    for (int ip = 0; ip < 4; ip++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float *u = s_ic[ip * 3 + c] + p;  // un-windowed tile, zero outside
+        const float sides = (u[-TX_P] + u[-1]) + (u[1] + u[TX_P]);
+        float acc;
+        if (c != 2) {  // kern_rb: corners 1/16, sides 1/8, centre 1/4
+          const float corners = (u[-TX_P - 1] + u[-TX_P + 1]) + (u[TX_P - 1] + u[TX_P + 1]);
+          acc = fmaf(0.0625f, corners, fmaf(0.125f, sides, 0.25f * u[0]));
+        } else {       // kern_g: sides 1/8, centre 1/2
+          acc = fmaf(0.125f, sides, 0.5f * u[0]);
+        }
+        acc *= (c != 2) ? f_rb : f_g;
+        if (tc.scale_shot > 0.f)  // tile_debayer_shot_corr (3022-3045)
+          acc = tc.scale_shot * ((acc > tc.min_shot) ? acc * rsqrtf(acc) : (tc.rsqrt_min_shot * acc));
+        d[ip][c] = acc * lw;
+        part[4 + c * 4 + ip] += d[ip][c];
+      }
+    if (tc.rows > 4) {  // per-colour rms across the used ports and their weighted norm
+      float sw = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++)
+          if (mask & (1 << ip)) { s0 += 1.f; s1 += d[ip][c]; }
+        // sqrt(s0*s2 - s1^2)/s0 evaluated as the centred sum (no cancellation)
+        const float m = __fdividef(s1, s0);
+        float v = 0.f;
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++)
+          if (mask & (1 << ip)) v = fmaf(d[ip][c] - m, d[ip][c] - m, v);
+        const float rms = __fdividef(sqrtf(v * s0), s0);
+        out[(8 + c) * 256 + i] = rms;
+        sw = fmaf(tc.col_weights[c] * rms, rms, sw);
+      }
+      out[11 * 256 + i] = sqrtf(sw);
+    }
+    // Weights are kept relative to the largest one (scale sc_w): every use of them below is
+    // a ratio or homogeneous of degree 1 (dust_remove), so FP32 exp() cannot underflow to
+    // 0/0 where the FP64 reference stays finite.  Where the reference's own weights
+    // underflow in double (exponent below -745.13), its 0/0 results are reproduced.
+    float pw[4] = {0.f, 0.f, 0.f, 0.f}, avg[3] = {0.f, 0.f, 0.f}, sc_w = 1.f;
+    if (used > 1) {
+      // pair weights: Gaussian of the weighted colour difference, scaled by the pair distance
+      float ea[6];
+      float amin = CUDART_INF_F;
+#pragma unroll
+      for (int a = 0, k = 0; a < 4; a++)
+#pragma unroll
+        for (int b = a + 1; b < 4; b++, k++) {
+          ea[k] = CUDART_INF_F;
+          if ((mask >> a) & (mask >> b) & 1) {
+            // squared port distance: 1 for side pairs, 2 for the diagonals (0,3) and (1,2)
+            const float pd = (a + b == 3) ? 0.5f * ksigma : ksigma;
+            float dd = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const float dc = d[a][c] - d[b][c];
+              dd = fmaf(tc.col_weights[c] * dc, dc, dd);
+            }
+            ea[k] = pd * (dd * rlw2);
+            amin = fminf(amin, ea[k]);
+          }
+        }
+      if (amin > TX_EXP_UNDERFLOW) {  // all pair weights 0 in double: 0/0 downstream
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++) pw[ip] = (mask & (1 << ip)) ? CUDART_NAN_F : 0.f;
+        avg[0] = avg[1] = avg[2] = CUDART_NAN_F;
+      } else {
+#pragma unroll
+        for (int a = 0, k = 0; a < 4; a++)
+#pragma unroll
+          for (int b = a + 1; b < 4; b++, k++)
+            if ((mask >> a) & (mask >> b) & 1) {
+              const float e = __expf(amin - ea[k]);
+              pw[a] += e;
+              pw[b] += e;
+            }
+        int b1 = 0;
+#pragma unroll
+        for (int ip = 1; ip < 4; ip++) if (pw[ip] > pw[b1]) b1 = ip;
+        int b2 = (b1 == 0) ? 1 : 0;
+#pragma unroll
+        for (int ip = b2 + 1; ip < 4; ip++) if (ip != b1 && pw[ip] > pw[b2]) b2 = ip;
+        float p1 = 0.f, p2 = 0.f;  // register-resident selection of the two best ports
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++) { if (ip == b1) p1 = pw[ip]; if (ip == b2) p2 = pw[ip]; }
+        const float wa = __fdividef(p1, p1 + p2), wb = 1.0f - wa;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          float v1 = 0.f, v2 = 0.f;
+#pragma unroll
+          for (int ip = 0; ip < 4; ip++) { if (ip == b1) v1 = d[ip][c]; if (ip == b2) v2 = d[ip][c]; }
+          avg[c] = wa * v1 + wb * v2;
+        }
+        // re-weight every used port by its distance from the best-pair average
+        float eb[4], bmin = CUDART_INF_F;
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++) {
+          float d2 = 0.f;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const float dc = d[ip][c] - avg[c];
+            d2 = fmaf(tc.col_weights[c] * dc, dc, d2);
+          }
+          eb[ip] = ksigma * (d2 * rlw2);
+          if (mask & (1 << ip)) bmin = fminf(bmin, eb[ip]);
+        }
+        const bool zero = bmin > TX_EXP_UNDERFLOW;  // all weights 0 in double
+#pragma unroll
+        for (int ip = 0; ip < 4; ip++)
+          if (mask & (1 << ip)) pw[ip] = zero ? 0.f : __expf(bmin - eb[ip]);
+        sc_w = zero ? 1.f : expf(-bmin);
+        const float kk = __fdividef(1.0f, ((pw[0] + pw[1]) + pw[2]) + pw[3]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          float v = 0.f;
+#pragma unroll
+          for (int ip = 0; ip < 4; ip++) v += kk * pw[ip] * d[ip][c];
+          avg[c] = v;
+        }
+      }
+    } else if (used > 0) {
+#pragma unroll
+      for (int ip = 0; ip < 4; ip++)
+        if (mask & (1 << ip)) {
+#pragma unroll
+          for (int c = 0; c < 3; c++) avg[c] = d[ip][c];
+          pw[ip] = 1.f;
+        }
+    }
+    if (tc.dust_remove && used == 4) {  // dust_remove (ImageDtt.java:3002-3019), from port 1 as there
+      int wi = 0;
+#pragma unroll
+      for (int ip = 1; ip < 4; ip++) if (pw[ip] < pw[wi]) wi = ip;
+      float a = 0.f, pwi = 0.f;
+#pragma unroll
+      for (int ip = 0; ip < 4; ip++) { if (ip >= 1 && ip != wi) a += pw[ip]; if (ip == wi) pwi = pw[ip]; }
+      a *= (1.0f / 3.0f);
+      const float scl = 1.0f + __fdividef(a - pwi, a * 3.f);
+#pragma unroll
+      for (int ip = 1; ip < 4; ip++) if (ip != wi) pw[ip] *= scl;
+#pragma unroll
+      for (int ip = 0; ip < 4; ip++) if (ip == wi) pw[ip] *= __fdividef(pwi, a);
+    }
+    float alpha = 0.f;
+#pragma unroll
+    for (int ip = 0; ip < 4; ip++) if (mask & (1 << ip)) alpha += pw[ip];
+    out[3 * 256 + i] = (alpha * sc_w) * (lw * inv_used);
+    if (tc.rows > 4) {
+#pragma unroll
+      for (int ip = 0; ip < 4; ip++) out[(4 + ip) * 256 + i] = pw[ip] * sc_w;
+    }
+    // max_diff partial (ImageDtt.java:2964-2981); a NaN average is skipped as there
+#pragma unroll
+    for (int ip = 0; ip < 4; ip++)
+      if (mask & (1 << ip)) {
+        float d2 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float dc = d[ip][c] - avg[c];
+          d2 = fmaf(dc * dc, tc.col_weights[c], d2);
+        }
+        part[ip] = fmaxf(part[ip], d2 * lw);
+      }
+    // RGB mix of the un-debayered tiles (ImageDtt.java:2788-2801)
+    float sw = ((pw[0] + pw[1]) + pw[2]) + pw[3];
+    if (sw != 0.f) sw = __fdividef(1.0f, sw);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float v = 0.f;
+#pragma unroll
+      for (int ip = 0; ip < 4; ip++) v += sw * pw[ip] * s_ic[ip * 3 + c][p];
+      v *= lw;  // the tiles are kept un-windowed
+      out[c * 256 + i] = v;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(TX_THREADS, 5) texture_kernel(const __grid_constant__ SceneDev sc,
                                                              const __grid_constant__ TexConst tc) {
   // per-port IMCLT tiles [port * 3 + colour][18 x 18]: the 16x16 tile inside a zero border,
@@ -149,195 +348,8 @@ __global__ void __launch_bounds__(TX_THREADS, 5) texture_kernel(const __grid_con
     float part[16];  // this thread's max_diff[4] and ports_rgb[12] partials
 #pragma unroll
     for (int k = 0; k < 16; k++) part[k] = 0.f;
-    for (int i = tid; i < 256; i += TX_THREADS) {
-      // tile_debayer (ImageDtt.java:3047-3147): 3x3 stencil over the un-windowed tile, the
-      // taps outside the tile dropped and the sum renormalised (k_corn / k_side); the
-      // neighbour weights (kernel x 1/window^2 x edge factor) serve all 12 planes
-      const int y = i >> 4, x = i & 15, p = (y + 1) * TX_P + x + 1;
-      const bool ey = (y == 0) || (y == 15), ex = (x == 0) || (x == 15);
-      const float f_rb = (ey && ex) ? (16.0f / 9.0f) : ((ey || ex) ? (4.0f / 3.0f) : 1.0f);
-      const float f_g = (ey && ex) ? (4.0f / 3.0f) : ((ey || ex) ? (8.0f / 7.0f) : 1.0f);
-      const float lw = s_win2[i], rlw = s_rwin2[p], rlw2 = rlw * rlw;
-      float d[4][3];
-#pragma unroll
-      for (int ip = 0; ip < 4; ip++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const float *u = s_ic[ip * 3 + c] + p;  // un-windowed tile, zero outside
-          const float sides = (u[-TX_P] + u[-1]) + (u[1] + u[TX_P]);
-          float acc;
-          if (c != 2) {  // kern_rb: corners 1/16, sides 1/8, centre 1/4
-            const float corners = (u[-TX_P - 1] + u[-TX_P + 1]) + (u[TX_P - 1] + u[TX_P + 1]);
-            acc = fmaf(0.0625f, corners, fmaf(0.125f, sides, 0.25f * u[0]));
-          } else {       // kern_g: sides 1/8, centre 1/2
-            acc = fmaf(0.125f, sides, 0.5f * u[0]);
-          }
-          acc *= (c != 2) ? f_rb : f_g;
-          if (tc.scale_shot > 0.f)  // tile_debayer_shot_corr (3022-3045)
-            acc = tc.scale_shot * ((acc > tc.min_shot) ? acc * rsqrtf(acc) : (tc.rsqrt_min_shot * acc));
-          d[ip][c] = acc * lw;
-          part[4 + c * 4 + ip] += d[ip][c];
-        }
-      if (tc.rows > 4) {  // per-colour rms across the used ports and their weighted norm
-        float sw = 0.f;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++)
-            if (mask & (1 << ip)) { s0 += 1.f; s1 += d[ip][c]; }
-          // sqrt(s0*s2 - s1^2)/s0 evaluated as the centred sum (no cancellation)
-          const float m = __fdividef(s1, s0);
-          float v = 0.f;
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++)
-            if (mask & (1 << ip)) v = fmaf(d[ip][c] - m, d[ip][c] - m, v);
-          const float rms = __fdividef(sqrtf(v * s0), s0);
-          out[(8 + c) * 256 + i] = rms;
-          sw = fmaf(tc.col_weights[c] * rms, rms, sw);
-        }
-        out[11 * 256 + i] = sqrtf(sw);
-      }
-      // Weights are kept relative to the largest one (scale sc_w): every use of them below is
-      // a ratio or homogeneous of degree 1 (dust_remove), so FP32 exp() cannot underflow to
-      // 0/0 where the FP64 reference stays finite.  Where the reference's own weights
-      // underflow in double (exponent below -745.13), its 0/0 results are reproduced.
-      float pw[4] = {0.f, 0.f, 0.f, 0.f}, avg[3] = {0.f, 0.f, 0.f}, sc_w = 1.f;
-      if (used > 1) {
-        // pair weights: Gaussian of the weighted colour difference, scaled by the pair distance
-        float ea[6];
-        float amin = CUDART_INF_F;
-#pragma unroll
-        for (int a = 0, k = 0; a < 4; a++)
-#pragma unroll
-          for (int b = a + 1; b < 4; b++, k++) {
-            ea[k] = CUDART_INF_F;
-            if ((mask >> a) & (mask >> b) & 1) {
-              // squared port distance: 1 for side pairs, 2 for the diagonals (0,3) and (1,2)
-              const float pd = (a + b == 3) ? 0.5f * ksigma : ksigma;
-              float dd = 0.f;
-#pragma unroll
-              for (int c = 0; c < 3; c++) {
-                const float dc = d[a][c] - d[b][c];
-                dd = fmaf(tc.col_weights[c] * dc, dc, dd);
-              }
-              ea[k] = pd * (dd * rlw2);
-              amin = fminf(amin, ea[k]);
-            }
-          }
-        if (amin > TX_EXP_UNDERFLOW) {  // all pair weights 0 in double: 0/0 downstream
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++) pw[ip] = (mask & (1 << ip)) ? CUDART_NAN_F : 0.f;
-          avg[0] = avg[1] = avg[2] = CUDART_NAN_F;
-        } else {
-#pragma unroll
-          for (int a = 0, k = 0; a < 4; a++)
-#pragma unroll
-            for (int b = a + 1; b < 4; b++, k++)
-              if ((mask >> a) & (mask >> b) & 1) {
-                const float e = __expf(amin - ea[k]);
-                pw[a] += e;
-                pw[b] += e;
-              }
-          int b1 = 0;
-#pragma unroll
-          for (int ip = 1; ip < 4; ip++) if (pw[ip] > pw[b1]) b1 = ip;
-          int b2 = (b1 == 0) ? 1 : 0;
-#pragma unroll
-          for (int ip = b2 + 1; ip < 4; ip++) if (ip != b1 && pw[ip] > pw[b2]) b2 = ip;
-          float p1 = 0.f, p2 = 0.f;  // register-resident selection of the two best ports
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++) { if (ip == b1) p1 = pw[ip]; if (ip == b2) p2 = pw[ip]; }
-          const float wa = __fdividef(p1, p1 + p2), wb = 1.0f - wa;
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            float v1 = 0.f, v2 = 0.f;
-#pragma unroll
-            for (int ip = 0; ip < 4; ip++) { if (ip == b1) v1 = d[ip][c]; if (ip == b2) v2 = d[ip][c]; }
-            avg[c] = wa * v1 + wb * v2;
-          }
-          // re-weight every used port by its distance from the best-pair average
-          float eb[4], bmin = CUDART_INF_F;
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++) {
-            float d2 = 0.f;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-              const float dc = d[ip][c] - avg[c];
-              d2 = fmaf(tc.col_weights[c] * dc, dc, d2);
-            }
-            eb[ip] = ksigma * (d2 * rlw2);
-            if (mask & (1 << ip)) bmin = fminf(bmin, eb[ip]);
-          }
-          const bool zero = bmin > TX_EXP_UNDERFLOW;  // all weights 0 in double
-#pragma unroll
-          for (int ip = 0; ip < 4; ip++)
-            if (mask & (1 << ip)) pw[ip] = zero ? 0.f : __expf(bmin - eb[ip]);
-          sc_w = zero ? 1.f : expf(-bmin);
-          const float kk = __fdividef(1.0f, ((pw[0] + pw[1]) + pw[2]) + pw[3]);
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            float v = 0.f;
-#pragma unroll
-            for (int ip = 0; ip < 4; ip++) v += kk * pw[ip] * d[ip][c];
-            avg[c] = v;
-          }
-        }
-      } else if (used > 0) {
-#pragma unroll
-        for (int ip = 0; ip < 4; ip++)
-          if (mask & (1 << ip)) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) avg[c] = d[ip][c];
-            pw[ip] = 1.f;
-          }
-      }
-      if (tc.dust_remove && used == 4) {  // dust_remove (ImageDtt.java:3002-3019), from port 1 as there
-        int wi = 0;
-#pragma unroll
-        for (int ip = 1; ip < 4; ip++) if (pw[ip] < pw[wi]) wi = ip;
-        float a = 0.f, pwi = 0.f;
-#pragma unroll
-        for (int ip = 0; ip < 4; ip++) { if (ip >= 1 && ip != wi) a += pw[ip]; if (ip == wi) pwi = pw[ip]; }
-        a *= (1.0f / 3.0f);
-        const float scl = 1.0f + __fdividef(a - pwi, a * 3.f);
-#pragma unroll
-        for (int ip = 1; ip < 4; ip++) if (ip != wi) pw[ip] *= scl;
-#pragma unroll
-        for (int ip = 0; ip < 4; ip++) if (ip == wi) pw[ip] *= __fdividef(pwi, a);
-      }
-      float alpha = 0.f;
-#pragma unroll
-      for (int ip = 0; ip < 4; ip++) if (mask & (1 << ip)) alpha += pw[ip];
-      out[3 * 256 + i] = (alpha * sc_w) * (lw * inv_used);
-      if (tc.rows > 4) {
-#pragma unroll
-        for (int ip = 0; ip < 4; ip++) out[(4 + ip) * 256 + i] = pw[ip] * sc_w;
-      }
-      // max_diff partial (ImageDtt.java:2964-2981); a NaN average is skipped as there
-#pragma unroll
-      for (int ip = 0; ip < 4; ip++)
-        if (mask & (1 << ip)) {
-          float d2 = 0.f;
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            const float dc = d[ip][c] - avg[c];
-            d2 = fmaf(dc * dc, tc.col_weights[c], d2);
-          }
-          part[ip] = fmaxf(part[ip], d2 * lw);
-        }
-      // RGB mix of the un-debayered tiles (ImageDtt.java:2788-2801)
-      float sw = ((pw[0] + pw[1]) + pw[2]) + pw[3];
-      if (sw != 0.f) sw = __fdividef(1.0f, sw);
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        float v = 0.f;
-#pragma unroll
-        for (int ip = 0; ip < 4; ip++) v += sw * pw[ip] * s_ic[ip * 3 + c][p];
-        v *= lw;  // the tiles are kept un-windowed
-        out[c * 256 + i] = v;
-      }
-    }
+    if (mask == 0xF) tex_pixels<true>(tc, s_ic, s_win2, s_rwin2, out, mask, used, inv_used, ksigma, tid, part);
+    else tex_pixels<false>(tc, s_ic, s_win2, s_rwin2, out, mask, used, inv_used, ksigma, tid, part);
     if (sc.tex_aux) {
       // one block reduction for max_diff (max) and ports_rgb (sum)
 #pragma unroll
