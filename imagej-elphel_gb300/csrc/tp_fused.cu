@@ -219,10 +219,11 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
 
 // phase B for pair pi: correlation surface to HBM, strip entries folded into cmb
 // (NT = strip entries per lane / 32 rounded up: 1 when the extraction reads <= 32 entries)
-template <int C, int NT>
+template <int C, int NT, bool OACC = false>
 __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, size_t tile, int P, int pi, int RE,
                                          bool log_mode, const short *strip_code, const float *s_clt, float *scr,
-                                         int lane, float cmb[8], float *corr_out = nullptr) {
+                                         int lane, float cmb[8], float *corr_out = nullptr,
+                                         float *oprod = nullptr) {
   const int q = lane >> 3, r = lane & 7;
   float *qb = scr;
   const PairDev pd = cfg.pairs[pi];
@@ -315,6 +316,17 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
     if (a && b) cs[(7 - a) * 15 + 7 - b] = 0.25f * (((A - B) - Cc) + D);
   }
   __syncwarp();
+  if (OACC && (pd.kind == 0 || pd.kind == 1) && !cfg.log_combine) {
+    // getMaxXSOrtho profile of a horizontal (lanes 0-14, columns) or vertical (lanes 16-30, rows)
+    // pair, symmetrised (even in i, so rows 0..7 carry it) and multiplied into this lane's oprod
+    const int half = lane >> 4, j = lane & 15;
+    if (half == pd.kind && j < 15) {
+      const int stride = half ? 1 : 15, base = half ? j * 15 : j;
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        oprod[i] *= 0.5f * (cs[base + i * stride] + cs[base + (14 - i) * stride]) + cfg.corr_offset;
+    }
+  }
   float *gc = corr_out ? corr_out : sc.corr + (tile * P + pi) * TP_CORR;
   for (int o2 = lane; o2 < TP_CORR; o2 += 32) gc[o2] = cs[o2];
   if (pd.in_combo) {
@@ -351,10 +363,10 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
 }
 
 // phase C: combined strip, integer argmax, centroid, ortho maxima, disparity record
-template <int NT>
+template <int NT, bool OACC = false>
 __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
                                             bool log_mode, int ncomb, size_t tile, float *scr, int lane,
-                                            const float cmb[8]) {
+                                            const float cmb[8], const float *oprod = nullptr) {
   // ---------------- stage 3c: extraction ----------------
   float *combo = scr;
 #pragma unroll
@@ -432,8 +444,8 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
       // loads of one pair are issued before their use
       float prod[8];
 #pragma unroll
-      for (int i = 0; i < 8; i++) prod[i] = 1.f;
-      for (int k = 0; k < np; k++) {
+      for (int i = 0; i < 8; i++) prod[i] = OACC ? oprod[i] : 1.f;
+      for (int k = 0; k < (OACC ? 0 : np); k++) {
         const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
         const int stride = half ? 1 : 15, base = half ? j * 15 : j;
         float a[8], b[8];
@@ -514,8 +526,12 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
     float cmb[8];
 #pragma unroll
     for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
-    for (int pi = 0; pi < P; pi++) fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
-    fwd_extract<NT>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
+    float oprod[8];  // hor / vert profile products of this lane's column (row), filled by phase B
+#pragma unroll
+    for (int i = 0; i < 8; i++) oprod[i] = 1.f;
+    for (int pi = 0; pi < P; pi++)
+      fwd_pair<C, NT, true>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr, oprod);
+    fwd_extract<NT, true>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
   }
 }
 
