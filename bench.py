@@ -51,7 +51,7 @@ DEFAULT_CONFIG = "c2_bayer_4x2592x1936"
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)  # ~0.6 s timed: several clock samples
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(CONFIGS))
@@ -63,6 +63,8 @@ def parse_args():
     p.add_argument("--adjoint-only", action="store_true",
                    help="only the 16-sensor forward / forward+adjoint / LM measurement (profiling)")
     p.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles per CPU sample (0 = auto)")
+    p.add_argument("--schedule", default="", help="tiles_per_cta,warps_per_cta of the forward instead of the autotuner "
+                                                  "(profiling)")
     return p.parse_args()
 
 
@@ -145,7 +147,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -469,8 +471,13 @@ def run_ours(args):
     stages = ["ports", "forward", "imclt"]
     fns = [lib.tp_ports, lib.tp_process, lib.tp_imclt]
     # schedule of the fused forward picked by the project's autotuner on this scene (outside the timing)
-    from tileproc.autotune import autotune
-    sched, sched_ms = autotune(tp, reps=5, warmup=2)
+    if args.schedule:
+        sched = tuple(int(v) for v in args.schedule.split(","))
+        sched_ms = {}
+        tp.setSchedule(*sched)
+    else:
+        from tileproc.autotune import autotune
+        sched, sched_ms = autotune(tp, reps=5, warmup=2)
     with_tex = S == 4 and Cn == 3
     if with_tex:
         tp.setTextureParams()
@@ -527,7 +534,7 @@ def run_ours(args):
             tp._ck(lib.tp_lma_refine(tp.h, C.byref(prm), sptr), "lma")
         torch.cuda.synchronize()
         l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        n_lma = max(3, args.steps)
+        n_lma = max(3, min(args.steps, 20))
         l0.record(stream)
         for _ in range(n_lma):
             tp._ck(lib.tp_lma_refine(tp.h, C.byref(prm), sptr), "lma")
@@ -579,14 +586,15 @@ def run_ours(args):
 
     batched = batched_small = None
     if rank == 0 and args.batch_scenes > 0:
-        batched = measure_batch(args.seed, args.batch_scenes, max(3, args.steps // 4), min(args.warmup, 3))
-        batched_small = measure_batch(args.seed, args.batch_scenes, max(3, args.steps // 4), min(args.warmup, 3),
+        nb_steps = max(3, min(args.steps // 4, 10))
+        batched = measure_batch(args.seed, args.batch_scenes, nb_steps, min(args.warmup, 3))
+        batched_small = measure_batch(args.seed, args.batch_scenes, nb_steps, min(args.warmup, 3),
                                       types=("c1_mono_4x512x384",))
         torch.cuda.set_stream(stream)
 
     fwd_adj = None
     if rank == 0 and not args.no_adjoint:
-        fwd_adj = measure_fwd_adjoint(args.seed, max(3, args.steps // 2), args.warmup)
+        fwd_adj = measure_fwd_adjoint(args.seed, max(3, min(args.steps // 2, 50)), args.warmup)
         torch.cuda.set_stream(stream)
 
     cpu = None
