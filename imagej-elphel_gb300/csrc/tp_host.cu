@@ -1147,6 +1147,16 @@ tp_status tp_default_lma_params(tp_lma_params *p) {
   p->rms_diff = 0.001f;
   p->num_iter = 20;
   p->pair_mask = 0x3f;
+  p->fo_correct = 1;
+  p->fo_far = 0;
+  p->fo_ortho = 1;
+  p->fo_min_strength = 0.1f;
+  p->fo_min_eff = 0.25f;
+  p->fo_min_eff_ratio = 0.65f;
+  p->fo_max_hwidth = 3.0f;
+  p->fo_min_diff = 0.2f;
+  p->fo_overcorrection = 0.0f;
+  p->fo_lim_overcorr = 2.0f;
   return TP_OK;
 }
 
@@ -1196,8 +1206,18 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   c.rms_diff = prm.rms_diff;
   c.num_iter = prm.num_iter;
   c.pair_mask = prm.pair_mask;
+  c.fo_correct = prm.fo_correct;
+  c.fo_far = prm.fo_far;
+  c.fo_ortho = prm.fo_ortho;
+  c.fo_min_strength = prm.fo_min_strength;
+  c.fo_min_eff = prm.fo_min_eff;
+  c.fo_min_eff_ratio = prm.fo_min_eff_ratio;
+  c.fo_max_hwidth = prm.fo_max_hwidth;
+  c.fo_min_diff = prm.fo_min_diff;
+  c.fo_overcorrection = prm.fo_overcorrection;
+  c.fo_lim_overcorr = prm.fo_lim_overcorr;
   CK(launch_lma(scene_of(h), h->corr_host, c, h->d_lma, st), "tp_lma_refine");
-  if (prm.mix_corr_poly) h->disp_mixed = 1;
+  if (prm.mix_corr_poly || prm.fo_correct) h->disp_mixed = 1;
   return TP_OK;
 }
 

@@ -176,6 +176,9 @@ struct TpLmaConst {
   float half_width, cost_wy, cost_wxy;
   float lambda_initial, lambda_scale_good, lambda_scale_bad, lambda_max, rms_diff;
   int num_iter, pair_mask;
+  int fo_correct, fo_far, fo_ortho;
+  float fo_min_strength, fo_min_eff, fo_min_eff_ratio, fo_max_hwidth, fo_min_diff, fo_overcorrection,
+      fo_lim_overcorr;
 };
 cudaError_t upload_lma_constants();
 cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out, cudaStream_t st);

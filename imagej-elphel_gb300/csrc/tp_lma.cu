@@ -27,6 +27,7 @@ constexpr int LMA_ORTHO_ENTRIES = 81;  // addSamples enumeration, ortho group
 constexpr int LMA_DIAG_ENTRIES = 145;  // addSamples enumeration, diagonal group
 constexpr int LMA_MAX_SAMPLES = 162;   // 9x9 window cells per group
 constexpr int LMA_NP = 6;              // X0, WM, WYD, WXY, AG0, AG1
+constexpr int LMA_STAGE_PAIRS = 6;     // pair surfaces staged in shared memory (the quad layout's six)
 
 // sample cell offsets from the (integer) centre, in the reference's enumeration order (global
 // memory: consecutive lanes read consecutive entries)
@@ -42,10 +43,14 @@ __device__ __forceinline__ void cp_async8(float *dst_smem, const float *src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
 
-// per-warp shared memory (floats)
-constexpr int LMA_PER_WARP = 2 * 225             // group surfaces
-                             + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 8  // samples
-                             + 28 * 33 + 64;     // reduction buffer, accepted / trial normal equations
+// per-warp shared memory (floats): group surfaces [2][225], samples x/y/v/w [4][162] + group bytes,
+// the reduction buffer [28][33], accepted / trial normal equations, and the staged pair surfaces,
+// which start on a 16-byte boundary for the 8-byte asynchronous copies
+constexpr int LMA_OFF_RED = 450 + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1;
+constexpr int LMA_OFF_STAGE = ((LMA_OFF_RED + 28 * 33 + 64) + 3) & ~3;
+constexpr int LMA_OFF_RES = LMA_OFF_STAGE + LMA_STAGE_PAIRS * 225;  // [4][4] orientation fits
+constexpr int LMA_PER_WARP = ((LMA_OFF_RES + 16) + 3) & ~3;
+static_assert(LMA_OFF_STAGE % 4 == 0 && LMA_PER_WARP % 4 == 0, "staged surfaces must be 16-byte aligned");
 
 struct LmaDev {
   const float *corr;   // [tiles][P][225]
@@ -54,7 +59,56 @@ struct LmaDev {
   const int *task_txy;
   int num_tasks, tilesX, P;
   int kinds[TP_MAXP];  // pair kind or -1 when the pair does not take part
+  int kind_count[4];   // taking part per kind
 };
+
+// Correlation2d.foregroundCorrect (Correlation2d.java:1663-1749) on the four orientation fits
+// (rows {disparity, strength, WM, WXY}); returns the corrected disparity (full_disp if none)
+__device__ __forceinline__ float foreground_correct(const TpLmaConst &c, const float dir[4][4], const bool valid[4],
+                                                   float full_disp) {
+  float mn = CUDART_NAN_F, mx = CUDART_NAN_F, eff[4], width_d[4];
+  int imn = -1, imx = -1;
+  bool strong[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    strong[i] = false;
+    width_d[i] = 0.f;
+    eff[i] = CUDART_NAN_F;
+    if (valid[i]) {
+      if (isnan(mn) || dir[i][0] < mn) { mn = dir[i][0]; imn = i; }
+      if (isnan(mx) || dir[i][0] > mx) { mx = dir[i][0]; imx = i; }
+      eff[i] = dir[i][1] * (dir[i][2] - dir[i][3]) / (dir[i][2] + dir[i][3]);
+      width_d[i] = dir[i][2] + dir[i][3];
+      strong[i] = (dir[i][1] >= c.fo_min_strength) && (eff[i] >= c.fo_min_eff);
+    }
+  }
+  const bool are_ortho = (imn ^ imx) == 1;
+  float corr = c.fo_overcorrection * (mx - mn);
+  const int isel = c.fo_far ? imn : imx, iother = c.fo_far ? imx : imn, iortho = isel ^ 1;
+  // the indexed reads as selects, so the small arrays stay in registers
+  float e_sel = 0.f, w_sel = 0.f, e_ortho = 0.f;
+  bool s_sel = false, s_other = false;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (i == isel) { e_sel = eff[i]; w_sel = width_d[i]; s_sel = strong[i]; }
+    if (i == iortho) e_ortho = eff[i];
+    if (i == iother) s_other = strong[i];
+  }
+  if (isel < 0 || !s_sel) corr = CUDART_NAN_F;
+  else if (w_sel > c.fo_max_hwidth) corr = CUDART_NAN_F;
+  else if (e_sel / e_ortho < c.fo_min_eff_ratio) corr = CUDART_NAN_F;
+  else {
+    if (c.fo_ortho && !are_ortho) corr = 0.0f;
+    else if (!s_other) corr = 0.0f;
+    if (!(mx >= (mn + c.fo_min_diff))) corr = CUDART_NAN_F;
+  }
+  float disp = full_disp;
+  if (!isnan(corr)) {
+    if (c.fo_far) disp = fmaxf(mn - corr, full_disp - (full_disp - mn) * c.fo_lim_overcorr);
+    else disp = fminf(mx + corr, full_disp + (mx - full_disp) * c.fo_lim_overcorr);
+  }
+  return disp;
+}
 
 // bits a..b (inclusive) of a row mask, none when b < a
 __device__ __forceinline__ unsigned bit_range(int a, int b) {
@@ -63,7 +117,6 @@ __device__ __forceinline__ unsigned bit_range(int a, int b) {
 
 constexpr int LMA_NEQ = 28;  // packed normal equations: A (upper 6x6, 21), b (6), weighted rms^2
 // floats from the sample arrays to the end of the reduction buffer, free before the samples exist
-constexpr int LMA_STAGE = 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1 + 28 * 33;
 
 // Weighted normal equations of the samples at parameters av (getFxJt, getWJtJlambda, getWYmFxRms),
 // written to out[LMA_NEQ] for every lane: per-lane partial sums are transposed through red
@@ -125,6 +178,304 @@ __device__ __forceinline__ void lma_eval(const float *sx, const float *sy, const
 
 }  // namespace
 
+// One Correlation2d.corrLMA fit of a tile from the staged pair surfaces `src` ([P][225]) of the
+// pair kinds in kmask (bit k: kind k), centred at xcenter: res = {disparity, strength, WM, WXY}
+// (getDisparityStrengthWidth); false when there are no samples or the fit did not converge.
+__device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, int kmask, float xcenter,
+                                        const float *src, float *gsurf, float *sx, float *sy, float *sv, float *sw,
+                                        unsigned char *sg, float *red, float *acc, float *trial, int lane,
+                                        float res[4]) {
+  const int hw = c.cnvx_hwnd_size;
+  const int ixc = (int)floorf(xcenter + 0.5f);
+  // ---- group surfaces (combineCompatiblePairs) ----
+  int np_ortho = 0, np_diag = 0;
+  for (int pi = 0; pi < ld.P; pi++) {
+    const int k = ld.kinds[pi];
+    if (k < 0 || !((kmask >> k) & 1)) continue;
+    np_ortho += (k <= 1);
+    np_diag += (k >= 2);
+  }
+  // group sums, pairs in index order (combineCompatiblePairs), 8 cells per lane in registers
+  float go[8], gdg[8];
+#pragma unroll
+  for (int t = 0; t < 8; t++) go[t] = gdg[t] = 0.f;
+  for (int pi = 0; pi < ld.P; pi++) {
+    const int k = ld.kinds[pi];
+    if (k < 0 || !((kmask >> k) & 1)) continue;
+    const float *cs = src + pi * TP_CORR;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int i = lane + 32 * t;
+      if (i < 225) {
+        const int r = i / 15, q = i - r * 15;
+        const float v = (k == 1) ? cs[q * 15 + r] : ((k == 3) ? cs[(14 - r) * 15 + q] : cs[i]);
+        if (k >= 2) gdg[t] += v;
+        else go[t] += v;
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    const int i = lane + 32 * t;
+    if (i < 225) {
+      gsurf[i] = (np_ortho > 1) ? go[t] / np_ortho : go[t];
+      gsurf[225 + i] = (np_diag > 1) ? gdg[t] / np_diag : gdg[t];
+    }
+  }
+  __syncwarp();
+  // ---- filterConvex, both groups at once: lanes 0-14 hold the ortho rows, lanes 16-30 the
+  // diagonal rows, as 15-bit masks (bit = column) of the convex and the selected cells ----
+  const int half = lane >> 4, r = lane & 15, hbase = half << 4;
+  const bool rowlane = r < 15 && (half ? np_diag : np_ortho) > 0;
+  const int x0 = ixc + 7, y0 = (half ? ixc : 0) + 7;
+  const int min_row = max(y0 - hw, 0), max_row = min(y0 + hw, 14);
+  const int min_col = max(x0 - hw, 0), max_col = min(x0 + hw, 14);
+  unsigned conv = 0, sel = 0;
+  if (rowlane) {
+    const float *d = gsurf + 225 * half;
+    if (r > min_row && r < max_row)
+      for (int col = min_col + 1; col < max_col; col++) {
+        const int i = r * 15 + col;
+        if ((2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - 15] + d[i + 15]))) conv |= 1u << col;
+      }
+    if (r == y0 && x0 >= min_col && x0 <= max_col) sel = 1u << x0;
+  }
+  {
+    const unsigned lmask = bit_range(min_col + 1, x0), rmask = bit_range(x0, max_col - 1);
+    const unsigned hmask = 0xffffu << hbase;
+    bool active = rowlane;
+    for (int istep = 0; istep < hw; istep++) {
+      const bool first = istep == 0;
+      const int smin_row = max(y0 - istep, 0), smax_row = min(y0 + istep, 14);
+      const unsigned cols = bit_range(max(x0 - istep, 0), min(x0 + istep, 14));
+      unsigned seln = sel;
+      // up / down: the source row's selected cells (convex, or the start) grow into the next row
+      const unsigned src = sel & cols & (first ? 0x7fffu : conv);
+      const bool up_ok = istep < y0, down_ok = (y0 + istep) < max_row;
+      const unsigned s_up = __shfl_sync(0xffffffffu, src, hbase + max(y0 - istep, 0));
+      const unsigned s_dn = __shfl_sync(0xffffffffu, src, hbase + min(y0 + istep, 14));
+      if (up_ok && r == y0 - istep - 1) {
+        const unsigned c1 = s_up & conv;
+        seln |= s_up | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
+      }
+      if (down_ok && r == y0 + istep + 1) {
+        const unsigned c1 = s_dn & conv;
+        seln |= s_dn | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
+      }
+      // left / right: the source column's cells grow sideways, and from a convex target up or
+      // down towards the centre row's side
+      unsigned push_up = 0, push_dn = 0;
+      const bool in_rows = r >= smin_row && r <= smax_row;
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        const int col = side ? x0 + istep : x0 - istep;
+        const bool ok = side ? ((x0 + istep) < max_col) : (istep < x0);
+        if (!ok || !in_rows || col < 0 || col > 14) continue;
+        const unsigned cb = 1u << col, tb = side ? (cb << 1) : (cb >> 1);
+        if ((sel & cb) && (first || (conv & cb))) {
+          seln |= tb;
+          if (conv & tb) {
+            if (r <= y0 && r > min_row) push_up |= tb;
+            if (r >= y0 && r < max_row) push_dn |= tb;
+          }
+        }
+      }
+      seln |= __shfl_down_sync(0xffffffffu, push_up, 1) | __shfl_up_sync(0xffffffffu, push_dn, 1);
+      if (!rowlane) seln = 0;
+      const unsigned changed = __ballot_sync(0xffffffffu, active && seln != sel) & hmask;
+      if (!changed) active = false;
+      if (active) sel = seln;
+      if (!__any_sync(0xffffffffu, active)) break;
+    }
+  }
+  // ---- samples (addSamples), compacted in the enumeration order ----
+  int ns = 0, ngroups = 0, gdiag_bits = 0;
+  for (int gd = 0; gd < 2; gd++) {
+    const int npg = gd ? np_diag : np_ortho;
+    if (npg == 0) continue;
+    const int base = gd ? LMA_ORTHO_ENTRIES : 0, cnt = gd ? LMA_DIAG_ENTRIES : LMA_ORTHO_ENTRIES;
+    const float *d = gsurf + 225 * gd;
+    int gnum = -1;  // groups are numbered in the order their first sample arrives
+    for (int e0 = 0; e0 < cnt; e0 += 32) {
+      const int e = e0 + lane;
+      float w = 0.f, v = 0.f, x = 0.f, y = 0.f;
+      int cxo = 99, cyo = 99;
+      if (e < cnt) {
+        cxo = __ldg(&g_lma_cx[base + e]);
+        cyo = __ldg(&g_lma_cy[base + e]);
+      }
+      const int cx = cxo + ixc, cy = cyo + (gd ? ixc : 0);
+      const bool inside = e < cnt && cx >= -7 && cx <= 7 && cy >= -7 && cy <= 7;
+      const int srow = inside ? cy + 7 : 0;
+      const unsigned rsel = __shfl_sync(0xffffffffu, sel, (gd << 4) + srow);
+      const unsigned rconv = __shfl_sync(0xffffffffu, conv, (gd << 4) + srow);
+      if (inside) {
+        {
+          const int idx = 112 + 15 * cy + cx, ccol = cx + 7, gy0 = (gd ? ixc : 0) + 7;
+          float wc = 0.f;
+          if ((rsel >> ccol) & 1) wc = ((rconv >> ccol) & 1) ? 1.0f : c.cnvx_weight;
+          else if (c.cnvx_add3x3 && srow >= gy0 - 1 && srow <= gy0 + 1 && ccol >= ixc + 6 && ccol <= ixc + 8)
+            wc = c.cnvx_weight;
+          w = wc * npg;
+          if (w > 0.f) {
+            v = d[idx];
+            if (c.ortho_vasw_pwr == 2.0f) w *= v * v;
+            else if (c.ortho_vasw_pwr != 0.0f) w *= powf(fabsf(v), c.ortho_vasw_pwr);
+            x = (gd ? 0.5f * (cxo + cyo) : (float)cxo) + (float)ixc;
+            y = gd ? 0.5f * (cyo - cxo) : (float)cyo;
+          }
+        }
+      }
+      const unsigned take = __ballot_sync(0xffffffffu, w > 0.f);
+      if (take && gnum < 0) {
+        gnum = ngroups++;
+        gdiag_bits |= gd << gnum;
+      }
+      if (w > 0.f) {
+        const int o = ns + __popc(take & ((1u << lane) - 1u));
+        if (o < LMA_MAX_SAMPLES) {
+          sx[o] = x; sy[o] = y; sv[o] = v; sw[o] = w;
+          sg[o] = (unsigned char)gnum;
+        }
+      }
+      ns = min(ns + __popc(take), LMA_MAX_SAMPLES);
+    }
+  }
+  __syncwarp();
+  if (ns == 0) return false;
+  // ---- initVector / setWeightsValues ----
+  float wsum = 0.f, gw0 = 0.f, gw1 = 0.f, vmax = -CUDART_INF_F, smax = 0.f;
+  int imx = 1 << 30;
+  for (int n = lane; n < ns; n += 32) {
+    float w = sw[n], v = sv[n];
+    if (sg[n] == 0) gw0 += w; else gw1 += w;
+    if (v > smax) smax = v;
+    if (isnan(v) || isnan(w)) { w = 0.f; v = 0.f; sw[n] = 0.f; sv[n] = 0.f; }
+    wsum += w;
+    if (v > vmax) { vmax = v; imx = n; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {  // first maximum of the sample values
+    const float ov = __shfl_xor_sync(0xffffffffu, vmax, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, imx, o);
+    if (ov > vmax || (ov == vmax && oi < imx)) { vmax = ov; imx = oi; }
+  }
+  wsum = warp_sum(wsum);
+  gw0 = warp_sum(gw0);
+  gw1 = warp_sum(gw1);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) smax = fmaxf(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+  const float pure = wsum;
+  const float tot = wsum + c.cost_wy + c.cost_wxy;
+  const float inv = (tot != 0.f) ? 1.0f / tot : 1.0f;
+  for (int n = lane; n < ns; n += 32) sw[n] *= inv;
+  __syncwarp();
+  const float w_wm = c.cost_wy * inv, w_wxy = c.cost_wxy * inv;
+  const float gwt[2] = {pure > 0.f ? gw0 / pure : gw0, pure > 0.f ? gw1 / pure : gw1};
+  const bool mask[LMA_NP] = {true, c.adjust_wm != 0, c.adjust_wy != 0, c.adjust_wxy != 0,
+                             c.adjust_ag != 0 && ngroups > 0, c.adjust_ag != 0 && ngroups > 1};
+  float av[LMA_NP] = {xcenter, c.half_width, 0.f, 0.f, vmax, vmax};
+  if (ngroups < 2) av[5] = 0.f;
+  // ---- runLma / lmaStep ----
+  // acc: normal equations at the accepted parameters; trial: at the proposed ones
+  lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, av, w_wm, w_wxy, c.half_width, red, acc, lane);
+  float last = sqrtf(acc[27]);
+  const float initial = last;
+  float lambda = c.lambda_initial;
+  bool success = false;
+  for (int iter = 0; iter < c.num_iter; iter++) {
+    // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held (identity rows).
+    // The matrix is symmetric positive (semi)definite: LDL^T without pivoting; a pivot that is
+    // not positive marks it singular, as the zero pivot of the reference's LU inverse does.
+    float M[LMA_NP][LMA_NP], rhs[LMA_NP];
+    {
+      int k = 0;
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++)
+#pragma unroll
+        for (int cc = a; cc < LMA_NP; cc++) {
+          const bool keep = mask[a] && mask[cc];
+          const float v = keep ? acc[k] : ((a == cc) ? 1.0f : 0.0f);
+          M[a][cc] = v;
+          M[cc][a] = v;
+          k++;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < LMA_NP; a++) {
+      if (mask[a]) M[a][a] += M[a][a] * lambda;
+      rhs[a] = mask[a] ? acc[21 + a] : 0.0f;
+    }
+    float Lm[LMA_NP][LMA_NP], Dd[LMA_NP], Dinv[LMA_NP];
+    bool singular = false;
+#pragma unroll
+    for (int r = 0; r < LMA_NP; r++) {
+#pragma unroll
+      for (int cc = 0; cc < r; cc++) {
+        float t = M[r][cc];
+#pragma unroll
+        for (int k = 0; k < cc; k++) t -= Lm[r][k] * Lm[cc][k] * Dd[k];
+        Lm[r][cc] = t * Dinv[cc];
+      }
+      float dd = M[r][r];
+#pragma unroll
+      for (int k = 0; k < r; k++) dd -= Lm[r][k] * Lm[r][k] * Dd[k];
+      if (!(dd > 0.0f)) singular = true;
+      Dd[r] = dd;
+      Dinv[r] = (dd > 0.0f) ? 1.0f / dd : 0.0f;
+    }
+    if (singular) break;
+    float delta[LMA_NP];
+#pragma unroll
+    for (int r = 0; r < LMA_NP; r++) {
+      float t = rhs[r];
+#pragma unroll
+      for (int k = 0; k < r; k++) t -= Lm[r][k] * delta[k];
+      delta[r] = t;
+    }
+#pragma unroll
+    for (int r = LMA_NP - 1; r >= 0; r--) {
+      float t = delta[r] * Dinv[r];
+#pragma unroll
+      for (int k = r + 1; k < LMA_NP; k++) t -= Lm[k][r] * delta[k];
+      delta[r] = t;
+    }
+    float nav[LMA_NP];
+#pragma unroll
+    for (int a = 0; a < LMA_NP; a++) nav[a] = av[a] + (mask[a] ? delta[a] : 0.0f);
+    lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, nav, w_wm, w_wxy, c.half_width, red, trial, lane);
+    const float rms = sqrtf(trial[27]);
+    bool done = false;
+    if (rms < last) {
+      success = true;
+      done = rms >= last * (1.0f - c.rms_diff);
+      last = rms;
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++) av[a] = nav[a];
+      if (lane < LMA_NEQ) acc[lane] = trial[lane];
+      __syncwarp();
+    } else {
+      success = false;
+    }
+    if (done) break;
+    if (success) lambda *= c.lambda_scale_good;
+    else {
+      lambda *= c.lambda_scale_bad;
+      if (lambda > c.lambda_max) break;
+    }
+  }
+  if (!success && last < initial) success = true;
+  if (!success) return false;
+  // ---- getDisparityStrength(Width) ----
+  float sum_amp = gwt[0] * av[4] + (ngroups > 1 ? gwt[1] * av[5] : 0.0f);
+  if (sum_amp > 1.25f * smax) sum_amp = smax;
+  res[0] = -av[0];
+  res[1] = sum_amp;
+  res[2] = av[1];
+  res[3] = av[3];
+  return true;
+}
+
 __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant__ LmaDev ld,
                                                          const __grid_constant__ TpLmaConst c) {
   extern __shared__ float sm[];
@@ -133,323 +484,79 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
   float *sx = gsurf + 450;                                      // samples
   float *sy = sx + LMA_MAX_SAMPLES, *sv = sy + LMA_MAX_SAMPLES, *sw = sv + LMA_MAX_SAMPLES;
   unsigned char *sg = (unsigned char *)(sw + LMA_MAX_SAMPLES);
-  float *red = sx + 4 * LMA_MAX_SAMPLES + LMA_MAX_SAMPLES / 4 + 1;  // [LMA_NEQ][33] transposed partial sums
+  float *red = gsurf + LMA_OFF_RED;                             // [LMA_NEQ][33] transposed partial sums
   float *acc = red + LMA_NEQ * 33, *trial = acc + 32;
-  const int hw = c.cnvx_hwnd_size;
+  float *stage = gsurf + LMA_OFF_STAGE;                         // [P][225] the tile's pair surfaces
+  float *dres = gsurf + LMA_OFF_RES;                            // [4][4] the orientation fits
   for (int task = blockIdx.x * LMA_NW + warp; task < ld.num_tasks; task += gridDim.x * LMA_NW) {
     const int txy = ld.task_txy[task];
     const size_t tile = (size_t)(txy >> 16) * ld.tilesX + (txy & 0xffff);
     float *rec = ld.lma + tile * 4;
     float *dm = ld.disp + tile * TP_NDISP;
-    const float cm = dm[1], strength = dm[2];  // the record's CM disparity and strength
+    const float cm = dm[1], strength0 = dm[2];  // the record's CM disparity and strength
     if (lane < 4) rec[lane] = CUDART_NAN_F;
-    if (isnan(cm) || !(strength > c.min_poly_strength)) continue;
-    const float xcenter = -cm;
-    const int ixc = (int)floorf(xcenter + 0.5f);
-    // ---- group surfaces (combineCompatiblePairs) ----
-    int np_ortho = 0, np_diag = 0;
-    for (int pi = 0; pi < ld.P; pi++) {
-      np_ortho += (ld.kinds[pi] == 0 || ld.kinds[pi] == 1);
-      np_diag += (ld.kinds[pi] == 2 || ld.kinds[pi] == 3);
-    }
-    // The tile's surfaces are contiguous (P x 900 bytes): when they fit they are copied
-    // asynchronously into the (still unused) sample and reduction region, all in flight at once,
-    // in 8-byte pieces when P is even (the tile's offset is then a multiple of 8 bytes).
+    if (isnan(cm) || !(strength0 > c.min_poly_strength)) continue;
+    // The tile's surfaces are contiguous (P x 900 bytes): copied asynchronously, all in flight at
+    // once, in 8-byte pieces when P is even (the tile's offset is then a multiple of 8 bytes).
     const float *src = ld.corr + tile * ld.P * TP_CORR;
-    if (ld.P * TP_CORR <= LMA_STAGE) {
+    if (ld.P <= LMA_STAGE_PAIRS) {
       if ((ld.P & 1) == 0) {
-        for (int k = lane; k < ld.P * TP_CORR / 2; k += 32) cp_async8(sx + 2 * k, src + 2 * k);
+        for (int k = lane; k < ld.P * TP_CORR / 2; k += 32) cp_async8(stage + 2 * k, src + 2 * k);
       } else {
-        for (int k = lane; k < ld.P * TP_CORR; k += 32) cp_async4(sx + k, src + k);
+        for (int k = lane; k < ld.P * TP_CORR; k += 32) cp_async4(stage + k, src + k);
       }
       asm volatile("cp.async.commit_group;\n" ::: "memory");
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       __syncwarp();
-      src = sx;
+      src = stage;
     }
-    // group sums, pairs in index order (combineCompatiblePairs), 8 cells per lane in registers
-    float go[8], gdg[8];
+    // fit 0: all pairs (corrLMA); fits 1-4 with fo_correct: one pair orientation each
+    // (corr4dirsLMA), centred at the (mixed) disparity.  One inlined copy of the fit serves all.
+    float main_res[4] = {0.f, 0.f, 0.f, 0.f};
+    float disparity = cm, strength = strength0, cm_out = cm, str_out = strength0;
+    unsigned valid = 0;
+    bool main_ok = false;
+    for (int f = 0; f < 5; f++) {
+      if (f > 0 && (!c.fo_correct || !(strength > 0.0f))) break;
+      if (f > 0 && ld.kind_count[f - 1] == 0) continue;
+      float res[4];
+      const bool ok = lma_fit(ld, c, f ? 1 << (f - 1) : 0xf, f ? -disparity : -cm, src, gsurf, sx, sy, sv, sw, sg,
+                              red, acc, trial, lane, res);
+      if (f == 0) {
+        if (!ok) break;
+        main_ok = true;
 #pragma unroll
-    for (int t = 0; t < 8; t++) go[t] = gdg[t] = 0.f;
-    for (int pi = 0; pi < ld.P; pi++) {
-      const int k = ld.kinds[pi];
-      if (k < 0) continue;
-      const float *cs = src + pi * TP_CORR;
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int i = lane + 32 * t;
-        if (i < 225) {
-          const int r = i / 15, q = i - r * 15;
-          const float v = (k == 1) ? cs[q * 15 + r] : ((k == 3) ? cs[(14 - r) * 15 + q] : cs[i]);
-          if (k >= 2) gdg[t] += v;
-          else go[t] += v;
+        for (int k = 0; k < 4; k++) main_res[k] = res[k];
+        if (c.mix_corr_poly) {
+          disparity = cm_out = res[0];
+          strength = str_out = res[1];
         }
+      } else if (ok) {
+        valid |= 1u << (f - 1);
+        if (lane < 4) dres[(f - 1) * 4 + lane] = (lane == 0) ? res[0] : ((lane == 1) ? res[1] : ((lane == 2) ? res[2] : res[3]));
       }
     }
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-      const int i = lane + 32 * t;
-      if (i < 225) {
-        gsurf[i] = (np_ortho > 1) ? go[t] / np_ortho : go[t];
-        gsurf[225 + i] = (np_diag > 1) ? gdg[t] / np_diag : gdg[t];
-      }
-    }
+    if (!main_ok) continue;
     __syncwarp();
-    // ---- filterConvex, both groups at once: lanes 0-14 hold the ortho rows, lanes 16-30 the
-    // diagonal rows, as 15-bit masks (bit = column) of the convex and the selected cells ----
-    const int half = lane >> 4, r = lane & 15, hbase = half << 4;
-    const bool rowlane = r < 15 && (half ? np_diag : np_ortho) > 0;
-    const int x0 = ixc + 7, y0 = (half ? ixc : 0) + 7;
-    const int min_row = max(y0 - hw, 0), max_row = min(y0 + hw, 14);
-    const int min_col = max(x0 - hw, 0), max_col = min(x0 + hw, 14);
-    unsigned conv = 0, sel = 0;
-    if (rowlane) {
-      const float *d = gsurf + 225 * half;
-      if (r > min_row && r < max_row)
-        for (int col = min_col + 1; col < max_col; col++) {
-          const int i = r * 15 + col;
-          if ((2 * d[i] > (d[i - 1] + d[i + 1])) && (2 * d[i] > (d[i - 15] + d[i + 15]))) conv |= 1u << col;
-        }
-      if (r == y0 && x0 >= min_col && x0 <= max_col) sel = 1u << x0;
+    if (c.fo_correct && strength > 0.0f) {  // foregroundCorrect (ImageDtt.java:2294-2335)
+      float dd[4][4];
+      bool vb[4];
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        vb[d] = (valid >> d) & 1;
+#pragma unroll
+        for (int k = 0; k < 4; k++) dd[d][k] = dres[d * 4 + k];
+      }
+      const float mod = foreground_correct(c, dd, vb, disparity);
+      if (mod != disparity && strength > c.fo_min_strength) cm_out = mod;
     }
-    {
-      const unsigned lmask = bit_range(min_col + 1, x0), rmask = bit_range(x0, max_col - 1);
-      const unsigned hmask = 0xffffu << hbase;
-      bool active = rowlane;
-      for (int istep = 0; istep < hw; istep++) {
-        const bool first = istep == 0;
-        const int smin_row = max(y0 - istep, 0), smax_row = min(y0 + istep, 14);
-        const unsigned cols = bit_range(max(x0 - istep, 0), min(x0 + istep, 14));
-        unsigned seln = sel;
-        // up / down: the source row's selected cells (convex, or the start) grow into the next row
-        const unsigned src = sel & cols & (first ? 0x7fffu : conv);
-        const bool up_ok = istep < y0, down_ok = (y0 + istep) < max_row;
-        const unsigned s_up = __shfl_sync(0xffffffffu, src, hbase + max(y0 - istep, 0));
-        const unsigned s_dn = __shfl_sync(0xffffffffu, src, hbase + min(y0 + istep, 14));
-        if (up_ok && r == y0 - istep - 1) {
-          const unsigned c1 = s_up & conv;
-          seln |= s_up | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
-        }
-        if (down_ok && r == y0 + istep + 1) {
-          const unsigned c1 = s_dn & conv;
-          seln |= s_dn | ((c1 & lmask) >> 1) | ((c1 & rmask) << 1);
-        }
-        // left / right: the source column's cells grow sideways, and from a convex target up or
-        // down towards the centre row's side
-        unsigned push_up = 0, push_dn = 0;
-        const bool in_rows = r >= smin_row && r <= smax_row;
-#pragma unroll
-        for (int side = 0; side < 2; side++) {
-          const int col = side ? x0 + istep : x0 - istep;
-          const bool ok = side ? ((x0 + istep) < max_col) : (istep < x0);
-          if (!ok || !in_rows || col < 0 || col > 14) continue;
-          const unsigned cb = 1u << col, tb = side ? (cb << 1) : (cb >> 1);
-          if ((sel & cb) && (first || (conv & cb))) {
-            seln |= tb;
-            if (conv & tb) {
-              if (r <= y0 && r > min_row) push_up |= tb;
-              if (r >= y0 && r < max_row) push_dn |= tb;
-            }
-          }
-        }
-        seln |= __shfl_down_sync(0xffffffffu, push_up, 1) | __shfl_up_sync(0xffffffffu, push_dn, 1);
-        if (!rowlane) seln = 0;
-        const unsigned changed = __ballot_sync(0xffffffffu, active && seln != sel) & hmask;
-        if (!changed) active = false;
-        if (active) sel = seln;
-        if (!__any_sync(0xffffffffu, active)) break;
-      }
-    }
-    // ---- samples (addSamples), compacted in the enumeration order ----
-    int ns = 0, ngroups = 0, gdiag_bits = 0;
-    for (int gd = 0; gd < 2; gd++) {
-      const int npg = gd ? np_diag : np_ortho;
-      if (npg == 0) continue;
-      const int base = gd ? LMA_ORTHO_ENTRIES : 0, cnt = gd ? LMA_DIAG_ENTRIES : LMA_ORTHO_ENTRIES;
-      const float *d = gsurf + 225 * gd;
-      int gnum = -1;  // groups are numbered in the order their first sample arrives
-      for (int e0 = 0; e0 < cnt; e0 += 32) {
-        const int e = e0 + lane;
-        float w = 0.f, v = 0.f, x = 0.f, y = 0.f;
-        int cxo = 99, cyo = 99;
-        if (e < cnt) {
-          cxo = __ldg(&g_lma_cx[base + e]);
-          cyo = __ldg(&g_lma_cy[base + e]);
-        }
-        const int cx = cxo + ixc, cy = cyo + (gd ? ixc : 0);
-        const bool inside = e < cnt && cx >= -7 && cx <= 7 && cy >= -7 && cy <= 7;
-        const int srow = inside ? cy + 7 : 0;
-        const unsigned rsel = __shfl_sync(0xffffffffu, sel, (gd << 4) + srow);
-        const unsigned rconv = __shfl_sync(0xffffffffu, conv, (gd << 4) + srow);
-        if (inside) {
-          {
-            const int idx = 112 + 15 * cy + cx, ccol = cx + 7, gy0 = (gd ? ixc : 0) + 7;
-            float wc = 0.f;
-            if ((rsel >> ccol) & 1) wc = ((rconv >> ccol) & 1) ? 1.0f : c.cnvx_weight;
-            else if (c.cnvx_add3x3 && srow >= gy0 - 1 && srow <= gy0 + 1 && ccol >= ixc + 6 && ccol <= ixc + 8)
-              wc = c.cnvx_weight;
-            w = wc * npg;
-            if (w > 0.f) {
-              v = d[idx];
-              if (c.ortho_vasw_pwr == 2.0f) w *= v * v;
-              else if (c.ortho_vasw_pwr != 0.0f) w *= powf(fabsf(v), c.ortho_vasw_pwr);
-              x = (gd ? 0.5f * (cxo + cyo) : (float)cxo) + (float)ixc;
-              y = gd ? 0.5f * (cyo - cxo) : (float)cyo;
-            }
-          }
-        }
-        const unsigned take = __ballot_sync(0xffffffffu, w > 0.f);
-        if (take && gnum < 0) {
-          gnum = ngroups++;
-          gdiag_bits |= gd << gnum;
-        }
-        if (w > 0.f) {
-          const int o = ns + __popc(take & ((1u << lane) - 1u));
-          if (o < LMA_MAX_SAMPLES) {
-            sx[o] = x; sy[o] = y; sv[o] = v; sw[o] = w;
-            sg[o] = (unsigned char)gnum;
-          }
-        }
-        ns = min(ns + __popc(take), LMA_MAX_SAMPLES);
-      }
-    }
-    __syncwarp();
-    if (ns == 0) continue;
-    // ---- initVector / setWeightsValues ----
-    float wsum = 0.f, gw0 = 0.f, gw1 = 0.f, vmax = -CUDART_INF_F, smax = 0.f;
-    int imx = 1 << 30;
-    for (int n = lane; n < ns; n += 32) {
-      float w = sw[n], v = sv[n];
-      if (sg[n] == 0) gw0 += w; else gw1 += w;
-      if (v > smax) smax = v;
-      if (isnan(v) || isnan(w)) { w = 0.f; v = 0.f; sw[n] = 0.f; sv[n] = 0.f; }
-      wsum += w;
-      if (v > vmax) { vmax = v; imx = n; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {  // first maximum of the sample values
-      const float ov = __shfl_xor_sync(0xffffffffu, vmax, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, imx, o);
-      if (ov > vmax || (ov == vmax && oi < imx)) { vmax = ov; imx = oi; }
-    }
-    wsum = warp_sum(wsum);
-    gw0 = warp_sum(gw0);
-    gw1 = warp_sum(gw1);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) smax = fmaxf(smax, __shfl_xor_sync(0xffffffffu, smax, o));
-    const float pure = wsum;
-    const float tot = wsum + c.cost_wy + c.cost_wxy;
-    const float inv = (tot != 0.f) ? 1.0f / tot : 1.0f;
-    for (int n = lane; n < ns; n += 32) sw[n] *= inv;
-    __syncwarp();
-    const float w_wm = c.cost_wy * inv, w_wxy = c.cost_wxy * inv;
-    const float gwt[2] = {pure > 0.f ? gw0 / pure : gw0, pure > 0.f ? gw1 / pure : gw1};
-    const bool mask[LMA_NP] = {true, c.adjust_wm != 0, c.adjust_wy != 0, c.adjust_wxy != 0,
-                               c.adjust_ag != 0 && ngroups > 0, c.adjust_ag != 0 && ngroups > 1};
-    float av[LMA_NP] = {xcenter, c.half_width, 0.f, 0.f, vmax, vmax};
-    if (ngroups < 2) av[5] = 0.f;
-    // ---- runLma / lmaStep ----
-    // acc: normal equations at the accepted parameters; trial: at the proposed ones
-    lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, av, w_wm, w_wxy, c.half_width, red, acc, lane);
-    float last = sqrtf(acc[27]);
-    const float initial = last;
-    float lambda = c.lambda_initial;
-    bool success = false;
-    for (int iter = 0; iter < c.num_iter; iter++) {
-      // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held (identity rows).
-      // The matrix is symmetric positive (semi)definite: LDL^T without pivoting; a pivot that is
-      // not positive marks it singular, as the zero pivot of the reference's LU inverse does.
-      float M[LMA_NP][LMA_NP], rhs[LMA_NP];
-      {
-        int k = 0;
-#pragma unroll
-        for (int a = 0; a < LMA_NP; a++)
-#pragma unroll
-          for (int cc = a; cc < LMA_NP; cc++) {
-            const bool keep = mask[a] && mask[cc];
-            const float v = keep ? acc[k] : ((a == cc) ? 1.0f : 0.0f);
-            M[a][cc] = v;
-            M[cc][a] = v;
-            k++;
-          }
-      }
-#pragma unroll
-      for (int a = 0; a < LMA_NP; a++) {
-        if (mask[a]) M[a][a] += M[a][a] * lambda;
-        rhs[a] = mask[a] ? acc[21 + a] : 0.0f;
-      }
-      float Lm[LMA_NP][LMA_NP], Dd[LMA_NP], Dinv[LMA_NP];
-      bool singular = false;
-#pragma unroll
-      for (int r = 0; r < LMA_NP; r++) {
-#pragma unroll
-        for (int cc = 0; cc < r; cc++) {
-          float t = M[r][cc];
-#pragma unroll
-          for (int k = 0; k < cc; k++) t -= Lm[r][k] * Lm[cc][k] * Dd[k];
-          Lm[r][cc] = t * Dinv[cc];
-        }
-        float dd = M[r][r];
-#pragma unroll
-        for (int k = 0; k < r; k++) dd -= Lm[r][k] * Lm[r][k] * Dd[k];
-        if (!(dd > 0.0f)) singular = true;
-        Dd[r] = dd;
-        Dinv[r] = (dd > 0.0f) ? 1.0f / dd : 0.0f;
-      }
-      if (singular) break;
-      float delta[LMA_NP];
-#pragma unroll
-      for (int r = 0; r < LMA_NP; r++) {
-        float t = rhs[r];
-#pragma unroll
-        for (int k = 0; k < r; k++) t -= Lm[r][k] * delta[k];
-        delta[r] = t;
-      }
-#pragma unroll
-      for (int r = LMA_NP - 1; r >= 0; r--) {
-        float t = delta[r] * Dinv[r];
-#pragma unroll
-        for (int k = r + 1; k < LMA_NP; k++) t -= Lm[k][r] * delta[k];
-        delta[r] = t;
-      }
-      float nav[LMA_NP];
-#pragma unroll
-      for (int a = 0; a < LMA_NP; a++) nav[a] = av[a] + (mask[a] ? delta[a] : 0.0f);
-      lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, nav, w_wm, w_wxy, c.half_width, red, trial, lane);
-      const float rms = sqrtf(trial[27]);
-      bool done = false;
-      if (rms < last) {
-        success = true;
-        done = rms >= last * (1.0f - c.rms_diff);
-        last = rms;
-#pragma unroll
-        for (int a = 0; a < LMA_NP; a++) av[a] = nav[a];
-        if (lane < LMA_NEQ) acc[lane] = trial[lane];
-        __syncwarp();
-      } else {
-        success = false;
-      }
-      if (done) break;
-      if (success) lambda *= c.lambda_scale_good;
-      else {
-        lambda *= c.lambda_scale_bad;
-        if (lambda > c.lambda_max) break;
-      }
-    }
-    if (!success && last < initial) success = true;
-    if (!success) continue;
-    // ---- getDisparityStrength ----
-    float sum_amp = gwt[0] * av[4] + (ngroups > 1 ? gwt[1] * av[5] : 0.0f);
-    if (sum_amp > 1.25f * smax) sum_amp = smax;
     if (lane == 0) {
-      rec[0] = -av[0];
-      rec[1] = sum_amp;
-      rec[2] = av[1];
-      rec[3] = av[3];
-      if (c.mix_corr_poly) {
-        dm[1] = -av[0];
-        dm[2] = sum_amp;
-      }
+      rec[0] = main_res[0];
+      rec[1] = main_res[1];
+      rec[2] = main_res[2];
+      rec[3] = main_res[3];
+      dm[1] = cm_out;
+      dm[2] = str_out;
     }
   }
 }
@@ -494,9 +601,11 @@ cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst
   ld.num_tasks = sc.num_tasks;
   ld.tilesX = sc.tilesX;
   ld.P = cc.num_pairs;
+  for (int k = 0; k < 4; k++) ld.kind_count[k] = 0;
   for (int i = 0; i < TP_MAXP; i++) {
     const int k = (i < cc.num_pairs) ? cc.pairs[i].kind : -1;
     ld.kinds[i] = (k >= 0 && k <= 3 && ((c.pair_mask >> i) & 1)) ? k : -1;
+    if (ld.kinds[i] >= 0) ld.kind_count[ld.kinds[i]]++;
   }
   const int bytes = lma_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(lma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);

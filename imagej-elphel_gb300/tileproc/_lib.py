@@ -61,7 +61,10 @@ class TpLmaParams(C.Structure):
                 ("adjust_wm", C.c_int), ("adjust_wy", C.c_int), ("adjust_wxy", C.c_int), ("adjust_ag", C.c_int),
                 ("half_width", C.c_float), ("cost_wy", C.c_float), ("cost_wxy", C.c_float),
                 ("lambda_initial", C.c_float), ("lambda_scale_good", C.c_float), ("lambda_scale_bad", C.c_float),
-                ("lambda_max", C.c_float), ("rms_diff", C.c_float), ("num_iter", C.c_int), ("pair_mask", C.c_int)]
+                ("lambda_max", C.c_float), ("rms_diff", C.c_float), ("num_iter", C.c_int), ("pair_mask", C.c_int),
+                ("fo_correct", C.c_int), ("fo_far", C.c_int), ("fo_ortho", C.c_int), ("fo_min_strength", C.c_float),
+                ("fo_min_eff", C.c_float), ("fo_min_eff_ratio", C.c_float), ("fo_max_hwidth", C.c_float),
+                ("fo_min_diff", C.c_float), ("fo_overcorrection", C.c_float), ("fo_lim_overcorr", C.c_float)]
 
 
 _H = C.c_void_p

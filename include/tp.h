@@ -232,7 +232,8 @@ tp_status tp_get_texture_aux(tp_handle *h, float *aux);
  * by Levenberg-Marquardt.  Output per tile {disparity, strength, half-width
  * WM, WXY} (getDisparityStrengthWidth; NaN where not run or not converged).
  * With mix_corr_poly the result also replaces TP_DISP_CM and TP_DISP_STRENGTH
- * of the disparity record, as the reference does; the pass then needs a new
+ * of the disparity record, and with fo_correct the far/foreground correction
+ * may replace TP_DISP_CM, as the reference does; the pass then needs a new
  * tp_process before it can run again.  Pair kinds 4 (general) do not take
  * part; cnvx_hwnd_size is at most 4.  Defaults: ImageDttParameters.java:32-109. */
 typedef struct {
@@ -247,6 +248,19 @@ typedef struct {
   float lambda_initial, lambda_scale_good, lambda_scale_bad, lambda_max, rms_diff; /* 0.1, 0.5, 8, 100, 0.001 */
   int num_iter;             /* 20 */
   int pair_mask;            /* bit i: pair i takes part (dbg_pair_mask 0x3f) */
+  /* far / foreground correction (corr4dirsLMA + foregroundCorrect, ImageDtt.java:2294-2335):
+   * one more fit per pair orientation; where they disagree by at least fo_min_diff the
+   * largest (fo_far: smallest) disparity replaces TP_DISP_CM */
+  int fo_correct;           /* 1 */
+  int fo_far;               /* 0 */
+  int fo_ortho;             /* 1: the extreme orientations must be orthogonal for the overcorrection */
+  float fo_min_strength;    /* 0.1 */
+  float fo_min_eff;         /* 0.25: strength x (WM - WXY) / (WM + WXY) */
+  float fo_min_eff_ratio;   /* 0.65 */
+  float fo_max_hwidth;      /* 3.0 */
+  float fo_min_diff;        /* 0.2 */
+  float fo_overcorrection;  /* 0.0 */
+  float fo_lim_overcorr;    /* 2.0 */
 } tp_lma_params;
 tp_status tp_default_lma_params(tp_lma_params *p);
 tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream);

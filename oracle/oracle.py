@@ -549,3 +549,39 @@ def corr_lma(corrs, kinds, xcenter, params=None):
     ok = _lma_lib().or_corr_lma(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], float(xcenter),
                                 C.byref(p), _d(out), C.byref(ns))
     return bool(ok), out, ns.value
+
+
+class FoParams(C.Structure):
+    _fields_ = [("fo_correct", C.c_int), ("fo_far", C.c_int), ("fo_ortho", C.c_int),
+                ("fo_min_strength", C.c_double), ("fo_min_eff", C.c_double), ("fo_min_eff_ratio", C.c_double),
+                ("fo_max_hwidth", C.c_double), ("fo_min_diff", C.c_double), ("fo_overcorrection", C.c_double),
+                ("fo_lim_overcorr", C.c_double)]
+
+
+def default_fo_params(**kw):
+    L = _lma_lib()
+    if not getattr(L, "_fo_set", False):
+        L.or_default_fo_params.argtypes = [C.POINTER(FoParams)]
+        L.or_default_fo_params.restype = None
+        L.or_lma_tile.argtypes = [_dp, C.POINTER(C.c_int), C.c_int, C.POINTER(LmaParams), C.POINTER(FoParams), _dp,
+                                  _dp]
+        L.or_lma_tile.restype = C.c_int
+        L._fo_set = True
+    f = FoParams()
+    L.or_default_fo_params(C.byref(f))
+    for k, v in kw.items():
+        setattr(f, k, v)
+    return f
+
+
+def lma_tile(corrs, kinds, cm, strength, params=None, fo=None):
+    """The record update of ImageDtt.java:2254-2335 for one tile -> (ran, {CM, strength, POLY}, main LMA [4])."""
+    fo = fo if fo is not None else default_fo_params()
+    p = params if params is not None else default_lma_params()
+    a = _f64(corrs)
+    k = np.ascontiguousarray(np.asarray(kinds, dtype=np.int32))
+    rec = np.array([cm, strength, np.nan], dtype=np.float64)
+    lma = np.zeros(4)
+    ran = _lma_lib().or_lma_tile(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], C.byref(p), C.byref(fo),
+                                 _d(rec), _d(lma))
+    return bool(ran), rec, lma

@@ -2039,3 +2039,90 @@ int or_corr_lma(const double *corrs, const int *kind, int np, double xcenter, co
   out[3] = L->all_pars[3];
   return 1;
 }
+
+void or_default_fo_params(or_fo_params *f) {
+  /* ImageDttParameters.java:54-63 */
+  f->fo_correct = 1; f->fo_far = 0; f->fo_ortho = 1;
+  f->fo_min_strength = 0.1; f->fo_min_eff = 0.25; f->fo_min_eff_ratio = 0.65; f->fo_max_hwidth = 3.0;
+  f->fo_min_diff = 0.2; f->fo_overcorrection = 0.0; f->fo_lim_overcorr = 2.0;
+}
+
+/* Correlation2d.foregroundCorrect (1663-1749) */
+void or_foreground_correct(int bg, int ortho, const double dir[4][4], const int valid[4], double full_disp,
+                           const or_fo_params *f, double rslt[4]) {
+  double mn = NAN, mx = NAN, eff[4], width_d[4];
+  int imn = -1, imx = -1, strong[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; i++) {
+    width_d[i] = 0.0;
+    if (valid[i]) {
+      if (isnan(mn) || (dir[i][0] < mn)) { mn = dir[i][0]; imn = i; }
+      if (isnan(mx) || (dir[i][0] > mx)) { mx = dir[i][0]; imx = i; }
+      eff[i] = dir[i][1] * (dir[i][2] - dir[i][3]) / (dir[i][2] + dir[i][3]);
+      width_d[i] = dir[i][2] + dir[i][3];
+      strong[i] = (dir[i][1] >= f->fo_min_strength) && (eff[i] >= f->fo_min_eff);
+    } else {
+      eff[i] = NAN;
+    }
+  }
+  const int are_ortho = (imn ^ imx) == 1;
+  double corr = f->fo_overcorrection * (mx - mn);
+  const int isel = bg ? imn : imx, iother = bg ? imx : imn, iortho = isel ^ 1;
+  if ((isel < 0) || !strong[isel]) corr = NAN;
+  else if (width_d[isel] > f->fo_max_hwidth) corr = NAN;
+  else if (eff[isel] / eff[iortho] < f->fo_min_eff_ratio) corr = NAN;
+  else {
+    if (ortho && !are_ortho) corr = 0.0;
+    else if (!strong[iother]) corr = 0.0;
+    if (!(mx >= (mn + f->fo_min_diff))) corr = NAN;
+  }
+  double disp = full_disp;
+  if (!isnan(corr)) {
+    if (bg) {
+      const double lim = full_disp - (full_disp - mn) * f->fo_lim_overcorr;
+      disp = fmax(mn - corr, lim);
+    } else {
+      const double lim = full_disp + (mx - full_disp) * f->fo_lim_overcorr;
+      disp = fmin(mx + corr, lim);
+    }
+  }
+  rslt[0] = disp;
+  rslt[1] = (isel >= 0) ? eff[isel] : 0.0;
+  rslt[2] = mx - mn;
+  rslt[3] = are_ortho ? 1.0 : 0.0;
+}
+
+int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_params *p, const or_fo_params *f,
+                double rec[3], double lma[4]) {
+  lma[0] = lma[1] = lma[2] = lma[3] = NAN;
+  rec[2] = NAN;
+  const double cm = rec[0], strength0 = rec[1];
+  if (isnan(cm) || !(strength0 > p->min_poly_strength)) return 0;
+  double out[4];
+  if (!or_corr_lma(corrs, kind, np, -cm, p, out, NULL)) return 0;
+  memcpy(lma, out, sizeof(out));
+  rec[2] = out[0];
+  double disparity = cm, strength = strength0;
+  if (p->mix_corr_poly) {
+    disparity = out[0];
+    strength = out[1];
+    rec[0] = disparity;
+    rec[1] = strength;
+  }
+  if (f->fo_correct && (strength > 0.0)) {
+    /* corr4dirsLMA: one LMA per pair orientation */
+    double dir[4][4];
+    int valid[4];
+    for (int d = 0; d < 4; d++) {
+      or_lma_params pd = *p;
+      int m = 0;
+      for (int i = 0; i < np; i++)
+        if (((p->pair_mask >> i) & 1) && kind[i] == d) m |= 1 << i;
+      pd.pair_mask = m;
+      valid[d] = m && or_corr_lma(corrs, kind, np, -disparity, &pd, dir[d], NULL);
+    }
+    double mod[4];
+    or_foreground_correct(f->fo_far, f->fo_ortho, (const double(*)[4])dir, valid, disparity, f, mod);
+    if (mod[0] != disparity && f->fo_correct && strength > f->fo_min_strength) rec[0] = mod[0];
+  }
+  return 1;
+}

@@ -231,6 +231,29 @@ void or_filter_convex(const double *corr225, int hwin, int x0c, int y0c, int add
 int or_corr_lma(const double *corrs, const int *kind, int np, double xcenter, const or_lma_params *p,
                 double out[4], int *n_samples);
 
+/* far/foreground correction (ImageDttParameters.java:54-63 defaults) */
+typedef struct {
+  int fo_correct, fo_far, fo_ortho;            /* 1, 0, 1 */
+  double fo_min_strength, fo_min_eff, fo_min_eff_ratio, fo_max_hwidth, fo_min_diff; /* 0.1, 0.25, 0.65, 3.0, 0.2 */
+  double fo_overcorrection, fo_lim_overcorr;   /* 0.0, 2.0 */
+} or_fo_params;
+void or_default_fo_params(or_fo_params *f);
+/* Correlation2d.foregroundCorrect (1663-1749): dir [4][4] rows {disparity, strength, WM, WXY}
+ * (valid[dir] = 0 for a missing direction) -> {disparity, eff strength, max - min, ortho} */
+void or_foreground_correct(int bg, int ortho, const double dir[4][4], const int valid[4], double full_disp,
+                           const or_fo_params *f, double rslt[4]);
+/*
+ * The disparity-record update of ImageDtt.java:2254-2335 for one tile: from the
+ * record's CM disparity and strength, the main LMA (corrLMA over pair_mask),
+ * the mix into CM / strength (mix_corr_poly), then with fo_correct the four
+ * single-direction LMAs (corr4dirsLMA 1591-1645: horizontal, vertical, main
+ * and other diagonal pairs) and foregroundCorrect.  rec [3] = {CM, strength,
+ * POLY} in/out (POLY NaN unless the LMA ran); lma [4] = the main LMA's
+ * {disparity, strength, WM, WXY} (NaN if none).  Returns 1 if the LMA ran.
+ */
+int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_params *p, const or_fo_params *f,
+                double rec[3], double lma[4]);
+
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {
   double min_shot, scale_shot;        /* CLTParameters 10.0, 3.0 */

@@ -50,7 +50,7 @@ def test_lma_matches_oracle(oracle, kind, size):
         tp.setFullFrameImages(np.full(T, 4.0, np.float32))
         tp.process()
         corr, disp = tp.getCorr(), tp.getDisparity()
-        lma = tp.lmaRefine(mix_corr_poly=0)
+        lma = tp.lmaRefine(mix_corr_poly=0, fo_correct=0)
         assert np.array_equal(tp.getDisparity(), disp, equal_nan=True), "mix_corr_poly=0 changed the record"
         errs = _compare(oracle, corr, disp, lma)
         print("%s: LMA |gpu - oracle| median %.2g max %.2g px over %d tiles" % (kind, np.median(errs), errs.max(),
@@ -66,7 +66,7 @@ def test_lma_mix_replaces_cm_and_needs_a_new_forward(oracle):
         tp.setFullFrameImages(np.full(T, 4.0, np.float32))
         tp.process()
         d0 = tp.getDisparity()
-        lma = tp.lmaRefine()
+        lma = tp.lmaRefine(fo_correct=0)
         d1 = tp.getDisparity()
         fit = np.isfinite(lma[:, 0])
         assert fit.sum() > 20
@@ -74,10 +74,40 @@ def test_lma_mix_replaces_cm_and_needs_a_new_forward(oracle):
         assert np.array_equal(d1[fit, oracle.DISP_STRENGTH], lma[fit, 1])
         assert np.array_equal(d1[~fit], d0[~fit], equal_nan=True)
         with pytest.raises(_lib.TpError, match="run tp_process"):
-            tp.lmaRefine()
+            tp.lmaRefine(fo_correct=0)
         tp.process()
         assert np.array_equal(tp.getDisparity(), d0, equal_nan=True)
         tp.lmaRefine()
+
+
+@pytest.mark.parametrize("kind,size", [("quad_mono", (128, 96)), ("quad_bayer", (128, 96))])
+def test_lma_record_update_matches_oracle(oracle, kind, size):
+    """Default settings: the LMA mixed into CM / strength and the far/foreground correction
+    (four orientation fits + foregroundCorrect) applied to CM, as ImageDtt.java:2254-2335 does.
+    Oracle on the GPU's surfaces and record; CM within 0.005 px and strength within 1e-3 relative
+    on >= 97% of the refined tiles (the correction's threshold tests may fall either side in FP32)."""
+    sc = synth.make_scene(kind, seed=44, width=size[0], height=size[1])
+    T = (size[0] // 8) * (size[1] // 8)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        corr, d0 = tp.getCorr(), tp.getDisparity()
+        lma = tp.lmaRefine()
+        d1 = tp.getDisparity()
+    n = ok = moved = 0
+    for t in range(T):
+        ran, rec, lm = oracle.lma_tile(corr[t].astype(np.float64), KINDS, float(d0[t, oracle.DISP_CM]),
+                                       float(d0[t, oracle.DISP_STRENGTH]))
+        if not ran:
+            continue
+        n += 1
+        moved += rec[0] != lm[0]
+        ok += (abs(d1[t, oracle.DISP_CM] - rec[0]) <= 0.005 and
+               abs(d1[t, oracle.DISP_STRENGTH] - rec[1]) <= 1e-3 * abs(rec[1]) + 1e-6)
+    assert n > 20 and moved > 0
+    assert ok >= 0.97 * n, "record agrees on %d of %d tiles (%d moved by the foreground correction)" % (ok, n, moved)
+    print("%s: record agrees on %d of %d tiles, %d moved by the foreground correction" % (kind, ok, n, moved))
 
 
 def test_lma_rejects_general_pairs(oracle):

@@ -50,3 +50,23 @@ def test_lma_without_diagonal_pairs_uses_one_group():
     p = O.default_lma_params(pair_mask=0x0f)
     ok, out, ns = O.corr_lma(_model_surfaces(0.8), KINDS, 1.0, p)
     assert ok and abs(out[0] + 0.8) < 2e-3 and abs(out[1] - 0.6) < 1e-2
+
+
+def test_foreground_correct_picks_the_nearest_strong_orientation():
+    f = O.default_fo_params()
+    # horizontal and vertical strong and narrow, 0.6 px apart: the larger disparity wins (fo_far = 0)
+    dirs = np.array([[1.0, 0.8, 1.0, 0.1], [1.6, 0.7, 1.0, 0.1], [1.2, 0.5, 1.0, 0.1], [1.3, 0.5, 1.0, 0.1]])
+    out = np.zeros(4)
+    L = O._lma_lib()
+    O.default_fo_params()
+    L.or_foreground_correct.argtypes = [O.C.c_int, O.C.c_int, O._dp, O.C.POINTER(O.C.c_int), O.C.c_double,
+                                        O.C.POINTER(O.FoParams), O._dp]
+    L.or_foreground_correct.restype = None
+    valid = (O.C.c_int * 4)(1, 1, 1, 1)
+    d = np.ascontiguousarray(dirs)
+    L.or_foreground_correct(0, 1, O._d(d), valid, 1.3, O.C.byref(f), O._d(out))
+    assert out[0] == 1.6 and out[3] == 1.0
+    # the extreme orientation too wide in disparity: no correction
+    d[1, 2] = 3.5
+    L.or_foreground_correct(0, 1, O._d(d), valid, 1.3, O.C.byref(f), O._d(out))
+    assert out[0] == 1.3
