@@ -49,6 +49,9 @@ struct tp_handle {
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
   float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
+  float *d_mismatch = nullptr;  // [tiles][pairs][3] lazy-eye mismatch of the last LMA pass that measured it
+  size_t mismatch_cap = 0;
+  int mismatch_pairs = -1;
   int disp_mixed = 0;        // the LMA replaced CM / strength since the last forward
   size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
@@ -411,7 +414,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
-                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma,
+                  h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
                   h->d_rig_rec};
   for (void *b : bufs) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1157,6 +1160,9 @@ tp_status tp_default_lma_params(tp_lma_params *p) {
   p->fo_min_diff = 0.2f;
   p->fo_overcorrection = 0.0f;
   p->fo_lim_overcorr = 2.0f;
+  p->mismatch = 0;
+  p->max_corr_radius = 3.9f;
+  p->mismatch_max_diff = 1.0f;
   return TP_OK;
 }
 
@@ -1216,9 +1222,34 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   c.fo_min_diff = prm.fo_min_diff;
   c.fo_overcorrection = prm.fo_overcorrection;
   c.fo_lim_overcorr = prm.fo_lim_overcorr;
-  CK(launch_lma(scene_of(h), h->corr_host, c, h->d_lma, st), "tp_lma_refine");
+  c.mismatch = prm.mismatch;
+  c.max_corr_radius = prm.max_corr_radius;
+  c.mismatch_max_diff = prm.mismatch_max_diff;
+  if (prm.mismatch) {
+    const size_t need = (size_t)h->ntiles * h->num_pairs * 3;
+    if (need > h->mismatch_cap) {
+      cudaFree(h->d_mismatch);
+      h->d_mismatch = nullptr;
+      h->mismatch_cap = 0;
+      if (dalloc(&h->d_mismatch, need) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, TP_ERR_NOMEM, "tp_lma_refine: mismatch buffer");
+      }
+      h->mismatch_cap = need;
+    }
+    h->mismatch_pairs = h->num_pairs;
+  }
+  CK(launch_lma(scene_of(h), h->corr_host, c, h->d_lma, prm.mismatch ? h->d_mismatch : nullptr, st),
+     "tp_lma_refine");
   if (prm.mix_corr_poly || prm.fo_correct) h->disp_mixed = 1;
   return TP_OK;
+}
+
+tp_status tp_get_lma_mismatch(tp_handle *h, float *out) {
+  if (!h || !out) return TP_ERR_ARG;
+  if (!h->d_mismatch || h->mismatch_pairs != h->num_pairs)
+    return fail(h, TP_ERR_STATE, "tp_get_lma_mismatch: run tp_lma_refine with mismatch set first");
+  return d2h(h, out, h->d_mismatch, (size_t)h->ntiles * h->num_pairs * 3 * sizeof(float), "tp_get_lma_mismatch");
 }
 
 tp_status tp_get_lma(tp_handle *h, float *out) {

@@ -179,9 +179,12 @@ struct TpLmaConst {
   int fo_correct, fo_far, fo_ortho;
   float fo_min_strength, fo_min_eff, fo_min_eff_ratio, fo_max_hwidth, fo_min_diff, fo_overcorrection,
       fo_lim_overcorr;
+  int mismatch;
+  float max_corr_radius, mismatch_max_diff;
 };
 cudaError_t upload_lma_constants();
-cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out, cudaStream_t st);
+cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out,
+                       float *mismatch_out, cudaStream_t st);
 cudaError_t launch_kernel_prep(const float *psf_dev, int nk, int normalize, float *clt_out, float *ext_out,
                                cudaStream_t st);
 cudaError_t launch_fill_coord_corr(float *ext, int kh, int kv, int C, int kern_step, cudaStream_t st);

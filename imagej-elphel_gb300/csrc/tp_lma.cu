@@ -56,6 +56,7 @@ struct LmaDev {
   const float *corr;   // [tiles][P][225]
   float *disp;         // [tiles][TP_NDISP]
   float *lma;          // [tiles][4]
+  float *mismatch;     // [tiles][P][3] lazy-eye mismatch, or null
   const int *task_txy;
   int num_tasks, tilesX, P;
   int kinds[TP_MAXP];  // pair kind or -1 when the pair does not take part
@@ -65,7 +66,7 @@ struct LmaDev {
 // Correlation2d.foregroundCorrect (Correlation2d.java:1663-1749) on the four orientation fits
 // (rows {disparity, strength, WM, WXY}); returns the corrected disparity (full_disp if none)
 __device__ __forceinline__ float foreground_correct(const TpLmaConst &c, const float dir[4][4], const bool valid[4],
-                                                   float full_disp) {
+                                                   float full_disp, float &spread) {
   float mn = CUDART_NAN_F, mx = CUDART_NAN_F, eff[4], width_d[4];
   int imn = -1, imx = -1;
   bool strong[4];
@@ -107,7 +108,39 @@ __device__ __forceinline__ float foreground_correct(const TpLmaConst &c, const f
     if (c.fo_far) disp = fmaxf(mn - corr, full_disp - (full_disp - mn) * c.fo_lim_overcorr);
     else disp = fminf(mx + corr, full_disp + (mx - full_disp) * c.fo_lim_overcorr);
   }
+  spread = mx - mn;
   return disp;
+}
+
+// Correlation2d.mismatchPairsCM (Correlation2d.java:1336-1431) for one pair of quad kind k:
+// centre of mass of the positive cells within the radius around the pair's expected peak
+__device__ __forceinline__ void mismatch_cm(const float *cs, int k, float xcenter, float radius, float out[3]) {
+  const int ixc = (int)floorf(xcenter + 0.5f);
+  const int icx = (k == 1) ? 0 : ixc, icy = (k == 0) ? 0 : ((k == 3) ? -ixc : ixc);
+  const int iradius = (int)fabsf(radius), ir2 = (int)(radius * radius);
+  const bool square = radius < 0.f;
+  float s0 = 0.f, sx = 0.f, sy = 0.f;
+  for (int y = -iradius; y <= iradius; y++) {
+    const int dy = icy + y;
+    if (dy < -7 || dy > 7) continue;
+    for (int x = -iradius; x <= iradius; x++) {
+      const int dx = icx + x;
+      if (dx >= -7 && dx <= 7 && (square || y * y + x * x <= ir2)) {
+        const float d = cs[112 + dy * 15 + dx];
+        if (d > 0.0f) {
+          s0 += d;
+          sx += d * dx;
+          sy += d * dy;
+        }
+      }
+    }
+  }
+  const float xm = sx / s0, ym = sy / s0;
+  const int ixm = isnan(xm) ? 0 : (int)floorf(xm + 0.5f), iym = isnan(ym) ? 0 : (int)floorf(ym + 0.5f);
+  const float sv = cs[112 + iym * 15 + ixm];
+  out[0] = (k == 1) ? -xm : xcenter - xm;
+  out[1] = (k == 0) ? -ym : ((k == 3) ? -xcenter - ym : xcenter - ym);
+  out[2] = sv;
 }
 
 // bits a..b (inclusive) of a row mask, none when b < a
@@ -495,6 +528,8 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
     float *dm = ld.disp + tile * TP_NDISP;
     const float cm = dm[1], strength0 = dm[2];  // the record's CM disparity and strength
     if (lane < 4) rec[lane] = CUDART_NAN_F;
+    if (ld.mismatch)  // {NaN, NaN, 0} unless measured below
+      for (int i = lane; i < 3 * ld.P; i += 32) ld.mismatch[tile * 3 * ld.P + i] = (i % 3 == 2) ? 0.f : CUDART_NAN_F;
     if (isnan(cm) || !(strength0 > c.min_poly_strength)) continue;
     // The tile's surfaces are contiguous (P x 900 bytes): copied asynchronously, all in flight at
     // once, in 8-byte pieces when P is even (the tile's offset is then a multiple of 8 bytes).
@@ -516,8 +551,9 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
     float disparity = cm, strength = strength0, cm_out = cm, str_out = strength0;
     unsigned valid = 0;
     bool main_ok = false;
+    const bool mism = ld.mismatch != nullptr;
     for (int f = 0; f < 5; f++) {
-      if (f > 0 && (!c.fo_correct || !(strength > 0.0f))) break;
+      if (f > 0 && !((c.fo_correct && strength > 0.0f) || mism)) break;
       if (f > 0 && ld.kind_count[f - 1] == 0) continue;
       float res[4];
       const bool ok = lma_fit(ld, c, f ? 1 << (f - 1) : 0xf, f ? -disparity : -cm, src, gsurf, sx, sy, sv, sw, sg,
@@ -538,7 +574,7 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
     }
     if (!main_ok) continue;
     __syncwarp();
-    if (c.fo_correct && strength > 0.0f) {  // foregroundCorrect (ImageDtt.java:2294-2335)
+    if ((c.fo_correct && strength > 0.0f) || mism) {  // foregroundCorrect (ImageDtt.java:2294-2418)
       float dd[4][4];
       bool vb[4];
 #pragma unroll
@@ -547,8 +583,18 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
 #pragma unroll
         for (int k = 0; k < 4; k++) dd[d][k] = dres[d * 4 + k];
       }
-      const float mod = foreground_correct(c, dd, vb, disparity);
-      if (mod != disparity && strength > c.fo_min_strength) cm_out = mod;
+      float spread;
+      const float mod = foreground_correct(c, dd, vb, disparity, spread);
+      // the corrected distance is not used while the mismatch is measured
+      if (!mism && c.fo_correct && mod != disparity && strength > c.fo_min_strength) cm_out = mod;
+      if (mism && spread <= c.mismatch_max_diff && lane < ld.P && ld.kinds[lane] >= 0) {
+        float m3[3];
+        mismatch_cm(src + lane * TP_CORR, ld.kinds[lane], -disparity, c.max_corr_radius, m3);
+        float *mo = ld.mismatch + (tile * ld.P + lane) * 3;
+        mo[0] = m3[0];
+        mo[1] = m3[1];
+        mo[2] = m3[2];
+      }
     }
     if (lane == 0) {
       rec[0] = main_res[0];
@@ -590,13 +636,24 @@ cudaError_t upload_lma_constants() {
 
 int lma_smem_bytes() { return LMA_NW * LMA_PER_WARP * 4; }
 
-cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out, cudaStream_t st) {
+__global__ void mismatch_init_kernel(float *m, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) m[i] = (i % 3 == 2) ? 0.f : CUDART_NAN_F;
+}
+
+cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out,
+                       float *mismatch_out, cudaStream_t st) {
+  if (mismatch_out) {  // tiles without a task keep {NaN, NaN, 0}
+    const int n = sc.tilesX * sc.tilesY * cc.num_pairs * 3;
+    mismatch_init_kernel<<<(n + 255) / 256, 256, 0, st>>>(mismatch_out, n);
+  }
   if (sc.num_tasks <= 0) return cudaSuccess;
   if (c.cnvx_hwnd_size < 0 || c.cnvx_hwnd_size > 4) return cudaErrorInvalidValue;  // 9x9 sample window
   LmaDev ld;
   ld.corr = sc.corr;
   ld.disp = sc.disp;
   ld.lma = lma_out;
+  ld.mismatch = mismatch_out;
   ld.task_txy = sc.task_txy;
   ld.num_tasks = sc.num_tasks;
   ld.tilesX = sc.tilesX;

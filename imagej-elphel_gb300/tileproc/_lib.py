@@ -64,7 +64,8 @@ class TpLmaParams(C.Structure):
                 ("lambda_max", C.c_float), ("rms_diff", C.c_float), ("num_iter", C.c_int), ("pair_mask", C.c_int),
                 ("fo_correct", C.c_int), ("fo_far", C.c_int), ("fo_ortho", C.c_int), ("fo_min_strength", C.c_float),
                 ("fo_min_eff", C.c_float), ("fo_min_eff_ratio", C.c_float), ("fo_max_hwidth", C.c_float),
-                ("fo_min_diff", C.c_float), ("fo_overcorrection", C.c_float), ("fo_lim_overcorr", C.c_float)]
+                ("fo_min_diff", C.c_float), ("fo_overcorrection", C.c_float), ("fo_lim_overcorr", C.c_float),
+                ("mismatch", C.c_int), ("max_corr_radius", C.c_float), ("mismatch_max_diff", C.c_float)]
 
 
 _H = C.c_void_p
@@ -113,6 +114,7 @@ PROTOTYPES = {
     "tp_default_lma_params": [C.POINTER(TpLmaParams)],
     "tp_lma_refine": [_H, C.POINTER(TpLmaParams), _vp],
     "tp_get_lma": [_H, _vp],
+    "tp_get_lma_mismatch": [_H, _vp],
     "tp_rig_correlate": [_H, _H, C.c_float, C.c_int, _vp],
     "tp_get_rig": [_H, _vp, _vp],
     "tp_batch_create": [C.POINTER(_H), C.c_int, C.POINTER(_H)],

@@ -286,6 +286,12 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_lma_refine(self.h, C.byref(params), stream), "tp_lma_refine")
         return self.getLma()
 
+    def getLmaMismatch(self):
+        """[tiles][pairs][3] lazy-eye mismatch {dx, dy, strength} of the last lmaRefine(mismatch=1)."""
+        out = np.zeros((self.tilesY * self.tilesX, self.num_pairs, 3), dtype=np.float32)
+        self._ck(self._lib.tp_get_lma_mismatch(self.h, _ptr(out)), "tp_get_lma_mismatch")
+        return out
+
     def getLma(self):
         out = np.zeros((self.tilesY * self.tilesX, 4), dtype=np.float32)
         self._ck(self._lib.tp_get_lma(self.h, _ptr(out)), "tp_get_lma")

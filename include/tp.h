@@ -261,11 +261,21 @@ typedef struct {
   float fo_min_diff;        /* 0.2 */
   float fo_overcorrection;  /* 0.0 */
   float fo_lim_overcorr;    /* 2.0 */
+  /* lazy-eye mismatch (clt_mismatch, ImageDtt.java:2340-2418; off by default as there): the
+   * orientation fits always run, the foreground correction is not applied to TP_DISP_CM, and
+   * where the fits agree to mismatch_max_diff every pair's peak centre of mass within
+   * max_corr_radius of the disparity (Correlation2d.mismatchPairsCM) goes to tp_get_lma_mismatch */
+  int mismatch;             /* 0 */
+  float max_corr_radius;    /* 3.9 (EyesisCorrectionParameters) */
+  float mismatch_max_diff;  /* 1.0 */
 } tp_lma_params;
 tp_status tp_default_lma_params(tp_lma_params *p);
 tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream);
 /* out [tilesY*tilesX][4] */
 tp_status tp_get_lma(tp_handle *h, float *out);
+/* out [tilesY*tilesX][num_pairs][3] = {dx, dy, strength} per pair (NaN, NaN, 0 where not measured),
+ * after tp_lma_refine with mismatch set */
+tp_status tp_get_lma_mismatch(tp_handle *h, float *out);
 
 /* ---- rig: main and auxiliary quad cameras (ImageDtt.clt_bi_quad, ImageDtt.java:8731-) ----
  * Inter-camera correlation of the sensor-averaged CLT of each camera

@@ -585,3 +585,23 @@ def lma_tile(corrs, kinds, cm, strength, params=None, fo=None):
     ran = _lma_lib().or_lma_tile(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], C.byref(p), C.byref(fo),
                                  _d(rec), _d(lma))
     return bool(ran), rec, lma
+
+
+def lma_tile_mismatch(corrs, kinds, cm, strength, max_corr_radius=3.9, mismatch_max_diff=1.0, params=None, fo=None):
+    """lma_tile with the lazy-eye mismatch -> (ran, {CM, strength, POLY}, main LMA [4], mismatch [np][3])."""
+    fo = fo if fo is not None else default_fo_params()
+    p = params if params is not None else default_lma_params()
+    L = _lma_lib()
+    if not getattr(L, "_mism_set", False):
+        L.or_lma_tile_mismatch.argtypes = [_dp, C.POINTER(C.c_int), C.c_int, C.POINTER(LmaParams),
+                                           C.POINTER(FoParams), C.c_double, C.c_double, _dp, _dp, _dp]
+        L.or_lma_tile_mismatch.restype = C.c_int
+        L._mism_set = True
+    a = _f64(corrs)
+    k = np.ascontiguousarray(np.asarray(kinds, dtype=np.int32))
+    rec = np.array([cm, strength, np.nan], dtype=np.float64)
+    lma = np.zeros(4)
+    mism = np.zeros((a.shape[0], 3))
+    ran = L.or_lma_tile_mismatch(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], C.byref(p), C.byref(fo),
+                                 float(max_corr_radius), float(mismatch_max_diff), _d(rec), _d(lma), _d(mism))
+    return bool(ran), rec, lma, mism

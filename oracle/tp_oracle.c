@@ -2091,10 +2091,46 @@ void or_foreground_correct(int bg, int ortho, const double dir[4][4], const int 
   rslt[3] = are_ortho ? 1.0 : 0.0;
 }
 
-int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_params *p, const or_fo_params *f,
-                double rec[3], double lma[4]) {
+/* Correlation2d.mismatchPairsCM (1336-1431) for one pair of quad kind k: {dx, dy, strength} */
+static void or_mismatch_cm_pair(const double *c, int k, double xcenter, double radius, double out[3]) {
+  const int W = OR_CORR, center = OR_DTT - 1, center_index = (W + 1) * center;
+  const int ixc = (int)floor(xcenter + 0.5);
+  int icx, icy;
+  if (k == 0) { icx = ixc; icy = 0; }
+  else if (k == 1) { icx = 0; icy = ixc; }
+  else if (k == 2) { icx = ixc; icy = ixc; }
+  else { icx = ixc; icy = -ixc; }
+  const int iradius = (int)fabs(radius), ir2 = (int)(radius * radius), square = radius < 0;
+  double s0 = 0, sx = 0, sy = 0;
+  for (int y = -iradius; y <= iradius; y++) {
+    const int dy = icy + y;
+    if (dy < -center || dy > center) continue;
+    for (int x = -iradius; x <= iradius; x++) {
+      const int dx = icx + x;
+      const double r2 = y * y + x * x;
+      if (dx >= -center && dx <= center && (square || r2 <= ir2)) {
+        const double d = c[dy * W + dx + center_index];
+        if (d > 0.0) { s0 += d; sx += d * dx; sy += d * dy; }
+      }
+    }
+  }
+  const double xm = sx / s0, ym = sy / s0;
+  const int ixm = isnan(xm) ? 0 : (int)floor(xm + 0.5), iym = isnan(ym) ? 0 : (int)floor(ym + 0.5);  /* Math.round */
+  const double sv = c[iym * W + ixm + center_index];
+  if (k == 0) { out[0] = xcenter - xm; out[1] = -ym; }
+  else if (k == 1) { out[0] = -xm; out[1] = xcenter - ym; }
+  else if (k == 2) { out[0] = xcenter - xm; out[1] = xcenter - ym; }
+  else { out[0] = xcenter - xm; out[1] = -xcenter - ym; }
+  out[2] = sv;
+}
+
+int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_lma_params *p,
+                         const or_fo_params *f, double max_corr_radius, double mismatch_max_diff, double rec[3],
+                         double lma[4], double *mism) {
   lma[0] = lma[1] = lma[2] = lma[3] = NAN;
   rec[2] = NAN;
+  if (mism)
+    for (int i = 0; i < np; i++) { mism[3 * i] = NAN; mism[3 * i + 1] = NAN; mism[3 * i + 2] = 0.0; }
   const double cm = rec[0], strength0 = rec[1];
   if (isnan(cm) || !(strength0 > p->min_poly_strength)) return 0;
   double out[4];
@@ -2108,7 +2144,7 @@ int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_param
     rec[0] = disparity;
     rec[1] = strength;
   }
-  if (f->fo_correct && (strength > 0.0)) {
+  if ((f->fo_correct && (strength > 0.0)) || mism) {
     /* corr4dirsLMA: one LMA per pair orientation */
     double dir[4][4];
     int valid[4];
@@ -2122,7 +2158,18 @@ int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_param
     }
     double mod[4];
     or_foreground_correct(f->fo_far, f->fo_ortho, (const double(*)[4])dir, valid, disparity, f, mod);
-    if (mod[0] != disparity && f->fo_correct && strength > f->fo_min_strength) rec[0] = mod[0];
+    /* the corrected distance is not used while the mismatch is measured */
+    if (mod[0] != disparity && !mism && f->fo_correct && strength > f->fo_min_strength) rec[0] = mod[0];
+    if (mism && mod[2] <= mismatch_max_diff)
+      for (int i = 0; i < np; i++)
+        if (((p->pair_mask >> i) & 1) && kind[i] >= 0 && kind[i] <= 3)
+          or_mismatch_cm_pair(corrs + (size_t)i * OR_CORR * OR_CORR, kind[i], -disparity, max_corr_radius,
+                              mism + 3 * i);
   }
   return 1;
+}
+
+int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_params *p, const or_fo_params *f,
+                double rec[3], double lma[4]) {
+  return or_lma_tile_mismatch(corrs, kind, np, p, f, 3.9, 1.0, rec, lma, NULL);
 }

@@ -253,6 +253,13 @@ void or_foreground_correct(int bg, int ortho, const double dir[4][4], const int 
  */
 int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_params *p, const or_fo_params *f,
                 double rec[3], double lma[4]);
+/* the same with the lazy-eye mismatch (clt_mismatch, ImageDtt.java:2340-2418): when mism is not
+ * NULL the orientation fits always run, CM is not foreground-corrected, and where their spread is
+ * at most mismatch_max_diff mism [np][3] receives mismatchPairsCM (Correlation2d.java:1336-1431)
+ * around the disparity with max_corr_radius (3.9); elsewhere {NaN, NaN, 0} */
+int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_lma_params *p,
+                         const or_fo_params *f, double max_corr_radius, double mismatch_max_diff, double rec[3],
+                         double lma[4], double *mism);
 
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {

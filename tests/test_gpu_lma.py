@@ -110,6 +110,36 @@ def test_lma_record_update_matches_oracle(oracle, kind, size):
     print("%s: record agrees on %d of %d tiles, %d moved by the foreground correction" % (kind, ok, n, moved))
 
 
+def test_lma_mismatch_matches_oracle(oracle):
+    """Lazy-eye mismatch (ImageDtt.java:2340-2418, Correlation2d.mismatchPairsCM): per pair the peak's
+    centre of mass around the LMA disparity, where the four orientation fits agree to 1 px; the
+    record's CM keeps the LMA value (no foreground correction while measuring).  Oracle on the GPU's
+    surfaces and record; {dx, dy, strength} within 1e-3 on >= 97% of the refined tiles."""
+    sc = synth.make_scene("quad_mono", seed=45, width=128, height=96)
+    T = 16 * 12
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        corr, d0 = tp.getCorr(), tp.getDisparity()
+        tp.lmaRefine(mismatch=1)
+        d1, mm = tp.getDisparity(), tp.getLmaMismatch()
+    n = ok = measured = 0
+    for t in range(T):
+        ran, rec, lm, om = oracle.lma_tile_mismatch(corr[t].astype(np.float64), KINDS, float(d0[t, oracle.DISP_CM]),
+                                                    float(d0[t, oracle.DISP_STRENGTH]))
+        if not ran:
+            assert np.all(np.isnan(mm[t, :, :2])) and np.all(mm[t, :, 2] == 0)
+            continue
+        n += 1
+        measured += bool(np.isfinite(om[:, 0]).all())
+        same = np.allclose(mm[t], om, atol=1e-3, equal_nan=True) and abs(d1[t, oracle.DISP_CM] - rec[0]) <= 0.005
+        ok += same
+    assert n > 20 and measured > 0.5 * n
+    assert ok >= 0.97 * n, "mismatch agrees on %d of %d tiles" % (ok, n)
+    print("mismatch: agrees on %d of %d tiles, measured on %d" % (ok, n, measured))
+
+
 def test_lma_rejects_general_pairs(oracle):
     from tileproc import _lib
     sc = synth.make_scene("circle_lwir", seed=43, width=64, height=64)
