@@ -30,7 +30,6 @@
 
 namespace {
 
-constexpr int FW_MAX_WARPS = 16;
 constexpr int SCR = 288;           // per-warp scratch floats: [4][8][9] transpose / surface buffer
 
 // ---------------------------------------------------------------------------

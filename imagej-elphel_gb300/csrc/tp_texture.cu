@@ -35,11 +35,6 @@ __constant__ float k_rhwin[8];      // 1 / sine half-window
 // distances (ImageDtt.java:1564-1569)
 __constant__ float k_port_off[4][2] = {{-0.5f, -0.5f}, {0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, 0.5f}};
 
-// ImageDtt.kern_rb / kern_g (43-50): tap dr of the 3x3 debayer kernel (corners, sides, centre)
-__device__ __forceinline__ constexpr float kern_tap(bool rb, int dr) {
-  return (dr == 4) ? (rb ? 0.25f : 0.5f) : ((dr & 1) ? 0.125f : (rb ? 0.0625f : 0.f));
-}
-
 }  // namespace
 
 // Per-pixel stage of a tile (debayer, shot noise, port weights, dust removal, alpha, RGB mix);
