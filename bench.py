@@ -83,6 +83,16 @@ def dist_init(world, use_cuda):
     return dist
 
 
+def max_over_ranks(seconds, dist, device="cuda"):
+    """The slowest rank's time (replicas: the job ends with its last rank); identity without dist."""
+    if not dist:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_workload(cfg_name, seed, rank=0):
     from tileproc import synth
     c = CONFIGS[cfg_name]
@@ -510,10 +520,7 @@ def run_ours(args):
         t1.record(stream)
         torch.cuda.synchronize()
     elapsed = t0.elapsed_time(t1) / 1000.0
-    if dist:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, dist)
     stage_ms = {s: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
                 for i, s in enumerate(stages)}
     value = world * T * args.steps / elapsed
@@ -580,10 +587,7 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - te
-    if dist:
-        t = torch.tensor([e2e_t], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = max_over_ranks(e2e_t, dist)
     e2e_val = world * T * args.steps / e2e_t
 
     batched = batched_small = None
