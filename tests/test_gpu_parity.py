@@ -270,3 +270,29 @@ def test_bayer_planes_input_matches_mosaic(oracle):
         tp.process()
         got = tp.getClt()
     assert np.array_equal(got, ref)
+
+
+def test_zero_contrast_tiles(oracle):
+    """Flat regions (all zero, all one) with a step edge: tiles without contrast have 0/0 in the
+    fat-zero normalisation, so their surfaces are NaN and they get no disparity, as in the oracle;
+    the tiles on the edge are compared as usual."""
+    sc = synth.make_scene("quad_mono", seed=8, width=64, height=64)
+    sc["images"][:] = 0.0
+    sc["images"][:, 32:, :] = 1.0
+    T = 64
+    ref = run_oracle(oracle, sc, 2.0)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation(fat_zero=0.05)
+        tp.setFullFrameImages(np.full(T, 2.0, np.float32))
+        tp.process()
+        corr = tp.getCorr().astype(np.float64)
+        d = tp.getDisparity()
+    nan_ref, nan_gpu = np.isnan(ref["corr"]), np.isnan(corr)
+    assert nan_ref.any() and np.array_equal(nan_ref, nan_gpu)
+    fin = ~np.isnan(ref["corr"]).any(axis=-1)
+    e = rel_l2(np.where(fin[..., None], corr, 0), np.where(fin[..., None], ref["corr"], 0), axis=-1)[fin]
+    assert e.max() <= CORR_TOL, e.max()
+    cm_ref, cm_gpu = ref["disp"][:, oracle.DISP_CM], d[:, oracle.DISP_CM]
+    assert np.array_equal(np.isnan(cm_ref), np.isnan(cm_gpu))
+    ok = ~np.isnan(cm_ref)
+    assert np.abs(cm_gpu[ok] - cm_ref[ok]).max() <= DISP_TOL
