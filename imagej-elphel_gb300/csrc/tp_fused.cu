@@ -907,12 +907,13 @@ cudaError_t launch_rig(const SceneDev &mn, const SceneDev &ax, const CorrConst &
 // 8-lane group, lane r owning row r of each quadrant.
 // ---------------------------------------------------------------------------
 constexpr int IMCLT_IR = 16;     // region = IR x IR blocks of 8x8 pixels
+constexpr int IMCLT_WARPS = 9;   // 36 8-lane groups: the four parity phases (64, 72, 72, 81 tiles) in 2+2+2+3 rounds
 
 template <int IR>
-__global__ void __launch_bounds__(256) imclt_fast_kernel(const __grid_constant__ SceneDev sc) {
+__global__ void __launch_bounds__(32 * IMCLT_WARPS) imclt_fast_kernel(const __grid_constant__ SceneDev sc) {
   constexpr int IPX = IR * 8, ISTR = IPX + 1;
   extern __shared__ float acc[];  // [IPX][ISTR]
-  __shared__ float tbuf_all[8][4 * 72];
+  __shared__ float tbuf_all[IMCLT_WARPS][4 * 72];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
   const int S = sc.num_sensors, C = sc.num_colors;
   const int plane = blockIdx.z, s = plane / C, c = plane - s * C;
@@ -934,7 +935,7 @@ __global__ void __launch_bounds__(256) imclt_fast_kernel(const __grid_constant__
     if ((tx0 & 1) != pxp) tx0++;
     if ((ty0 & 1) != pyp) ty0++;
     const int ntx = (bx0 + IR - 1 - tx0) / 2 + 1, nty = (by0 + IR - 1 - ty0) / 2 + 1;
-    for (int k0 = warp * 4; k0 < ntx * nty; k0 += 32) {
+    for (int k0 = warp * 4; k0 < ntx * nty; k0 += 4 * IMCLT_WARPS) {
       const int k = k0 + q;
       const int tx = tx0 + 2 * (k % ntx), ty = ty0 + 2 * (k / ntx);
       bool act = k < ntx * nty && tx >= 0 && ty >= 0 && tx < sc.tilesX && ty < sc.tilesY;
@@ -1002,7 +1003,7 @@ cudaError_t launch_imclt_fast(const SceneDev &sc, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(imclt_fast_kernel<IR>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   dim3 grid((sc.tilesX + 1 + IR - 1) / IR, (sc.tilesY + 1 + IR - 1) / IR, sc.num_sensors * sc.num_colors);
-  imclt_fast_kernel<IR><<<grid, 256, bytes, st>>>(sc);
+  imclt_fast_kernel<IR><<<grid, 32 * IMCLT_WARPS, bytes, st>>>(sc);
   return cudaGetLastError();
 }
 
