@@ -1163,6 +1163,9 @@ tp_status tp_default_lma_params(tp_lma_params *p) {
   p->mismatch = 0;
   p->max_corr_radius = 3.9f;
   p->mismatch_max_diff = 1.0f;
+  p->ly_poly = 0;
+  p->ly_crazy_poly = 1.0f;
+  p->ly_poly_backup = 1;
   return TP_OK;
 }
 
@@ -1180,7 +1183,7 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   bool quad = false;
   for (int i = 0; i < h->num_pairs; i++) {
     const int k = h->corr_host.pairs[i].kind;
-    if (k >= 0 && k <= 3 && ((prm.pair_mask >> i) & 1)) quad = true;
+    if (k >= 0 && k <= 3 && i < 32 && ((prm.pair_mask >> i) & 1)) quad = true;
   }
   if (!quad) return fail(h, TP_ERR_ARG, "tp_lma_refine: needs pairs of the quad kinds 0..3");
   cudaStream_t st = pick_stream(h, stream);
@@ -1225,6 +1228,9 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   c.mismatch = prm.mismatch;
   c.max_corr_radius = prm.max_corr_radius;
   c.mismatch_max_diff = prm.mismatch_max_diff;
+  c.ly_poly = prm.ly_poly;
+  c.ly_poly_backup = prm.ly_poly_backup;
+  c.ly_crazy_poly = prm.ly_crazy_poly;
   if (prm.mismatch) {
     const size_t need = (size_t)h->ntiles * h->num_pairs * 3;
     if (need > h->mismatch_cap) {

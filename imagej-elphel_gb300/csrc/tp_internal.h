@@ -181,6 +181,8 @@ struct TpLmaConst {
       fo_lim_overcorr;
   int mismatch;
   float max_corr_radius, mismatch_max_diff;
+  int ly_poly, ly_poly_backup;
+  float ly_crazy_poly;
 };
 cudaError_t upload_lma_constants();
 cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out,

@@ -28,6 +28,8 @@ constexpr int LMA_DIAG_ENTRIES = 145;  // addSamples enumeration, diagonal group
 constexpr int LMA_MAX_SAMPLES = 162;   // 9x9 window cells per group
 constexpr int LMA_NP = 6;              // X0, WM, WYD, WXY, AG0, AG1
 constexpr int LMA_STAGE_PAIRS = 6;     // pair surfaces staged in shared memory (the quad layout's six)
+constexpr int LMA_POLY_CHUNK = 6;      // pairs per polynomial-mismatch pass (one solving lane each)
+constexpr int LMA_POLY_SCRATCH = 48;   // doubles of solver scratch per lane
 
 // sample cell offsets from the (integer) centre, in the reference's enumeration order (global
 // memory: consecutive lanes read consecutive entries)
@@ -51,6 +53,11 @@ constexpr int LMA_OFF_STAGE = ((LMA_OFF_RED + 28 * 33 + 64) + 3) & ~3;
 constexpr int LMA_OFF_RES = LMA_OFF_STAGE + LMA_STAGE_PAIRS * 225;  // [4][4] orientation fits
 constexpr int LMA_PER_WARP = ((LMA_OFF_RES + 16) + 3) & ~3;
 static_assert(LMA_OFF_STAGE % 4 == 0 && LMA_PER_WARP % 4 == 0, "staged surfaces must be 16-byte aligned");
+// polynomial mismatch scratch: moments over the reduction buffer, solver rows over the group
+// surfaces and samples, both 8-byte aligned and clear of the staged surfaces
+static_assert(((LMA_OFF_RED + 1) & ~1) + 2 * 21 * LMA_POLY_CHUNK <= LMA_OFF_STAGE, "moments overlap the stage");
+static_assert(2 * LMA_POLY_SCRATCH * LMA_POLY_CHUNK <= LMA_OFF_RED, "solver scratch overlaps the moments");
+static_assert(LMA_POLY_CHUNK <= 32, "one solving lane per pair");
 
 struct LmaDev {
   const float *corr;   // [tiles][P][225]
@@ -214,17 +221,21 @@ __device__ __forceinline__ void lma_eval(const float *sx, const float *sy, const
 // One Correlation2d.corrLMA fit of a tile from the staged pair surfaces `src` ([P][225]) of the
 // pair kinds in kmask (bit k: kind k), centred at xcenter: res = {disparity, strength, WM, WXY}
 // (getDisparityStrengthWidth); false when there are no samples or the fit did not converge.
-__device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, int kmask, float xcenter,
-                                        const float *src, float *gsurf, float *sx, float *sy, float *sv, float *sw,
-                                        unsigned char *sg, float *red, float *acc, float *trial, int lane,
-                                        float res[4]) {
+// Samples of the pairs in pmask (bit = pair index; pairs of kind -1 never): the group surfaces
+// (combineCompatiblePairs), filterConvex around the integer centre and addSamples with weights
+// x |value|^vasw_pwr, compacted into sx/sy/sv/sw/sg in the reference's order.  Returns the
+// sample count; ngroups / gdiag_bits (bit g: group g is the diagonal one) describe the groups.
+__device__ __forceinline__ int lma_samples(const LmaDev &ld, const TpLmaConst &c, unsigned pmask, float xcenter,
+                                           float vasw_pwr, const float *src, float *gsurf, float *sx, float *sy,
+                                           float *sv, float *sw, unsigned char *sg, int lane, int &ngroups_out,
+                                           int &gdiag_bits_out) {
   const int hw = c.cnvx_hwnd_size;
   const int ixc = (int)floorf(xcenter + 0.5f);
   // ---- group surfaces (combineCompatiblePairs) ----
   int np_ortho = 0, np_diag = 0;
   for (int pi = 0; pi < ld.P; pi++) {
     const int k = ld.kinds[pi];
-    if (k < 0 || !((kmask >> k) & 1)) continue;
+    if (k < 0 || !((pmask >> pi) & 1)) continue;
     np_ortho += (k <= 1);
     np_diag += (k >= 2);
   }
@@ -234,7 +245,7 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
   for (int t = 0; t < 8; t++) go[t] = gdg[t] = 0.f;
   for (int pi = 0; pi < ld.P; pi++) {
     const int k = ld.kinds[pi];
-    if (k < 0 || !((kmask >> k) & 1)) continue;
+    if (k < 0 || !((pmask >> pi) & 1)) continue;
     const float *cs = src + pi * TP_CORR;
 #pragma unroll
     for (int t = 0; t < 8; t++) {
@@ -352,8 +363,8 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
           w = wc * npg;
           if (w > 0.f) {
             v = d[idx];
-            if (c.ortho_vasw_pwr == 2.0f) w *= v * v;
-            else if (c.ortho_vasw_pwr != 0.0f) w *= powf(fabsf(v), c.ortho_vasw_pwr);
+            if (vasw_pwr == 2.0f) w *= v * v;
+            else if (vasw_pwr != 0.0f) w *= powf(fabsf(v), vasw_pwr);
             x = (gd ? 0.5f * (cxo + cyo) : (float)cxo) + (float)ixc;
             y = gd ? 0.5f * (cyo - cxo) : (float)cyo;
           }
@@ -375,6 +386,23 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
     }
   }
   __syncwarp();
+  ngroups_out = ngroups;
+  gdiag_bits_out = gdiag_bits;
+  return ns;
+}
+
+// Correlation2d.corrLMA (1754-1877) on the pairs of the kinds in kmask: samples, then the
+// Levenberg-Marquardt fit; res = {disparity, strength, WM, WXY}
+__device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, int kmask, float xcenter,
+                                        const float *src, float *gsurf, float *sx, float *sy, float *sv, float *sw,
+                                        unsigned char *sg, float *red, float *acc, float *trial, int lane,
+                                        float res[4]) {
+  unsigned pmask = 0;
+  for (int pi = 0; pi < ld.P; pi++)
+    if (ld.kinds[pi] >= 0 && ((kmask >> ld.kinds[pi]) & 1)) pmask |= 1u << pi;
+  int ngroups, gdiag_bits;
+  const int ns = lma_samples(ld, c, pmask, xcenter, c.ortho_vasw_pwr, src, gsurf, sx, sy, sv, sw, sg, lane, ngroups,
+                             gdiag_bits);
   if (ns == 0) return false;
   // ---- initVector / setWeightsValues ----
   float wsum = 0.f, gw0 = 0.f, gw1 = 0.f, vmax = -CUDART_INF_F, smax = 0.f;
@@ -509,6 +537,143 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
   return true;
 }
 
+// Gaussian elimination with partial pivoting (the LU factorisation Jama's Matrix.det / solve use)
+// of a [n][n+1] (matrix | right-hand side, row stride n + 1) in place, by one thread: returns the
+// determinant and leaves the solution in column n.  Multipliers and back substitution use the
+// pivot's reciprocal (FP64 division is a long sequence on this part; the results differ from
+// dividing in the last bits only).
+__device__ double gauss_det_solve(double *a, int n) {
+  const int st = n + 1;
+  double det = 1.0;
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    for (int i = k + 1; i < n; i++)
+      if (fabs(a[i * st + k]) > fabs(a[p * st + k])) p = i;
+    if (p != k) {
+      for (int j = k; j < st; j++) {
+        const double t = a[p * st + j];
+        a[p * st + j] = a[k * st + j];
+        a[k * st + j] = t;
+      }
+      det = -det;
+    }
+    const double piv = a[k * st + k];
+    det *= piv;
+    const double rp = 1.0 / piv;
+    a[k * st + k] = rp;  // the reciprocal, for the back substitution
+    if (piv != 0.0)
+      for (int i = k + 1; i < n; i++) {
+        const double m = a[i * st + k] * rp;
+        for (int j = k + 1; j < st; j++) a[i * st + j] = fma(-m, a[k * st + j], a[i * st + j]);
+      }
+  }
+  for (int k = n - 1; k >= 0; k--) {
+    double x = a[k * st + n];
+    for (int j = k + 1; j < n; j++) x = fma(-a[k * st + j], a[j * st + n], x);
+    a[k * st + n] = x * a[k * st + k];
+  }
+  return det;
+}
+
+// squared product of the row norms of a [n][n] with row stride st (PolynomialApproximation.normMatix
+// squared: the determinant tests |det| / norm < t are taken as det^2 < t^2 norm^2)
+__device__ double row_norm_product_sq(const double *a, int n, int st) {
+  double norm = 1.0;
+  for (int i = 0; i < n; i++) {
+    double d = 0.0;
+    for (int j = 0; j < n; j++) d = fma(a[i * st + j], a[i * st + j], d);
+    norm *= d;
+  }
+  return norm;
+}
+
+// |det| / sqrt(nsq) >= t, with nsq == 0 failing (quadraticApproximation's well-posedness test)
+__device__ __forceinline__ bool det_ok(double det, double nsq, double t) {
+  return nsq != 0.0 && det * det >= t * t * nsq;
+}
+
+// one level of a reduce-scatter: lanes with bit o keep the upper half of v (after their partner's
+// values are added), the others the lower half
+template <int HALF>
+__device__ __forceinline__ void scatter_level(double *v, int lane, int o) {
+  const bool hi = (lane & o) != 0;
+#pragma unroll
+  for (int k = 0; k < HALF; k++) {
+    const double give = hi ? v[k] : v[k + HALF], keep = hi ? v[k + HALF] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, give, o);
+  }
+}
+
+// Weighted moments of the samples for the quadric fit of quadraticApproximation (350-585): S00 S10
+// S01 S20 S11 S02 S30 S21 S12 S03 S40 S31 S22 S13 S04 of the weights, then Z00 Z10 Z01 Z20 Z11
+// Z02 of weight x value; samples with weight <= 0 are skipped.  Per-lane sums in FP64, then a
+// reduce-scatter across the warp (21 values padded to 22 -> 11 -> 12 -> 6 -> 3 -> 4 -> 2 -> 1,
+// 23 additions per lane instead of 105 for a full butterfly): lane 11 b4 + 6 b3 + 3 b2 + 2 b1 + b0
+// (bits of the lane index) ends with that moment, except the lanes that hold a pad; each writes
+// its moment to dst[21].
+__device__ __forceinline__ void quadric_moments(const float *sx, const float *sy, const float *sv, const float *sw,
+                                                int ns, int lane, double *dst) {
+  double m[22];
+#pragma unroll
+  for (int i = 0; i < 22; i++) m[i] = 0.0;
+  for (int n = lane; n < ns; n += 32) {
+    const double w = sw[n];
+    if (!(w > 0.0)) continue;
+    const double x = sx[n], y = sy[n], x2 = x * x, y2 = y * y, wz = w * (double)sv[n];
+    const double x3 = x2 * x, y3 = y2 * y;
+    m[0] += w; m[1] += w * x; m[2] += w * y; m[3] += w * x2; m[4] += w * x * y; m[5] += w * y2;
+    m[6] += w * x3; m[7] += w * x2 * y; m[8] += w * x * y2; m[9] += w * y3;
+    m[10] += w * x3 * x; m[11] += w * x3 * y; m[12] += w * x2 * y2; m[13] += w * x * y3; m[14] += w * y3 * y;
+    m[15] += wz; m[16] += wz * x; m[17] += wz * y; m[18] += wz * x2; m[19] += wz * x * y; m[20] += wz * y2;
+  }
+  m[21] = 0.0;
+  scatter_level<11>(m, lane, 16);
+  m[11] = 0.0;
+  scatter_level<6>(m, lane, 8);
+  scatter_level<3>(m, lane, 4);
+  m[3] = 0.0;
+  scatter_level<2>(m, lane, 2);
+  scatter_level<1>(m, lane, 1);
+  const int b0 = lane & 1, b1 = (lane >> 1) & 1, b2 = (lane >> 2) & 1, b3 = (lane >> 3) & 1, b4 = (lane >> 4) & 1;
+  const int l4 = 2 * b1 + b0, l2 = 6 * b3 + 3 * b2 + l4, idx = 11 * b4 + l2;
+  if (l4 != 3 && l2 != 11 && idx != 21) dst[idx] = m[0];
+}
+
+// Correlations2dLMA.getMaxXYPoly (641-704) from the moments, by one thread in FP64: the quadric
+// A x^2 + B y^2 + C xy + D x + E y + F (quadraticApproximation, with the linear / quadratic
+// determinant-to-norm thresholds 1e-20 / 1e-30 of quadraticMaxV2dX2Y2XY 201-221) and its
+// maximum.  dm: >= 48 doubles of scratch.  Returns false when a test fails or the stationary
+// point is not a maximum with a non-negative value.
+__device__ bool quadric_max(const double *m, int ns, double *dm, double xyv[3]) {
+  if (ns <= 0) return false;
+  const double S00 = m[0], S10 = m[1], S01 = m[2], S20 = m[3], S11 = m[4], S02 = m[5], S30 = m[6], S21 = m[7],
+               S12 = m[8], S03 = m[9], S40 = m[10], S31 = m[11], S22 = m[12], S13 = m[13], S04 = m[14];
+  const double lin[12] = {S20, S11, S10, 0.0, S11, S02, S01, 0.0, S10, S01, S00, 0.0};
+  for (int i = 0; i < 12; i++) dm[i] = lin[i];
+  double nsq = row_norm_product_sq(dm, 3, 4);
+  if (!det_ok(gauss_det_solve(dm, 3), nsq, 1.0e-20)) return false;  // linear fit only: no maximum
+  const double q[42] = {S40, S22, S31, S30, S21, S20, m[18], S22, S04, S13, S12, S03, S02, m[20],
+                        S31, S13, S22, S21, S12, S11, m[19], S30, S12, S21, S20, S11, S10, m[16],
+                        S21, S03, S12, S11, S02, S01, m[17], S20, S02, S11, S10, S01, S00, m[15]};
+  for (int i = 0; i < 42; i++) dm[i] = q[i];
+  nsq = row_norm_product_sq(dm, 6, 7);
+  if (!det_ok(gauss_det_solve(dm, 6), nsq, 1.0e-30)) return false;  // linear fit only
+  const double A = dm[6], B = dm[13], Cq = dm[20], D = dm[27], E = dm[34], F = dm[41];
+  double *t = dm + 42;
+  t[0] = 2.0 * A; t[1] = Cq; t[2] = -D; t[3] = Cq; t[4] = 2.0 * B; t[5] = -E;
+  nsq = row_norm_product_sq(t, 2, 3);
+  if (!det_ok(gauss_det_solve(t, 2), nsq, 1.0e-30)) return false;
+  const double x = t[2], y = t[5];
+  const double v = A * x * x + B * y * y + Cq * x * y + D * x + E * y + F;
+  if (v < 0.0 || A >= 0.0 || B >= 0.0) return false;  // negative strength, or not a maximum
+  xyv[0] = x;
+  xyv[1] = y;
+  xyv[2] = v;
+  return true;
+}
+
+// LY_POLY: the instantiation with the polynomial mismatch measure (the other never carries it)
+template <bool LY_POLY>
 __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant__ LmaDev ld,
                                                          const __grid_constant__ TpLmaConst c) {
   extern __shared__ float sm[];
@@ -521,6 +686,10 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
   float *acc = red + LMA_NEQ * 33, *trial = acc + 32;
   float *stage = gsurf + LMA_OFF_STAGE;                         // [P][225] the tile's pair surfaces
   float *dres = gsurf + LMA_OFF_RES;                            // [4][4] the orientation fits
+  // quadric moments [LMA_POLY_CHUNK][21] over the reduction buffer and the per-lane solver scratch
+  // [LMA_POLY_CHUNK][LMA_POLY_SCRATCH] over the group surfaces (both free once the fits are done)
+  double *dmom = (double *)(gsurf + ((LMA_OFF_RED + 1) & ~1));
+  double *dsolve = (double *)gsurf;
   for (int task = blockIdx.x * LMA_NW + warp; task < ld.num_tasks; task += gridDim.x * LMA_NW) {
     const int txy = ld.task_txy[task];
     const size_t tile = (size_t)(txy >> 16) * ld.tilesX + (txy & 0xffff);
@@ -587,13 +756,64 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
       const float mod = foreground_correct(c, dd, vb, disparity, spread);
       // the corrected distance is not used while the mismatch is measured
       if (!mism && c.fo_correct && mod != disparity && strength > c.fo_min_strength) cm_out = mod;
-      if (mism && spread <= c.mismatch_max_diff && lane < ld.P && ld.kinds[lane] >= 0) {
-        float m3[3];
-        mismatch_cm(src + lane * TP_CORR, ld.kinds[lane], -disparity, c.max_corr_radius, m3);
-        float *mo = ld.mismatch + (tile * ld.P + lane) * 3;
-        mo[0] = m3[0];
-        mo[1] = m3[1];
-        mo[2] = m3[2];
+      if (mism && spread <= c.mismatch_max_diff) {
+        bool need_cm = true;
+        if (LY_POLY) {
+          // ImageDtt.java:2349-2383: each pair alone (mismatchPairs 1434-1503), the quadric's
+          // maximum; an implausible offset zeroes the pair's strength, and with the backup any
+          // failed or implausible pair sends the tile to the centre-of-mass measure
+          // Pairs go in chunks: the warp samples each pair and reduces its moments, then lane j
+          // solves the chunk's j-th pair (the solves are serial FP64 work, so one per lane).
+          bool has_nan = false;
+          const double xc = -(double)disparity;
+          for (int c0 = 0; c0 < ld.P; c0 += LMA_POLY_CHUNK) {
+            const int c1 = min(c0 + LMA_POLY_CHUNK, ld.P);
+            int my_ns = 0;
+            for (int pi = c0; pi < c1; pi++) {
+              if (ld.kinds[pi] < 0) continue;
+              int ng, gdb;
+              const int ns = lma_samples(ld, c, 1u << pi, -disparity, c.max_corr_radius, src, gsurf, sx, sy, sv, sw, sg,
+                                         lane, ng, gdb);
+              quadric_moments(sx, sy, sv, sw, ns, lane, dmom + (pi - c0) * 21);
+              if (lane == pi - c0) my_ns = ns;
+              __syncwarp();  // the next pair's samples overwrite these; the moments are written
+            }
+            const int pi = c0 + lane;
+            bool bad = false;
+            if (pi < c1 && ld.kinds[pi] >= 0) {
+              const int k = ld.kinds[pi];
+              double q[3], o0 = CUDART_NAN, o1 = CUDART_NAN, o2 = 0.0;
+              if (quadric_max(dmom + lane * 21, my_ns, dsolve + lane * LMA_POLY_SCRATCH, q)) {
+                if (k == 0) { o0 = xc - q[0]; o1 = -q[1]; }
+                else if (k == 1) { o0 = -q[1]; o1 = xc - q[0]; }
+                else if (k == 2) { o0 = xc - q[0] + q[1]; o1 = xc - q[0] - q[1]; }
+                else { o0 = xc - q[0] + q[1]; o1 = -xc + q[0] + q[1]; }
+                o2 = isnan(q[2]) ? 0.0 : q[2];
+              }
+              if (isnan(o0) || isnan(o1)) bad = true;
+              else if (o2 != 0.0 && (fabs(o0) > c.ly_crazy_poly || fabs(o1) > c.ly_crazy_poly)) {
+                o2 = 0.0;
+                bad = true;
+              }
+              float *mo = ld.mismatch + (tile * ld.P + pi) * 3;
+              mo[0] = (float)o0;
+              mo[1] = (float)o1;
+              mo[2] = (float)o2;
+            }
+            has_nan |= __any_sync(0xffffffffu, bad);
+            __syncwarp();  // the scratch lies over the next chunk's group surfaces
+          }
+          need_cm = c.ly_poly_backup && has_nan;
+          __syncwarp();
+        }
+        if (need_cm && lane < ld.P && ld.kinds[lane] >= 0) {
+          float m3[3];
+          mismatch_cm(src + lane * TP_CORR, ld.kinds[lane], -disparity, c.max_corr_radius, m3);
+          float *mo = ld.mismatch + (tile * ld.P + lane) * 3;
+          mo[0] = m3[0];
+          mo[1] = m3[1];
+          mo[2] = m3[2];
+        }
       }
     }
     if (lane == 0) {
@@ -661,19 +881,20 @@ cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst
   for (int k = 0; k < 4; k++) ld.kind_count[k] = 0;
   for (int i = 0; i < TP_MAXP; i++) {
     const int k = (i < cc.num_pairs) ? cc.pairs[i].kind : -1;
-    ld.kinds[i] = (k >= 0 && k <= 3 && ((c.pair_mask >> i) & 1)) ? k : -1;
+    ld.kinds[i] = (k >= 0 && k <= 3 && i < 32 && ((c.pair_mask >> i) & 1)) ? k : -1;  // the mask holds 32 pairs
     if (ld.kinds[i] >= 0) ld.kind_count[ld.kinds[i]]++;
   }
   const int bytes = lma_smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(lma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  const auto kern = (mismatch_out && c.ly_poly) ? lma_kernel<true> : lma_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lma_kernel, 32 * LMA_NW, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * LMA_NW, bytes);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   const int units = (sc.num_tasks + LMA_NW - 1) / LMA_NW;
   const int grid = units < sms * per_sm ? units : sms * per_sm;
-  lma_kernel<<<grid, 32 * LMA_NW, bytes, st>>>(ld, c);
+  kern<<<grid, 32 * LMA_NW, bytes, st>>>(ld, c);
   return cudaGetLastError();
 }

@@ -65,7 +65,8 @@ class TpLmaParams(C.Structure):
                 ("fo_correct", C.c_int), ("fo_far", C.c_int), ("fo_ortho", C.c_int), ("fo_min_strength", C.c_float),
                 ("fo_min_eff", C.c_float), ("fo_min_eff_ratio", C.c_float), ("fo_max_hwidth", C.c_float),
                 ("fo_min_diff", C.c_float), ("fo_overcorrection", C.c_float), ("fo_lim_overcorr", C.c_float),
-                ("mismatch", C.c_int), ("max_corr_radius", C.c_float), ("mismatch_max_diff", C.c_float)]
+                ("mismatch", C.c_int), ("max_corr_radius", C.c_float), ("mismatch_max_diff", C.c_float),
+                ("ly_poly", C.c_int), ("ly_crazy_poly", C.c_float), ("ly_poly_backup", C.c_int)]
 
 
 _H = C.c_void_p

@@ -268,6 +268,15 @@ typedef struct {
   int mismatch;             /* 0 */
   float max_corr_radius;    /* 3.9 (EyesisCorrectionParameters) */
   float mismatch_max_diff;  /* 1.0 */
+  /* the polynomial measure instead (ImageDttParameters.java:50-52; ImageDtt.java:2349-2405): each
+   * pair sampled alone like the LMA (weights x |value|^max_corr_radius, as there) and fitted by a
+   * weighted quadric A x^2 + B y^2 + C xy + D x + E y + F, whose maximum gives the pair's offsets
+   * and strength (Correlation2d.mismatchPairs 1434-1503, Correlations2dLMA.getMaxXYPoly 641-704);
+   * an offset beyond ly_crazy_poly zeroes the pair's strength, and with ly_poly_backup any failed
+   * or implausible pair sends all pairs of the tile to the centre-of-mass measure */
+  int ly_poly;              /* 0 */
+  float ly_crazy_poly;      /* 1.0 */
+  int ly_poly_backup;       /* 1 */
 } tp_lma_params;
 tp_status tp_default_lma_params(tp_lma_params *p);
 tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream);

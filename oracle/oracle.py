@@ -587,21 +587,44 @@ def lma_tile(corrs, kinds, cm, strength, params=None, fo=None):
     return bool(ran), rec, lma
 
 
-def lma_tile_mismatch(corrs, kinds, cm, strength, max_corr_radius=3.9, mismatch_max_diff=1.0, params=None, fo=None):
-    """lma_tile with the lazy-eye mismatch -> (ran, {CM, strength, POLY}, main LMA [4], mismatch [np][3])."""
+class LyParams(C.Structure):
+    """The mismatch measure (ImageDttParameters.java:50-52): ly_poly, ly_crazy_poly, ly_poly_backup."""
+    _fields_ = [("ly_poly", C.c_int), ("ly_crazy_poly", C.c_double), ("ly_poly_backup", C.c_int)]
+
+
+def lma_tile_mismatch(corrs, kinds, cm, strength, max_corr_radius=3.9, mismatch_max_diff=1.0, params=None, fo=None,
+                      ly_poly=False, ly_crazy_poly=1.0, ly_poly_backup=True):
+    """lma_tile with the lazy-eye mismatch -> (ran, {CM, strength, POLY}, main LMA [4], mismatch [np][3]);
+    ly_poly selects mismatchPairs (quadric maxima) over mismatchPairsCM."""
     fo = fo if fo is not None else default_fo_params()
     p = params if params is not None else default_lma_params()
     L = _lma_lib()
     if not getattr(L, "_mism_set", False):
-        L.or_lma_tile_mismatch.argtypes = [_dp, C.POINTER(C.c_int), C.c_int, C.POINTER(LmaParams),
-                                           C.POINTER(FoParams), C.c_double, C.c_double, _dp, _dp, _dp]
-        L.or_lma_tile_mismatch.restype = C.c_int
+        L.or_lma_tile_mismatch_ly.argtypes = [_dp, C.POINTER(C.c_int), C.c_int, C.POINTER(LmaParams),
+                                              C.POINTER(FoParams), C.c_double, C.c_double, C.POINTER(LyParams),
+                                              _dp, _dp, _dp]
+        L.or_lma_tile_mismatch_ly.restype = C.c_int
         L._mism_set = True
+    ly = LyParams(int(bool(ly_poly)), float(ly_crazy_poly), int(bool(ly_poly_backup)))
     a = _f64(corrs)
     k = np.ascontiguousarray(np.asarray(kinds, dtype=np.int32))
     rec = np.array([cm, strength, np.nan], dtype=np.float64)
     lma = np.zeros(4)
     mism = np.zeros((a.shape[0], 3))
-    ran = L.or_lma_tile_mismatch(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], C.byref(p), C.byref(fo),
-                                 float(max_corr_radius), float(mismatch_max_diff), _d(rec), _d(lma), _d(mism))
+    ran = L.or_lma_tile_mismatch_ly(_d(a), k.ctypes.data_as(C.POINTER(C.c_int)), a.shape[0], C.byref(p),
+                                    C.byref(fo), float(max_corr_radius), float(mismatch_max_diff), C.byref(ly),
+                                    _d(rec), _d(lma), _d(mism))
     return bool(ran), rec, lma, mism
+
+
+def quadratic_max(x, y, v, w):
+    """Correlations2dLMA.getMaxXYPoly on samples: (ok, {x, y, value}) of the weighted quadric's maximum."""
+    L = _lma_lib()
+    if not getattr(L, "_qmax_set", False):
+        L.or_quadratic_max.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp]
+        L.or_quadratic_max.restype = C.c_int
+        L._qmax_set = True
+    xs, ys, vs, ws = (_f64(a) for a in (x, y, v, w))
+    out = np.full(3, np.nan)
+    ok = L.or_quadratic_max(_d(xs), _d(ys), _d(vs), _d(ws), len(xs), _d(out))
+    return bool(ok), out

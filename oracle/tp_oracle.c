@@ -2124,9 +2124,144 @@ static void or_mismatch_cm_pair(const double *c, int k, double xcenter, double r
   out[2] = sv;
 }
 
+/* LU decomposition with partial pivoting of a [n][n] in place (Jama LUDecomposition, as used by
+ * Matrix.det / Matrix.solve): returns the determinant, piv the row order */
+static double lu_decompose(double *a, int n, int *piv) {
+  double det = 1.0;
+  for (int i = 0; i < n; i++) piv[i] = i;
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    for (int i = k + 1; i < n; i++)
+      if (fabs(a[i * n + k]) > fabs(a[p * n + k])) p = i;
+    if (p != k) {
+      for (int j = 0; j < n; j++) {
+        const double t = a[p * n + j];
+        a[p * n + j] = a[k * n + j];
+        a[k * n + j] = t;
+      }
+      const int t = piv[p];
+      piv[p] = piv[k];
+      piv[k] = t;
+      det = -det;
+    }
+    if (a[k * n + k] != 0.0)
+      for (int i = k + 1; i < n; i++) {
+        a[i * n + k] /= a[k * n + k];
+        for (int j = k + 1; j < n; j++) a[i * n + j] -= a[i * n + k] * a[k * n + j];
+      }
+  }
+  for (int k = 0; k < n; k++) det *= a[k * n + k];
+  return det;
+}
+
+/* solves with the factors of lu_decompose: b (in original row order) -> x in b */
+static void lu_solve(const double *lu, const int *piv, int n, double *b) {
+  double x[6];
+  for (int i = 0; i < n; i++) x[i] = b[piv[i]];
+  for (int k = 0; k < n; k++)
+    for (int i = k + 1; i < n; i++) x[i] -= x[k] * lu[i * n + k];
+  for (int k = n - 1; k >= 0; k--) {
+    x[k] /= lu[k * n + k];
+    for (int i = 0; i < k; i++) x[i] -= x[k] * lu[i * n + k];
+  }
+  for (int i = 0; i < n; i++) b[i] = x[i];
+}
+
+/* PolynomialApproximation.normMatix (common/PolynomialApproximation.java:590-598): product of the
+ * row norms */
+static double row_norm_product(const double *a, int n) {
+  double norm = 1.0;
+  for (int i = 0; i < n; i++) {
+    double d = 0.0;
+    for (int j = 0; j < n; j++) d += a[i * n + j] * a[i * n + j];
+    norm *= sqrt(d);
+  }
+  return norm;
+}
+
+/* Correlations2dLMA.getMaxXYPoly (Correlations2dLMA.java:641-704) over samples with weight > 0:
+ * the weighted least-squares quadric A x^2 + B y^2 + C xy + D x + E y + F
+ * (PolynomialApproximation.quadraticApproximation 350-585 with the linear / quadratic
+ * determinant-to-norm thresholds 1e-20 / 1e-30 of quadraticMaxV2dX2Y2XY 201-221) and its
+ * maximum.  Returns 1 with xyv = {x, y, value} when both fits are well-posed, the stationary
+ * point exists and is a maximum with a non-negative value. */
+int or_quadratic_max(const double *x, const double *y, const double *v, const double *w, int n, double xyv[3]) {
+  if (n <= 0) return 0;
+  double S00 = 0, S10 = 0, S01 = 0, S20 = 0, S11 = 0, S02 = 0, S30 = 0, S21 = 0, S12 = 0, S03 = 0;
+  double S40 = 0, S31 = 0, S22 = 0, S13 = 0, S04 = 0;
+  double Z00 = 0, Z10 = 0, Z01 = 0, Z20 = 0, Z11 = 0, Z02 = 0;
+  for (int i = 0; i < n; i++) {
+    const double wi = w[i];
+    if (!(wi > 0)) continue;
+    const double xi = x[i], yi = y[i], x2 = xi * xi, y2 = yi * yi;
+    S00 += wi; S10 += wi * xi; S01 += wi * yi; S11 += wi * xi * yi; S20 += wi * x2; S02 += wi * y2;
+    const double x3 = x2 * xi, x4 = x3 * xi, y3 = y2 * yi, y4 = y3 * yi;
+    S30 += wi * x3; S21 += wi * x2 * yi; S12 += wi * xi * y2; S03 += wi * y3;
+    S40 += wi * x4; S31 += wi * x3 * yi; S22 += wi * x2 * y2; S13 += wi * xi * y3; S04 += wi * y4;
+    const double wz = wi * v[i];
+    Z00 += wz; Z10 += wz * xi; Z01 += wz * yi; Z20 += wz * x2; Z11 += wz * xi * yi; Z02 += wz * y2;
+  }
+  int piv[6];
+  double ml[9] = {S20, S11, S10, S11, S02, S01, S10, S01, S00};
+  const double nml = row_norm_product(ml, 3);
+  if (nml == 0.0 || fabs(lu_decompose(ml, 3, piv)) / nml < 1.0e-20) return 0;  /* linear fit only */
+  double mq[36] = {S40, S22, S31, S30, S21, S20, S22, S04, S13, S12, S03, S02, S31, S13, S22, S21, S12, S11,
+                   S30, S12, S21, S20, S11, S10, S21, S03, S12, S11, S02, S01, S20, S02, S11, S10, S01, S00};
+  const double nmq = row_norm_product(mq, 6);
+  if (nmq == 0.0 || fabs(lu_decompose(mq, 6, piv)) / nmq < 1.0e-30) return 0;  /* linear fit only */
+  double co[6] = {Z20, Z02, Z11, Z10, Z01, Z00};
+  lu_solve(mq, piv, 6, co);
+  const double A = co[0], B = co[1], Cc = co[2], D = co[3], E = co[4], F = co[5];
+  double m2[4] = {2 * A, Cc, Cc, 2 * B};
+  const double nm2 = row_norm_product(m2, 2);
+  if (nm2 == 0.0 || fabs(lu_decompose(m2, 2, piv)) / nm2 < 1.0e-30) return 0;
+  double xy[2] = {-D, -E};
+  lu_solve(m2, piv, 2, xy);
+  const double vmax = A * xy[0] * xy[0] + B * xy[1] * xy[1] + Cc * xy[0] * xy[1] + D * xy[0] + E * xy[1] + F;
+  if (vmax < 0.0 || A >= 0.0 || B >= 0.0) return 0;  /* negative strength, or not a maximum */
+  xyv[0] = xy[0];
+  xyv[1] = xy[1];
+  xyv[2] = vmax;
+  return 1;
+}
+
+/* Correlation2d.mismatchPairs (1434-1503) for one pair of quad kind k: the pair alone as a group
+ * (corrLMA with run_poly_instead, 1754-1831, samples weighted by |value|^vasw_pwr) and the
+ * quadric's maximum -> {dx, dy, strength}; {NaN, NaN, 0} when the fit fails */
+static void or_mismatch_poly_pair(const double *c, int k, double xcenter, double vasw_pwr, const or_lma_params *p,
+                                  double out[3]) {
+  static or_lma Ls;
+  or_lma *L = &Ls;
+  memset(L, 0, sizeof(*L));
+  double g[OR_CORR * OR_CORR];
+  for (int r = 0; r < OR_CORR; r++)
+    for (int q = 0; q < OR_CORR; q++)
+      g[r * OR_CORR + q] = (k == 1) ? c[q * OR_CORR + r] : ((k == 3) ? c[(OR_CORR - r - 1) * OR_CORR + q]
+                                                                      : c[r * OR_CORR + q]);
+  or_lma_params pp = *p;
+  pp.ortho_vasw_pwr = vasw_pwr;
+  lma_add_group(L, g, k >= 2, 1, xcenter, &pp);
+  out[0] = out[1] = NAN;
+  out[2] = 0.0;
+  double m[3];
+  if (!or_quadratic_max(L->x, L->y, L->v, L->w, L->ns, m)) return;
+  if (k == 0) { out[0] = xcenter - m[0]; out[1] = -m[1]; }
+  else if (k == 1) { out[0] = -m[1]; out[1] = xcenter - m[0]; }
+  else if (k == 2) { out[0] = xcenter - m[0] + m[1]; out[1] = xcenter - m[0] - m[1]; }
+  else { out[0] = xcenter - m[0] + m[1]; out[1] = -xcenter + m[0] + m[1]; }
+  out[2] = isnan(m[2]) ? 0.0 : m[2];
+}
+
 int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_lma_params *p,
                          const or_fo_params *f, double max_corr_radius, double mismatch_max_diff, double rec[3],
                          double lma[4], double *mism) {
+  const or_ly_params ly = {0, 1.0, 1};
+  return or_lma_tile_mismatch_ly(corrs, kind, np, p, f, max_corr_radius, mismatch_max_diff, &ly, rec, lma, mism);
+}
+
+int or_lma_tile_mismatch_ly(const double *corrs, const int *kind, int np, const or_lma_params *p,
+                            const or_fo_params *f, double max_corr_radius, double mismatch_max_diff,
+                            const or_ly_params *ly, double rec[3], double lma[4], double *mism) {
   lma[0] = lma[1] = lma[2] = lma[3] = NAN;
   rec[2] = NAN;
   if (mism)
@@ -2160,11 +2295,32 @@ int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_
     or_foreground_correct(f->fo_far, f->fo_ortho, (const double(*)[4])dir, valid, disparity, f, mod);
     /* the corrected distance is not used while the mismatch is measured */
     if (mod[0] != disparity && !mism && f->fo_correct && strength > f->fo_min_strength) rec[0] = mod[0];
-    if (mism && mod[2] <= mismatch_max_diff)
-      for (int i = 0; i < np; i++)
-        if (((p->pair_mask >> i) & 1) && kind[i] >= 0 && kind[i] <= 3)
-          or_mismatch_cm_pair(corrs + (size_t)i * OR_CORR * OR_CORR, kind[i], -disparity, max_corr_radius,
-                              mism + 3 * i);
+    if (mism && mod[2] <= mismatch_max_diff) {
+      /* ImageDtt.java:2349-2405: with ly_poly the quadric maxima; a failed or implausible pair (an
+       * offset beyond ly_crazy_poly, its strength then zeroed) sends all pairs to the centre of
+       * mass when ly_poly_backup is set */
+      int need_cm = 1;
+      if (ly->ly_poly) {
+        int has_nan = 0;
+        for (int i = 0; i < np; i++)
+          if (((p->pair_mask >> i) & 1) && kind[i] >= 0 && kind[i] <= 3) {
+            double *m = mism + 3 * i;
+            or_mismatch_poly_pair(corrs + (size_t)i * OR_CORR * OR_CORR, kind[i], -disparity, max_corr_radius, p,
+                                  m);
+            if (isnan(m[0]) || isnan(m[1])) has_nan = 1;
+            else if (m[2] != 0.0 && (fabs(m[0]) > ly->ly_crazy_poly || fabs(m[1]) > ly->ly_crazy_poly)) {
+              m[2] = 0.0;
+              has_nan = 1;
+            }
+          }
+        need_cm = ly->ly_poly_backup && has_nan;
+      }
+      if (need_cm)
+        for (int i = 0; i < np; i++)
+          if (((p->pair_mask >> i) & 1) && kind[i] >= 0 && kind[i] <= 3)
+            or_mismatch_cm_pair(corrs + (size_t)i * OR_CORR * OR_CORR, kind[i], -disparity, max_corr_radius,
+                                mism + 3 * i);
+    }
   }
   return 1;
 }

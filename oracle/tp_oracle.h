@@ -260,6 +260,21 @@ int or_lma_tile(const double *corrs, const int *kind, int np, const or_lma_param
 int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_lma_params *p,
                          const or_fo_params *f, double max_corr_radius, double mismatch_max_diff, double rec[3],
                          double lma[4], double *mism);
+/* the polynomial mismatch (ImageDttParameters.java:50-52 defaults) */
+typedef struct {
+  int ly_poly;           /* 0: mismatchPairs (quadric maxima) instead of mismatchPairsCM */
+  double ly_crazy_poly;  /* 1.0: a larger quadric offset zeroes the pair's strength */
+  int ly_poly_backup;    /* 1: any failed / implausible pair sends all pairs to mismatchPairsCM */
+} or_ly_params;
+/* or_lma_tile_mismatch with the choice of mismatch measure (ImageDtt.java:2349-2405); with
+ * ly_poly each pair is sampled alone like corrLMA (|value|^max_corr_radius weights, as there)
+ * and measured by or_quadratic_max (Correlation2d.mismatchPairs 1434-1503) */
+int or_lma_tile_mismatch_ly(const double *corrs, const int *kind, int np, const or_lma_params *p,
+                            const or_fo_params *f, double max_corr_radius, double mismatch_max_diff,
+                            const or_ly_params *ly, double rec[3], double lma[4], double *mism);
+/* Correlations2dLMA.getMaxXYPoly (641-704): weighted quadric fit of n samples (weight > 0 taken)
+ * and its maximum -> xyv {x, y, value}; 0 when the fit or the maximum does not exist */
+int or_quadratic_max(const double *x, const double *y, const double *v, const double *w, int n, double xyv[3]);
 
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {

@@ -140,6 +140,38 @@ def test_lma_mismatch_matches_oracle(oracle):
     print("mismatch: agrees on %d of %d tiles, measured on %d" % (ok, n, measured))
 
 
+@pytest.mark.parametrize("backup", [True, False])
+def test_lma_poly_mismatch_matches_oracle(oracle, backup):
+    """The polynomial mismatch (ly_poly; ImageDtt.java:2349-2383, Correlation2d.mismatchPairs): each pair
+    alone, the maximum of its weighted quadric; implausible pairs (offset > ly_crazy_poly) get zero
+    strength and, with ly_poly_backup, send the tile to the centre of mass.  Oracle on the GPU's
+    surfaces and record; {dx, dy, strength} within 1e-3 on >= 97% of the refined tiles, and the quadric
+    (not the centre of mass) decides a share of them."""
+    sc = synth.make_scene("quad_mono", seed=45, width=128, height=96)
+    T = 16 * 12
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(np.full(T, 4.0, np.float32))
+        tp.process()
+        corr, d0 = tp.getCorr(), tp.getDisparity()
+        tp.lmaRefine(mismatch=1, ly_poly=1, ly_poly_backup=int(backup))
+        mm = tp.getLmaMismatch()
+    n = ok = by_poly = 0
+    for t in range(T):
+        args = (corr[t].astype(np.float64), KINDS, float(d0[t, oracle.DISP_CM]), float(d0[t, oracle.DISP_STRENGTH]))
+        ran, _, _, om = oracle.lma_tile_mismatch(*args, ly_poly=True, ly_poly_backup=backup)
+        if not ran:
+            assert np.all(np.isnan(mm[t, :, :2])) and np.all(mm[t, :, 2] == 0)
+            continue
+        n += 1
+        _, _, _, ocm = oracle.lma_tile_mismatch(*args)
+        by_poly += not np.allclose(om, ocm, atol=1e-9, equal_nan=True)
+        ok += np.allclose(mm[t], om, atol=1e-3, equal_nan=True)
+    assert n > 20 and by_poly > 0.2 * n
+    assert ok >= 0.97 * n, "poly mismatch agrees on %d of %d tiles" % (ok, n)
+    print("poly mismatch (backup %s): agrees on %d of %d tiles, %d by the quadric" % (backup, ok, n, by_poly))
+
+
 def test_lma_rejects_general_pairs(oracle):
     from tileproc import _lib
     sc = synth.make_scene("circle_lwir", seed=43, width=64, height=64)

@@ -70,3 +70,68 @@ def test_foreground_correct_picks_the_nearest_strong_orientation():
     d[1, 2] = 3.5
     L.or_foreground_correct(0, 1, O._d(d), valid, 1.3, O.C.byref(f), O._d(out))
     assert out[0] == 1.3
+
+
+def test_quadratic_max_recovers_an_exact_quadric():
+    rng = np.random.default_rng(3)
+    x, y = rng.uniform(-4, 4, 60), rng.uniform(-4, 4, 60)
+    A, B, Cc, D, E, F = -0.3, -0.2, 0.05, 0.4, -0.1, 0.7
+    v = A * x * x + B * y * y + Cc * x * y + D * x + E * y + F
+    ok, out = O.quadratic_max(x, y, v, rng.uniform(0.1, 1.0, 60))
+    xy = np.linalg.solve([[2 * A, Cc], [Cc, 2 * B]], [-D, -E])
+    assert ok and np.allclose(out[:2], xy, atol=1e-10)
+    assert abs(out[2] - (A * xy[0] ** 2 + B * xy[1] ** 2 + Cc * xy[0] * xy[1] + D * xy[0] + E * xy[1] + F)) < 1e-10
+    # a minimum, a collinear sample set and no positive weight have no maximum
+    assert not O.quadratic_max(x, y, -v, np.ones(60))[0]
+    assert not O.quadratic_max(x, 0.5 * x, v, np.ones(60))[0]
+    assert not O.quadratic_max(x, y, v, np.zeros(60))[0]
+
+
+def _offset_surfaces(x0, offs, amp=(0.6, 0.5), w=2.0):
+    """Quad pair surfaces with each pair's peak moved by its own (along, across) offset."""
+    yy, xx = np.mgrid[-7:8, -7:8].astype(np.float64)
+    out = []
+    for k, (px, py) in zip(KINDS, offs):
+        if k < 2:
+            c = amp[0] * (1 - ((xx - x0 - px) / w) ** 2 - ((yy - py) / w) ** 2)
+        else:
+            a, b, s = (xx + yy) / 2.0, (yy - xx) / 2.0, np.sqrt(2.0)
+            c = amp[1] * (1 - ((a - x0 - px) * s / w) ** 2 - ((b - py) * s / w) ** 2)
+        out.append((c.T if k == 1 else (c[::-1] if k == 3 else c)).ravel())
+    return np.stack(out)
+
+
+def _expected_mismatch(xc, x0, offs):
+    """mismatchPairs' per-kind offsets (Correlation2d.java:1474-1490) of peaks at x0 + px, py."""
+    rows = []
+    for k, (px, py) in zip(KINDS, offs):
+        X, Y = x0 + px, py
+        rows.append({0: (xc - X, -Y), 1: (-Y, xc - X), 2: (xc - X + Y, xc - X - Y), 3: (xc - X + Y, -xc + X + Y)}[k])
+    return np.array(rows)
+
+
+def test_poly_mismatch_recovers_pair_offsets():
+    offs = [(0.1, 0.05), (-0.1, 0.0), (0.15, -0.1), (0.0, 0.1), (0.05, 0.05), (-0.05, 0.1)]
+    x0 = 1.3
+    s = _offset_surfaces(x0, offs)
+    ran, rec, _, m = O.lma_tile_mismatch(s, KINDS, -x0, 0.6, ly_poly=True)
+    assert ran
+    assert np.allclose(m[:, :2], _expected_mismatch(-rec[0], x0, offs), atol=1e-9)
+    assert np.allclose(m[:, 2], [0.6] * 4 + [0.5] * 2, atol=1e-9)  # the quadric's value at its peak
+    # the centre of mass sees the same offsets only roughly
+    _, _, _, mc = O.lma_tile_mismatch(s, KINDS, -x0, 0.6, ly_poly=False)
+    assert not np.allclose(mc, m, atol=1e-3)
+
+
+def test_poly_mismatch_crazy_pair_falls_back_to_centre_of_mass():
+    offs = [(0.1, 0.05), (-0.1, 0.0), (0.15, -0.1), (0.0, 0.1), (0.05, 0.05), (-0.05, 0.1)]
+    s = _offset_surfaces(1.3, offs)
+    _, _, _, mc = O.lma_tile_mismatch(s, KINDS, -1.3, 0.6, ly_poly=False)
+    # a limit below the largest offset: one implausible pair sends every pair to the CM measure
+    _, _, _, mb = O.lma_tile_mismatch(s, KINDS, -1.3, 0.6, ly_poly=True, ly_crazy_poly=0.1)
+    assert np.array_equal(mb, mc)
+    # without the backup the implausible pairs keep their offsets with zero strength
+    _, rec, _, mn = O.lma_tile_mismatch(s, KINDS, -1.3, 0.6, ly_poly=True, ly_crazy_poly=0.1, ly_poly_backup=False)
+    big = np.max(np.abs(mn[:, :2]), axis=1) > 0.1
+    assert big.any() and not big.all()
+    assert np.all(mn[big, 2] == 0.0) and np.all(mn[~big, 2] > 0.4)
