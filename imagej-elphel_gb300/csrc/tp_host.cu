@@ -53,6 +53,7 @@ struct tp_handle {
   size_t mismatch_cap = 0;
   int mismatch_pairs = -1;
   int disp_mixed = 0;        // the LMA replaced CM / strength since the last forward
+  int lma_valid = 0;         // d_lma holds the LMA of the current forward (POLY for the textures)
   size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
@@ -753,6 +754,7 @@ tp_status tp_convert_correct(tp_handle *h, void *stream) {
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
   CK(launch_convert_correct(scene_of(h), st), "convert_correct");
+  h->lma_valid = 0;
   return TP_OK;
 }
 
@@ -837,9 +839,18 @@ tp_status tp_textures(tp_handle *h, void *stream) {
   tc.corr_magic_scale = p.corr_magic_scale;
   tc.dust_remove = p.dust_remove;
   tc.rows = rows;
-  // corr_mode -> disparity slot (ImageDtt.java:2422-2426); POLY is not produced here
+  // corr_mode -> disparity slot (ImageDtt.java:2422-2426): INT, CM, HOR, VERT from the disparity
+  // record; POLY is the LMA disparity of tp_lma_refine on the current forward (none without it,
+  // as a NaN POLY gives no shift in the reference)
   static const int slot[5] = {0, 1, -1, 3, 5};
+  tc.extra_src = h->d_disp;
+  tc.extra_stride = TP_NDISP;
   tc.extra_index = (p.corr_mode >= 0) ? slot[p.corr_mode] : -1;
+  if (p.corr_mode == 2 && h->lma_valid && h->d_lma) {
+    tc.extra_src = h->d_lma;
+    tc.extra_stride = 4;
+    tc.extra_index = 0;
+  }
   if (tc.extra_index >= 0 && h->num_pairs == 0) tc.extra_index = -1;
   CK(launch_textures(scene_of(h), tc, st), "textures");
   h->tex_rows = rows;
@@ -858,6 +869,7 @@ tp_status tp_process(tp_handle *h, void *stream) {
   h->fwd_valid = 1;
   h->strips_valid = sc.strips ? 1 : 0;
   h->disp_mixed = 0;
+  h->lma_valid = 0;
   return TP_OK;
 }
 
@@ -1074,6 +1086,7 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
     h->fwd_valid = 1;
     h->strips_valid = 0;
     h->disp_mixed = 0;
+    h->lma_valid = 0;
   }
   return TP_OK;
 }
@@ -1248,6 +1261,7 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   CK(launch_lma(scene_of(h), h->corr_host, c, h->d_lma, prm.mismatch ? h->d_mismatch : nullptr, st),
      "tp_lma_refine");
   if (prm.mix_corr_poly || prm.fo_correct) h->disp_mixed = 1;
+  h->lma_valid = 1;
   return TP_OK;
 }
 
@@ -1498,6 +1512,7 @@ tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
     h->fwd_valid = 1;
     h->strips_valid = 0;
     h->disp_mixed = 0;
+    h->lma_valid = 0;
   }
   return TP_OK;
 }

@@ -119,7 +119,9 @@ struct TexConst {
   float corr_magic_scale;
   int dust_remove;
   int rows;                 // 4 (RGBA) or 12 (keep_weights)
-  int extra_index;          // disparity slot for the extra shift, -1: none
+  const float *extra_src;   // [tiles][extra_stride] disparities for the extra shift
+  int extra_stride;
+  int extra_index;          // slot in extra_src, -1: no extra shift
 };
 
 // launchers (tp_plan.cu / tp_kernels.cu)

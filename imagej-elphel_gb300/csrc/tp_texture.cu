@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(TX_THREADS, 5) texture_kernel(const __grid_con
     // extra disparity (ImageDtt.java:2422-2427, 2663): not for forced-disparity tiles
     float extra = 0.f;
     if (tc.extra_index >= 0 && !(op & 0x100)) {
-      extra = sc.disp[tile * TP_NDISP + tc.extra_index];
+      extra = tc.extra_src[tile * tc.extra_stride + tc.extra_index];
       if (isnan(extra)) extra = 0.f;
     }
     // ---------------- per-port IMCLT ----------------

@@ -126,8 +126,9 @@ typedef struct {
   float corr_magic_scale;  /* 0.85: extra shift = disparity x port offset / this */
   int dust_remove;         /* 1 */
   int keep_weights;        /* 1: 12 rows per tile (RGBA, 4 port weights, 4 rms), 0: 4 rows */
-  int corr_mode;           /* 2: disparity used for the extra shift: 0 INT, 1 CM, 3 HOR, 4 VERT;
-                              2 (POLY, not computed here) and -1 give no extra shift */
+  int corr_mode;           /* 2: disparity used for the extra shift: 0 INT, 1 CM, 2 POLY (the LMA
+                              disparity of tp_lma_refine after the current forward; none without
+                              it), 3 HOR, 4 VERT; -1 gives no extra shift */
   int aux;                 /* 1: also keep per tile max_diff[4] and ports_rgb[12] */
 } tp_texture_params;
 

@@ -296,3 +296,82 @@ def test_zero_contrast_tiles(oracle):
     assert np.array_equal(np.isnan(cm_ref), np.isnan(cm_gpu))
     ok = ~np.isnan(cm_ref)
     assert np.abs(cm_gpu[ok] - cm_ref[ok]).max() <= DISP_TOL
+
+
+def test_full_size_bayer_sampled_tiles(oracle):
+    """The full-size workload (4 Bayer sensors 2592x1936 uint16, per-sensor/colour kernel tables on a
+    16-px grid, 78,408 tiles, per-tile disparity in [0, 8] px) forward on the GPU; the oracle checks
+    every 97th tile plus the four corners (about 800 tiles) at the stated tolerances, and the task
+    list covers the frame in row-major order (bit-exact)."""
+    sc = synth.make_scene("quad_bayer", seed=21, width=2592, height=1936)
+    W, H = sc["width"], sc["height"]
+    tX, tY = W // 8, H // 8
+    T = tX * tY
+    rng = np.random.default_rng(23)
+    k, e = synth.random_clt_kernels(rng, 4, H // 16 + 2, W // 16 + 2, 3)
+    disp = rng.uniform(0.0, 8.0, T).astype(np.float32)
+    sel = np.union1d(np.arange(0, T, 97), [0, tX - 1, T - tX, T - 1])
+    op = np.zeros(T, np.int32)
+    op[sel] = 1
+    ref = run_oracle(oracle, sc, disp.astype(np.float64), kernels=k, kext=e, tile_op=op)
+    with make_gpu(sc, k, e) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(disp)
+        tp.process()
+        assert tp.numTasks() == T
+        assert np.array_equal(tp.getTaskTiles(), (np.arange(T) % tX) | ((np.arange(T) // tX) << 16))
+        assert np.array_equal(tp.getPorts()[sel], ref["ports"][sel])
+        tl, res = tp.getSubtiles()
+        assert np.array_equal(tl[sel], ref["int_tl"][sel])
+        assert np.array_equal(res[sel], ref["residual"][sel].astype(np.float32))
+        clt = tp.getClt()[sel].astype(np.float64)
+        ec = rel_l2(clt, ref["clt"][sel], axis=(-2, -1))
+        assert ec.max() <= CLT_TOL, "CLT rel L2 max %.3g" % ec.max()
+        del clt
+        corr = tp.getCorr()[sel].astype(np.float64)
+        er = rel_l2(corr, ref["corr"][sel], axis=-1)
+        assert er.max() <= CORR_TOL, "corr rel L2 max %.3g" % er.max()
+        d = tp.getDisparity()[sel].astype(np.float64)
+    r = ref["disp"][sel]
+    agree = np.isfinite(r[:, oracle.DISP_CM]) & np.isfinite(d[:, oracle.DISP_CM]) & \
+        (d[:, oracle.DISP_IXY] == r[:, oracle.DISP_IXY])
+    n = np.isfinite(r[:, oracle.DISP_CM]).sum()
+    assert n > 0.9 * len(sel) and agree.sum() >= 0.995 * n
+    assert np.abs(d[agree, oracle.DISP_CM] - r[agree, oracle.DISP_CM]).max() <= DISP_TOL
+    print("full size: %d tiles checked, CLT max %.3g, corr max %.3g" % (len(sel), ec.max(), er.max()))
+
+
+def test_full_size_circle16_sampled_tiles(oracle):
+    """The full-size 16-sensor LWIR workload (640x512, 5120 tiles, all 120 pairs, extrinsic
+    perturbations, per-tile disparity in [0, 4] px) under the default schedule; the oracle checks
+    every 7th tile plus the corners (about 730 tiles)."""
+    sc = synth.make_scene("circle_lwir", seed=25, dmax=4.0)
+    W, H = sc["width"], sc["height"]
+    tX, T = W // 8, (W // 8) * (H // 8)
+    pairs = synth.circle_pairs(sc["geometry"])
+    opairs = [(a, b, bx, by, kind) for (a, b, kind, _, bx, by) in pairs]
+    disp = np.random.default_rng(27).uniform(0.0, 4.0, T).astype(np.float32)
+    sel = np.union1d(np.arange(0, T, 7), [0, tX - 1, T - tX, T - 1])
+    op = np.zeros(T, np.int32)
+    op[sel] = 1
+    ref = run_oracle(oracle, sc, disp.astype(np.float64), pairs=opairs, tile_op=op)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation(pairs=pairs)
+        tp.setFullFrameImages(disp)
+        tp.process()
+        assert tp.numTasks() == T
+        assert np.array_equal(tp.getPorts()[sel], ref["ports"][sel])
+        tl, _ = tp.getSubtiles()
+        assert np.array_equal(tl[sel], ref["int_tl"][sel])
+        ec = rel_l2(tp.getClt()[sel].astype(np.float64), ref["clt"][sel], axis=(-2, -1))
+        assert ec.max() <= CLT_TOL, "CLT rel L2 max %.3g" % ec.max()
+        er = rel_l2(tp.getCorr()[sel].astype(np.float64), ref["corr"][sel], axis=-1)
+        assert er.max() <= CORR_TOL, "corr rel L2 max %.3g" % er.max()
+        d = tp.getDisparity()[sel].astype(np.float64)
+    r = ref["disp"][sel]
+    agree = np.isfinite(r[:, oracle.DISP_CM]) & np.isfinite(d[:, oracle.DISP_CM]) & \
+        (d[:, oracle.DISP_IXY] == r[:, oracle.DISP_IXY])
+    n = np.isfinite(r[:, oracle.DISP_CM]).sum()
+    assert n > 0.9 * len(sel) and agree.sum() >= 0.99 * n
+    assert np.abs(d[agree, oracle.DISP_CM] - r[agree, oracle.DISP_CM]).max() <= DISP_TOL
+    print("full size LWIR: %d tiles checked, CLT max %.3g, corr max %.3g" % (len(sel), ec.max(), er.max()))

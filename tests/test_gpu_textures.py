@@ -104,6 +104,39 @@ def test_textures_on_gpu_clt(oracle):
     print(_compare(got[tiles], aux[tiles], want, want_aux))
 
 
+def test_textures_poly_shift_after_lma(oracle):
+    """corr_mode 2 (the default): the extra shift is the LMA ("POLY") disparity of tp_lma_refine on the
+    current forward (ImageDtt.java:2424), zero where the LMA did not fit; the oracle gets the GPU's CLT
+    and LMA record.  Without an LMA pass after the forward there is no extra shift."""
+    sc = synth.make_scene("quad_bayer", seed=29, width=192, height=128)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    rng = np.random.default_rng(30)
+    ops = _scene_ops(T, rng)
+    disp = sc["disparity_gt"].reshape(-1).astype(np.float32) + rng.normal(0, 0.3, T).astype(np.float32)
+    with make_gpu(sc) as tp:
+        tp.setCorrelation()
+        tp.setFullFrameImages(disp, tile_op=ops)
+        tp.process()
+        lma = tp.lmaRefine().astype(np.float64)
+        tp.setTextureParams(corr_mode=2)
+        tp.execTextures()
+        got = tp.getTextures().astype(np.float64)
+        aux = tp.getTextureAux().astype(np.float64)
+        clt = tp.getClt().astype(np.float64)
+        tp.process()  # a new forward drops the LMA: no extra shift
+        tp.execTextures()
+        got0 = tp.getTextures().astype(np.float64)
+    tiles = np.nonzero(ops)[0]
+    shifted = tiles[np.isfinite(lma[tiles, 0]) & (lma[tiles, 0] != 0) & ((ops[tiles] & 0x100) == 0)]
+    assert len(shifted) > 0.5 * len(tiles)
+    want, want_aux = _oracle_textures(oracle, clt, lma, ops, tiles, extra_slot=0)
+    print(_compare(got[tiles], aux[tiles], want, want_aux))
+    want0, _ = _oracle_textures(oracle, clt, lma, ops, tiles)
+    g0 = np.nan_to_num(got0[tiles, :4])
+    assert np.allclose(g0, np.nan_to_num(want0[:, :4]), rtol=1e-3, atol=1e-3 * np.abs(g0).max())
+
+
 def test_textures_end_to_end(oracle):
     """Image -> CLT -> textures on the GPU vs the oracle's own chain (default corr_mode: no extra shift)."""
     sc = synth.make_scene("quad_bayer", seed=23, width=128, height=96)
