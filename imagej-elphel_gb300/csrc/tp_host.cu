@@ -54,6 +54,7 @@ struct tp_handle {
   int mismatch_pairs = -1;
   int disp_mixed = 0;        // the LMA replaced CM / strength since the last forward
   int lma_valid = 0;         // d_lma holds the LMA of the current forward (POLY for the textures)
+  int rig_aux = 0;           // the geometry is a rig's auxiliary camera (tp_set_rig_geometry)
   size_t psf_stage_kernels = 0;
   // adjoint buffers (allocated by the first tp_backward)
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
@@ -429,8 +430,24 @@ tp_status tp_last_error(const tp_handle *h, char *buf, int n) {
   return TP_OK;
 }
 
-tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
-  if (!h || !g) return TP_ERR_ARG;
+// RigOffset.getRotMatrix (GeometryCorrection.java:770-800): aux roll (with zoom) x tilt x azimuth
+static void host_rig_matrix(const tp_rig_offset *r, double m[3][3]) {
+  const double ca = cos(r->aux_azimuth), sa = sin(r->aux_azimuth);
+  const double ct = cos(r->aux_tilt), st = sin(r->aux_tilt);
+  const double zoom = 1.0 + r->aux_zoom;
+  const double cr = cos(r->aux_roll) * zoom, sr = sin(r->aux_roll) * zoom;
+  const double AZ = -1.0, TL = 1.0, RL = 1.0;
+  const double a_az[3][3] = {{ca, 0.0, sa * AZ}, {0.0, 1.0, 0.0}, {-sa * AZ, 0.0, ca}};
+  const double a_t[3][3] = {{1.0, 0.0, 0.0}, {0.0, ct, st * TL}, {0.0, -st * TL, ct}};
+  const double a_r[3][3] = {{cr, sr * RL, 0.0}, {-sr * RL, cr, 0.0}, {0.0, 0.0, 1.0}};
+  double t[3][3];
+  m3mul(a_t, a_az, t);
+  m3mul(a_r, t, m);
+}
+
+// the device geometry of camera g; the tile centre is undistorted with gc (g itself, or a rig's
+// main camera), whose reverse distortion table is uploaded
+static tp_status upload_geometry(tp_handle *h, const tp_geometry *g, const tp_geometry *gc, const tp_rig_offset *rig) {
   const int S = h->cfg.num_sensors;
   GeomDev &gd = h->geom_host;
   memset(&gd, 0, sizeof(gd));
@@ -440,6 +457,10 @@ tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
   gd.focal_length = g->focal_length;
   gd.pixel_size = g->pixel_size;
   gd.distortion_radius = g->distortion_radius;
+  gd.c_pixel_width = gc->pixel_width;
+  gd.c_pixel_height = gc->pixel_height;
+  gd.c_pixel_size = gc->pixel_size;
+  gd.c_distortion_radius = gc->distortion_radius;
   for (int i = 0; i < 7; i++) gd.rad_coeff[i] = g->distortion[i];
   for (int s = 0; s < S; s++)
     for (int k = 0; k < 2; k++) {
@@ -447,18 +468,57 @@ tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
       gd.pXY0[s][k] = g->pXY0[s][k];
     }
   host_rotations(g, S, &gd);
+  if (rig) {
+    // RigOffset.recalcRXY (728-747): baseline offset plus the aux-roll-rotated lens offsets
+    const double xc_pix = rig->baseline * cos(rig->aux_angle) / rig->aux_disparity_radius;
+    const double yc_pix = rig->baseline * sin(rig->aux_angle) / rig->aux_disparity_radius;
+    const double ssr = 1.0;
+    for (int s = 0; s < S; s++) {
+      gd.rXY[s][0] = xc_pix + cos(rig->aux_roll) * g->rXY[s][0] + ssr * sin(rig->aux_roll) * g->rXY[s][1];
+      gd.rXY[s][1] = yc_pix - ssr * sin(rig->aux_roll) * g->rXY[s][0] + cos(rig->aux_roll) * g->rXY[s][1];
+    }
+    // CorrVector.getRotMatrices(rigMatrix) (1016-1025): each sensor's rotation, then the rig's
+    double rm[3][3], t[3][3];
+    host_rig_matrix(rig, rm);
+    for (int s = 0; s < S; s++) {
+      m3mul(gd.rots[s], rm, t);
+      memcpy(gd.rots[s], t, sizeof(t));
+      for (int k = 0; k < 4; k++) {
+        m3mul(gd.drots[s][k], rm, t);
+        memcpy(gd.drots[s][k], t, sizeof(t));
+      }
+    }
+    gd.rig = 1;
+    gd.disp_num = rig->aux_disparity_radius;
+    gd.disp_den = rig->main_disparity_radius;
+  }
   std::vector<double> tbl;
-  gd.tbl_len = host_rdist_table(g, tbl);
+  gd.tbl_len = host_rdist_table(gc, tbl);
   if (gd.tbl_len > 2048 + 64) return fail(h, TP_ERR_ARG, "distortion table too long");
   CK(cudaMemcpyAsync(h->d_geom, &gd, sizeof(gd), cudaMemcpyHostToDevice, h->stream), "tp_set_geometry");
   CK(cudaMemcpyAsync(h->d_rdist, tbl.data(), sizeof(double) * gd.tbl_len, cudaMemcpyHostToDevice, h->stream),
      "tp_set_geometry");
   CK(cudaStreamSynchronize(h->stream), "tp_set_geometry");
   h->have_geometry = 1;
+  h->rig_aux = rig != nullptr;
   h->planned = 0;
   h->deriv_valid = 0;
   h->fwd_valid = 0;
   return TP_OK;
+}
+
+tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g) {
+  if (!h || !g) return TP_ERR_ARG;
+  return upload_geometry(h, g, g, nullptr);
+}
+
+tp_status tp_set_rig_geometry(tp_handle *h, const tp_geometry *aux, const tp_geometry *main_camera,
+                              const tp_rig_offset *rig) {
+  if (!h || !aux) return TP_ERR_ARG;
+  if (!main_camera || !rig) return upload_geometry(h, aux, aux, nullptr);
+  if (!(rig->main_disparity_radius > 0.0) || !(rig->aux_disparity_radius > 0.0))
+    return fail(h, TP_ERR_ARG, "tp_set_rig_geometry: disparity radii must be positive");
+  return upload_geometry(h, aux, main_camera, rig);
 }
 
 tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const float *offs, int layout) {
@@ -1355,6 +1415,8 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
   if (h->cfg.num_colors != 1) return fail(h, TP_ERR_ARG, "tp_backward: the adjoint is implemented for mono sensors");
   if (!h->ports_from_geometry || !h->have_geometry)
     return fail(h, TP_ERR_STATE, "tp_backward: needs tile ops with ports from the geometry (tp_set_tile_ops)");
+  if (h->rig_aux)
+    return fail(h, TP_ERR_STATE, "tp_backward: not for a rig's auxiliary camera (its disparities are the main camera's)");
   if (!h->fwd_valid || h->num_pairs == 0)
     return fail(h, TP_ERR_STATE, "tp_backward: run tp_process (with correlation pairs) first");
   cudaStream_t st = pick_stream(h, stream);

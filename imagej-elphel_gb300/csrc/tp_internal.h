@@ -29,6 +29,12 @@ struct GeomDev {
   int pixel_width, pixel_height;
   int tbl_len;
   double focal_length, pixel_size, distortion_radius;
+  // the model that undistorts the tile centre (the reference's gc_main): this camera's own, or
+  // the main camera's for a rig's auxiliary camera, whose reverse distortion table is then loaded
+  int c_pixel_width, c_pixel_height;
+  double c_pixel_size, c_distortion_radius;
+  int rig;                     // 1: task disparities are main-camera ones, scaled by disp_num / disp_den
+  double disp_num, disp_den;   // aux / main disparity radius
   double rad_coeff[7];
   double rXY[TP_MAXS][2];
   double pXY0[TP_MAXS][2];

@@ -42,15 +42,23 @@ __device__ __forceinline__ void mat3_vec(const double m[3][3], const double v[3]
   }
 }
 
+// undistorted tile centre, the sensor-independent head of getPortsCoordinatesAndDerivatives, with
+// the centre model (gc_main, 2179-2185)
+__device__ __forceinline__ void center_undistort(const GeomDev &g, const double *tbl, double px, double py,
+                                                 double &pXc, double &pYc) {
+  const double pXcd = DSUB(px, DMUL(0.5, (double)g.c_pixel_width));
+  const double pYcd = DSUB(py, DMUL(0.5, (double)g.c_pixel_height));
+  const double rD = DMUL(DMUL(DSQRT(DADD(DMUL(pXcd, pXcd), DMUL(pYcd, pYcd))), 0.001), g.c_pixel_size);
+  const double rND2R = r_by_rdist(tbl, g.tbl_len, DDIV(rD, g.c_distortion_radius));
+  pXc = DMUL(pXcd, rND2R);
+  pYc = DMUL(pYcd, rND2R);
+}
+
 // getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2159-2314) for one sensor
 __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double py, double disparity, int i,
                         double &ox, double &oy, double *deriv /* [2][5] or null */) {
-  double pXcd = DSUB(px, DMUL(0.5, (double)g.pixel_width));
-  double pYcd = DSUB(py, DMUL(0.5, (double)g.pixel_height));
-  double rD = DMUL(DMUL(DSQRT(DADD(DMUL(pXcd, pXcd), DMUL(pYcd, pYcd))), 0.001), g.pixel_size);
-  double rND2R = r_by_rdist(tbl, g.tbl_len, DDIV(rD, g.distortion_radius));
-  double pXc = DMUL(pXcd, rND2R);
-  double pYc = DMUL(pYcd, rND2R);
+  double pXc, pYc;
+  center_undistort(g, tbl, px, py, pXc, pYc);
   double fl_pix = DDIV(g.focal_length, DMUL(0.001, g.pixel_size));
   double ri_scale = DDIV(DMUL(0.001, g.pixel_size), g.distortion_radius);
   double vi[3] = {DSUB(pXc, DMUL(disparity, g.rXY[i][0])), DSUB(pYc, DMUL(disparity, g.rXY[i][1])), fl_pix};
@@ -101,17 +109,6 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
   }
 }
 
-// undistorted tile centre, the sensor-independent head of getPortsCoordinatesAndDerivatives
-__device__ __forceinline__ void center_undistort(const GeomDev &g, const double *tbl, double px, double py,
-                                                 double &pXc, double &pYc) {
-  const double pXcd = DSUB(px, DMUL(0.5, (double)g.pixel_width));
-  const double pYcd = DSUB(py, DMUL(0.5, (double)g.pixel_height));
-  const double rD = DMUL(DMUL(DSQRT(DADD(DMUL(pXcd, pXcd), DMUL(pYcd, pYcd))), 0.001), g.pixel_size);
-  const double rND2R = r_by_rdist(tbl, g.tbl_len, DDIV(rD, g.distortion_radius));
-  pXc = DMUL(pXcd, rND2R);
-  pYc = DMUL(pYcd, rND2R);
-}
-
 // sensor part of getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2190-2217)
 __device__ __forceinline__ void sensor_port(const GeomDev &g, double pXc, double pYc, double disparity, int i,
                                             double &ox, double &oy) {
@@ -148,6 +145,8 @@ __device__ __forceinline__ void plan_task(const SceneDev &sc, int task, int s0, 
   if (sc.ports_from_geometry) {
     center_undistort(*sc.geom, sc.rdist_tbl, ctx, cty, pXc, pYc);
     disparity = (double)sc.task_disp[task];
+    // a rig's auxiliary camera: disparity_main * aux radius / main radius (ImageDtt.java:8973)
+    if (sc.geom->rig) disparity = DDIV(DMUL(disparity, sc.geom->disp_num), sc.geom->disp_den);
   }
   const int ks = sc.kernel_step;
   const bool pow2 = ks > 0 && (ks & (ks - 1)) == 0;

@@ -35,6 +35,12 @@ class TpGeometry(C.Structure):
                 ("roll", C.c_double * TP_MAX_SENSORS), ("zoom", C.c_double * TP_MAX_SENSORS)]
 
 
+class TpRigOffset(C.Structure):
+    _fields_ = [("main_disparity_radius", C.c_double), ("aux_disparity_radius", C.c_double),
+                ("baseline", C.c_double), ("aux_angle", C.c_double), ("aux_azimuth", C.c_double),
+                ("aux_tilt", C.c_double), ("aux_roll", C.c_double), ("aux_zoom", C.c_double)]
+
+
 class TpPair(C.Structure):
     _fields_ = [("cam1", C.c_int), ("cam2", C.c_int), ("kind", C.c_int), ("in_combo", C.c_int),
                 ("bx", C.c_float), ("by", C.c_float)]
@@ -81,6 +87,7 @@ PROTOTYPES = {
     "tp_default_texture_params": [C.POINTER(TpTextureParams)],
     "tp_quad_pairs": [C.POINTER(TpPair), C.POINTER(C.c_int)],
     "tp_set_geometry": [_H, C.POINTER(TpGeometry)],
+    "tp_set_rig_geometry": [_H, C.POINTER(TpGeometry), C.POINTER(TpGeometry), C.POINTER(TpRigOffset)],
     "tp_set_kernels": [_H, C.c_int, _vp, _vp, C.c_int],
     "tp_set_image": [_H, C.c_int, _vp, C.c_int, C.c_size_t],
     "tp_set_image_async": [_H, C.c_int, _vp, C.c_int, C.c_size_t, _vp],

@@ -61,22 +61,37 @@ class GPUTileProcessor:
         self.close()
 
     # ---- inputs (GPUTileProcessor.java:363-527, 780-848) ----
-    def setGeometry(self, g):
-        """g: dict with keys width, height, focal_length, pixel_size, distortion_radius,
-        distortion[7], rXY[S][2], pXY0[S][2], azimuth/tilt/roll/zoom[S]."""
+    @staticmethod
+    def _geometry(g, num_sensors):
         G = L.TpGeometry()
         G.pixel_width, G.pixel_height = int(g["width"]), int(g["height"])
         G.focal_length, G.pixel_size = float(g["focal_length"]), float(g["pixel_size"])
         G.distortion_radius = float(g["distortion_radius"])
         for i in range(7):
             G.distortion[i] = float(g["distortion"][i])
-        for s in range(self.num_sensors):
+        for s in range(num_sensors):
             for k in range(2):
                 G.rXY[s][k] = float(g["rXY"][s][k])
                 G.pXY0[s][k] = float(g["pXY0"][s][k])
             G.azimuth[s], G.tilt[s] = float(g["azimuth"][s]), float(g["tilt"][s])
             G.roll[s], G.zoom[s] = float(g["roll"][s]), float(g["zoom"][s])
+        return G
+
+    def setGeometry(self, g):
+        """g: dict with keys width, height, focal_length, pixel_size, distortion_radius,
+        distortion[7], rXY[S][2], pXY0[S][2], azimuth/tilt/roll/zoom[S]."""
+        G = self._geometry(g, self.num_sensors)
         self._ck(self._lib.tp_set_geometry(self.h, C.byref(G)), "tp_set_geometry")
+
+    def setRigGeometry(self, aux, main, rig):
+        """This camera as a rig's auxiliary one (GeometryCorrection.RigOffset; the ports of
+        ImageDtt.clt_bi_quad): aux / main geometry dicts as setGeometry's (main with the main camera's
+        sensor count), rig a dict of main_disparity_radius, aux_disparity_radius, baseline, aux_angle,
+        aux_azimuth, aux_tilt, aux_roll, aux_zoom.  Task disparities are then the main camera's."""
+        A = self._geometry(aux, self.num_sensors)
+        M = self._geometry(main, int(main.get("num_sensors", self.num_sensors)))
+        R = L.TpRigOffset(*[float(rig[name]) for name, _ in L.TpRigOffset._fields_])
+        self._ck(self._lib.tp_set_rig_geometry(self.h, C.byref(A), C.byref(M), C.byref(R)), "tp_set_rig_geometry")
 
     def setConvolutionKernel(self, kernel, kernel_offsets, ncam, layout=L.TP_KERNELS_GPU):
         k = np.ascontiguousarray(kernel, dtype=np.float32)

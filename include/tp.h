@@ -148,6 +148,26 @@ tp_status tp_quad_pairs(tp_pair *pairs, int *n);
 /* inputs */
 /* GeometryCorrection set-up used by stage 1 (getPortsCoordinatesAndDerivatives) */
 tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g);
+
+/* The auxiliary camera of a rig (GeometryCorrection.RigOffset, GeometryCorrection.java:256-975). */
+typedef struct {
+  double main_disparity_radius;  /* mm: GeometryCorrection.disparityRadius of the main camera */
+  double aux_disparity_radius;   /* mm: of the auxiliary camera */
+  double baseline;               /* mm: auxiliary centre from the main one */
+  double aux_angle;              /* rad: direction of the baseline */
+  double aux_azimuth, aux_tilt, aux_roll; /* rad: the auxiliary camera's rotation */
+  double aux_zoom;               /* zoom - 1 */
+} tp_rig_offset;
+/* Makes h a rig's auxiliary camera, with ports as ImageDtt.clt_bi_quad computes them
+ * (ImageDtt.java:8972-8996, getPortsCoordinatesAndDerivatives(gc_main, use_rig_offsets = true)):
+ * aux is this camera's own model, main_camera the main camera's.  Task disparities are then the
+ * main camera's, scaled by aux / main disparity radius; the tile centre is undistorted with the
+ * main camera's model; the lens offsets are RigOffset.rXY_aux (recalcRXY 728-747: the baseline
+ * offset plus the lens offsets rotated by aux_roll); each sensor's rotation is followed by the rig
+ * rotation (CorrVector.getRotMatrices(rigMatrix) 1016-1025, RigOffset.getRotMatrix 770-800).
+ * main_camera or rig NULL: as tp_set_geometry(h, aux).  tp_backward refuses such a handle. */
+tp_status tp_set_rig_geometry(tp_handle *h, const tp_geometry *aux, const tp_geometry *main_camera,
+                              const tp_rig_offset *rig);
 /* setConvolutionKernel (GPUTileProcessor.java:373-379) / setConvolutionKernels (381-435) */
 tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const float *kernel_offsets, int layout);
 /* setBayerImage (GPUTileProcessor.java:437-450); pitch in elements (0 = width) */

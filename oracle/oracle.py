@@ -84,6 +84,10 @@ def lib():
         L.or_r_by_rdist.restype = C.c_double
         L.or_ports.argtypes = [C.POINTER(Geometry), _dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
                                C.c_double, _dp, _dp]
+        L.or_rig_aux_ports.argtypes = [C.POINTER(Geometry), C.POINTER(Geometry), C.POINTER(RigOffset), C.c_double,
+                                       C.c_double, C.c_double, _dp]
+        L.or_rig_rxy.argtypes = [C.POINTER(Geometry), C.POINTER(RigOffset), _dp]
+        L.or_rig_matrix.argtypes = [C.POINTER(RigOffset), _dp]
         L.or_default_corr_params.argtypes = [C.POINTER(CorrParams)]
         L.or_quad_pairs.argtypes = [C.POINTER(Pairs)]
         L.or_correlate_pair.argtypes = [_dp, _dp, C.c_int, _dp, _dp, C.c_double, _dp]
@@ -295,6 +299,38 @@ def ports(g, px, py, disparity, deriv=False):
     lib().or_ports(C.byref(G), _d(rots), _d(drots), _d(tbl), n, float(px), float(py), float(disparity),
                    _d(out), _d(dv) if deriv else None)
     return (out[:S], dv[:S]) if deriv else out[:S]
+
+
+class RigOffset(C.Structure):
+    """GeometryCorrection.RigOffset of an auxiliary camera (GeometryCorrection.java:256-975)."""
+    _fields_ = [("main_disparity_radius", C.c_double), ("aux_disparity_radius", C.c_double),
+                ("baseline", C.c_double), ("aux_angle", C.c_double), ("aux_azimuth", C.c_double),
+                ("aux_tilt", C.c_double), ("aux_roll", C.c_double), ("aux_zoom", C.c_double)]
+
+
+def make_rig(r):
+    """r: dict with the RigOffset fields above."""
+    R = RigOffset()
+    for name, _ in RigOffset._fields_:
+        setattr(R, name, float(r[name]))
+    return R
+
+
+def rig_aux_ports(aux, main, rig, px, py, disparity_main):
+    """ImageDtt.clt_bi_quad's auxiliary-camera ports (ImageDtt.java:8972-8996) -> [S][2]."""
+    A, M, R = make_geometry(aux), make_geometry(main), make_rig(rig)
+    out = np.zeros((OR_MAX_SENSORS, 2))
+    lib().or_rig_aux_ports(C.byref(A), C.byref(M), C.byref(R), float(px), float(py), float(disparity_main),
+                           _d(out))
+    return out[:A.num_sensors]
+
+
+def rig_rxy(aux, rig):
+    """RigOffset.recalcRXY -> rXY_aux [S][2]."""
+    A, R = make_geometry(aux), make_rig(rig)
+    out = np.zeros((OR_MAX_SENSORS, 2))
+    lib().or_rig_rxy(C.byref(A), C.byref(R), _d(out))
+    return out[:A.num_sensors]
 
 
 # ---- correlation ----

@@ -570,13 +570,15 @@ static void mat3_vec(const double m[3][3], const double v[3], double r[3]) {
 }
 
 /* getPortsCoordinatesAndDerivatives (2159-2314), main camera (gc_main == this, no rig) */
-void or_ports(const or_geometry *g, const double rots[][3][3], const double drots[][4][3][3],
-              const double *tbl, int tbl_len, double px, double py, double disparity,
-              double pXY[][2], double deriv[][2][4]) {
-  double pXcd = px - 0.5 * g->pixel_width;
-  double pYcd = py - 0.5 * g->pixel_height;
-  double rD = sqrt(pXcd * pXcd + pYcd * pYcd) * 0.001 * g->pixel_size;
-  double rND2R = or_r_by_rdist(tbl, tbl_len, rD / g->distortion_radius);
+/* getPortsCoordinatesAndDerivatives with the tile centre undistorted by the model gc (the
+ * reference's gc_main argument, 2179-2185) and everything after by g */
+static void ports_core(const or_geometry *gc, const double *tblc, int tblc_len, const or_geometry *g,
+                       const double rots[][3][3], const double drots[][4][3][3], double px, double py,
+                       double disparity, double pXY[][2], double deriv[][2][4]) {
+  double pXcd = px - 0.5 * gc->pixel_width;
+  double pYcd = py - 0.5 * gc->pixel_height;
+  double rD = sqrt(pXcd * pXcd + pYcd * pYcd) * 0.001 * gc->pixel_size;
+  double rND2R = or_r_by_rdist(tblc, tblc_len, rD / gc->distortion_radius);
   double pXc = pXcd * rND2R;
   double pYc = pYcd * rND2R;
   const double *rad_coeff = g->distortion; /* C, B, A, A5, A6, A7, A8 */
@@ -629,6 +631,57 @@ void or_ports(const or_geometry *g, const double rots[][3][3], const double drot
       }
     }
   }
+}
+
+void or_ports(const or_geometry *g, const double rots[][3][3], const double drots[][4][3][3],
+              const double *tbl, int tbl_len, double px, double py, double disparity,
+              double pXY[][2], double deriv[][2][4]) {
+  ports_core(g, tbl, tbl_len, g, rots, drots, px, py, disparity, pXY, deriv);
+}
+
+/* RigOffset.getRotMatrix (GeometryCorrection.java:770-800): aux roll (with zoom) x tilt x azimuth */
+void or_rig_matrix(const or_rig_offset *rig, double m[3][3]) {
+  const double ca = cos(rig->aux_azimuth), sa = sin(rig->aux_azimuth);
+  const double ct = cos(rig->aux_tilt), st = sin(rig->aux_tilt);
+  const double zoom = 1.0 + rig->aux_zoom;
+  const double cr = cos(rig->aux_roll) * zoom, sr = sin(rig->aux_roll) * zoom;
+  const double AZ = -1.0, TL = 1.0, RL = 1.0; /* ROT_AZ_SGN, ROT_TL_SGN, ROT_RL_SGN */
+  const double a_az[3][3] = {{ca, 0.0, sa * AZ}, {0.0, 1.0, 0.0}, {-sa * AZ, 0.0, ca}};
+  const double a_t[3][3] = {{1.0, 0.0, 0.0}, {0.0, ct, st * TL}, {0.0, -st * TL, ct}};
+  const double a_r[3][3] = {{cr, sr * RL, 0.0}, {-sr * RL, cr, 0.0}, {0.0, 0.0, 1.0}};
+  double t[3][3];
+  mat3_mul(a_t, a_az, t);
+  mat3_mul(a_r, t, m);
+}
+
+/* RigOffset.recalcRXY (728-747): per-sensor lens offsets of the auxiliary camera in its own
+ * disparity units: the baseline offset plus the rXY rotated by the aux roll */
+void or_rig_rxy(const or_geometry *aux, const or_rig_offset *rig, double rxy[][2]) {
+  const double xc_pix = rig->baseline * cos(rig->aux_angle) / rig->aux_disparity_radius;
+  const double yc_pix = rig->baseline * sin(rig->aux_angle) / rig->aux_disparity_radius;
+  const double ssr = 1.0;
+  for (int i = 0; i < aux->num_sensors; i++) {
+    rxy[i][0] = xc_pix + cos(rig->aux_roll) * aux->rXY[i][0] + ssr * sin(rig->aux_roll) * aux->rXY[i][1];
+    rxy[i][1] = yc_pix - ssr * sin(rig->aux_roll) * aux->rXY[i][0] + cos(rig->aux_roll) * aux->rXY[i][1];
+  }
+}
+
+void or_rig_aux_ports(const or_geometry *aux, const or_geometry *main_g, const or_rig_offset *rig, double px,
+                      double py, double disparity_main, double pXY[][2]) {
+  or_geometry g = *aux;
+  or_rig_rxy(aux, rig, g.rXY);
+  double rots[OR_MAX_SENSORS][3][3], rm[3][3];
+  or_rot_matrices(aux, rots);
+  or_rig_matrix(rig, rm);
+  for (int i = 0; i < aux->num_sensors; i++) { /* CorrVector.getRotMatrices(rigMatrix) 1016-1025 */
+    double t[3][3];
+    mat3_mul(rots[i], rm, t);
+    memcpy(rots[i], t, sizeof(t));
+  }
+  static double tbl[2100];
+  const int tbl_len = or_reverse_distortion_table(main_g, tbl, 2100);
+  const double disparity = disparity_main * rig->aux_disparity_radius / rig->main_disparity_radius;
+  ports_core(main_g, tbl, tbl_len, &g, (const double(*)[3][3])rots, NULL, px, py, disparity, pXY, NULL);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -129,6 +129,23 @@ void or_ports(const or_geometry *g, const double rots[][3][3],
               double px, double py, double disparity,
               double pXY[][2], double deriv[][2][4]);
 
+/* GeometryCorrection.RigOffset (256-975): the auxiliary camera's place in a rig */
+typedef struct {
+  double main_disparity_radius, aux_disparity_radius; /* mm, each camera's disparityRadius */
+  double baseline, aux_angle;                         /* mm, rad: aux centre from the main one */
+  double aux_azimuth, aux_tilt, aux_roll, aux_zoom;   /* rad, rad, rad, zoom - 1 */
+} or_rig_offset;
+/* RigOffset.getRotMatrix (770-800) */
+void or_rig_matrix(const or_rig_offset *rig, double m[3][3]);
+/* RigOffset.recalcRXY (728-747): rXY_aux [S][2] */
+void or_rig_rxy(const or_geometry *aux, const or_rig_offset *rig, double rxy[][2]);
+/* the auxiliary camera's ports as ImageDtt.clt_bi_quad computes them (8972-8996): the main
+ * camera's disparity scaled by aux / main disparity radius, the centre undistorted with the main
+ * camera's model, rXY_aux, each sensor's rotation times the rig matrix
+ * (CorrVector.getRotMatrices(rigMatrix) 1016-1025) */
+void or_rig_aux_ports(const or_geometry *aux, const or_geometry *main_g, const or_rig_offset *rig, double px,
+                      double py, double disparity_main, double pXY[][2]);
+
 /* ---- Correlation2d ---- */
 typedef struct {
   int num_pairs;

@@ -77,3 +77,57 @@ def test_rig_rejects_mismatched_cameras():
         tm.setCorrelation()
         with pytest.raises(_lib.TpError, match="differ in tile grid"):
             tm.rigCorrelate(ta)
+
+
+def _aux_geometry(g, rng):
+    """Another quad camera: its own lens (focal length, distortion, sensor centres) and extrinsics."""
+    a = {k: (np.array(v, dtype=np.float64).copy() if isinstance(v, (list, tuple, np.ndarray)) else v)
+         for k, v in g.items()}
+    a["focal_length"] = g["focal_length"] * 1.05
+    a["distortion"] = np.asarray(g["distortion"], np.float64) * 0.9
+    a["pXY0"] = np.asarray(g["pXY0"], np.float64) + rng.uniform(-1.5, 1.5, (g["num_sensors"], 2))
+    for k in ("azimuth", "tilt", "roll"):
+        a[k] = np.asarray(g[k], np.float64) + rng.normal(0, 2e-3, g["num_sensors"])
+    a["zoom"] = np.asarray(g["zoom"], np.float64) + rng.normal(0, 1e-3, g["num_sensors"])
+    return a
+
+
+RIG = dict(main_disparity_radius=21.0, aux_disparity_radius=18.5, baseline=6.0, aux_angle=0.35,
+           aux_azimuth=1.5e-3, aux_tilt=-2e-3, aux_roll=4e-3, aux_zoom=1e-3)
+
+
+def test_rig_aux_geometry(oracle):
+    """The auxiliary camera's ports with GeometryCorrection.RigOffset (ImageDtt.clt_bi_quad,
+    ImageDtt.java:8972-8996): main-camera disparities scaled by the radii, the centre undistorted with
+    the main camera's lens, rXY_aux and the rig rotation.  Ports bit-exact against the oracle on every
+    tile, the auxiliary CLT / correlation at the forward's tolerances, then the rig correlation."""
+    from helpers import run_oracle
+    sc = synth.make_scene("quad_mono", seed=31, width=128, height=96)
+    W, H = sc["width"], sc["height"]
+    T = (W // 8) * (H // 8)
+    rng = np.random.default_rng(32)
+    g_main = sc["geometry"]
+    g_aux = _aux_geometry(g_main, rng)
+    disp = rng.uniform(0.5, 4.0, T).astype(np.float32)  # main-camera disparities
+    tx, ty = np.arange(T) % (W // 8), np.arange(T) // (W // 8)
+    want = np.array([oracle.rig_aux_ports(g_aux, g_main, RIG, x * 8 + 4, y * 8 + 4, d)
+                     for x, y, d in zip(tx, ty, disp.astype(np.float64))])
+    ref = run_oracle(oracle, sc, 0.0, ports_in=want)
+    with make_gpu(sc) as tm, make_gpu(sc) as ta:
+        ta.setRigGeometry(g_aux, g_main, RIG)
+        for tp in (tm, ta):
+            tp.setCorrelation()
+            tp.setFullFrameImages(disp)
+            tp.process()
+        got = ta.getPorts()
+        assert np.array_equal(got, want), "aux ports differ: max %g" % np.abs(got - want).max()
+        e = rel_l2(ta.getClt().astype(np.float64), ref["clt"], axis=(-2, -1))
+        assert e.max() <= 2e-6, "aux CLT rel L2 max %.3g" % e.max()
+        e = rel_l2(ta.getCorr().astype(np.float64), ref["corr"], axis=-1)
+        assert e.max() <= 1e-5, "aux corr rel L2 max %.3g" % e.max()
+        _rig_check(oracle, tm, ta, np.ones(T, np.int32))
+        # without the rig the same handle computes the camera's own ports
+        ta.setGeometry(g_aux)
+        ta.process()
+        own = np.array([oracle.ports(g_aux, x * 8 + 4, y * 8 + 4, d) for x, y, d in zip(tx, ty, disp.astype(np.float64))])
+        assert np.array_equal(ta.getPorts(), own)
