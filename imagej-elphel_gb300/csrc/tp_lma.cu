@@ -221,11 +221,13 @@ __device__ __forceinline__ void lma_eval(const float *sx, const float *sy, const
 // One Correlation2d.corrLMA fit of a tile from the staged pair surfaces `src` ([P][225]) of the
 // pair kinds in kmask (bit k: kind k), centred at xcenter: res = {disparity, strength, WM, WXY}
 // (getDisparityStrengthWidth); false when there are no samples or the fit did not converge.
-// Samples of the pairs in pmask (bit = pair index; pairs of kind -1 never): the group surfaces
-// (combineCompatiblePairs), filterConvex around the integer centre and addSamples with weights
-// x |value|^vasw_pwr, compacted into sx/sy/sv/sw/sg in the reference's order.  Returns the
-// sample count; ngroups / gdiag_bits (bit g: group g is the diagonal one) describe the groups.
-__device__ __forceinline__ int lma_samples(const LmaDev &ld, const TpLmaConst &c, unsigned pmask, float xcenter,
+// Samples of the selected pairs (BY_PAIR: bit = pair index, else bit = pair kind; pairs of kind -1
+// never): the group surfaces (combineCompatiblePairs), filterConvex around the integer centre and
+// addSamples with weights x |value|^vasw_pwr, compacted into sx/sy/sv/sw/sg in the reference's
+// order.  Returns the sample count; ngroups / gdiag_bits (bit g: group g is the diagonal one)
+// describe the groups.
+template <bool BY_PAIR>
+__device__ __forceinline__ int lma_samples(const LmaDev &ld, const TpLmaConst &c, unsigned sel_mask, float xcenter,
                                            float vasw_pwr, const float *src, float *gsurf, float *sx, float *sy,
                                            float *sv, float *sw, unsigned char *sg, int lane, int &ngroups_out,
                                            int &gdiag_bits_out) {
@@ -235,7 +237,7 @@ __device__ __forceinline__ int lma_samples(const LmaDev &ld, const TpLmaConst &c
   int np_ortho = 0, np_diag = 0;
   for (int pi = 0; pi < ld.P; pi++) {
     const int k = ld.kinds[pi];
-    if (k < 0 || !((pmask >> pi) & 1)) continue;
+    if (k < 0 || !((sel_mask >> (BY_PAIR ? pi : k)) & 1)) continue;
     np_ortho += (k <= 1);
     np_diag += (k >= 2);
   }
@@ -245,7 +247,7 @@ __device__ __forceinline__ int lma_samples(const LmaDev &ld, const TpLmaConst &c
   for (int t = 0; t < 8; t++) go[t] = gdg[t] = 0.f;
   for (int pi = 0; pi < ld.P; pi++) {
     const int k = ld.kinds[pi];
-    if (k < 0 || !((pmask >> pi) & 1)) continue;
+    if (k < 0 || !((sel_mask >> (BY_PAIR ? pi : k)) & 1)) continue;
     const float *cs = src + pi * TP_CORR;
 #pragma unroll
     for (int t = 0; t < 8; t++) {
@@ -397,12 +399,9 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
                                         const float *src, float *gsurf, float *sx, float *sy, float *sv, float *sw,
                                         unsigned char *sg, float *red, float *acc, float *trial, int lane,
                                         float res[4]) {
-  unsigned pmask = 0;
-  for (int pi = 0; pi < ld.P; pi++)
-    if (ld.kinds[pi] >= 0 && ((kmask >> ld.kinds[pi]) & 1)) pmask |= 1u << pi;
   int ngroups, gdiag_bits;
-  const int ns = lma_samples(ld, c, pmask, xcenter, c.ortho_vasw_pwr, src, gsurf, sx, sy, sv, sw, sg, lane, ngroups,
-                             gdiag_bits);
+  const int ns = lma_samples<false>(ld, c, (unsigned)kmask, xcenter, c.ortho_vasw_pwr, src, gsurf, sx, sy, sv, sw, sg,
+                                    lane, ngroups, gdiag_bits);
   if (ns == 0) return false;
   // ---- initVector / setWeightsValues ----
   float wsum = 0.f, gw0 = 0.f, gw1 = 0.f, vmax = -CUDART_INF_F, smax = 0.f;
@@ -772,8 +771,8 @@ __global__ void __launch_bounds__(32 * LMA_NW) lma_kernel(const __grid_constant_
             for (int pi = c0; pi < c1; pi++) {
               if (ld.kinds[pi] < 0) continue;
               int ng, gdb;
-              const int ns = lma_samples(ld, c, 1u << pi, -disparity, c.max_corr_radius, src, gsurf, sx, sy, sv, sw, sg,
-                                         lane, ng, gdb);
+              const int ns = lma_samples<true>(ld, c, 1u << pi, -disparity, c.max_corr_radius, src, gsurf, sx, sy, sv,
+                                               sw, sg, lane, ng, gdb);
               quadric_moments(sx, sy, sv, sw, ns, lane, dmom + (pi - c0) * 21);
               if (lane == pi - c0) my_ns = ns;
               __syncwarp();  // the next pair's samples overwrite these; the moments are written
