@@ -623,12 +623,20 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
+        # the reference arm's own measurement, in a fresh process: this one holds the CUDA context,
+        # torch's thread pools and the timing threads, which slowed the oracle's threads by ~2.5x
         sample = args.cpu_sample_tiles or (4000 if Cn == 3 else 2000)
-        v, n, dt = cpu_baseline_runs(w, sample, threads, 1, 2)
-        cpu = {"value": v, "unit": "tiles/s", "cores": threads, "kind": "port",
-               "sample": "%d of %d tiles (every %d-th) per run, 1 warm-up + 2 timed runs, stages 1-4%s, "
-                         "FP64 C restatement" % (n, T, max(1, T // sample), "b" if with_tex else "a")}
+        env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--config", args.config,
+                            "--seed", str(args.seed), "--steps", "2", "--warmup", "1", "--cpu-sample-tiles",
+                            str(sample)], env=env, capture_output=True, text=True, check=True)
+        ref_line = json.loads(r.stdout.strip().splitlines()[-1])
+        cb = ref_line["cpu_baseline"]
+        cpu = {"value": cb["value"], "unit": "tiles/s", "cores": cb["cores"], "kind": "port",
+               "sample": "%d of %d tiles (every %d-th) per run, 1 warm-up + 2 timed runs, stages 1-4%s, FP64 C "
+                         "restatement, in a separate process (bench.py --impl reference)" % (
+                             ref_line["config"]["sample_tiles_per_step"], T, max(1, T // sample),
+                             "b" if with_tex else "a")}
     launches_per_step = 5 + int(with_tex)  # plan, tile map, disparity init, fused forward, imclt, textures
     line = {
         "metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,

@@ -131,3 +131,12 @@ def test_rig_aux_geometry(oracle):
         ta.process()
         own = np.array([oracle.ports(g_aux, x * 8 + 4, y * 8 + 4, d) for x, y, d in zip(tx, ty, disp.astype(np.float64))])
         assert np.array_equal(ta.getPorts(), own)
+
+
+def test_rig_geometry_rejects_bad_radii():
+    from tileproc import _lib
+    sc = synth.make_scene("quad_mono", seed=33, width=64, height=64)
+    bad = dict(RIG, aux_disparity_radius=0.0)
+    with make_gpu(sc) as ta:
+        with pytest.raises(_lib.TpError, match="disparity radii"):
+            ta.setRigGeometry(sc["geometry"], sc["geometry"], bad)
