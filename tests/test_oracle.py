@@ -217,3 +217,41 @@ def test_texture_outlier_port_is_suppressed(oracle):
     centre[4:12, 4:12] = True
     w = rgba[4:8].reshape(4, 16, 16)[:, centre]
     assert np.median(w[1]) < 0.2 and np.median(w[0]) > 0.9
+
+
+def _rig(**kw):
+    r = dict(main_disparity_radius=20.0, aux_disparity_radius=20.0, baseline=0.0, aux_angle=0.0, aux_azimuth=0.0,
+             aux_tilt=0.0, aux_roll=0.0, aux_zoom=0.0)
+    r.update(kw)
+    return r
+
+
+def test_rig_ports_reduce_to_the_camera_ports(oracle):
+    """RigOffset with no offset, no rotation and equal radii: the auxiliary ports are the camera's own."""
+    g = synth.make_scene("quad_mono", seed=3, width=128, height=96)["geometry"]
+    for px, py, d in ((20.0, 12.0, 0.5), (100.0, 76.0, 3.25)):
+        assert np.array_equal(oracle.rig_aux_ports(g, g, _rig(), px, py, d), oracle.ports(g, px, py, d))
+
+
+def test_rig_baseline_is_a_lens_offset_at_the_scaled_disparity(oracle):
+    """A pure baseline (recalcRXY): rXY_aux = rXY + baseline (cos, sin)(angle) / aux radius, and the main
+    camera's disparity is scaled by aux / main radius (ImageDtt.java:8973)."""
+    g = synth.make_scene("quad_mono", seed=3, width=128, height=96)["geometry"]
+    rig = _rig(main_disparity_radius=25.0, aux_disparity_radius=20.0, baseline=8.0, aux_angle=0.6)
+    shifted = dict(g)
+    off = np.array([8.0 * np.cos(0.6), 8.0 * np.sin(0.6)]) / 20.0
+    shifted["rXY"] = np.asarray(g["rXY"], np.float64) + off
+    got = oracle.rig_aux_ports(g, g, rig, 64.0, 40.0, 2.0)
+    want = oracle.ports(shifted, 64.0, 40.0, 2.0 * 20.0 / 25.0)
+    assert np.allclose(got, want, atol=1e-12)
+    rxy = oracle.rig_rxy(g, rig)
+    assert np.allclose(rxy, shifted["rXY"], atol=1e-15)
+
+
+def test_rig_roll_rotates_the_lens_offsets(oracle):
+    g = synth.make_scene("quad_mono", seed=3, width=128, height=96)["geometry"]
+    a = 0.3
+    rxy = oracle.rig_rxy(g, _rig(aux_roll=a))
+    r = np.asarray(g["rXY"], np.float64)
+    want = np.stack([np.cos(a) * r[:, 0] + np.sin(a) * r[:, 1], -np.sin(a) * r[:, 0] + np.cos(a) * r[:, 1]], -1)
+    assert np.allclose(rxy, want, atol=1e-15)
