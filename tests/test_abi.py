@@ -69,3 +69,33 @@ def test_argument_validation_without_gpu():
     assert L.tp_quad_pairs(pairs, ctypes.byref(n)) == _lib.TP_OK and n.value == 6
     assert [(pairs[i].cam1, pairs[i].cam2, pairs[i].kind) for i in range(6)] == \
         [(0, 1, 0), (2, 3, 0), (0, 2, 1), (1, 3, 1), (0, 3, 2), (2, 1, 3)]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror of an include/tp.h struct has the C layout: sizeof and each field's offset,
+    from a probe compiled against the header with the host compiler."""
+    import shutil
+    import subprocess
+    from tileproc import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [("tp_config", _lib.TpConfig), ("tp_geometry", _lib.TpGeometry), ("tp_rig_offset", _lib.TpRigOffset),
+             ("tp_pair", _lib.TpPair), ("tp_corr_params", _lib.TpCorrParams),
+             ("tp_texture_params", _lib.TpTextureParams), ("tp_lma_params", _lib.TpLmaParams)]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "tp.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append('  printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (l.split() for l in out if l.strip())}
+    for cname, py in pairs:
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
