@@ -438,72 +438,80 @@ __device__ __forceinline__ bool lma_fit(const LmaDev &ld, const TpLmaConst &c, i
   if (ngroups < 2) av[5] = 0.f;
   // ---- runLma / lmaStep ----
   // acc: normal equations at the accepted parameters; trial: at the proposed ones
-  lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, av, w_wm, w_wxy, c.half_width, red, acc, lane);
-  float last = sqrtf(acc[27]);
-  const float initial = last;
+  // iteration -1 evaluates the start (into acc); one inlined evaluation serves all
+  float last = 0.f, initial = 0.f;
   float lambda = c.lambda_initial;
   bool success = false;
-  for (int iter = 0; iter < c.num_iter; iter++) {
-    // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held (identity rows).
-    // The matrix is symmetric positive (semi)definite: LDL^T without pivoting; a pivot that is
-    // not positive marks it singular, as the zero pivot of the reference's LU inverse does.
-    float M[LMA_NP][LMA_NP], rhs[LMA_NP];
-    {
-      int k = 0;
-#pragma unroll
-      for (int a = 0; a < LMA_NP; a++)
-#pragma unroll
-        for (int cc = a; cc < LMA_NP; cc++) {
-          const bool keep = mask[a] && mask[cc];
-          const float v = keep ? acc[k] : ((a == cc) ? 1.0f : 0.0f);
-          M[a][cc] = v;
-          M[cc][a] = v;
-          k++;
-        }
-    }
-#pragma unroll
-    for (int a = 0; a < LMA_NP; a++) {
-      if (mask[a]) M[a][a] += M[a][a] * lambda;
-      rhs[a] = mask[a] ? acc[21 + a] : 0.0f;
-    }
-    float Lm[LMA_NP][LMA_NP], Dd[LMA_NP], Dinv[LMA_NP];
-    bool singular = false;
-#pragma unroll
-    for (int r = 0; r < LMA_NP; r++) {
-#pragma unroll
-      for (int cc = 0; cc < r; cc++) {
-        float t = M[r][cc];
-#pragma unroll
-        for (int k = 0; k < cc; k++) t -= Lm[r][k] * Lm[cc][k] * Dd[k];
-        Lm[r][cc] = t * Dinv[cc];
-      }
-      float dd = M[r][r];
-#pragma unroll
-      for (int k = 0; k < r; k++) dd -= Lm[r][k] * Lm[r][k] * Dd[k];
-      if (!(dd > 0.0f)) singular = true;
-      Dd[r] = dd;
-      Dinv[r] = (dd > 0.0f) ? 1.0f / dd : 0.0f;
-    }
-    if (singular) break;
-    float delta[LMA_NP];
-#pragma unroll
-    for (int r = 0; r < LMA_NP; r++) {
-      float t = rhs[r];
-#pragma unroll
-      for (int k = 0; k < r; k++) t -= Lm[r][k] * delta[k];
-      delta[r] = t;
-    }
-#pragma unroll
-    for (int r = LMA_NP - 1; r >= 0; r--) {
-      float t = delta[r] * Dinv[r];
-#pragma unroll
-      for (int k = r + 1; k < LMA_NP; k++) t -= Lm[k][r] * delta[k];
-      delta[r] = t;
-    }
+  for (int iter = -1; iter < c.num_iter; iter++) {
     float nav[LMA_NP];
+    if (iter < 0) {
 #pragma unroll
-    for (int a = 0; a < LMA_NP; a++) nav[a] = av[a] + (mask[a] ? delta[a] : 0.0f);
-    lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, nav, w_wm, w_wxy, c.half_width, red, trial, lane);
+      for (int a = 0; a < LMA_NP; a++) nav[a] = av[a];
+    } else {
+      // (JtJ + lambda diag JtJ) delta = Jt W (y - f), masked parameters held (identity rows).
+      // The matrix is symmetric positive (semi)definite: LDL^T without pivoting; a pivot that is
+      // not positive marks it singular, as the zero pivot of the reference's LU inverse does.
+      float M[LMA_NP][LMA_NP], rhs[LMA_NP];
+      {
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < LMA_NP; a++)
+#pragma unroll
+          for (int cc = a; cc < LMA_NP; cc++) {
+            const bool keep = mask[a] && mask[cc];
+            const float v = keep ? acc[k] : ((a == cc) ? 1.0f : 0.0f);
+            M[a][cc] = v;
+            M[cc][a] = v;
+            k++;
+          }
+      }
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++) {
+        if (mask[a]) M[a][a] += M[a][a] * lambda;
+        rhs[a] = mask[a] ? acc[21 + a] : 0.0f;
+      }
+      float Lm[LMA_NP][LMA_NP], Dd[LMA_NP], Dinv[LMA_NP];
+      bool singular = false;
+#pragma unroll
+      for (int r = 0; r < LMA_NP; r++) {
+#pragma unroll
+        for (int cc = 0; cc < r; cc++) {
+          float t = M[r][cc];
+#pragma unroll
+          for (int k = 0; k < cc; k++) t -= Lm[r][k] * Lm[cc][k] * Dd[k];
+          Lm[r][cc] = t * Dinv[cc];
+        }
+        float dd = M[r][r];
+#pragma unroll
+        for (int k = 0; k < r; k++) dd -= Lm[r][k] * Lm[r][k] * Dd[k];
+        if (!(dd > 0.0f)) singular = true;
+        Dd[r] = dd;
+        Dinv[r] = (dd > 0.0f) ? 1.0f / dd : 0.0f;
+      }
+      if (singular) break;
+      float delta[LMA_NP];
+#pragma unroll
+      for (int r = 0; r < LMA_NP; r++) {
+        float t = rhs[r];
+#pragma unroll
+        for (int k = 0; k < r; k++) t -= Lm[r][k] * delta[k];
+        delta[r] = t;
+      }
+#pragma unroll
+      for (int r = LMA_NP - 1; r >= 0; r--) {
+        float t = delta[r] * Dinv[r];
+#pragma unroll
+        for (int k = r + 1; k < LMA_NP; k++) t -= Lm[k][r] * delta[k];
+        delta[r] = t;
+      }
+#pragma unroll
+      for (int a = 0; a < LMA_NP; a++) nav[a] = av[a] + (mask[a] ? delta[a] : 0.0f);
+    }
+    lma_eval(sx, sy, sv, sw, sg, gdiag_bits, ns, nav, w_wm, w_wxy, c.half_width, red, iter < 0 ? acc : trial, lane);
+    if (iter < 0) {
+      last = initial = sqrtf(acc[27]);
+      continue;
+    }
     const float rms = sqrtf(trial[27]);
     bool done = false;
     if (rms < last) {
