@@ -10,9 +10,11 @@ flush is needed between steps.
 
   value : tiles/s with all inputs resident in HBM (CUDA events on the launch stream)
   e2e   : tiles/s through the public C ABI with host buffers: H2D of the 4 raw
-          images and the tile ops + disparity from pinned memory, the forward,
-          and D2H of the disparity map, every step (host wall clock); the next
-          frame's images go up on a copy stream while IMCLT / textures run
+          images and the tile ops + disparity from pinned memory, the step, and
+          D2H of the disparity map and of every camera's RBG frames (what the
+          reference's caller reads back), every step (host wall clock); the next
+          frame's images go up on a copy stream while IMCLT / textures run, the
+          frames come down on another during the textures and the next forward
   --impl reference : the reference CPU path (the FP64 C restatement of
           ImageDtt/Correlation2d, the Java reference cannot run here) on all
           host cores, a bounded tile sample per step.
@@ -561,10 +563,13 @@ def run_ours(args):
     pin_op = torch.from_numpy(tile_op).pin_memory()
     pin_disp = torch.from_numpy(w["target"].copy()).pin_memory()
     out_disp = torch.empty((T, L.DISP_N), dtype=torch.float32).pin_memory()
+    # every camera's colour frames, as the reference's caller reads them (GPUTileProcessor.getRBG)
+    out_rbg = [torch.empty((Cn, w["H"] + 8, w["W"] + 8), dtype=torch.float32).pin_memory() for _ in range(S)]
     np_imgs = [p.numpy() for p in pin_imgs]
     np_op, np_disp, np_out = pin_op.numpy(), pin_disp.numpy(), out_disp.numpy()
+    np_rbg = [o.numpy() for o in out_rbg]
     h2d = sum(a.nbytes for a in np_imgs) + np_op.nbytes + np_disp.nbytes
-    d2h = np_out.nbytes
+    d2h = np_out.nbytes + sum(a.nbytes for a in np_rbg)
 
     # Frames are double-buffered the way a camera loop would run them: the sensor images are read
     # only by the forward, so the next frame's pinned images go up on a copy stream while this
@@ -573,6 +578,11 @@ def run_ours(args):
     copy_stream = torch.cuda.Stream()
     cptr = C.c_void_p(copy_stream.cuda_stream)
     up_done, fwd_done = torch.cuda.Event(), torch.cuda.Event()
+    # frame k's colour frames go down on their own stream during frame k's textures and frame
+    # k+1's forward; frame k+1's IMCLT (which rewrites them) waits for that copy
+    down_stream = torch.cuda.Stream()
+    dptr = C.c_void_p(down_stream.cuda_stream)
+    rbg_done = torch.cuda.Event()
 
     def upload_images():
         for s in range(S):
@@ -589,7 +599,11 @@ def run_ours(args):
         fwd_done.record(stream)
         copy_stream.wait_event(fwd_done)
         upload_images()
+        stream.wait_event(rbg_done)
         tp._ck(lib.tp_imclt(tp.h, sptr), "imclt")
+        for s in range(S):
+            tp._ck(lib.tp_get_rbg_async(tp.h, s, C.c_void_p(np_rbg[s].ctypes.data), dptr), "rbg")
+        rbg_done.record(down_stream)
         if with_tex:
             tp._ck(lib.tp_textures(tp.h, sptr), "textures")
         tp._ck(lib.tp_get_disparity(tp.h, C.c_void_p(np_out.ctypes.data)), "disp")
@@ -658,7 +672,9 @@ def run_ours(args):
                      "frac": ach / peak, "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": stage_b[dom]},
         "e2e": {"value": e2e_val, "unit": "tiles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "pipeline": "next frame's images uploaded on a copy stream during IMCLT and textures"},
+                "reads_back": "disparity record + every camera's RBG frames (getRBG), pinned host buffers",
+                "pipeline": "next frame's images uploaded on a copy stream during IMCLT and textures; RBG frames "
+                            "read back on a download stream during textures and the next forward"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,

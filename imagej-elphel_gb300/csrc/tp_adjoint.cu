@@ -120,7 +120,7 @@ __device__ __forceinline__ Win make_win(const SceneDev &sc, const SubtilePlan &p
   w.pitch = sc.img_pitch;
   w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
   w.u16 = sc.img_dtype[s];
-  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
+  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx <= sc.width - 16) && (p.tly <= sc.height - 16);
   w.scale = sc.color_scale[0];
   return w;
 }

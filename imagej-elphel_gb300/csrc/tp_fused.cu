@@ -178,7 +178,7 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
   w.pitch = sc.img_pitch;
   w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
   w.u16 = sc.img_dtype[sidx];
-  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx + 16 <= sc.width) && (p.tly + 16 <= sc.height);
+  w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx <= sc.width - 16) && (p.tly <= sc.height - 16);
   w.scale = sc.color_scale[c];
   float o[4][8];
   float *tbuf = scr + q * 72;

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
+#include <unordered_map>
 #include <string>
 #include <vector>
 
@@ -19,6 +21,8 @@ struct tp_handle {
   tp_config cfg;
   int tilesX = 0, tilesY = 0, ntiles = 0;
   cudaStream_t stream = nullptr;
+  // recorded on the stream of every call that enqueues work; the getters' copies wait for it
+  cudaEvent_t ev_work = nullptr;
   std::string err;
   // device buffers
   void *d_images[TP_MAXS] = {};
@@ -60,6 +64,7 @@ struct tp_handle {
   float *d_sens = nullptr, *d_dval = nullptr, *d_jac_e = nullptr, *d_jac_d = nullptr, *d_grad_d = nullptr;
   float *d_partial = nullptr, *d_grad_e = nullptr, *d_dldd = nullptr;
   int adj_recompute = 0, fwd_valid = 0, have_jac = 0;
+  int images_since_fwd = 0;  // an image was set after the last forward (the adjoint's CLT recompute reads them)
   int tex_rows_alloc = 0, tex_rows = 0;  // allocated rows, rows of the last run
   // host state
   int num_tasks = 0;
@@ -71,6 +76,8 @@ struct tp_handle {
   GeomDev geom_host;
   CorrDev corr_host;
   tp_texture_params tex_params;
+  size_t dev_bytes = 0;                          // device bytes allocated through dalloc
+  std::unordered_map<void *, size_t> dev_sizes;  // their sizes, for dfree
 };
 
 static tp_status fail(tp_handle *h, tp_status st, const std::string &msg) {
@@ -92,8 +99,46 @@ static tp_status d2h(tp_handle *h, void *dst, const void *src, size_t bytes, con
 
 static cudaStream_t pick_stream(tp_handle *h, void *s) { return s ? (cudaStream_t)s : h->stream; }
 
+// marks the end of the work just enqueued on st: the getters order their copies after it
+static tp_status mark_work(tp_handle *h, cudaStream_t st) {
+  const cudaError_t e = cudaEventRecord(h->ev_work, st);
+  if (e != cudaSuccess) {
+    h->err = std::string("event record: ") + cudaGetErrorString(e);
+    return TP_ERR_CUDA;
+  }
+  return TP_OK;
+}
+
+// Device allocations of a handle are counted against the process-wide cap of
+// tp_set_memory_limit (0 = none): an allocation beyond it fails as a failed cudaMalloc does.
+static std::atomic<size_t> g_mem_limit{0};
+
 template <typename T>
-static cudaError_t dalloc(T **p, size_t n) {
+static cudaError_t dalloc(tp_handle *h, T **p, size_t n) {
+  const size_t bytes = n * sizeof(T) > 0 ? n * sizeof(T) : 1;
+  const size_t lim = g_mem_limit.load();
+  if (lim && h->dev_bytes + bytes > lim) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMalloc((void **)p, bytes);
+  if (e == cudaSuccess) {
+    h->dev_bytes += bytes;
+    h->dev_sizes[(void *)*p] = bytes;
+  }
+  return e;
+}
+
+static void dfree(tp_handle *h, void *p) {
+  if (!p) return;
+  auto it = h->dev_sizes.find(p);
+  if (it != h->dev_sizes.end()) {
+    h->dev_bytes -= it->second;
+    h->dev_sizes.erase(it);
+  }
+  cudaFree(p);
+}
+
+// batch tables (not counted against a handle)
+template <typename T>
+static cudaError_t dalloc_batch(T **p, size_t n) {
   return cudaMalloc((void **)p, n * sizeof(T) > 0 ? n * sizeof(T) : 1);
 }
 
@@ -360,6 +405,7 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   const size_t nt = h->ntiles, npix = (size_t)cfg->width * cfg->height;
   bool ok = cudaSetDevice(cfg->device) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&h->ev_work, cudaEventDisableTiming) == cudaSuccess;
   ok = ok && upload_kernel_constants() == cudaSuccess;
   ok = ok && upload_fused_constants() == cudaSuccess;
   ok = ok && upload_texture_constants() == cudaSuccess;
@@ -368,23 +414,23 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
   ok = ok && upload_lma_constants() == cudaSuccess;
   tp_default_texture_params(&h->tex_params);
   for (int s = 0; ok && s < S; s++) {
-    ok = dalloc((float **)&h->d_images[s], npix) == cudaSuccess;
+    ok = dalloc(h, (float **)&h->d_images[s], npix) == cudaSuccess;
     if (ok && cfg->kernels_hor > 0) {
       size_t nk = (size_t)cfg->kernels_hor * cfg->kernels_vert * C;
-      ok = dalloc(&h->d_kern[s], nk * TP_CLT) == cudaSuccess && dalloc(&h->d_kext[s], nk * 8) == cudaSuccess;
+      ok = dalloc(h, &h->d_kern[s], nk * TP_CLT) == cudaSuccess && dalloc(h, &h->d_kext[s], nk * 8) == cudaSuccess;
     }
   }
-  ok = ok && dalloc(&h->d_task_txy, nt) == cudaSuccess && dalloc(&h->d_task_op, nt) == cudaSuccess;
-  ok = ok && dalloc(&h->d_task_disp, nt) == cudaSuccess && dalloc(&h->d_task_xy, nt * S * 2) == cudaSuccess;
-  ok = ok && dalloc(&h->d_tile_op, nt) == cudaSuccess && dalloc(&h->d_tile_disp, nt) == cudaSuccess;
-  ok = ok && dalloc(&h->d_num_tasks, 2 + nt / 1024 + 1) == cudaSuccess;  // count + per-block counts
-  ok = ok && dalloc(&h->d_ports, nt * S * 2) == cudaSuccess;
-  ok = ok && dalloc(&h->d_plan, nt * S * C) == cudaSuccess && dalloc(&h->d_tile_task, nt) == cudaSuccess;
-  ok = ok && dalloc(&h->d_clt, nt * S * C * TP_CLT) == cudaSuccess;
-  ok = ok && dalloc(&h->d_disp, nt * TP_NDISP) == cudaSuccess;
-  ok = ok && dalloc(&h->d_lpf_rbg, 3 * 64) == cudaSuccess;
-  ok = ok && dalloc(&h->d_geom, 1) == cudaSuccess && dalloc(&h->d_rdist, 2048 + 64) == cudaSuccess;
-  ok = ok && dalloc(&h->d_corr_cfg, 1) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_task_txy, nt) == cudaSuccess && dalloc(h, &h->d_task_op, nt) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_task_disp, nt) == cudaSuccess && dalloc(h, &h->d_task_xy, nt * S * 2) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_tile_op, nt) == cudaSuccess && dalloc(h, &h->d_tile_disp, nt) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_num_tasks, 2 + nt / 1024 + 1) == cudaSuccess;  // count + per-block counts
+  ok = ok && dalloc(h, &h->d_ports, nt * S * 2) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_plan, nt * S * C) == cudaSuccess && dalloc(h, &h->d_tile_task, nt) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_clt, nt * S * C * TP_CLT) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_disp, nt * TP_NDISP) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_lpf_rbg, 3 * 64) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_geom, 1) == cudaSuccess && dalloc(h, &h->d_rdist, 2048 + 64) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_corr_cfg, 1) == cudaSuccess;
   if (ok) ok = cudaMemsetAsync(h->d_clt, 0, nt * S * C * TP_CLT * sizeof(float), h->stream) == cudaSuccess;
   if (ok) ok = cudaStreamSynchronize(h->stream) == cudaSuccess;
   if (!ok) {
@@ -408,9 +454,9 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out) {
 tp_status tp_destroy(tp_handle *h) {
   if (!h) return TP_ERR_ARG;
   for (int s = 0; s < TP_MAXS; s++) {
-    cudaFree(h->d_images[s]);
-    cudaFree(h->d_kern[s]);
-    cudaFree(h->d_kext[s]);
+    dfree(h, h->d_images[s]);
+    dfree(h, h->d_kern[s]);
+    dfree(h, h->d_kext[s]);
   }
   void *bufs[] = {h->d_task_txy, h->d_task_op, h->d_task_disp, h->d_task_xy, h->d_tile_op, h->d_tile_disp,
                   h->d_num_tasks, h->d_ports, h->d_port_deriv, h->d_plan, h->d_tile_task, h->d_clt, h->d_corr,
@@ -418,9 +464,21 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
                   h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
                   h->d_rig_rec};
-  for (void *b : bufs) cudaFree(b);
+  for (void *b : bufs) dfree(h, b);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->ev_work) cudaEventDestroy(h->ev_work);
   delete h;
+  return TP_OK;
+}
+
+tp_status tp_set_memory_limit(size_t max_bytes_per_handle) {
+  g_mem_limit.store(max_bytes_per_handle);
+  return TP_OK;
+}
+
+tp_status tp_get_memory_usage(const tp_handle *h, size_t *bytes) {
+  if (!h || !bytes) return TP_ERR_ARG;
+  *bytes = h->dev_bytes;
   return TP_OK;
 }
 
@@ -556,10 +614,10 @@ tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_de
   } else {
     const size_t chunk = nk < 8192 ? nk : 8192;  // kernel tiles per staged upload (128 MB)
     if (h->psf_stage_kernels < chunk) {
-      cudaFree(h->d_psf_stage);
+      dfree(h, h->d_psf_stage);
       h->d_psf_stage = nullptr;
       h->psf_stage_kernels = 0;
-      if (dalloc(&h->d_psf_stage, chunk * 4096) != cudaSuccess) {
+      if (dalloc(h, &h->d_psf_stage, chunk * 4096) != cudaSuccess) {
         cudaGetLastError();
         return fail(h, TP_ERR_NOMEM, "tp_calc_kernels: PSF staging buffer");
       }
@@ -582,7 +640,7 @@ tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_de
   h->planned = 0;
   h->deriv_valid = 0;
   h->fwd_valid = 0;
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_get_kernels(tp_handle *h, int cam, float *kernels, float *kernel_offsets) {
@@ -595,15 +653,18 @@ tp_status tp_get_kernels(tp_handle *h, int cam, float *kernels, float *kernel_of
   return r;
 }
 
+// Images and colour scales are read only by the forward (and by the adjoint when it recomputes
+// the CLT): the last forward's products stay valid for the passes that read them (LMA, rig,
+// IMCLT, textures), as in a frame loop that uploads the next frame during those passes.
 tp_status tp_set_color_scales(tp_handle *h, const float *scales) {
-  if (h) h->fwd_valid = 0;
+  if (h) h->images_since_fwd = 1;
   if (!h || !scales) return TP_ERR_ARG;
   for (int i = 0; i < 3; i++) h->color_scale[i] = scales[i];
   return TP_OK;
 }
 
 tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size_t pitch) {
-  if (h) h->fwd_valid = 0;
+  if (h) h->images_since_fwd = 1;
   if (!h || !image) return TP_ERR_ARG;
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_image: bad camera");
   if (dtype != TP_F32 && dtype != TP_U16) return fail(h, TP_ERR_ARG, "tp_set_image: bad dtype");
@@ -619,7 +680,7 @@ tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size
 }
 
 tp_status tp_set_image_async(tp_handle *h, int cam, const void *image, int dtype, size_t pitch, void *stream) {
-  if (h) h->fwd_valid = 0;
+  if (h) h->images_since_fwd = 1;
   if (!h || !image) return TP_ERR_ARG;
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_image_async: bad camera");
   if (dtype != TP_F32 && dtype != TP_U16) return fail(h, TP_ERR_ARG, "tp_set_image_async: bad dtype");
@@ -639,12 +700,24 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
   const int S = h->cfg.num_sensors, rec = 2 + 2 * S;
   std::vector<int> txy(n), op(n);
   std::vector<float> xy((size_t)n * S * 2);
+  const float lim[2][2] = {{-(float)TP_PORT_MARGIN, (float)(h->cfg.width + TP_PORT_MARGIN)},
+                           {-(float)TP_PORT_MARGIN, (float)(h->cfg.height + TP_PORT_MARGIN)}};
   for (int i = 0; i < n; i++) {
     memcpy(&op[i], packed + (size_t)i * rec, 4);
     memcpy(&txy[i], packed + (size_t)i * rec + 1, 4);
     int tx = txy[i] & 0xffff, ty = txy[i] >> 16;
     if (tx >= h->tilesX || ty >= h->tilesY || ty < 0) return fail(h, TP_ERR_ARG, "tp_set_tasks: tile out of range");
-    for (int k = 0; k < 2 * S; k++) xy[(size_t)i * 2 * S + k] = packed[(size_t)i * rec + 2 + k];
+    for (int k = 0; k < 2 * S; k++) {
+      const float v = packed[(size_t)i * rec + 2 + k];
+      // NaN fails both comparisons
+      if (!(v >= lim[k & 1][0] && v <= lim[k & 1][1])) {
+        char msg[160];
+        snprintf(msg, sizeof(msg), "tp_set_tasks: task %d sensor %d port %c = %g is not finite or more than %d px "
+                 "outside the image", i, k >> 1, (k & 1) ? 'y' : 'x', (double)v, TP_PORT_MARGIN);
+        return fail(h, TP_ERR_ARG, msg);
+      }
+      xy[(size_t)i * 2 * S + k] = v;
+    }
   }
   if (n > 0) {
     CK(cudaMemcpyAsync(h->d_task_txy, txy.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream), "tp_set_tasks");
@@ -665,6 +738,15 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
 tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
   if (!h || !tile_op || !disp) return TP_ERR_ARG;
   if (!h->have_geometry) return fail(h, TP_ERR_STATE, "tp_set_tile_ops: geometry not set");
+  for (int i = 0; i < h->ntiles; i++) {
+    // NaN fails the comparison
+    if (tile_op[i] != 0 && !(fabsf(disp[i]) <= TP_MAX_DISPARITY)) {
+      char msg[160];
+      snprintf(msg, sizeof(msg), "tp_set_tile_ops: tile %d disparity %g is not finite or beyond +-%g px", i,
+               (double)disp[i], (double)TP_MAX_DISPARITY);
+      return fail(h, TP_ERR_ARG, msg);
+    }
+  }
   CK(cudaMemcpyAsync(h->d_tile_op, tile_op, h->ntiles * sizeof(int), cudaMemcpyHostToDevice, h->stream),
      "tp_set_tile_ops");
   CK(cudaMemcpyAsync(h->d_tile_disp, disp, h->ntiles * sizeof(float), cudaMemcpyHostToDevice, h->stream),
@@ -767,16 +849,16 @@ tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pair
         cd.strip_code[kind][e][dn] = code;
       }
   if (np > h->corr_capacity) {
-    cudaFree(h->d_corr);
+    dfree(h, h->d_corr);
     h->d_corr = nullptr;
     h->corr_capacity = 0;
-    if (dalloc(&h->d_corr, (size_t)h->ntiles * np * TP_CORR) != cudaSuccess) {
+    if (dalloc(h, &h->d_corr, (size_t)h->ntiles * np * TP_CORR) != cudaSuccess) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_set_corr: correlation buffer");
     }
     h->corr_capacity = np;
   }
-  if (!h->d_combo && dalloc(&h->d_combo, (size_t)h->ntiles * TP_MAX_STRIP * 15) != cudaSuccess) {
+  if (!h->d_combo && dalloc(h, &h->d_combo, (size_t)h->ntiles * TP_MAX_STRIP * 15) != cudaSuccess) {
     cudaGetLastError();
     return fail(h, TP_ERR_NOMEM, "tp_set_corr: combined strip buffer");
   }
@@ -805,7 +887,9 @@ tp_status tp_ports(tp_handle *h, void *stream) {
   h->planned = 0;
   h->deriv_valid = 0;
   h->fwd_valid = 0;
-  return ensure_plan(h, pick_stream(h, stream));
+  cudaStream_t st = pick_stream(h, stream);
+  tp_status r = ensure_plan(h, st);
+  return r != TP_OK ? r : mark_work(h, st);
 }
 
 tp_status tp_convert_correct(tp_handle *h, void *stream) {
@@ -815,7 +899,7 @@ tp_status tp_convert_correct(tp_handle *h, void *stream) {
   if (r != TP_OK) return r;
   CK(launch_convert_correct(scene_of(h), st), "convert_correct");
   h->lma_valid = 0;
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_correlate(tp_handle *h, void *stream) {
@@ -825,7 +909,7 @@ tp_status tp_correlate(tp_handle *h, void *stream) {
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
   CK(launch_correlate(scene_of(h), st), "correlate");
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_extract(tp_handle *h, void *stream) {
@@ -835,7 +919,7 @@ tp_status tp_extract(tp_handle *h, void *stream) {
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
   CK(launch_extract(scene_of(h), st), "extract");
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_imclt(tp_handle *h, void *stream) {
@@ -845,13 +929,13 @@ tp_status tp_imclt(tp_handle *h, void *stream) {
   if (r != TP_OK) return r;
   if (!h->d_rbg) {
     size_t n = (size_t)h->cfg.num_sensors * h->cfg.num_colors * (h->cfg.width + 8) * (h->cfg.height + 8);
-    if (dalloc(&h->d_rbg, n) != cudaSuccess) {
+    if (dalloc(h, &h->d_rbg, n) != cudaSuccess) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_imclt: frame buffer");
     }
   }
   CK(launch_imclt_fast(scene_of(h), st), "imclt");
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_set_texture_params(tp_handle *h, const tp_texture_params *p) {
@@ -875,16 +959,16 @@ tp_status tp_textures(tp_handle *h, void *stream) {
   const tp_texture_params &p = h->tex_params;
   const int rows = p.keep_weights ? 12 : 4;
   if (rows > h->tex_rows_alloc) {
-    cudaFree(h->d_tex);
+    dfree(h, h->d_tex);
     h->d_tex = nullptr;
     h->tex_rows_alloc = 0;
-    if (dalloc(&h->d_tex, (size_t)h->ntiles * rows * 256) != cudaSuccess) {
+    if (dalloc(h, &h->d_tex, (size_t)h->ntiles * rows * 256) != cudaSuccess) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_textures: texture buffer");
     }
     h->tex_rows_alloc = rows;
   }
-  if (p.aux && !h->d_tex_aux && dalloc(&h->d_tex_aux, (size_t)h->ntiles * 16) != cudaSuccess) {
+  if (p.aux && !h->d_tex_aux && dalloc(h, &h->d_tex_aux, (size_t)h->ntiles * 16) != cudaSuccess) {
     cudaGetLastError();
     return fail(h, TP_ERR_NOMEM, "tp_textures: aux buffer");
   }
@@ -914,7 +998,7 @@ tp_status tp_textures(tp_handle *h, void *stream) {
   if (tc.extra_index >= 0 && h->num_pairs == 0) tc.extra_index = -1;
   CK(launch_textures(scene_of(h), tc, st), "textures");
   h->tex_rows = rows;
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_process(tp_handle *h, void *stream) {
@@ -927,10 +1011,11 @@ tp_status tp_process(tp_handle *h, void *stream) {
   const SceneDev sc = scene_of(h);
   CK(launch_fused_forward(sc, h->corr_host, h->sched_tpb, h->sched_nw, st), "fused forward");
   h->fwd_valid = 1;
+  h->images_since_fwd = 0;
   h->strips_valid = sc.strips ? 1 : 0;
   h->disp_mixed = 0;
   h->lma_valid = 0;
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block) {
@@ -950,6 +1035,7 @@ tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block
 
 tp_status tp_synchronize(tp_handle *h) {
   if (!h) return TP_ERR_ARG;
+  CK(cudaEventSynchronize(h->ev_work), "tp_synchronize");
   CK(cudaStreamSynchronize(h->stream), "tp_synchronize");
   return TP_OK;
 }
@@ -960,12 +1046,23 @@ tp_status tp_get_num_tasks(const tp_handle *h, int *n) {
   return TP_OK;
 }
 
+// Host copy of a device result: on the handle's own stream, after the last work enqueued through
+// the handle (on whatever stream that went), then that stream alone is synchronised.
 static tp_status d2h(tp_handle *h, void *dst, const void *src, size_t bytes, const char *where) {
   if (!dst) return fail(h, TP_ERR_ARG, where);
   if (!src) return fail(h, TP_ERR_STATE, std::string(where) + ": not computed");
+  CK(cudaStreamWaitEvent(h->stream, h->ev_work, 0), where);
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream), where);
   CK(cudaStreamSynchronize(h->stream), where);
-  CK(cudaDeviceSynchronize(), where);
-  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), where);
+  return TP_OK;
+}
+
+// as d2h, enqueued on st after the handle's last work, without waiting
+static tp_status d2h_async(tp_handle *h, void *dst, const void *src, size_t bytes, cudaStream_t st, const char *where) {
+  if (!dst) return fail(h, TP_ERR_ARG, where);
+  if (!src) return fail(h, TP_ERR_STATE, std::string(where) + ": not computed");
+  CK(cudaStreamWaitEvent(st, h->ev_work, 0), where);
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), where);
   return TP_OK;
 }
 
@@ -1017,6 +1114,20 @@ tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg) {
   return d2h(h, rbg, h->d_rbg ? h->d_rbg + plane * cam : nullptr, plane * sizeof(float), "tp_get_rbg");
 }
 
+tp_status tp_get_rbg_async(tp_handle *h, int cam, float *rbg, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_get_rbg_async: bad camera");
+  size_t plane = (size_t)(h->cfg.width + 8) * (h->cfg.height + 8) * h->cfg.num_colors;
+  return d2h_async(h, rbg, h->d_rbg ? h->d_rbg + plane * cam : nullptr, plane * sizeof(float),
+                   pick_stream(h, stream), "tp_get_rbg_async");
+}
+
+tp_status tp_get_disparity_async(tp_handle *h, float *disp, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  return d2h_async(h, disp, h->d_disp, (size_t)h->ntiles * TP_NDISP * sizeof(float), pick_stream(h, stream),
+                   "tp_get_disparity_async");
+}
+
 tp_status tp_get_textures(tp_handle *h, float *tex) {
   if (!h) return TP_ERR_ARG;
   const int rows = h->tex_rows;
@@ -1034,7 +1145,7 @@ tp_status tp_get_texture_aux(tp_handle *h, float *aux) {
 struct tp_batch {
   std::vector<tp_handle *> scenes;
   std::vector<SceneDev> h_scenes;           // all scenes, for the batched plan
-  std::vector<int> h_task_off, graph_tasks;
+  std::vector<int> h_task_off;
   std::vector<SceneDev> h_cls[3];           // per schedule class: scenes sharing the persistent queue
   std::vector<int> h_cls_off[3];
   std::vector<tp_handle *> solo[3];         // scenes large enough to keep their own launch
@@ -1044,10 +1155,28 @@ struct tp_batch {
   int device = 0, total_tasks = 0;
   cudaStream_t stream = nullptr, cls_stream[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_done = nullptr;  // after the last enqueued step: the scene tables it reads may then be rewritten
+  std::vector<unsigned char> up_tables;  // bytes of the scene tables on the device
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  std::vector<std::vector<unsigned char>> graph_keys;  // scene_key of every scene when the graph was captured
   std::string err;
 };
+
+// Everything about a scene that a captured batch step holds by value: the SceneDev (device
+// pointers, task count, dtypes, colour scales, pair count, strip rows), the correlation set-up the
+// solo launches take as a kernel parameter, and the schedule.  Both structs are zero-filled
+// before their fields are set (scene_of, tp_set_corr), so their bytes compare exactly.
+static std::vector<unsigned char> scene_key(tp_handle *h) {
+  SceneDev sc = scene_of(h);
+  sc.strips = nullptr;  // batched forwards do not record strip samples
+  const int sched[2] = {h->sched_tpb, h->sched_nw};
+  std::vector<unsigned char> k(sizeof(SceneDev) + sizeof(CorrConst) + sizeof(sched));
+  memcpy(k.data(), &sc, sizeof(SceneDev));
+  memcpy(k.data() + sizeof(SceneDev), static_cast<const CorrConst *>(&h->corr_host), sizeof(CorrConst));
+  memcpy(k.data() + sizeof(SceneDev) + sizeof(CorrConst), sched, sizeof(sched));
+  return k;
+}
 
 static tp_status bfail(tp_batch *b, tp_status st, const std::string &msg) {
   if (b) b->err = msg;
@@ -1085,12 +1214,28 @@ static tp_status batch_tables(tp_batch *b) {
   }
   b->h_task_off[n] = t;
   b->total_tasks = t;
+  for (int c = 0; c < 3; c++) b->cls_units[c] = b->h_cls_off[c].back();
+  // upload only when a table changed, after the last step that read the old ones has finished
+  std::vector<unsigned char> tb;
+  auto put = [&tb](const void *p, size_t n) { tb.insert(tb.end(), (const unsigned char *)p, (const unsigned char *)p + n); };
+  put(b->h_scenes.data(), n * sizeof(SceneDev));
+  put(b->h_task_off.data(), (n + 1) * sizeof(int));
+  for (int c = 0; c < 3; c++) {
+    const int m = (int)b->h_cls[c].size();
+    put(&m, sizeof(m));
+    put(b->h_cls[c].data(), m * sizeof(SceneDev));
+    put(b->h_cls_off[c].data(), (m + 1) * sizeof(int));
+  }
+  if (tb == b->up_tables) return TP_OK;
+  if (cudaEventSynchronize(b->ev_done) != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, TP_ERR_CUDA, "batch: waiting for the previous step");
+  }
   bool ok = cudaMemcpy(b->d_scenes, b->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(b->d_task_off, b->h_task_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
                 cudaSuccess;
   for (int c = 0; ok && c < 3; c++) {
     const int m = (int)b->h_cls[c].size();
-    b->cls_units[c] = b->h_cls_off[c].back();
     if (m == 0) continue;
     ok = cudaMemcpy(b->d_cls[c], b->h_cls[c].data(), m * sizeof(SceneDev), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(b->d_cls_off[c], b->h_cls_off[c].data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
@@ -1098,8 +1243,10 @@ static tp_status batch_tables(tp_batch *b) {
   }
   if (!ok) {
     cudaGetLastError();
+    b->up_tables.clear();
     return bfail(b, TP_ERR_CUDA, "batch: scene table upload");
   }
+  b->up_tables.swap(tb);
   return TP_OK;
 }
 
@@ -1144,6 +1291,7 @@ static tp_status batch_enqueue(tp_batch *b, int replan, cudaStream_t st) {
   }
   for (tp_handle *h : b->scenes) {
     h->fwd_valid = 1;
+    h->images_since_fwd = 0;
     h->strips_valid = 0;
     h->disp_mixed = 0;
     h->lma_valid = 0;
@@ -1164,8 +1312,10 @@ static void batch_drop_graph(tp_batch *b) {
   b->graph = nullptr;
 }
 
-// Device address of the compaction scratch array, looked up once per device
-// (cudaGetSymbolAddress with that device current) and cached.
+// Device address of the compaction scratch array per device (cudaGetSymbolAddress with that
+// device current).  A call outside a stream capture looks it up again, so a device reset that
+// reloaded the module is followed; a call inside a capture uses the address of the last call
+// outside one.
 static std::mutex g_scratch_mu;
 static int *g_scratch_ptr[TP_NOALLOC_MAX_DEVICES];
 
@@ -1179,10 +1329,16 @@ tp_status tp_compact_tile_ops_noalloc(const int *tile_op, const float *disparity
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TP_ERR_CUDA;
   if (dev < 0 || dev >= TP_NOALLOC_MAX_DEVICES) return TP_ERR_ARG;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing((cudaStream_t)stream, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;  // unknown: do not call the symbol lookup
+  }
   int *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
+      if (cap != cudaStreamCaptureStatusNone) return TP_ERR_STATE;  // first call on a device inside a capture
       int *p = nullptr;
       if (compact_scratch_address(&p) != cudaSuccess || !p) {
         cudaGetLastError();
@@ -1261,7 +1417,7 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   if (!quad) return fail(h, TP_ERR_ARG, "tp_lma_refine: needs pairs of the quad kinds 0..3");
   cudaStream_t st = pick_stream(h, stream);
   if (!h->d_lma) {
-    if (dalloc(&h->d_lma, (size_t)h->ntiles * 4) != cudaSuccess) {
+    if (dalloc(h, &h->d_lma, (size_t)h->ntiles * 4) != cudaSuccess) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_lma_refine: buffer");
     }
@@ -1307,10 +1463,10 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   if (prm.mismatch) {
     const size_t need = (size_t)h->ntiles * h->num_pairs * 3;
     if (need > h->mismatch_cap) {
-      cudaFree(h->d_mismatch);
+      dfree(h, h->d_mismatch);
       h->d_mismatch = nullptr;
       h->mismatch_cap = 0;
-      if (dalloc(&h->d_mismatch, need) != cudaSuccess) {
+      if (dalloc(h, &h->d_mismatch, need) != cudaSuccess) {
         cudaGetLastError();
         return fail(h, TP_ERR_NOMEM, "tp_lma_refine: mismatch buffer");
       }
@@ -1322,7 +1478,7 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
      "tp_lma_refine");
   if (prm.mix_corr_poly || prm.fo_correct) h->disp_mixed = 1;
   h->lma_valid = 1;
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_get_lma_mismatch(tp_handle *h, float *out) {
@@ -1350,15 +1506,15 @@ tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_norma
     return fail(h, TP_ERR_STATE, "tp_rig_correlate: run tp_process on both cameras first");
   cudaStream_t st = pick_stream(h, stream);
   if (!h->d_rig_corr) {
-    if (dalloc(&h->d_rig_corr, (size_t)h->ntiles * TP_CORR) != cudaSuccess ||
-        dalloc(&h->d_rig_rec, (size_t)h->ntiles * 4) != cudaSuccess) {
+    if (dalloc(h, &h->d_rig_corr, (size_t)h->ntiles * TP_CORR) != cudaSuccess ||
+        dalloc(h, &h->d_rig_rec, (size_t)h->ntiles * 4) != cudaSuccess) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_rig_correlate: buffers");
     }
     CK(cudaMemsetAsync(h->d_rig_corr, 0, (size_t)h->ntiles * TP_CORR * sizeof(float), st), "tp_rig_correlate");
   }
-  CK(cudaStreamSynchronize(aux->stream), "tp_rig_correlate");
-  CK(cudaStreamSynchronize(h->stream), "tp_rig_correlate");
+  CK(cudaStreamWaitEvent(st, aux->ev_work, 0), "tp_rig_correlate");  // both cameras' forwards
+  CK(cudaStreamWaitEvent(st, h->ev_work, 0), "tp_rig_correlate");
   CorrConst cc = h->corr_host;  // the main camera's correlation set-up, one horizontal pair
   cc.num_pairs = 1;
   cc.num_combo = 1;
@@ -1372,7 +1528,7 @@ tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_norma
   cc.pairs[0].by = 0.f;
   CK(launch_rig(scene_of(h), scene_of(aux), cc, h->d_rig_corr, h->d_rig_rec, cm_max_normalization, no_int_x0, st),
      "tp_rig_correlate");
-  return TP_OK;
+  return mark_work(h, st);
 }
 
 tp_status tp_get_rig(tp_handle *h, float *corr, float *rec) {
@@ -1389,11 +1545,11 @@ tp_status tp_get_rig(tp_handle *h, float *corr, float *rec) {
 static tp_status enable_strip_recording(tp_handle *h) {
   const size_t need = strips_need(h);
   if (need > h->strips_cap) {
-    cudaFree(h->d_strips);
+    dfree(h, h->d_strips);
     h->d_strips = nullptr;
     h->strips_cap = 0;
     h->strips_valid = 0;
-    if (dalloc(&h->d_strips, need) != cudaSuccess) {
+    if (dalloc(h, &h->d_strips, need) != cudaSuccess) {
       cudaGetLastError();
       h->adj_record = 0;
       return fail(h, TP_ERR_NOMEM, "adjoint: strip-sample buffer");
@@ -1419,15 +1575,17 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
     return fail(h, TP_ERR_STATE, "tp_backward: not for a rig's auxiliary camera (its disparities are the main camera's)");
   if (!h->fwd_valid || h->num_pairs == 0)
     return fail(h, TP_ERR_STATE, "tp_backward: run tp_process (with correlation pairs) first");
+  if (h->adj_recompute && h->images_since_fwd)
+    return fail(h, TP_ERR_STATE, "tp_backward: the CLT recompute reads the images, which changed since tp_process");
   cudaStream_t st = pick_stream(h, stream);
   const size_t nt = h->ntiles, S = h->cfg.num_sensors;
   const int nb = (int)((nt + 256 / S - 1) / (256 / S));  // blocks of the contraction kernel (256 / S tasks each)
   if (!h->d_sens) {
-    bool ok = dalloc(&h->d_port_deriv, nt * S * 10) == cudaSuccess && dalloc(&h->d_sens, nt * S * 2) == cudaSuccess &&
-              dalloc(&h->d_dval, nt) == cudaSuccess && dalloc(&h->d_jac_e, nt * S * 4) == cudaSuccess &&
-              dalloc(&h->d_jac_d, nt) == cudaSuccess && dalloc(&h->d_grad_d, nt) == cudaSuccess &&
-              dalloc(&h->d_partial, (size_t)nb * S * 4) == cudaSuccess && dalloc(&h->d_grad_e, S * 4) == cudaSuccess &&
-              dalloc(&h->d_dldd, nt) == cudaSuccess;
+    bool ok = dalloc(h, &h->d_port_deriv, nt * S * 10) == cudaSuccess && dalloc(h, &h->d_sens, nt * S * 2) == cudaSuccess &&
+              dalloc(h, &h->d_dval, nt) == cudaSuccess && dalloc(h, &h->d_jac_e, nt * S * 4) == cudaSuccess &&
+              dalloc(h, &h->d_jac_d, nt) == cudaSuccess && dalloc(h, &h->d_grad_d, nt) == cudaSuccess &&
+              dalloc(h, &h->d_partial, (size_t)nb * S * 4) == cudaSuccess && dalloc(h, &h->d_grad_e, S * 4) == cudaSuccess &&
+              dalloc(h, &h->d_dldd, nt) == cudaSuccess;
     if (!ok) {
       cudaGetLastError();
       return fail(h, TP_ERR_NOMEM, "tp_backward: adjoint buffers");
@@ -1449,6 +1607,8 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
                     h->d_jac_e, h->d_jac_d, h->d_grad_d, h->d_partial, h->d_grad_e, st),
      "tp_backward adjoint");
   h->have_jac = 1;
+  tp_status rm = mark_work(h, st);
+  if (rm != TP_OK) return rm;
   if (dl_dextr) CK(cudaMemcpyAsync(dl_dextr, h->d_grad_e, S * 4 * sizeof(float), cudaMemcpyDeviceToHost, st), "tp_backward");
   if (dl_dtile_disp)
     CK(cudaMemcpyAsync(dl_dtile_disp, h->d_grad_d, nt * sizeof(float), cudaMemcpyDeviceToHost, st), "tp_backward");
@@ -1499,11 +1659,12 @@ tp_status tp_batch_create(tp_handle *const *scenes, int n, tp_batch **out) {
   bool ok = cudaSetDevice(dev) == cudaSuccess &&
             cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
-            dalloc(&b->d_scenes, n) == cudaSuccess && dalloc(&b->d_task_off, n + 1) == cudaSuccess;
+            cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) == cudaSuccess &&
+            dalloc_batch(&b->d_scenes, n) == cudaSuccess && dalloc_batch(&b->d_task_off, n + 1) == cudaSuccess;
   for (int c = 0; ok && c < 3; c++)
     ok = cudaStreamCreateWithFlags(&b->cls_stream[c], cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&b->ev_join[c], cudaEventDisableTiming) == cudaSuccess &&
-         dalloc(&b->d_cls[c], n) == cudaSuccess && dalloc(&b->d_cls_off[c], n + 1) == cudaSuccess;
+         dalloc_batch(&b->d_cls[c], n) == cudaSuccess && dalloc_batch(&b->d_cls_off[c], n + 1) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     tp_batch_destroy(b);
@@ -1525,6 +1686,7 @@ tp_status tp_batch_destroy(tp_batch *b) {
     if (b->ev_join[c]) cudaEventDestroy(b->ev_join[c]);
   }
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_done) cudaEventDestroy(b->ev_done);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return TP_OK;
@@ -1539,20 +1701,30 @@ tp_status tp_batch_last_error(const tp_batch *b, char *buf, int n) {
 tp_status tp_batch_process(tp_batch *b, int replan, void *stream) {
   if (!b) return TP_ERR_ARG;
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-  for (tp_handle *h : b->scenes) CK_B(cudaStreamSynchronize(h->stream));
+  for (tp_handle *h : b->scenes) {
+    CK_B(cudaStreamSynchronize(h->stream));       // set-up copies on the handles' own streams
+    CK_B(cudaStreamWaitEvent(st, h->ev_work, 0));  // each scene's earlier work, on any stream
+  }
   tp_status r = batch_tables(b);
   if (r != TP_OK) return r;
-  return batch_enqueue(b, replan, st);
+  r = batch_enqueue(b, replan, st);
+  if (r == TP_OK) CK_B(cudaEventRecord(b->ev_done, st));
+  for (tp_handle *h : b->scenes)
+    if (r == TP_OK && mark_work(h, st) != TP_OK) r = bfail(b, TP_ERR_CUDA, "batch: " + h->err);
+  return r;
 }
 
 tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
   if (!b) return TP_ERR_ARG;
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-  bool stale = !b->exec || b->graph_tasks.size() != b->scenes.size();
-  for (size_t i = 0; !stale && i < b->scenes.size(); i++) stale = b->graph_tasks[i] != b->scenes[i]->num_tasks;
+  bool stale = !b->exec || b->graph_keys.size() != b->scenes.size();
+  for (size_t i = 0; !stale && i < b->scenes.size(); i++) stale = b->graph_keys[i] != scene_key(b->scenes[i]);
   if (stale) {
     batch_drop_graph(b);
-    for (tp_handle *h : b->scenes) CK_B(cudaStreamSynchronize(h->stream));
+    for (tp_handle *h : b->scenes) {
+      CK_B(cudaStreamSynchronize(h->stream));
+      CK_B(cudaEventSynchronize(h->ev_work));
+    }
     tp_status r = batch_tables(b);
     if (r != TP_OK) return r;
     CK_B(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
@@ -1566,12 +1738,17 @@ tp_status tp_batch_run_graph(tp_batch *b, void *stream) {
     if (ec != cudaSuccess) return bfail(b, TP_ERR_CUDA, std::string("batch: capture: ") + cudaGetErrorString(ec));
     b->graph = g;
     CK_B(cudaGraphInstantiate(&b->exec, b->graph, 0));
-    b->graph_tasks.clear();
-    for (tp_handle *h : b->scenes) b->graph_tasks.push_back(h->num_tasks);
+    b->graph_keys.clear();
+    for (tp_handle *h : b->scenes) b->graph_keys.push_back(scene_key(h));
   }
+  for (tp_handle *h : b->scenes) CK_B(cudaStreamWaitEvent(st, h->ev_work, 0));
   CK_B(cudaGraphLaunch(b->exec, st));
+  CK_B(cudaEventRecord(b->ev_done, st));
+  for (tp_handle *h : b->scenes)
+    if (mark_work(h, st) != TP_OK) return bfail(b, TP_ERR_CUDA, "batch: " + h->err);
   for (tp_handle *h : b->scenes) {
     h->fwd_valid = 1;
+    h->images_since_fwd = 0;
     h->strips_valid = 0;
     h->disp_mixed = 0;
     h->lma_valid = 0;

@@ -8,6 +8,7 @@
 // ImageDtt.extract_correct_tile.  GB300 FP64 throughput is low, so this runs
 // as its own kernel with one thread per (task, sensor): ~100 FP64 operations
 // per port instead of the FP32 pipeline paying for them per coefficient.
+#include "tp.h"
 #include "tp_internal.h"
 #include <math_constants.h>
 
@@ -21,6 +22,18 @@
 __device__ __forceinline__ double java_round(double x) {
   double f = floor(x);
   return (DSUB(x, f) >= 0.5) ? DADD(f, 1.0) : f;
+}
+
+// Window corner (an integral double) -> int.  A corner further than TP_PORT_MARGIN outside the
+// image is moved to the margin keeping its parity: every pixel of such a window is outside the
+// image, and the mirrored edge pixels it reads (Win::at, mirror) depend only on the corner's
+// parity, so the window content is unchanged and the int arithmetic of the kernels that read it
+// cannot overflow.  NaN (a port beyond the reverse distortion table) goes to the lower bound.
+__device__ __forceinline__ int clamp_corner(double t, int n) {
+  const double lo = -(double)(TP_PORT_MARGIN + 16), hi = (double)(n + TP_PORT_MARGIN);
+  if (t >= lo && t <= hi) return (int)t;
+  const int par = (t == t) ? (int)fabs(fmod(t, 2.0)) : 0;
+  return (t > hi) ? (int)hi - (((int)hi & 1) ^ par) : (int)lo + (((int)lo & 1) ^ par);
 }
 
 // GeometryCorrection.getRByRDist (GeometryCorrection.java:2802-2827)
@@ -193,8 +206,8 @@ __device__ __forceinline__ void plan_task(const SceneDev &sc, int task, int s0, 
       }
       const double tl = -java_round(-px), tt = -java_round(-py);
       SubtilePlan p;
-      p.tlx = (int)tl;
-      p.tly = (int)tt;
+      p.tlx = clamp_corner(tl, sc.width);
+      p.tly = clamp_corner(tt, sc.height);
       p.kidx = kidx;
       p.rx = (float)(-(DSUB(px, tl)));
       p.ry = (float)(-(DSUB(py, tt)));

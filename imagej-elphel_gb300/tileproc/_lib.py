@@ -83,6 +83,8 @@ PROTOTYPES = {
     "tp_create": [C.POINTER(TpConfig), C.POINTER(_H)],
     "tp_destroy": [_H],
     "tp_last_error": [_H, C.c_char_p, C.c_int],
+    "tp_set_memory_limit": [C.c_size_t],
+    "tp_get_memory_usage": [_H, C.POINTER(C.c_size_t)],
     "tp_default_corr_params": [C.POINTER(TpCorrParams)],
     "tp_default_texture_params": [C.POINTER(TpTextureParams)],
     "tp_quad_pairs": [C.POINTER(TpPair), C.POINTER(C.c_int)],
@@ -116,6 +118,8 @@ PROTOTYPES = {
     "tp_get_corr": [_H, _vp],
     "tp_get_disparity": [_H, _vp],
     "tp_get_rbg": [_H, C.c_int, _vp],
+    "tp_get_rbg_async": [_H, C.c_int, _vp, _vp],
+    "tp_get_disparity_async": [_H, _vp, _vp],
     "tp_get_textures": [_H, _vp],
     "tp_get_texture_aux": [_H, _vp],
     "tp_compact_tile_ops_noalloc": [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],

@@ -35,10 +35,17 @@ def _evaluate(tp, geometry, disparity, tile_op):
     return d, ok, float(np.sum(np.where(ok, d * d, 0.0)))
 
 
+# largest change of a tile's target disparity in one step, px: beyond about a pixel the
+# linearisation no longer holds (window corners and the integer maximum switch)
+MAX_DISPARITY_STEP = 1.0
+
+
 def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_disparity=True,
            fixed_sensor=None, callback=None):
     """Runs `iterations` LM steps; returns (geometry, disparity, history) where history
-    holds the cost (sum d^2 over tiles with a peak) before each step and after the last."""
+    holds the cost (sum d^2 over tiles with a peak) before each step and after the last.
+    The per-tile disparity steps are clipped to +-MAX_DISPARITY_STEP (a tile whose
+    disparity derivative is close to zero would otherwise take an unbounded step)."""
     T = tp.tilesY * tp.tilesX
     S = tp.num_sensors
     g = copy.deepcopy(geometry)
@@ -66,7 +73,7 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_
                 M = JtJ + lam * np.diag(dA) - A.T @ (A * (b * b * inv)[:, None])
                 rhs = -(A.T @ r) + A.T @ (b * b * inv * r)
                 de = np.linalg.solve(M + 1e-12 * np.eye(S * 4), rhs)
-                dd = -inv * b * (r + A @ de)
+                dd = np.clip(-inv * b * (r + A @ de), -MAX_DISPARITY_STEP, MAX_DISPARITY_STEP)
             else:
                 de = np.linalg.solve(JtJ + lam * np.diag(dA) + 1e-12 * np.eye(S * 4), -(A.T @ r))
                 dd = np.zeros(T)

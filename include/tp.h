@@ -15,7 +15,10 @@
  *    (the reference never frees its buffers);
  *  - one handle per host thread / stream; a handle is not thread-safe;
  *  - `stream` arguments are cudaStream_t passed as void* (NULL = the handle's
- *    own stream);  get/set calls synchronise their stream before returning.
+ *    own stream);  every call that enqueues work records the end of that work;
+ *    the tp_get_* calls copy on the handle's own stream after it (wherever it
+ *    was enqueued) and synchronise that stream only, never the device; the
+ *    *_async getters enqueue the copy on the caller's stream and return.
  *
  * Array layouts (row-major, C order):
  *  image       [height][pitch]           f32 or u16 (Bayer mosaic or mono)
@@ -39,6 +42,18 @@ extern "C" {
 
 #define TP_MAX_SENSORS 16
 #define TP_MAX_PAIRS 120
+/* Task-input limits, checked on the host before anything is uploaded or launched
+ * (the reference trusts its Java host instead, GPUTileProcessor.java:363-371, 686-778):
+ *  - tp_set_tasks: every port must be finite and lie within TP_PORT_MARGIN pixels
+ *    of the image, -TP_PORT_MARGIN <= x <= width + TP_PORT_MARGIN (y likewise);
+ *  - tp_set_tile_ops: the target disparity of every tile with tile_op != 0 must be
+ *    finite with |disparity| <= TP_MAX_DISPARITY pixels.
+ * A violation returns TP_ERR_ARG and leaves the handle unchanged.  Ports computed on
+ * the device from the geometry are not limited: a window corner further than the
+ * margin outside the image is moved to the margin keeping its parity, which leaves
+ * the (edge-mirrored) window content and the residual shift unchanged. */
+#define TP_PORT_MARGIN 1024
+#define TP_MAX_DISPARITY 4096.0f
 
 typedef struct tp_handle tp_handle;
 
@@ -137,6 +152,15 @@ tp_status tp_create(const tp_config *cfg, tp_handle **out);
 tp_status tp_destroy(tp_handle *h);
 /* copies the last error message (NUL-terminated) */
 tp_status tp_last_error(const tp_handle *h, char *buf, int buf_len);
+/* Process-wide cap on the device bytes one handle may hold (0 = no cap, the default), for a GPU
+ * shared with other work: an allocation that would exceed it fails like a failed cudaMalloc --
+ * tp_create returns TP_ERR_NOMEM and frees what it had allocated; a lazily allocated buffer
+ * (correlation surfaces, frames, textures, LMA, adjoint) fails its call with TP_ERR_NOMEM and
+ * leaves the handle usable.  No reference counterpart (GPUTileProcessor allocates fixed sizes in
+ * its constructor and never frees). */
+tp_status tp_set_memory_limit(size_t max_bytes_per_handle);
+/* device bytes the handle holds now */
+tp_status tp_get_memory_usage(const tp_handle *h, size_t *bytes);
 /* fills the reference defaults (ImageDttParameters.java:30-112, fat_zero 0.05, corr_sigma 0.8) */
 tp_status tp_default_corr_params(tp_corr_params *p);
 /* CLTParameters defaults of the texture path (min_shot 10, scale_shot 3, diff_sigma 5,
@@ -237,6 +261,13 @@ tp_status tp_get_corr(tp_handle *h, float *corr);
 tp_status tp_get_disparity(tp_handle *h, float *disparity);
 /* getRBG (GPUTileProcessor.java:599-626): [num_colors][height+8][width+8] */
 tp_status tp_get_rbg(tp_handle *h, int cam, float *rbg);
+/* as tp_get_rbg / tp_get_disparity, but only enqueued on `stream` (NULL = the handle's stream)
+ * after the handle's last enqueued work; the host buffer (best page-locked) holds the result once
+ * the stream has passed the copy.  No reference counterpart: getRBG copies synchronously.  A
+ * frame loop reads frame k's colour frames this way while frame k+1 is processed; work that
+ * rewrites the frames (the next tp_imclt) must be ordered after the copy by the caller. */
+tp_status tp_get_rbg_async(tp_handle *h, int cam, float *rbg, void *stream);
+tp_status tp_get_disparity_async(tp_handle *h, float *disparity, void *stream);
 /* texture_tiles[ty][tx]: [tilesY*tilesX][4 or 12][256] (R, B, G, alpha, weights, rms) */
 tp_status tp_get_textures(tp_handle *h, float *tex);
 /* [tilesY*tilesX][16]: max_diff[4] (IMG_DIFF0_INDEX), ports_rgb[12] (IMG_TONE_RGB, colour * 4 + port) */
@@ -341,8 +372,11 @@ tp_status tp_batch_last_error(const tp_batch *b, char *buf, int buf_len);
 /* plans every scene (always when replan != 0, else only where missing), then the one forward launch */
 tp_status tp_batch_process(tp_batch *b, int replan, void *stream);
 /* the same step (with replanning) captured once into a CUDA graph and replayed; the graph is
- * rebuilt when a scene's task count changed; inputs updated in place (tp_set_image, ...) are
- * picked up by the replay */
+ * rebuilt when anything the capture holds by value changed for a scene -- its task count, a
+ * device buffer reallocated (e.g. tp_set_corr with more pairs), the image dtype, colour scales,
+ * pair count, strip rows, correlation parameters or schedule; inputs updated in place in the same
+ * buffers (tp_set_image with the same dtype, tp_set_tile_ops, tp_set_geometry, tp_set_kernels)
+ * are picked up by the replay */
 tp_status tp_batch_run_graph(tp_batch *b, void *stream);
 tp_status tp_batch_synchronize(tp_batch *b);
 
@@ -388,9 +422,11 @@ tp_status tp_get_port_derivatives(tp_handle *h, double *deriv);
  * 686-778).  It allocates nothing -- no cudaMalloc/cudaFree and no allocating
  * library; its per-block counts live in a fixed device array of
  * TP_COMPACT_MAX_TILES / 1024 ints inside libtp.  num_tiles above
- * TP_COMPACT_MAX_TILES returns TP_ERR_SCRATCH_LIMIT.  The first call on a
- * device looks the array's address up (cudaGetSymbolAddress) and caches it;
- * make that first call before any stream capture.  Calls on one device share
+ * TP_COMPACT_MAX_TILES returns TP_ERR_SCRATCH_LIMIT.  A call outside a stream
+ * capture looks the array's address up (cudaGetSymbolAddress) on the current
+ * device and keeps it; a call on a capturing stream uses the address kept by
+ * the last call outside one, so make the first call on each device before any
+ * stream capture (else TP_ERR_STATE).  Calls on one device share
  * the array: calls that overlap in time (different streams or threads) race;
  * serialise them.  Runs on the current device and `stream` (NULL = the default
  * stream), asynchronously. */

@@ -4,8 +4,9 @@ TEST INFRASTRUCTURE ONLY.  The reference GPU kernels (convert_correct_tiles,
 imclt_rbg) live in src/main/resources/{dtt8x8.cuh,TileProcessor.cuh} and are
 normally compiled by NVRTC at run time with a block of #defines prepended
 (GPUTileProcessor.java:262-295).  This recipe does the same with nvcc, for
-sm_103a, reading the sources where they lie under /root/reference and writing
-only into oracle/_ref/ (git-ignored).  The cubin is device code only; the GPU
+sm_103a, reading the sources where they lie in the reference checkout
+(the directory named by the environment variable TP_REFERENCE_DIR, default
+/root/reference) and writing only into oracle/_ref/ (git-ignored).  The cubin is device code only; the GPU
 box loads it through the CUDA driver API (oracle/ref_gpu.py) to produce the
 golden vectors committed under tests/golden/.  Nothing of the reference source
 is copied into the repository.
@@ -16,7 +17,12 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_RES = "/root/reference/src/main/resources"
+REF_DIR = os.environ.get("TP_REFERENCE_DIR", "/root/reference")
+REF_RES = os.path.join(REF_DIR, "src", "main", "resources")
+
+
+def reference_present():
+    return os.path.isdir(REF_RES)
 OUT_DIR = os.path.join(HERE, "_ref")
 
 # compile-time geometry of the golden scene (GPUTileProcessor #defines)
@@ -35,7 +41,7 @@ def defines(width, height):
 
 
 def build(width=GOLDEN_GEOM["IMG_WIDTH"], height=GOLDEN_GEOM["IMG_HEIGHT"], force=False):
-    if not os.path.isdir(REF_RES):
+    if not reference_present():
         return None  # reference sources only exist on the build machine
     os.makedirs(OUT_DIR, exist_ok=True)
     out = cubin_path(width, height)

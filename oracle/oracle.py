@@ -108,6 +108,12 @@ def lib():
                              C.POINTER(_dp), _ip, _dp, C.POINTER(Pairs), C.POINTER(CorrParams),
                              _dp, _dp, _dp, _dp, _ip, _dp]
         L.or_run.restype = C.c_int
+        L.or_run_diag.argtypes = L.or_run.argtypes + [_dp]
+        L.or_run_diag.restype = C.c_int
+        L.or_cm_at.argtypes = [C.POINTER(CorrParams), _dp, C.c_int, C.c_int, _dp]
+        L.or_cm_at.restype = C.c_int
+        L.or_ortho_at.argtypes = [_dp, C.c_int, _dp]
+        L.or_ortho_at.restype = None
         _lib = L
     return _lib
 
@@ -434,14 +440,37 @@ def run(width, height, images, tile_op, disparity, geometry=None, ports_in=None,
     out["disp"] = np.zeros((T, DISP_N)) if ("disp" in want and corr) else None
     out["int_tl"] = np.zeros((T, S, Cn, 2), dtype=np.int32) if "int_tl" in want else None
     out["residual"] = np.zeros((T, S, Cn, 2)) if "residual" in want else None
+    out["diag"] = np.full((T, DIAG_N), np.nan) if ("diag" in want and corr) else None
     nd = lambda k: _d(out[k]) if out[k] is not None else None
-    rc = L.or_run(C.byref(cfg), C.byref(G), _d(pin) if pin is not None else None, img_ptrs,
-                  kern_ptrs, kext_ptrs, _i(tile_op), _d(disparity), C.byref(P), C.byref(cp),
-                  nd("ports"), nd("clt"), nd("corr"), nd("disp"),
-                  _i(out["int_tl"]) if out["int_tl"] is not None else None, nd("residual"))
+    rc = L.or_run_diag(C.byref(cfg), C.byref(G), _d(pin) if pin is not None else None, img_ptrs,
+                       kern_ptrs, kext_ptrs, _i(tile_op), _d(disparity), C.byref(P), C.byref(cp),
+                       nd("ports"), nd("clt"), nd("corr"), nd("disp"),
+                       _i(out["int_tl"]) if out["int_tl"] is not None else None, nd("residual"), nd("diag"))
     if rc != 0:
         raise RuntimeError("or_run failed: %d" % rc)
     return {k: v for k, v in out.items() if v is not None}
+
+
+# per-tile diagnostics of run(..., want=(..., "diag")): the combined strip rows [16][15]
+# (the first min(corr_strip_hight, 16) rows filled), the horizontal and the vertical ortho profiles [15]
+DIAG_ROWS = 16
+DIAG_N = DIAG_ROWS * 15 + 30
+DIAG_HOR, DIAG_VERT = DIAG_ROWS * 15, DIAG_ROWS * 15 + 15
+
+
+def cm_at(corr_params, combo_rows, hwidth, ix):
+    """getMaxXCm of a combined strip [rows][15] at the integer maximum ix: (x, s0, sigma) or None."""
+    r = np.zeros(3)
+    c = _f64(combo_rows).reshape(-1)
+    ok = lib().or_cm_at(C.byref(corr_params), _d(c), int(hwidth), int(ix), _d(r))
+    return r if ok else None
+
+
+def ortho_at(c1d, icenter):
+    """getMaxXSOrtho's (xcenter - 7, strength) of a 15-entry profile around the integer maximum icenter."""
+    r = np.zeros(2)
+    lib().or_ortho_at(_d(_f64(c1d).reshape(15)), int(icenter), _d(r))
+    return r
 
 
 def imclt_frames(clt, tilesX, tilesY, scale=0.25, lpf=None, present=None, num_threads=None):

@@ -971,14 +971,14 @@ void or_ortho_notch(double enhortho_width, double enhortho_scale, double *notch)
  * quadratic fit (PolynomialApproximation.polynomialApproximation1d, exact
  * interpolation through 3 points) is evaluated in closed form.
  */
-int or_max_xs_ortho(const double *corrs, const int *use, int np, double offset, int is_vert,
-                    const double *notch, double rslt[2]) {
+/* the 15-entry profile c1d of getMaxXSOrtho (2502-2651): returns 0 when no pair is used */
+int or_max_xs_ortho_profile(const double *corrs, const int *use, int np, double offset, int is_vert,
+                            const double *notch, double c1d[15]) {
   const int cs = 15;
   int pairs[OR_MAX_PAIRS], n = 0;
   for (int p = 0; p < np; p++) if (use[p]) pairs[n++] = p;
   if (n == 0) return 0;
   double w = 1.0 / n;
-  double c1d[15];
   for (int j = 0; j < cs; j++) {
     c1d[j] = 0;
     for (int i = 0; i < cs; i++) {
@@ -995,8 +995,12 @@ int or_max_xs_ortho(const double *corrs, const int *use, int np, double offset, 
       c1d[j] += combo * notch[i];
     }
   }
-  int icenter = 0;
-  for (int i = 1; i < cs; i++) if (c1d[i] > c1d[icenter]) icenter = i;
+  return 1;
+}
+
+/* the sub-pixel maximum of a profile around the integer maximum icenter: {xcenter - 7, strength} */
+void or_ortho_at(const double *c1d, int icenter, double rslt[2]) {
+  const int cs = 15;
   double xcenter = icenter;
   if ((icenter > 0) && (icenter < (cs - 1))) {
     double f0 = c1d[icenter - 1], f1 = c1d[icenter], f2 = c1d[icenter + 1];
@@ -1008,7 +1012,24 @@ int or_max_xs_ortho(const double *corrs, const int *use, int np, double offset, 
   if (icenter > cs - 1) icenter = cs - 1;
   rslt[0] = xcenter - 7;
   rslt[1] = c1d[icenter] / ((cs + 1) / 2);
+}
+
+int or_max_xs_ortho(const double *corrs, const int *use, int np, double offset, int is_vert,
+                    const double *notch, double rslt[2]) {
+  double c1d[15];
+  if (!or_max_xs_ortho_profile(corrs, use, np, offset, is_vert, notch, c1d)) return 0;
+  int icenter = 0;
+  for (int i = 1; i < 15; i++) if (c1d[i] > c1d[icenter]) icenter = i;
+  or_ortho_at(c1d, icenter, rslt);
   return 1;
+}
+
+/* getMaxXCm (936-1032) of a combined strip at the integer maximum ix, with the y / x windows of cp */
+int or_cm_at(const or_corr_params *cp, const double *combo, int hw, int ix, double rslt[3]) {
+  double wndy[32], wndx[32];
+  or_half_flat_top_window(cp->corr_wndy_size, cp->corr_wndy_hwidth, cp->corr_wndy_blur, 1, 0, 1.0, wndy);
+  or_half_flat_top_window(cp->corr_wndx_size, cp->corr_wndx_hwidth, cp->corr_wndx_blur, 1, 0, 2.0, wndx);
+  return or_max_x_cm(combo, hw, ix, wndy, cp->corr_wndy_size, wndx, cp->corr_wndx_size, rslt);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1372,6 +1393,7 @@ typedef struct {
   double *ports, *clt, *corr, *disp;
   int *int_tl;
   double *residual;
+  double *diag;  /* [T][OR_DIAG_N] or NULL: combined strip rows, hor / vert ortho profiles */
   double (*rots)[3][3];
   double *tbl;
   int tbl_len;
@@ -1474,6 +1496,11 @@ static void run_tile(run_ctx *c, int nTile, double *wk_clt, double *wk_corr, dou
     or_combine_strips(wk_strips, use, P, is_diag, hw, c->cp->corr_offset, c->cp->twice_diagonal, combo);
   }
   double *dm = c->disp + (size_t)nTile * OR_DISP_N;
+  double *dg = c->diag ? c->diag + (size_t)nTile * OR_DIAG_N : NULL;
+  if (dg) {
+    for (int i = 0; i < OR_DIAG_N; i++) dg[i] = NAN;
+    memcpy(dg, combo, sizeof(double) * (hw < OR_DIAG_ROWS ? hw : OR_DIAG_ROWS) * 15);
+  }
   int ix;
   if (or_max_xy_int_axis(combo, hw, c->cp->min_corr, &ix)) {
     double strength = combo[ix + 8 - 1];
@@ -1492,11 +1519,13 @@ static void run_tile(run_ctx *c, int nTile, double *wk_clt, double *wk_corr, dou
   if (or_max_xs_ortho(wk_corr, useo, P, c->cp->corr_offset, 0, c->notch, r)) {
     dm[OR_DISP_HOR] = -r[0];
     dm[OR_DISP_HOR_STRENGTH] = r[1];
+    if (dg) or_max_xs_ortho_profile(wk_corr, useo, P, c->cp->corr_offset, 0, c->notch, dg + OR_DIAG_ROWS * 15);
   }
   for (int p = 0; p < P; p++) useo[p] = (c->pairs->kind[p] == 1);
   if (or_max_xs_ortho(wk_corr, useo, P, c->cp->corr_offset, 1, c->notch, r)) {
     dm[OR_DISP_VERT] = -r[0];
     dm[OR_DISP_VERT_STRENGTH] = r[1];
+    if (dg) or_max_xs_ortho_profile(wk_corr, useo, P, c->cp->corr_offset, 1, c->notch, dg + OR_DIAG_ROWS * 15 + 15);
   }
 }
 
@@ -1517,6 +1546,15 @@ int or_run(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
            const double *const *images, const double *const *kern, const double *const *kext,
            const int *tile_op, const double *disparity, const or_pairs *pairs, const or_corr_params *cp,
            double *ports, double *clt, double *corr, double *disp, int *int_tl, double *residual) {
+  return or_run_diag(cfg, g, ports_in, images, kern, kext, tile_op, disparity, pairs, cp, ports, clt, corr, disp,
+                     int_tl, residual, NULL);
+}
+
+int or_run_diag(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
+                const double *const *images, const double *const *kern, const double *const *kext,
+                const int *tile_op, const double *disparity, const or_pairs *pairs, const or_corr_params *cp,
+                double *ports, double *clt, double *corr, double *disp, int *int_tl, double *residual,
+                double *diag) {
   tables();
   if (cfg->num_sensors < 1 || cfg->num_sensors > OR_MAX_SENSORS) return -1;
   if (cfg->num_colors != 1 && cfg->num_colors != 3) return -2;
@@ -1526,6 +1564,7 @@ int or_run(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
   c.cfg = cfg; c.g = g; c.ports_in = ports_in; c.images = images; c.kern = kern; c.kext = kext;
   c.tile_op = tile_op; c.disparity = disparity; c.pairs = pairs; c.cp = cp;
   c.ports = ports; c.clt = clt; c.corr = corr; c.disp = disp; c.int_tl = int_tl; c.residual = residual;
+  c.diag = diag;
   c.num_tiles = (cfg->width / 8) * (cfg->height / 8);
   double rots[OR_MAX_SENSORS][3][3];
   double tbl[2100];

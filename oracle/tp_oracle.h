@@ -196,6 +196,13 @@ void or_ortho_notch(double enhortho_width, double enhortho_scale, double *notch1
 /* getMaxXSOrtho (2502-2651) with the 3-point parabola in closed form */
 int or_max_xs_ortho(const double *corrs, const int *use, int num_pairs, double offset,
                     int is_vert, const double *notch15, double rslt[2]);
+/* its two halves: the 15-entry profile (0 when no pair is used), and the sub-pixel maximum
+ * {xcenter - 7, strength} around a given integer maximum of a profile */
+int or_max_xs_ortho_profile(const double *corrs, const int *use, int num_pairs, double offset,
+                            int is_vert, const double *notch15, double c1d[15]);
+void or_ortho_at(const double *c1d, int icenter, double rslt[2]);
+/* getMaxXCm of a combined strip at the integer maximum ix with the windows of cp (1 / 0 as or_max_x_cm) */
+int or_cm_at(const or_corr_params *cp, const double *combo, int hwidth, int ix, double rslt[3]);
 
 /* ---- IMCLT / textures ---- */
 /* iclt_2d (ImageDtt.java:3559-3666) into the padded frame (W+8)x(H+8) (no edge
@@ -348,6 +355,17 @@ int or_run(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
            const or_pairs *pairs, const or_corr_params *cp,
            double *ports, double *clt, double *corr, double *disp,
            int *int_tl, double *residual);
+/* or_run with per-tile diagnostics for the parity tests: diag [T][OR_DIAG_N] (NaN where absent) =
+ * the combined strip rows [16][15] (the first min(corr_strip_hight, 16) rows filled), then the
+ * horizontal and the vertical ortho profile [15] each (getMaxXSOrtho c1d) */
+#define OR_DIAG_ROWS 16
+#define OR_DIAG_N (OR_DIAG_ROWS * 15 + 30)
+int or_run_diag(const or_run_cfg *cfg, const or_geometry *g, const double *ports_in,
+                const double *const *images, const double *const *kern, const double *const *kext,
+                const int *tile_op, const double *disparity,
+                const or_pairs *pairs, const or_corr_params *cp,
+                double *ports, double *clt, double *corr, double *disp,
+                int *int_tl, double *residual, double *diag);
 
 #ifdef __cplusplus
 }

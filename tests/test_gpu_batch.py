@@ -27,6 +27,13 @@ def _scenes():
     return out
 
 
+def _twelve_pairs():
+    """The quad pairs and the same six the other way round (general kind, reversed strip axis)."""
+    quad = [(0, 1, 0, 1, 1.0, 0.0), (2, 3, 0, 1, 1.0, 0.0), (0, 2, 1, 1, 0.0, 1.0), (1, 3, 1, 1, 0.0, 1.0),
+            (0, 3, 2, 1, 1.0, 1.0), (2, 1, 3, 1, 1.0, -1.0)]
+    return quad + [(b, a, 4, 1, -bx, -by) for a, b, _, _, bx, by in quad]
+
+
 def _make(sc, k, e, pairs, disp):
     tp = make_gpu(sc, k, e)
     tp.setCorrelation(pairs=pairs)
@@ -76,6 +83,25 @@ def test_batch_matches_per_scene():
             b.run_graph()
             b.synchronize()
             _same(_results(tps[1]), want)
+            # more pairs: the correlation buffer is reallocated and the scene changes schedule class;
+            # the next replay must not reuse the captured step
+            tps[1].setCorrelation(pairs=_twelve_pairs())
+            tps[1].process()
+            want = _results(tps[1])
+            assert want[1].shape[1] == 12
+            b.run_graph()
+            b.synchronize()
+            _same(_results(tps[1]), want)
+            # a correlation parameter of the scene with its own launch (captured by value)
+            tps[3].setCorrelation(fat_zero=0.1)
+            tps[3].process()
+            want = _results(tps[3])
+            b.run_graph()
+            b.synchronize()
+            _same(_results(tps[3]), want)
+            b.process(replan=False)
+            b.synchronize()
+            _same(_results(tps[3]), want)
     finally:
         for tp in tps:
             tp.close()

@@ -5,13 +5,16 @@ Tolerances (stated by the port specification):
   * ports (FP64 on the device): bit-exact;
   * CLT coefficients: relative L2 per (tile, sensor, colour) <= 2e-6;
   * correlation surfaces: relative L2 per (tile, pair) <= 1e-5;
-  * disparity (centroid and ortho): |gpu - oracle| <= 0.005 px on tiles whose
-    integer argmax is not a near-tie (top two strip values differ by > 1e-4).
+  * disparity (centroid and ortho): |gpu - oracle| <= 0.005 px on every tile the
+    oracle processed, no quantile.  Where the GPU's integer maximum differs from
+    the oracle's, the oracle's own values at the two maxima must be a near tie
+    (relative gap <= 1e-4, helpers.NEAR_TIE) and the GPU's disparity must equal
+    the oracle's evaluated at the GPU's maximum (helpers.check_disparity_strict).
 """
 import numpy as np
 import pytest
 
-from helpers import make_gpu, rel_l2, run_oracle
+from helpers import check_disparity_strict, make_gpu, rel_l2, run_oracle
 from tileproc import synth
 
 pytestmark = pytest.mark.gpu
@@ -47,24 +50,8 @@ def _check_corr(tp, ref, tile_mask=None):
     return e
 
 
-def _check_disp(O, tp, ref, check_ortho=True, min_frac=0.995):
-    d = tp.getDisparity().astype(np.float64)
-    r = ref["disp"]
-    both = np.isfinite(r[:, O.DISP_CM]) & np.isfinite(d[:, O.DISP_CM])
-    agree = both & (d[:, O.DISP_IXY] == r[:, O.DISP_IXY])
-    n = np.isfinite(r[:, O.DISP_CM]).sum()
-    assert n > 0
-    frac = agree.sum() / n
-    assert frac >= min_frac, "integer argmax agrees on %.4f of tiles" % frac
-    err = np.abs(d[agree, O.DISP_CM] - r[agree, O.DISP_CM])
-    assert err.max() <= DISP_TOL, "centroid disparity max err %.4g px" % err.max()
-    if check_ortho:
-        for k in (O.DISP_HOR, O.DISP_VERT):
-            ok = np.isfinite(r[:, k]) & np.isfinite(d[:, k])
-            e = np.abs(d[ok, k] - r[ok, k])
-            assert np.quantile(e, 0.995) <= DISP_TOL, "ortho %d err q99.5 %.4g" % (k, np.quantile(e, 0.995))
-    # tiles without a task keep the reference's initial values
-    return err
+def _check_disp(O, tp, ref, check_ortho=True):
+    return check_disparity_strict(O, tp.getDisparity().astype(np.float64), ref, check_ortho=check_ortho)
 
 
 def test_quad_mono_identity(oracle):
@@ -136,7 +123,7 @@ def test_circle16_extrinsics(oracle, sched):
         _check_tiles(oracle, tp, ref, 1)
         _check_clt(tp, ref)
         _check_corr(tp, ref)
-        _check_disp(oracle, tp, ref, check_ortho=False, min_frac=0.99)
+        _check_disp(oracle, tp, ref, check_ortho=False)
 
 
 def test_float_tasks_ragged(oracle):
@@ -248,9 +235,8 @@ def test_stage_kernels_and_schedules_agree(oracle, sched):
     for corr in (corr_s, corr_f):
         e2 = rel_l2(corr.astype(np.float64), ref["corr"], axis=-1)
         assert e2.max() <= CORR_TOL
-    ok = np.isfinite(ref["disp"][:, oracle.DISP_CM]) & (d_f[:, oracle.DISP_IXY] == ref["disp"][:, oracle.DISP_IXY])
-    assert np.abs(d_f[ok, oracle.DISP_CM] - ref["disp"][ok, oracle.DISP_CM]).max() <= DISP_TOL
-    assert np.abs(d_f[ok, oracle.DISP_CM] - d_s[ok, oracle.DISP_CM]).max() <= DISP_TOL
+    for d in (d_s, d_f):
+        check_disparity_strict(oracle, d.astype(np.float64), ref)
 
 
 def test_bayer_planes_input_matches_mosaic(oracle):
@@ -331,14 +317,11 @@ def test_full_size_bayer_sampled_tiles(oracle):
         corr = tp.getCorr()[sel].astype(np.float64)
         er = rel_l2(corr, ref["corr"][sel], axis=-1)
         assert er.max() <= CORR_TOL, "corr rel L2 max %.3g" % er.max()
-        d = tp.getDisparity()[sel].astype(np.float64)
-    r = ref["disp"][sel]
-    agree = np.isfinite(r[:, oracle.DISP_CM]) & np.isfinite(d[:, oracle.DISP_CM]) & \
-        (d[:, oracle.DISP_IXY] == r[:, oracle.DISP_IXY])
-    n = np.isfinite(r[:, oracle.DISP_CM]).sum()
-    assert n > 0.9 * len(sel) and agree.sum() >= 0.995 * n
-    assert np.abs(d[agree, oracle.DISP_CM] - r[agree, oracle.DISP_CM]).max() <= DISP_TOL
-    print("full size: %d tiles checked, CLT max %.3g, corr max %.3g" % (len(sel), ec.max(), er.max()))
+        d = tp.getDisparity().astype(np.float64)
+    assert np.isfinite(ref["disp"][sel, oracle.DISP_CM]).sum() > 0.9 * len(sel)
+    summ = check_disparity_strict(oracle, d, ref, tiles=sel)
+    print("full size: %d tiles checked, CLT max %.3g, corr max %.3g, disparity %s" % (len(sel), ec.max(), er.max(),
+                                                                                       summ))
 
 
 def test_full_size_circle16_sampled_tiles(oracle):
@@ -367,11 +350,8 @@ def test_full_size_circle16_sampled_tiles(oracle):
         assert ec.max() <= CLT_TOL, "CLT rel L2 max %.3g" % ec.max()
         er = rel_l2(tp.getCorr()[sel].astype(np.float64), ref["corr"][sel], axis=-1)
         assert er.max() <= CORR_TOL, "corr rel L2 max %.3g" % er.max()
-        d = tp.getDisparity()[sel].astype(np.float64)
-    r = ref["disp"][sel]
-    agree = np.isfinite(r[:, oracle.DISP_CM]) & np.isfinite(d[:, oracle.DISP_CM]) & \
-        (d[:, oracle.DISP_IXY] == r[:, oracle.DISP_IXY])
-    n = np.isfinite(r[:, oracle.DISP_CM]).sum()
-    assert n > 0.9 * len(sel) and agree.sum() >= 0.99 * n
-    assert np.abs(d[agree, oracle.DISP_CM] - r[agree, oracle.DISP_CM]).max() <= DISP_TOL
-    print("full size LWIR: %d tiles checked, CLT max %.3g, corr max %.3g" % (len(sel), ec.max(), er.max()))
+        d = tp.getDisparity().astype(np.float64)
+    assert np.isfinite(ref["disp"][sel, oracle.DISP_CM]).sum() > 0.9 * len(sel)
+    summ = check_disparity_strict(oracle, d, ref, tiles=sel, check_ortho=False)
+    print("full size LWIR: %d tiles checked, CLT max %.3g, corr max %.3g, disparity %s" % (
+        len(sel), ec.max(), er.max(), summ))
