@@ -19,7 +19,7 @@ class LinearProcessor:
         self.tilesX, self.tilesY, self.num_sensors = TX, TY, S
         self.A = rng.normal(size=(T, S * 4))
         self.b = rng.uniform(0.5, 1.5, T)
-        self.r0 = rng.normal(size=T)
+        self.r0 = 0.2 * rng.normal(size=T)  # steps inside lma.MAX_DISPARITY_STEP
         self.D0 = rng.uniform(1, 3, T)
         self.g = None
         self.D = None
@@ -64,9 +64,21 @@ def test_step_equals_full_normal_equations():
     JtJ = J.T @ J
     step = np.linalg.solve(JtJ + lam * np.diag(np.diag(JtJ)), -J.T @ r)
     de = np.array([g1[k][s] for s in range(S) for k in lma.KEYS])
+    assert np.abs(step[S * 4:]).max() < lma.MAX_DISPARITY_STEP
     assert np.allclose(de, step[:S * 4], atol=2e-5)
     assert np.allclose(D1 - D0, step[S * 4:], atol=2e-5)
     assert hist[1] < hist[0]
+
+
+def test_disparity_step_is_clipped():
+    """A tile whose residual barely depends on its disparity would take an unbounded step."""
+    rng = np.random.default_rng(3)
+    tp = LinearProcessor(rng)
+    tp.b[4] = 1e-4
+    tp.r0[4] = 0.5
+    g1, D1, hist = lma.refine(tp, _geom(), tp.D0.copy(), iterations=1, lam=0.3)
+    assert np.abs(D1 - tp.D0).max() <= lma.MAX_DISPARITY_STEP
+    assert abs(D1[4] - tp.D0[4]) == lma.MAX_DISPARITY_STEP
 
 
 def test_iterations_reduce_cost_fixed_disparity():
