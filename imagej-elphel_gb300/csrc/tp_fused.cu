@@ -36,8 +36,8 @@ constexpr int SCR = 288;           // per-warp scratch floats: [4][8][9] transpo
 // phase A: CLT of one sub-tile, lane r of the 8-lane group holds row r
 // (= horizontal frequency r) of each quadrant on return: o[m][v].
 // ---------------------------------------------------------------------------
-template <int KIND>  // 0 mono, 1 Bayer red/blue, 2 Bayer green
-__device__ __forceinline__ void subtile_clt(const Win &w, float rx, float ry, int pc, int pr, int pg, int r,
+template <int KIND, typename PIX = Win>  // 0 mono, 1 Bayer red/blue, 2 Bayer green; PIX: at(row, col)
+__device__ __forceinline__ void subtile_clt(const PIX &w, float rx, float ry, int pc, int pr, int pg, int r,
                                             float *tbuf, float o[4][8]) {
   float ahs, ahc, avs, avc;
   __sincosf(CUDART_PI_F * 0.0625f * rx, &ahs, &ahc);
@@ -45,7 +45,7 @@ __device__ __forceinline__ void subtile_clt(const Win &w, float rx, float ry, in
   const FoldIdx fv = fold_idx(r);
   float vw0, vw1, hw0[8], hw1[8];
   fold_weights(ahc, ahs, avc, avs, fv, vw0, vw1, hw0, hw1);
-  if (KIND == 1) {
+  if constexpr (KIND == 1) {
     // one nonzero pixel per folded value: the term whose source row/column has the colour's parity
     const bool a1 = (fv.src0 & 1) != pr;
     const int srow = a1 ? fv.src1 : fv.src0;
@@ -72,7 +72,7 @@ __device__ __forceinline__ void subtile_clt(const Win &w, float rx, float ry, in
       o[2][v] = sv * o[0][7 - v];
       o[3][v] = sv * o[1][7 - v];
     }
-  } else if (KIND == 2) {
+  } else if constexpr (KIND == 2) {
     // two nonzero pixels per folded value (checkerboard): CC and SC folds
     float ycc[8], ysc[8];
 #pragma unroll
@@ -535,13 +535,172 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
+// Warp per tile with staged image windows: scenes of 4 (or fewer) u16 Bayer sensors.
+// The image reads of phase A are its main cost (the warp waits on them once per
+// colour item), so each item's four 16x16 sensor windows are copied into shared
+// memory one item ahead, while the warp computes the previous item: 16 rows x 24
+// u16 from the 16-byte boundary below the window corner, three 16-byte cp.async
+// chunks per row, into the CLT slot of (sensor, colour) -- that slot holds nothing
+// until the item writes its CLT there, after its last window read.  The next
+// tile's first windows go in after its correlation phase has read the CLT slots.
+// Windows that cross the image border are gathered with the edge mirroring.
+// ---------------------------------------------------------------------------
+constexpr int WROW = 24;  // staged window row: 24 u16 (48 bytes)
+
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// pixel source of subtile_clt: a staged window, column sx of the 16-byte aligned copy
+struct SWin {
+  const uint16_t *base;
+  int sx;
+  float scale;
+  __device__ __forceinline__ float at(int row, int col) const { return (float)base[row * WROW + sx + col] * scale; }
+};
+
+// lanes 8q..8q+7 (r = lane & 7) copy sensor q's window at corner (tlx, tly) into dst: 48 chunks,
+// 6 per lane; chunk 2 of a row is left out where it would pass the row's end (then tlx is
+// 16-byte aligned and the window lies in chunks 0 and 1)
+__device__ __forceinline__ void stage_window(const SceneDev &sc, const uint16_t *img, int tlx, int tly,
+                                             uint16_t *dst, int r) {
+  const int x0 = tlx & ~7, W = sc.width, H = sc.height;
+  const int64_t pitch = sc.img_pitch;
+  if (tlx >= 0 && tly >= 0 && tlx <= W - 16 && tly <= H - 16) {
+    const bool third = x0 + WROW <= W;
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      const int k = r + 8 * j, row = k / 3, part = k - row * 3;
+      if (part < 2 || third) cp_async16(dst + row * WROW + part * 8, img + (size_t)(tly + row) * pitch + x0 + part * 8);
+    }
+  } else {
+#pragma unroll 1
+    for (int j = 0; j < 6; j++) {
+      const int k = r + 8 * j, row = k / 3, part = k - row * 3;
+      const size_t yo = (size_t)mirror(tly + row, H) * pitch;
+#pragma unroll
+      for (int e = 0; e < 8; e++) dst[row * WROW + part * 8 + e] = __ldg(img + yo + mirror(x0 + part * 8 + e, W));
+    }
+  }
+}
+
+__device__ __forceinline__ SubtilePlan load_plan(const SceneDev &sc, int task, int s, int c) {
+  return sc.plan[((size_t)task * sc.num_sensors + s) * 3 + c];
+}
+
+// phase A item c (colour) of a staged tile: the window of (sensor q, c) is in its CLT slot; pn is
+// the plan of item c + 1, whose windows are staged once this item's are read
+__device__ __forceinline__ void fwd_clt_item_win(const SceneDev &sc, const uint16_t *img, int S, size_t tile, int c,
+                                                 const SubtilePlan &p, const SubtilePlan &pn, float *s_clt,
+                                                 float *scr, int lane) {
+  const int q = lane >> 3, r = lane & 7;
+  const int rr = sc.bayer_red_row, rc = sc.bayer_red_col;
+  const bool act = q < S;
+  const int sidx = act ? q : S - 1;
+  SWin w;
+  w.base = (const uint16_t *)(s_clt + ((size_t)sidx * 3 + c) * TP_CLT);
+  w.sx = p.tlx - (p.tlx & ~7);
+  w.scale = sc.color_scale[c];
+  float o[4][8];
+  float *tbuf = scr + q * 72;
+  if (c < 2) {
+    const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
+    subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
+  } else {
+    const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
+    subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
+  }
+  // every lane has read this item's windows (the transposes in subtile_clt synchronise the warp)
+  if (c < 2) {
+    if (act) stage_window(sc, img, pn.tlx, pn.tly, (uint16_t *)(s_clt + ((size_t)q * 3 + c + 1) * TP_CLT), r);
+    cp_async_commit();
+  }
+  const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
+  conv_shift(o, kp, p.rx, p.ry, r);
+  if (act) {
+    float *gdst = sc.clt + ((tile * S + q) * 3 + c) * TP_CLT + r * 8;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+      *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+    }
+    float *sdst = s_clt + ((size_t)q * 3 + c) * TP_CLT + r * 8;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      *(float4 *)(sdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+      *(float4 *)(sdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+    }
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(128, 4) fused_forward_win_kernel(const __grid_constant__ SceneDev sc,
+                                                                   const __grid_constant__ FwdShape fs,
+                                                                   const __grid_constant__ CorrConst cfg) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
+  const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
+  float *s_clt = sm + warp * fs.per_warp;
+  float *scr = s_clt + fs.clt_floats;
+  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
+  const bool log_mode = cfg.log_combine;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  const bool act = q < S;
+  const int sidx = act ? q : S - 1;
+  const uint16_t *img = (const uint16_t *)sc.images[sidx];
+  const int stride = gridDim.x * NW;
+  SubtilePlan pc;
+  int task = blockIdx.x * NW + warp;
+  if (task < sc.num_tasks) {
+    pc = load_plan(sc, task, sidx, 0);
+    if (act) stage_window(sc, img, pc.tlx, pc.tly, (uint16_t *)(s_clt + (size_t)q * 3 * TP_CLT), r);
+    cp_async_commit();
+  }
+  for (; task < sc.num_tasks; task += stride) {
+    const int txy = sc.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+#pragma unroll 1
+    for (int c = 0; c < 3; c++) {
+      const SubtilePlan pn = load_plan(sc, task, sidx, c < 2 ? c + 1 : c);
+      cp_async_wait_all();  // this item's windows, copied by every lane
+      __syncwarp();
+      fwd_clt_item_win(sc, img, S, tile, c, pc, pn, s_clt, scr, lane);
+      pc = pn;
+    }
+    __syncwarp();
+    const int next = task + stride;
+    if (next < sc.num_tasks) pc = load_plan(sc, next, sidx, 0);
+    float cmb[8];
+#pragma unroll
+    for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
+    float oprod[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) oprod[i] = 1.f;
+    for (int pi = 0; pi < P; pi++)
+      fwd_pair<3, NT, true>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr, oprod);
+    if (next < sc.num_tasks) {  // the CLT slots are read (fwd_pair ends with __syncwarp): next tile's windows
+      if (act) stage_window(sc, img, pc.tlx, pc.tly, (uint16_t *)(s_clt + (size_t)q * 3 * TP_CLT), r);
+      cp_async_commit();
+    }
+    fwd_extract<NT, true>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
+  }
+  cp_async_wait_all();
+}
+
+// ---------------------------------------------------------------------------
 // pair-per-warp schedule: a CTA of nw warps per tile shares the tile's CLT; the
 // warps split the (colour, sensor-group) items, then the pairs, and warp 0
 // combines their partial strip products for the extraction.  For many pairs
 // (16 sensors, 120 pairs) this holds one CLT per CTA instead of one per warp.
+// MAXT / MINB: the launch bounds.  With 3 warps for a quad colour scene (one colour
+// item, then two pairs per warp) and 8 CTAs per SM the register budget is 85 per
+// thread, for 24 resident warps sharing 8 tile CLTs.
 // ---------------------------------------------------------------------------
-template <int C, int NT>
-__global__ void __launch_bounds__(128, 4) fused_split_kernel(const __grid_constant__ SceneDev sc,
+template <int C, int NT, int MAXT = 128, int MINB = 4>
+__global__ void __launch_bounds__(MAXT, MINB) fused_split_kernel(const __grid_constant__ SceneDev sc,
                                                           const __grid_constant__ FwdShape fs,
                                                           const __grid_constant__ CorrConst cfg) {
   extern __shared__ float sm[];
@@ -1072,6 +1231,15 @@ cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tp
   if (f.nw > 4) return cudaErrorInvalidConfiguration;
   if (tpb == 1 && f.nw > 1) {
     const int bytes = split_smem_floats(f) * 4;
+    if (f.nw == 3) {  // quad colour scenes: one colour item per warp, 8 CTAs per SM
+      if (f.RE <= 32)
+        return sc.num_colors == 3
+                   ? launch_persistent(fused_split_kernel<3, 1, 96, 8>, 96, bytes, sc.num_tasks, sc, f, cc, st)
+                   : launch_persistent(fused_split_kernel<1, 1, 96, 8>, 96, bytes, sc.num_tasks, sc, f, cc, st);
+      return sc.num_colors == 3
+                 ? launch_persistent(fused_split_kernel<3, 8, 96, 8>, 96, bytes, sc.num_tasks, sc, f, cc, st)
+                 : launch_persistent(fused_split_kernel<1, 8, 96, 8>, 96, bytes, sc.num_tasks, sc, f, cc, st);
+    }
     if (f.RE <= 32)
       return sc.num_colors == 3
                  ? launch_persistent(fused_split_kernel<3, 1>, f.nw * 32, bytes, sc.num_tasks, sc, f, cc, st)
@@ -1082,6 +1250,12 @@ cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tp
   }
   const int bytes = f.per_warp * f.nw * 4;
   const int units = (sc.num_tasks + f.nw - 1) / f.nw;
+  bool all16 = true;
+  for (int i = 0; i < sc.num_sensors; i++) all16 = all16 && sc.img_dtype[i] == 1;
+  if (sc.num_colors == 3 && sc.num_sensors <= 4 && all16) {  // staged windows
+    if (f.RE <= 32) return launch_persistent(fused_forward_win_kernel<1>, f.nw * 32, bytes, units, sc, f, cc, st);
+    return launch_persistent(fused_forward_win_kernel<8>, f.nw * 32, bytes, units, sc, f, cc, st);
+  }
   if (f.RE <= 32)
     return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3, 1>, f.nw * 32, bytes, units, sc, f, cc, st)
                               : launch_persistent(fused_forward_kernel<1, 1>, f.nw * 32, bytes, units, sc, f, cc, st);

@@ -505,22 +505,30 @@ def texture_params(**kw):
     return p
 
 
-def texture_tile(clt, lpf, img_mask=0xf, col_weights=(0.25, 0.25, 0.5), extra_disparity=0.0, params=None):
+def texture_tile(clt, lpf, img_mask=0xf, col_weights=(0.25, 0.25, 0.5), extra_disparity=0.0, params=None,
+                 diag=False, near_tie=1e-6):
     """ImageDtt texture branch (2662-2812) for one tile: clt [4][3][4][64] ->
-    (rgba [12][256], aux [16] = max_diff[4], ports_rgb[12])."""
+    (rgba [12][256], aux [16] = max_diff[4], ports_rgb[12]) and with diag the per-tile
+    diagnostics [3] (smallest relative margins of the second-port and dust-removal choices,
+    smallest distance of a weight exponent from the double underflow of exp) and the tile
+    [12][256] with every near-tie choice (0 < relative margin < near_tie) taken the other way."""
     L = lib()
     if not getattr(L, "_tex_set", False):
-        L.or_texture_tile.argtypes = [_dp, _dp, C.c_int, _dp, C.c_double, C.POINTER(TexParams), _dp, _dp]
-        L.or_texture_tile.restype = None
+        L.or_texture_tile_diag.argtypes = [_dp, _dp, C.c_int, _dp, C.c_double, C.POINTER(TexParams), _dp, _dp,
+                                           _dp, _dp, C.c_double]
+        L.or_texture_tile_diag.restype = None
         L._tex_set = True
     c = _f64(clt).reshape(4, 3, 4, 64)
     lp = _f64(lpf).reshape(64)
     cw = _f64(col_weights).reshape(3)
     out = np.zeros((12, 256))
     aux = np.zeros(16)
-    L.or_texture_tile(_d(c), _d(lp), int(img_mask), _d(cw), float(extra_disparity),
-                      C.byref(params if params is not None else texture_params()), _d(out), _d(aux))
-    return out, aux
+    dg = np.zeros(3)
+    alt = np.zeros((12, 256))
+    L.or_texture_tile_diag(_d(c), _d(lp), int(img_mask), _d(cw), float(extra_disparity),
+                           C.byref(params if params is not None else texture_params()), _d(out), _d(aux), _d(dg),
+                           _d(alt) if diag else None, float(near_tie))
+    return (out, aux, dg, alt) if diag else (out, aux)
 
 
 def texture_tiles(clt, tiles, img_mask, lpf, col_weights=(0.25, 0.25, 0.5), extra=None, params=None,

@@ -1090,12 +1090,30 @@ static void tile_debayer_shot_corr(int rb, const double *tile, const double *win
   for (int i = 0; i < 256; i++) out[i] = out[i] * window2[i];
 }
 
-/* dust_remove (3002-3019), port weights [4][256] */
-static void dust_remove(double pw[4][256]) {
+/* relative margin below which a discrete choice of the texture stage counts as a near tie (the
+ * test diagnostics flip such choices to measure their effect); set by or_texture_tile_diag */
+static __thread double or_tex_near_tie = 1e-6;
+
+/* dust_remove (3002-3019), port weights [4][256]; diag: the smallest relative margin of the
+ * weakest-port choice (test diagnostics, may be NULL); flip: take the second weakest port where
+ * the margin is a near tie (0 < margin < or_tex_near_tie) */
+static void dust_remove(double pw[4][256], double *diag, int flip) {
   const int np = 4;
   for (int i = 0; i < 256; i++) {
     int wi = 0;
     for (int ip = 1; ip < np; ip++) if (pw[ip][i] < pw[wi][i]) wi = ip;
+    if (diag || flip) {
+      double mx = 0, next = INFINITY;
+      int wn = -1;
+      for (int ip = 0; ip < np; ip++) {
+        if (pw[ip][i] > mx) mx = pw[ip][i];
+        if (ip != wi && pw[ip][i] < next) { next = pw[ip][i]; wn = ip; }
+      }
+      const double m = mx > 0 ? (next - pw[wi][i]) / mx : INFINITY;
+      if (diag && m < diag[1]) diag[1] = m;
+      /* an exact tie comes from identical inputs, which FP32 resolves the same way */
+      if (flip && m > 0 && m < or_tex_near_tie && wn >= 0) wi = wn;
+    }
     double avg = 0;
     for (int ip = 1; ip < np; ip++) if (ip != wi) avg += pw[ip][i];
     avg /= (np - 1);
@@ -1108,8 +1126,14 @@ static void dust_remove(double pw[4][256]) {
 static const double PORT_OFFSETS[4][2] = {{-0.5, -0.5}, {0.5, -0.5}, {-0.5, 0.5}, {0.5, 0.5}};
 
 /* tile_combine_rgba (2830-3000), keep_weights layout; iclt [4][3][256], window = lt_window2 */
+/* diag (test diagnostics, may be NULL): [0] smallest relative margin over the pixels between the
+ * second port of the best pair and the next one, [1] of dust_remove's weakest-port choice, [2]
+ * smallest distance of a pixel's weight exponents from the double underflow of exp (745.13);
+ * flip: where a margin is a near tie (0 < margin < or_tex_near_tie), take the other port (the
+ * sensitivity of the output) */
 static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, int port_mask, double diff_sigma,
-                              const double *chn_weights, int dust, double *rgba /* [12][256] */) {
+                              const double *chn_weights, int dust, double *rgba /* [12][256] */, double *diag,
+                              int flip) {
   const int ports = 4, numcol = 3;
   int usedPorts = ((port_mask >> 0) & 1) + ((port_mask >> 1) & 1) + ((port_mask >> 2) & 1) + ((port_mask >> 3) & 1);
   double pw[4][256], color_avg[3][256];
@@ -1145,6 +1169,7 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
           }
     for (int i = 0; i < 256; i++) {
       for (int ip = 0; ip < ports; ip++) pw[ip][i] = 0.0;
+      double amin = INFINITY;
       for (int ip = 0; ip < np; ip++) {
         double d = 0;
         for (int chn = 0; chn < numcol; chn++) {
@@ -1152,6 +1177,7 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
           dc /= lt_window[i];
           d += chn_weights[chn] * dc * dc;
         }
+        if (pair_dist2r[ip] * d < amin) amin = pair_dist2r[ip] * d;
         d = exp(-pair_dist2r[ip] * d);
         pw[pp[ip][0]][i] += d;
         pw[pp[ip][1]][i] += d;
@@ -1160,6 +1186,18 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
       for (int ip = b1 + 1; ip < ports; ip++) if (pw[ip][i] > pw[b1][i]) b1 = ip;
       int b2 = (b1 == 0) ? 1 : 0;
       for (int ip = b2 + 1; ip < ports; ip++) if ((ip != b1) && (pw[ip][i] > pw[b2][i])) b2 = ip;
+      if (diag || flip) {
+        /* the pair {b1, b2} is a set (its average does not depend on their order): what can flip
+         * is the second port against the best of the others */
+        double r2 = 0;
+        int b3 = -1;
+        for (int ip = 0; ip < ports; ip++)
+          if ((port_mask & (1 << ip)) && ip != b1 && ip != b2 && pw[ip][i] > r2) { r2 = pw[ip][i]; b3 = ip; }
+        const double m = (pw[b1][i] > 0 && b3 >= 0) ? (pw[b2][i] - r2) / pw[b1][i] : INFINITY;
+        if (diag && m < diag[0]) diag[0] = m;
+        if (diag && fabs(amin - 745.13) < diag[2]) diag[2] = fabs(amin - 745.13);
+        if (flip && m > 0 && m < or_tex_near_tie) b2 = b3;
+      }
       double w1 = pw[b1][i] / (pw[b1][i] + pw[b2][i]), w2 = 1.0 - w1;
       for (int chn = 0; chn < numcol; chn++) color_avg[chn][i] = w1 * iclt[b1][chn][i] + w2 * iclt[b2][chn][i];
       double d2[4];
@@ -1173,6 +1211,12 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
           }
           pw[ip][i] = exp(-ksigma * d2[ip]);
         }
+      if (diag && !flip) {
+        double bmin = INFINITY;
+        for (int ip = 0; ip < ports; ip++)
+          if ((port_mask & (1 << ip)) && ksigma * d2[ip] < bmin) bmin = ksigma * d2[ip];
+        if (fabs(bmin - 745.13) < diag[2]) diag[2] = fabs(bmin - 745.13);
+      }
       double k = 0.0;
       for (int ip = 0; ip < ports; ip++) k += pw[ip][i];
       k = 1.0 / k;
@@ -1189,7 +1233,7 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
           pw[ip][i] = 1.0;
         }
   }
-  if (dust && (usedPorts == 4)) dust_remove(pw);
+  if (dust && (usedPorts == 4)) dust_remove(pw, diag, flip);
   for (int i = 0; i < 256; i++) {
     double alpha = 0.0;
     for (int ip = 0; ip < ports; ip++) if (port_mask & (1 << ip)) alpha += pw[ip][i];
@@ -1200,40 +1244,11 @@ static void tile_combine_rgba(double iclt[4][3][256], const double *lt_window, i
   for (int ip = 0; ip < ports; ip++) memcpy(rgba + (numcol + 1 + ip) * 256, pw[ip], sizeof(pw[ip]));
 }
 
-void or_texture_tile(const double *clt_in, const double *filter, int img_mask, const double *col_weights,
-                     double extra_disparity, const or_tex_params *tp, double *out, double *aux) {
-  tables();
-  double lt_window[256], lt_window2[256];
-  or_win2d(lt_window);
-  for (int i = 0; i < 256; i++) lt_window2[i] = lt_window[i] * lt_window[i];
-  double(*ic)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
-  double(*db)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
-  double *clt = (double *)malloc(sizeof(double) * 4 * 3 * 256);
-  memcpy(clt, clt_in, sizeof(double) * 4 * 3 * 256);
-  if (extra_disparity != 0.0) /* 2663-2678 */
-    for (int chn = 0; chn < 3; chn++)
-      for (int i = 0; i < 4; i++)
-        or_fract_shift((double(*)[64])(clt + (i * 3 + chn) * 256),
-                       extra_disparity * PORT_OFFSETS[i][0] / tp->corr_magic_scale,
-                       extra_disparity * PORT_OFFSETS[i][1] / tp->corr_magic_scale);
-  const double scale = 0.25;
-  for (int i = 0; i < 4; i++)
-    for (int chn = 0; chn < 3; chn++) {
-      for (int dct_mode = 0; dct_mode < 4; dct_mode++) {
-        double t[64], tdct[64], mdct[256];
-        const double *src = clt + ((i * 3 + chn) * 4 + dct_mode) * 64;
-        for (int j = 0; j < 64; j++) t[j] = src[j] * (scale * filter[j]);
-        int idct_mode = ((dct_mode << 1) & 2) | ((dct_mode >> 1) & 1);
-        or_dttt_iv(t, tdct, idct_mode);
-        or_unfold_tile(tdct, dct_mode, mdct);
-        for (int j = 0; j < 256; j++) {
-          if (dct_mode == 0) ic[i][chn][j] = mdct[j];
-          else ic[i][chn][j] += mdct[j];
-        }
-      }
-      tile_debayer_shot_corr(chn != 2, ic[i][chn], lt_window2, tp->min_shot, tp->scale_shot, db[i][chn]);
-    }
-  tile_combine_rgba(db, lt_window2, img_mask, tp->diff_sigma, col_weights, tp->dust_remove, out);
+/* port weighting, aux values and the RGB mix of a tile's per-port tiles (ic: IMCLT, db: debayered) */
+static void texture_tail(double ic[4][3][256], double db[4][3][256], const double *lt_window2, int img_mask,
+                         const double *col_weights, const or_tex_params *tp, double *out, double *aux, double *diag,
+                         int flip) {
+  tile_combine_rgba(db, lt_window2, img_mask, tp->diff_sigma, col_weights, tp->dust_remove, out, diag, flip);
   if (aux) { /* max_diff (2964-2981) from the combined average, ports_rgb (2982-2994) */
     for (int ip = 0; ip < 4; ip++) {
       double md = 0;
@@ -1267,6 +1282,51 @@ void or_texture_tile(const double *clt_in, const double *filter, int img_mask, c
       out[chn * 256 + i] = v;
     }
   }
+}
+
+void or_texture_tile(const double *clt_in, const double *filter, int img_mask, const double *col_weights,
+                     double extra_disparity, const or_tex_params *tp, double *out, double *aux) {
+  or_texture_tile_diag(clt_in, filter, img_mask, col_weights, extra_disparity, tp, out, aux, NULL, NULL, 0.0);
+}
+
+void or_texture_tile_diag(const double *clt_in, const double *filter, int img_mask, const double *col_weights,
+                          double extra_disparity, const or_tex_params *tp, double *out, double *aux, double *diag,
+                          double *out_alt, double near_tie) {
+  tables();
+  or_tex_near_tie = near_tie;
+  if (diag) diag[0] = diag[1] = diag[2] = INFINITY;
+  double lt_window[256], lt_window2[256];
+  or_win2d(lt_window);
+  for (int i = 0; i < 256; i++) lt_window2[i] = lt_window[i] * lt_window[i];
+  double(*ic)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
+  double(*db)[3][256] = (double(*)[3][256])malloc(sizeof(double) * 4 * 3 * 256);
+  double *clt = (double *)malloc(sizeof(double) * 4 * 3 * 256);
+  memcpy(clt, clt_in, sizeof(double) * 4 * 3 * 256);
+  if (extra_disparity != 0.0) /* 2663-2678 */
+    for (int chn = 0; chn < 3; chn++)
+      for (int i = 0; i < 4; i++)
+        or_fract_shift((double(*)[64])(clt + (i * 3 + chn) * 256),
+                       extra_disparity * PORT_OFFSETS[i][0] / tp->corr_magic_scale,
+                       extra_disparity * PORT_OFFSETS[i][1] / tp->corr_magic_scale);
+  const double scale = 0.25;
+  for (int i = 0; i < 4; i++)
+    for (int chn = 0; chn < 3; chn++) {
+      for (int dct_mode = 0; dct_mode < 4; dct_mode++) {
+        double t[64], tdct[64], mdct[256];
+        const double *src = clt + ((i * 3 + chn) * 4 + dct_mode) * 64;
+        for (int j = 0; j < 64; j++) t[j] = src[j] * (scale * filter[j]);
+        int idct_mode = ((dct_mode << 1) & 2) | ((dct_mode >> 1) & 1);
+        or_dttt_iv(t, tdct, idct_mode);
+        or_unfold_tile(tdct, dct_mode, mdct);
+        for (int j = 0; j < 256; j++) {
+          if (dct_mode == 0) ic[i][chn][j] = mdct[j];
+          else ic[i][chn][j] += mdct[j];
+        }
+      }
+      tile_debayer_shot_corr(chn != 2, ic[i][chn], lt_window2, tp->min_shot, tp->scale_shot, db[i][chn]);
+    }
+  texture_tail(ic, db, lt_window2, img_mask, col_weights, tp, out, aux, diag, 0);
+  if (out_alt) texture_tail(ic, db, lt_window2, img_mask, col_weights, tp, out_alt, NULL, NULL, 1);
   free(ic);
   free(db);
   free(clt);

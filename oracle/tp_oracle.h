@@ -319,6 +319,16 @@ typedef struct {
  */
 void or_texture_tile(const double *clt, const double *filter, int img_mask, const double *col_weights,
                      double extra_disparity, const or_tex_params *tp, double *out, double *aux);
+/* or_texture_tile with test diagnostics diag[3]: the smallest relative margin over the pixels
+ * between the second port of the best pair and the next port, of dust_remove's weakest-port
+ * choice, and the smallest distance of a pixel's weight exponents from the double underflow of
+ * exp (745.13); INFINITY where a choice is not made.  out_alt (may be NULL) [12][256]: the tile
+ * with every choice whose margin is above 0 and below near_tie taken the other way (the outputs'
+ * sensitivity to the near ties an FP32 evaluation may resolve differently; an exact tie comes
+ * from identical inputs and is resolved the same way). */
+void or_texture_tile_diag(const double *clt, const double *filter, int img_mask, const double *col_weights,
+                          double extra_disparity, const or_tex_params *tp, double *out, double *aux,
+                          double *diag, double *out_alt, double near_tie);
 /* or_texture_tile over tiles[n] of clt [tiles][4][3][256] on num_threads threads;
  * out [n][12][256], aux [n][16] (or NULL), extra [n] (or NULL) */
 int or_texture_tiles(const double *clt, const int *tiles, const int *img_mask, const double *extra, int n,

@@ -8,15 +8,20 @@ N(0, 1e-3) rad and target disparities off the truth by N(0, 0.2) px so the
 measured residual disparities d are not zero.
 
 Tolerances: port derivatives (FP64 on the device) to 1e-10 relative; the
-per-tile port sensitivities dd/dport to 2e-3 + 3% of the finite difference on
-95% of the samples; the loss gradient at 200 seeded coordinates to 3% of the
-finite difference on 95% of them.  Steps: 1e-4 for the tile disparities (as
-specified); 1e-6 rad for the extrinsics.  The forward is only piecewise
-smooth (integer window corners and the integer argmax switch), and 1e-4 rad
-moves every port of a sensor by ~0.04 px, switching the corners of ~8% of
-its sub-tiles: on this scene the central difference for sensor 0's azimuth
-is 9029 at 1e-4, 3821 at 1e-5 and 4242 at 3e-6 ... 3e-7, so only the small
-step measures the derivative.
+per-tile port sensitivities dd/dport to 2e-3 + 3% of the finite difference;
+the loss gradient at 200 seeded coordinates to 3% of the finite difference.
+Every sample is held to its tolerance except the ones whose central difference
+straddles a discontinuity of the forward, which the oracle lists: an integer
+window corner (-round(-px)), a tile's integer argmax, or a combined-strip
+sample clipped to zero (a pair's strip value + offset <= 0 zeroes the geometric
+mean, and a small change un-clips it: x^(1/n) has an infinite slope at 0) that
+differs between the + and the - evaluation.  The adjoint holds those fixed, so
+there the finite difference measures a jump, not the derivative.  Steps: 1e-4 for the tile
+disparities (as specified); 1e-6 rad for the extrinsics, because 1e-4 rad
+moves every port of a sensor by ~0.04 px and switches the corners of ~8% of
+its sub-tiles: on this scene the central difference for sensor 0's azimuth is
+9029 at 1e-4, 3821 at 1e-5 and 4242 at 3e-6 ... 3e-7, so only the small step
+measures the derivative.
 """
 import copy
 
@@ -52,12 +57,30 @@ def _gpu(sc, g, pairs, D):
     return tp
 
 
-def _oracle_d(O, sc, g, pairs, D, tile_op=None, ports_in=None):
+def _oracle_run(O, sc, g, pairs, D, tile_op=None, ports_in=None):
+    """(centroid disparity [T], integer window corners [T][S][1][2], integer argmax [T], clipped
+    combined-strip samples [T][rows * 15] (exactly 0 or NaN))"""
     op = np.ones(T, np.int32) if tile_op is None else tile_op
     P = O.make_pairs([(a, b, bx, by, kind) for (a, b, kind, _, bx, by) in pairs])
     r = O.run(W, H, sc["images"][:, None].astype(np.float64), op, np.asarray(D, np.float64),
-              geometry=None if ports_in is not None else g, ports_in=ports_in, pairs=P, want=("disp",))
-    return r["disp"][:, O.DISP_CM]
+              geometry=None if ports_in is not None else g, ports_in=ports_in, pairs=P,
+              want=("disp", "int_tl", "diag"))
+    rows = O.default_corr_params().corr_wndy_size  # the rows the centroid reads
+    combo = r["diag"][:, :15 * rows]
+    return r["disp"][:, O.DISP_CM], r["int_tl"], r["disp"][:, O.DISP_IXY], (combo == 0.0) | np.isnan(combo)
+
+
+def _oracle_d(O, sc, g, pairs, D, tile_op=None, ports_in=None):
+    return _oracle_run(O, sc, g, pairs, D, tile_op, ports_in)[0]
+
+
+def _switched(a, b, tiles=slice(None)):
+    """a discontinuity of the forward between two oracle evaluations: a window corner, an integer
+    argmax or a clipped combined-strip sample of one of the tiles differs"""
+    _, tl_a, ix_a, z_a = a
+    _, tl_b, ix_b, z_b = b
+    return (not np.array_equal(tl_a[tiles], tl_b[tiles])) or (
+        not np.array_equal(ix_a[tiles], ix_b[tiles], equal_nan=True)) or (not np.array_equal(z_a[tiles], z_b[tiles]))
 
 
 def test_port_derivatives_match_oracle(oracle):
@@ -99,15 +122,18 @@ def test_port_sensitivities_match_finite_differences(oracle):
             for ax in range(2):
                 pp = ports.copy()
                 pp[t, s, ax] += h
-                dp = _oracle_d(oracle, sc, g, pairs, D, op, pp)[tile]
+                rp = _oracle_run(oracle, sc, g, pairs, D, op, pp)
                 pp[t, s, ax] -= 2 * h
-                dm = _oracle_d(oracle, sc, g, pairs, D, op, pp)[tile]
-                fd = (dp - dm) / (2 * h)
-                errs.append((sens[tile, s, ax], fd))
-    e = np.array(errs)
-    bad = np.abs(e[:, 0] - e[:, 1]) > 2e-3 + 0.03 * np.abs(e[:, 1])
-    print("dd/dport: max |fd| %.3g, max err %.3g" % (np.abs(e[:, 1]).max(), np.abs(e[:, 0] - e[:, 1]).max()))
-    assert bad.mean() <= 0.05, e[bad]
+                rm = _oracle_run(oracle, sc, g, pairs, D, op, pp)
+                fd = (rp[0][tile] - rm[0][tile]) / (2 * h)
+                errs.append((sens[tile, s, ax], fd, _switched(rp, rm, tile)))
+    e = np.array([(a, b) for a, b, _ in errs])
+    sw = np.array([c for _, _, c in errs])
+    bad = (np.abs(e[:, 0] - e[:, 1]) > 2e-3 + 0.03 * np.abs(e[:, 1])) & ~sw
+    print("dd/dport: max |fd| %.3g, max err %.3g, %d of %d samples straddle a switch" % (
+        np.abs(e[:, 1]).max(), np.abs(e[~sw, 0] - e[~sw, 1]).max(), sw.sum(), len(sw)))
+    assert not bad.any(), e[bad]
+    assert sw.mean() <= 0.2
 
 
 def test_loss_gradient_matches_finite_differences(oracle):
@@ -124,8 +150,8 @@ def test_loss_gradient_matches_finite_differences(oracle):
     keys = ("azimuth", "tilt", "roll", "zoom")
     h, he = 1e-4, 1e-6
 
-    def loss(gg, DD):
-        d = _oracle_d(oracle, sc, gg, pairs, DD)
+    def loss(r):
+        d = r[0]
         return float(np.nansum(np.where(np.isfinite(d), d * d, 0.0)))
 
     rows = []
@@ -134,7 +160,8 @@ def test_loss_gradient_matches_finite_differences(oracle):
         gp, gm = copy.deepcopy(g), copy.deepcopy(g)
         gp[keys[k]][s] += he
         gm[keys[k]][s] -= he
-        rows.append(("e", ge[s, k], (loss(gp, D) - loss(gm, D)) / (2 * he)))
+        rp, rm = _oracle_run(oracle, sc, gp, pairs, D), _oracle_run(oracle, sc, gm, pairs, D)
+        rows.append(("e", ge[s, k], (loss(rp) - loss(rm)) / (2 * he), _switched(rp, rm)))
     valid = np.nonzero(np.isfinite(d0))[0]
     for t in rng.choice(valid, 160, replace=False):
         op = np.zeros(T, np.int32)
@@ -142,16 +169,22 @@ def test_loss_gradient_matches_finite_differences(oracle):
         Dp, Dm = D.astype(np.float64), D.astype(np.float64)
         Dp[t] += h
         Dm[t] -= h
-        dp = _oracle_d(oracle, sc, g, pairs, Dp, op)[t]
-        dm = _oracle_d(oracle, sc, g, pairs, Dm, op)[t]
-        rows.append(("d", gd[t], (dp * dp - dm * dm) / (2 * h)))
+        rp = _oracle_run(oracle, sc, g, pairs, Dp, op)
+        rm = _oracle_run(oracle, sc, g, pairs, Dm, op)
+        dp, dm = rp[0][t], rm[0][t]
+        rows.append(("d", gd[t], (dp * dp - dm * dm) / (2 * h), _switched(rp, rm, t)))
     got = np.array([r[1] for r in rows], np.float64)
     fd = np.array([r[2] for r in rows], np.float64)
-    scale = np.array([np.abs(fd[:40]).max()] * 40 + [np.abs(fd[40:]).max()] * 160)
+    sw = np.array([r[3] for r in rows])
+    held = ~sw
+    scale = np.array([np.abs(fd[:40][held[:40]]).max()] * 40 + [np.abs(fd[40:][held[40:]]).max()] * 160)
     rel = np.abs(got - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
-    print("loss gradient: extrinsic rel err median %.3g max %.3g; disparity median %.3g max %.3g" % (
-        np.median(rel[:40]), rel[:40].max(), np.median(rel[40:]), rel[40:].max()))
-    assert np.mean(rel <= 0.03) >= 0.95, np.sort(rel)[-12:]
+    print("loss gradient: extrinsic rel err median %.3g max %.3g (%d of 40 straddle a switch); disparity median "
+          "%.3g max %.3g (%d of 160)" % (np.median(rel[:40][held[:40]]), rel[:40][held[:40]].max(), sw[:40].sum(),
+                                       np.median(rel[40:][held[40:]]), rel[40:][held[40:]].max(), sw[40:].sum()))
+    bad = (rel > 0.03) & held
+    assert not bad.any(), [(i, rows[i][0], got[i], fd[i]) for i in np.nonzero(bad)[0]]
+    assert sw[:40].sum() <= 16 and sw[40:].sum() <= 16
 
 
 def test_recompute_mode_matches_stored_clt(oracle):

@@ -1,13 +1,26 @@
 """GPU texture tiles (ImageDtt.java:2662-2812) vs the FP64 oracle (needs a GB300).
 
 The oracle is fed the GPU's own CLT (so only the texture stage is compared) and,
-in the end-to-end case, its own CLT.  Tolerances: per tile and output row group,
-relative L2 <= 2e-5 for RGB and alpha, <= 1e-4 for the port weights (exp of a
-weighted squared difference divided by window^2), absolute <= 1e-3 x the tile's
-RGB scale for the rms rows (the oracle's s0*s2 - s1^2 loses digits the GPU's
-centred sum keeps); the best-pair choice may flip on exact near-ties, so 99.5%
-of tiles must meet the bounds and every tile must meet 10x them.  Pixels where
-the FP64 reference's weights underflow (0/0 -> NaN) must be NaN on the GPU too.
+in the end-to-end case, its own CLT.  Tolerances per tile: relative L2 <= 2e-5
+for RGB and alpha, <= 1e-4 for the port weights (exp of a weighted squared
+difference divided by window^2), absolute <= 1e-3 x the tile's RGB scale for the
+rms rows (the oracle's s0*s2 - s1^2 loses digits the GPU's centred sum keeps),
+<= 1e-4 of the tile's scale for max_diff and 1e-5 for ports_rgb, and the same
+NaN pattern (the FP64 reference's weights underflow to 0/0 -> NaN where every
+weight exponent exceeds 745.13; the GPU reproduces it).
+
+The texture stage makes discrete per-pixel choices (the second port of the best
+pair against the next port, dust_remove's weakest port) on weights that FP32
+computes to about 1e-6 relative (an exponent argument of tens carries ~6e-8 relative error each), so a choice whose FP64 margin is below
+TIE_RES = 1e-5 may go either way.  The oracle evaluates each tile both ways
+(oracle.texture_tile(..., diag=True): every such near tie taken the other way).
+Every tile must meet the bounds against the reference in which each output
+element is the closer of the two resolutions -- for a tile without such ties
+that is the oracle's own output.  max_diff is checked on the tiles without
+such ties, and tiles in which a pixel's weight exponents come within UF_MARGIN
+of the double underflow of exp (745.13: FP32 may land on the other side of it)
+compare the elements that are finite in both.  The tiles with ties are counted
+and printed.
 """
 import numpy as np
 import pytest
@@ -26,10 +39,14 @@ def _col_weights(corr_red=0.5, corr_blue=0.2):
     return np.array([corr_red * g, corr_blue * g, g])
 
 
+UF_MARGIN = 0.05
+TIE_RES = 1e-5
+
+
 def _oracle_textures(O, clt, disp, tile_op, tiles, extra_slot=None, params=None, **kw):
     lpf = O.corr_lpf(0.8)
     cw = _col_weights()
-    outs, auxs = [], []
+    outs, auxs, diags, alts = [], [], [], []
     for t in tiles:
         op = int(tile_op[t])
         extra = 0.0
@@ -37,36 +54,49 @@ def _oracle_textures(O, clt, disp, tile_op, tiles, extra_slot=None, params=None,
             extra = float(disp[t, extra_slot])
             if not np.isfinite(extra):
                 extra = 0.0
-        o, a = O.texture_tile(clt[t], lpf, op & 0xF, cw, extra, params or O.texture_params(**kw))
+        o, a, dg, alt = O.texture_tile(clt[t], lpf, op & 0xF, cw, extra, params or O.texture_params(**kw),
+                                       diag=True, near_tie=TIE_RES)
         outs.append(o)
         auxs.append(a)
-    return np.array(outs), np.array(auxs)
+        diags.append(dg)
+        alts.append(alt)
+    return np.array(outs), np.array(auxs), np.array(diags), np.array(alts)
 
 
-def _compare(got, aux, want, want_aux, frac=0.995):
+def _compare(got, aux, want, want_aux, diag, alt, rows=12):
     n = len(got)
-    # NaN where the FP64 reference's weights underflow to 0/0 must be NaN on the GPU too
-    nan_g, nan_w = np.isnan(got[:, :8]), np.isnan(want[:, :8])
-    assert (nan_g != nan_w).mean() <= 1e-4, "NaN pattern differs at %d values" % (nan_g != nan_w).sum()
+    tied = ~np.all(np.isclose(np.nan_to_num(alt[:, :8]), np.nan_to_num(want[:, :8]), rtol=0, atol=0), axis=(1, 2))
+    uflow = diag[:, 2] < UF_MARGIN
+    # the reference: each element the closer of the two tie resolutions (the oracle's own where none)
+    k = min(rows, 8)
+    want = want.copy()
+    closer = np.abs(np.nan_to_num(got[:, :k] - alt[:, :k])) < np.abs(np.nan_to_num(got[:, :k] - want[:, :k]))
+    want[:, :k] = np.where(closer, alt[:, :k], want[:, :k])
+    nan_g, nan_w = np.isnan(got[:, :min(rows, 8)]), np.isnan(want[:, :min(rows, 8)])
+    nan_bad = (nan_g != nan_w).reshape(n, -1).any(axis=-1) & ~uflow
     both = nan_g | nan_w
-    g8 = np.where(both, 0.0, got[:, :8])
-    w8 = np.where(both, 0.0, want[:, :8])
+    g8 = np.where(both, 0.0, got[:, :min(rows, 8)])
+    w8 = np.where(both, 0.0, want[:, :min(rows, 8)])
     e_rgb = rel_l2(g8[:, 0:3].reshape(n, -1), w8[:, 0:3].reshape(n, -1), axis=-1)
     e_a = rel_l2(g8[:, 3], w8[:, 3], axis=-1)
-    e_w = rel_l2(g8[:, 4:8].reshape(n, -1), w8[:, 4:8].reshape(n, -1), axis=-1)
-    scale = np.abs(w8[:, 0:3]).reshape(n, -1).max(axis=-1)
-    rms_d = np.where(np.isnan(want[:, 8:12]), 0.0, np.abs(got[:, 8:12] - want[:, 8:12]))
-    e_r = rms_d.reshape(n, -1).max(axis=-1) / np.maximum(scale, 1e-30)
-    good = (e_rgb <= RGB_TOL) & (e_a <= RGB_TOL) & (e_w <= W_TOL) & (e_r <= 1e-3)
-    msg = "rgb %.3g alpha %.3g weights %.3g rms %.3g (max), good %.4f, NaN values %d" % (
-        e_rgb.max(), e_a.max(), e_w.max(), e_r.max(), good.mean(), nan_w.sum())
-    assert good.mean() >= frac, msg
-    assert e_rgb.max() <= 10 * RGB_TOL and e_a.max() <= 10 * RGB_TOL and e_w.max() <= 10 * W_TOL, msg
-    # max_diff and ports_rgb
-    e_md = np.abs(aux[:, :4] - want_aux[:, :4]) / np.maximum(np.abs(want_aux[:, :4]).max(), 1e-30)
-    e_pr = np.abs(aux[:, 4:] - want_aux[:, 4:]) / np.maximum(np.abs(want_aux[:, 4:]).max(), 1e-30)
-    assert np.quantile(e_md, frac) <= 1e-4 and e_pr.max() <= 1e-5, "max_diff %.3g ports_rgb %.3g" % (
-        e_md.max(), e_pr.max())
+    bad = nan_bad | (e_rgb > RGB_TOL) | (e_a > RGB_TOL)
+    e_w = e_r = np.zeros(n)
+    if rows > 4:
+        e_w = rel_l2(g8[:, 4:8].reshape(n, -1), w8[:, 4:8].reshape(n, -1), axis=-1)
+        scale = np.abs(w8[:, 0:3]).reshape(n, -1).max(axis=-1)
+        rms_d = np.where(np.isnan(want[:, 8:12]), 0.0, np.abs(got[:, 8:12] - want[:, 8:12]))
+        e_r = rms_d.reshape(n, -1).max(axis=-1) / np.maximum(scale, 1e-30)
+        bad |= (e_w > W_TOL) | (e_r > 1e-3)
+    if aux is not None:
+        e_md = (np.abs(aux[:, :4] - want_aux[:, :4]) / np.maximum(np.abs(want_aux[:, :4]).max(), 1e-30)).max(axis=-1)
+        e_pr = (np.abs(aux[:, 4:] - want_aux[:, 4:]) / np.maximum(np.abs(want_aux[:, 4:]).max(), 1e-30)).max(axis=-1)
+        bad |= ((e_md > 1e-4) & ~tied) | (e_pr > 1e-5)
+    msg = "%d tiles: rgb %.3g alpha %.3g weights %.3g rms %.3g (max); %d with near ties, %d at the underflow" % (
+        n, np.nanmax(e_rgb), np.nanmax(e_a), np.nanmax(e_w), np.nanmax(e_r), tied.sum(), uflow.sum())
+    fails = np.nonzero(bad)[0]
+    assert len(fails) == 0, "%d tiles out of tolerance %s (rgb %s, alpha %s, weights %s, near ties %s); %s" % (
+        len(fails), fails[:6].tolist(), e_rgb[fails[:6]].tolist(), e_a[fails[:6]].tolist(), e_w[fails[:6]].tolist(),
+        tied[fails[:6]].tolist(), msg)
     return msg
 
 
@@ -100,8 +130,8 @@ def test_textures_on_gpu_clt(oracle):
         clt = tp.getClt().astype(np.float64)
         d = tp.getDisparity().astype(np.float64)
     tiles = np.nonzero(ops)[0]
-    want, want_aux = _oracle_textures(oracle, clt, d, ops, tiles, extra_slot=oracle.DISP_CM)
-    print(_compare(got[tiles], aux[tiles], want, want_aux))
+    want, want_aux, diag, alt = _oracle_textures(oracle, clt, d, ops, tiles, extra_slot=oracle.DISP_CM)
+    print(_compare(got[tiles], aux[tiles], want, want_aux, diag, alt))
 
 
 def test_textures_poly_shift_after_lma(oracle):
@@ -130,9 +160,9 @@ def test_textures_poly_shift_after_lma(oracle):
     tiles = np.nonzero(ops)[0]
     shifted = tiles[np.isfinite(lma[tiles, 0]) & (lma[tiles, 0] != 0) & ((ops[tiles] & 0x100) == 0)]
     assert len(shifted) > 0.5 * len(tiles)
-    want, want_aux = _oracle_textures(oracle, clt, lma, ops, tiles, extra_slot=0)
-    print(_compare(got[tiles], aux[tiles], want, want_aux))
-    want0, _ = _oracle_textures(oracle, clt, lma, ops, tiles)
+    want, want_aux, diag, alt = _oracle_textures(oracle, clt, lma, ops, tiles, extra_slot=0)
+    print(_compare(got[tiles], aux[tiles], want, want_aux, diag, alt))
+    want0, _, _, _ = _oracle_textures(oracle, clt, lma, ops, tiles)
     g0 = np.nan_to_num(got0[tiles, :4])
     assert np.allclose(g0, np.nan_to_num(want0[:, :4]), rtol=1e-3, atol=1e-3 * np.abs(g0).max())
 
@@ -154,8 +184,8 @@ def test_textures_end_to_end(oracle):
         got = tp.getTextures().astype(np.float64)
         aux = tp.getTextureAux().astype(np.float64)
     tiles = np.nonzero(ops)[0]
-    want, want_aux = _oracle_textures(oracle, ref["clt"], ref["disp"], ops, tiles)
-    print(_compare(got[tiles], aux[tiles], want, want_aux))
+    want, want_aux, diag, alt = _oracle_textures(oracle, ref["clt"], ref["disp"], ops, tiles)
+    print(_compare(got[tiles], aux[tiles], want, want_aux, diag, alt))
 
 
 def test_textures_rgba_only_and_no_shot(oracle):
@@ -174,12 +204,8 @@ def test_textures_rgba_only_and_no_shot(oracle):
         d = tp.getDisparity().astype(np.float64)
     assert got.shape[1] == 4
     tiles = np.arange(T)
-    want, _ = _oracle_textures(oracle, clt, d, ops, tiles, scale_shot=0.0, dust_remove=0)
-    bad = np.isnan(got[:, :4]) | np.isnan(want[:, :4])
-    assert (np.isnan(got[:, :4]) != np.isnan(want[:, :4])).mean() <= 1e-4
-    g, wv = np.where(bad, 0.0, got[:, :4]), np.where(bad, 0.0, want[:, :4])
-    e = rel_l2(g.reshape(T, -1), wv.reshape(T, -1), axis=-1)
-    assert np.mean(e <= RGB_TOL) >= 0.995 and e.max() <= 10 * RGB_TOL, "rgba rel L2 max %.3g" % e.max()
+    want, _, diag, alt = _oracle_textures(oracle, clt, d, ops, tiles, scale_shot=0.0, dust_remove=0)
+    print(_compare(got, None, want, None, diag, alt, rows=4))
 
 
 def test_textures_reject_mono(oracle):
