@@ -148,6 +148,27 @@ __device__ __forceinline__ void conv_shift(float o[4][8], const float *kp, float
   }
 }
 
+// the stored CLT of row r (horizontal frequency r) of the four quadrants; with the colour's bit
+// in clt_lpf_mask multiplied by the LPF, as the reference GPU stores it (lpf_mask,
+// TileProcessor.cuh:1037-1061, GPUTileProcessor.java:547); the correlation keeps the unfiltered copy
+__device__ __forceinline__ void store_clt(const SceneDev &sc, int c, int r, float *gdst, const float o[4][8]) {
+  if (sc.lpf_rbg && ((sc.clt_lpf_mask >> c) & 1)) {
+    const float4 *lp = (const float4 *)(sc.lpf_rbg + c * 64 + r * 8);
+    const float4 la = __ldg(lp), lb = __ldg(lp + 1);
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      *(float4 *)(gdst + m * 64) = make_float4(o[m][0] * la.x, o[m][1] * la.y, o[m][2] * la.z, o[m][3] * la.w);
+      *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4] * lb.x, o[m][5] * lb.y, o[m][6] * lb.z, o[m][7] * lb.w);
+    }
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
+    *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
+  }
+}
+
 struct FwdShape {
   int nw;                 // warps per CTA (each warp owns whole tiles)
   int S, C, P, RE, quad;  // sensors, colours, pairs, strip entries, quad layout
@@ -198,12 +219,7 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
   const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
   conv_shift(o, kp, p.rx, p.ry, r);
   if (act) {
-    float *gdst = sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
-      *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
-    }
+    store_clt(sc, c, r, sc.clt + ((tile * S + s) * C + c) * TP_CLT + r * 8, o);
     // all four quadrants: after the convolution and the shift the Bayer symmetries no longer hold
     float *sdst = s_clt + ((size_t)s * C + c) * TP_CLT + r * 8;
 #pragma unroll
@@ -621,12 +637,7 @@ __device__ __forceinline__ void fwd_clt_item_win(const SceneDev &sc, const uint1
   const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
   conv_shift(o, kp, p.rx, p.ry, r);
   if (act) {
-    float *gdst = sc.clt + ((tile * S + q) * 3 + c) * TP_CLT + r * 8;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      *(float4 *)(gdst + m * 64) = make_float4(o[m][0], o[m][1], o[m][2], o[m][3]);
-      *(float4 *)(gdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
-    }
+    store_clt(sc, c, r, sc.clt + ((tile * S + q) * 3 + c) * TP_CLT + r * 8, o);
     float *sdst = s_clt + ((size_t)q * 3 + c) * TP_CLT + r * 8;
 #pragma unroll
     for (int m = 0; m < 4; m++) {
@@ -1081,7 +1092,8 @@ __global__ void __launch_bounds__(32 * IMCLT_WARPS) imclt_fast_kernel(const __gr
   for (int i = threadIdx.x; i < IPX * ISTR; i += blockDim.x) acc[i] = 0.f;
   __syncthreads();
   float *tbuf = tbuf_all[warp] + q * 72;
-  const float *lpf = sc.lpf_rbg ? sc.lpf_rbg + c * 64 : nullptr;
+  // (a stored CLT that already carries the LPF, clt_lpf_mask, is not filtered again)
+  const float *lpf = (sc.lpf_rbg && !((sc.clt_lpf_mask >> c) & 1)) ? sc.lpf_rbg + c * 64 : nullptr;
   // unfold rows fed by source row r (DttRad2.get_unfold_index_signs, 392-404)
   const int i1 = (r >= 4) ? r - 4 : 11 - r, i2 = (r >= 4) ? 11 - r : r + 12;
   const float sa1 = (r >= 4) ? 1.f : -1.f, sb1 = 1.f;    // signs (cos, sin branch) of row i1

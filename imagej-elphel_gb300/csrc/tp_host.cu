@@ -72,6 +72,7 @@ struct tp_handle {
   int have_geometry = 0, have_tasks = 0, have_corr = 0, lpf_on = 0, planned = 0;
   int num_pairs = 0, corr_capacity = 0;
   int sched_tpb = 0, sched_nw = 0;  // fused-kernel schedule (0 = defaults)
+  int clt_lpf_mask = 0;             // colours whose stored CLT carries the tp_set_lpf filter
   float color_scale[3] = {1.f, 1.f, 1.f};
   GeomDev geom_host;
   CorrDev corr_host;
@@ -188,6 +189,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.disp = h->d_disp;
   sc.rbg = h->d_rbg;
   sc.lpf_rbg = h->lpf_on ? h->d_lpf_rbg : nullptr;
+  sc.clt_lpf_mask = h->lpf_on ? h->clt_lpf_mask : 0;
   sc.corr_cfg = h->d_corr_cfg;
   sc.combo = h->d_combo;
   sc.strips = (h->adj_record && h->d_strips && strips_need(h) <= h->strips_cap) ? h->d_strips : nullptr;
@@ -776,6 +778,18 @@ tp_status tp_set_lpf(tp_handle *h, const float *lpf) {
   return TP_OK;
 }
 
+tp_status tp_set_clt_lpf_mask(tp_handle *h, int lpf_mask) {
+  if (!h) return TP_ERR_ARG;
+  if (lpf_mask < 0 || (lpf_mask >> h->cfg.num_colors) != 0)
+    return fail(h, TP_ERR_ARG, "tp_set_clt_lpf_mask: one bit per colour");
+  h->clt_lpf_mask = lpf_mask;
+  h->fwd_valid = 0;
+  return TP_OK;
+}
+
+// the passes that read the stored CLT expect it unfiltered
+static bool clt_filtered(const tp_handle *h) { return h->lpf_on && h->clt_lpf_mask; }
+
 tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int np) {
   if (h) h->fwd_valid = 0;
   if (!h || !p || (!pairs && np > 0)) return TP_ERR_ARG;
@@ -905,6 +919,7 @@ tp_status tp_convert_correct(tp_handle *h, void *stream) {
 tp_status tp_correlate(tp_handle *h, void *stream) {
   if (!h) return TP_ERR_ARG;
   if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_correlate: no pairs set");
+  if (clt_filtered(h)) return fail(h, TP_ERR_STATE, "tp_correlate: the stored CLT is low-pass filtered (tp_set_clt_lpf_mask)");
   cudaStream_t st = pick_stream(h, stream);
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
@@ -953,6 +968,7 @@ tp_status tp_textures(tp_handle *h, void *stream) {
   if (h->cfg.num_sensors != 4 || h->cfg.num_colors != 3)
     return fail(h, TP_ERR_ARG, "tp_textures: texture tiles need 4 sensors x 3 colours");
   if (!h->have_corr) return fail(h, TP_ERR_STATE, "tp_textures: correlation set-up (LPF, colour weights) missing");
+  if (clt_filtered(h)) return fail(h, TP_ERR_STATE, "tp_textures: the stored CLT is low-pass filtered (tp_set_clt_lpf_mask)");
   cudaStream_t st = pick_stream(h, stream);
   tp_status r = ensure_plan(h, st);
   if (r != TP_OK) return r;
@@ -1503,6 +1519,8 @@ tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_norma
   if (!h->have_corr) return fail(h, TP_ERR_STATE, "tp_rig_correlate: main camera has no correlation set-up");
   if (!h->fwd_valid || !aux->fwd_valid)
     return fail(h, TP_ERR_STATE, "tp_rig_correlate: run tp_process on both cameras first");
+  if (clt_filtered(h) || clt_filtered(aux))
+    return fail(h, TP_ERR_STATE, "tp_rig_correlate: a stored CLT is low-pass filtered (tp_set_clt_lpf_mask)");
   cudaStream_t st = pick_stream(h, stream);
   if (!h->d_rig_corr) {
     if (dalloc(h, &h->d_rig_corr, (size_t)h->ntiles * TP_CORR) != cudaSuccess ||
@@ -1574,6 +1592,8 @@ tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, floa
     return fail(h, TP_ERR_STATE, "tp_backward: not for a rig's auxiliary camera (its disparities are the main camera's)");
   if (!h->fwd_valid || h->num_pairs == 0)
     return fail(h, TP_ERR_STATE, "tp_backward: run tp_process (with correlation pairs) first");
+  if (clt_filtered(h) && !h->adj_recompute)
+    return fail(h, TP_ERR_STATE, "tp_backward: the stored CLT is low-pass filtered (tp_set_clt_lpf_mask)");
   if (h->adj_recompute && h->images_since_fwd)
     return fail(h, TP_ERR_STATE, "tp_backward: the CLT recompute reads the images, which changed since tp_process");
   cudaStream_t st = pick_stream(h, stream);

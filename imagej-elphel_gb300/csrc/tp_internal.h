@@ -106,6 +106,7 @@ struct SceneDev {
   float *disp;               // [tiles][TP_NDISP]
   float *rbg;                // [S][C][H+8][W+8]
   const float *lpf_rbg;      // [C][64] or null
+  int clt_lpf_mask;          // colours whose stored CLT is multiplied by lpf_rbg (the reference GPU's lpf_mask)
   const CorrDev *corr_cfg;
   float *combo;              // [tiles][RE] combined strip rows the extraction reads, or null
   float *strips;             // [tiles][pairs][RE] per-pair strip samples (adjoint input), or null

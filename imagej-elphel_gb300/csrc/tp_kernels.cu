@@ -237,10 +237,13 @@ __global__ void __launch_bounds__(CC_WARPS * 32) convert_correct_kernel(SceneDev
     int txy = sc.task_txy[task];
     size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
     float *dst = sc.clt + ((tile * S + s) * C + c) * TP_CLT;
+    // the reference GPU's lpf_mask (TileProcessor.cuh:1037-1061): the stored CLT times the LPF
+    const bool lp = sc.lpf_rbg && ((sc.clt_lpf_mask >> c) & 1);
+    const float l0 = lp ? sc.lpf_rbg[c * 64 + lane] : 1.f, l1 = lp ? sc.lpf_rbg[c * 64 + lane + 32] : 1.f;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      dst[q * 64 + lane] = o[q][0];
-      dst[q * 64 + lane + 32] = o[q][1];
+      dst[q * 64 + lane] = o[q][0] * l0;
+      dst[q * 64 + lane + 32] = o[q][1] * l1;
     }
   }
 }
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(IM_WARPS * 32) imclt_kernel(SceneDev sc) {
   for (int i = threadIdx.x; i < IM_PX * IM_STRIDE; i += blockDim.x) acc[i] = 0.f;
   __syncthreads();
   float *b1 = wbuf[warp], *b2 = b1 + QBUF;
-  const float *lpf = sc.lpf_rbg ? sc.lpf_rbg + c * 64 : nullptr;
+  const float *lpf = (sc.lpf_rbg && !((sc.clt_lpf_mask >> c) & 1)) ? sc.lpf_rbg + c * 64 : nullptr;
   // tiles touching the region: tx in [bx0-1, bx0+IM_REG-1]
   for (int ph = 0; ph < 4; ph++) {
     const int px_ = ph & 1, py_ = ph >> 1;

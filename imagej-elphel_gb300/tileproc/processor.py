@@ -190,6 +190,11 @@ class GPUTileProcessor:
         l = np.ascontiguousarray(lpf, dtype=np.float32).reshape(self.num_colors, 64)
         self._ck(self._lib.tp_set_lpf(self.h, _ptr(l)), "tp_set_lpf")
 
+    def setCltLpfMask(self, lpf_mask=7):
+        """Store the CLT low-pass filtered as GPUTileProcessor.execConverCorrectTiles does (its
+        lpf_mask = 7, GPUTileProcessor.java:547), with the filter of setLpfRbg; 0 = unfiltered."""
+        self._ck(self._lib.tp_set_clt_lpf_mask(self.h, int(lpf_mask)), "tp_set_clt_lpf_mask")
+
     def setCorrelation(self, params=None, pairs=None, **kw):
         """params: TpCorrParams or None (reference defaults, overridable by keyword)."""
         if params is None:

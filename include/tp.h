@@ -224,6 +224,17 @@ tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_de
 tp_status tp_get_kernels(tp_handle *h, int cam, float *kernels, float *kernel_offsets);
 /* setLpfRbg (GPUTileProcessor.java:780-812): lpf[num_colors][64] applied by tp_imclt; NULL = off */
 tp_status tp_set_lpf(tp_handle *h, const float *lpf);
+/* execConverCorrectTiles stores a low-pass filtered CLT: it passes lpf_mask = 7
+ * (GPUTileProcessor.java:547) and convertCorrectTile multiplies the CLT of every colour whose bit
+ * is set by that colour's LPF (TileProcessor.cuh:1037-1061).  With a mask set here, the CLT stored
+ * by tp_process / tp_convert_correct (tp_get_clt, and what tp_imclt reads) carries the filter of
+ * tp_set_lpf for those colours the same way, and tp_imclt does not apply it again, so the RBG
+ * frames are unchanged.  The correlation of tp_process still uses the unfiltered CLT (the CPU
+ * path's semantics); tp_correlate, tp_textures, tp_rig_correlate and tp_backward (unless it
+ * recomputes the CLT) read the stored CLT and return TP_ERR_STATE while a mask is in effect.
+ * One bit per colour (0..2^num_colors - 1); default 0 (the CPU path's unfiltered CLT); it takes
+ * effect only while tp_set_lpf has a filter set. */
+tp_status tp_set_clt_lpf_mask(tp_handle *h, int lpf_mask);
 /* correlation set-up (ImageDtt.clt_aberrations_quad_corr_new arguments, ImageDtt.java:1491-1546) */
 tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int num_pairs);
 /* texture set-up; the LPF and colour weights are those of tp_set_corr */

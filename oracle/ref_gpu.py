@@ -36,6 +36,15 @@ class RefGpu:
         if r != 0:
             raise RuntimeError("%s failed: CUresult %d" % (what, r))
 
+    def get_global(self, name, count):
+        """a float32 __constant__ / __device__ array of the module (e.g. lpf_data [3][64])"""
+        ptr = C.c_uint64()
+        size = C.c_size_t()
+        self._ck(self.cu.cuModuleGetGlobal_v2(C.byref(ptr), C.byref(size), self.mod, name.encode()), "getglobal")
+        out = np.zeros(count, np.float32)
+        self._ck(self.cu.cuMemcpyDtoH_v2(out.ctypes.data_as(C.c_void_p), ptr, C.c_size_t(count * 4)), "dtoh")
+        return out
+
     def _launch(self, fn, grid, block, args):
         holders = []
         ptrs = (C.c_void_p * len(args))()

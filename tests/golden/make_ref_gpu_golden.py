@@ -14,6 +14,13 @@ so that no window corner or kernel index sits within 2e-3 of a rounding tie
 (the reference GPU rounds with floorf(x+0.5f)/lrintf in FP32, the CPU path
 with Math.round in FP64).  Saved: the inputs, the reference GPU CLT of the
 tasked tiles and the reference imclt_rbg frames (lpf_mask = 0).
+
+    python tests/golden/make_ref_gpu_golden.py OUT.npz --lpf
+
+writes the same inputs with the CLT of lpf_mask = 7, the mask GPUTileProcessor.
+execConverCorrectTiles passes (GPUTileProcessor.java:547): each colour's stored
+CLT multiplied by the module's lpf_data table (TileProcessor.cuh:1037-1061),
+which is saved too.
 """
 import os
 import sys
@@ -72,13 +79,23 @@ def make_inputs(seed=2024):
                 tasks=tasks, tx=txs, ty=tys, xy=xy)
 
 
-def main(out):
+def main(out, lpf=False):
     from oracle import build_ref_gpu
     from oracle.ref_gpu import RefGpu
     inp = make_inputs()
     # setConvolutionKernels uploads each 8x8 quadrant transposed (GPUTileProcessor.java:406-410)
     kg = inp["kernels"].reshape(4, KV, KH, 3, 4, 8, 8).swapaxes(-1, -2).reshape(4, KV, KH, 3, 4, 64)
     ref = RefGpu(build_ref_gpu.cubin_path(W, H), W, H)
+    if lpf:
+        clt, rbg = ref.run(inp["mosaics"], kg, inp["kext"], inp["tasks"], lpf_mask=7)
+        ref_clt = clt[:, inp["ty"], inp["tx"]]
+        np.savez_compressed(out, mosaic_u16=inp["mosaic_u16"], kernels_f16=inp["kernels"].astype(np.float16),
+                            kext=inp["kext"], tasks=inp["tasks"], ref_clt=np.ascontiguousarray(ref_clt.swapaxes(0, 1)),
+                            lpf_data=ref.get_global("lpf_data", 3 * 64).reshape(3, 64), width=W, height=H,
+                            bayer=np.array([0, 1]), lpf_mask=7,
+                            note="reference convert_correct_tiles (TileProcessor.cuh) compiled for sm_103a, lpf_mask 7")
+        print("wrote", out, "tasks", len(inp["tx"]), "clt absmax", np.abs(ref_clt).max())
+        return
     clt, rbg = ref.run(inp["mosaics"], kg, inp["kext"], inp["tasks"])
     ref_clt = clt[:, inp["ty"], inp["tx"]]  # [4][n][3][4][64]
     np.savez_compressed(out, mosaic_u16=inp["mosaic_u16"], kernels_f16=inp["kernels"].astype(np.float16),
@@ -89,4 +106,5 @@ def main(out):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "ref_gpu_128x96.npz")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else "ref_gpu_128x96.npz", lpf="--lpf" in sys.argv)

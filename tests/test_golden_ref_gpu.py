@@ -111,3 +111,63 @@ def test_gb300_matches_reference_gpu(oracle, tp_lib):
             ref_rbg = g["ref_rbg"][cam].astype(np.float64)
             err = np.abs(rbg - ref_rbg)[..., mask].max() / np.abs(ref_rbg).max()
             assert err < TOL, "cam %d IMCLT vs reference imclt_rbg rel err %.3g" % (cam, err)
+
+
+GOLD_LPF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu_128x96_lpf.npz")
+
+
+def test_oracle_matches_reference_gpu_clt_lpf(oracle):
+    """The reference convert_correct_tiles with lpf_mask = 7: the oracle's CLT times the module's
+    lpf_data table (elementwise; the table is symmetric, so its orientation is the CLT's)."""
+    if not os.path.exists(GOLD_LPF):
+        pytest.skip("golden file not generated")
+    g, W, H = _load()
+    gl = dict(np.load(GOLD_LPF))
+    lpf = gl["lpf_data"].astype(np.float64)  # [3][64]
+    want = _oracle_clt(oracle, g, W, H) * lpf[None, None, :, None, :]
+    got = gl["ref_clt"].astype(np.float64)
+    got = got.reshape(got.shape[:-1] + (8, 8)).swapaxes(-1, -2).reshape(got.shape)
+    e = np.sqrt(((got - want) ** 2).sum((-2, -1)) / (want ** 2).sum((-2, -1)))
+    assert e.max() < TOL, "reference GPU low-pass CLT vs oracle rel L2 max %.3g" % e.max()
+
+
+@pytest.mark.gpu
+def test_gb300_lpf_mask_matches_reference_gpu(oracle, tp_lib):
+    """The stored CLT with the reference GPU's lpf_mask = 7 (tp_set_clt_lpf_mask) and its lpf_data
+    table set through tp_set_lpf, against the reference convert_correct_tiles run with that mask;
+    the IMCLT frames do not change (the filter is not applied twice)."""
+    if not os.path.exists(GOLD_LPF):
+        pytest.skip("golden file not generated")
+    g, W, H = _load()
+    gl = dict(np.load(GOLD_LPF))
+    assert np.array_equal(gl["tasks"], g["tasks"])
+    from tileproc import GPUTileProcessor, _lib
+    kv, kh = g["kernels"].shape[1:3]
+    # the module's table is symmetric in its two frequency indices, so its orientation is the CLT's
+    lpf = gl["lpf_data"].astype(np.float32)
+    assert np.array_equal(lpf.reshape(3, 8, 8), lpf.reshape(3, 8, 8).swapaxes(-1, -2))
+    with GPUTileProcessor(4, W, H, num_colors=3, kernels_hor=kh, kernels_vert=kv) as tp:
+        tp.setColorScales([1.0, 1.0, 0.5])
+        tp.setBayerImages(g["mosaic_u16"])
+        tp.setConvolutionKernels(g["kernels"], g["kext"], layout=_lib.TP_KERNELS_CPU)
+        tp.setTasks(g["tasks"])
+        tp.setCorrelation()
+        tp.setLpfRbg(lpf)
+        tp.process()
+        tp.execImcltRbg()
+        rbg0 = [tp.getRBG(cam) for cam in range(4)]
+        corr0 = tp.getCorr()
+        tp.setCltLpfMask(7)
+        tp.process()
+        tp.execImcltRbg()
+        tiles = g["ty"] * (W // 8) + g["tx"]
+        got = tp.getClt()[tiles].astype(np.float64)
+        ref = gl["ref_clt"].astype(np.float64)
+        ref = ref.reshape(ref.shape[:-1] + (8, 8)).swapaxes(-1, -2).reshape(ref.shape)
+        e = np.sqrt(((got - ref) ** 2).sum((-2, -1)) / (ref ** 2).sum((-2, -1)))
+        assert e.max() < TOL, "GB300 vs reference GPU low-pass CLT rel L2 max %.3g" % e.max()
+        for cam in range(4):
+            assert np.allclose(tp.getRBG(cam), rbg0[cam], rtol=1e-5, atol=1e-5 * np.abs(rbg0[cam]).max())
+        assert np.array_equal(tp.getCorr(), corr0)  # the correlation reads the unfiltered CLT
+        with pytest.raises(_lib.TpError):
+            tp.execTextures()
