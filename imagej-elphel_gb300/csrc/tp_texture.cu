@@ -37,43 +37,81 @@ __constant__ float k_port_off[4][2] = {{-0.5f, -0.5f}, {0.5f, -0.5f}, {-0.5f, 0.
 
 }  // namespace
 
+// square root from the reciprocal square root (about 2 ulp; 0 at 0): for the rms rows, whose
+// tolerance is far wider than the IEEE root's accuracy
+__device__ __forceinline__ float sqrt_approx(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
+// tile_debayer (ImageDtt.java:3047-3147) of two vertically adjacent pixels (y0, x), (y0 + 1, x):
+// 3x3 stencil over the un-windowed tile (zero outside), the taps outside the tile dropped and the
+// sum renormalised (k_corn / k_side edge factors); kern_rb = (1 2 1)^T (1 2 1) / 16 is separable,
+// so the row sums of rows y0 - 1 .. y0 + 2 serve both pixels; then the shot-noise correction
+// (tile_debayer_shot_corr, 3022-3045) and the window
+__device__ __forceinline__ void debayer2(const TexConst &tc, float (*s_ic)[TX_P * TX_P], const float *s_win2, int x,
+                                         int y0, float d[2][4][3], float part[16]) {
+  const int p = (y0 + 1) * TX_P + x + 1;
+  const bool ex = (x == 0) || (x == 15);
+  float f_rb[2], f_g[2], lw[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int y = y0 + k;
+    const bool ey = (y == 0) || (y == 15);
+    f_rb[k] = (ey && ex) ? (16.0f / 9.0f) : ((ey || ex) ? (4.0f / 3.0f) : 1.0f);
+    f_g[k] = (ey && ex) ? (4.0f / 3.0f) : ((ey || ex) ? (8.0f / 7.0f) : 1.0f);
+    lw[k] = s_win2[y * 16 + x];
+  }
+#pragma unroll
+  for (int ip = 0; ip < 4; ip++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float *u = s_ic[ip * 3 + c] + p;  // pixel (y0, x)
+      float acc[2];
+      if (c != 2) {  // kern_rb
+        float h[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float *row = u + (k - 1) * TX_P;
+          h[k] = fmaf(2.0f, row[0], row[-1] + row[1]);
+        }
+        acc[0] = 0.0625f * fmaf(2.0f, h[1], h[0] + h[2]);
+        acc[1] = 0.0625f * fmaf(2.0f, h[2], h[1] + h[3]);
+      } else {       // kern_g: sides 1/8, centre 1/2
+        const float v0 = u[-TX_P], v1 = u[0], v2 = u[TX_P], v3 = u[2 * TX_P];
+        acc[0] = fmaf(0.125f, (v0 + u[-1]) + (u[1] + v2), 0.5f * v1);
+        acc[1] = fmaf(0.125f, (v1 + u[TX_P - 1]) + (u[TX_P + 1] + v3), 0.5f * v2);
+      }
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        float a = acc[k] * ((c != 2) ? f_rb[k] : f_g[k]);
+        if (tc.scale_shot > 0.f)
+          a = tc.scale_shot * ((a > tc.min_shot) ? a * rsqrtf(a) : (tc.rsqrt_min_shot * a));
+        d[k][ip][c] = a * lw[k];
+        part[4 + c * 4 + ip] += d[k][ip][c];
+      }
+    }
+}
+
 // Per-pixel stage of a tile (debayer, shot noise, port weights, dust removal, alpha, RGB mix);
-// FULL: all four ports used (the usual tile mask 0xF), so every mask test folds away.
+// FULL: all four ports used (the usual tile mask 0xF), so every mask test folds away.  Thread
+// pr covers column pr & 15 of rows 2 (pr >> 4) and 2 (pr >> 4) + 1.
 template <bool FULL>
 __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_P * TX_P], const float *s_win2,
                                            const float *s_rwin2, float *out, int mask_rt, int used_rt,
                                            float inv_used, float ksigma, int tid, float part[16]) {
   const int mask = FULL ? 0xF : mask_rt;
   const int used = FULL ? 4 : used_rt;
-  for (int i = tid; i < 256; i += TX_THREADS) {
-    // tile_debayer (ImageDtt.java:3047-3147): 3x3 stencil over the un-windowed tile, the
-    // taps outside the tile dropped and the sum renormalised (k_corn / k_side); the
-    // neighbour weights (kernel x 1/window^2 x edge factor) serve all 12 planes
-    const int y = i >> 4, x = i & 15, p = (y + 1) * TX_P + x + 1;
-    const bool ey = (y == 0) || (y == 15), ex = (x == 0) || (x == 15);
-    const float f_rb = (ey && ex) ? (16.0f / 9.0f) : ((ey || ex) ? (4.0f / 3.0f) : 1.0f);
-    const float f_g = (ey && ex) ? (4.0f / 3.0f) : ((ey || ex) ? (8.0f / 7.0f) : 1.0f);
+  for (int pr = tid; pr < 128; pr += TX_THREADS) {
+  const int x = pr & 15, y0 = (pr >> 4) * 2;
+  float dd[2][4][3];
+  debayer2(tc, s_ic, s_win2, x, y0, dd, part);
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    const int y = y0 + k, i = y * 16 + x, p = (y + 1) * TX_P + x + 1;
     const float lw = s_win2[i], rlw = s_rwin2[p], rlw2 = rlw * rlw;
     float d[4][3];
 #pragma unroll
     for (int ip = 0; ip < 4; ip++)
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const float *u = s_ic[ip * 3 + c] + p;  // un-windowed tile, zero outside
-        const float sides = (u[-TX_P] + u[-1]) + (u[1] + u[TX_P]);
-        float acc;
-        if (c != 2) {  // kern_rb: corners 1/16, sides 1/8, centre 1/4
-          const float corners = (u[-TX_P - 1] + u[-TX_P + 1]) + (u[TX_P - 1] + u[TX_P + 1]);
-          acc = fmaf(0.0625f, corners, fmaf(0.125f, sides, 0.25f * u[0]));
-        } else {       // kern_g: sides 1/8, centre 1/2
-          acc = fmaf(0.125f, sides, 0.5f * u[0]);
-        }
-        acc *= (c != 2) ? f_rb : f_g;
-        if (tc.scale_shot > 0.f)  // tile_debayer_shot_corr (3022-3045)
-          acc = tc.scale_shot * ((acc > tc.min_shot) ? acc * rsqrtf(acc) : (tc.rsqrt_min_shot * acc));
-        d[ip][c] = acc * lw;
-        part[4 + c * 4 + ip] += d[ip][c];
-      }
+      for (int c = 0; c < 3; c++) d[ip][c] = k ? dd[1][ip][c] : dd[0][ip][c];
     if (tc.rows > 4) {  // per-colour rms across the used ports and their weighted norm
       float sw = 0.f;
 #pragma unroll
@@ -88,11 +126,11 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
 #pragma unroll
         for (int ip = 0; ip < 4; ip++)
           if (mask & (1 << ip)) v = fmaf(d[ip][c] - m, d[ip][c] - m, v);
-        const float rms = __fdividef(sqrtf(v * s0), s0);
+        const float rms = __fdividef(sqrt_approx(v * s0), s0);
         out[(8 + c) * 256 + i] = rms;
         sw = fmaf(tc.col_weights[c] * rms, rms, sw);
       }
-      out[11 * 256 + i] = sqrtf(sw);
+      out[11 * 256 + i] = sqrt_approx(sw);
     }
     // Weights are kept relative to the largest one (scale sc_w): every use of them below is
     // a ratio or homogeneous of degree 1 (dust_remove), so FP32 exp() cannot underflow to
@@ -233,6 +271,7 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
       v *= lw;  // the tiles are kept un-windowed
       out[c * 256 + i] = v;
     }
+  }
   }
 }
 
