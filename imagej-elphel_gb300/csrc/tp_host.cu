@@ -52,6 +52,8 @@ struct tp_handle {
   int adj_record = 0, strips_valid = 0, deriv_valid = 0;
   float *d_psf_stage = nullptr;  // staging of host PSF tables for tp_calc_kernels
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
+  float *d_rig_tmp = nullptr;  // rig LMA: disparity record [tiles][TP_NDISP], then the fit [tiles][4]
+  int rig_lma_done = 0;        // the rig record already holds the LMA branch's values
   float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
   float *d_mismatch = nullptr;  // [tiles][pairs][3] lazy-eye mismatch of the last LMA pass that measured it
   size_t mismatch_cap = 0;
@@ -465,7 +467,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
                   h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
-                  h->d_rig_rec};
+                  h->d_rig_rec, h->d_rig_tmp};
   for (void *b : bufs) dfree(h, b);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->ev_work) cudaEventDestroy(h->ev_work);
@@ -1413,31 +1415,8 @@ tp_status tp_default_lma_params(tp_lma_params *p) {
   return TP_OK;
 }
 
-tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
-  if (!h) return TP_ERR_ARG;
-  tp_lma_params prm;
-  if (p) prm = *p;
-  else tp_default_lma_params(&prm);
-  if (prm.cnvx_hwnd_size < 0 || prm.cnvx_hwnd_size > 4 || prm.num_iter < 0)
-    return fail(h, TP_ERR_ARG, "tp_lma_refine: cnvx_hwnd_size must be 0..4");
-  if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_lma_refine: no correlation pairs");
-  if (!h->fwd_valid) return fail(h, TP_ERR_STATE, "tp_lma_refine: run tp_process first");
-  if (h->disp_mixed)
-    return fail(h, TP_ERR_STATE, "tp_lma_refine: the disparity record already holds the LMA result; run tp_process");
-  bool quad = false;
-  for (int i = 0; i < h->num_pairs; i++) {
-    const int k = h->corr_host.pairs[i].kind;
-    if (k >= 0 && k <= 3 && i < 32 && ((prm.pair_mask >> i) & 1)) quad = true;
-  }
-  if (!quad) return fail(h, TP_ERR_ARG, "tp_lma_refine: needs pairs of the quad kinds 0..3");
-  cudaStream_t st = pick_stream(h, stream);
-  if (!h->d_lma) {
-    if (dalloc(h, &h->d_lma, (size_t)h->ntiles * 4) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(h, TP_ERR_NOMEM, "tp_lma_refine: buffer");
-    }
-  }
-  CK(cudaMemsetAsync(h->d_lma, 0xff, (size_t)h->ntiles * 4 * sizeof(float), st), "tp_lma_refine");  // NaN
+// the device copy of the LMA settings
+static TpLmaConst lma_const_of(const tp_lma_params &prm) {
   TpLmaConst c;
   c.min_poly_strength = prm.min_poly_strength;
   c.mix_corr_poly = prm.mix_corr_poly;
@@ -1475,6 +1454,35 @@ tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
   c.ly_poly = prm.ly_poly;
   c.ly_poly_backup = prm.ly_poly_backup;
   c.ly_crazy_poly = prm.ly_crazy_poly;
+  return c;
+}
+
+tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream) {
+  if (!h) return TP_ERR_ARG;
+  tp_lma_params prm;
+  if (p) prm = *p;
+  else tp_default_lma_params(&prm);
+  if (prm.cnvx_hwnd_size < 0 || prm.cnvx_hwnd_size > 4 || prm.num_iter < 0)
+    return fail(h, TP_ERR_ARG, "tp_lma_refine: cnvx_hwnd_size must be 0..4");
+  if (!h->have_corr || h->num_pairs == 0) return fail(h, TP_ERR_STATE, "tp_lma_refine: no correlation pairs");
+  if (!h->fwd_valid) return fail(h, TP_ERR_STATE, "tp_lma_refine: run tp_process first");
+  if (h->disp_mixed)
+    return fail(h, TP_ERR_STATE, "tp_lma_refine: the disparity record already holds the LMA result; run tp_process");
+  bool quad = false;
+  for (int i = 0; i < h->num_pairs; i++) {
+    const int k = h->corr_host.pairs[i].kind;
+    if (k >= 0 && k <= 3 && i < 32 && ((prm.pair_mask >> i) & 1)) quad = true;
+  }
+  if (!quad) return fail(h, TP_ERR_ARG, "tp_lma_refine: needs pairs of the quad kinds 0..3");
+  cudaStream_t st = pick_stream(h, stream);
+  if (!h->d_lma) {
+    if (dalloc(h, &h->d_lma, (size_t)h->ntiles * 4) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_lma_refine: buffer");
+    }
+  }
+  CK(cudaMemsetAsync(h->d_lma, 0xff, (size_t)h->ntiles * 4 * sizeof(float), st), "tp_lma_refine");  // NaN
+  const TpLmaConst c = lma_const_of(prm);
   if (prm.mismatch) {
     const size_t need = (size_t)h->ntiles * h->num_pairs * 3;
     if (need > h->mismatch_cap) {
@@ -1509,6 +1517,22 @@ tp_status tp_get_lma(tp_handle *h, float *out) {
   return d2h(h, out, h->d_lma, (size_t)h->ntiles * 4 * sizeof(float), "tp_get_lma");
 }
 
+// the main camera's correlation set-up with one horizontal pair: camera 0 = main, 1 = auxiliary
+static CorrConst rig_corr_const(const tp_handle *h) {
+  CorrConst cc = h->corr_host;
+  cc.num_pairs = 1;
+  cc.num_combo = 1;
+  cc.log_combine = 0;
+  cc.num_hor = cc.num_vert = 0;
+  cc.pairs[0].cam1 = 0;
+  cc.pairs[0].cam2 = 1;
+  cc.pairs[0].kind = 0;
+  cc.pairs[0].in_combo = 1;
+  cc.pairs[0].bx = 1.f;
+  cc.pairs[0].by = 0.f;
+  return cc;
+}
+
 tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_normalization, int no_int_x0,
                            void *stream) {
   tp_handle *h = main_h;
@@ -1532,19 +1556,34 @@ tp_status tp_rig_correlate(tp_handle *main_h, tp_handle *aux, float cm_max_norma
   }
   CK(cudaStreamWaitEvent(st, aux->ev_work, 0), "tp_rig_correlate");  // both cameras' forwards
   CK(cudaStreamWaitEvent(st, h->ev_work, 0), "tp_rig_correlate");
-  CorrConst cc = h->corr_host;  // the main camera's correlation set-up, one horizontal pair
-  cc.num_pairs = 1;
-  cc.num_combo = 1;
-  cc.log_combine = 0;
-  cc.num_hor = cc.num_vert = 0;
-  cc.pairs[0].cam1 = 0;
-  cc.pairs[0].cam2 = 1;
-  cc.pairs[0].kind = 0;
-  cc.pairs[0].in_combo = 1;
-  cc.pairs[0].bx = 1.f;
-  cc.pairs[0].by = 0.f;
+  const CorrConst cc = rig_corr_const(h);
   CK(launch_rig(scene_of(h), scene_of(aux), cc, h->d_rig_corr, h->d_rig_rec, cm_max_normalization, no_int_x0, st),
      "tp_rig_correlate");
+  h->rig_lma_done = 0;
+  return mark_work(h, st);
+}
+
+tp_status tp_rig_lma(tp_handle *main_h, const tp_lma_params *p, int use_poly, int use_xy_poly, void *stream) {
+  tp_handle *h = main_h;
+  if (!h) return TP_ERR_ARG;
+  tp_lma_params prm;
+  if (p) prm = *p;
+  else tp_default_lma_params(&prm);
+  if (prm.cnvx_hwnd_size < 0 || prm.cnvx_hwnd_size > 4 || prm.num_iter < 0)
+    return fail(h, TP_ERR_ARG, "tp_rig_lma: cnvx_hwnd_size must be 0..4");
+  if (!h->d_rig_corr) return fail(h, TP_ERR_STATE, "tp_rig_lma: run tp_rig_correlate first");
+  if (h->rig_lma_done)
+    return fail(h, TP_ERR_STATE, "tp_rig_lma: the rig record already holds the LMA result; run tp_rig_correlate");
+  cudaStream_t st = pick_stream(h, stream);
+  if (!h->d_rig_tmp && dalloc(h, &h->d_rig_tmp, (size_t)h->ntiles * (TP_NDISP + 4)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, TP_ERR_NOMEM, "tp_rig_lma: buffer");
+  }
+  CK(cudaStreamWaitEvent(st, h->ev_work, 0), "tp_rig_lma");
+  CK(launch_rig_lma(scene_of(h), rig_corr_const(h), lma_const_of(prm), h->d_rig_corr, h->d_rig_rec, h->d_rig_tmp,
+                    h->d_rig_tmp + (size_t)h->ntiles * TP_NDISP, use_poly, use_xy_poly, st),
+     "tp_rig_lma");
+  h->rig_lma_done = 1;
   return mark_work(h, st);
 }
 

@@ -196,6 +196,10 @@ struct TpLmaConst {
 cudaError_t upload_lma_constants();
 cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out,
                        float *mismatch_out, cudaStream_t st);
+// the LMA branch of the rig's inter-camera correlation (tp_lma.cu); cc1: the one-pair set-up
+cudaError_t launch_rig_lma(const SceneDev &mn, const CorrConst &cc1, const TpLmaConst &c, const float *rig_corr,
+                           float *rig_rec, float *tmp_disp, float *tmp_lma, int use_poly, int use_xy_poly,
+                           cudaStream_t st);
 cudaError_t launch_kernel_prep(const float *psf_dev, int nk, int normalize, float *clt_out, float *ext_out,
                                cudaStream_t st);
 cudaError_t launch_fill_coord_corr(float *ext, int kh, int kv, int C, int kern_step, cudaStream_t st);

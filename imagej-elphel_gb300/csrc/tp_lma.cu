@@ -863,6 +863,116 @@ cudaError_t upload_lma_constants() {
 
 int lma_smem_bytes() { return LMA_NW * LMA_PER_WARP * 4; }
 
+// ---------------------------------------------------------------------------
+// The LMA branch of ImageDtt.tileInterCamCorrs (ImageDtt.java:7497-7560) for a rig: the LMA pass
+// above runs on the inter-camera surfaces ([tiles][1][225], one horizontal pair) from a record
+// whose CM / strength are the rig's centre-of-mass values; then, where it converged, its
+// disparity / strength replace the rig record's (use_poly), and the peak's 2D offset around x = 0
+// fills dx, dy: single2dPoly (Correlation2d.java:1509-1536: the quadric of the convex-region
+// samples, values as weights to ortho_vasw_pwr) with use_xy_poly, else single2dCM within
+// max_corr_radius (1538-1585).  Warp per task.
+// ---------------------------------------------------------------------------
+__global__ void rig_disp_kernel(const float *rig_rec, float *disp, int ntiles) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntiles * TP_NDISP) return;
+  const int t = i / TP_NDISP, k = i - t * TP_NDISP;
+  disp[i] = (k == 1) ? rig_rec[t * 4] : ((k == 2) ? rig_rec[t * 4 + 1] : CUDART_NAN_F);
+}
+
+__global__ void __launch_bounds__(32 * LMA_NW) rig_xy_kernel(const __grid_constant__ LmaDev ld,
+                                                            const __grid_constant__ TpLmaConst c, float *rig_rec,
+                                                            int use_poly, int use_xy_poly) {
+  extern __shared__ float sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *gsurf = sm + warp * LMA_PER_WARP;
+  float *sx = gsurf + 450;
+  float *sy = sx + LMA_MAX_SAMPLES, *sv = sy + LMA_MAX_SAMPLES, *sw = sv + LMA_MAX_SAMPLES;
+  unsigned char *sg = (unsigned char *)(sw + LMA_MAX_SAMPLES);
+  double *dmom = (double *)(gsurf + ((LMA_OFF_RED + 1) & ~1));
+  double *dsolve = (double *)gsurf;  // the group surfaces are no longer needed when the solver runs
+  for (int task = blockIdx.x * LMA_NW + warp; task < ld.num_tasks; task += gridDim.x * LMA_NW) {
+    const int txy = ld.task_txy[task];
+    const size_t tile = (size_t)(txy >> 16) * ld.tilesX + (txy & 0xffff);
+    const float *lr = ld.lma + tile * 4;
+    if (isnan(lr[0])) continue;  // the LMA did not run or did not converge
+    const float *src = ld.corr + tile * TP_CORR;
+    float dx = CUDART_NAN_F, dy = CUDART_NAN_F;
+    if (use_xy_poly) {
+      int ng, gdb;
+      const int ns = lma_samples<true>(ld, c, 1u, 0.0f, c.ortho_vasw_pwr, src, gsurf, sx, sy, sv, sw, sg, lane, ng,
+                                       gdb);
+      quadric_moments(sx, sy, sv, sw, ns, lane, dmom);
+      __syncwarp();
+      if (lane == 0) {
+        double q[3];
+        if (quadric_max(dmom, ns, dsolve, q)) {
+          dx = (float)(0.0 - q[0]);
+          dy = (float)(-q[1]);
+        }
+      }
+      __syncwarp();
+    } else if (lane == 0) {
+      float m3[3];
+      mismatch_cm(src, 0, 0.0f, c.max_corr_radius, m3);
+      dx = m3[0];
+      dy = m3[1];
+    }
+    if (lane == 0) {
+      float *rr = rig_rec + tile * 4;
+      if (use_poly) {
+        rr[0] = lr[0];
+        rr[1] = lr[1];
+      }
+      rr[2] = dx;
+      rr[3] = dy;
+    }
+  }
+}
+
+cudaError_t launch_rig_lma(const SceneDev &mn, const CorrConst &cc1, const TpLmaConst &c, const float *rig_corr,
+                           float *rig_rec, float *tmp_disp, float *tmp_lma, int use_poly, int use_xy_poly,
+                           cudaStream_t st) {
+  const int ntiles = mn.tilesX * mn.tilesY;
+  rig_disp_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(rig_rec, tmp_disp, ntiles);
+  cudaError_t e = cudaMemsetAsync(tmp_lma, 0xff, (size_t)ntiles * 4 * sizeof(float), st);  // NaN
+  if (e != cudaSuccess) return e;
+  SceneDev sc = mn;
+  sc.corr = const_cast<float *>(rig_corr);
+  sc.disp = tmp_disp;
+  TpLmaConst cl = c;
+  cl.fo_correct = 0;
+  cl.mismatch = 0;
+  cl.mix_corr_poly = 0;
+  cl.pair_mask = 1;
+  e = launch_lma(sc, cc1, cl, tmp_lma, nullptr, st);
+  if (e != cudaSuccess || mn.num_tasks <= 0) return e;
+  LmaDev ld;
+  ld.corr = rig_corr;
+  ld.disp = tmp_disp;
+  ld.lma = tmp_lma;
+  ld.mismatch = nullptr;
+  ld.task_txy = mn.task_txy;
+  ld.num_tasks = mn.num_tasks;
+  ld.tilesX = mn.tilesX;
+  ld.P = 1;
+  for (int k = 0; k < 4; k++) ld.kind_count[k] = 0;
+  for (int i = 0; i < TP_MAXP; i++) ld.kinds[i] = -1;
+  ld.kinds[0] = 0;
+  ld.kind_count[0] = 1;
+  const int bytes = lma_smem_bytes();
+  e = cudaFuncSetAttribute(rig_xy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rig_xy_kernel, 32 * LMA_NW, bytes);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int units = (mn.num_tasks + LMA_NW - 1) / LMA_NW;
+  const int grid = units < sms * per_sm ? units : sms * per_sm;
+  rig_xy_kernel<<<grid, 32 * LMA_NW, bytes, st>>>(ld, cl, rig_rec, use_poly, use_xy_poly);
+  return cudaGetLastError();
+}
+
 __global__ void mismatch_init_kernel(float *m, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) m[i] = (i % 3 == 2) ? 0.f : CUDART_NAN_F;

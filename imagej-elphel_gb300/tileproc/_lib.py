@@ -130,6 +130,7 @@ PROTOTYPES = {
     "tp_get_lma_mismatch": [_H, _vp],
     "tp_rig_correlate": [_H, _H, C.c_float, C.c_int, _vp],
     "tp_get_rig": [_H, _vp, _vp],
+    "tp_rig_lma": [_H, C.POINTER(TpLmaParams), C.c_int, C.c_int, _vp],
     "tp_batch_create": [C.POINTER(_H), C.c_int, C.POINTER(_H)],
     "tp_batch_destroy": [_H],
     "tp_batch_last_error": [_H, C.c_char_p, C.c_int],

@@ -329,6 +329,20 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_get_rig(self.h, _ptr(corr), _ptr(rec)), "tp_get_rig")
         return corr, rec
 
+    def rigLma(self, use_poly=True, use_xy_poly=True, params=None, stream=None, **kw):
+        """The LMA branch of the last rigCorrelate (ImageDtt.tileInterCamCorrs, ImageDtt.java:7497-7560,
+        rig.use_poly / rig.use_xy_poly): returns the updated rec [tiles][4]."""
+        if params is None:
+            params = L.TpLmaParams()
+            self._ck(self._lib.tp_default_lma_params(C.byref(params)), "tp_default_lma_params")
+        for k, v in kw.items():
+            setattr(params, k, v)
+        self._ck(self._lib.tp_rig_lma(self.h, C.byref(params), int(bool(use_poly)), int(bool(use_xy_poly)), stream),
+                 "tp_rig_lma")
+        rec = np.zeros((self.tilesY * self.tilesX, 4), dtype=np.float32)
+        self._ck(self._lib.tp_get_rig(self.h, None, _ptr(rec)), "tp_get_rig")
+        return rec
+
     # ---- adjoint ----
     def setAdjointMode(self, recompute_clt=False):
         self._ck(self._lib.tp_set_adjoint_mode(self.h, int(bool(recompute_clt))), "tp_set_adjoint_mode")

@@ -355,9 +355,9 @@ tp_status tp_get_lma_mismatch(tp_handle *h, float *out);
  * Inter-camera correlation of the sensor-averaged CLT of each camera
  * (Correlation2d.correlateInterCamerasFD / cltMixCameras, Correlation2d.java:401-448)
  * with the main camera's correlation set-up, and its disparity along the rig
- * baseline (ImageDtt.tileInterCamCorrs 7370-7560 without the LMA branch):
+ * baseline (ImageDtt.tileInterCamCorrs 7370-7496; the LMA branch is tp_rig_lma):
  * rec = {BI_DISP_CROSS, BI_STR_CROSS (mass / (sigma x cm_max_normalization)^2),
- * BI_DISP_CROSS_DX, BI_DISP_CROSS_DY (NaN: LMA only)}.  Both cameras share the
+ * BI_DISP_CROSS_DX, BI_DISP_CROSS_DY (NaN until tp_rig_lma)}.  Both cameras share the
  * tile grid and colours and have run tp_process (each with its own geometry and
  * target disparities); tiles the auxiliary camera has no task for get
  * {NaN, 0, NaN, NaN}.  Results are kept by the main handle. */
@@ -365,6 +365,17 @@ tp_status tp_rig_correlate(tp_handle *main_camera, tp_handle *aux_camera, float 
                            void *stream);
 /* corr [tilesY*tilesX][15*15], rec [tilesY*tilesX][4]; either may be NULL */
 tp_status tp_get_rig(tp_handle *main_camera, float *corr, float *rec);
+/* The LMA branch of tileInterCamCorrs (ImageDtt.java:7497-7560) on the last tp_rig_correlate:
+ * where the record's strength exceeds p->min_poly_strength, the LMA of tp_lma_refine runs on the
+ * inter-camera surface (one horizontal pair, centred at -disparity; fo_correct, mismatch and
+ * mix_corr_poly do not apply), and where it converges use_poly (rig.use_poly) replaces
+ * BI_DISP_CROSS / BI_STR_CROSS by its disparity / strength, and the peak's offset around x = 0
+ * fills BI_DISP_CROSS_DX / DY: with use_xy_poly (rig.use_xy_poly) the maximum of the quadric fit
+ * to the convex-region samples weighted x |value|^ortho_vasw_pwr (Correlation2d.single2dPoly
+ * 1509-1536; NaN where the fit has no maximum), else the centre of mass of the positive cells
+ * within max_corr_radius (single2dCM 1538-1585).  Runs once per tp_rig_correlate (TP_ERR_STATE
+ * otherwise); p NULL: tp_default_lma_params. */
+tp_status tp_rig_lma(tp_handle *main_camera, const tp_lma_params *p, int use_poly, int use_xy_poly, void *stream);
 
 /* ---- batches (no reference counterpart: the reference processes one scene per
  * GPUTileProcessor instance and launch) ----

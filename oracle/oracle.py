@@ -592,6 +592,8 @@ def _lma_lib():
         L.or_corr_lma.restype = C.c_int
         L.or_filter_convex.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp]
         L.or_filter_convex.restype = None
+        L.or_rig_lma.argtypes = [_dp, C.POINTER(LmaParams), C.c_int, C.c_int, C.c_double, _dp]
+        L.or_rig_lma.restype = C.c_int
         L._lma_set = True
     return L
 
@@ -602,6 +604,16 @@ def default_lma_params(**kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def rig_lma(corr225, rec, params=None, use_poly=True, use_xy_poly=True, max_corr_radius=3.9):
+    """The LMA branch of ImageDtt.tileInterCamCorrs (ImageDtt.java:7497-7560) on one rig tile:
+    (converged, rec') with rec = {disparity, strength, dx, dy} of the centre-of-mass record."""
+    r = np.array(rec, dtype=np.float64)
+    p = params if params is not None else default_lma_params()
+    ok = _lma_lib().or_rig_lma(_d(_f64(corr225).reshape(225)), C.byref(p), int(bool(use_poly)),
+                               int(bool(use_xy_poly)), float(max_corr_radius), _d(r))
+    return bool(ok), r
 
 
 def filter_convex(corr225, hwin, x0c, y0c, add3x3=True, nc_cost=0.5):

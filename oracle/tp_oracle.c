@@ -2404,6 +2404,32 @@ static void or_mismatch_poly_pair(const double *c, int k, double xcenter, double
   out[2] = isnan(m[2]) ? 0.0 : m[2];
 }
 
+/* The LMA branch of ImageDtt.tileInterCamCorrs (ImageDtt.java:7497-7560) on one rig tile.
+ * rec = {disparity, strength, dx, dy} of the centre-of-mass record.  Where the strength exceeds
+ * min_poly_strength, corrLMA of the single horizontal surface (Correlation2d.java:1903-2011: one
+ * ortho group, scale 1) runs at xcenter = -disparity; if it converges, use_poly takes its
+ * disparity / strength, and the offset of the peak around x = 0 fills dx, dy: single2dPoly
+ * (1509-1536, the quadric of the same sampling with |value|^ortho_vasw_pwr weights) or
+ * single2dCM (1538-1585, centre of mass within max_corr_radius).  Returns 1 when the LMA ran and
+ * converged, 0 otherwise (rec unchanged). */
+int or_rig_lma(const double *corr225, const or_lma_params *p, int use_poly, int use_xy_poly, double max_corr_radius,
+               double rec[4]) {
+  if (isnan(rec[0]) || !(rec[1] > p->min_poly_strength)) return 0;
+  const int kind = 0;
+  double out[4];
+  if (!or_corr_lma(corr225, &kind, 1, -rec[0], p, out, NULL)) return 0;
+  if (use_poly) {
+    rec[0] = out[0];
+    rec[1] = out[1];
+  }
+  double xy[3];
+  if (use_xy_poly) or_mismatch_poly_pair(corr225, 0, 0.0, p->ortho_vasw_pwr, p, xy);
+  else or_mismatch_cm_pair(corr225, 0, 0.0, max_corr_radius, xy);
+  rec[2] = xy[0];
+  rec[3] = xy[1];
+  return 1;
+}
+
 int or_lma_tile_mismatch(const double *corrs, const int *kind, int np, const or_lma_params *p,
                          const or_fo_params *f, double max_corr_radius, double mismatch_max_diff, double rec[3],
                          double lma[4], double *mism) {

@@ -299,6 +299,10 @@ int or_lma_tile_mismatch_ly(const double *corrs, const int *kind, int np, const 
 /* Correlations2dLMA.getMaxXYPoly (641-704): weighted quadric fit of n samples (weight > 0 taken)
  * and its maximum -> xyv {x, y, value}; 0 when the fit or the maximum does not exist */
 int or_quadratic_max(const double *x, const double *y, const double *v, const double *w, int n, double xyv[3]);
+/* the LMA branch of the rig's inter-camera correlation (ImageDtt.java:7497-7560) on one tile:
+ * rec {disparity, strength, dx, dy} updated in place; 1 when the LMA ran and converged */
+int or_rig_lma(const double *corr225, const or_lma_params *p, int use_poly, int use_xy_poly, double max_corr_radius,
+               double rec[4]);
 
 /* ---- texture tiles (ImageDtt.java:2662-2812) ---- */
 typedef struct {

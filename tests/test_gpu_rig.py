@@ -69,6 +69,54 @@ def test_rig_inter_camera(oracle, kind):
         _rig_check(oracle, tm, ta, aux_op, no_int_x0=True)
 
 
+def _rig_lma_compare(oracle, corr, rec0, rec, use_poly, use_xy_poly):
+    """GPU rig record after rigLma against oracle.rig_lma fed the GPU's surfaces and CM record:
+    disparity 0.005 px, strength 1e-3 relative, dx / dy 1e-3 px (or NaN on both) on >= 97% of the
+    tiles the branch runs on; the rest keep the CM record unchanged."""
+    p = oracle.default_lma_params()
+    n = ok = fitted = 0
+    bad = []
+    for t in range(rec0.shape[0]):
+        if not (np.isfinite(rec0[t, 0]) and rec0[t, 1] > p.min_poly_strength):
+            assert np.array_equal(rec[t], rec0[t], equal_nan=True), "tile %d changed without the LMA" % t
+            continue
+        conv, want = oracle.rig_lma(corr[t], rec0[t], use_poly=use_poly, use_xy_poly=use_xy_poly)
+        n += 1
+        fitted += conv
+        g = rec[t].astype(np.float64)
+        same = (abs(g[0] - want[0]) <= 0.005 and abs(g[1] - want[1]) <= 1e-3 * abs(want[1]) + 1e-6 and
+                np.allclose(g[2:], want[2:], rtol=0, atol=1e-3, equal_nan=True))
+        ok += same
+        if not same:
+            bad.append((t, g.tolist(), want.tolist()))
+    assert n > 20 and fitted > 0.5 * n, "rig LMA ran on %d tiles, converged on %d" % (n, fitted)
+    assert ok >= 0.97 * n, "rig LMA record agrees on %d of %d tiles: %s" % (ok, n, bad[:3])
+
+
+@pytest.mark.parametrize("kind", ["quad_bayer", "quad_mono"])
+def test_rig_lma(oracle, kind):
+    """The LMA branch of tileInterCamCorrs (ImageDtt.java:7497-7560) with rig.use_poly and
+    rig.use_xy_poly on and off: the rig surface fitted like corrLMA, then single2dPoly or single2dCM."""
+    from tileproc import _lib
+    sc = synth.make_scene(kind, seed=23, width=128, height=96)
+    T = (sc["width"] // 8) * (sc["height"] // 8)
+    aux = dict(sc)
+    aux["images"] = np.ascontiguousarray(np.roll(sc["images"], 2, axis=-1))
+    with make_gpu(sc) as tm, make_gpu(aux) as ta:
+        for tp in (tm, ta):
+            tp.setCorrelation()
+            tp.setFullFrameImages(np.full(T, 2.0, np.float32))
+            tp.process()
+        for use_poly, use_xy_poly in ((True, True), (True, False), (False, True)):
+            corr, rec0 = tm.rigCorrelate(ta)
+            rec = tm.rigLma(use_poly=use_poly, use_xy_poly=use_xy_poly)
+            _rig_lma_compare(oracle, corr, rec0, rec, use_poly, use_xy_poly)
+            if not use_poly:
+                assert np.array_equal(rec[:, :2], rec0[:, :2], equal_nan=True)
+        with pytest.raises(_lib.TpError, match="already holds"):
+            tm.rigLma()
+
+
 def test_rig_rejects_mismatched_cameras():
     from tileproc import _lib
     sc = synth.make_scene("quad_mono", seed=22, width=64, height=64)

@@ -135,3 +135,18 @@ def test_poly_mismatch_crazy_pair_falls_back_to_centre_of_mass():
     big = np.max(np.abs(mn[:, :2]), axis=1) > 0.1
     assert big.any() and not big.all()
     assert np.all(mn[big, 2] == 0.0) and np.all(mn[~big, 2] > 0.4)
+
+
+def test_rig_lma_branch():
+    """tileInterCamCorrs' LMA branch (ImageDtt.java:7497-7560) on the model surface of one horizontal
+    pair: the fit recovers the disparity, the quadric (single2dPoly) an exact peak offset, the centre
+    of mass (single2dCM) one close to it; use_poly off keeps the CM record, a weak tile is left alone."""
+    x0 = -1.3
+    corr = _model_surfaces(x0)[0]
+    rec = [-x0 + 0.2, 0.9, np.nan, np.nan]
+    ok, r = O.rig_lma(corr, rec, use_poly=True, use_xy_poly=True)
+    assert ok and abs(r[0] - (-x0)) < 1e-6 and abs(r[2] - (-x0)) < 1e-9 and abs(r[3]) < 1e-9
+    ok, r = O.rig_lma(corr, rec, use_poly=False, use_xy_poly=False)
+    assert ok and r[0] == rec[0] and r[1] == rec[1] and abs(r[2] - (-x0)) < 0.3 and abs(r[3]) < 1e-12
+    ok, r = O.rig_lma(corr, [1.0, 0.1, np.nan, np.nan])
+    assert not ok and r[0] == 1.0 and np.isnan(r[2])
