@@ -398,16 +398,30 @@ def measure_batch(seed, n_scenes, steps, warmup, types=("c2_bayer_4x2592x1936", 
             tp.setFullFrameImages(w["target"], tile_op=np.full(w["T"], 0xF, np.int32))
             tiles += w["T"]
         lib = tps[0]._lib
+        # the autotuner's schedule per scene type, picked on the type's first scene and set on all
+        from tileproc.autotune import autotune
+        picks = {}
+        for i, t in enumerate(types[:n_scenes]):
+            best, ms = autotune(tps[i], reps=3, warmup=1)
+            picks[t] = {"pick": "%d,%d" % best, "ms": {"%d,%d" % k: round(v, 4) for k, v in ms.items()}}
+            for tp in tps[i::len(types)]:
+                tp.setSchedule(*best)
 
-        def plain():
-            for tp in tps:
-                tp._ck(lib.tp_ports(tp.h, sptr), "ports")
-                tp._ck(lib.tp_process(tp.h, sptr), "process")
+        def plain_of(sel):
+            def fn():
+                for tp in sel:
+                    tp._ck(lib.tp_ports(tp.h, sptr), "ports")
+                    tp._ck(lib.tp_process(tp.h, sptr), "process")
+            return fn
 
         b = Batch(tps)
-        out = {"workload": "%d scenes alternating %s" % (n_scenes, " / ".join(types)), "tiles_per_step": tiles}
-        for name, fn in (("plain", plain), ("batched", lambda: b.process(True, sptr)),
-                         ("graph", lambda: b.run_graph(sptr))):
+        out = {"workload": "%d scenes alternating %s" % (n_scenes, " / ".join(types)), "tiles_per_step": tiles,
+               "autotune": picks}
+        runs = [("plain", plain_of(tps)), ("batched", lambda: b.process(True, sptr)),
+                ("graph", lambda: b.run_graph(sptr))]
+        # the per-scene step split by scene type: what each type costs inside the plain step
+        runs += [("plain_" + t, plain_of(tps[i::len(types)])) for i, t in enumerate(types[:n_scenes])]
+        for name, fn in runs:
             for _ in range(warmup):
                 fn()
             torch.cuda.synchronize()
@@ -419,7 +433,8 @@ def measure_batch(seed, n_scenes, steps, warmup, types=("c2_bayer_4x2592x1936", 
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / steps
             out[name + "_ms"] = ms
-            out[name + "_tiles_per_s"] = tiles / (ms / 1000.0)
+            if not name.startswith("plain_"):
+                out[name + "_tiles_per_s"] = tiles / (ms / 1000.0)
         out["batched_over_plain"] = out["plain_ms"] / out["batched_ms"]
         out["graph_over_plain"] = out["plain_ms"] / out["graph_ms"]
         b.close()
