@@ -18,6 +18,15 @@ of the per-tile target disparities can absorb any residual, so the
 extrinsics move only as far as the damping of the disparity block lets them;
 with free_disparity=False the target disparities stay fixed and the
 extrinsics alone are fitted.
+
+Two things make the iteration robust far from the solution, where ports are
+off by a pixel or more:
+- A tile without a correlation peak (NaN disparity) counts invalid_cost px^2
+  in the cost, so a step cannot lower the cost by losing tiles.
+- There the measured disparity responds more weakly than its local
+  derivative says (the smeared peak of the combined strip saturates), and the
+  Gauss-Newton step falls short. An accepted step is therefore doubled while
+  the cost keeps falling, up to 8 times its length (expand).
 """
 import copy
 
@@ -26,13 +35,15 @@ import numpy as np
 KEYS = ("azimuth", "tilt", "roll", "zoom")
 
 
-def _evaluate(tp, geometry, disparity, tile_op):
+def _evaluate(tp, geometry, disparity, tile_op, invalid_cost=0.0):
+    """(d, ok, cost): cost = sum of d^2 over the tiles with a peak + invalid_cost per tile without"""
     tp.setGeometry(geometry)
     tp.setFullFrameImages(disparity, tile_op=tile_op)
     tp.process()
     d = tp.getDisparity()[:, 1].astype(np.float64)
     ok = np.isfinite(d) & (tile_op != 0)
-    return d, ok, float(np.sum(np.where(ok, d * d, 0.0)))
+    lost = int(np.count_nonzero((tile_op != 0) & ~ok))
+    return d, ok, float(np.sum(np.where(ok, d * d, 0.0))) + invalid_cost * lost
 
 
 # largest change of a tile's target disparity in one step, px: beyond about a pixel the
@@ -40,18 +51,29 @@ def _evaluate(tp, geometry, disparity, tile_op):
 MAX_DISPARITY_STEP = 1.0
 
 
+def _moved(g, D, de, dd, scale):
+    g_try = copy.deepcopy(g)
+    S = len(g[KEYS[0]])
+    for s in range(S):
+        for k, key in enumerate(KEYS):
+            g_try[key][s] = float(g_try[key][s] + scale * de[s * 4 + k])
+    return g_try, D + np.clip(scale * dd, -MAX_DISPARITY_STEP, MAX_DISPARITY_STEP)
+
+
 def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_disparity=True,
-           fixed_sensor=None, callback=None):
+           fixed_sensor=None, callback=None, invalid_cost=1.0, expand=True):
     """Runs `iterations` LM steps; returns (geometry, disparity, history) where history
-    holds the cost (sum d^2 over tiles with a peak) before each step and after the last.
-    The per-tile disparity steps are clipped to +-MAX_DISPARITY_STEP (a tile whose
-    disparity derivative is close to zero would otherwise take an unbounded step)."""
+    holds the cost (sum d^2 over tiles with a peak, plus invalid_cost per tile without one)
+    before each step and after the last.  The per-tile disparity steps are clipped to
+    +-MAX_DISPARITY_STEP (a tile whose disparity derivative is close to zero would otherwise
+    take an unbounded step); with expand an accepted step is doubled while that lowers the
+    cost, up to 8 times its length."""
     T = tp.tilesY * tp.tilesX
     S = tp.num_sensors
     g = copy.deepcopy(geometry)
     D = np.asarray(disparity, dtype=np.float64).reshape(T).copy()
     op = np.ones(T, np.int32) if tile_op is None else np.asarray(tile_op, np.int32).reshape(T)
-    d, ok, cost = _evaluate(tp, g, D.astype(np.float32), op)
+    d, ok, cost = _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
     history = [cost]
     for it in range(iterations):
         tp.backward()
@@ -73,19 +95,26 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_
                 M = JtJ + lam * np.diag(dA) - A.T @ (A * (b * b * inv)[:, None])
                 rhs = -(A.T @ r) + A.T @ (b * b * inv * r)
                 de = np.linalg.solve(M + 1e-12 * np.eye(S * 4), rhs)
-                dd = np.clip(-inv * b * (r + A @ de), -MAX_DISPARITY_STEP, MAX_DISPARITY_STEP)
+                dd = -inv * b * (r + A @ de)
             else:
                 de = np.linalg.solve(JtJ + lam * np.diag(dA) + 1e-12 * np.eye(S * 4), -(A.T @ r))
                 dd = np.zeros(T)
-            g_try = copy.deepcopy(g)
-            for s in range(S):
-                for k, key in enumerate(KEYS):
-                    g_try[key][s] = float(g_try[key][s] + de[s * 4 + k])
-            D_try = D + dd
-            d_try, ok_try, c_try = _evaluate(tp, g_try, D_try.astype(np.float32), op)
+            g_try, D_try = _moved(g, D, de, dd, 1.0)
+            d_try, ok_try, c_try = _evaluate(tp, g_try, D_try.astype(np.float32), op, invalid_cost)
             if c_try < cost or lam > 1e8:
+                g_base, D_base = g, D
                 g, D, cost = g_try, D_try, c_try
                 lam = max(lam / 3.0, 1e-7)
+                scale = 1.0
+                while expand and scale < 8.0:
+                    scale *= 2.0
+                    g_x, D_x = _moved(g_base, D_base, de, dd, scale)
+                    c_x = _evaluate(tp, g_x, D_x.astype(np.float32), op, invalid_cost)[2]
+                    if not c_x < cost:
+                        # the processor's last forward was the rejected trial: back to the accepted one
+                        _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
+                        break
+                    g, D, cost = g_x, D_x, c_x
                 break
             lam *= 4.0
         history.append(cost)

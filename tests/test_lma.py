@@ -57,7 +57,7 @@ def test_step_equals_full_normal_equations():
     tp = LinearProcessor(rng)
     lam = 0.3
     g0, D0 = _geom(), tp.D0.copy()
-    g1, D1, hist = lma.refine(tp, g0, D0, iterations=1, lam=lam)
+    g1, D1, hist = lma.refine(tp, g0, D0, iterations=1, lam=lam, expand=False)
     # full system: [A b] with damping lam * diag(J^T J)
     J = np.concatenate([tp.A, np.diag(tp.b)], axis=1)
     r = tp.r0
@@ -76,7 +76,7 @@ def test_disparity_step_is_clipped():
     tp = LinearProcessor(rng)
     tp.b[4] = 1e-4
     tp.r0[4] = 0.5
-    g1, D1, hist = lma.refine(tp, _geom(), tp.D0.copy(), iterations=1, lam=0.3)
+    g1, D1, hist = lma.refine(tp, _geom(), tp.D0.copy(), iterations=1, lam=0.3, expand=False)
     assert np.abs(D1 - tp.D0).max() <= lma.MAX_DISPARITY_STEP
     assert abs(D1[4] - tp.D0[4]) == lma.MAX_DISPARITY_STEP
 
@@ -89,3 +89,39 @@ def test_iterations_reduce_cost_fixed_disparity():
     e = np.array([g[k][s] for s in range(S) for k in lma.KEYS])
     best = np.linalg.lstsq(tp.A, -tp.r0, rcond=None)[0]
     assert np.allclose(e, best, atol=1e-3)
+
+
+class WeakResponseProcessor(LinearProcessor):
+    """The measured residual moves 5x less than the reported Jacobian says (a saturated peak)."""
+
+    def process(self):
+        self.d = self.r0 + 0.2 * (self.A @ self._e()) + self.b * (self.D - self.D0)
+
+
+def test_step_expansion_recovers_a_short_gauss_newton_step():
+    rng = np.random.default_rng(4)
+    tp = WeakResponseProcessor(rng)
+    _, _, h0 = lma.refine(tp, _geom(), tp.D0.copy(), iterations=3, free_disparity=False, expand=False)
+    _, _, h1 = lma.refine(tp, _geom(), tp.D0.copy(), iterations=3, free_disparity=False)
+    e = np.linalg.lstsq(tp.A, -tp.r0, rcond=None)[0]
+    floor = float(np.sum((tp.r0 + tp.A @ e) ** 2))  # the least-squares minimum of the cost
+    assert h1[-1] - floor < 0.2 * (h0[-1] - floor)
+
+
+class DroppingProcessor(LinearProcessor):
+    """Tiles whose residual exceeds 1 px lose their peak (NaN), as smeared correlation peaks do."""
+
+    def getDisparity(self):
+        out = super().getDisparity()
+        out[np.abs(self.d) > 1.0, 1] = np.nan
+        return out
+
+
+def test_lost_tiles_count_in_the_cost():
+    rng = np.random.default_rng(5)
+    tp = DroppingProcessor(rng)
+    tp.setGeometry(_geom())
+    tp.setFullFrameImages(tp.D0 + 3.0)  # residual 3 b > 1: every tile without a peak
+    tp.process()
+    d, ok, cost = lma._evaluate(tp, _geom(), tp.D0 + 3.0, np.ones(T, np.int32), invalid_cost=2.0)
+    assert not ok.any() and cost == 2.0 * T
