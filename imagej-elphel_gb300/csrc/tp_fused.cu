@@ -377,13 +377,13 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
   __syncwarp();
 }
 
-// phase C: combined strip, integer argmax, centroid, ortho maxima, disparity record
+// phase C, lane-parallel half: the combined strip (geometric mean of the pairs' strips) into
+// combo (shared) and sc.combo, and this lane's getMaxXSOrtho profile value (lanes 0-14 the
+// horizontal pairs' column j, lanes 16-30 the vertical pairs' row j; -inf elsewhere)
 template <int NT, bool OACC = false>
-__device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
-                                            bool log_mode, int ncomb, size_t tile, float *scr, int lane,
-                                            const float cmb[8], const float *oprod = nullptr) {
-  // ---------------- stage 3c: extraction ----------------
-  float *combo = scr;
+__device__ __forceinline__ float fwd_extract_values(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
+                                                    bool log_mode, int ncomb, size_t tile, float *combo, int lane,
+                                                    const float cmb[8], const float *oprod) {
 #pragma unroll
   for (int t = 0; t < NT; t++) {
     const int e = lane + 32 * t;
@@ -392,10 +392,50 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
       if (log_mode) v = isnan(v) ? CUDART_NAN_F : (isinf(v) ? 0.0f : expf(v / cfg.num_combo) - cfg.corr_offset);
       else if (v > 0.0f) v = powf(v, 1.0f / ncomb) - cfg.corr_offset;
       combo[e] = v;
-      if (sc.combo) sc.combo[tile * RE + e] = v;  // kept for the adjoint
+      if (sc.combo) sc.combo[tile * RE + e] = v;  // kept for the adjoint (and the split extraction)
+    }
+  }
+  float sum = -CUDART_INF_F;
+  if (quad && (cfg.num_hor > 0 || cfg.num_vert > 0)) {
+    // the surfaces of this tile were just written by this warp (L1/L2 resident)
+    const int half = lane >> 4, j = lane & 15;
+    const int np = half ? cfg.num_vert : cfg.num_hor;
+    if (j < 15 && np > 0) {
+      // the symmetrised profile is even in i (d[i] == d[14 - i]), so rows 0..7 carry it; all
+      // loads of one pair are issued before their use
+      float prod[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) prod[i] = OACC ? oprod[i] : 1.f;
+      for (int k = 0; k < (OACC ? 0 : np); k++) {
+        const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
+        const int stride = half ? 1 : 15, base = half ? j * 15 : j;
+        float a[8], b[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          a[i] = cc[base + i * stride];
+          b[i] = cc[base + (14 - i) * stride];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) prod[i] *= 0.5f * (a[i] + b[i]) + cfg.corr_offset;
+      }
+      sum = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float p = prod[i];
+        const float v = (p > 0.0f) ? ((np == 2) ? sqrtf(p) : ((np == 1) ? p : powf(p, 1.0f / np))) - cfg.corr_offset
+                                   : -cfg.corr_offset;
+        sum += v * ((i < 7) ? cfg.notch[i] + cfg.notch[14 - i] : cfg.notch[7]);
+      }
     }
   }
   __syncwarp();
+  return sum;
+}
+
+// phase C, serial half: integer argmax and windowed centroid of the combined strip (getMaxXYInt,
+// getMaxXCm), the maxima of the ortho profiles (getMaxXSOrtho), the disparity record
+__device__ __forceinline__ void fwd_extract_finish(const SceneDev &sc, const CorrConst &cfg, int quad, size_t tile,
+                                                   const float *combo, float sum, int lane) {
   float res[TP_NDISP];
 #pragma unroll
   for (int k = 0; k < TP_NDISP; k++) res[k] = (k == 2 || k == 4 || k == 6) ? 0.f : CUDART_NAN_F;
@@ -450,37 +490,7 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
   }
   if (quad && (cfg.num_hor > 0 || cfg.num_vert > 0)) {
     // getMaxXSOrtho: lanes 0-14 horizontal pairs, lanes 16-30 vertical pairs
-    // the surfaces of this tile were just written by this warp (L1/L2 resident)
     const int half = lane >> 4, j = lane & 15;
-    const int np = half ? cfg.num_vert : cfg.num_hor;
-    float sum = -CUDART_INF_F;
-    if (j < 15 && np > 0) {
-      // the symmetrised profile is even in i (d[i] == d[14 - i]), so rows 0..7 carry it; all
-      // loads of one pair are issued before their use
-      float prod[8];
-#pragma unroll
-      for (int i = 0; i < 8; i++) prod[i] = OACC ? oprod[i] : 1.f;
-      for (int k = 0; k < (OACC ? 0 : np); k++) {
-        const float *cc = sc.corr + (tile * P + (half ? cfg.vert_pairs[k] : cfg.hor_pairs[k])) * TP_CORR;
-        const int stride = half ? 1 : 15, base = half ? j * 15 : j;
-        float a[8], b[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-          a[i] = cc[base + i * stride];
-          b[i] = cc[base + (14 - i) * stride];
-        }
-#pragma unroll
-        for (int i = 0; i < 8; i++) prod[i] *= 0.5f * (a[i] + b[i]) + cfg.corr_offset;
-      }
-      sum = 0.f;
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const float p = prod[i];
-        const float v = (p > 0.0f) ? ((np == 2) ? sqrtf(p) : ((np == 1) ? p : powf(p, 1.0f / np))) - cfg.corr_offset
-                                   : -cfg.corr_offset;
-        sum += v * ((i < 7) ? cfg.notch[i] + cfg.notch[14 - i] : cfg.notch[7]);
-      }
-    }
     float best = sum;
     int bi = (j < 15) ? j : 99;
 #pragma unroll
@@ -514,6 +524,15 @@ __device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst 
     dm[lane] = v;
   }
   __syncwarp();
+}
+
+// phase C: combined strip, integer argmax, centroid, ortho maxima, disparity record
+template <int NT, bool OACC = false>
+__device__ __forceinline__ void fwd_extract(const SceneDev &sc, const CorrConst &cfg, int quad, int P, int RE,
+                                            bool log_mode, int ncomb, size_t tile, float *scr, int lane,
+                                            const float cmb[8], const float *oprod = nullptr) {
+  const float sum = fwd_extract_values<NT, OACC>(sc, cfg, quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
+  fwd_extract_finish(sc, cfg, quad, tile, scr, sum, lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -647,7 +666,7 @@ __device__ __forceinline__ void fwd_clt_item_win(const SceneDev &sc, const uint1
   }
 }
 
-template <int NT>
+template <int NT, bool SPLIT_X>
 __global__ void __launch_bounds__(128, 4) fused_forward_win_kernel(const __grid_constant__ SceneDev sc,
                                                                    const __grid_constant__ FwdShape fs,
                                                                    const __grid_constant__ CorrConst cfg) {
@@ -696,9 +715,52 @@ __global__ void __launch_bounds__(128, 4) fused_forward_win_kernel(const __grid_
       if (act) stage_window(sc, img, pc.tlx, pc.tly, (uint16_t *)(s_clt + (size_t)q * 3 * TP_CLT), r);
       cp_async_commit();
     }
-    fwd_extract<NT, true>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
+    if (SPLIT_X) {
+      // phase C in extract_kernel: the strip products and ortho profile products go out as they are
+#pragma unroll
+      for (int t = 0; t < NT; t++) {
+        const int e = lane + 32 * t;
+        if (e < RE) sc.combo[tile * RE + e] = cmb[t];
+      }
+      float4 *ob = (float4 *)(sc.osum + (tile * 32 + lane) * 8);
+      ob[0] = make_float4(oprod[0], oprod[1], oprod[2], oprod[3]);
+      ob[1] = make_float4(oprod[4], oprod[5], oprod[6], oprod[7]);
+    } else {
+      fwd_extract<NT, true>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
+    }
   }
   cp_async_wait_all();
+}
+
+// Phase C for the tiles of a fused forward that left it out: warp per task, from the strip
+// products (in sc.combo, replaced by the combined strip) and the ortho profile products (sc.osum)
+// the forward wrote.  Phase C is short chains of dependent shuffles, divides and powers; the
+// fused kernel's 16 warps per SM cannot hide their latency, while this kernel's few registers
+// and no CLT buffer let 64 warps share an SM.
+template <int NT>
+__global__ void __launch_bounds__(128) extract_kernel(const __grid_constant__ SceneDev sc,
+                                                      const __grid_constant__ CorrConst cfg, int quad, int RE) {
+  __shared__ float s_combo[4][TP_MAX_STRIP * 15];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int task = blockIdx.x * 4 + warp;
+  if (task >= sc.num_tasks) return;  // whole warps
+  const int txy = sc.task_txy[task];
+  const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
+  float cmb[8], oprod[8];
+#pragma unroll
+  for (int t = 0; t < NT; t++) {
+    const int e = lane + 32 * t;
+    cmb[t] = (e < RE) ? sc.combo[tile * RE + e] : 0.f;
+  }
+  const float4 *ob = (const float4 *)(sc.osum + (tile * 32 + lane) * 8);
+  const float4 o0 = ob[0], o1 = ob[1];
+  oprod[0] = o0.x; oprod[1] = o0.y; oprod[2] = o0.z; oprod[3] = o0.w;
+  oprod[4] = o1.x; oprod[5] = o1.y; oprod[6] = o1.z; oprod[7] = o1.w;
+  const int ncomb = cfg.twice_diagonal ? 2 * cfg.num_combo : cfg.num_combo;
+  float *combo = s_combo[warp];
+  const float sum = fwd_extract_values<NT, true>(sc, cfg, quad, sc.num_pairs, RE, cfg.log_combine, ncomb, tile, combo,
+                                                 lane, cmb, oprod);
+  fwd_extract_finish(sc, cfg, quad, tile, combo, sum, lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -1265,8 +1327,16 @@ cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tp
   bool all16 = true;
   for (int i = 0; i < sc.num_sensors; i++) all16 = all16 && sc.img_dtype[i] == 1;
   if (sc.num_colors == 3 && sc.num_sensors <= 4 && all16) {  // staged windows
-    if (f.RE <= 32) return launch_persistent(fused_forward_win_kernel<1>, f.nw * 32, bytes, units, sc, f, cc, st);
-    return launch_persistent(fused_forward_win_kernel<8>, f.nw * 32, bytes, units, sc, f, cc, st);
+    if (sc.combo && sc.osum) {  // the extraction's serial half in its own pass
+      e = (f.RE <= 32) ? launch_persistent(fused_forward_win_kernel<1, true>, f.nw * 32, bytes, units, sc, f, cc, st)
+                       : launch_persistent(fused_forward_win_kernel<8, true>, f.nw * 32, bytes, units, sc, f, cc, st);
+      if (e != cudaSuccess) return e;
+      if (f.RE <= 32) extract_kernel<1><<<(sc.num_tasks + 3) / 4, 128, 0, st>>>(sc, cc, f.quad, f.RE);
+      else extract_kernel<8><<<(sc.num_tasks + 3) / 4, 128, 0, st>>>(sc, cc, f.quad, f.RE);
+      return cudaGetLastError();
+    }
+    if (f.RE <= 32) return launch_persistent(fused_forward_win_kernel<1, false>, f.nw * 32, bytes, units, sc, f, cc, st);
+    return launch_persistent(fused_forward_win_kernel<8, false>, f.nw * 32, bytes, units, sc, f, cc, st);
   }
   if (f.RE <= 32)
     return sc.num_colors == 3 ? launch_persistent(fused_forward_kernel<3, 1>, f.nw * 32, bytes, units, sc, f, cc, st)

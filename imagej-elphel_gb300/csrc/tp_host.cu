@@ -45,6 +45,7 @@ struct tp_handle {
   CorrDev *d_corr_cfg = nullptr;
   float *d_tex = nullptr, *d_tex_aux = nullptr;
   float *d_combo = nullptr;  // [tiles][RE] combined strip rows of the last forward (adjoint input)
+  float *d_osum = nullptr;   // [tiles][32][8] ortho profile products handed to the extraction pass
   // Once the adjoint is in use (adj_record) the forward keeps what it needs: per-pair strip
   // samples [tiles][pairs][RE] and the plan's FP64 port derivatives
   float *d_strips = nullptr;
@@ -194,6 +195,7 @@ static SceneDev scene_of(tp_handle *h) {
   sc.clt_lpf_mask = h->lpf_on ? h->clt_lpf_mask : 0;
   sc.corr_cfg = h->d_corr_cfg;
   sc.combo = h->d_combo;
+  sc.osum = h->d_osum;
   sc.strips = (h->adj_record && h->d_strips && strips_need(h) <= h->strips_cap) ? h->d_strips : nullptr;
   sc.tex = h->d_tex;
   sc.tex_aux = h->tex_params.aux ? h->d_tex_aux : nullptr;
@@ -467,7 +469,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
                   h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
-                  h->d_rig_rec, h->d_rig_tmp};
+                  h->d_rig_rec, h->d_rig_tmp, h->d_osum};
   for (void *b : bufs) dfree(h, b);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->ev_work) cudaEventDestroy(h->ev_work);
@@ -877,6 +879,10 @@ tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pair
   if (!h->d_combo && dalloc(h, &h->d_combo, (size_t)h->ntiles * TP_MAX_STRIP * 15) != cudaSuccess) {
     cudaGetLastError();
     return fail(h, TP_ERR_NOMEM, "tp_set_corr: combined strip buffer");
+  }
+  if (!h->d_osum && dalloc(h, &h->d_osum, (size_t)h->ntiles * 256) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, TP_ERR_NOMEM, "tp_set_corr: ortho profile buffer");
   }
   CK(cudaMemcpy(h->d_corr_cfg, &cd, sizeof(cd), cudaMemcpyHostToDevice), "tp_set_corr");
   h->num_pairs = np;

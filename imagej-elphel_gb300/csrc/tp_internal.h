@@ -109,6 +109,7 @@ struct SceneDev {
   int clt_lpf_mask;          // colours whose stored CLT is multiplied by lpf_rbg (the reference GPU's lpf_mask)
   const CorrDev *corr_cfg;
   float *combo;              // [tiles][RE] combined strip rows the extraction reads, or null
+  float *osum;               // [tiles][32][8] per-lane ortho profile products for the separate extraction pass, or null
   float *strips;             // [tiles][pairs][RE] per-pair strip samples (adjoint input), or null
   float *tex;                // [tiles][rows][256] texture tiles (R, B, G, alpha[, 4 weights, 4 rms])
   float *tex_aux;            // [tiles][16] max_diff[4], ports_rgb[12] or null
