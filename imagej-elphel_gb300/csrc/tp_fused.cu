@@ -1250,6 +1250,51 @@ __global__ void disp_init_kernel(float *disp, int n) {
 
 cudaError_t upload_fused_constants() { return upload_dtt_constants(); }
 
+// GPU_DTT24_DRV (dtt8x8.cuh:100-158): every 8x8 block of a float image through the 2D transform of
+// one mode, rows first (bit 0: DST), then columns (bit 1); modes 0-3 DCT-IV / DST-IV, 4-7 the
+// orthonormal DCT-II / DST-II (the DCT-IIe butterflies with the constant term scaled by 1/sqrt 2).
+// An 8-lane group per block, lane r holding row r, then column r after the transpose.
+__device__ __forceinline__ void dtt8_mode(const float x[8], float y[8], int mode, bool sine) {
+  if (mode < 4) {
+    dtt4_fast(x, y, sine);
+  } else {
+    dtt2e_fast(x, y, sine);
+    if (sine) y[7] *= 0.70710678118654752f;
+    else y[0] *= 0.70710678118654752f;
+  }
+}
+
+__global__ void __launch_bounds__(128) dtt8x8_kernel(float *dst, const float *src, int stride, int bw, int nblocks,
+                                                     int mode) {
+  __shared__ float tb[16][72];
+  const int g = threadIdx.x >> 3, r = threadIdx.x & 7;
+  const int blk = blockIdx.x * 16 + g;
+  const bool act = blk < nblocks;
+  const int b = act ? blk : nblocks - 1;  // every group takes part in the warp's transposes
+  const int by = b / bw, bx = b - by * bw;
+  const float *s = src + (size_t)(by * 8 + r) * stride + bx * 8;
+  float x[8], y[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) x[c] = s[c];
+  dtt8_mode(x, y, mode, mode & 1);
+  group_transpose(y, tb[g], r);
+  dtt8_mode(y, x, mode, (mode >> 1) & 1);
+  group_transpose(x, tb[g], r);
+  if (act) {
+    float *d = dst + (size_t)(by * 8 + r) * stride + bx * 8;
+#pragma unroll
+    for (int c = 0; c < 8; c++) d[c] = x[c];
+  }
+}
+
+cudaError_t launch_dtt8x8(float *dst, const float *src, int stride, int width, int height, int mode,
+                          cudaStream_t st) {
+  const int bw = width / 8, nblocks = bw * (height / 8);
+  if (nblocks <= 0) return cudaSuccess;
+  dtt8x8_kernel<<<(nblocks + 15) / 16, 128, 0, st>>>(dst, src, stride, bw, nblocks, mode);
+  return cudaGetLastError();
+}
+
 static FwdShape make_shape(const SceneDev &sc, int nw) {
   FwdShape f;
   f.S = sc.num_sensors;

@@ -1335,6 +1335,38 @@ static void batch_drop_graph(tp_batch *b) {
   b->graph = nullptr;
 }
 
+// the DTT tables this translation unit's kernels read are uploaded once per device
+static std::mutex g_dtt_mu;
+static bool g_dtt_ready[64];
+
+tp_status tp_dtt8x8(float *dst, const float *src, int src_stride, int width, int height, int dtt_mode,
+                    void *stream) {
+  if (!dst || !src || width <= 0 || height <= 0 || (width & 7) || (height & 7) || src_stride < width ||
+      dtt_mode < 0 || dtt_mode > 7)
+    return TP_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return TP_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= 64) return TP_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lock(g_dtt_mu);
+    if (!g_dtt_ready[dev]) {
+      if (upload_fused_constants() != cudaSuccess) {
+        cudaGetLastError();
+        return TP_ERR_CUDA;
+      }
+      g_dtt_ready[dev] = true;
+    }
+  }
+  if (launch_dtt8x8(dst, src, src_stride, width, height, dtt_mode, (cudaStream_t)stream) != cudaSuccess) {
+    cudaGetLastError();
+    return TP_ERR_CUDA;
+  }
+  return TP_OK;
+}
+
 // Device address of the compaction scratch array per device (cudaGetSymbolAddress with that
 // device current).  A call outside a stream capture looks it up again, so a device reset that
 // reloaded the module is followed; a call inside a capture uses the address of the last call

@@ -148,6 +148,9 @@ cudaError_t upload_kernel_constants();
 // tpb/nw = tiles and warps per CTA (<= 0: defaults for the sensor/colour layout)
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st);
 cudaError_t upload_fused_constants();
+// GPU_DTT24_DRV counterpart (tp_fused.cu): 2D DTT of one mode on every 8x8 block
+cudaError_t launch_dtt8x8(float *dst, const float *src, int stride, int width, int height, int mode,
+                          cudaStream_t st);
 int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);
 // batched plans (tp_plan.cu) and persistent forward over many scenes (tp_fused.cu):
 // scene classes 0 = colour warp-per-tile, 1 = mono warp-per-tile, 2 = mono pair-per-warp

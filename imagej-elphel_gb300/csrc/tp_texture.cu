@@ -385,17 +385,27 @@ __global__ void __launch_bounds__(TX_THREADS, 5) texture_kernel(const __grid_con
     if (mask == 0xF) tex_pixels<true>(tc, s_ic, s_win2, s_rwin2, out, mask, used, inv_used, ksigma, tid, part);
     else tex_pixels<false>(tc, s_ic, s_win2, s_rwin2, out, mask, used, inv_used, ksigma, tid, part);
     if (sc.tex_aux) {
-      // one block reduction for max_diff (max) and ports_rgb (sum)
+      // one block reduction for max_diff (max, entries 0-3) and ports_rgb (sum): a reduce-scatter
+      // over the warp (each exchange halves the entries a lane keeps: 15 shuffles instead of 80),
+      // after which lanes 2k and 2k + 1 hold entry k, then across the four warps
 #pragma unroll
-      for (int k = 0; k < 16; k++)
+      for (int half = 8, m = 16; half > 0; half >>= 1, m >>= 1) {
+        const bool up = (lane & m) != 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float v = __shfl_xor_sync(0xffffffffu, part[k], o);
-          part[k] = (k < 4) ? fmaxf(part[k], v) : part[k] + v;
+        for (int i = 0; i < half; i++) {
+          const float keep = up ? part[half + i] : part[i];
+          const float v = __shfl_xor_sync(0xffffffffu, up ? part[i] : part[half + i], m);
+          // the entry kept here: index (lane >> 1) at the end, (lane >> 1) & ~(half - 1) + i now
+          const int k = ((lane >> 1) & ~(half - 1) & 15) + i;
+          part[i] = (k < 4) ? fmaxf(keep, v) : keep + v;
         }
-      if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 16; k++) s_red[warp][k] = part[k];
+      }
+      {
+        const int k = lane >> 1;
+        const float v = __shfl_xor_sync(0xffffffffu, part[0], 1);
+        part[0] = (k < 4) ? fmaxf(part[0], v) : part[0] + v;
+        if (!(lane & 1)) s_red[warp][k] = part[0];
+      }
       __syncthreads();
       if (tid < 16) {
         float* aux = sc.tex_aux + tile * 16;

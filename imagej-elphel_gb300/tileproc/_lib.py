@@ -99,6 +99,7 @@ PROTOTYPES = {
     "tp_set_lpf": [_H, _vp],
     "tp_set_clt_lpf_mask": [_H, C.c_int],
     "tp_calc_kernels": [_H, C.c_int, _vp, C.c_int, C.c_int, C.c_int, _vp],
+    "tp_dtt8x8": [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp],
     "tp_get_kernels": [_H, C.c_int, _vp, _vp],
     "tp_set_corr": [_H, C.POINTER(TpCorrParams), C.POINTER(TpPair), C.c_int],
     "tp_set_texture_params": [_H, C.POINTER(TpTextureParams)],

@@ -60,14 +60,23 @@ def _moved(g, D, de, dd, scale):
     return g_try, D + np.clip(scale * dd, -MAX_DISPARITY_STEP, MAX_DISPARITY_STEP)
 
 
-def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_disparity=True,
+# damping range of one iteration; past LAM_MAX no damping found a lower cost
+LAM_MIN, LAM_MAX, LAM_RESTART = 1e-7, 1e6, 1e-2
+# lengths tried for the undamped step when no damping lowers the cost
+STALL_SCALES = (2.0, 4.0, 8.0, 0.5, 0.25)
+
+
+def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART, free_disparity=True,
            fixed_sensor=None, callback=None, invalid_cost=1.0, expand=True):
     """Runs `iterations` LM steps; returns (geometry, disparity, history) where history
     holds the cost (sum d^2 over tiles with a peak, plus invalid_cost per tile without one)
-    before each step and after the last.  The per-tile disparity steps are clipped to
-    +-MAX_DISPARITY_STEP (a tile whose disparity derivative is close to zero would otherwise
-    take an unbounded step); with expand an accepted step is doubled while that lowers the
-    cost, up to 8 times its length."""
+    before each step and after the last; it never increases.  The per-tile disparity steps are
+    clipped to +-MAX_DISPARITY_STEP (a tile whose disparity derivative is close to zero would
+    otherwise take an unbounded step).  With expand an accepted step is doubled while that lowers
+    the cost, up to 8 times its length.  The cost is only piecewise smooth (window corners move
+    by whole pixels, peaks appear and vanish), so a point can be a dead end for every damping:
+    then the undamped step is tried at other lengths (STALL_SCALES), the best that lowers the cost
+    is taken, and the damping starts again from LAM_RESTART."""
     T = tp.tilesY * tp.tilesX
     S = tp.num_sensors
     g = copy.deepcopy(geometry)
@@ -87,36 +96,50 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=1e-2, free_
         JtJ = A.T @ A
         dA = np.diag(JtJ).copy()
         dA[dA == 0] = 1.0
-        while True:
+
+        def solve(lm):
             if free_disparity:
-                # disparity block diag(b^2 (1 + lam)), eliminated by its Schur complement
-                hdd = b * b * (1.0 + lam)
+                # disparity block diag(b^2 (1 + lm)), eliminated by its Schur complement
+                hdd = b * b * (1.0 + lm)
                 inv = np.where(hdd > 0, 1.0 / np.maximum(hdd, 1e-30), 0.0)
-                M = JtJ + lam * np.diag(dA) - A.T @ (A * (b * b * inv)[:, None])
+                M = JtJ + lm * np.diag(dA) - A.T @ (A * (b * b * inv)[:, None])
                 rhs = -(A.T @ r) + A.T @ (b * b * inv * r)
                 de = np.linalg.solve(M + 1e-12 * np.eye(S * 4), rhs)
-                dd = -inv * b * (r + A @ de)
-            else:
-                de = np.linalg.solve(JtJ + lam * np.diag(dA) + 1e-12 * np.eye(S * 4), -(A.T @ r))
-                dd = np.zeros(T)
-            g_try, D_try = _moved(g, D, de, dd, 1.0)
-            d_try, ok_try, c_try = _evaluate(tp, g_try, D_try.astype(np.float32), op, invalid_cost)
-            if c_try < cost or lam > 1e8:
-                g_base, D_base = g, D
-                g, D, cost = g_try, D_try, c_try
-                lam = max(lam / 3.0, 1e-7)
+                return de, -inv * b * (r + A @ de)
+            de = np.linalg.solve(JtJ + lm * np.diag(dA) + 1e-12 * np.eye(S * 4), -(A.T @ r))
+            return de, np.zeros(T)
+
+        def cost_at(scale, de, dd):
+            g_x, D_x = _moved(g, D, de, dd, scale)
+            return _evaluate(tp, g_x, D_x.astype(np.float32), op, invalid_cost)[2], g_x, D_x
+
+        best = None  # (cost, geometry, disparity) of the step taken
+        while lam <= LAM_MAX:
+            de, dd = solve(lam)
+            c1, g1, D1 = cost_at(1.0, de, dd)
+            if c1 < cost:
+                best = (c1, g1, D1)
                 scale = 1.0
                 while expand and scale < 8.0:
                     scale *= 2.0
-                    g_x, D_x = _moved(g_base, D_base, de, dd, scale)
-                    c_x = _evaluate(tp, g_x, D_x.astype(np.float32), op, invalid_cost)[2]
-                    if not c_x < cost:
-                        # the processor's last forward was the rejected trial: back to the accepted one
-                        _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
+                    cx = cost_at(scale, de, dd)
+                    if not cx[0] < best[0]:
                         break
-                    g, D, cost = g_x, D_x, c_x
+                    best = cx
+                lam = max(lam / 3.0, LAM_MIN)
                 break
             lam *= 4.0
+        if best is None:  # a dead end for every damping
+            de, dd = solve(LAM_RESTART)
+            for scale in STALL_SCALES:
+                cx = cost_at(scale, de, dd)
+                if cx[0] < cost and (best is None or cx[0] < best[0]):
+                    best = cx
+            lam = LAM_RESTART
+        if best is not None:
+            cost, g, D = best
+        # the next backward differentiates the accepted point: the last forward was a trial
+        _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
         history.append(cost)
         if callback:
             callback(it, cost, lam)

@@ -235,6 +235,15 @@ tp_status tp_set_lpf(tp_handle *h, const float *lpf);
  * One bit per colour (0..2^num_colors - 1); default 0 (the CPU path's unfiltered CLT); it takes
  * effect only while tp_set_lpf has a filter set. */
 tp_status tp_set_clt_lpf_mask(tp_handle *h, int lpf_mask);
+/* GPU_DTT24_DRV (dtt8x8.cuh:100-158, the reference's kernel for testing and profiling the
+ * transforms alone): every 8x8 block of a float image in device memory through one 2D transform,
+ * rows first (horizontal: DST if bit 0 of dtt_mode is set, else DCT), then columns (vertical:
+ * bit 1); modes 0-3 DCT-IV / DST-IV, 4-7 DCT-II / DST-II, all orthonormal as DttRad2.dct_iv /
+ * dst_iv / dct_ii.  dst and src (device pointers, dst may equal src) share src_stride (floats);
+ * width and height are multiples of 8.  Enqueued on stream (NULL: the default stream); the first
+ * call on a device uploads the transform tables (a synchronous copy). */
+tp_status tp_dtt8x8(float *dst, const float *src, int src_stride, int width, int height, int dtt_mode,
+                    void *stream);
 /* correlation set-up (ImageDtt.clt_aberrations_quad_corr_new arguments, ImageDtt.java:1491-1546) */
 tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pairs, int num_pairs);
 /* texture set-up; the LPF and colour weights are those of tp_set_corr */

@@ -60,6 +60,8 @@ def lib():
         L.or_dct_iv8.argtypes = [_dp, _dp]
         L.or_dst_iv8.argtypes = [_dp, _dp]
         L.or_dct_ii8.argtypes = [_dp, _dp]
+        L.or_dst_ii8.argtypes = [_dp, _dp]
+        L.or_dtt24.argtypes = [_dp, _dp, C.c_int]
         L.or_dctiv_direct.argtypes = [_dp, _dp]
         for f in (L.or_dttt_iv, L.or_dttt_iie, L.or_dttt_iiie):
             f.argtypes = [_dp, _dp, C.c_int]
@@ -141,6 +143,7 @@ def _vec8(fn, x):
 def dct_iv8(x): return _vec8(lib().or_dct_iv8, x)
 def dst_iv8(x): return _vec8(lib().or_dst_iv8, x)
 def dct_ii8(x): return _vec8(lib().or_dct_ii8, x)
+def dst_ii8(x): return _vec8(lib().or_dst_ii8, x)
 def dctiv_direct(x): return _vec8(lib().or_dctiv_direct, x)
 
 
@@ -154,6 +157,22 @@ def _dttt(fn, x, mode):
 def dttt_iv(x, mode): return _dttt(lib().or_dttt_iv, x, mode)
 def dttt_iie(x, mode): return _dttt(lib().or_dttt_iie, x, mode)
 def dttt_iiie(x, mode): return _dttt(lib().or_dttt_iiie, x, mode)
+
+
+def dtt24_image(img, mode):
+    """GPU_DTT24_DRV (dtt8x8.cuh:100-158) on a float image: every 8x8 block transformed in place
+    (rows, then columns; mode 0-3 DCT-IV / DST-IV, 4-7 DCT-II / DST-II)"""
+    a = _f64(img)
+    h, w = a.shape
+    out = np.zeros((h, w))
+    fn = lib().or_dtt24
+    for by in range(0, h, 8):
+        for bx in range(0, w, 8):
+            x = np.ascontiguousarray(a[by:by + 8, bx:bx + 8]).reshape(64)
+            y = np.zeros(64)
+            fn(_d(x), _d(y), int(mode))
+            out[by:by + 8, bx:bx + 8] = y.reshape(8, 8)
+    return out
 
 
 def hwindow():

@@ -45,6 +45,21 @@ class RefGpu:
         self._ck(self.cu.cuMemcpyDtoH_v2(out.ctypes.data_as(C.c_void_p), ptr, C.c_size_t(count * 4)), "dtoh")
         return out
 
+    def dtt24(self, img, mode):
+        """GPU_DTT24_DRV (dtt8x8.cuh:100-158) on a float image whose width is a multiple of 32 and
+        height of 16 (the kernel's 32x16-pixel blocks of 8x4x2 threads)"""
+        torch = self.torch
+        fn = C.c_void_p()
+        self._ck(self.cu.cuModuleGetFunction(C.byref(fn), self.mod, b"GPU_DTT24_DRV"), "getfn")
+        h, w = img.shape
+        src = torch.from_numpy(np.ascontiguousarray(img, dtype=np.float32)).to("cuda")
+        dst = torch.zeros_like(src)
+        torch.cuda.synchronize()
+        self._launch(fn, (w // 32, h // 16, 1), (8, 4, 2),
+                     [C.c_uint64(dst.data_ptr()), C.c_uint64(src.data_ptr()), C.c_int(w), C.c_int(mode)])
+        self._ck(self.cu.cuCtxSynchronize(), "sync")
+        return dst.cpu().numpy()
+
     def _launch(self, fn, grid, block, args):
         holders = []
         ptrs = (C.c_void_p * len(args))()

@@ -191,6 +191,34 @@ void or_dct_ii8(const double *x, double *y) {  /* dct_ii (68-78) */
   for (int i = 0; i < 8; i++) y[i] *= scale;
 }
 
+/* DST-II as the reference GPU computes it (dttii_shared_mem with dst_not_dct, dtt8x8.cuh:296-378):
+ * the DCT-II of the input with its odd samples negated, output in reverse order */
+void or_dst_ii8(const double *x, double *y) {
+  double xs[8], t[8];
+  for (int i = 0; i < 8; i++) xs[i] = (i & 1) ? -x[i] : x[i];
+  or_dct_ii8(xs, t);
+  for (int i = 0; i < 8; i++) y[i] = t[7 - i];
+}
+
+/* GPU_DTT24_DRV (dtt8x8.cuh:100-158) on one 8x8 block, row-major in and out: every row
+ * transformed (horizontal pass: DCT if bit 0 of mode is clear, else DST), then every column
+ * (vertical pass: bit 1); modes 0-3 DCT-IV / DST-IV (DttRad2.dct_iv / dst_iv), 4-7 DCT-II /
+ * DST-II (DttRad2.dct_ii and its DST counterpart above) */
+void or_dtt24(const double *x, double *y, int mode) {
+  void (*fc)(const double *, double *) = (mode > 3) ? or_dct_ii8 : or_dct_iv8;
+  void (*fs)(const double *, double *) = (mode > 3) ? or_dst_ii8 : or_dst_iv8;
+  double tmp[64], line[8], out[8];
+  for (int r = 0; r < 8; r++) {
+    ((mode & 1) ? fs : fc)(x + 8 * r, out);
+    memcpy(tmp + 8 * r, out, sizeof(out));
+  }
+  for (int c = 0; c < 8; c++) {
+    for (int r = 0; r < 8; r++) line[r] = tmp[8 * r + c];
+    ((mode & 2) ? fs : fc)(line, out);
+    for (int r = 0; r < 8; r++) y[8 * r + c] = out[r];
+  }
+}
+
 static void mat8(const double m[8][8], const double *x, double *y) {
   for (int i = 0; i < 8; i++) {
     y[i] = 0.0;

@@ -57,6 +57,10 @@ enum {
 void or_dct_iv8(const double *x, double *y);           /* DttRad2.dct_iv   (80-85)  */
 void or_dst_iv8(const double *x, double *y);           /* DttRad2.dst_iv   (87-98)  */
 void or_dct_ii8(const double *x, double *y);           /* DttRad2.dct_ii   (68-78)  */
+void or_dst_ii8(const double *x, double *y);           /* dtt8x8.cuh dttii_shared_mem, DST (296-378) */
+/* GPU_DTT24_DRV (dtt8x8.cuh:100-158) on one row-major 8x8 block: rows (bit 0 of mode: DST), then
+ * columns (bit 1); modes 0-3 DCT-IV / DST-IV, 4-7 DCT-II / DST-II */
+void or_dtt24(const double *x, double *y, int mode);
 /* mode bit0: horizontal sine, bit1: vertical sine; output transposed */
 void or_dttt_iv(const double *x, double *y, int mode);   /* DttRad2.dttt_iv   (503-519) */
 void or_dttt_iie(const double *x, double *y, int mode);  /* DttRad2.dttt_iie  (595-614) */

@@ -21,6 +21,11 @@ writes the same inputs with the CLT of lpf_mask = 7, the mask GPUTileProcessor.
 execConverCorrectTiles passes (GPUTileProcessor.java:547): each colour's stored
 CLT multiplied by the module's lpf_data table (TileProcessor.cuh:1037-1061),
 which is saved too.
+
+    python tests/golden/make_ref_gpu_golden.py OUT.npz --dtt
+
+runs the reference's transform test kernel GPU_DTT24_DRV (dtt8x8.cuh:100-158) on a seeded 64x32
+image in its eight modes (DCT-IV / DST-IV and DCT-II / DST-II, rows then columns).
 """
 import os
 import sys
@@ -79,6 +84,21 @@ def make_inputs(seed=2024):
                 tasks=tasks, tx=txs, ty=tys, xy=xy)
 
 
+def main_dtt(out):
+    """GPU_DTT24_DRV, the reference's transform test kernel (dtt8x8.cuh:100-158), on a seeded
+    64x32 image in all eight modes"""
+    from oracle import build_ref_gpu
+    from oracle.ref_gpu import RefGpu
+    rng = np.random.default_rng(77)
+    yy, xx = np.mgrid[0:32, 0:64]
+    img = (rng.normal(size=(32, 64)) + np.sin(xx / 3.0) * np.cos(yy / 5.0) + 0.01 * xx).astype(np.float32)
+    ref = RefGpu(build_ref_gpu.cubin_path(W, H), W, H)
+    outs = np.stack([ref.dtt24(img, m) for m in range(8)])
+    np.savez_compressed(out, src=img, ref_dtt=outs,
+                        note="reference GPU_DTT24_DRV (dtt8x8.cuh) compiled for sm_103a, modes 0-7")
+    print("wrote", out, "absmax", np.abs(outs).max())
+
+
 def main(out, lpf=False):
     from oracle import build_ref_gpu
     from oracle.ref_gpu import RefGpu
@@ -107,4 +127,7 @@ def main(out, lpf=False):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(args[0] if args else "ref_gpu_128x96.npz", lpf="--lpf" in sys.argv)
+    if "--dtt" in sys.argv:
+        main_dtt(args[0] if args else "ref_gpu_dtt24.npz")
+    else:
+        main(args[0] if args else "ref_gpu_128x96.npz", lpf="--lpf" in sys.argv)

@@ -171,3 +171,58 @@ def test_gb300_lpf_mask_matches_reference_gpu(oracle, tp_lib):
         assert np.array_equal(tp.getCorr(), corr0)  # the correlation reads the unfiltered CLT
         with pytest.raises(_lib.TpError):
             tp.execTextures()
+
+
+GOLD_DTT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu_dtt24.npz")
+DTT_TOL = 1e-5  # relative L2 per 8x8 block: the reference's 6-digit FP32 constants against FP64 / our FP32
+
+
+def _load_dtt():
+    if not os.path.exists(GOLD_DTT):
+        pytest.skip("golden file not generated")
+    return dict(np.load(GOLD_DTT))
+
+
+def _block_rel_l2(got, want):
+    h, w = want.shape
+    g = got.reshape(h // 8, 8, w // 8, 8).swapaxes(1, 2).reshape(-1, 64).astype(np.float64)
+    r = want.reshape(h // 8, 8, w // 8, 8).swapaxes(1, 2).reshape(-1, 64).astype(np.float64)
+    return np.sqrt(((g - r) ** 2).sum(1) / (r ** 2).sum(1))
+
+
+def test_oracle_matches_reference_gpu_dtt24(oracle):
+    """The oracle's 2D transforms (DttRad2.dct_iv / dst_iv / dct_ii and the GPU's DST-II, rows then
+    columns) against the reference GPU_DTT24_DRV in all eight modes."""
+    g = _load_dtt()
+    for mode in range(8):
+        e = _block_rel_l2(oracle.dtt24_image(g["src"], mode), g["ref_dtt"][mode])
+        assert e.max() < DTT_TOL, "mode %d: oracle vs reference GPU_DTT24_DRV rel L2 max %.3g" % (mode, e.max())
+
+
+@pytest.mark.gpu
+def test_gb300_dtt8x8_matches_reference_gpu(oracle, tp_lib):
+    """tp_dtt8x8 (through the C ABI, device buffers) against the reference GPU_DTT24_DRV and the oracle
+    in all eight modes, out of place and in place; sizes that are not multiples of 8 are refused."""
+    import ctypes as C
+    import torch
+    from tileproc import _lib
+    L = _lib.load()
+    g = _load_dtt()
+    src = torch.from_numpy(np.ascontiguousarray(g["src"])).cuda()
+    h, w = src.shape
+    for mode in range(8):
+        dst = torch.zeros_like(src)
+        assert L.tp_dtt8x8(C.c_void_p(dst.data_ptr()), C.c_void_p(src.data_ptr()), w, w, h, mode, None) == 0
+        torch.cuda.synchronize()
+        got = dst.cpu().numpy()
+        e = _block_rel_l2(got, g["ref_dtt"][mode])
+        assert e.max() < DTT_TOL, "mode %d: GB300 vs reference GPU_DTT24_DRV rel L2 max %.3g" % (mode, e.max())
+        e = _block_rel_l2(got, oracle.dtt24_image(g["src"], mode))
+        assert e.max() < DTT_TOL, "mode %d: GB300 vs oracle rel L2 max %.3g" % (mode, e.max())
+        inplace = src.clone()
+        assert L.tp_dtt8x8(C.c_void_p(inplace.data_ptr()), C.c_void_p(inplace.data_ptr()), w, w, h, mode, None) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(inplace.cpu().numpy(), got)
+    dst = torch.zeros_like(src)
+    assert L.tp_dtt8x8(C.c_void_p(dst.data_ptr()), C.c_void_p(src.data_ptr()), w, w - 4, h, 0, None) == _lib.TP_ERR_ARG
+    assert L.tp_dtt8x8(C.c_void_p(dst.data_ptr()), C.c_void_p(src.data_ptr()), w, w, h, 8, None) == _lib.TP_ERR_ARG
