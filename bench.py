@@ -348,7 +348,7 @@ def measure_fwd_adjoint(seed, steps, warmup, lma_iterations=20):
 
         out["lma"] = {"iterations": lma_iterations, "cost_start": hist[0], "cost_end": hist[-1],
                       "cost_at_truth": cost_truth, "valid_tiles_start": valid["start"], "valid_tiles_end": valid["end"],
-                      "cost": "sum over tiles of d^2 (px^2), 1 px^2 for a tile without a correlation peak",
+                      "cost": "sum over tiles of min(d^2, 1) (px^2), 1 px^2 for a tile without a correlation peak",
                       "seconds": secs,
                       "start": "extrinsics + N(0, 3e-3) rad on all 16 sensors, target disparity = scene truth "
                                "(held fixed: free_disparity=False)",

@@ -22,7 +22,12 @@ extrinsics alone are fitted.
 Two things make the iteration robust far from the solution, where ports are
 off by a pixel or more:
 - A tile without a correlation peak (NaN disparity) counts invalid_cost px^2
-  in the cost, so a step cannot lower the cost by losing tiles.
+  in the cost, so a step cannot lower the cost by losing tiles; and a tile's
+  d^2 counts at most invalid_cost (a truncated square), with the tiles past it
+  left out of the normal equations.  Without the cap a tile whose peak is on
+  the edge of existing, with a residual of a few pixels, makes every step a
+  dead end: the smallest move (1e-9 rad was measured) brings its peak back and
+  adds its d^2 to the cost.
 - There the measured disparity responds more weakly than its local
   derivative says (the smeared peak of the combined strip saturates), and the
   Gauss-Newton step falls short. An accepted step is therefore doubled while
@@ -35,15 +40,18 @@ import numpy as np
 KEYS = ("azimuth", "tilt", "roll", "zoom")
 
 
-def _evaluate(tp, geometry, disparity, tile_op, invalid_cost=0.0):
-    """(d, ok, cost): cost = sum of d^2 over the tiles with a peak + invalid_cost per tile without"""
+def _evaluate(tp, geometry, disparity, tile_op, invalid_cost=None):
+    """(d, ok, cost): cost = sum over the tiles with a peak of d^2, capped at invalid_cost, plus
+    invalid_cost per tile without a peak (invalid_cost None: plain sum of d^2 over the tiles with one)"""
     tp.setGeometry(geometry)
     tp.setFullFrameImages(disparity, tile_op=tile_op)
     tp.process()
     d = tp.getDisparity()[:, 1].astype(np.float64)
     ok = np.isfinite(d) & (tile_op != 0)
+    if invalid_cost is None:
+        return d, ok, float(np.sum(np.where(ok, d * d, 0.0)))
     lost = int(np.count_nonzero((tile_op != 0) & ~ok))
-    return d, ok, float(np.sum(np.where(ok, d * d, 0.0))) + invalid_cost * lost
+    return d, ok, float(np.sum(np.where(ok, np.minimum(d * d, invalid_cost), 0.0))) + invalid_cost * lost
 
 
 # largest change of a tile's target disparity in one step, px: beyond about a pixel the
@@ -69,8 +77,8 @@ STALL_SCALES = (2.0, 4.0, 8.0, 0.5, 0.25)
 def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART, free_disparity=True,
            fixed_sensor=None, callback=None, invalid_cost=1.0, expand=True):
     """Runs `iterations` LM steps; returns (geometry, disparity, history) where history
-    holds the cost (sum d^2 over tiles with a peak, plus invalid_cost per tile without one)
-    before each step and after the last; it never increases.  The per-tile disparity steps are
+    holds the cost (sum over tiles with a peak of min(d^2, invalid_cost), plus invalid_cost per
+    tile without one) before each step and after the last; it never increases.  The per-tile disparity steps are
     clipped to +-MAX_DISPARITY_STEP (a tile whose disparity derivative is close to zero would
     otherwise take an unbounded step).  With expand an accepted step is doubled while that lowers
     the cost, up to 8 times its length.  The cost is only piecewise smooth (window corners move
@@ -88,6 +96,8 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART
         tp.backward()
         je, jd, dv = tp.getDisparityJacobian()
         ok = np.isfinite(dv) & (op != 0)
+        if invalid_cost is not None:  # past the cap the truncated square is flat
+            ok &= np.where(ok, dv, 0.0) ** 2 < invalid_cost
         r = np.where(ok, dv, 0.0).astype(np.float64)
         A = np.where(ok[:, None], je.reshape(T, S * 4), 0.0).astype(np.float64)
         b = np.where(ok, jd, 0.0).astype(np.float64)

@@ -216,8 +216,8 @@ def test_recorded_strip_samples_match_reinterpolation(oracle):
 
 def test_lma_reduces_cost(oracle):
     """Levenberg-Marquardt on the analytic Jacobian from extrinsics perturbed by N(0, 3e-3) rad on the
-    160x128 crop, target disparities at the scene truth (free_disparity=False): the cost (1 px^2 for
-    a tile without a peak) falls at every step and to below half.  The crop's 320 tiles do not pin
+    160x128 crop, target disparities at the scene truth (free_disparity=False): the cost (d^2 capped
+    at 1 px^2, 1 px^2 for a tile without a peak) falls at every step and to below half.  The crop's 320 tiles do not pin
     the 64 extrinsics (the fit lowers the cost without approaching the truth); the full scene does,
     test_lma_recovers_extrinsics_full_scene."""
     from tileproc import lma
