@@ -139,6 +139,7 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
     float pw[4] = {0.f, 0.f, 0.f, 0.f}, avg[3] = {0.f, 0.f, 0.f}, sc_w = 1.f;
     if (used > 1) {
       // pair weights: Gaussian of the weighted colour difference, scaled by the pair distance
+      const float ks = ksigma * rlw2, ksd = 0.5f * ks;
       float ea[6];
       float amin = CUDART_INF_F;
 #pragma unroll
@@ -148,14 +149,13 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
           ea[k] = CUDART_INF_F;
           if ((mask >> a) & (mask >> b) & 1) {
             // squared port distance: 1 for side pairs, 2 for the diagonals (0,3) and (1,2)
-            const float pd = (a + b == 3) ? 0.5f * ksigma : ksigma;
             float dd = 0.f;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
               const float dc = d[a][c] - d[b][c];
               dd = fmaf(tc.col_weights[c] * dc, dc, dd);
             }
-            ea[k] = pd * (dd * rlw2);
+            ea[k] = ((a + b == 3) ? ksd : ks) * dd;
             amin = fminf(amin, ea[k]);
           }
         }
@@ -183,13 +183,11 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
 #pragma unroll
         for (int ip = 0; ip < 4; ip++) { if (ip == b1) p1 = pw[ip]; if (ip == b2) p2 = pw[ip]; }
         const float wa = __fdividef(p1, p1 + p2), wb = 1.0f - wa;
+        float wv[4];  // the best pair's weights as a vector over the ports (the others 0)
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-          float v1 = 0.f, v2 = 0.f;
+        for (int ip = 0; ip < 4; ip++) wv[ip] = (ip == b1) ? wa : ((ip == b2) ? wb : 0.f);
 #pragma unroll
-          for (int ip = 0; ip < 4; ip++) { if (ip == b1) v1 = d[ip][c]; if (ip == b2) v2 = d[ip][c]; }
-          avg[c] = wa * v1 + wb * v2;
-        }
+        for (int c = 0; c < 3; c++) avg[c] = fmaf(wv[3], d[3][c], fmaf(wv[2], d[2][c], fmaf(wv[1], d[1][c], wv[0] * d[0][c])));
         // re-weight every used port by its distance from the best-pair average
         float eb[4], bmin = CUDART_INF_F;
 #pragma unroll
@@ -200,7 +198,7 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
             const float dc = d[ip][c] - avg[c];
             d2 = fmaf(tc.col_weights[c] * dc, dc, d2);
           }
-          eb[ip] = ksigma * (d2 * rlw2);
+          eb[ip] = ks * d2;
           if (mask & (1 << ip)) bmin = fminf(bmin, eb[ip]);
         }
         const bool zero = bmin > TX_EXP_UNDERFLOW;  // all weights 0 in double
