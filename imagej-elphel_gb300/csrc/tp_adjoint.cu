@@ -1,4 +1,4 @@
-// tp_adjoint.cu -- hand-written adjoint of the forward chain for mono sensors.
+// tp_adjoint.cu -- hand-written adjoint of the forward chain (mono and Bayer colour sensors).
 //
 // For every tile the centroid disparity d (getMaxXCm over the combined strip,
 // Correlation2d.java:936-1032) is a function of the residual shifts (rx, ry)
@@ -36,7 +36,7 @@ namespace {
 constexpr float K16 = 0.19634954084936207f;  // pi / 16
 
 struct AdjShape {
-  int S, P, RE;
+  int S, C, P, RE;
   int per_warp;   // floats of shared memory per warp
   int recompute;  // 1: recompute the CLT from the image instead of reading it back
   int use_strips; // 1: the forward recorded its per-pair strip samples in sc.strips
@@ -114,16 +114,29 @@ __device__ __forceinline__ void convolve_t(float o[4][8], const float *kp, int r
   }
 }
 
-__device__ __forceinline__ Win make_win(const SceneDev &sc, const SubtilePlan &p, int s) {
+__device__ __forceinline__ Win make_win(const SceneDev &sc, const SubtilePlan &p, int s, int c = 0) {
   Win w;
   w.img = sc.images[s];
   w.pitch = sc.img_pitch;
   w.tlx = p.tlx; w.tly = p.tly; w.W = sc.width; w.H = sc.height;
   w.u16 = sc.img_dtype[s];
   w.inside = (p.tlx >= 0) && (p.tly >= 0) && (p.tlx <= sc.width - 16) && (p.tly <= sc.height - 16);
-  w.scale = sc.color_scale[0];
+  w.scale = sc.color_scale[c];
   return w;
 }
+
+// one colour plane of a Bayer mosaic seen through a window: the mosaic's pixels of colour c
+// (0 red, 1 blue, 2 green, on the Bayer phase (red row, red column)), zero elsewhere -- the
+// sparse plane the forward transforms (the mirrored border keeps the pixel parity)
+struct BayerWin {
+  Win w;
+  int c, rr, rc;
+  __device__ __forceinline__ float at(int row, int col) const {
+    const bool ry = ((w.tly + row) & 1) == rr, rx = ((w.tlx + col) & 1) == rc;
+    const bool keep = (c == 0) ? (ry && rx) : ((c == 1) ? (!ry && !rx) : (ry != rx));
+    return keep ? w.at(row, col) : 0.f;
+  }
+};
 
 // taps of one strip sample (sample_code / strip_sample): returns the tap count
 __device__ __forceinline__ int code_taps(int code, int idx[4], float wt[4]) {
@@ -178,6 +191,98 @@ __device__ __forceinline__ float strip_entry(const float *c, const short *strip_
 
 constexpr int AD_NW = 4;  // warps per tile
 
+// dd/d(port x, port y) of one (sensor, colour) sub-tile, 8-lane group (lane r holds row r):
+// the dd/dCLT gl of the sub-tile is taken back once through the phase rotation, the kernel
+// convolution and the 2D DCT-IV/DST-IV (symmetric transforms: the transpose runs through the same
+// butterflies) to the folded tile, which is dotted with the fold of the pixels under the
+// derivative window, one fold per direction, plus the rotation's own derivative.  gl is
+// overwritten (with the folded gradient) where `own` is set.  Result in out[] of every lane.
+template <typename PIX>
+__device__ __forceinline__ void shift_sens(const SceneDev &sc, const PIX &w, const SubtilePlan &p, int s,
+                                           const float *clt, float *gl_all, float *tbq, int r, bool own,
+                                           float out[2]) {
+  const float *kp = (p.kidx >= 0) ? sc.kernels[s] + (size_t)p.kidx * TP_CLT : nullptr;
+  float ahs, ahc, avs, avc;
+  __sincosf(CUDART_PI_F * 0.0625f * p.rx, &ahs, &ahc);
+  __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
+  const FoldIdx fv = fold_idx(r);
+  const float *cl = clt + r * 8, *gl = gl_all + r * 8;
+  // the rotation's own derivative (pi/16 (2k+1) x the CLT turned by 90 degrees) dotted with dd/dCLT
+  float gdir[2] = {0.f, 0.f};
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const float c0 = cl[v], c1 = cl[64 + v], c2 = cl[128 + v], c3 = cl[192 + v];
+    const float g0 = gl[v], g1 = gl[64 + v], g2 = gl[128 + v], g3 = gl[192 + v];
+    const float fx = K16 * (2 * r + 1), fy = K16 * (2 * v + 1);
+    gdir[0] = fmaf(fx, (g1 * c0 - g0 * c1) + (g3 * c2 - g2 * c3), gdir[0]);
+    gdir[1] = fmaf(fy, (g2 * c0 - g0 * c2) + (g3 * c1 - g1 * c3), gdir[1]);
+  }
+  float *gfs = gl_all + r * 8;  // gfs[m * 64 + j] for folded row r
+  {
+    float gf[4][8];
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+      for (int v = 0; v < 8; v++) gf[m][v] = gl[m * 64 + v];
+    rotate_t(gf, p.rx, p.ry, r);
+    convolve_t(gf, kp, r);
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      float u[8];
+      dtt4_fast(gf[m], u, (m >> 1) & 1);
+      group_transpose(u, tbq, r);
+      dtt4_fast(u, gf[m], m & 1);
+    }
+    if (own) {
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int j2 = 0; j2 < 8; j2++) gfs[m * 64 + j2] = gf[m][j2];
+    }
+  }
+  __syncwarp();
+  // per direction: the fold with the derivative window dotted with the folded gradient
+#pragma unroll
+  for (int dir = 0; dir < 2; dir++) {
+    float vw0, vw1, hw0[8], hw1[8];
+    if (dir == 0) fold_weights(-K16 * ahs, K16 * ahc, avc, avs, fv, vw0, vw1, hw0, hw1);
+    else fold_weights(ahc, ahs, -K16 * avs, K16 * avc, fv, vw0, vw1, hw0, hw1);
+    float acc = 0.f;
+#pragma unroll
+    for (int vb = 0; vb < 2; vb++) {
+      const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
+      float vc[16];
+#pragma unroll
+      for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+#pragma unroll
+      for (int hb = 0; hb < 2; hb++)
+#pragma unroll
+        for (int j2 = 0; j2 < 8; j2++) {
+          const FoldIdx fh = fold_idx(j2);
+          const float h0 = (hb ? fh.ss0 : fh.sc0) * hw0[j2], h1 = (hb ? fh.ss1 : fh.sc1) * hw1[j2];
+          acc = fmaf(fmaf(h1, vc[fh.src1], h0 * vc[fh.src0]), gfs[(vb * 2 + hb) * 64 + j2], acc);
+        }
+    }
+    gdir[dir] += acc;
+  }
+#pragma unroll
+  for (int dir = 0; dir < 2; dir++) {
+    gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 1);
+    gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 2);
+    gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 4);
+  }
+  // residual = TL - px: dd/dpx = -dd/drx; the kernel-centre offsets add the dependence of px, py
+  // on the port through kdx, kdy (ImageDtt.java:4930-4939)
+  const float gpx = -gdir[0], gpy = -gdir[1];
+  out[0] = gpx;
+  out[1] = gpy;
+  if (p.kidx >= 0) {
+    const float4 e1 = __ldg((const float4 *)(sc.kext[s] + (size_t)p.kidx * 8) + 1);
+    out[0] = gpx * (1.0f - e1.x) - gpy * e1.z;
+    out[1] = -gpx * e1.y + gpy * (1.0f - e1.w);
+  }
+}
+
 // x = T^T y for the DCT-IIe / DST-IIe of dtt2e_fast (its transposed data flow)
 __device__ __forceinline__ void dtt2e_transposed(const float y[8], float x[8], bool sine) {
   const float S = 0.5f;
@@ -209,11 +314,12 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
                                                              float *dval) {
   extern __shared__ float sm[];
   __shared__ float s_d;
+  __shared__ float s_sens[2 * TP_MAXS * 3];  // dd/d(port x, y) of every (sensor, colour)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = lane >> 3, r = lane & 7;
-  const int S = as.S, P = as.P, RE = as.RE;
-  float *s_clt = sm;                  // [S][256]
-  float *s_g = s_clt + S * TP_CLT;    // [S][256] dd/dCLT
-  float *gcmb = s_g + S * TP_CLT;     // [240] dd/dcombo
+  const int S = as.S, C = as.C, P = as.P, RE = as.RE;
+  float *s_clt = sm;                      // [S][C][256]
+  float *s_g = s_clt + S * C * TP_CLT;    // [S][C][256] dd/dCLT
+  float *gcmb = s_g + S * C * TP_CLT;     // [240] dd/dcombo
   float *gG = gcmb + 240;             // [240] combo + offset
   float *gs = gG + 240 + warp * 816;  // per warp: [240] dd/dsurface of the current pair
   float *qb = gs + 240;               // [4][72] quadrant buffer
@@ -249,10 +355,10 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
         }
       }
     } else {
-      const float4 *src = (const float4 *)(sc.clt + tile * S * TP_CLT);
-      for (int i = tid; i < S * 64; i += 32 * AD_NW) ((float4 *)s_clt)[i] = __ldg(src + i);
+      const float4 *src = (const float4 *)(sc.clt + tile * S * C * TP_CLT);
+      for (int i = tid; i < S * C * 64; i += 32 * AD_NW) ((float4 *)s_clt)[i] = __ldg(src + i);
     }
-    for (int i = tid; i < S * TP_CLT; i += 32 * AD_NW) s_g[i] = 0.f;
+    for (int i = tid; i < S * C * TP_CLT; i += 32 * AD_NW) s_g[i] = 0.f;
 
     // ---------------- centroid of the forward's combined strip, and dd/dcombo ----------------
     if (warp == 0) {
@@ -399,167 +505,116 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
         for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];
         __syncwarp();
       }
-      // LPF and the fat-zero normalised product (correlateSingleColorFD)
-      const float *c1 = s_clt + (size_t)pd.cam1 * TP_CLT, *c2 = s_clt + (size_t)pd.cam2 * TP_CLT;
-      float d1[4][2], d2[4][2], a2[2], ia2[2], s1v[2], s2v[2];
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        float s1 = 0.f, s2 = 0.f;
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-          d1[m][h] = c1[m * 64 + lane + 32 * h];
-          d2[m][h] = c2[m * 64 + lane + 32 * h];
-          s1 = fmaf(d1[m][h], d1[m][h], s1);
-          s2 = fmaf(d2[m][h], d2[m][h], s2);
-        }
-        // |d1| |d2| with the forward's approximate square root; ia2 = 1 / a2 (0 where a2 = 0)
-        const float pr = s1 * s2;
-        ia2[h] = (pr > 0.0f) ? rsqrtf(pr) : 0.0f;
-        a2[h] = pr * ia2[h];
-        s1v[h] = s1;
-        s2v[h] = s2;
-      }
-      const float fzz = cfg.fat_zero * cfg.fat_zero;
-      const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
-      float tg[4][2], dbar[2];
+      // LPF, colour mix and the fat-zero normalised product of each colour
+      // (correlateSingleColorFD / correlateCompositeFD): acc = sum_c w_c t_c / (a2_c + fz2_c)
+      float gq[4][2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const int idx = lane + 32 * h;
         const float l = cfg.lpf[idx];
         const int off = (idx >> 3) * 9 + (idx & 7);
-        float gq[4];
 #pragma unroll
-        for (int qq = 0; qq < 4; qq++) gq[qq] = qb[qq * 72 + off] * l;
-        const float sw = __fdividef(1.0f, a2[h] + fz2);
-        const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
-        const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
-        const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
-        const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
-        const float swbar = gq[0] * t0 + gq[1] * t1 + gq[2] * t2 + gq[3] * t3;
-        dbar[h] = -swbar * sw * sw;
-#pragma unroll
-        for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq] * sw;
+        for (int qq = 0; qq < 4; qq++) gq[qq][h] = qb[qq * 72 + off] * l;
       }
-      const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
+      const float fzz = cfg.fat_zero * cfg.fat_zero;
+      for (int c = 0; c < C; c++) {
+        const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
+        const float *c1 = s_clt + ((size_t)pd.cam1 * C + c) * TP_CLT, *c2 = s_clt + ((size_t)pd.cam2 * C + c) * TP_CLT;
+        float d1[4][2], d2[4][2], a2[2], ia2[2], s1v[2], s2v[2];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int idx = lane + 32 * h;
-        const float a2bar = dbar[h] + dsum;
-        const float T0 = tg[0][h], T1 = tg[1][h], T2 = tg[2][h], T3 = tg[3][h];
-        float g1[4], g2[4];
-        g1[0] = T0 * d2[0][h] + T1 * d2[1][h] + T2 * d2[2][h] + T3 * d2[3][h];
-        g1[1] = T0 * d2[1][h] - T1 * d2[0][h] + T2 * d2[3][h] - T3 * d2[2][h];
-        g1[2] = T0 * d2[2][h] + T1 * d2[3][h] - T2 * d2[0][h] - T3 * d2[1][h];
-        g1[3] = T0 * d2[3][h] - T1 * d2[2][h] - T2 * d2[1][h] + T3 * d2[0][h];
-        g2[0] = T0 * d1[0][h] - T1 * d1[1][h] - T2 * d1[2][h] + T3 * d1[3][h];
-        g2[1] = T0 * d1[1][h] + T1 * d1[0][h] - T2 * d1[3][h] - T3 * d1[2][h];
-        g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
-        g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
-        // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
-        const float k1 = a2bar * s2v[h] * ia2[h];
-        const float k2 = a2bar * s1v[h] * ia2[h];
+        for (int h = 0; h < 2; h++) {
+          float s1 = 0.f, s2 = 0.f;
 #pragma unroll
-        for (int m = 0; m < 4; m++) {
-          atomicAdd(&s_g[pd.cam1 * TP_CLT + m * 64 + idx], fmaf(k1, d1[m][h], g1[m]));
-          atomicAdd(&s_g[pd.cam2 * TP_CLT + m * 64 + idx], fmaf(k2, d2[m][h], g2[m]));
+          for (int m = 0; m < 4; m++) {
+            d1[m][h] = c1[m * 64 + lane + 32 * h];
+            d2[m][h] = c2[m * 64 + lane + 32 * h];
+            s1 = fmaf(d1[m][h], d1[m][h], s1);
+            s2 = fmaf(d2[m][h], d2[m][h], s2);
+          }
+          // |d1| |d2| with the forward's approximate square root; ia2 = 1 / a2 (0 where a2 = 0)
+          const float pr = s1 * s2;
+          ia2[h] = (pr > 0.0f) ? rsqrtf(pr) : 0.0f;
+          a2[h] = pr * ia2[h];
+          s1v[h] = s1;
+          s2v[h] = s2;
+        }
+        const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
+        float tg[4][2], dbar[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const float u = __fdividef(1.0f, a2[h] + fz2);
+          const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
+          const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
+          const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
+          const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
+          const float swbar = gq[0][h] * t0 + gq[1][h] * t1 + gq[2][h] * t2 + gq[3][h] * t3;
+          dbar[h] = -wgt * swbar * u * u;
+          const float sw = wgt * u;
+#pragma unroll
+          for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq][h] * sw;
+        }
+        const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
+        float *g1p = s_g + ((size_t)pd.cam1 * C + c) * TP_CLT, *g2p = s_g + ((size_t)pd.cam2 * C + c) * TP_CLT;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int idx = lane + 32 * h;
+          const float a2bar = dbar[h] + dsum;
+          const float T0 = tg[0][h], T1 = tg[1][h], T2 = tg[2][h], T3 = tg[3][h];
+          float g1[4], g2[4];
+          g1[0] = T0 * d2[0][h] + T1 * d2[1][h] + T2 * d2[2][h] + T3 * d2[3][h];
+          g1[1] = T0 * d2[1][h] - T1 * d2[0][h] + T2 * d2[3][h] - T3 * d2[2][h];
+          g1[2] = T0 * d2[2][h] + T1 * d2[3][h] - T2 * d2[0][h] - T3 * d2[1][h];
+          g1[3] = T0 * d2[3][h] - T1 * d2[2][h] - T2 * d2[1][h] + T3 * d2[0][h];
+          g2[0] = T0 * d1[0][h] - T1 * d1[1][h] - T2 * d1[2][h] + T3 * d1[3][h];
+          g2[1] = T0 * d1[1][h] + T1 * d1[0][h] - T2 * d1[3][h] - T3 * d1[2][h];
+          g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
+          g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
+          // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
+          const float k1 = a2bar * s2v[h] * ia2[h];
+          const float k2 = a2bar * s1v[h] * ia2[h];
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            atomicAdd(&g1p[m * 64 + idx], fmaf(k1, d1[m][h], g1[m]));
+            atomicAdd(&g2p[m * 64 + idx], fmaf(k2, d2[m][h], g2[m]));
+          }
         }
       }
       __syncwarp();
     }
     __syncthreads();
 
-    // ---------------- dd/drx, dd/dry per sensor (forward mode on the CLT) ----------------
-    for (int g = warp; g < groups; g += AD_NW) {
-      const int s = g * 4 + q;
-      const int sidx = s < S ? s : S - 1;
-      const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
-      const Win w = make_win(sc, p, sidx);
-      const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
-      float ahs, ahc, avs, avc;
-      __sincosf(CUDART_PI_F * 0.0625f * p.rx, &ahs, &ahc);
-      __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
-      const FoldIdx fv = fold_idx(r);
-      const float *cl = s_clt + sidx * TP_CLT + r * 8, *gl = s_g + sidx * TP_CLT + r * 8;
-      // the rotation's own derivative (pi/16 (2k+1) x the CLT turned by 90 degrees) dotted with dd/dCLT
-      float gdir[2] = {0.f, 0.f};
-#pragma unroll
-      for (int v = 0; v < 8; v++) {
-        const float c0 = cl[v], c1 = cl[64 + v], c2 = cl[128 + v], c3 = cl[192 + v];
-        const float g0 = gl[v], g1 = gl[64 + v], g2 = gl[128 + v], g3 = gl[192 + v];
-        const float fx = K16 * (2 * r + 1), fy = K16 * (2 * v + 1);
-        gdir[0] = fmaf(fx, (g1 * c0 - g0 * c1) + (g3 * c2 - g2 * c3), gdir[0]);
-        gdir[1] = fmaf(fy, (g2 * c0 - g0 * c2) + (g3 * c1 - g1 * c3), gdir[1]);
+    // ---------------- dd/drx, dd/dry per sensor and colour (forward mode on the CLT) ----------------
+    const int items = S * C;
+    for (int g = warp; g < (items + 3) / 4; g += AD_NW) {
+      const int it = g * 4 + q;
+      const int itc = it < items ? it : items - 1;
+      const int s = itc / C, c = itc - s * C;
+      const SubtilePlan p = sc.plan[(size_t)task * S * C + itc];
+      float gxy[2];
+      if (C == 1) {
+        shift_sens(sc, make_win(sc, p, s), p, s, s_clt + (size_t)itc * TP_CLT, s_g + (size_t)itc * TP_CLT,
+                   tb + q * 72, r, it < items, gxy);
+      } else {
+        BayerWin bw;
+        bw.w = make_win(sc, p, s, c);
+        bw.c = c;
+        bw.rr = sc.bayer_red_row;
+        bw.rc = sc.bayer_red_col;
+        shift_sens(sc, bw, p, s, s_clt + (size_t)itc * TP_CLT, s_g + (size_t)itc * TP_CLT, tb + q * 72, r,
+                   it < items, gxy);
       }
-      // dd/dCLT taken back once through the phase rotation, the kernel convolution and the 2D
-      // DCT-IV/DST-IV (symmetric transforms: the transpose runs through the same butterflies) to
-      // the folded tile, written over this lane's own dd/dCLT slots: gfs[m * 64 + j] for folded row r
-      float *gfs = s_g + sidx * TP_CLT + r * 8;
-      {
-        float gf[4][8];
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-#pragma unroll
-          for (int v = 0; v < 8; v++) gf[m][v] = gl[m * 64 + v];
-        rotate_t(gf, p.rx, p.ry, r);
-        convolve_t(gf, kp, r);
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-          float u[8];
-          dtt4_fast(gf[m], u, (m >> 1) & 1);
-          group_transpose(u, tb + q * 72, r);
-          dtt4_fast(u, gf[m], m & 1);
-        }
-        if (s < S) {
-#pragma unroll
-          for (int m = 0; m < 4; m++)
-#pragma unroll
-            for (int j2 = 0; j2 < 8; j2++) gfs[m * 64 + j2] = gf[m][j2];
-        }
+      if (r == 0 && it < items) {
+        s_sens[it * 2] = gxy[0];
+        s_sens[it * 2 + 1] = gxy[1];
       }
-      __syncwarp();
-      // per direction: the fold with the derivative window dotted with the folded gradient
-#pragma unroll
-      for (int dir = 0; dir < 2; dir++) {
-        float vw0, vw1, hw0[8], hw1[8];
-        if (dir == 0) fold_weights(-K16 * ahs, K16 * ahc, avc, avs, fv, vw0, vw1, hw0, hw1);
-        else fold_weights(ahc, ahs, -K16 * avs, K16 * avc, fv, vw0, vw1, hw0, hw1);
-        float acc = 0.f;
-#pragma unroll
-        for (int vb = 0; vb < 2; vb++) {
-          const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
-          float vc[16];
-#pragma unroll
-          for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
-#pragma unroll
-          for (int hb = 0; hb < 2; hb++)
-#pragma unroll
-            for (int j2 = 0; j2 < 8; j2++) {
-              const FoldIdx fh = fold_idx(j2);
-              const float h0 = (hb ? fh.ss0 : fh.sc0) * hw0[j2], h1 = (hb ? fh.ss1 : fh.sc1) * hw1[j2];
-              acc = fmaf(fmaf(h1, vc[fh.src1], h0 * vc[fh.src0]), gfs[(vb * 2 + hb) * 64 + j2], acc);
-            }
-        }
-        gdir[dir] += acc;
-      }
-#pragma unroll
-      for (int dir = 0; dir < 2; dir++) {
-        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 1);
-        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 2);
-        gdir[dir] += __shfl_xor_sync(0xffffffffu, gdir[dir], 4);
-      }
-      if (r == 0 && s < S) {
-        // residual = TL - px: dd/dpx = -dd/drx; the kernel-centre offsets add the
-        // dependence of px, py on the port through kdx, kdy (ImageDtt.java:4930-4939)
-        const float gpx = -gdir[0], gpy = -gdir[1];
-        float gx = gpx, gy = gpy;
-        if (p.kidx >= 0) {
-          const float4 e1 = __ldg((const float4 *)(sc.kext[s] + (size_t)p.kidx * 8) + 1);
-          gx = gpx * (1.0f - e1.x) - gpy * e1.z;
-          gy = -gpx * e1.y + gpy * (1.0f - e1.w);
-        }
-        sens[(tile * S + s) * 2] = gx;
-        sens[(tile * S + s) * 2 + 1] = gy;
-      }
+    }
+    __syncthreads();
+    // a sensor's colours share its port: their sensitivities add, in colour order
+    for (int i = tid; i < 2 * S; i += 32 * AD_NW) {
+      const int s = i >> 1, k = i & 1;
+      float v = 0.f;
+      for (int c = 0; c < C; c++) v += s_sens[(s * C + c) * 2 + k];
+      sens[(tile * S + s) * 2 + k] = v;
     }
     if (tid == 0) dval[tile] = dres;
     __syncthreads();
@@ -633,22 +688,25 @@ cudaError_t upload_adjoint_constants() {
   return cudaSuccess;
 }
 
-int adjoint_smem_bytes(int S) { return (S * 2 * TP_CLT + 240 + 240 + AD_NW * 816) * 4; }
+int adjoint_smem_bytes(int S, int C) { return (S * C * 2 * TP_CLT + 240 + 240 + AD_NW * 816) * 4; }
 
 cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, int use_strips, float *sens,
                            float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st) {
   if (sc.num_tasks <= 0) return cudaSuccess;
-  if (sc.num_colors != 1 || !sc.port_deriv || !sc.combo) return cudaErrorInvalidValue;
+  // colour scenes: quad Bayer sensors with the stored CLT (the recompute path folds mono windows)
+  if ((sc.num_colors != 1 && (sc.num_colors != 3 || recompute)) || !sc.port_deriv || !sc.combo)
+    return cudaErrorInvalidValue;
   AdjShape as;
   as.S = sc.num_sensors;
+  as.C = sc.num_colors;
   as.P = sc.num_pairs;
   as.RE = (sc.strip_rows < sc.wndy_size ? sc.strip_rows : sc.wndy_size) * 15;
-  as.per_warp = adjoint_smem_bytes(as.S) / 4;
+  as.per_warp = adjoint_smem_bytes(as.S, as.C) / 4;
   as.recompute = recompute;
   as.use_strips = (use_strips && sc.strips) ? 1 : 0;
-  const int bytes = adjoint_smem_bytes(as.S);
+  const int bytes = adjoint_smem_bytes(as.S, as.C);
   cudaError_t e = cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 152, per_sm = 1;

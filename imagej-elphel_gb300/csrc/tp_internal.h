@@ -171,7 +171,7 @@ cudaError_t launch_compact_tasks_scratch(const int *tile_op, const float *dispar
                                          int *scratch, cudaStream_t st);
 // adjoint (tp_adjoint.cu): per-tile dd/dport, Jacobian rows, loss gradient
 cudaError_t upload_adjoint_constants();
-int adjoint_smem_bytes(int S);
+int adjoint_smem_bytes(int S, int C);
 cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recompute, int use_strips, float *sens, float *dval,
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st);

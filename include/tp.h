@@ -425,14 +425,18 @@ tp_status tp_batch_synchronize(tp_batch *b);
  * L = sum over tiles of l(d) with dl/dd given per tile in dl_ddisp
  * ([tilesY*tilesX], host; NULL means l = d^2, i.e. 2 d).  Integer window
  * corners and the integer argmax are held fixed (piecewise constant).
- * Mono sensors, ports from the geometry (tp_set_tile_ops); run after tp_process.
+ * Mono sensors, or Bayer colour sensors (the three colour planes of a sensor
+ * share its port: their sensitivities add, and the pair chain runs back through
+ * the colour mix of the correlation); ports from the geometry (tp_set_tile_ops);
+ * run after tp_process.
  * dl_dextr [num_sensors][4] and dl_dtile_disp [tilesY*tilesX] are host
  * outputs (either may be NULL).  From the first tp_backward (or
  * tp_set_adjoint_mode) on, tp_process also records every pair's strip samples
  * ([tiles][pairs][strip entries] floats on the device) for the adjoint to read. */
 tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream);
 /* 1: the adjoint recomputes each tile's CLT from the images instead of reading
- * the stored CLT back (for when the CLT buffer is not kept); default 0.  Also
+ * the stored CLT back (for when the CLT buffer is not kept; mono sensors only:
+ * tp_backward returns TP_ERR_ARG for a colour handle in this mode); default 0.  Also
  * starts the strip-sample recording described at tp_backward. */
 tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt);
 /* Jacobian of the last tp_backward: jac_extr [tiles][num_sensors][4] (dd per
