@@ -521,6 +521,10 @@ static tp_status upload_geometry(tp_handle *h, const tp_geometry *g, const tp_ge
   gd.focal_length = g->focal_length;
   gd.pixel_size = g->pixel_size;
   gd.distortion_radius = g->distortion_radius;
+  // per-camera constants of getPortsCoordinatesAndDerivatives, divided once here (IEEE division:
+  // the same double as the device's correctly rounded one; host code is built without contraction)
+  gd.fl_pix = g->focal_length / (0.001 * g->pixel_size);
+  gd.ri_scale = (0.001 * g->pixel_size) / g->distortion_radius;
   gd.c_pixel_width = gc->pixel_width;
   gd.c_pixel_height = gc->pixel_height;
   gd.c_pixel_size = gc->pixel_size;

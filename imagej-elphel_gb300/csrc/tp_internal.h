@@ -29,6 +29,7 @@ struct GeomDev {
   int pixel_width, pixel_height;
   int tbl_len;
   double focal_length, pixel_size, distortion_radius;
+  double fl_pix, ri_scale;  // focal_length / (0.001 pixel_size), 0.001 pixel_size / distortion_radius
   // the model that undistorts the tile centre (the reference's gc_main): this camera's own, or
   // the main camera's for a rig's auxiliary camera, whose reverse distortion table is then loaded
   int c_pixel_width, c_pixel_height;

@@ -72,8 +72,7 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
                         double &ox, double &oy, double *deriv /* [2][5] or null */) {
   double pXc, pYc;
   center_undistort(g, tbl, px, py, pXc, pYc);
-  double fl_pix = DDIV(g.focal_length, DMUL(0.001, g.pixel_size));
-  double ri_scale = DDIV(DMUL(0.001, g.pixel_size), g.distortion_radius);
+  const double fl_pix = g.fl_pix, ri_scale = g.ri_scale;
   double vi[3] = {DSUB(pXc, DMUL(disparity, g.rXY[i][0])), DSUB(pYc, DMUL(disparity, g.rXY[i][1])), fl_pix};
   double rvi[3];
   mat3_vec(g.rots[i], vi, rvi);
@@ -125,8 +124,7 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
 // sensor part of getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2190-2217)
 __device__ __forceinline__ void sensor_port(const GeomDev &g, double pXc, double pYc, double disparity, int i,
                                             double &ox, double &oy) {
-  const double fl_pix = DDIV(g.focal_length, DMUL(0.001, g.pixel_size));
-  const double ri_scale = DDIV(DMUL(0.001, g.pixel_size), g.distortion_radius);
+  const double fl_pix = g.fl_pix, ri_scale = g.ri_scale;
   const double vi[3] = {DSUB(pXc, DMUL(disparity, g.rXY[i][0])), DSUB(pYc, DMUL(disparity, g.rXY[i][1])), fl_pix};
   double rvi[3];
   mat3_vec(g.rots[i], vi, rvi);
