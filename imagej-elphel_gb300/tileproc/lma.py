@@ -21,13 +21,16 @@ extrinsics alone are fitted.
 
 Two things make the iteration robust far from the solution, where ports are
 off by a pixel or more:
-- A tile without a correlation peak (NaN disparity) counts invalid_cost px^2
-  in the cost, so a step cannot lower the cost by losing tiles; and a tile's
-  d^2 counts at most invalid_cost (a truncated square), with the tiles past it
-  left out of the normal equations.  Without the cap a tile whose peak is on
-  the edge of existing, with a residual of a few pixels, makes every step a
-  dead end: the smallest move (1e-9 rad was measured) brings its peak back and
-  adds its d^2 to the cost.
+- A tile without a correlation peak (NaN disparity) counts a cap (px^2) in
+  the cost, so a step cannot lower the cost by losing tiles; and a tile's d^2
+  counts at most the cap (a truncated square), with the tiles past it left out
+  of the normal equations.  Without the cap a tile whose peak is on the edge
+  of existing, with a residual of a few pixels, makes every step a dead end:
+  the smallest move (1e-9 rad was measured) brings its peak back and adds its
+  d^2 to the cost.  The cap narrows from 9 to 4 to invalid_cost (1) over the
+  iterations (ANNEAL), so that while the extrinsics are far off the tiles a
+  pixel or two off still pull; with the narrow cap from the start one run in
+  four stopped with a hundred tiles lost.
 - There the measured disparity responds more weakly than its local
   derivative says (the smeared peak of the combined strip saturates), and the
   Gauss-Newton step falls short. An accepted step is therefore doubled while
@@ -74,17 +77,51 @@ LAM_MIN, LAM_MAX, LAM_RESTART = 1e-7, 1e6, 1e-2
 STALL_SCALES = (2.0, 4.0, 8.0, 0.5, 0.25)
 
 
+# caps of the first and the second quarter of the iterations (px^2): the truncated square starts
+# wide and narrows to invalid_cost, so tiles a pixel or two off still pull while the extrinsics
+# are far off, and none of them can hold the iteration at a dead end later
+ANNEAL = (9.0, 4.0)
+
+
+def refine_stages(iterations, invalid_cost=1.0, anneal=ANNEAL):
+    """[(iterations, cap)] of the stages refine runs"""
+    if invalid_cost is None or not anneal:
+        return [(iterations, invalid_cost)]
+    q = iterations // 4
+    return [(q, anneal[0]), (q, anneal[1]), (iterations - 2 * q, invalid_cost)]
+
+
 def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART, free_disparity=True,
-           fixed_sensor=None, callback=None, invalid_cost=1.0, expand=True):
-    """Runs `iterations` LM steps; returns (geometry, disparity, history) where history
-    holds the cost (sum over tiles with a peak of min(d^2, invalid_cost), plus invalid_cost per
-    tile without one) before each step and after the last; it never increases.  The per-tile disparity steps are
-    clipped to +-MAX_DISPARITY_STEP (a tile whose disparity derivative is close to zero would
-    otherwise take an unbounded step).  With expand an accepted step is doubled while that lowers
-    the cost, up to 8 times its length.  The cost is only piecewise smooth (window corners move
-    by whole pixels, peaks appear and vanish), so a point can be a dead end for every damping:
-    then the undamped step is tried at other lengths (STALL_SCALES), the best that lowers the cost
-    is taken, and the damping starts again from LAM_RESTART."""
+           fixed_sensor=None, callback=None, invalid_cost=1.0, expand=True, anneal=ANNEAL):
+    """Runs `iterations` LM steps; returns (geometry, disparity, history) where history holds the
+    cost before each step and after the last: the sum over tiles with a peak of min(d^2, cap),
+    plus cap per tile without one, with the cap of the step's stage (refine_stages: anneal[0] for
+    the first quarter of the iterations, anneal[1] for the second, invalid_cost for the rest;
+    each stage's first entry is its start point under its own cap).  It never increases: within a
+    stage no step that raises the cost is taken, and the caps only narrow.  The per-tile disparity steps are clipped to +-MAX_DISPARITY_STEP (a tile
+    whose disparity derivative is close to zero would otherwise take an unbounded step).  With
+    expand an accepted step is doubled while that lowers the cost, up to 8 times its length.  The
+    cost is only piecewise smooth (window corners move by whole pixels, peaks appear and vanish),
+    so a point can be a dead end for every damping: then the undamped step is tried at other
+    lengths (STALL_SCALES), the best that lowers the cost is taken, and the damping starts again
+    from LAM_RESTART."""
+    g, D, history, done = geometry, disparity, [], 0
+    for its, cap in refine_stages(iterations, invalid_cost, anneal):
+        if its <= 0:
+            continue
+        g, D, h = _refine_stage(tp, g, D, tile_op, its, lam, free_disparity, fixed_sensor, callback, cap, expand,
+                                done)
+        history += h
+        done += its
+    if not history:
+        history = [_evaluate(tp, copy.deepcopy(geometry), np.asarray(disparity, np.float32),
+                             np.ones(tp.tilesY * tp.tilesX, np.int32) if tile_op is None else tile_op,
+                             invalid_cost)[2]]
+    return g, D, history
+
+
+def _refine_stage(tp, geometry, disparity, tile_op, iterations, lam, free_disparity, fixed_sensor, callback,
+                  invalid_cost, expand, it0):
     T = tp.tilesY * tp.tilesX
     S = tp.num_sensors
     g = copy.deepcopy(geometry)
@@ -152,5 +189,5 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART
         _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
         history.append(cost)
         if callback:
-            callback(it, cost, lam)
+            callback(it0 + it, cost, lam)
     return g, D, history

@@ -237,10 +237,9 @@ def test_lma_reduces_cost(oracle):
 def test_lma_recovers_extrinsics_full_scene(oracle):
     """The same on the full 16x640x512 scene (5120 tiles), 80 iterations: the error of the extrinsics
     against the seeded truth, less each parameter's mean over the 16 sensors (a rotation or zoom of
-    the whole camera, which pair disparities do not see), falls to below a third (measured after 60
-    iterations: from 2.6e-3 to 1.1e-4 ... 5.9e-4 rad; runs differ because the adjoint's
-    shared-memory atomic sums differ in their last bits, which the iteration amplifies into
-    different paths, some slower to converge)."""
+    the whole camera, which pair disparities do not see), falls to below a fifth (measured: from
+    2.6e-3 to 1.0e-4 ... 1.2e-4 rad; runs differ in detail because the adjoint's shared-memory
+    atomic sums differ in their last bits, which the iteration amplifies)."""
     from tileproc import lma
     w, h = 640, 512
     t = (w // 8) * (h // 8)
@@ -265,4 +264,4 @@ def test_lma_recovers_extrinsics_full_scene(oracle):
 
     print("LMA cost %.4g -> %.4g, error %.3g -> %.3g" % (hist[0], hist[-1], err(g0), err(g)))
     assert all(b <= a for a, b in zip(hist, hist[1:]))
-    assert err(g) < err(g0) / 3
+    assert err(g) < err(g0) / 5
