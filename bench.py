@@ -687,19 +687,20 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         # the reference arm's own measurement, in a fresh process: this one holds the CUDA context,
-        # torch's thread pools and the timing threads, which slowed the oracle's threads by ~2.5x
-        sample = args.cpu_sample_tiles or (4000 if Cn == 3 else 2000)
+        # torch's thread pools and the timing threads, which slowed the oracle's threads by ~2.5x.
+        # The whole scene per run, 3 timed runs: about 10 s of CPU work.
+        sample = args.cpu_sample_tiles or T
         env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--config", args.config,
-                            "--seed", str(args.seed), "--steps", "2", "--warmup", "1", "--cpu-sample-tiles",
+                            "--seed", str(args.seed), "--steps", "3", "--warmup", "1", "--cpu-sample-tiles",
                             str(sample)], env=env, capture_output=True, text=True, check=True)
         ref_line = json.loads(r.stdout.strip().splitlines()[-1])
         cb = ref_line["cpu_baseline"]
         cpu = {"value": cb["value"], "unit": "tiles/s", "cores": cb["cores"], "kind": "port",
-               "sample": "%d of %d tiles (every %d-th) per run, 1 warm-up + 2 timed runs, stages 1-4%s, FP64 C "
-                         "restatement, in a separate process (bench.py --impl reference)" % (
+               "sample": "%d of %d tiles (every %d-th) per run, 1 warm-up + 3 timed runs (%.1f s), stages 1-4%s, "
+                         "FP64 C restatement, in a separate process (bench.py --impl reference)" % (
                              ref_line["config"]["sample_tiles_per_step"], T, max(1, T // sample),
-                             "b" if with_tex else "a")}
+                             ref_line["ms_per_step"] * 3 / 1000.0, "b" if with_tex else "a")}
     # plan, tile map, disparity init, fused forward, imclt, textures; the staged-window forward of u16
     # Bayer quads hands the serial half of its extraction to a second kernel
     win = Cn == 3 and S <= 4 and w["scene"]["images"].dtype == np.uint16

@@ -1162,6 +1162,9 @@ __global__ void __launch_bounds__(32 * IMCLT_WARPS) imclt_fast_kernel(const __gr
   const float sa2 = -1.f, sb2 = (r >= 4) ? 1.f : -1.f;   // signs of row i2
   const float w1 = k_hwin[i1 < 8 ? i1 : 15 - i1], w2 = k_hwin[i2 < 8 ? i2 : 15 - i2];
   const float kc1 = sa1 * w1, ks1 = sb1 * w1, kc2 = sa2 * w2, ks2 = sb2 * w2;
+  float lk[8];  // 0.25 x the colour's LPF for row r (the iclt_2d scale)
+#pragma unroll
+  for (int v = 0; v < 8; v++) lk[v] = 0.25f * (lpf ? lpf[r * 8 + v] : 1.0f);
   for (int ph = 0; ph < 4; ph++) {
     const int pxp = ph & 1, pyp = ph >> 1;
     int tx0 = bx0 - 1, ty0 = by0 - 1;
@@ -1187,11 +1190,9 @@ __global__ void __launch_bounds__(32 * IMCLT_WARPS) imclt_fast_kernel(const __gr
         o[m][4] = b.x; o[m][5] = b.y; o[m][6] = b.z; o[m][7] = b.w;
       }
 #pragma unroll
-      for (int v = 0; v < 8; v++) {
-        const float l = 0.25f * (lpf ? lpf[r * 8 + v] : 1.0f);
+      for (int v = 0; v < 8; v++)
 #pragma unroll
-        for (int m = 0; m < 4; m++) o[m][v] *= l;
-      }
+        for (int m = 0; m < 4; m++) o[m][v] *= lk[v];
       // inverse 2D DCT-IV/DST-IV with the swapped mode (ImageDtt.java:3628):
       // rows (vertical frequency) first, then columns
       float t[4][8];
