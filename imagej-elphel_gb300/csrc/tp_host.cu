@@ -55,6 +55,11 @@ struct tp_handle {
   float *d_rig_corr = nullptr, *d_rig_rec = nullptr;  // inter-camera correlation with an auxiliary camera
   float *d_rig_tmp = nullptr;  // rig LMA: disparity record [tiles][TP_NDISP], then the fit [tiles][4]
   int rig_lma_done = 0;        // the rig record already holds the LMA branch's values
+  // page-locked copies of the last tile ops / disparities (tp_set_tile_ops returns before its
+  // upload runs), reused once the event after their upload has passed
+  int *h_stage_op = nullptr;
+  float *h_stage_disp = nullptr;
+  cudaEvent_t ev_stage = nullptr;
   float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
   float *d_mismatch = nullptr;  // [tiles][pairs][3] lazy-eye mismatch of the last LMA pass that measured it
   size_t mismatch_cap = 0;
@@ -471,6 +476,12 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
                   h->d_rig_rec, h->d_rig_tmp, h->d_osum};
   for (void *b : bufs) dfree(h, b);
+  if (h->ev_stage) {
+    cudaEventSynchronize(h->ev_stage);
+    cudaEventDestroy(h->ev_stage);
+  }
+  if (h->h_stage_op) cudaFreeHost(h->h_stage_op);
+  if (h->h_stage_disp) cudaFreeHost(h->h_stage_disp);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->ev_work) cudaEventDestroy(h->ev_work);
   delete h;
@@ -729,6 +740,7 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
       xy[(size_t)i * 2 * S + k] = v;
     }
   }
+  CK(cudaStreamWaitEvent(h->stream, h->ev_work, 0), "tp_set_tasks");  // in-flight work reads the old list
   if (n > 0) {
     CK(cudaMemcpyAsync(h->d_task_txy, txy.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream), "tp_set_tasks");
     CK(cudaMemcpyAsync(h->d_task_op, op.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream), "tp_set_tasks");
@@ -745,9 +757,14 @@ tp_status tp_set_tasks(tp_handle *h, const float *packed, int n) {
   return TP_OK;
 }
 
+// The tile ops go up without a host round trip: the task count is counted here (the compaction on
+// the device selects the same tiles, tile_op != 0), the arrays are copied into page-locked staging
+// (so the caller's buffers are free on return) and uploaded and compacted on the handle's stream
+// after the handle's last work, which still reads the task list it replaces.
 tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
   if (!h || !tile_op || !disp) return TP_ERR_ARG;
   if (!h->have_geometry) return fail(h, TP_ERR_STATE, "tp_set_tile_ops: geometry not set");
+  int n = 0;
   for (int i = 0; i < h->ntiles; i++) {
     // NaN fails the comparison
     if (tile_op[i] != 0 && !(fabsf(disp[i]) <= TP_MAX_DISPARITY)) {
@@ -756,23 +773,37 @@ tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *disp) {
                (double)disp[i], (double)TP_MAX_DISPARITY);
       return fail(h, TP_ERR_ARG, msg);
     }
+    n += tile_op[i] != 0;
   }
-  CK(cudaMemcpyAsync(h->d_tile_op, tile_op, h->ntiles * sizeof(int), cudaMemcpyHostToDevice, h->stream),
+  if (!h->h_stage_op) {
+    if (cudaEventCreateWithFlags(&h->ev_stage, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost((void **)&h->h_stage_op, h->ntiles * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost((void **)&h->h_stage_disp, h->ntiles * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_set_tile_ops: staging buffers");
+    }
+  } else {
+    CK(cudaEventSynchronize(h->ev_stage), "tp_set_tile_ops");  // the previous upload has read them
+  }
+  memcpy(h->h_stage_op, tile_op, h->ntiles * sizeof(int));
+  memcpy(h->h_stage_disp, disp, h->ntiles * sizeof(float));
+  CK(cudaStreamWaitEvent(h->stream, h->ev_work, 0), "tp_set_tile_ops");
+  CK(cudaMemcpyAsync(h->d_tile_op, h->h_stage_op, h->ntiles * sizeof(int), cudaMemcpyHostToDevice, h->stream),
      "tp_set_tile_ops");
-  CK(cudaMemcpyAsync(h->d_tile_disp, disp, h->ntiles * sizeof(float), cudaMemcpyHostToDevice, h->stream),
+  CK(cudaMemcpyAsync(h->d_tile_disp, h->h_stage_disp, h->ntiles * sizeof(float), cudaMemcpyHostToDevice,
+                     h->stream),
      "tp_set_tile_ops");
+  CK(cudaEventRecord(h->ev_stage, h->stream), "tp_set_tile_ops");
   CK(launch_compact_tasks(h->d_tile_op, h->d_tile_disp, h->tilesX, h->ntiles, h->d_task_txy, h->d_task_op,
                           h->d_task_disp, h->d_num_tasks, h->stream),
      "tp_set_tile_ops");
-  CK(cudaMemcpyAsync(&h->num_tasks, h->d_num_tasks, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
-     "tp_set_tile_ops");
-  CK(cudaStreamSynchronize(h->stream), "tp_set_tile_ops");
+  h->num_tasks = n;
   h->ports_from_geometry = 1;
   h->have_tasks = 1;
   h->planned = 0;
   h->deriv_valid = 0;
   h->fwd_valid = 0;
-  return TP_OK;
+  return mark_work(h, h->stream);
 }
 
 tp_status tp_set_lpf(tp_handle *h, const float *lpf) {
@@ -898,6 +929,7 @@ static tp_status ensure_plan(tp_handle *h, cudaStream_t st) {
   if (!h->have_tasks) return fail(h, TP_ERR_STATE, "no tasks set (tp_set_tasks / tp_set_tile_ops)");
   if (h->ports_from_geometry && !h->have_geometry) return fail(h, TP_ERR_STATE, "geometry not set");
   if (h->planned) return TP_OK;
+  CK(cudaStreamWaitEvent(st, h->ev_work, 0), "plan");  // the task list, uploaded on the handle's stream
   SceneDev sc = scene_of(h);
   const bool with_deriv = h->adj_record && h->d_port_deriv && h->ports_from_geometry;
   if (with_deriv) sc.port_deriv = h->d_port_deriv;  // the adjoint's port derivatives, same ports

@@ -209,7 +209,10 @@ tp_status tp_set_color_scales(tp_handle *h, const float *scales);
 tp_status tp_set_tasks(tp_handle *h, const float *packed_tasks, int num_tasks);
 /* setFullFrameImages(float[] target_disparities) + getTileSubcamOffsets
  * (GPUTileProcessor.java:472-527, 686-778) computed on the device in FP64:
- * tiles with tile_op != 0 (ImageDtt tile_op[ty][tx]) become tasks in row-major order. */
+ * tiles with tile_op != 0 (ImageDtt tile_op[ty][tx]) become tasks in row-major order.
+ * Returns without waiting for the device: the arrays are copied (the caller's buffers are free
+ * on return) and uploaded after the handle's last work, and the handle's next work runs after
+ * the upload; tp_get_num_tasks is known at once. */
 tp_status tp_set_tile_ops(tp_handle *h, const int *tile_op, const float *target_disparity);
 /* The aberration-kernel chain of QuadCLT.calculateCLTKernel (QuadCLT.java:433-667,
  * ImageDtt.java:4625-4734) on the device: psf [kernels_vert][kernels_hor][num_colors][64][64]
