@@ -259,15 +259,21 @@ def run_reference(args):
         return 0
     w = make_workload(args.config, args.seed)
     threads = os.cpu_count() or 1
-    sample = args.cpu_sample_tiles or (4000 if w["C"] == 3 else 2000)
+    sample = args.cpu_sample_tiles
+    if not sample:
+        # as large a sample as keeps the W + K runs near 90 s: one untimed run of the whole scene
+        # gives the rate (a small sample would mostly time the oracle's per-call set-up)
+        rate = cpu_baseline(w, w["T"], threads)[0]
+        sample = int(min(w["T"], max(2000, rate * 90.0 / max(1, args.steps + args.warmup))))
     value, n_run, tot_t = cpu_baseline_runs(w, sample, threads, args.warmup, args.steps)
     line = {"metric": METRIC, "value": value, "unit": "tiles/s", "impl": "reference", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.config, "tiles_per_scene": w["T"], "sample_tiles_per_step": n_run},
             "cpu_baseline": {"value": value, "unit": "tiles/s", "cores": threads, "kind": "port",
-                             "sample": "%d of %d tiles per step, stages 1-4%s" % (n_run, w["T"],
-                                                                                  "b" if w["C"] == 3 else "a")},
+                             "sample": "%d of %d tiles per step (sized for about 90 s over the warm-up and timed "
+                                       "steps from one untimed whole-scene run), stages 1-4%s, FP64 C restatement"
+                                       % (n_run, w["T"], "b" if w["C"] == 3 else "a")},
             "e2e": {"value": value, "unit": "tiles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -698,7 +704,7 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         # the reference arm's own measurement, in a fresh process: this one holds the CUDA context,
         # torch's thread pools and the timing threads, which slowed the oracle's threads by ~2.5x.
-        # The whole scene per run, 3 timed runs: about 10 s of CPU work.
+        # The whole scene per run, 3 timed runs: about 5-10 s of CPU work.
         sample = args.cpu_sample_tiles or T
         env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--config", args.config,
