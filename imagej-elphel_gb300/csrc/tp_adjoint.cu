@@ -26,9 +26,11 @@
 // live in shared memory; warp 0 takes the centroid of the combined strip the
 // forward kernel kept; then the warps split the pairs, each running a pair's
 // reverse chain in registers and per-warp buffers (the transposed DCT-IIe is
-// the transposed butterfly of the forward one) and adding into the gradient
-// with shared-memory atomics; finally they split the sensors for the
-// forward-mode shift derivatives.
+// the transposed butterfly of the forward one) and adding into the gradient;
+// the pairs go in rounds of four on distinct sensors (scheduled on the host),
+// a barrier between rounds, so the gradient sums are taken in a fixed order
+// without atomics; finally the warps split the sensors for the forward-mode
+// shift derivatives.
 #include "tp_dtt.cuh"
 
 namespace {
@@ -433,155 +435,167 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
       continue;
     }
 
-    // ---------------- reverse pass over the pairs, AD_NW pairs at a time ----------------
-    // With the forward's strip samples recorded and one entry per lane, the next pair's sample
-    // is loaded one iteration ahead so its latency overlaps this pair.
+    // ---------------- reverse pass over the pairs, one round of AD_NW pairs at a time ----------------
+    // A round's pairs are on distinct sensors (the host's schedule), so the warps add their CLT
+    // gradients into disjoint parts of s_g; the barrier after each round orders the rounds, so
+    // every gradient entry is summed in the same order in every run.  With the forward's strip
+    // samples recorded and one entry per lane, the next round's sample is loaded one round ahead
+    // so its latency overlaps this pair.
     const bool pre = as.use_strips && RE <= 32;
+    const short *sched = &sc.corr_cfg->adj_round[0][0];
+    int pnext = cfg.adj_rounds > 0 ? sched[warp] : -1;
     float vnext = 0.f;
-    if (pre && warp < P && lane < RE) vnext = sc.strips[(tile * P + warp) * RE + lane];
-    for (int pi = warp; pi < P; pi += AD_NW) {
+    if (pre && pnext >= 0 && lane < RE) vnext = sc.strips[(tile * P + pnext) * RE + lane];
+    for (int rd = 0; rd < cfg.adj_rounds; rd++) {
+      const int pi = pnext;
       const float vcur = vnext;
-      if (pre && pi + AD_NW < P && lane < RE) vnext = sc.strips[(tile * P + pi + AD_NW) * RE + lane];
-      const PairDev pd = cfg.pairs[pi];
-      if (!pd.in_combo) continue;
-      const float *c = sc.corr + (tile * P + pi) * TP_CORR;
-      for (int i = lane; i < 240; i += 32) gs[i] = 0.f;
-      for (int i = lane; i < 288; i += 32) qb[i] = 0.f;
-      __syncwarp();
-      // strip entries: d combo / d v_p = G / (n v_p) for the geometric mean of n pairs
-      bool any = false;
-      for (int e = lane; e < RE; e += 32) {
-        if (gcmb[e] == 0.f) continue;
-        const float d = pre ? vcur
-                            : (as.use_strips ? sc.strips[(tile * P + pi) * RE + e] : strip_entry(c, strip_code, pd, e));
-        const float v = d + cfg.corr_offset;
-        if (!(v > 0.0f)) continue;
-        const float f = __fdividef(gcmb[e] * gG[e] * inv_n, v);
-        const int row = e / 15;
-        const float half = row > 0 ? 0.5f : 1.0f;
-        for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
-          int idx[4];
-          float wt[4];
-          int n;
-          if (pd.kind <= 3) {
-            const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
-            n = code_taps(side ? code.y : code.x, idx, wt);
-          } else {
-            n = general_taps(pd.bx, pd.by, row, e - row * 15 - 7, side ? 1 : -1, idx, wt);
-          }
-          for (int k = 0; k < n; k++) atomicAdd(&gs[idx[k]], f * half * wt[k]);
-        }
-        any = true;
-      }
-      if (!__any_sync(0xffffffffu, any)) continue;
-      __syncwarp();
-      // 15x15 unfold (DttRad2.corr_unfold_tile) transposed into the four quadrants
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const int a = (lane >> 3) + 4 * k, b = lane & 7;
-        const float g1 = gs[(7 + a) * 15 + 7 + b];
-        const float g2 = b ? gs[(7 + a) * 15 + 7 - b] : 0.f;
-        const float g3 = a ? gs[(7 - a) * 15 + 7 + b] : 0.f;
-        const float g4 = (a && b) ? gs[(7 - a) * 15 + 7 - b] : 0.f;
-        qb[a * 9 + b] = 0.25f * (((g1 + g2) + g3) + g4);
-        if (b) qb[72 + a * 9 + b - 1] = 0.25f * (((g1 - g2) + g3) - g4);
-        if (a) qb[144 + (a - 1) * 9 + b] = 0.25f * (((g1 + g2) - g3) - g4);
-        if (a && b) qb[216 + (a - 1) * 9 + b - 1] = 0.25f * (((g1 - g2) - g3) + g4);
-      }
-      __syncwarp();
-      // 2D DCT-IIe/DST-IIe transposed: forward Z = Ta X^T Tb^T, so Xbar = Tb^T Zbar^T Ta
-      {
-        float z[8], v[8];
-#pragma unroll
-        for (int k = 0; k < 8; k++) z[k] = qb[q * 72 + k * 9 + r];  // column r of Zbar
-        dtt2e_transposed(z, v, (q >> 1) & 1);                        // row r of V = Zbar^T Ta
-#pragma unroll
-        for (int n = 0; n < 8; n++) tb[q * 72 + r * 9 + n] = v[n];
+      pnext = rd + 1 < cfg.adj_rounds ? sched[(rd + 1) * AD_NW + warp] : -1;
+      if (pre && pnext >= 0 && lane < RE) vnext = sc.strips[(tile * P + pnext) * RE + lane];
+      do {  // this warp's pair of the round (break: nothing to add)
+        if (pi < 0) break;
+        const PairDev pd = cfg.pairs[pi];
+        if (!pd.in_combo) break;
+        const float *c = sc.corr + (tile * P + pi) * TP_CORR;
+        for (int i = lane; i < 240; i += 32) gs[i] = 0.f;
+        for (int i = lane; i < 288; i += 32) qb[i] = 0.f;
         __syncwarp();
-#pragma unroll
-        for (int k = 0; k < 8; k++) z[k] = tb[q * 72 + k * 9 + r];  // column r of V
-        dtt2e_transposed(z, v, q & 1);                               // column r of Xbar
-#pragma unroll
-        for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];
-        __syncwarp();
-      }
-      // LPF, colour mix and the fat-zero normalised product of each colour
-      // (correlateSingleColorFD / correlateCompositeFD): acc = sum_c w_c t_c / (a2_c + fz2_c)
-      float gq[4][2];
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int idx = lane + 32 * h;
-        const float l = cfg.lpf[idx];
-        const int off = (idx >> 3) * 9 + (idx & 7);
-#pragma unroll
-        for (int qq = 0; qq < 4; qq++) gq[qq][h] = qb[qq * 72 + off] * l;
-      }
-      const float fzz = cfg.fat_zero * cfg.fat_zero;
-      for (int c = 0; c < C; c++) {
-        const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
-        const float *c1 = s_clt + ((size_t)pd.cam1 * C + c) * TP_CLT, *c2 = s_clt + ((size_t)pd.cam2 * C + c) * TP_CLT;
-        float d1[4][2], d2[4][2], a2[2], ia2[2], s1v[2], s2v[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          float s1 = 0.f, s2 = 0.f;
-#pragma unroll
-          for (int m = 0; m < 4; m++) {
-            d1[m][h] = c1[m * 64 + lane + 32 * h];
-            d2[m][h] = c2[m * 64 + lane + 32 * h];
-            s1 = fmaf(d1[m][h], d1[m][h], s1);
-            s2 = fmaf(d2[m][h], d2[m][h], s2);
+        // strip entries: d combo / d v_p = G / (n v_p) for the geometric mean of n pairs
+        bool any = false;
+        for (int e = lane; e < RE; e += 32) {
+          if (gcmb[e] == 0.f) continue;
+          const float d = pre ? vcur
+                              : (as.use_strips ? sc.strips[(tile * P + pi) * RE + e]
+                                               : strip_entry(c, strip_code, pd, e));
+          const float v = d + cfg.corr_offset;
+          if (!(v > 0.0f)) continue;
+          const float f = __fdividef(gcmb[e] * gG[e] * inv_n, v);
+          const int row = e / 15;
+          const float half = row > 0 ? 0.5f : 1.0f;
+          for (int side = 0; side < (row > 0 ? 2 : 1); side++) {
+            int idx[4];
+            float wt[4];
+            int n;
+            if (pd.kind <= 3) {
+              const short2 code = *(const short2 *)&strip_code[(pd.kind * TP_MAX_STRIP * 15 + e) * 2];
+              n = code_taps(side ? code.y : code.x, idx, wt);
+            } else {
+              n = general_taps(pd.bx, pd.by, row, e - row * 15 - 7, side ? 1 : -1, idx, wt);
+            }
+            for (int k = 0; k < n; k++) atomicAdd(&gs[idx[k]], f * half * wt[k]);
           }
-          // |d1| |d2| with the forward's approximate square root; ia2 = 1 / a2 (0 where a2 = 0)
-          const float pr = s1 * s2;
-          ia2[h] = (pr > 0.0f) ? rsqrtf(pr) : 0.0f;
-          a2[h] = pr * ia2[h];
-          s1v[h] = s1;
-          s2v[h] = s2;
+          any = true;
         }
-        const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
-        float tg[4][2], dbar[2];
+        if (!__any_sync(0xffffffffu, any)) break;
+        __syncwarp();
+        // 15x15 unfold (DttRad2.corr_unfold_tile) transposed into the four quadrants
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const float u = __fdividef(1.0f, a2[h] + fz2);
-          const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
-          const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
-          const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
-          const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
-          const float swbar = gq[0][h] * t0 + gq[1][h] * t1 + gq[2][h] * t2 + gq[3][h] * t3;
-          dbar[h] = -wgt * swbar * u * u;
-          const float sw = wgt * u;
-#pragma unroll
-          for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq][h] * sw;
+        for (int k = 0; k < 2; k++) {
+          const int a = (lane >> 3) + 4 * k, b = lane & 7;
+          const float g1 = gs[(7 + a) * 15 + 7 + b];
+          const float g2 = b ? gs[(7 + a) * 15 + 7 - b] : 0.f;
+          const float g3 = a ? gs[(7 - a) * 15 + 7 + b] : 0.f;
+          const float g4 = (a && b) ? gs[(7 - a) * 15 + 7 - b] : 0.f;
+          qb[a * 9 + b] = 0.25f * (((g1 + g2) + g3) + g4);
+          if (b) qb[72 + a * 9 + b - 1] = 0.25f * (((g1 - g2) + g3) - g4);
+          if (a) qb[144 + (a - 1) * 9 + b] = 0.25f * (((g1 + g2) - g3) - g4);
+          if (a && b) qb[216 + (a - 1) * 9 + b - 1] = 0.25f * (((g1 - g2) - g3) + g4);
         }
-        const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
-        float *g1p = s_g + ((size_t)pd.cam1 * C + c) * TP_CLT, *g2p = s_g + ((size_t)pd.cam2 * C + c) * TP_CLT;
+        __syncwarp();
+        // 2D DCT-IIe/DST-IIe transposed: forward Z = Ta X^T Tb^T, so Xbar = Tb^T Zbar^T Ta
+        {
+          float z[8], v[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) z[k] = qb[q * 72 + k * 9 + r];  // column r of Zbar
+          dtt2e_transposed(z, v, (q >> 1) & 1);                        // row r of V = Zbar^T Ta
+#pragma unroll
+          for (int n = 0; n < 8; n++) tb[q * 72 + r * 9 + n] = v[n];
+          __syncwarp();
+#pragma unroll
+          for (int k = 0; k < 8; k++) z[k] = tb[q * 72 + k * 9 + r];  // column r of V
+          dtt2e_transposed(z, v, q & 1);                               // column r of Xbar
+#pragma unroll
+          for (int k = 0; k < 8; k++) qb[q * 72 + k * 9 + r] = v[k];
+          __syncwarp();
+        }
+        // LPF, colour mix and the fat-zero normalised product of each colour
+        // (correlateSingleColorFD / correlateCompositeFD): acc = sum_c w_c t_c / (a2_c + fz2_c)
+        float gq[4][2];
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int idx = lane + 32 * h;
-          const float a2bar = dbar[h] + dsum;
-          const float T0 = tg[0][h], T1 = tg[1][h], T2 = tg[2][h], T3 = tg[3][h];
-          float g1[4], g2[4];
-          g1[0] = T0 * d2[0][h] + T1 * d2[1][h] + T2 * d2[2][h] + T3 * d2[3][h];
-          g1[1] = T0 * d2[1][h] - T1 * d2[0][h] + T2 * d2[3][h] - T3 * d2[2][h];
-          g1[2] = T0 * d2[2][h] + T1 * d2[3][h] - T2 * d2[0][h] - T3 * d2[1][h];
-          g1[3] = T0 * d2[3][h] - T1 * d2[2][h] - T2 * d2[1][h] + T3 * d2[0][h];
-          g2[0] = T0 * d1[0][h] - T1 * d1[1][h] - T2 * d1[2][h] + T3 * d1[3][h];
-          g2[1] = T0 * d1[1][h] + T1 * d1[0][h] - T2 * d1[3][h] - T3 * d1[2][h];
-          g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
-          g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
-          // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
-          const float k1 = a2bar * s2v[h] * ia2[h];
-          const float k2 = a2bar * s1v[h] * ia2[h];
+          const float l = cfg.lpf[idx];
+          const int off = (idx >> 3) * 9 + (idx & 7);
 #pragma unroll
-          for (int m = 0; m < 4; m++) {
-            atomicAdd(&g1p[m * 64 + idx], fmaf(k1, d1[m][h], g1[m]));
-            atomicAdd(&g2p[m * 64 + idx], fmaf(k2, d2[m][h], g2[m]));
+          for (int qq = 0; qq < 4; qq++) gq[qq][h] = qb[qq * 72 + off] * l;
+        }
+        const float fzz = cfg.fat_zero * cfg.fat_zero;
+        for (int c = 0; c < C; c++) {
+          const float wgt = (C == 1) ? 1.0f : cfg.col_weights[c];
+          const float *c1 = s_clt + ((size_t)pd.cam1 * C + c) * TP_CLT;
+          const float *c2 = s_clt + ((size_t)pd.cam2 * C + c) * TP_CLT;
+          float d1[4][2], d2[4][2], a2[2], ia2[2], s1v[2], s2v[2];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+              d1[m][h] = c1[m * 64 + lane + 32 * h];
+              d2[m][h] = c2[m * 64 + lane + 32 * h];
+              s1 = fmaf(d1[m][h], d1[m][h], s1);
+              s2 = fmaf(d2[m][h], d2[m][h], s2);
+            }
+            // |d1| |d2| with the forward's approximate square root; ia2 = 1 / a2 (0 where a2 = 0)
+            const float pr = s1 * s2;
+            ia2[h] = (pr > 0.0f) ? rsqrtf(pr) : 0.0f;
+            a2[h] = pr * ia2[h];
+            s1v[h] = s1;
+            s2v[h] = s2;
+          }
+          const float fz2 = warp_sum(a2[0] + a2[1]) * (1.0f / 64) * fzz;
+          float tg[4][2], dbar[2];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const float u = __fdividef(1.0f, a2[h] + fz2);
+            const float t0 = d1[0][h] * d2[0][h] + d1[1][h] * d2[1][h] + d1[2][h] * d2[2][h] + d1[3][h] * d2[3][h];
+            const float t1 = -d1[1][h] * d2[0][h] + d1[0][h] * d2[1][h] - d1[3][h] * d2[2][h] + d1[2][h] * d2[3][h];
+            const float t2 = -d1[2][h] * d2[0][h] - d1[3][h] * d2[1][h] + d1[0][h] * d2[2][h] + d1[1][h] * d2[3][h];
+            const float t3 = d1[3][h] * d2[0][h] - d1[2][h] * d2[1][h] - d1[1][h] * d2[2][h] + d1[0][h] * d2[3][h];
+            const float swbar = gq[0][h] * t0 + gq[1][h] * t1 + gq[2][h] * t2 + gq[3][h] * t3;
+            dbar[h] = -wgt * swbar * u * u;
+            const float sw = wgt * u;
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) tg[qq][h] = gq[qq][h] * sw;
+          }
+          const float dsum = warp_sum(dbar[0] + dbar[1]) * (1.0f / 64) * fzz;
+          float *g1p = s_g + ((size_t)pd.cam1 * C + c) * TP_CLT, *g2p = s_g + ((size_t)pd.cam2 * C + c) * TP_CLT;
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int idx = lane + 32 * h;
+            const float a2bar = dbar[h] + dsum;
+            const float T0 = tg[0][h], T1 = tg[1][h], T2 = tg[2][h], T3 = tg[3][h];
+            float g1[4], g2[4];
+            g1[0] = T0 * d2[0][h] + T1 * d2[1][h] + T2 * d2[2][h] + T3 * d2[3][h];
+            g1[1] = T0 * d2[1][h] - T1 * d2[0][h] + T2 * d2[3][h] - T3 * d2[2][h];
+            g1[2] = T0 * d2[2][h] + T1 * d2[3][h] - T2 * d2[0][h] - T3 * d2[1][h];
+            g1[3] = T0 * d2[3][h] - T1 * d2[2][h] - T2 * d2[1][h] + T3 * d2[0][h];
+            g2[0] = T0 * d1[0][h] - T1 * d1[1][h] - T2 * d1[2][h] + T3 * d1[3][h];
+            g2[1] = T0 * d1[1][h] + T1 * d1[0][h] - T2 * d1[3][h] - T3 * d1[2][h];
+            g2[2] = T0 * d1[2][h] - T1 * d1[3][h] + T2 * d1[0][h] - T3 * d1[1][h];
+            g2[3] = T0 * d1[3][h] + T1 * d1[2][h] + T2 * d1[1][h] + T3 * d1[0][h];
+            // a2 = sqrt(s1 s2): d a2 / d d1[m] = d1[m] s2 / a2
+            const float k1 = a2bar * s2v[h] * ia2[h];
+            const float k2 = a2bar * s1v[h] * ia2[h];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {  // no other warp adds to these sensors in this round
+              g1p[m * 64 + idx] += fmaf(k1, d1[m][h], g1[m]);
+              g2p[m * 64 + idx] += fmaf(k2, d2[m][h], g2[m]);
+            }
           }
         }
-      }
-      __syncwarp();
+        __syncwarp();
+      } while (0);
+      __syncthreads();
     }
-    __syncthreads();
 
     // ---------------- dd/drx, dd/dry per sensor and colour (forward mode on the CLT) ----------------
     const int items = S * C;

@@ -118,6 +118,18 @@ static tp_status mark_work(tp_handle *h, cudaStream_t st) {
   return TP_OK;
 }
 
+// A setter that overwrites a device buffer first waits for the handle's work in flight, which may
+// still read it on another stream: on the stream of its copy (after_work), or on the host before a
+// synchronous copy or a free (work_done).
+static tp_status after_work(tp_handle *h, cudaStream_t st, const char *where) {
+  CK(cudaStreamWaitEvent(st, h->ev_work, 0), where);
+  return TP_OK;
+}
+static tp_status work_done(tp_handle *h, const char *where) {
+  CK(cudaEventSynchronize(h->ev_work), where);
+  return TP_OK;
+}
+
 // Device allocations of a handle are counted against the process-wide cap of
 // tp_set_memory_limit (0 = none): an allocation beyond it fails as a failed cudaMalloc does.
 static std::atomic<size_t> g_mem_limit{0};
@@ -574,6 +586,7 @@ static tp_status upload_geometry(tp_handle *h, const tp_geometry *g, const tp_ge
   std::vector<double> tbl;
   gd.tbl_len = host_rdist_table(gc, tbl);
   if (gd.tbl_len > 2048 + 64) return fail(h, TP_ERR_ARG, "distortion table too long");
+  if (after_work(h, h->stream, "tp_set_geometry") != TP_OK) return TP_ERR_CUDA;
   CK(cudaMemcpyAsync(h->d_geom, &gd, sizeof(gd), cudaMemcpyHostToDevice, h->stream), "tp_set_geometry");
   CK(cudaMemcpyAsync(h->d_rdist, tbl.data(), sizeof(double) * gd.tbl_len, cudaMemcpyHostToDevice, h->stream),
      "tp_set_geometry");
@@ -605,16 +618,16 @@ tp_status tp_set_kernels(tp_handle *h, int cam, const float *kernels, const floa
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_set_kernels: bad camera");
   if (h->cfg.kernels_hor <= 0) return fail(h, TP_ERR_STATE, "tp_set_kernels: handle created without kernels");
   size_t nk = (size_t)h->cfg.kernels_hor * h->cfg.kernels_vert * h->cfg.num_colors;
+  if (layout != TP_KERNELS_GPU && layout != TP_KERNELS_CPU) return fail(h, TP_ERR_ARG, "tp_set_kernels: bad layout");
+  if (work_done(h, "tp_set_kernels") != TP_OK) return TP_ERR_CUDA;
   if (layout == TP_KERNELS_GPU) {
     // undo the 8x8 transpose of GPUTileProcessor.setConvolutionKernels (406-410)
     std::vector<float> t(nk * TP_CLT);
     for (size_t k = 0; k < nk * 4; k++)
       for (int i0 = 0; i0 < 64; i0++) t[k * 64 + (((i0 & 7) << 3) | (i0 >> 3))] = kernels[k * 64 + i0];
     CK(cudaMemcpy(h->d_kern[cam], t.data(), nk * TP_CLT * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
-  } else if (layout == TP_KERNELS_CPU) {
-    CK(cudaMemcpy(h->d_kern[cam], kernels, nk * TP_CLT * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
   } else {
-    return fail(h, TP_ERR_ARG, "tp_set_kernels: bad layout");
+    CK(cudaMemcpy(h->d_kern[cam], kernels, nk * TP_CLT * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
   }
   CK(cudaMemcpy(h->d_kext[cam], offs, nk * 8 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_kernels");
   h->planned = 0;
@@ -629,6 +642,7 @@ tp_status tp_calc_kernels(tp_handle *h, int cam, const float *psf, int psf_on_de
   if (cam < 0 || cam >= h->cfg.num_sensors) return fail(h, TP_ERR_ARG, "tp_calc_kernels: bad camera");
   if (h->cfg.kernels_hor <= 0) return fail(h, TP_ERR_STATE, "tp_calc_kernels: handle created without kernels");
   cudaStream_t st = pick_stream(h, stream);
+  if (after_work(h, st, "tp_calc_kernels") != TP_OK) return TP_ERR_CUDA;
   const size_t nk = (size_t)h->cfg.kernels_hor * h->cfg.kernels_vert * h->cfg.num_colors;
   if (psf_on_device) {
     CK(launch_kernel_prep(psf, (int)nk, normalize, h->d_kern[cam], h->d_kext[cam], st), "tp_calc_kernels");
@@ -692,6 +706,7 @@ tp_status tp_set_image(tp_handle *h, int cam, const void *image, int dtype, size
   size_t es = dtype == TP_U16 ? 2 : 4;
   if (pitch == 0) pitch = h->cfg.width;
   if (pitch < (size_t)h->cfg.width) return fail(h, TP_ERR_ARG, "tp_set_image: pitch < width");
+  if (after_work(h, h->stream, "tp_set_image") != TP_OK) return TP_ERR_CUDA;
   CK(cudaMemcpy2DAsync(h->d_images[cam], h->cfg.width * es, image, pitch * es, h->cfg.width * es, h->cfg.height,
                        cudaMemcpyHostToDevice, h->stream),
      "tp_set_image");
@@ -708,6 +723,7 @@ tp_status tp_set_image_async(tp_handle *h, int cam, const void *image, int dtype
   size_t es = dtype == TP_U16 ? 2 : 4;
   if (pitch == 0) pitch = h->cfg.width;
   if (pitch < (size_t)h->cfg.width) return fail(h, TP_ERR_ARG, "tp_set_image_async: pitch < width");
+  if (after_work(h, pick_stream(h, stream), "tp_set_image_async") != TP_OK) return TP_ERR_CUDA;
   CK(cudaMemcpy2DAsync(h->d_images[cam], h->cfg.width * es, image, pitch * es, h->cfg.width * es, h->cfg.height,
                        cudaMemcpyHostToDevice, pick_stream(h, stream)),
      "tp_set_image_async");
@@ -812,6 +828,7 @@ tp_status tp_set_lpf(tp_handle *h, const float *lpf) {
     h->lpf_on = 0;
     return TP_OK;
   }
+  if (work_done(h, "tp_set_lpf") != TP_OK) return TP_ERR_CUDA;
   CK(cudaMemcpy(h->d_lpf_rbg, lpf, h->cfg.num_colors * 64 * sizeof(float), cudaMemcpyHostToDevice), "tp_set_lpf");
   h->lpf_on = 1;
   return TP_OK;
@@ -901,6 +918,32 @@ tp_status tp_set_corr(tp_handle *h, const tp_corr_params *p, const tp_pair *pair
         }
         cd.strip_code[kind][e][dn] = code;
       }
+  // the adjoint's rounds: greedily, in pair order, up to 4 combined-strip pairs on distinct sensors
+  {
+    std::vector<int> left;
+    for (int i = 0; i < np; i++)
+      if (pairs[i].in_combo) left.push_back(i);
+    int nr = 0;
+    while (!left.empty()) {
+      std::vector<int> rest;
+      unsigned long long used = 0;
+      int k = 0;
+      for (int i : left) {
+        const unsigned long long m = (1ull << pairs[i].cam1) | (1ull << pairs[i].cam2);
+        if (k < 4 && !(used & m)) {
+          cd.adj_round[nr][k++] = (short)i;
+          used |= m;
+        } else {
+          rest.push_back(i);
+        }
+      }
+      for (; k < 4; k++) cd.adj_round[nr][k] = -1;
+      nr++;
+      left.swap(rest);
+    }
+    cd.adj_rounds = nr;
+  }
+  if (work_done(h, "tp_set_corr") != TP_OK) return TP_ERR_CUDA;  // before the free and the table copy
   if (np > h->corr_capacity) {
     dfree(h, h->d_corr);
     h->d_corr = nullptr;
@@ -1080,8 +1123,10 @@ tp_status tp_process(tp_handle *h, void *stream) {
 
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block) {
   if (!h) return TP_ERR_ARG;
-  // warp per tile: tiles per CTA == warps per CTA (<= 4); pair per warp: 1 tile per CTA of 2, 3 or 4 warps
-  if (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4)
+  // warp per tile: tiles per CTA == warps per CTA (<= 4); pair per warp: 1 tile per CTA of 2, 3 or 4 warps;
+  // (1, 6): the two-pass forward (CLT pass, then a CTA of one warp per pair)
+  const bool two_pass = tiles_per_block == 1 && warps_per_block == 6;
+  if (!two_pass && (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4))
     return fail(h, TP_ERR_ARG, "tp_set_schedule: out of range");
   if (warps_per_block == 0) warps_per_block = tiles_per_block;
   if (tiles_per_block > 1 && tiles_per_block != warps_per_block)

@@ -67,6 +67,7 @@ struct CorrConst {
   float wndx[32];
   float notch[15];
   int hor_pairs[8], vert_pairs[8];  // pair indices of kind 0 / 1 (ortho maxima)
+  int adj_rounds;                   // rounds of the adjoint's pair schedule (CorrDev::adj_round)
   PairDev pairs[TP_MAXP];
 };
 
@@ -75,6 +76,10 @@ struct CorrDev : CorrConst {
   // iy0*15+ix0 in bits 0-7, interpolation case in bits 8-9, -1 outside the surface
   // (lane-divergent reads: kept in global memory, L1-cached)
   short strip_code[4][TP_MAX_STRIP * 15][2];
+  // the adjoint's pair schedule: per round up to 4 pairs of the combined strip (-1: none) whose
+  // sensors are all distinct, so the four warps of a tile add their pairs' CLT gradients into
+  // disjoint sensors, and every sensor's gradient is summed in the same pair order in every run
+  short adj_round[TP_MAXP][4];
 };
 
 struct SceneDev {
@@ -152,7 +157,6 @@ cudaError_t upload_fused_constants();
 // GPU_DTT24_DRV counterpart (tp_fused.cu): 2D DTT of one mode on every 8x8 block
 cudaError_t launch_dtt8x8(float *dst, const float *src, int stride, int width, int height, int mode,
                           cudaStream_t st);
-int fused_smem_bytes(const SceneDev &sc, int tpb, int nw);
 // batched plans (tp_plan.cu) and persistent forward over many scenes (tp_fused.cu):
 // scene classes 0 = colour warp-per-tile, 1 = mono warp-per-tile, 2 = mono pair-per-warp
 cudaError_t launch_plan_batch(const SceneDev *scenes_dev, const int *task_off_dev, int n, int total_tasks,

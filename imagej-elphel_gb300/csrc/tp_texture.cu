@@ -92,7 +92,9 @@ __device__ __forceinline__ void debayer2(const TexConst &tc, float (*s_ic)[TX_P 
 
 // Per-pixel stage of a tile (debayer, shot noise, port weights, dust removal, alpha, RGB mix);
 // FULL: all four ports used (the usual tile mask 0xF), so every mask test folds away.  Thread
-// pr covers column pr & 15 of rows 2 (pr >> 4) and 2 (pr >> 4) + 1.
+// pr covers column pr & 15 of rows y0, y0 + 1: y0 = 2 (pr >> 5) for the first 16 lanes of a warp,
+// 8 rows further down for the other 16, whose 18-float rows then start 144 floats (16 banks) on,
+// so a warp's shared-memory reads of the stencils fall on 32 distinct banks.
 template <bool FULL>
 __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_P * TX_P], const float *s_win2,
                                            const float *s_rwin2, float *out, int mask_rt, int used_rt,
@@ -100,7 +102,7 @@ __device__ __forceinline__ void tex_pixels(const TexConst &tc, float (*s_ic)[TX_
   const int mask = FULL ? 0xF : mask_rt;
   const int used = FULL ? 4 : used_rt;
   for (int pr = tid; pr < 128; pr += TX_THREADS) {
-  const int x = pr & 15, y0 = (pr >> 4) * 2;
+  const int x = pr & 15, y0 = ((pr >> 5) << 1) + (((pr >> 4) & 1) << 3);
   float dd[2][4][3];
   debayer2(tc, s_ic, s_win2, x, y0, dd, part);
 #pragma unroll 1

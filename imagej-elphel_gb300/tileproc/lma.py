@@ -84,11 +84,12 @@ ANNEAL = (9.0, 4.0)
 
 
 def refine_stages(iterations, invalid_cost=1.0, anneal=ANNEAL):
-    """[(iterations, cap)] of the stages refine runs"""
+    """[(iterations, cap)] of the stages refine runs: iterations / (2 len(anneal)) under each cap of
+    anneal in turn, the rest (at least half) under invalid_cost"""
     if invalid_cost is None or not anneal:
         return [(iterations, invalid_cost)]
-    q = iterations // 4
-    return [(q, anneal[0]), (q, anneal[1]), (iterations - 2 * q, invalid_cost)]
+    q = iterations // (2 * len(anneal))
+    return [(q, a) for a in anneal] + [(iterations - q * len(anneal), invalid_cost)]
 
 
 def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART, free_disparity=True,
@@ -104,7 +105,7 @@ def refine(tp, geometry, disparity, tile_op=None, iterations=20, lam=LAM_RESTART
     cost is only piecewise smooth (window corners move by whole pixels, peaks appear and vanish),
     so a point can be a dead end for every damping: then the undamped step is tried at other
     lengths (STALL_SCALES), the best that lowers the cost is taken, and the damping starts again
-    from LAM_RESTART."""
+    from LAM_RESTART.  callback(iteration, cost, damping, geometry) follows every iteration."""
     g, D, history, done = geometry, disparity, [], 0
     for its, cap in refine_stages(iterations, invalid_cost, anneal):
         if its <= 0:
@@ -189,5 +190,5 @@ def _refine_stage(tp, geometry, disparity, tile_op, iterations, lam, free_dispar
         _evaluate(tp, g, D.astype(np.float32), op, invalid_cost)
         history.append(cost)
         if callback:
-            callback(it0 + it, cost, lam)
+            callback(it0 + it, cost, lam, g)
     return g, D, history

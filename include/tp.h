@@ -169,7 +169,11 @@ tp_status tp_default_texture_params(tp_texture_params *p);
 /* the 6 quad pairs Correlation2d.PAIRS[0..5]; returns the count in *n */
 tp_status tp_quad_pairs(tp_pair *pairs, int *n);
 
-/* inputs */
+/* inputs
+ * A setter that overwrites a device buffer is ordered after the handle's work already enqueued,
+ * on whichever stream: the asynchronous ones (tp_set_image_async, tp_calc_kernels,
+ * tp_set_tile_ops) wait for it on their stream, the synchronous ones (tp_set_geometry,
+ * tp_set_kernels, tp_set_image, tp_set_lpf, tp_set_corr) on the host before they copy. */
 /* GeometryCorrection set-up used by stage 1 (getPortsCoordinatesAndDerivatives) */
 tp_status tp_set_geometry(tp_handle *h, const tp_geometry *g);
 
@@ -270,9 +274,11 @@ tp_status tp_textures(tp_handle *h, void *stream);
 tp_status tp_process(tp_handle *h, void *stream);
 /* schedule of the fused forward kernel: tiles per CTA and warps per CTA (0 = defaults): warp per
  * tile with 1, 2 or 4 tiles per CTA (tiles_per_block == warps_per_block), or one tile per CTA of 2,
- * 3 or 4 warps splitting its colour items and pairs (3 warps: 80 registers, 8 CTAs per SM);
- * chosen by tileproc.autotune (no reference counterpart: the reference hard-codes
- * TILES_PER_BLOCK, GPUTileProcessor.java:92) */
+ * 3 or 4 warps splitting its colour items and pairs (3 warps: 80 registers, 8 CTAs per SM), or
+ * (1, 6): two passes, the CLT of every tile first, then one CTA per tile with a warp per pair
+ * (u16 Bayer quads of at most 6 pairs with an unfiltered stored CLT; other scenes take the
+ * default); all give identical results; chosen by tileproc.autotune (no reference counterpart:
+ * the reference hard-codes TILES_PER_BLOCK, GPUTileProcessor.java:92) */
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block);
 tp_status tp_synchronize(tp_handle *h);
 

@@ -168,3 +168,17 @@ def test_colour_adjoint_recompute_is_refused():
         tp.setAdjointMode(recompute_clt=True)
         with pytest.raises(_lib.TpError, match="mono"):
             tp.backward()
+
+
+def test_colour_backward_is_deterministic():
+    """The colour adjoint sums in a fixed order too: repeated passes agree bit for bit."""
+    sc, k, e, D = _setup()
+    with _gpu(sc, k, e, D) as tp:
+        runs = []
+        for _ in range(3):
+            ge, gd = tp.backward()
+            runs.append((ge, gd, tp.getPortSensitivities()) + tuple(tp.getDisparityJacobian()))
+    assert np.isfinite(runs[0][2]).any()
+    for r in runs[1:]:
+        for a, b in zip(runs[0], r):
+            assert np.array_equal(a, b, equal_nan=True)
