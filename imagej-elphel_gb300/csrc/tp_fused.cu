@@ -764,155 +764,6 @@ __global__ void __launch_bounds__(128) extract_kernel(const __grid_constant__ Sc
 }
 
 // ---------------------------------------------------------------------------
-// Two-pass forward for u16 Bayer quads: clt_win_kernel computes every tile's CLT
-// (phase A) into HBM, pair_kernel then correlates a tile's pairs with one warp per
-// pair (phase B) and extract_kernel extracts (phase C).  The fused kernel holds a
-// tile's 12 KB CLT per warp for its pairs, which caps it at 16 warps per SM; here
-// the CLT pass keeps only two window slots (6 KB) per warp and the pair pass one
-// CLT (double-buffered) per CTA of six warps.  The CLT makes one more trip
-// through HBM.  The arithmetic is the fused kernel's, item for item and pair for
-// pair, and the pairs' strip and ortho factors are multiplied in pair order, so
-// the outputs are identical.
-// ---------------------------------------------------------------------------
-constexpr int AW_SLOT = 4 * 16 * WROW / 2;      // floats: one item's four staged sensor windows
-constexpr int AW_FLOATS = 2 * AW_SLOT + 4 * 72; // per warp: two window slots, four transpose buffers
-constexpr int CLT_WARPS = 4;
-
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-__global__ void __launch_bounds__(32 * CLT_WARPS, 5) clt_win_kernel(const __grid_constant__ SceneDev sc) {
-  extern __shared__ float sm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
-  const int S = sc.num_sensors, rr = sc.bayer_red_row, rc = sc.bayer_red_col;
-  float *smw = sm + warp * AW_FLOATS;
-  float *tbuf = smw + 2 * AW_SLOT + q * 72;
-  const bool act = q < S;
-  const int sidx = act ? q : S - 1;
-  const uint16_t *img = (const uint16_t *)sc.images[sidx];
-  const int stride = gridDim.x * CLT_WARPS;
-  int task = blockIdx.x * CLT_WARPS + warp;
-  if (task >= sc.num_tasks) return;  // whole warps; no CTA barriers below
-  SubtilePlan p = load_plan(sc, task, sidx, 0);
-  if (act) stage_window(sc, img, p.tlx, p.tly, (uint16_t *)(smw + q * (AW_SLOT / 4)), r);
-  cp_async_commit();
-  int k = 0;  // item counter: item k's windows are in slot k & 1
-  for (; task < sc.num_tasks; task += stride) {
-    const int txy = sc.task_txy[task];
-    const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-#pragma unroll 1
-    for (int c = 0; c < 3; c++, k++) {
-      // the next item's windows go into the other slot, which item k - 1 has read
-      const int nt = c < 2 ? task : task + stride;
-      SubtilePlan pn = p;
-      __syncwarp();
-      if (nt < sc.num_tasks) {
-        pn = load_plan(sc, nt, sidx, c < 2 ? c + 1 : 0);
-        if (act) stage_window(sc, img, pn.tlx, pn.tly, (uint16_t *)(smw + ((k + 1) & 1) * AW_SLOT + q * (AW_SLOT / 4)), r);
-      }
-      cp_async_commit();
-      cp_async_wait_prev();  // this item's windows, copied by every lane
-      __syncwarp();
-      SWin w;
-      w.base = (const uint16_t *)(smw + (k & 1) * AW_SLOT + sidx * (AW_SLOT / 4));
-      w.sx = p.tlx - (p.tlx & ~7);
-      w.scale = sc.color_scale[c];
-      float o[4][8];
-      if (c < 2) {
-        const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
-        subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
-      } else {
-        const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
-        subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
-      }
-      const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
-      conv_shift(o, kp, p.rx, p.ry, r);
-      if (act) store_clt(sc, c, r, sc.clt + ((tile * S + q) * 3 + c) * TP_CLT + r * 8, o);
-      p = pn;
-    }
-  }
-  cp_async_wait_all();
-}
-
-// one CTA of P (<= 6) warps per tile, grid-stride: warp pi runs pair pi of the tile whose CLT the
-// CTA copied into shared memory during the previous tile; warp 0 multiplies the pairs' strip and
-// ortho factors in pair order into the combined-strip buffer and the ortho products for
-// extract_kernel.  Shared: [2][S * 3 * 256] CLT, [P][SCR] scratch, [P][32 NT] strip factors,
-// [P][32][8] ortho factors.
-template <int NT>
-__global__ void __launch_bounds__(192, 4) pair_kernel(const __grid_constant__ SceneDev sc,
-                                                      const __grid_constant__ FwdShape fs,
-                                                      const __grid_constant__ CorrConst cfg) {
-  extern __shared__ float sm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int P = fs.P, RE = fs.RE, cf = fs.clt_floats, nch = cf / 4;
-  float *scr = sm + 2 * cf + warp * SCR;
-  float *fcmb = sm + 2 * cf + P * SCR;
-  float *fort = fcmb + P * 32 * NT;
-  const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
-  const bool log_mode = cfg.log_combine;
-  int task = blockIdx.x;
-  if (task >= sc.num_tasks) return;  // the whole CTA
-  int txy = sc.task_txy[task];
-  size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-  for (int i = threadIdx.x; i < nch; i += blockDim.x) cp_async16(sm + 4 * i, sc.clt + tile * cf + 4 * i);
-  cp_async_commit();
-  for (int k = 0; task < sc.num_tasks; task += gridDim.x, k++) {
-    const int next = task + gridDim.x;
-    size_t ntile = 0;
-    if (next < sc.num_tasks) {  // into the buffer the CTA finished reading before the last barrier
-      txy = sc.task_txy[next];
-      ntile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
-      float *dst = sm + ((k + 1) & 1) * cf;
-      for (int i = threadIdx.x; i < nch; i += blockDim.x) cp_async16(dst + 4 * i, sc.clt + ntile * cf + 4 * i);
-    }
-    cp_async_commit();
-    cp_async_wait_prev();  // this tile's CLT, copied by every thread
-    __syncthreads();
-    float cmb[8], oprod[8];
-#pragma unroll
-    for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
-#pragma unroll
-    for (int i = 0; i < 8; i++) oprod[i] = 1.f;
-    fwd_pair<3, NT, true>(sc, cfg, tile, P, warp, RE, log_mode, strip_code, sm + (k & 1) * cf, scr, lane, cmb,
-                          nullptr, oprod);
-#pragma unroll
-    for (int t = 0; t < NT; t++) fcmb[warp * 32 * NT + lane + 32 * t] = cmb[t];
-    float4 *of = (float4 *)(fort + (warp * 32 + lane) * 8);
-    of[0] = make_float4(oprod[0], oprod[1], oprod[2], oprod[3]);
-    of[1] = make_float4(oprod[4], oprod[5], oprod[6], oprod[7]);
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-      for (int t = 0; t < NT; t++) {
-        const int e = lane + 32 * t;
-        if (e < RE) {
-          float v = log_mode ? 0.f : 1.f;
-          for (int pi = 0; pi < P; pi++) {
-            const float f = fcmb[pi * 32 * NT + e];
-            v = log_mode ? v + f : v * f;
-          }
-          sc.combo[tile * RE + e] = v;
-        }
-      }
-      float o[8];
-#pragma unroll
-      for (int i = 0; i < 8; i++) o[i] = 1.f;
-      for (int pi = 0; pi < P; pi++) {
-        const float4 *fp = (const float4 *)(fort + (pi * 32 + lane) * 8);
-        const float4 a = fp[0], b = fp[1];
-        o[0] *= a.x; o[1] *= a.y; o[2] *= a.z; o[3] *= a.w;
-        o[4] *= b.x; o[5] *= b.y; o[6] *= b.z; o[7] *= b.w;
-      }
-      float4 *ob = (float4 *)(sc.osum + (tile * 32 + lane) * 8);
-      ob[0] = make_float4(o[0], o[1], o[2], o[3]);
-      ob[1] = make_float4(o[4], o[5], o[6], o[7]);
-    }
-    tile = ntile;
-  }
-  cp_async_wait_all();
-}
-
-// ---------------------------------------------------------------------------
 // pair-per-warp schedule: a CTA of nw warps per tile shares the tile's CLT; the
 // warps split the (colour, sensor-group) items, then the pairs, and warp 0
 // combines their partial strip products for the extraction.  For many pairs
@@ -1478,54 +1329,14 @@ static cudaError_t launch_persistent(K kernel, int threads, int bytes, int units
   return cudaGetLastError();
 }
 
-// the two-pass forward's conditions: staged u16 Bayer quad windows, the separate extraction's
-// buffers, at most 6 pairs, and a stored CLT that is the correlation's (not low-pass filtered)
-static bool two_pass_ok(const SceneDev &sc) {
-  bool all16 = true;
-  for (int i = 0; i < sc.num_sensors; i++) all16 = all16 && sc.img_dtype[i] == 1;
-  return all16 && sc.num_colors == 3 && sc.num_sensors <= 4 && sc.combo && sc.osum && sc.num_pairs >= 1 &&
-         sc.num_pairs <= 6 && !(sc.lpf_rbg && sc.clt_lpf_mask);
-}
-
-static cudaError_t launch_two_pass(const SceneDev &sc, const CorrConst &cc, cudaStream_t st) {
-  const int abytes = CLT_WARPS * AW_FLOATS * 4;
-  cudaError_t e = cudaFuncSetAttribute(clt_win_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, abytes);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 152, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, clt_win_kernel, 32 * CLT_WARPS, abytes);
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const int units = (sc.num_tasks + CLT_WARPS - 1) / CLT_WARPS;
-  clt_win_kernel<<<units < sms * per_sm ? units : sms * per_sm, 32 * CLT_WARPS, abytes, st>>>(sc);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  FwdShape f = make_shape(sc, 1);
-  f.nw = f.P;
-  const int nt = f.RE <= 32 ? 1 : 8;
-  const int bbytes = (2 * f.clt_floats + f.P * SCR + f.P * 32 * nt + f.P * 256) * 4;
-  e = (nt == 1) ? launch_persistent(pair_kernel<1>, 32 * f.P, bbytes, sc.num_tasks, sc, f, cc, st)
-                : launch_persistent(pair_kernel<8>, 32 * f.P, bbytes, sc.num_tasks, sc, f, cc, st);
-  if (e != cudaSuccess) return e;
-  if (nt == 1) extract_kernel<1><<<(sc.num_tasks + 3) / 4, 128, 0, st>>>(sc, cc, f.quad, f.RE);
-  else extract_kernel<8><<<(sc.num_tasks + 3) / 4, 128, 0, st>>>(sc, cc, f.quad, f.RE);
-  return cudaGetLastError();
-}
-
 // Schedules: tiles_per_block == warps_per_block (<= 4): warp per tile;
-// tiles_per_block == 1 with warps_per_block 2, 3 or 4: pair per warp (CTA per tile);
-// tiles_per_block == 1 with warps_per_block 6: the two-pass forward (u16 Bayer quads; other
-// scenes take the default).
+// tiles_per_block == 1 with warps_per_block 2, 3 or 4: pair per warp (CTA per tile).
 cudaError_t launch_fused_forward(const SceneDev &sc, const CorrConst &cc, int tpb, int nw, cudaStream_t st) {
   const int ntiles = sc.tilesX * sc.tilesY;
   disp_init_kernel<<<(ntiles * TP_NDISP + 255) / 256, 256, 0, st>>>(sc.disp, ntiles);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || sc.num_tasks <= 0) return e;
   if (sc.strip_rows * 15 > 8 * 32) return cudaErrorInvalidConfiguration;
-  if (tpb == 1 && nw == 6) {
-    if (two_pass_ok(sc)) return launch_two_pass(sc, cc, st);
-    tpb = nw = 0;
-  }
   if (tpb <= 0 && nw <= 0 && sc.num_pairs > 8) {  // default for many pairs: four warps share a tile
     tpb = 1;
     nw = 4;

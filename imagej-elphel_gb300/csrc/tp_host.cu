@@ -1123,10 +1123,8 @@ tp_status tp_process(tp_handle *h, void *stream) {
 
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block) {
   if (!h) return TP_ERR_ARG;
-  // warp per tile: tiles per CTA == warps per CTA (<= 4); pair per warp: 1 tile per CTA of 2, 3 or 4 warps;
-  // (1, 6): the two-pass forward (CLT pass, then a CTA of one warp per pair)
-  const bool two_pass = tiles_per_block == 1 && warps_per_block == 6;
-  if (!two_pass && (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4))
+  // warp per tile: tiles per CTA == warps per CTA (<= 4); pair per warp: 1 tile per CTA of 2, 3 or 4 warps
+  if (warps_per_block < 0 || warps_per_block > 4 || tiles_per_block < 0 || tiles_per_block > 4)
     return fail(h, TP_ERR_ARG, "tp_set_schedule: out of range");
   if (warps_per_block == 0) warps_per_block = tiles_per_block;
   if (tiles_per_block > 1 && tiles_per_block != warps_per_block)

@@ -9,9 +9,7 @@ budget:
                           warps sharing the tile's CLT, up to 128 registers;
   (1, 3)                  one tile per CTA of 3 warps (one colour item, then two pairs
                           per warp for a quad colour scene), 80 registers for 8 CTAs
-                          (24 warps) per SM;
-  (1, 6)                  two passes for u16 Bayer quads: the CLT of every tile (6 KB of
-                          shared memory per warp), then a CTA of one warp per pair.
+                          (24 warps) per SM.
 The reference fixes its launch shape at compile time (TILES_PER_BLOCK,
 THREADS_PER_TILE, GPUTileProcessor.java:92-93); here every candidate is timed on
 the caller's own scene and the fastest is kept, per (sensors, colours, pairs,
@@ -19,7 +17,7 @@ size) key.
 """
 import time
 
-SCHEDULES = ((1, 1), (2, 2), (4, 4), (1, 2), (1, 3), (1, 4), (1, 6))
+SCHEDULES = ((1, 1), (2, 2), (4, 4), (1, 2), (1, 3), (1, 4))
 
 _cache = {}
 

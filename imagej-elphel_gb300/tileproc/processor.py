@@ -214,6 +214,7 @@ class GPUTileProcessor:
                 arr[i] = L.TpPair(a, b, kind, in_combo, bx, by)
         self._ck(self._lib.tp_set_corr(self.h, C.byref(params), arr, np_), "tp_set_corr")
         self.num_pairs = np_
+        self.pairs = [(arr[i].cam1, arr[i].cam2, arr[i].kind, arr[i].in_combo) for i in range(np_)]
 
     def setTextureParams(self, params=None, **kw):
         """Texture-tile settings: TpTextureParams or None (CLTParameters defaults), keyword overrides."""

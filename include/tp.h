@@ -274,11 +274,9 @@ tp_status tp_textures(tp_handle *h, void *stream);
 tp_status tp_process(tp_handle *h, void *stream);
 /* schedule of the fused forward kernel: tiles per CTA and warps per CTA (0 = defaults): warp per
  * tile with 1, 2 or 4 tiles per CTA (tiles_per_block == warps_per_block), or one tile per CTA of 2,
- * 3 or 4 warps splitting its colour items and pairs (3 warps: 80 registers, 8 CTAs per SM), or
- * (1, 6): two passes, the CLT of every tile first, then one CTA per tile with a warp per pair
- * (u16 Bayer quads of at most 6 pairs with an unfiltered stored CLT; other scenes take the
- * default); all give identical results; chosen by tileproc.autotune (no reference counterpart:
- * the reference hard-codes TILES_PER_BLOCK, GPUTileProcessor.java:92) */
+ * 3 or 4 warps splitting its colour items and pairs (3 warps: 80 registers, 8 CTAs per SM);
+ * chosen by tileproc.autotune (no reference counterpart: the reference hard-codes
+ * TILES_PER_BLOCK, GPUTileProcessor.java:92) */
 tp_status tp_set_schedule(tp_handle *h, int tiles_per_block, int warps_per_block);
 tp_status tp_synchronize(tp_handle *h);
 

@@ -209,7 +209,7 @@ def test_imclt(oracle):
         assert np.abs(got - want[2]).max() / np.abs(want[2]).max() < 2e-6
 
 
-@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (2, 2), (4, 4), (1, 2), (1, 3), (1, 4), (1, 6)])
+@pytest.mark.parametrize("sched", [(0, 0), (1, 1), (2, 2), (4, 4), (1, 2), (1, 3), (1, 4)])
 def test_stage_kernels_and_schedules_agree(oracle, sched):
     """Per-stage kernels (execConverCorrectTiles/execCorrelate/execExtract) and the fused
     kernel under several CTA schedules give the same results."""
@@ -356,26 +356,3 @@ def test_full_size_circle16_sampled_tiles(oracle):
     print("full size LWIR: %d tiles checked, CLT max %.3g, corr max %.3g, disparity %s" % (
         len(sel), ec.max(), er.max(), summ))
 
-
-def test_two_pass_forward_is_identical():
-    """The two-pass forward (schedule (1, 6): the CLT pass, then a CTA of one warp per pair) runs
-    the fused kernel's arithmetic and multiplies the pairs' factors in pair order: CLT, correlation
-    surfaces and disparity records equal the warp-per-tile kernel's bit for bit, on a ragged task
-    list (a random half of the tiles, the image border included)."""
-    sc = synth.make_scene("quad_bayer", seed=21, width=256, height=192)
-    T = (sc["width"] // 8) * (sc["height"] // 8)
-    rng = np.random.default_rng(8)
-    k, e = synth.random_clt_kernels(rng, 4, 192 // 16 + 2, 256 // 16 + 2, 3)
-    op = (rng.random(T) < 0.5).astype(np.int32)
-    D = (sc["disparity_gt"].reshape(-1) + rng.normal(0, 0.3, T)).astype(np.float32)
-    out = {}
-    with make_gpu(sc, k, e) as tp:
-        tp.setCorrelation()
-        for sched in ((1, 1), (1, 6)):
-            tp.setSchedule(*sched)
-            tp.setFullFrameImages(D, tile_op=op)
-            tp.process()
-            out[sched] = (tp.getClt(), tp.getCorr(), tp.getDisparity())
-    for a, b in zip(out[(1, 1)], out[(1, 6)]):
-        assert np.array_equal(a, b, equal_nan=True)
-    assert np.isfinite(out[(1, 6)][2][op != 0, 1]).mean() > 0.5
