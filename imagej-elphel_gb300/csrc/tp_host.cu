@@ -63,6 +63,8 @@ struct tp_handle {
   float *d_lma = nullptr;    // [tiles][4] LMA disparity, strength, WM, WXY
   float *d_mismatch = nullptr;  // [tiles][pairs][3] lazy-eye mismatch of the last LMA pass that measured it
   size_t mismatch_cap = 0;
+  float *d_pairmax = nullptr;   // [tiles][pairs][3] 2D maxima of the pair surfaces (tp_get_pair_maxima)
+  size_t pairmax_cap = 0;
   int mismatch_pairs = -1;
   int disp_mixed = 0;        // the LMA replaced CM / strength since the last forward
   int lma_valid = 0;         // d_lma holds the LMA of the current forward (POLY for the textures)
@@ -486,6 +488,7 @@ tp_status tp_destroy(tp_handle *h) {
                   h->d_disp, h->d_rbg, h->d_lpf_rbg, h->d_geom, h->d_rdist, h->d_corr_cfg,
                   h->d_tex, h->d_tex_aux, h->d_sens, h->d_dval, h->d_jac_e, h->d_jac_d, h->d_grad_d,
                   h->d_partial, h->d_grad_e, h->d_dldd, h->d_combo, h->d_psf_stage, h->d_rig_corr, h->d_strips, h->d_lma, h->d_mismatch,
+                  h->d_pairmax,
                   h->d_rig_rec, h->d_rig_tmp, h->d_osum};
   for (void *b : bufs) dfree(h, b);
   if (h->ev_stage) {
@@ -1626,6 +1629,28 @@ tp_status tp_get_lma_mismatch(tp_handle *h, float *out) {
   if (!h->d_mismatch || h->mismatch_pairs != h->num_pairs)
     return fail(h, TP_ERR_STATE, "tp_get_lma_mismatch: run tp_lma_refine with mismatch set first");
   return d2h(h, out, h->d_mismatch, (size_t)h->ntiles * h->num_pairs * 3 * sizeof(float), "tp_get_lma_mismatch");
+}
+
+tp_status tp_get_pair_maxima(tp_handle *h, float *out) {
+  if (!h || !out) return TP_ERR_ARG;
+  if (!h->have_corr || h->num_pairs == 0 || !h->d_corr || !h->fwd_valid)
+    return fail(h, TP_ERR_STATE, "tp_get_pair_maxima: run tp_process first");
+  const size_t need = (size_t)h->ntiles * h->num_pairs * 3;
+  if (need > h->pairmax_cap) {
+    if (work_done(h, "tp_get_pair_maxima") != TP_OK) return TP_ERR_CUDA;  // before the free
+    dfree(h, h->d_pairmax);
+    h->d_pairmax = nullptr;
+    h->pairmax_cap = 0;
+    if (dalloc(h, &h->d_pairmax, need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, TP_ERR_NOMEM, "tp_get_pair_maxima: buffer");
+    }
+    h->pairmax_cap = need;
+  }
+  CK(cudaStreamWaitEvent(h->stream, h->ev_work, 0), "tp_get_pair_maxima");
+  CK(launch_pair_maxima(scene_of(h), h->num_pairs, h->d_pairmax, h->stream), "tp_get_pair_maxima");
+  if (mark_work(h, h->stream) != TP_OK) return TP_ERR_CUDA;
+  return d2h(h, out, h->d_pairmax, need * sizeof(float), "tp_get_pair_maxima");
 }
 
 tp_status tp_get_lma(tp_handle *h, float *out) {

@@ -203,6 +203,7 @@ struct TpLmaConst {
   float ly_crazy_poly;
 };
 cudaError_t upload_lma_constants();
+cudaError_t launch_pair_maxima(const SceneDev &sc, int P, float *out, cudaStream_t st);
 cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst &c, float *lma_out,
                        float *mismatch_out, cudaStream_t st);
 // the LMA branch of the rig's inter-camera correlation (tp_lma.cu); cc1: the one-pair set-up

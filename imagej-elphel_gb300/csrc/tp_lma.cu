@@ -1015,3 +1015,69 @@ cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst
   kern<<<grid, 32 * LMA_NW, bytes, st>>>(ld, c);
   return cudaGetLastError();
 }
+
+// The 2D maximum of every task tile's pair surfaces, one warp per surface: the first cell of the
+// largest value in index order (NaN cells count as -inf), then a parabola through it and its two
+// neighbours on each axis (FP64, the fraction clamped to +-0.5 and taken as 0 where a neighbour is
+// not finite).  out [tiles][P][3] = {dx, dy, strength}, px from the centre (x right, y down);
+// {NaN, NaN, 0} where the maximum is on the border or not finite, all NaN outside the task list.
+__global__ void __launch_bounds__(128) pair_max_kernel(const float *__restrict__ corr,
+                                                       const int *__restrict__ task_txy, int num_tasks,
+                                                       int tilesX, int P, float *out) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (long long)num_tasks * P) return;  // whole warps
+  const int task = (int)(w / P), pi = (int)(w - (long long)task * P);
+  const int txy = task_txy[task];
+  const size_t s = ((size_t)(txy >> 16) * tilesX + (txy & 0xffff)) * P + pi;
+  const float *c = corr + s * TP_CORR;
+  float best = -CUDART_INF_F;
+  int bi = lane;
+  for (int i = lane; i < TP_CORR; i += 32) {
+    const float v = c[i];
+    if (v > best) {  // false for NaN
+      best = v;
+      bi = i;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  if (lane != 0) return;
+  const int iy = bi / 15, ix = bi - 15 * iy;
+  float *o = out + s * 3;
+  if (ix < 1 || ix > 13 || iy < 1 || iy > 13 || !isfinite(best)) {
+    o[0] = CUDART_NAN_F;
+    o[1] = CUDART_NAN_F;
+    o[2] = 0.f;
+    return;
+  }
+  float f[2];
+  for (int a = 0; a < 2; a++) {
+    const int st = a ? 15 : 1;
+    const float m = c[bi - st], p = c[bi + st];
+    double fr = 0.0;
+    if (isfinite(m) && isfinite(p)) {
+      const double den = ((double)m - 2.0 * (double)best) + (double)p;
+      if (den < 0.0) fr = fmin(0.5, fmax(-0.5, 0.5 * ((double)m - (double)p) / den));
+    }
+    f[a] = (float)(((a ? iy : ix) - 7) + fr);
+  }
+  o[0] = f[0];
+  o[1] = f[1];
+  o[2] = best;
+}
+
+cudaError_t launch_pair_maxima(const SceneDev &sc, int P, float *out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0xff, (size_t)sc.tilesX * sc.tilesY * P * 3 * sizeof(float), st);  // NaN
+  if (e != cudaSuccess || sc.num_tasks <= 0 || P <= 0) return e;
+  const long long warps = (long long)sc.num_tasks * P;
+  pair_max_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(sc.corr, sc.task_txy, sc.num_tasks, sc.tilesX, P, out);
+  return cudaGetLastError();
+}

@@ -129,6 +129,7 @@ PROTOTYPES = {
     "tp_lma_refine": [_H, C.POINTER(TpLmaParams), _vp],
     "tp_get_lma": [_H, _vp],
     "tp_get_lma_mismatch": [_H, _vp],
+    "tp_get_pair_maxima": [_H, _vp],
     "tp_rig_correlate": [_H, _H, C.c_float, C.c_int, _vp],
     "tp_get_rig": [_H, _vp, _vp],
     "tp_rig_lma": [_H, C.POINTER(TpLmaParams), C.c_int, C.c_int, _vp],

@@ -114,7 +114,8 @@ LOST_PX = 7.0
 def pair_peaks(corr):
     """corr [n][225] (15 x 15 surfaces) -> offsets [n][2] (x right, y down, px from the centre) and
     strength [n]: the integer maximum refined by a parabola through it and its two neighbours on
-    each axis; NaN offsets where the maximum is on the surface's border or not finite"""
+    each axis; NaN offsets where the maximum is on the border or not finite.  The host statement
+    of tp_get_pair_maxima, which the coarse stage reads (the parity test compares the two)."""
     c = np.asarray(corr, np.float32).reshape(-1, 225)
     filled = np.where(np.isnan(c), -np.inf, c)
     i = np.argmax(filled, axis=1)
@@ -155,11 +156,8 @@ def _pair_measure(tp, g, D, op, pairs, huber):
     J = tp.getPortDerivatives()  # [n][S][2][5]: d(x, y) / d(azimuth, tilt, roll, zoom, disparity)
     txy = tp.getTaskTiles()
     tiles = (txy >> 16) * tp.tilesX + (txy & 0xFFFF)
-    corr = tp.getCorr()
-    r = np.empty((len(tiles), len(pairs), 2))
-    st = np.empty((len(tiles), len(pairs)))
-    for k in range(len(pairs)):
-        r[:, k], st[:, k] = pair_peaks(corr[tiles, k])
+    pm = tp.getPairMaxima()[tiles].astype(np.float64)  # [n][P][3]: dx, dy, strength
+    r, st = pm[..., :2], pm[..., 2]
     ok = np.isfinite(r).all(axis=2)
     rn = np.where(ok, np.hypot(r[..., 0], r[..., 1]), 0.0)
     cost = float(np.sum(np.where(ok, _huber(rn, huber), 0.0)) + _huber(LOST_PX, huber) * np.count_nonzero(~ok))
@@ -201,23 +199,31 @@ def _coarse_stage(tp, geometry, disparity, tile_op, iterations, free_disparity, 
         U = np.zeros((n, 4 * S))  # disparity coupling per tile (free_disparity)
         hd = np.zeros(n)
         sd = np.zeros(n)
-        for k, (a, b, _kind, _inc) in enumerate(pairs):
-            wk = w[:, k]
-            Ja, Jb = J[:, a, :, :4], J[:, b, :, :4]
+        ca = np.array([p[0] for p in pairs])
+        cb = np.array([p[1] for p in pairs])
+        Ja, Jb = J[:, ca, :, :4], J[:, cb, :, :4]  # [n][P][2][4]
+        Naa = np.einsum("tp,tpik,tpil->pkl", w, Ja, Ja)
+        Nbb = np.einsum("tp,tpik,tpil->pkl", w, Jb, Jb)
+        Nab = np.einsum("tp,tpik,tpil->pkl", w, Ja, Jb)
+        ga = np.einsum("tp,tpik,tpi->pk", w, Ja, rr)
+        gb = np.einsum("tp,tpik,tpi->pk", w, Jb, rr)
+        for k, (a, b) in enumerate(zip(ca, cb)):
             ia, ib = slice(4 * a, 4 * a + 4), slice(4 * b, 4 * b + 4)
-            Nab = np.einsum("t,tik,til->kl", wk, Ja, Jb)
-            N[ia, ia] += np.einsum("t,tik,til->kl", wk, Ja, Ja)
-            N[ib, ib] += np.einsum("t,tik,til->kl", wk, Jb, Jb)
-            N[ia, ib] -= Nab
-            N[ib, ia] -= Nab.T
-            gv[ia] += np.einsum("t,tik,ti->k", wk, Ja, rr[:, k])
-            gv[ib] -= np.einsum("t,tik,ti->k", wk, Jb, rr[:, k])
-            if free_disparity:
-                kd = J[:, a, :, 4] - J[:, b, :, 4]  # [n][2]
-                hd += wk * np.einsum("ti,ti->t", kd, kd)
-                sd += wk * np.einsum("ti,ti->t", kd, rr[:, k])
-                U[:, ia] += wk[:, None] * np.einsum("tik,ti->tk", Ja, kd)
-                U[:, ib] -= wk[:, None] * np.einsum("tik,ti->tk", Jb, kd)
+            N[ia, ia] += Naa[k]
+            N[ib, ib] += Nbb[k]
+            N[ia, ib] -= Nab[k]
+            N[ib, ia] -= Nab[k].T
+            gv[ia] += ga[k]
+            gv[ib] -= gb[k]
+        if free_disparity:
+            kd = J[:, ca][..., 4] - J[:, cb][..., 4]  # [n][P][2]
+            hd = np.einsum("tp,tpi,tpi->t", w, kd, kd)
+            sd = np.einsum("tp,tpi,tpi->t", w, kd, rr)
+            ua = np.einsum("tp,tpik,tpi->tpk", w, Ja, kd)
+            ub = np.einsum("tp,tpik,tpi->tpk", w, Jb, kd)
+            for k, (a, b) in enumerate(zip(ca, cb)):
+                U[:, 4 * a:4 * a + 4] += ua[:, k]
+                U[:, 4 * b:4 * b + 4] -= ub[:, k]
         inv = np.where(hd > 0, 1.0 / np.maximum(hd, 1e-30), 0.0)
         if free_disparity:  # the per-tile disparities eliminated (their block is diagonal)
             N -= U.T @ (U * inv[:, None])

@@ -313,6 +313,12 @@ class GPUTileProcessor:
         self._ck(self._lib.tp_get_lma_mismatch(self.h, _ptr(out)), "tp_get_lma_mismatch")
         return out
 
+    def getPairMaxima(self):
+        """[tiles][pairs][3] 2D maximum {dx, dy, strength} of every pair surface of the last process()."""
+        out = np.zeros((self.tilesY * self.tilesX, self.num_pairs, 3), dtype=np.float32)
+        self._ck(self._lib.tp_get_pair_maxima(self.h, _ptr(out)), "tp_get_pair_maxima")
+        return out
+
     def getLma(self):
         out = np.zeros((self.tilesY * self.tilesX, 4), dtype=np.float32)
         self._ck(self._lib.tp_get_lma(self.h, _ptr(out)), "tp_get_lma")

@@ -363,6 +363,18 @@ tp_status tp_default_lma_params(tp_lma_params *p);
 tp_status tp_lma_refine(tp_handle *h, const tp_lma_params *p, void *stream);
 /* out [tilesY*tilesX][4] */
 tp_status tp_get_lma(tp_handle *h, float *out);
+/* The 2D maximum of every pair's correlation surface of the last tp_process: out
+ * [tilesY*tilesX][num_pairs][3] = {dx, dy, strength}, px from the surface centre (x right,
+ * y down): the first cell of the largest value in index order (NaN cells skipped), refined by a
+ * parabola through it and its two neighbours on each axis (the fraction clamped to +-0.5); {NaN,
+ * NaN, 0} where the maximum is on the surface's border or no cell is finite, all NaN for tiles
+ * outside the task list.  A pair's maximum lies at (port error of cam1) - (port error of cam2):
+ * the per-pair offsets of any pair layout that the extrinsic refinement's coarse stage fits, as
+ * the reference's extrinsic fitting consumes its lazy-eye pair offsets (clt_mismatch,
+ * ImageDtt.java:2340-2418; AlignmentCorrection).  No reference counterpart as an entry point.
+ * Computed on the device (a warp per surface) after the handle's work, then copied like the
+ * other getters. */
+tp_status tp_get_pair_maxima(tp_handle *h, float *out);
 /* out [tilesY*tilesX][num_pairs][3] = {dx, dy, strength} per pair (NaN, NaN, 0 where not measured),
  * after tp_lma_refine with mismatch set */
 tp_status tp_get_lma_mismatch(tp_handle *h, float *out);

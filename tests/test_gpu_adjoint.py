@@ -317,3 +317,24 @@ def test_coarse_stage_recovers_extrinsics(seed):
     assert err(g) < err(g0) / 20
     for k in lma.KEYS:
         assert abs(sum(g[k]) - sum(g0[k])) < 1e-6
+
+
+def test_pair_maxima_match_host_statement():
+    """tp_get_pair_maxima (a warp per pair surface on the device) against lma.pair_peaks on the
+    surfaces read back: the same cells (border and non-finite maxima in the same places), the same
+    strengths, offsets within 1e-5 px (the parabola's FP64 arithmetic rounds one difference
+    differently)."""
+    from tileproc import lma
+    sc, g, pairs, D = _setup()
+    with _gpu(sc, g, pairs, D) as tp:
+        pm = tp.getPairMaxima()
+        corr = tp.getCorr()
+    P = len(pairs)
+    off, st = lma.pair_peaks(corr.reshape(-1, 225))
+    off, st = off.reshape(T, P, 2), st.reshape(T, P)
+    ok = np.isfinite(off).all(axis=-1)
+    assert ok.mean() > 0.9
+    assert np.array_equal(ok, np.isfinite(pm[..., :2]).all(axis=-1))
+    assert np.abs(pm[..., :2][ok] - off[ok]).max() < 1e-5
+    assert np.array_equal(pm[..., 2][ok], st[ok].astype(np.float32))
+    assert (pm[..., 2][~ok] == 0).all()

@@ -185,8 +185,9 @@ class PairPeakProcessor:
         t = np.arange(self.T)
         return ((t // self.tilesX) << 16) | (t % self.tilesX)
 
-    def getCorr(self):
-        return self.corr
+    def getPairMaxima(self):
+        off, st = lma.pair_peaks(self.corr.reshape(-1, 225))
+        return np.concatenate([off, st[:, None]], axis=1).reshape(self.T, self.num_pairs, 3).astype(np.float32)
 
 
 def _geom_of(e, S):
