@@ -28,9 +28,10 @@
 // reverse chain in registers and per-warp buffers (the transposed DCT-IIe is
 // the transposed butterfly of the forward one) and adding into the gradient;
 // the pairs go in rounds of four on distinct sensors (scheduled on the host),
-// a barrier between rounds, so the gradient sums are taken in a fixed order
-// without atomics; finally the warps split the sensors for the forward-mode
-// shift derivatives.
+// a barrier between rounds, so the gradient sums over the pairs are taken in a
+// fixed order without atomics (a pair's strip taps go into its own 15x15
+// gradient with one warp's shared-memory atomics); finally the warps split the
+// sensors for the forward-mode shift derivatives.
 #include "tp_dtt.cuh"
 
 namespace {

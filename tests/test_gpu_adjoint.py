@@ -269,9 +269,10 @@ def test_lma_recovers_extrinsics_full_scene(oracle):
 
 
 def test_backward_is_deterministic():
-    """Every sum of the adjoint is taken in a fixed order (the pairs of a tile in rounds on
-    distinct sensors, the tiles' gradient terms in block order), so repeated backward passes over
-    the same forward agree bit for bit; the extrinsic refinement then repeats exactly."""
+    """The adjoint's sums over pairs and tiles are taken in a fixed order (the pairs of a tile in
+    rounds on distinct sensors, the tiles' gradient terms in block order; only a pair's own strip
+    taps use one warp's shared-memory atomics), and repeated backward passes over the same forward
+    agree bit for bit; the extrinsic refinement then repeats exactly."""
     sc, g, pairs, D = _setup()
     with _gpu(sc, g, pairs, D) as tp:
         runs = []
