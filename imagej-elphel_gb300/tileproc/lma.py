@@ -17,7 +17,13 @@ Note on observability: with only the combined disparity per tile, a change
 of the per-tile target disparities can absorb any residual, so the
 extrinsics move only as far as the damping of the disparity block lets them;
 with free_disparity=False the target disparities stay fixed and the
-extrinsics alone are fitted.
+extrinsics alone are fitted.  The pairs' 2D maxima of the coarse stage see
+each pair's offset across its baseline as well, so there free disparities
+cost little: measured on the 16 x 640 x 512 scene with target disparities
+also off by N(0, 0.3) px, the coarse stage reaches 1e-5 rad and a median
+disparity error of 0.14 px (from 0.20), while the 20 adjoint-driven
+iterations after it, whose disparities absorb the residual, drift to 1e-4 ..
+5e-4 rad and 0.30 px.
 
 Far from the solution, with ports off by a pixel or more, each pair's peak lies
 off its strip line, the combined strip is smeared and the combined disparity

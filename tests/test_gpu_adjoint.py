@@ -285,13 +285,15 @@ def test_backward_is_deterministic():
             assert np.array_equal(a, b, equal_nan=True)
 
 
-@pytest.mark.parametrize("seed", [13, 14])
-def test_coarse_stage_recovers_extrinsics(seed):
+@pytest.mark.parametrize("seed,free", [(13, False), (14, False), (13, True)])
+def test_coarse_stage_recovers_extrinsics(seed, free):
     """The coarse stage alone (lma._coarse_stage) on the full 16x640x512 scene from extrinsics off
     by N(0, 3e-3) rad, the starts where the adjoint-driven iteration alone stops in a dead end: the
     error less each parameter's mean over the sensors falls below a twentieth (measured: 2.6e-3 ..
     3.3e-3 to 3e-5 rad for azimuth and tilt, 1e-5 for roll and zoom, in 3 to 5 steps), and the sums
-    over the sensors, which the offsets barely see, are held."""
+    over the sensors, which the offsets barely see, are held.  With free disparities (target
+    disparities also off by N(0, 0.3) px and fitted per tile) the extrinsics reach 1e-5 rad and the
+    disparities' median error falls from 0.20 to 0.14 px (measured)."""
     from tileproc import lma
     w, h = 640, 512
     t = (w // 8) * (h // 8)
@@ -301,12 +303,13 @@ def test_coarse_stage_recovers_extrinsics(seed):
     g0 = copy.deepcopy(gt)
     for k in lma.KEYS:
         g0[k] = (np.asarray(g0[k]) + rng.normal(0, 3e-3, 16)).tolist()
-    D = sc["disparity_gt"].reshape(-1).astype(np.float32)
+    Dt = sc["disparity_gt"].reshape(-1).astype(np.float64)
+    D = Dt + rng.normal(0, 0.3, t) if free else Dt
     with GPUTileProcessor(16, w, h) as tp:
         tp.setGeometry(g0)
         tp.setBayerImages(sc["images"])
         tp.setCorrelation(pairs=synth.circle_pairs(gt))
-        g, _, costs = lma._coarse_stage(tp, g0, D, np.ones(t, np.int32), lma.COARSE, False, None)
+        g, Dn, costs = lma._coarse_stage(tp, g0, D, np.ones(t, np.int32), lma.COARSE, free, None)
 
     def err(gg):
         e = np.array([np.asarray(gg[k]) - np.asarray(gt[k]) for k in lma.KEYS])
@@ -318,6 +321,10 @@ def test_coarse_stage_recovers_extrinsics(seed):
     assert err(g) < err(g0) / 20
     for k in lma.KEYS:
         assert abs(sum(g[k]) - sum(g0[k])) < 1e-6
+    if free:
+        before, after = np.median(np.abs(D - Dt)), np.median(np.abs(Dn - Dt))
+        print("disparity median error %.3f -> %.3f px" % (before, after))
+        assert after < 0.8 * before
 
 
 def test_pair_maxima_match_host_statement():
