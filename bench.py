@@ -710,9 +710,35 @@ def run_ours(args):
         torch.cuda.set_stream(stream)
 
     fwd_adj = None
+    colour_adj = None
     if rank == 0 and not args.no_adjoint:
         fwd_adj = measure_fwd_adjoint(args.seed, max(3, min(args.steps // 2, 50)), args.warmup)
         torch.cuda.set_stream(stream)
+        if Cn == 3:
+            # the colour adjoint on this workload's own handle: forward (ports + fused forward) vs
+            # forward + tp_backward (the Bayer planes' colour mix reversed, ports' FP64 derivatives)
+            def fwd_only():
+                tp._ck(lib.tp_ports(tp.h, sptr), "ports")
+                tp._ck(lib.tp_process(tp.h, sptr), "process")
+
+            def fwd_bwd():
+                fwd_only()
+                tp._ck(lib.tp_backward(tp.h, None, None, None, sptr), "backward")
+
+            colour_adj = {"workload": args.config, "tiles": T}
+            n_c = max(3, min(args.steps // 2, 50))
+            for name, fn in (("fwd", fwd_only), ("fwd_adjoint", fwd_bwd)):
+                for _ in range(max(args.warmup, 3)):
+                    fn()
+                torch.cuda.synchronize()
+                c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                c0.record(stream)
+                for _ in range(n_c):
+                    fn()
+                c1.record(stream)
+                torch.cuda.synchronize()
+                colour_adj[name + "_ms"] = c0.elapsed_time(c1) / n_c
+            colour_adj["adjoint_over_fwd"] = colour_adj["fwd_adjoint_ms"] / colour_adj["fwd_ms"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -765,6 +791,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "fwd_adjoint": fwd_adj,
+        "fwd_adjoint_colour": colour_adj,
         "lma_disparity": lma_line,
         "batched": batched,
         "batched_small_scenes": batched_small,

@@ -328,7 +328,6 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
   float *qb = gs + 240;               // [4][72] quadrant buffer
   float *tb = qb + 288;               // [4][72] transpose buffer
   const short *strip_code = &sc.corr_cfg->strip_code[0][0][0];
-  const int groups = (S + 3) >> 2;
   const float inv_n = 1.0f / cfg.num_combo;
 
   for (int task = blockIdx.x; task < sc.num_tasks; task += gridDim.x) {
@@ -336,25 +335,37 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
     const size_t tile = (size_t)(txy >> 16) * sc.tilesX + (txy & 0xffff);
     // ---------------- the tile's CLT ----------------
     if (as.recompute) {
-      for (int g = warp; g < groups; g += AD_NW) {
-        const int s = g * 4 + q;
-        const int sidx = s < S ? s : S - 1;
-        const SubtilePlan p = sc.plan[(size_t)task * S + sidx];
-        const Win w = make_win(sc, p, sidx);
+      // every (sensor, colour) item, four per 8-lane group: a Bayer colour as the sparse plane of
+      // its pixels (the dense fold of the masked window is the forward's CLT of that plane)
+      const int items = S * C;
+      for (int g = warp; g < (items + 3) / 4; g += AD_NW) {
+        const int it = g * 4 + q;
+        const int itc = it < items ? it : items - 1;
+        const int s = itc / C, c = itc - s * C;
+        const SubtilePlan p = sc.plan[(size_t)task * items + itc];
         float ahs, ahc, avs, avc;
         __sincosf(CUDART_PI_F * 0.0625f * p.rx, &ahs, &ahc);
         __sincosf(CUDART_PI_F * 0.0625f * p.ry, &avs, &avc);
         const FoldIdx fv = fold_idx(r);
         float vw0, vw1, hw0[8], hw1[8], o[4][8];
         fold_weights(ahc, ahs, avc, avs, fv, vw0, vw1, hw0, hw1);
-        fold_dtt_dense(w, fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
-        convolve(o, (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr, r);
+        if (C == 1) {
+          fold_dtt_dense(make_win(sc, p, s), fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
+        } else {
+          BayerWin bw;
+          bw.w = make_win(sc, p, s, c);
+          bw.c = c;
+          bw.rr = sc.bayer_red_row;
+          bw.rc = sc.bayer_red_col;
+          fold_dtt_dense(bw, fv, vw0, vw1, hw0, hw1, r, tb + q * 72, o);
+        }
+        convolve(o, (p.kidx >= 0) ? sc.kernels[s] + (size_t)p.kidx * TP_CLT : nullptr, r);
         rotate(o, p.rx, p.ry, r);
-        if (s < S) {
+        if (it < items) {
 #pragma unroll
           for (int m = 0; m < 4; m++)
 #pragma unroll
-            for (int v = 0; v < 8; v++) s_clt[s * TP_CLT + m * 64 + r * 8 + v] = o[m][v];
+            for (int v = 0; v < 8; v++) s_clt[it * TP_CLT + m * 64 + r * 8 + v] = o[m][v];
         }
       }
     } else {
@@ -710,9 +721,7 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
                            const float *dl_dd, float *jac_e, float *jac_d, float *grad_d, float *partial,
                            float *grad_e, cudaStream_t st) {
   if (sc.num_tasks <= 0) return cudaSuccess;
-  // colour scenes: quad Bayer sensors with the stored CLT (the recompute path folds mono windows)
-  if ((sc.num_colors != 1 && (sc.num_colors != 3 || recompute)) || !sc.port_deriv || !sc.combo)
-    return cudaErrorInvalidValue;
+  if ((sc.num_colors != 1 && sc.num_colors != 3) || !sc.port_deriv || !sc.combo) return cudaErrorInvalidValue;
   AdjShape as;
   as.S = sc.num_sensors;
   as.C = sc.num_colors;

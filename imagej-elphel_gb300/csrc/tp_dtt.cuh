@@ -156,8 +156,10 @@ __device__ __forceinline__ void fold_weights(float hc, float hs, float vc, float
 }
 
 // fold of a dense 16x16 window and the four 2D DCT-IV/DST-IV (fold_tile, dttt_iv):
-// lane r of the 8-lane group holds horizontal frequency r of each quadrant, o[m][v]
-__device__ __forceinline__ void fold_dtt_dense(const Win &w, const FoldIdx &fv, float vw0, float vw1,
+// lane r of the 8-lane group holds horizontal frequency r of each quadrant, o[m][v];
+// PIX: the pixel source, at(row, col)
+template <typename PIX = Win>
+__device__ __forceinline__ void fold_dtt_dense(const PIX &w, const FoldIdx &fv, float vw0, float vw1,
                                                const float hw0[8], const float hw1[8], int r, float *tbuf,
                                                float o[4][8]) {
   // vertical 2-tap combine once, then the two horizontal variants

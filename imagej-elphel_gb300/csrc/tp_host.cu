@@ -1766,8 +1766,6 @@ tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt) {
 
 tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream) {
   if (!h) return TP_ERR_ARG;
-  if (h->cfg.num_colors != 1 && h->adj_recompute)
-    return fail(h, TP_ERR_ARG, "tp_backward: recomputing the CLT is implemented for mono sensors");
   if (!h->ports_from_geometry || !h->have_geometry)
     return fail(h, TP_ERR_STATE, "tp_backward: needs tile ops with ports from the geometry (tp_set_tile_ops)");
   if (h->rig_aux)

@@ -454,9 +454,9 @@ tp_status tp_batch_synchronize(tp_batch *b);
  * ([tiles][pairs][strip entries] floats on the device) for the adjoint to read. */
 tp_status tp_backward(tp_handle *h, const float *dl_ddisp, float *dl_dextr, float *dl_dtile_disp, void *stream);
 /* 1: the adjoint recomputes each tile's CLT from the images instead of reading
- * the stored CLT back (for when the CLT buffer is not kept; mono sensors only:
- * tp_backward returns TP_ERR_ARG for a colour handle in this mode); default 0.  Also
- * starts the strip-sample recording described at tp_backward. */
+ * the stored CLT back (for when the CLT buffer is not kept; a Bayer colour as the
+ * dense fold of its sparse plane, which equals the forward's CLT to rounding);
+ * default 0.  Also starts the strip-sample recording described at tp_backward. */
 tp_status tp_set_adjoint_mode(tp_handle *h, int recompute_clt);
 /* Jacobian of the last tp_backward: jac_extr [tiles][num_sensors][4] (dd per
  * azimuth, tilt, roll, zoom), jac_disp [tiles] (dd per target disparity),
