@@ -318,6 +318,8 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
   extern __shared__ float sm[];
   __shared__ float s_d;
   __shared__ float s_sens[2 * TP_MAXS * 3];  // dd/d(port x, y) of every (sensor, colour)
+  __shared__ float s_lpf[64];                // the correlation LPF, read per lane
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_lpf[i] = cfg.lpf[i];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = lane >> 3, r = lane & 7;
   const int S = as.S, C = as.C, P = as.P, RE = as.RE;
   float *s_clt = sm;                      // [S][C][256]
@@ -535,7 +537,7 @@ __global__ void __launch_bounds__(32 * AD_NW, 4) adjoint_kernel(const __grid_con
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int idx = lane + 32 * h;
-          const float l = cfg.lpf[idx];
+          const float l = s_lpf[idx];
           const int off = (idx >> 3) * 9 + (idx & 7);
 #pragma unroll
           for (int qq = 0; qq < 4; qq++) gq[qq][h] = qb[qq * 72 + off] * l;

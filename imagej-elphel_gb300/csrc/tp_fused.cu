@@ -234,11 +234,13 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
 
 // phase B for pair pi: correlation surface to HBM, strip entries folded into cmb
 // (NT = strip entries per lane / 32 rounded up: 1 when the extraction reads <= 32 entries)
+// lpf: the correlation LPF (64 floats) in shared memory: each lane reads its own two entries,
+// which from the kernel's parameter space would take one constant-cache access per lane
 template <int C, int NT, bool OACC = false>
-__device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, size_t tile, int P, int pi, int RE,
-                                         bool log_mode, const short *strip_code, const float *s_clt, float *scr,
-                                         int lane, float cmb[8], float *corr_out = nullptr,
-                                         float *oprod = nullptr) {
+__device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cfg, const float *lpf, size_t tile,
+                                         int P, int pi, int RE, bool log_mode, const short *strip_code,
+                                         const float *s_clt, float *scr, int lane, float cmb[8],
+                                         float *corr_out = nullptr, float *oprod = nullptr) {
   const int q = lane >> 3, r = lane & 7;
   float *qb = scr;
   const PairDev pd = cfg.pairs[pi];
@@ -284,7 +286,7 @@ __device__ __forceinline__ void fwd_pair(const SceneDev &sc, const CorrConst &cf
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int idx = lane + 32 * h;
-    const float l = cfg.lpf[idx];
+    const float l = lpf[idx];
     const int off = (idx >> 3) * 9 + (idx & 7);
 #pragma unroll
     for (int qq = 0; qq < 4; qq++) qb[qq * 72 + off] = acc[qq][h] * l;
@@ -543,6 +545,9 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
                                                                const __grid_constant__ FwdShape fs,
                                                                const __grid_constant__ CorrConst cfg) {
   extern __shared__ float sm[];
+  __shared__ float s_lpf[64];  // the correlation LPF, read per lane by fwd_pair
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_lpf[i] = cfg.lpf[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
   // per-warp shared memory: CLT of the tile [S][C][4][64] and a 288-float scratch buffer
@@ -564,7 +569,8 @@ __global__ void __launch_bounds__(128, 4) fused_forward_kernel(const __grid_cons
 #pragma unroll
     for (int i = 0; i < 8; i++) oprod[i] = 1.f;
     for (int pi = 0; pi < P; pi++)
-      fwd_pair<C, NT, true>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr, oprod);
+      fwd_pair<C, NT, true>(sc, cfg, s_lpf, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr,
+                            oprod);
     fwd_extract<NT, true>(sc, cfg, fs.quad, P, RE, log_mode, ncomb, tile, scr, lane, cmb, oprod);
   }
 }
@@ -671,6 +677,9 @@ __global__ void __launch_bounds__(128, 4) fused_forward_win_kernel(const __grid_
                                                                    const __grid_constant__ FwdShape fs,
                                                                    const __grid_constant__ CorrConst cfg) {
   extern __shared__ float sm[];
+  __shared__ float s_lpf[64];  // the correlation LPF, read per lane by fwd_pair
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_lpf[i] = cfg.lpf[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane >> 3, r = lane & 7;
   const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
   float *s_clt = sm + warp * fs.per_warp;
@@ -710,7 +719,8 @@ __global__ void __launch_bounds__(128, 4) fused_forward_win_kernel(const __grid_
 #pragma unroll
     for (int i = 0; i < 8; i++) oprod[i] = 1.f;
     for (int pi = 0; pi < P; pi++)
-      fwd_pair<3, NT, true>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr, oprod);
+      fwd_pair<3, NT, true>(sc, cfg, s_lpf, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb, nullptr,
+                            oprod);
     if (next < sc.num_tasks) {  // the CLT slots are read (fwd_pair ends with __syncwarp): next tile's windows
       if (act) stage_window(sc, img, pc.tlx, pc.tly, (uint16_t *)(s_clt + (size_t)q * 3 * TP_CLT), r);
       cp_async_commit();
@@ -777,6 +787,9 @@ __global__ void __launch_bounds__(MAXT, MINB) fused_split_kernel(const __grid_co
                                                           const __grid_constant__ FwdShape fs,
                                                           const __grid_constant__ CorrConst cfg) {
   extern __shared__ float sm[];
+  __shared__ float s_lpf[64];  // the correlation LPF, read per lane by fwd_pair
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_lpf[i] = cfg.lpf[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = fs.S, P = fs.P, RE = fs.RE, NW = fs.nw;
   float *s_clt = sm;
@@ -795,7 +808,7 @@ __global__ void __launch_bounds__(MAXT, MINB) fused_split_kernel(const __grid_co
 #pragma unroll
     for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
     for (int pi = warp; pi < P; pi += NW)
-      fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+      fwd_pair<C, NT>(sc, cfg, s_lpf, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
     for (int t = 0; t < NT; t++) {
       const int e = lane + 32 * t;
@@ -899,7 +912,7 @@ __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
 #pragma unroll
       for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
       for (int pi = warp; pi < P; pi += NW)
-        fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+        fwd_pair<C, NT>(sc, cfg, cfg.lpf, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
 #pragma unroll
       for (int t = 0; t < NT; t++) {
         const int e = lane + 32 * t;
@@ -932,7 +945,7 @@ __global__ void __launch_bounds__(NW * 32, (NW == 1) ? 16 : 4)
 #pragma unroll
         for (int t = 0; t < NT; t++) cmb[t] = log_mode ? 0.f : 1.f;
         for (int pi = 0; pi < P; pi++)
-          fwd_pair<C, NT>(sc, cfg, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
+          fwd_pair<C, NT>(sc, cfg, cfg.lpf, tile, P, pi, RE, log_mode, strip_code, s_clt, scr, lane, cmb);
         fwd_extract<NT>(sc, cfg, P <= 8, P, RE, log_mode, ncomb, tile, scr, lane, cmb);
       }
     }
@@ -1007,6 +1020,9 @@ __global__ void __launch_bounds__(128, 4) rig_kernel(const __grid_constant__ Sce
                                                      const __grid_constant__ CorrConst cfg, float *rig_corr,
                                                      float *rig_rec, float cm_norm, int no_int_x0, int per_warp) {
   extern __shared__ float sm[];
+  __shared__ float s_lpf[64];  // the correlation LPF, read per lane by fwd_pair
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_lpf[i] = cfg.lpf[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, NW = blockDim.x >> 5;
   float *mix = sm + warp * per_warp;  // [2][C][256]
   float *scr = mix + 2 * C * TP_CLT;
@@ -1032,7 +1048,7 @@ __global__ void __launch_bounds__(128, 4) rig_kernel(const __grid_constant__ Sce
     float cmb[8];
 #pragma unroll
     for (int t = 0; t < NT; t++) cmb[t] = 1.f;
-    fwd_pair<C, NT>(mn, cfg, tile, 1, 0, RE, false, strip_code, mix, scr, lane, cmb, rig_corr + tile * TP_CORR);
+    fwd_pair<C, NT>(mn, cfg, s_lpf, tile, 1, 0, RE, false, strip_code, mix, scr, lane, cmb, rig_corr + tile * TP_CORR);
     float *combo = scr;
 #pragma unroll
     for (int t = 0; t < NT; t++) {
