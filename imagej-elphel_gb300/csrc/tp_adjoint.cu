@@ -701,13 +701,22 @@ __global__ void __launch_bounds__(256) adjoint_contract_kernel(const __grid_cons
   }
 }
 
-__global__ void adjoint_final_kernel(const float *partial, int nblocks, int n, float *grad_e) {
-  const int i = threadIdx.x;
-  if (i < n) {
-    float v = 0.f;
-    for (int b = 0; b < nblocks; b++) v += partial[(size_t)b * n + i];
-    grad_e[i] = v;
+// One block per extrinsic coordinate i: thread t sums the partials of blocks t, t + 256, ... in
+// order, then a fixed tree over the 256 threads (deterministic; a single thread walking all
+// partials waited on one dependent load per block)
+__global__ void __launch_bounds__(256) adjoint_final_kernel(const float *partial, int nblocks, int n,
+                                                            float *grad_e) {
+  __shared__ float s[256];
+  const int i = blockIdx.x, t = threadIdx.x;
+  float v = 0.f;
+  for (int b = t; b < nblocks; b += 256) v += partial[(size_t)b * n + i];
+  s[t] = v;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (t < h) s[t] += s[t + h];
+    __syncthreads();
   }
+  if (t == 0) grad_e[i] = s[0];
 }
 
 cudaError_t upload_adjoint_constants() {
@@ -748,6 +757,6 @@ cudaError_t launch_adjoint(const SceneDev &sc, const CorrConst &cc, int recomput
   adjoint_contract_kernel<<<nb, 256, 0, st>>>(sc, sens, dval, dl_dd, jac_e, jac_d, grad_d, partial);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  adjoint_final_kernel<<<1, 64, 0, st>>>(partial, nb, sc.num_sensors * 4, grad_e);
+  adjoint_final_kernel<<<sc.num_sensors * 4, 256, 0, st>>>(partial, nb, sc.num_sensors * 4, grad_e);
   return cudaGetLastError();
 }

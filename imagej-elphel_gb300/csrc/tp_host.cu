@@ -555,7 +555,10 @@ static tp_status upload_geometry(tp_handle *h, const tp_geometry *g, const tp_ge
   gd.c_pixel_height = gc->pixel_height;
   gd.c_pixel_size = gc->pixel_size;
   gd.c_distortion_radius = gc->distortion_radius;
-  for (int i = 0; i < 7; i++) gd.rad_coeff[i] = g->distortion[i];
+  for (int i = 0; i < 7; i++) {
+    gd.rad_coeff[i] = g->distortion[i];
+    gd.rad_dcoeff[i] = g->distortion[i] * (double)(i + 1);
+  }
   for (int s = 0; s < S; s++)
     for (int k = 0; k < 2; k++) {
       gd.rXY[s][k] = g->rXY[s][k];

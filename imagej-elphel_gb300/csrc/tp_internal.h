@@ -37,6 +37,7 @@ struct GeomDev {
   int rig;                     // 1: task disparities are main-camera ones, scaled by disp_num / disp_den
   double disp_num, disp_den;   // aux / main disparity radius
   double rad_coeff[7];
+  double rad_dcoeff[7];  // rad_coeff[j] * (j + 1), the derivative's coefficients (the same products)
   double rXY[TP_MAXS][2];
   double pXY0[TP_MAXS][2];
   double rots[TP_MAXS][3][3];

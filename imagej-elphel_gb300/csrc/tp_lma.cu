@@ -1018,8 +1018,8 @@ cudaError_t launch_lma(const SceneDev &sc, const CorrConst &cc, const TpLmaConst
 
 // The 2D maximum of every task tile's pair surfaces, one warp per surface: the first cell of the
 // largest value in index order (NaN cells count as -inf), then a parabola through it and its two
-// neighbours on each axis (FP64, the fraction clamped to +-0.5 and taken as 0 where a neighbour is
-// not finite).  out [tiles][P][3] = {dx, dy, strength}, px from the centre (x right, y down);
+// neighbours on each axis (FP32: an FP64 division costs this part's FP64 pipe 1/64 of the FP32
+// rate per warp; the fraction clamped to +-0.5 and taken as 0 where a neighbour is not finite).  out [tiles][P][3] = {dx, dy, strength}, px from the centre (x right, y down);
 // {NaN, NaN, 0} where the maximum is on the border or not finite, all NaN outside the task list.
 __global__ void __launch_bounds__(128) pair_max_kernel(const float *__restrict__ corr,
                                                        const int *__restrict__ task_txy, int num_tasks,
@@ -1062,12 +1062,12 @@ __global__ void __launch_bounds__(128) pair_max_kernel(const float *__restrict__
   for (int a = 0; a < 2; a++) {
     const int st = a ? 15 : 1;
     const float m = c[bi - st], p = c[bi + st];
-    double fr = 0.0;
+    float fr = 0.f;
     if (isfinite(m) && isfinite(p)) {
-      const double den = ((double)m - 2.0 * (double)best) + (double)p;
-      if (den < 0.0) fr = fmin(0.5, fmax(-0.5, 0.5 * ((double)m - (double)p) / den));
+      const float den = (m - 2.f * best) + p;
+      if (den < 0.f) fr = fminf(0.5f, fmaxf(-0.5f, 0.5f * (m - p) / den));
     }
-    f[a] = (float)(((a ? iy : ix) - 7) + fr);
+    f[a] = (float)((a ? iy : ix) - 7) + fr;
   }
   o[0] = f[0];
   o[1] = f[1];

@@ -68,10 +68,9 @@ __device__ __forceinline__ void center_undistort(const GeomDev &g, const double 
 }
 
 // getPortsCoordinatesAndDerivatives (GeometryCorrection.java:2159-2314) for one sensor
-__device__ void port_xy(const GeomDev &g, const double *tbl, double px, double py, double disparity, int i,
-                        double &ox, double &oy, double *deriv /* [2][5] or null */) {
-  double pXc, pYc;
-  center_undistort(g, tbl, px, py, pXc, pYc);
+// (pXc, pYc): the task's undistorted centre (center_undistort), the same for every sensor
+__device__ void port_xy(const GeomDev &g, double pXc, double pYc, double disparity, int i, double &ox, double &oy,
+                        double *deriv /* [2][5] or null */) {
   const double fl_pix = g.fl_pix, ri_scale = g.ri_scale;
   double vi[3] = {DSUB(pXc, DMUL(disparity, g.rXY[i][0])), DSUB(pYc, DMUL(disparity, g.rXY[i][1])), fl_pix};
   double rvi[3];
@@ -90,11 +89,16 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
   ox = DADD(DMUL(pXci, rD2rND), g.pXY0[i][0]);
   oy = DADD(DMUL(pYci, rD2rND), g.pXY0[i][1]);
   if (deriv) {
+    // quotients shared by the five parameters (a product with a reciprocal where the reference
+    // divides: the derivatives differ from its by an ulp, the ports are not touched)
+    const double ri_rnd = DDIV(ri_scale, rNDi);
+    const double inv_rz = DDIV(1.0, rvi[2]);
+    const double pXr = DMUL(pXci, inv_rz), pYr = DMUL(pYci, inv_rz);
     double drD2rND_dri = 0.0;
     rri = 1.0;
 #pragma unroll
     for (int j = 0; j < 7; j++) {
-      drD2rND_dri = DADD(drD2rND_dri, DMUL(DMUL(g.rad_coeff[j], (double)(j + 1)), rri));
+      drD2rND_dri = DADD(drD2rND_dri, DMUL(g.rad_dcoeff[j], rri));
       rri = DMUL(rri, ri);
     }
 #pragma unroll
@@ -106,13 +110,13 @@ __device__ void port_xy(const GeomDev &g, const double *tbl, double px, double p
         const double dvi[3] = {-g.rXY[i][0], -g.rXY[i][1], 0.0};
         mat3_vec(g.rots[i], dvi, dr);
       }
-      double dpX = DSUB(DMUL(dr[0], norm_z), DDIV(DMUL(pXci, dr[2]), rvi[2]));
-      double dpY = DSUB(DMUL(dr[1], norm_z), DDIV(DMUL(pYci, dr[2]), rvi[2]));
+      double dpX = DSUB(DMUL(dr[0], norm_z), DMUL(pXr, dr[2]));
+      double dpY = DSUB(DMUL(dr[1], norm_z), DMUL(pYr, dr[2]));
       if (k == 2) {  // roll: the reference keeps only the rotation term
         deriv[k] = DMUL(dpX, rD2rND);
         deriv[5 + k] = DMUL(dpY, rD2rND);
       } else {
-        double dri = DMUL(DDIV(ri_scale, rNDi), DADD(DMUL(pXci, dpX), DMUL(pYci, dpY)));
+        double dri = DMUL(ri_rnd, DADD(DMUL(pXci, dpX), DMUL(pYci, dpY)));
         double drD = DMUL(drD2rND_dri, dri);
         deriv[k] = DADD(DMUL(dpX, rD2rND), DMUL(pXci, drD));
         deriv[5 + k] = DADD(DMUL(dpY, rD2rND), DMUL(pYci, drD));
@@ -167,7 +171,7 @@ __device__ __forceinline__ void plan_task(const SceneDev &sc, int task, int s0, 
     if (sc.ports_from_geometry) {
       if (sc.port_deriv) {
         double dv[10];
-        port_xy(*sc.geom, sc.rdist_tbl, ctx, cty, disparity, s, cx, cy, dv);
+        port_xy(*sc.geom, pXc, pYc, disparity, s, cx, cy, dv);
         double *o = sc.port_deriv + ((size_t)task * S + s) * 10;
 #pragma unroll
         for (int k = 0; k < 10; k++) o[k] = dv[k];

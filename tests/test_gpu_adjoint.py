@@ -330,8 +330,7 @@ def test_coarse_stage_recovers_extrinsics(seed, free):
 def test_pair_maxima_match_host_statement():
     """tp_get_pair_maxima (a warp per pair surface on the device) against lma.pair_peaks on the
     surfaces read back: the same cells (border and non-finite maxima in the same places), the same
-    strengths, offsets within 1e-5 px (the parabola's FP64 arithmetic rounds one difference
-    differently)."""
+    strengths, offsets within 1e-4 px (the device evaluates the parabola in FP32, the host in FP64)."""
     from tileproc import lma
     sc, g, pairs, D = _setup()
     with _gpu(sc, g, pairs, D) as tp:
@@ -343,6 +342,6 @@ def test_pair_maxima_match_host_statement():
     ok = np.isfinite(off).all(axis=-1)
     assert ok.mean() > 0.9
     assert np.array_equal(ok, np.isfinite(pm[..., :2]).all(axis=-1))
-    assert np.abs(pm[..., :2][ok] - off[ok]).max() < 1e-5
+    assert np.abs(pm[..., :2][ok] - off[ok]).max() < 1e-4
     assert np.array_equal(pm[..., 2][ok], st[ok].astype(np.float32))
     assert (pm[..., 2][~ok] == 0).all()
