@@ -178,9 +178,6 @@ struct FwdShape {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// the fused kernel: one warp carries a tile through all stages, no CTA barriers
-// ---------------------------------------------------------------------------
-// ---------------------------------------------------------------------------
 // the three phases of the forward for one tile, shared by the schedules
 // ---------------------------------------------------------------------------
 // phase A item gt = (colour, group of 4 sensors): lanes 8q..8q+7 own sensor 4g+q
@@ -203,18 +200,14 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
   w.scale = sc.color_scale[c];
   float o[4][8];
   float *tbuf = scr + q * 72;
-  float sg0 = 1.f, sg1 = 1.f;  // symmetry signs kept for the correlation reads
   if (C == 1) {
     subtile_clt<0>(w, p.rx, p.ry, 0, 0, 0, r, tbuf, o);
   } else if (c < 2) {
     const int pc = ((c == 0 ? rc : 1 - rc) - p.tlx) & 1, pr = ((c == 0 ? rr : 1 - rr) - p.tly) & 1;
     subtile_clt<1>(w, p.rx, p.ry, pc, pr, 0, r, tbuf, o);
-    sg0 = pc ? -1.f : 1.f;
-    sg1 = pr ? -1.f : 1.f;
   } else {
     const int pg = (p.tlx + p.tly + rc + rr + 1) & 1;
     subtile_clt<2>(w, p.rx, p.ry, 0, 0, pg, r, tbuf, o);
-    sg0 = pg ? -1.f : 1.f;
   }
   const float *kp = (p.kidx >= 0) ? sc.kernels[sidx] + (size_t)p.kidx * TP_CLT : nullptr;
   conv_shift(o, kp, p.rx, p.ry, r);
@@ -228,8 +221,6 @@ __device__ __forceinline__ void fwd_clt_item(const SceneDev &sc, int S, int task
       *(float4 *)(sdst + m * 64 + 4) = make_float4(o[m][4], o[m][5], o[m][6], o[m][7]);
     }
   }
-  (void)sg0;
-  (void)sg1;
 }
 
 // phase B for pair pi: correlation surface to HBM, strip entries folded into cmb
