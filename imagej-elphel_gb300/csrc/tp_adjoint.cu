@@ -244,6 +244,14 @@ __device__ __forceinline__ void shift_sens(const SceneDev &sc, const PIX &w, con
     }
   }
   __syncwarp();
+  // the lane's two source rows of the window, read once for both directions and both vertical
+  // variants
+  float p0[16], p1[16];
+#pragma unroll
+  for (int cix = 0; cix < 16; cix++) {
+    p0[cix] = w.at(fv.src0, cix);
+    p1[cix] = w.at(fv.src1, cix);
+  }
   // per direction: the fold with the derivative window dotted with the folded gradient
 #pragma unroll
   for (int dir = 0; dir < 2; dir++) {
@@ -256,7 +264,7 @@ __device__ __forceinline__ void shift_sens(const SceneDev &sc, const PIX &w, con
       const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
       float vc[16];
 #pragma unroll
-      for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+      for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, p1[cix], k0 * p0[cix]);
 #pragma unroll
       for (int hb = 0; hb < 2; hb++)
 #pragma unroll

@@ -162,13 +162,20 @@ template <typename PIX = Win>
 __device__ __forceinline__ void fold_dtt_dense(const PIX &w, const FoldIdx &fv, float vw0, float vw1,
                                                const float hw0[8], const float hw1[8], int r, float *tbuf,
                                                float o[4][8]) {
+  // the lane's two source rows, read once for both vertical variants
+  float p0[16], p1[16];
+#pragma unroll
+  for (int cix = 0; cix < 16; cix++) {
+    p0[cix] = w.at(fv.src0, cix);
+    p1[cix] = w.at(fv.src1, cix);
+  }
   // vertical 2-tap combine once, then the two horizontal variants
 #pragma unroll
   for (int vb = 0; vb < 2; vb++) {
     const float k0 = (vb ? fv.ss0 : fv.sc0) * vw0, k1 = (vb ? fv.ss1 : fv.sc1) * vw1;
     float vc[16];
 #pragma unroll
-    for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, w.at(fv.src1, cix), k0 * w.at(fv.src0, cix));
+    for (int cix = 0; cix < 16; cix++) vc[cix] = fmaf(k1, p1[cix], k0 * p0[cix]);
 #pragma unroll
     for (int hb = 0; hb < 2; hb++) {
       float y[8];
