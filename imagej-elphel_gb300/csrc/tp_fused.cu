@@ -1145,8 +1145,8 @@ cudaError_t launch_rig(const SceneDev &mn, const SceneDev &ax, const CorrConst &
 // without atomics and in a fixed order.  A warp carries 4 tiles at once, one per
 // 8-lane group, lane r owning row r of each quadrant.
 // ---------------------------------------------------------------------------
-constexpr int IMCLT_IR = 16;     // region = IR x IR blocks of 8x8 pixels
-constexpr int IMCLT_WARPS = 9;   // 36 8-lane groups: the four parity phases (64, 72, 72, 81 tiles) in 2+2+2+3 rounds
+constexpr int IMCLT_IR = 14;     // region = IR x IR blocks of 8x8 pixels (14: 0.41 ms, 16: 0.43, 12: 0.44 on 4x2592x1936)
+constexpr int IMCLT_WARPS = 9;   // 36 8-lane groups: the four parity phases (49, 56, 56, 64 tiles) in 2 rounds each
 
 template <int IR>
 __global__ void __launch_bounds__(32 * IMCLT_WARPS) imclt_fast_kernel(const __grid_constant__ SceneDev sc) {
